@@ -1,0 +1,47 @@
+/*
+ * nrltb_input.h -- C restatement of the reference's input API: the SKIN file
+ * (static.f:697-1030), the NRL parameter file (input.f:137-359), the structure
+ * block (input1.f:466-862), lattice construction (setlat.f:147-1024) and the
+ * k-point list (kptin.f:66-366, explicit-list paths).  Host-only, no device.
+ *
+ * A SKIN handle owns every array that the returned structs point into; the
+ * arrays of a structure stay valid until the next nrltb_skin_next call.
+ */
+#ifndef NRLTB_INPUT_H
+#define NRLTB_INPUT_H
+#include "nrltb.h"
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct nrltb_skin nrltb_skin;
+
+/* Open a SKIN file, read Mode= (static.f:706-708, modeparse.f), tkb and eigcut
+ * (static.f:818) and the parameter file it names (input.f), resolved relative
+ * to the SKIN file's directory. */
+int nrltb_skin_open(const char *path, nrltb_skin **out);
+/* Global settings of an open SKIN file.  par's arrays are owned by the handle. */
+int nrltb_skin_info(const nrltb_skin *s, int *mode, double *tkb, double *eigcut,
+                    nrltb_params *par);
+/* Read the next structure: title, label, zcharge (static.f:938-950), input1.f,
+ * setlat.f, the lattice-to-Cartesian step (static.f:1088-1103) and kptin.f.
+ * Returns NRLTB_E_EOF after the last structure.  title must hold 71 chars and
+ * label 21 (NUL included). */
+int nrltb_skin_next(nrltb_skin *s, nrltb_structure *st, nrltb_kmesh *km,
+                    char *title, char *label);
+/* Line number (1-based) of the SKIN file where the last error happened. */
+int nrltb_skin_error_line(const nrltb_skin *s);
+void nrltb_skin_close(nrltb_skin *s);
+
+/* Parameter file alone (input.f:137-359). */
+typedef struct nrltb_parfile nrltb_parfile;
+int nrltb_parfile_read(const char *path, nrltb_parfile **out, nrltb_params *par);
+void nrltb_parfile_close(nrltb_parfile *p);
+
+/* Number of parameters for `kinds` species: kinds(29 + 68 kinds) (input.f:275). */
+int nrltb_nparams(int kinds);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

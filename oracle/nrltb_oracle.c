@@ -1,0 +1,864 @@
+/*
+ * nrltb_oracle.c -- CPU restatement of the reference's per-k-point path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This file is the checker: the parity tests, the
+ * smoke test and the CPU baseline leg of the benchmark call it; the product
+ * library never links or calls it.
+ *
+ * It restates, routine by routine and in the reference's own operation order,
+ * the NRL "static" v1.33 code (paths relative to the NRLtb project root):
+ *   search2  src/search2.f:95-223      pair list, inclusion test, screening
+ *   setpar   src/setpar.f:399-884      densities, SK integrals, on-site terms
+ *   setparv  src/setparv.f:426-886     their volume derivatives
+ *   setham   src/setham.f:279-453      Bloch sum into packed-upper H, S
+ *   rotate   src/rotate.f:131-326      Slater-Koster table, parity, phase
+ *   sethamv  src/sethamv.f:236-365     dH/dV, dS/dV
+ *   diag     src/diag.f:320-455        zhpgv(1,'V'|'N','U') driver
+ *   perturb  src/perturb.f:73-216      first-order (Hellmann-Feynman) shifts
+ *   fermi    src/fermi.f:162-425       Newton / bisection Fermi level
+ *   bande    src/bande.f:1069-1446     E(T), dE/dV sums, pressure formula
+ * The LAPACK step uses the same driver as the reference, zhpgv / zhpev, taken
+ * from the LAPACK that SciPy ships (function pointers installed by
+ * oracle_set_lapack); the reference's vendored copy (src/lapack.f) is Netlib
+ * reference LAPACK with the same semantics.
+ *
+ * Compile with -ffp-contract=off so that no multiply-add is fused: the GPU
+ * neighbour list reproduces this file's integer results bit for bit.
+ */
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#include <complex.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+#include "nrltb.h"
+
+typedef double _Complex zc;
+
+/* Fortran-ABI LAPACK entry points as exported by scipy.linalg.cython_lapack */
+typedef void (*zhpgv_fn)(int *itype, char *jobz, char *uplo, int *n, zc *ap, zc *bp,
+                         double *w, zc *z, int *ldz, zc *work, double *rwork, int *info);
+typedef void (*zhpev_fn)(char *jobz, char *uplo, int *n, zc *ap, double *w, zc *z,
+                         int *ldz, zc *work, double *rwork, int *info);
+static zhpgv_fn p_zhpgv = 0;
+static zhpev_fn p_zhpev = 0;
+
+void oracle_set_lapack(void *zhpgv, void *zhpev)
+{
+    p_zhpgv = (zhpgv_fn)zhpgv;
+    p_zhpev = (zhpev_fn)zhpev;
+}
+
+/* ---------------------------------------------------------------------- */
+/* parameter index arithmetic (setpar.f:461, 567-578, 654-667, 852-856)    */
+/* all results are 1-based Fortran indices into param(...)                 */
+static int ip_density(int kind) { return (kind - 1) * 17 + 1; }
+static int ip_hop(int kinds, int jk1, int jk2)
+{
+    int base = kinds * (1 + 4 * (3 * kinds + 1));
+    if (jk1 == jk2) return base + 40 * (jk1 - 1);
+    return base + 40 * kinds + 56 * ((jk2 - 1) * (jk2 - 2) / 2 + jk1 - 1);
+}
+static int ip_over(int kinds, int jk1, int jk2)
+{
+    int base = kinds * (1 + 4 * (3 * kinds + 1));
+    if (jk1 == jk2) return base + 40 * kinds + 56 * (kinds * (kinds - 1) / 2) + 40 * (jk1 - 1);
+    return base + 80 * kinds + 56 * (kinds * (kinds - 1) / 2) + 56 * ((jk2 - 1) * (jk2 - 2) / 2 + jk1 - 1);
+}
+static int ip_cross_onsite(int kinds, int jk1, int jk2)
+{
+    int jkx = jk1 > jk2 ? jk1 : jk2, jkm = jk1 < jk2 ? jk1 : jk2;
+    int ip = kinds * 17 + 24 * ((jkx - 1) * (jkx - 2) / 2 + jkm - 1);
+    if (jk2 < jkx) ip += 12;
+    return ip;
+}
+static int interaction_type(int kinds, int k1, int k2) /* search2.f:138-144, 1-based */
+{
+    if (k1 == k2) return k1;
+    int jk1 = k1 < k2 ? k1 : k2, jk2 = k1 < k2 ? k2 : k1;
+    return kinds + (jk2 - 1) * (jk2 - 2) / 2 + jk1;
+}
+
+static const double ovlnull[10] = {1, 0, 1, 1, 0, 0, 0, 1, 1, 1};          /* setpar.f:393 */
+static const double harsign[9] = {-1, 1, 1, -1, -1, -1, 1, -1, 1};          /* setparv.f:400 */
+
+/* ---------------------------------------------------------------------- */
+/* search2 (src/search2.f:95-223)                                          */
+int oracle_search2(const nrltb_structure *st, const nrltb_params *par, int kneigh_in,
+                   nrltb_pairs *out, int *kneigh_out, double *dismin)
+{
+    const double eps = 1e-3;
+    int kneigh = kneigh_in, np = 0, overflow = 0;
+    double dismin2 = 1e10;
+    int nd1 = st->nd[0], nd2 = st->nd[1], nd3 = st->nd[2];
+    for (int iat = 0; iat < st->natoms; ++iat) {
+        for (int jat = iat; jat < st->natoms; ++jat) {
+            int t = interaction_type(par->kinds, st->kkind[iat], st->kkind[jat]) - 1;
+            double dnnsq = par->dnn[t] * par->dnn[t];
+            double scrninv = 1.0 / par->screenl[t];
+            double screenr = par->dnn[t] - 5.0 * par->screenl[t];
+            for (int ix = 0; ix < 2 * nd1 + 1; ++ix)
+            for (int iy = 0; iy < 2 * nd2 + 1; ++iy)
+            for (int iz = 0; iz < 2 * nd3 + 1; ++iz) {
+                int im[3] = {ix - nd1, iy - nd2, iz - nd3};
+                double T[3], dsq = 0.0;
+                for (int i = 0; i < 3; ++i) {
+                    double rlv = 0.0;
+                    for (int j = 0; j < 3; ++j) rlv = rlv + st->plv[j][i] * (double)im[j];
+                    T[i] = st->posn[3 * jat + i] + rlv - st->posn[3 * iat + i];
+                    dsq = dsq + T[i] * T[i];
+                }
+                double dd = dsq - eps;
+                if (dd > dnnsq) continue;
+                if (dd < dnnsq) kneigh = 1;
+                if (dd < eps) kneigh = 0;
+                if (dd > eps && dsq < dismin2) dismin2 = dsq;
+                if (kneigh == 0) continue;
+                if (np >= out->capacity) { overflow = 1; ++np; continue; }
+                double dist = sqrt(dsq), tinv = 1.0 / dist;
+                double expdl = exp((dist - screenr) * scrninv);
+                double screen = 1.0 / (expdl + 1.0);
+                for (int j = 0; j < 3; ++j) {
+                    out->tt[3 * np + j] = T[j] * tinv;
+                    out->dlv[3 * np + j] = im[j];
+                }
+                out->dist[np] = dist;
+                out->screen[np] = screen;
+                out->dscrn[np] = -expdl * screen * scrninv;
+                out->jkind[2 * np] = st->kkind[iat];
+                out->jkind[2 * np + 1] = st->kkind[jat];
+                out->jatm[2 * np] = iat + 1;
+                out->jatm[2 * np + 1] = jat + 1;
+                ++np;
+            }
+        }
+    }
+    out->npairs = np;
+    if (kneigh_out) *kneigh_out = kneigh;
+    if (dismin) *dismin = sqrt(dismin2);
+    return overflow ? NRLTB_E_CAPACITY : NRLTB_OK;
+}
+
+/* ---------------------------------------------------------------------- */
+/* setpar (src/setpar.f:399-884), collinear, jspin = 1, no spin flips      */
+int oracle_setpar(const nrltb_structure *st, const nrltb_params *par, const nrltb_pairs *pr,
+                  double *hop, double *over, double *paros, double *den)
+{
+    const int kinds = par->kinds;
+    const double *P = par->param - 1; /* 1-based view */
+    const int realov = (par->nltype == 1 || par->nltype == 3);
+    const int harrison = (par->nltype == 2 || par->nltype == 3);
+    for (int i = 0; i < st->natoms * kinds; ++i) den[i] = 0.0;
+    for (int p = 0; p < pr->npairs; ++p) {
+        int iat = pr->jatm[2 * p] - 1, jat = pr->jatm[2 * p + 1] - 1;
+        int k1 = pr->jkind[2 * p], k2 = pr->jkind[2 * p + 1];
+        double dist = pr->dist[p], scr = pr->screen[p];
+        /* densities, setpar.f:500-536 */
+        double b = P[ip_density(k2)] * P[ip_density(k2)];
+        double dent = exp(-b * dist) * scr;
+        den[iat * kinds + (k2 - 1)] += dent;
+        if (jat != iat) {
+            b = P[ip_density(k1)] * P[ip_density(k1)];
+            dent = exp(-b * dist) * scr;
+            den[jat * kinds + (k1 - 1)] += dent;
+        }
+        int jk1 = k1 < k2 ? k1 : k2, jk2 = k1 < k2 ? k2 : k1;
+        int npk = (jk1 == jk2) ? 10 : 14;
+        double *h = hop + 14 * p, *o = over + 14 * p;
+        for (int j = 0; j < 14; ++j) { h[j] = 0.0; o[j] = 0.0; }
+        /* hopping integrals, setpar.f:586-636 */
+        int ip = ip_hop(kinds, jk1, jk2);
+        if (par->nltype != 90000) {
+            for (int j = 1; j <= npk; ++j) {
+                double abr = P[ip + 4 * j - 3] + dist * (P[ip + 4 * j - 2] + dist * P[ip + 4 * j - 1]);
+                double p32m = -(P[ip + 4 * j] * P[ip + 4 * j]);
+                h[j - 1] = abr * exp(p32m * dist) * scr;
+            }
+            if (harrison && jk1 == jk2)
+                for (int j = 0; j < 9; ++j) h[j] = harsign[j] * fabs(h[j]);
+        } else {
+            int j = 1;
+            double abr = P[ip + 4 * j - 3] + dist * (P[ip + 4 * j - 2] + dist * (P[ip + 4 * j - 1] +
+                         dist * (P[ip + 4 * j + 1] + dist * P[ip + 4 * j + 2])));
+            double p32m = -(P[ip + 4 * j] * P[ip + 4 * j]);
+            h[0] = abr * exp(p32m * dist) * scr;
+        }
+        /* overlap integrals, setpar.f:643-728 */
+        if (par->jsover) {
+            int usenew = realov && (jk1 == jk2);
+            int iop = ip_over(kinds, jk1, jk2);
+            if (par->nltype != 90000) {
+                for (int j = 1; j <= npk; ++j) {
+                    double abr = P[iop + 4 * j - 3] + dist * (P[iop + 4 * j - 2] + dist * P[iop + 4 * j - 1]);
+                    double p32m = -(P[iop + 4 * j] * P[iop + 4 * j]);
+                    if (usenew) abr = ovlnull[j - 1] + dist * abr;
+                    o[j - 1] = abr * exp(p32m * dist) * scr;
+                }
+                if (harrison && jk1 == jk2)
+                    for (int j = 0; j < 9; ++j) o[j] = -harsign[j] * fabs(o[j]);
+            } else {
+                int j = 1;
+                double abr = P[iop + 4 * j - 3] + dist * (P[iop + 4 * j - 2] + dist * (P[iop + 4 * j - 1] +
+                             dist * (P[iop + 4 * j + 1] + dist * P[iop + 4 * j + 2])));
+                double p32m = -(P[iop + 4 * j] * P[iop + 4 * j]);
+                o[0] = abr * exp(p32m * dist) * scr;
+            }
+        }
+    }
+    /* on-site terms, setpar.f:735-884 */
+    const double twtrd = 2.0 / 3.0;
+    for (int iat = 0; iat < st->natoms; ++iat) {
+        int jk1 = st->kkind[iat];
+        int ip = ip_density(jk1);
+        double vm23 = pow(den[iat * kinds + jk1 - 1], twtrd);
+        for (int k = 0; k < 4; ++k) {
+            paros[4 * iat + k] = P[ip + 1] + vm23 * (P[ip + 2] + vm23 * (P[ip + 3] + vm23 * P[ip + 4]));
+            ip += 4;
+        }
+        for (int jk2 = 1; jk2 <= kinds; ++jk2) {
+            double d = den[iat * kinds + jk2 - 1];
+            if (jk2 == jk1 || d == 0.0) continue;
+            vm23 = pow(d, twtrd);
+            ip = ip_cross_onsite(kinds, jk1, jk2);
+            for (int k = 0; k < 4; ++k) {
+                paros[4 * iat + k] = paros[4 * iat + k] +
+                    vm23 * (P[ip + 1] + vm23 * (P[ip + 2] + vm23 * P[ip + 3]));
+                ip += 3;
+            }
+        }
+    }
+    return NRLTB_OK;
+}
+
+/* setparv (src/setparv.f:426-886), collinear, jspin = 1 */
+int oracle_setparv(const nrltb_structure *st, const nrltb_params *par, const nrltb_pairs *pr,
+                   const double *den, double *dhop, double *dover, double *dparos)
+{
+    const int kinds = par->kinds;
+    const double *P = par->param - 1;
+    const int realov = (par->nltype == 1 || par->nltype == 3);
+    const int harrison = (par->nltype == 2 || par->nltype == 3);
+    const double third = 1.0 / 3.0, twtrd = 2.0 / 3.0, threeh = 3.0 / 2.0;
+    double *vden = (double *)calloc((size_t)st->natoms * kinds, sizeof(double));
+    if (!vden) return NRLTB_E_NOMEM;
+    for (int p = 0; p < pr->npairs; ++p) {
+        int iat = pr->jatm[2 * p] - 1, jat = pr->jatm[2 * p + 1] - 1;
+        int k1 = pr->jkind[2 * p], k2 = pr->jkind[2 * p + 1];
+        double dist = pr->dist[p], scr = pr->screen[p], dsc = pr->dscrn[p];
+        double vdist = third * dist / st->volume;
+        double b = P[ip_density(k2)] * P[ip_density(k2)];
+        double dent = exp(-b * dist) * scr;
+        vden[iat * kinds + k2 - 1] += (dsc - b) * dent * vdist;
+        if (jat != iat) {
+            b = P[ip_density(k1)] * P[ip_density(k1)];
+            dent = exp(-b * dist) * scr;
+            vden[jat * kinds + k1 - 1] += (dsc - b) * dent * vdist;
+        }
+        int jk1 = k1 < k2 ? k1 : k2, jk2 = k1 < k2 ? k2 : k1;
+        int npk = (jk1 == jk2) ? 10 : 14;
+        int usehar = harrison && (jk1 == jk2);
+        double *h = dhop + 14 * p, *o = dover + 14 * p;
+        for (int j = 0; j < 14; ++j) { h[j] = 0.0; o[j] = 0.0; }
+        int ip = ip_hop(kinds, jk1, jk2);
+        if (par->nltype != 90000) {
+            for (int j = 1; j <= npk; ++j) {
+                double abr = P[ip + 4 * j - 3] + dist * (P[ip + 4 * j - 2] + dist * P[ip + 4 * j - 1]);
+                double p32m = -(P[ip + 4 * j] * P[ip + 4 * j]);
+                double par21 = abr * exp(p32m * dist) * scr;
+                h[j - 1] = vdist * (((P[ip + 4 * j - 2] + 2.0 * dist * P[ip + 4 * j - 1]) + p32m * abr) *
+                                    exp(p32m * dist) * scr + dsc * par21);
+                if (usehar && j < npk) h[j - 1] = harsign[j - 1] * h[j - 1] * (abr >= 0 ? 1.0 : -1.0);
+            }
+        } else {
+            int j = 1;
+            double abr = P[ip + 4 * j - 3] + dist * (P[ip + 4 * j - 2] + dist * (P[ip + 4 * j - 1] +
+                         dist * (P[ip + 4 * j + 1] + dist * P[ip + 4 * j + 2])));
+            double p32m = -(P[ip + 4 * j] * P[ip + 4 * j]);
+            double par21 = abr * exp(p32m * dist) * scr;
+            h[0] = vdist * (((P[ip + 4 * j - 2] + dist * (2.0 * P[ip + 4 * j - 1] + dist * (3.0 * P[ip + 4 * j + 1] +
+                             dist * (4.0 * P[ip + 4 * j + 2])))) + p32m * abr) * exp(p32m * dist) * scr + dsc * par21);
+        }
+        if (par->jsover) {
+            int usenew = realov && (jk1 == jk2);
+            int iop = ip_over(kinds, jk1, jk2);
+            /* setparv.f:640 tests nltype against 9000, a value input.f never leaves,
+             * so the polynomial forms below are always the ones taken */
+            for (int j = 1; j <= npk; ++j) {
+                double abr, d1;
+                double p32m = -(P[iop + 4 * j] * P[iop + 4 * j]);
+                if (usenew) {
+                    abr = ovlnull[j - 1] + dist * (P[iop + 4 * j - 3] + dist * (P[iop + 4 * j - 2] + dist * P[iop + 4 * j - 1]));
+                    d1 = P[iop + 4 * j - 3] + 2.0 * dist * P[iop + 4 * j - 2] + 3.0 * dist * dist * P[iop + 4 * j - 1];
+                } else {
+                    abr = P[iop + 4 * j - 3] + dist * (P[iop + 4 * j - 2] + dist * P[iop + 4 * j - 1]);
+                    d1 = P[iop + 4 * j - 2] + 2.0 * dist * P[iop + 4 * j - 1];
+                }
+                double ovl21 = abr * exp(p32m * dist) * scr;
+                o[j - 1] = vdist * ((d1 + p32m * abr) * exp(p32m * dist) * scr + dsc * ovl21);
+                if (usehar && j < npk) o[j - 1] = -harsign[j - 1] * o[j - 1] * (abr >= 0 ? 1.0 : -1.0);
+            }
+        }
+    }
+    for (int iat = 0; iat < st->natoms; ++iat) {
+        int jk1 = st->kkind[iat];
+        int ip = ip_density(jk1);
+        double vm13 = pow(den[iat * kinds + jk1 - 1], third);
+        double vm23 = vm13 * vm13, vm2t = 2.0 * vm23, vm3t = threeh * vm23;
+        double drho = twtrd * vden[iat * kinds + jk1 - 1] / vm13;
+        for (int k = 0; k < 4; ++k) {
+            dparos[4 * iat + k] = drho * (P[ip + 2] + vm2t * (P[ip + 3] + vm3t * P[ip + 4]));
+            ip += 4;
+        }
+        for (int jk2 = 1; jk2 <= kinds; ++jk2) {
+            double d = den[iat * kinds + jk2 - 1];
+            if (jk2 == jk1 || d == 0.0) continue;
+            vm13 = pow(d, third);
+            vm23 = vm13 * vm13; vm2t = 2.0 * vm23; vm3t = threeh * vm23;
+            drho = twtrd * vden[iat * kinds + jk2 - 1] / vm13;
+            ip = ip_cross_onsite(kinds, jk1, jk2);
+            for (int k = 0; k < 4; ++k) {
+                dparos[4 * iat + k] = dparos[4 * iat + k] +
+                    drho * (P[ip + 1] + vm2t * (P[ip + 2] + vm3t * P[ip + 3]));
+                ip += 3;
+            }
+        }
+    }
+    free(vden);
+    return NRLTB_OK;
+}
+
+/* ---------------------------------------------------------------------- */
+/* rotate (src/rotate.f:131-258): the parameter vector p(1..14) seen from
+ * (jkind(1), jkind(2)) after setham.f:318-344 filled par(:, jk2, jk1) and its
+ * mirrored slot, then the 9x9 Slater-Koster block e(i,j).                  */
+static void sk_params(const double *v, int k1, int k2, double p[14])
+{
+    for (int j = 0; j < 14; ++j) p[j] = v[j];
+    if (k1 == k2) {
+        p[10] = -v[1]; p[11] = v[4]; p[12] = -v[5]; p[13] = -v[6];
+    } else if (k1 > k2) {
+        p[1] = -v[10]; p[4] = v[11]; p[5] = -v[12]; p[6] = -v[13];
+        p[10] = -v[1]; p[11] = v[4]; p[12] = -v[5]; p[13] = -v[6];
+    }
+}
+
+static void sk_block(double l, double m, double n, const double p[14], int unlike, double e[9][9])
+{
+    const double rt3 = 1.732050807568877, half = 0.5;
+    const double rt3h = half * rt3, rt3q = half * rt3h, rt32 = 2.0 * rt3;
+    static const double parity[9] = {1, -1, -1, -1, 1, 1, 1, 1, 1};
+    double ll = l * l, mm = m * m, nn = n * n, lm = l * m, mn = m * n, nl = n * l, lmn = lm * n;
+    double P1 = p[0], P2 = p[1], P3 = p[2], P4 = p[3], P5 = p[4], P6 = p[5], P7 = p[6], P8 = p[7], P9 = p[8], P10 = p[9];
+    e[0][0] = P1;
+    e[0][1] = l * P2; e[0][2] = m * P2; e[0][3] = n * P2;
+    double rp5 = rt3 * P5;
+    e[0][4] = mn * rp5; e[0][5] = nl * rp5; e[0][6] = lm * rp5;
+    e[0][7] = half * rp5 * (ll - mm);
+    e[0][8] = (nn - half * (ll + mm)) * P5;
+    double p34 = P3 - P4;
+    e[1][1] = P4 + ll * p34; e[2][2] = P4 + mm * p34; e[3][3] = P4 + nn * p34;
+    e[1][2] = lm * p34; e[1][3] = nl * p34; e[2][3] = mn * p34;
+    double p67 = rt3 * P6 - 2.0 * P7;
+    e[1][4] = lmn * p67;
+    e[1][5] = n * (ll * p67 + P7);
+    e[1][6] = m * (ll * p67 + P7);
+    e[2][4] = n * (mm * p67 + P7);
+    e[2][5] = e[1][4];
+    e[2][6] = l * (mm * p67 + P7);
+    e[3][4] = m * (nn * p67 + P7);
+    e[3][5] = l * (nn * p67 + P7);
+    e[3][6] = e[1][4];
+    e[1][7] = l * (half * (ll - mm) * p67 + P7);
+    double p67a = P6 - rt3 * P7;
+    e[1][8] = l * (nn * p67a - (half * (ll + mm)) * P6);
+    e[2][7] = m * (half * (ll - mm) * p67 - P7);
+    e[2][8] = m * (nn * p67a - (half * (ll + mm)) * P6);
+    e[3][7] = n * (half * (ll - mm) * p67);
+    e[3][8] = n * (nn * P6 - half * (ll + mm) * (P6 - rt32 * P7));
+    double p8910 = (3.0 * P8 + P10) - 4.0 * P9;
+    e[4][4] = ll * P10 + mm * (nn * p8910) + (mm + nn) * P9;
+    double p910m = P9 - P10;
+    e[4][5] = lm * (p910m + nn * p8910);
+    e[4][6] = nl * (p910m + mm * p8910);
+    e[5][5] = mm * P10 + ll * (nn * p8910) + (ll + nn) * P9;
+    e[5][6] = mn * (p910m + ll * p8910);
+    e[6][6] = nn * P10 + ll * (mm * p8910) + (ll + mm) * P9;
+    e[4][7] = mn * ((half * (ll - mm)) * p8910 - p910m);
+    e[5][7] = nl * ((half * (ll - mm)) * p8910 + p910m);
+    e[6][7] = lm * (half * (ll - mm)) * p8910;
+    double p89 = P8 - 2.0 * P9, p8910a = p89 + P10, p8910b = p8910a + p89, p89m = P8 - P9;
+    e[4][8] = rt3 * mn * (nn * p89m - (half * (ll + mm)) * p8910a);
+    e[5][8] = rt3 * nl * (nn * p89m - (half * (ll + mm)) * p8910a);
+    e[6][8] = rt3h * lm * (P10 - (ll + mm) * P8 + nn * p8910b);
+    e[7][7] = (ll + mm) * P9 + nn * P10 + ((half * (ll - mm)) * (half * (ll - mm))) * p8910;
+    e[7][8] = rt3q * (ll - mm) * (P10 - (ll + mm) * P8 + nn * p8910b);
+    e[8][8] = nn * nn * P8 + (ll + mm) * (0.25 * (ll + mm) * (3.0 * P10 + P8) - nn * (P8 - 3.0 * P9));
+    for (int i = 1; i < 9; ++i)
+        for (int j = 0; j < i; ++j) e[i][j] = parity[i] * (e[j][i] * parity[j]);
+    if (unlike) {
+        double P11 = p[10], P12 = p[11], P13 = p[12], P14 = p[13];
+        e[1][0] = l * P11; e[2][0] = m * P11; e[3][0] = n * P11;
+        double rp12 = rt3 * P12;
+        e[4][0] = mn * rp12; e[5][0] = nl * rp12; e[6][0] = lm * rp12;
+        e[7][0] = half * rp12 * (ll - mm);
+        e[8][0] = (nn - half * (ll + mm)) * P12;
+        double p134 = rt3 * P13 - 2.0 * P14;
+        e[4][1] = lmn * p134;
+        e[5][1] = n * (ll * p134 + P14);
+        e[6][1] = m * (ll * p134 + P14);
+        e[4][2] = n * (mm * p134 + P14);
+        e[5][2] = e[4][1];
+        e[6][2] = l * (mm * p134 + P14);
+        e[4][3] = m * (nn * p134 + P14);
+        e[5][3] = l * (nn * p134 + P14);
+        e[6][3] = e[4][1];
+        e[7][1] = l * (half * (ll - mm) * p134 + P14);
+        double p134a = P13 - rt3 * P14;
+        e[8][1] = l * (nn * p134a - (half * (ll + mm)) * P13);
+        e[7][2] = m * (half * (ll - mm) * p134 - P14);
+        e[8][2] = m * (nn * p134a - (half * (ll + mm)) * P13);
+        e[7][3] = n * (half * (ll - mm) * p134);
+        e[8][3] = n * (nn * P13 - half * (ll + mm) * (P13 - rt32 * P14));
+    }
+}
+
+/* packed upper triangle, 0-based (i <= j): i + j(j+1)/2  (rotate.f:261-290) */
+static inline size_t pk(int i, int j) { return (size_t)i + (size_t)j * (j + 1) / 2; }
+
+/* setham / sethamv for one k: packed-upper H and S (or dH, dS) */
+void oracle_setham_packed(const nrltb_structure *st, const nrltb_params *par, const nrltb_pairs *pr,
+                          const double *hop, const double *over, const double *paros,
+                          const double *ak, int deriv, zc *hmat, zc *smat)
+{
+    const double tpi = 6.283185307179586;
+    int *ksk = (int *)malloc(sizeof(int) * (size_t)st->natoms);
+    int nv = 0;
+    for (int i = 0; i < st->natoms; ++i) { ksk[i] = nv; nv += par->kbas[st->kkind[i] - 1]; }
+    size_t npk = (size_t)nv * (nv + 1) / 2;
+    for (size_t i = 0; i < npk; ++i) { hmat[i] = 0; if (smat) smat[i] = 0; }
+    const double *posq = st->posq;
+    for (int p = 0; p < pr->npairs; ++p) {
+        int a1 = pr->jatm[2 * p] - 1, a2 = pr->jatm[2 * p + 1] - 1;
+        int k1 = pr->jkind[2 * p], k2 = pr->jkind[2 * p + 1];
+        int kk1 = ksk[a1], kk2 = ksk[a2];
+        int kb1 = par->kbas[k1 - 1], kb2 = par->kbas[k2 - 1];
+        double dot = 0.0;
+        {
+            double q[3];
+            for (int c = 0; c < 3; ++c) {
+                double pq2 = posq ? posq[3 * a2 + c] : 0.0, pq1 = posq ? posq[3 * a1 + c] : 0.0;
+                q[c] = (double)pr->dlv[3 * p + c] - pq2 + pq1;
+            }
+            dot = ak[0] * q[0] + ak[1] * q[1] + ak[2] * q[2];
+        }
+        double cs = cos(tpi * dot), sn = sin(tpi * dot);
+        double e[9][9], pv[14];
+        for (int pass = 0; pass < 2; ++pass) {
+            zc *mat = pass == 0 ? hmat : smat;
+            if (pass == 1 && (!par->jsover || !smat)) break;
+            sk_params((pass == 0 ? hop : over) + 14 * p, k1, k2, pv);
+            sk_block(pr->tt[3 * p], pr->tt[3 * p + 1], pr->tt[3 * p + 2], pv, k1 != k2, e);
+            if (kk2 > kk1) {
+                for (int j = 0; j < kb2; ++j)
+                    for (int i = 0; i < kb1; ++i)
+                        mat[pk(kk1 + i, kk2 + j)] += CMPLX(e[i][j] * cs, e[i][j] * sn);
+            } else {
+                for (int j = 0; j < kb2; ++j)
+                    for (int i = 0; i <= j; ++i)
+                        mat[pk(kk1 + i, kk2 + j)] += CMPLX(e[i][j] * cs, e[i][j] * sn);
+            }
+        }
+    }
+    /* on-site terms, setham.f:399-453 / sethamv.f:314-349 */
+    for (int iat = 0; iat < st->natoms; ++iat) {
+        int kk = ksk[iat], kb = par->kbas[st->kkind[iat] - 1];
+        for (int j = 1; j <= kb; ++j) {
+            int cls = (j == 1) ? 0 : (j <= 4) ? 1 : (j <= 7) ? 2 : 3;
+            int d = kk + j - 1;
+            hmat[pk(d, d)] += paros[4 * iat + cls];
+            if (!deriv && par->jsover && smat) smat[pk(d, d)] += 1.0;
+        }
+    }
+    free(ksk);
+}
+
+/* ---------------------------------------------------------------------- */
+/* perturb (src/perturb.f:73-216); the reference's nine-fold degeneracy
+ * limit (perturb.f:47,106) is lifted: larger groups go through zhpev.      */
+static int oracle_perturb(int n, const zc *dh, const zc *ds, const zc *z, const double *eig,
+                          double eigcut, int *ntot, double *deig)
+{
+    const double tol = 1e-8;
+    zc *work = (zc *)malloc(sizeof(zc) * (size_t)n);
+    int start = 0;
+    while (1) {
+        if (eig[start] > eigcut) { *ntot = start; free(work); return 0; }
+        int num = n - start;
+        for (int j = start + 1; j < n; ++j)
+            if (fabs(eig[j] - eig[start]) > tol) { num = j - start; break; }
+        zc *hd = (zc *)malloc(sizeof(zc) * (size_t)num * (num + 1) / 2);
+        int m = 0;
+        for (int i = 0; i < num; ++i) {
+            int is = start + i;
+            for (int j = 0; j < n; ++j) {
+                zc csum = 0;
+                for (int k = 0; k < j; ++k) {
+                    size_t mjk = pk(k, j); /* element (k, j), k < j, conjugated for row j */
+                    csum += conj(dh[mjk] - eig[start] * ds[mjk]) * z[(size_t)is * n + k];
+                }
+                for (int k = j; k < n; ++k) {
+                    size_t mjk = pk(j, k);
+                    csum += (dh[mjk] - eig[start] * ds[mjk]) * z[(size_t)is * n + k];
+                }
+                work[j] = csum;
+            }
+            for (int j = 0; j <= i; ++j) {
+                int js = start + j;
+                zc csum = 0;
+                for (int k = 0; k < n; ++k) csum += conj(z[(size_t)js * n + k]) * work[k];
+                hd[m++] = csum;
+            }
+        }
+        if (num == 1) {
+            deig[start] = creal(hd[0]);
+        } else if (num == 2) {
+            double sq = sqrt(creal(hd[0] - hd[2]) * creal(hd[0] - hd[2]) + 4.0 * creal(conj(hd[1]) * hd[1]));
+            deig[start] = 0.5 * (creal(hd[0] + hd[2]) - sq);
+            deig[start + 1] = 0.5 * (creal(hd[0] + hd[2]) + sq);
+        } else {
+            char jobz = 'N', uplo = 'U';
+            int info = 0, ld = 1;
+            double *seig = (double *)malloc(sizeof(double) * num);
+            zc *zw = (zc *)malloc(sizeof(zc) * (2 * num));
+            double *rw = (double *)malloc(sizeof(double) * (3 * num));
+            zc zd[1];
+            p_zhpev(&jobz, &uplo, &num, hd, seig, zd, &ld, zw, rw, &info);
+            for (int i = 0; i < num; ++i) deig[start + i] = seig[i];
+            free(seig); free(zw); free(rw);
+            if (info != 0) { free(hd); free(work); return -1; }
+        }
+        free(hd);
+        start = start + num;
+        if (start >= n) break;
+    }
+    *ntot = n;
+    free(work);
+    return 0;
+}
+
+/* ---------------------------------------------------------------------- */
+/* fermi (src/fermi.f:162-425); el = 2 (non-spin), eigen[k][nv] ascending   */
+double oracle_fermi(int nv, int nk, const double *eigen, const double *w, double tkb,
+                    double zfill, double tol, int *iterations)
+{
+    const double nearz = 1e-5, el = 2.0;
+    if (tol <= 0) tol = 1e-8;
+    int it = 0;
+    double beta = (tkb < nearz) ? 1.0 / nearz : 1.0 / tkb;
+    int nfill = (int)(zfill / el + nearz);
+    int linst = fabs(zfill / el - (double)nfill) < tol;
+    double muhigh = eigen[nv - 1], mulow = eigen[0];
+    double stlow = eigen[nfill - 1], sthigh = eigen[nfill < nv ? nfill : nv - 1];
+    for (int k = 0; k < nk; ++k) {
+        const double *e = eigen + (size_t)k * nv;
+        if (e[nfill - 1] > stlow) stlow = e[nfill - 1];
+        if (nfill < nv && e[nfill] < sthigh) sthigh = e[nfill];
+        for (int i = 0; i < nv; ++i) {
+            if (e[i] > muhigh) muhigh = e[i];
+            if (e[i] < mulow) mulow = e[i];
+        }
+    }
+    if (linst && (sthigh - stlow > 20.0 * tkb)) {
+        if (iterations) *iterations = 0;
+        return 0.5 * (stlow + sthigh);
+    }
+    double mu = 0.5 * (stlow + sthigh);
+    for (;;) {
+        ++it;
+        double nsum = 0, dnsum = 0;
+        double mum20 = mu - tkb * 20.0, mup20 = mu + tkb * 20.0, btmu = -beta * mu;
+        for (int k = 0; k < nk; ++k) {
+            const double *e = eigen + (size_t)k * nv;
+            double nks = 0, dnks = 0;
+            for (int i = 0; i < nv; ++i) {
+                if (e[i] < mum20) nks = nks + 1.0;
+                else if (e[i] < mup20) {
+                    double ex = exp(beta * e[i] + btmu);
+                    double f = 1.0 / (1.0 + ex);
+                    nks = nks + f;
+                    dnks = dnks + ex * f * f;
+                } else break;
+            }
+            nsum = nsum + w[k] * nks;
+            dnsum = dnsum + w[k] * dnks;
+        }
+        nsum = el * nsum;
+        dnsum = beta * el * dnsum;
+        if (fabs(nsum - zfill) < tol) break;
+        if (nsum < zfill) mulow = mu; else muhigh = mu;
+        double mu1;
+        if (dnsum < tol) mu1 = 0.5 * (mulow + muhigh);
+        else {
+            mu1 = mu + (zfill - nsum) / dnsum;
+            if (mu1 > muhigh) mu1 = 0.5 * (mu + muhigh);
+            else if (mu1 < mulow) mu1 = 0.5 * (mu + mulow);
+        }
+        if (muhigh - mulow > tol) mu = mu1;
+        else break;
+        if (it > 100000) break;
+    }
+    if (iterations) *iterations = it;
+    return mu;
+}
+
+/* ---------------------------------------------------------------------- */
+/* full-k-path helpers                                                      */
+typedef struct {
+    nrltb_pairs pr;
+    double *hop, *over, *paros, *den, *dhop, *dover, *dparos;
+    int nv;
+} orc_struct;
+
+static int alloc_pairs(nrltb_pairs *pr, int cap)
+{
+    pr->capacity = cap; pr->npairs = 0;
+    pr->tt = (double *)malloc(sizeof(double) * 3 * (size_t)cap);
+    pr->dlv = (int *)malloc(sizeof(int) * 3 * (size_t)cap);
+    pr->dist = (double *)malloc(sizeof(double) * (size_t)cap);
+    pr->screen = (double *)malloc(sizeof(double) * (size_t)cap);
+    pr->dscrn = (double *)malloc(sizeof(double) * (size_t)cap);
+    pr->jkind = (int *)malloc(sizeof(int) * 2 * (size_t)cap);
+    pr->jatm = (int *)malloc(sizeof(int) * 2 * (size_t)cap);
+    return (pr->tt && pr->dlv && pr->dist && pr->screen && pr->dscrn && pr->jkind && pr->jatm) ? 0 : -1;
+}
+static void free_pairs(nrltb_pairs *pr)
+{
+    free(pr->tt); free(pr->dlv); free(pr->dist); free(pr->screen); free(pr->dscrn);
+    free(pr->jkind); free(pr->jatm);
+}
+
+/* Pair count upper bound for allocation: atoms pairs x search box. */
+static long pair_bound(const nrltb_structure *st)
+{
+    long box = (long)(2 * st->nd[0] + 1) * (2 * st->nd[1] + 1) * (2 * st->nd[2] + 1);
+    return (long)st->natoms * (st->natoms + 1) / 2 * box;
+}
+
+/* Expand packed-upper to full column-major (lower = conjugate). */
+void oracle_unpack(int n, const zc *ap, zc *full)
+{
+    for (int j = 0; j < n; ++j)
+        for (int i = 0; i <= j; ++i) {
+            full[(size_t)j * n + i] = ap[pk(i, j)];
+            full[(size_t)i * n + j] = conj(ap[pk(i, j)]);
+        }
+}
+
+/* Dense H, S (or dH, dS) for each k, full column-major, for parity tests. */
+int oracle_setham(const nrltb_structure *st, const nrltb_params *par, const nrltb_kmesh *km,
+                  int which, int kneigh_in, double *hout, double *sout)
+{
+    nrltb_pairs pr;
+    long cap = pair_bound(st);
+    if (alloc_pairs(&pr, (int)cap)) return NRLTB_E_NOMEM;
+    oracle_search2(st, par, kneigh_in, &pr, NULL, NULL);
+    int nv = 0;
+    for (int i = 0; i < st->natoms; ++i) nv += par->kbas[st->kkind[i] - 1];
+    size_t P = (size_t)pr.npairs;
+    double *hop = calloc(14 * P + 1, 8), *over = calloc(14 * P + 1, 8);
+    double *paros = calloc(4 * (size_t)st->natoms, 8), *den = calloc((size_t)st->natoms * par->kinds, 8);
+    double *dhop = calloc(14 * P + 1, 8), *dover = calloc(14 * P + 1, 8), *dparos = calloc(4 * (size_t)st->natoms, 8);
+    oracle_setpar(st, par, &pr, hop, over, paros, den);
+    if (which == 1) oracle_setparv(st, par, &pr, den, dhop, dover, dparos);
+    size_t np = (size_t)nv * (nv + 1) / 2, nn = (size_t)nv * nv;
+    int rc = NRLTB_OK;
+#pragma omp parallel for schedule(dynamic)
+    for (int k = 0; k < km->nk; ++k) {
+        zc *hp = malloc(sizeof(zc) * np), *sp = malloc(sizeof(zc) * np);
+        if (which == 1)
+            oracle_setham_packed(st, par, &pr, dhop, dover, dparos, km->k + 3 * k, 1, hp, sp);
+        else
+            oracle_setham_packed(st, par, &pr, hop, over, paros, km->k + 3 * k, 0, hp, sp);
+        oracle_unpack(nv, hp, (zc *)hout + nn * k);
+        if (sout) oracle_unpack(nv, sp, (zc *)sout + nn * k);
+        free(hp); free(sp);
+    }
+    free(hop); free(over); free(paros); free(den); free(dhop); free(dover); free(dparos);
+    free_pairs(&pr);
+    return rc;
+}
+
+/* diag (src/diag.f:320-455) on packed H, S; returns ioverr. */
+static int oracle_diag_packed(int n, int want_vec, int jsover, zc *hp, zc *sp, double *en, zc *z)
+{
+    if (n == 1) {
+        if (jsover) {
+            double h1 = creal(hp[0]), s1 = creal(sp[0]);
+            if (s1 > 0) { en[0] = h1 / s1; if (z) z[0] = 1.0 / sqrt(s1); return 0; }
+            en[0] = fabs(h1 / s1); return 1;
+        }
+        en[0] = creal(hp[0]); if (z) z[0] = 1.0; return 0;
+    }
+    size_t np = (size_t)n * (n + 1) / 2;
+    zc *s1 = malloc(sizeof(zc) * np);
+    if (jsover) memcpy(s1, sp, sizeof(zc) * np);
+    zc *work = malloc(sizeof(zc) * (2 * (size_t)n));
+    double *rwork = malloc(sizeof(double) * (3 * (size_t)n));
+    zc zdummy[1];
+    int info = 0, one = 1, ldz = want_vec ? n : 1;
+    char jobz = want_vec ? 'V' : 'N', uplo = 'U';
+    if (jsover) p_zhpgv(&one, &jobz, &uplo, &n, hp, sp, en, want_vec ? z : zdummy, &ldz, work, rwork, &info);
+    else p_zhpev(&jobz, &uplo, &n, hp, en, want_vec ? z : zdummy, &ldz, work, rwork, &info);
+    int ioverr = 0;
+    if (info != 0) {
+        /* diag.f:429-455: report the overlap's own eigenvalues in en */
+        char jn = 'N';
+        int ld1 = 1;
+        p_zhpev(&jn, &uplo, &n, s1, en, zdummy, &ld1, work, rwork, &info);
+        ioverr = 1;
+    }
+    free(s1); free(work); free(rwork);
+    return ioverr;
+}
+
+/* Generalized eigensolve of full column-major H, S (parity of the solver alone). */
+int oracle_diag_dense(int nv, int nk, const double *hd, const double *sd, double *eig, double *zout,
+                      int *status)
+{
+    size_t nn = (size_t)nv * nv, np = (size_t)nv * (nv + 1) / 2;
+#pragma omp parallel for schedule(dynamic)
+    for (int k = 0; k < nk; ++k) {
+        const zc *H = (const zc *)hd + nn * k, *S = (const zc *)sd + nn * k;
+        zc *hp = malloc(sizeof(zc) * np), *sp = malloc(sizeof(zc) * np);
+        for (int j = 0; j < nv; ++j)
+            for (int i = 0; i <= j; ++i) { hp[pk(i, j)] = H[(size_t)j * nv + i]; sp[pk(i, j)] = S[(size_t)j * nv + i]; }
+        int st = oracle_diag_packed(nv, zout != NULL, 1, hp, sp, eig + (size_t)k * nv, zout ? (zc *)zout + nn * k : NULL);
+        if (status) status[k] = st ? NRLTB_K_S_NOT_PD : NRLTB_K_OK;
+        free(hp); free(sp);
+    }
+    return NRLTB_OK;
+}
+
+/* ---------------------------------------------------------------------- */
+/* bande (src/bande.f:816-1446) for one structure, k loop parallel over
+ * threads (the reference's k data parallelism, one k per thread).          */
+int oracle_bande(const nrltb_structure *st, const nrltb_params *par, const nrltb_kmesh *km,
+                 const nrltb_opts *opt, nrltb_result *res, int nthreads)
+{
+    if (!p_zhpgv || !p_zhpev) return NRLTB_E_ARG;
+    int lpress = (opt->mode == 2 || opt->mode == 4);
+    int nv = 0;
+    double zfill = st->zcharge;
+    for (int i = 0; i < st->natoms; ++i) { nv += par->kbas[st->kkind[i] - 1]; zfill += par->valence[st->kkind[i] - 1]; }
+    nrltb_pairs pr;
+    long cap = pair_bound(st);
+    if (alloc_pairs(&pr, (int)cap)) return NRLTB_E_NOMEM;
+    int kneigh_out = 0;
+    double dismin = 0;
+    oracle_search2(st, par, opt->kneigh_in, &pr, &kneigh_out, &dismin);
+    size_t P = (size_t)pr.npairs;
+    double *hop = calloc(14 * P + 1, 8), *over = calloc(14 * P + 1, 8);
+    double *paros = calloc(4 * (size_t)st->natoms, 8), *den = calloc((size_t)st->natoms * par->kinds, 8);
+    double *dhop = calloc(14 * P + 1, 8), *dover = calloc(14 * P + 1, 8), *dparos = calloc(4 * (size_t)st->natoms, 8);
+    oracle_setpar(st, par, &pr, hop, over, paros, den);
+    if (lpress) oracle_setparv(st, par, &pr, den, dhop, dover, dparos);
+    int nk = km->nk;
+    double *esk = malloc(sizeof(double) * (size_t)nv * nk);
+    double *desk = calloc((size_t)nv * nk, sizeof(double));
+    int *ncut = calloc((size_t)nk, sizeof(int));
+    int *kst = calloc((size_t)nk, sizeof(int));
+    size_t np = (size_t)nv * (nv + 1) / 2;
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#endif
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int k = 0; k < nk; ++k) {
+        zc *hp = malloc(sizeof(zc) * np), *sp = malloc(sizeof(zc) * np);
+        zc *z = lpress ? malloc(sizeof(zc) * (size_t)nv * nv) : NULL;
+        oracle_setham_packed(st, par, &pr, hop, over, paros, km->k + 3 * k, 0, hp, sp);
+        int ioverr = oracle_diag_packed(nv, lpress, par->jsover, hp, sp, esk + (size_t)k * nv, z);
+        kst[k] = ioverr ? NRLTB_K_S_NOT_PD : NRLTB_K_OK;
+        if (!ioverr && lpress) {
+            oracle_setham_packed(st, par, &pr, dhop, dover, dparos, km->k + 3 * k, 1, hp, sp);
+            if (!par->jsover) for (size_t i = 0; i < np; ++i) sp[i] = 0;
+            oracle_perturb(nv, hp, sp, z, esk + (size_t)k * nv, opt->eigcut, &ncut[k], desk + (size_t)k * nv);
+        }
+        free(hp); free(sp); free(z);
+    }
+    /* fermi.f, then the sums of bande.f:1162-1330 in the reference's k order */
+    double tkb = opt->tkb;
+    double efermi = oracle_fermi(nv, nk, esk, km->w, tkb, zfill, opt->fermi_tol, NULL);
+    double tkbi = (tkb < 1e-5) ? 1e5 : 1.0 / tkb;
+#define FB(x) (1.0 / (1.0 + exp(tkbi * (x))))
+    double etol = 20.0 * tkb, efp = efermi + etol, efm = efermi - etol;
+    double esum = 0, desum1 = 0, desum2 = 0, desum3 = 0, dfbsum = 0, dferm = 0;
+    const double sfac = 2.0;
+    for (int k = 0; k < nk; ++k) {
+        const double *e = esk + (size_t)k * nv, *de = desk + (size_t)k * nv;
+        double wt = sfac * km->w[k];
+        int nlim = lpress ? ncut[k] : nv;
+        for (int i = 0; i < nlim; ++i) {
+            if (!(e[i] < efp)) continue;
+            double ewt = wt * e[i];
+            if (e[i] < efm) {
+                esum = esum + ewt;
+                if (lpress) desum1 = desum1 + wt * de[i];
+            } else {
+                double fbe = FB(e[i] - efermi);
+                esum = esum + ewt * fbe;
+                if (lpress) {
+                    double dfbe = -tkbi * FB(e[i] - efermi) * FB(-(e[i] - efermi));
+                    dfbsum = dfbsum + dfbe * wt;
+                    desum3 = desum3 + dfbe * ewt;
+                    double dewt = wt * de[i];
+                    desum1 = desum1 + dewt * fbe;
+                    dferm = dferm + dfbe * dewt;
+                    desum2 = desum2 + dfbe * ewt * de[i];
+                }
+            }
+        }
+    }
+#undef FB
+    res->efermi = efermi;
+    res->e_total = esum;
+    res->fermi_shift = 0;
+    res->pressure = 0;
+    if (lpress) {
+        double dfermi = (fabs(dfbsum) > 1e-10) ? dferm / dfbsum : 0.0;
+        res->fermi_shift = dfermi;
+        res->pressure = -(desum1 + (desum2 - dfermi * desum3));
+    }
+    res->dismin = dismin;
+    res->npairs = pr.npairs;
+    res->nv = nv;
+    res->nk = nk;
+    res->kneigh_out = kneigh_out;
+    res->nonphysical_k = 0;
+    for (int k = 0; k < nk; ++k) res->nonphysical_k += (kst[k] != 0);
+    if (res->eig) memcpy(res->eig, esk, sizeof(double) * (size_t)nv * nk);
+    if (res->deig) memcpy(res->deig, desk, sizeof(double) * (size_t)nv * nk);
+    if (res->ncut) memcpy(res->ncut, ncut, sizeof(int) * (size_t)nk);
+    if (res->k_status) memcpy(res->k_status, kst, sizeof(int) * (size_t)nk);
+    free(esk); free(desk); free(ncut); free(kst);
+    free(hop); free(over); free(paros); free(den); free(dhop); free(dover); free(dparos);
+    free_pairs(&pr);
+    return NRLTB_OK;
+}
+
+/* Timing helper for the CPU baseline: setham + diag (+ sethamv + perturb in
+ * mode 4) for k points [k0, k1) only, all host threads; no Fermi/sums. */
+int oracle_ksolve_sample(const nrltb_structure *st, const nrltb_params *par, const nrltb_kmesh *km,
+                         const nrltb_opts *opt, int k0, int k1, int nthreads, double *eig_out)
+{
+    nrltb_kmesh sub = *km;
+    sub.nk = k1 - k0;
+    sub.k = km->k + 3 * k0;
+    sub.w = km->w + k0;
+    nrltb_result r;
+    memset(&r, 0, sizeof r);
+    r.eig = eig_out;
+    return oracle_bande(st, par, &sub, opt, &r, nthreads);
+}
+
+int oracle_pair_bound(const nrltb_structure *st) { return (int)pair_bound(st); }

@@ -1,0 +1,43 @@
+"""The C-ABI libraries load and export every entry point include/*.h declares
+(no compute calls: these run without a GPU)."""
+import ctypes
+import os
+import re
+
+from conftest import REPO
+from nrltb import abi, build
+
+
+def _declared(header):
+    txt = open(os.path.join(REPO, "include", header)).read()
+    return set(re.findall(r"^\s*(?:int|void|long long|const char \*)\s*\**\s*(nrltb_\w+)\s*\(", txt, re.M))
+
+
+def test_library_builds_and_exports_all_symbols():
+    build.build_all()
+    lib = ctypes.CDLL(abi.GPU_LIB)
+    names = _declared("nrltb.h") | _declared("nrltb_input.h")
+    assert len(names) >= 20
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_abi_version_and_error_string():
+    lib = abi.load_gpu()
+    assert lib.nrltb_abi_version() == 1
+    assert isinstance(lib.nrltb_last_error(), bytes)
+
+
+def test_host_library_symbols():
+    lib = ctypes.CDLL(abi.HOST_LIB)
+    for n in _declared("nrltb_input.h"):
+        assert hasattr(lib, n), n
+
+
+def test_bad_arguments_fail_cleanly():
+    lib = abi.load_gpu()
+    # null context / pointers are rejected before any device work
+    assert lib.nrltb_bande(None, None, None, None, None, None) == abi.NRLTB_E_ARG
+    assert lib.nrltb_fetch(None, None) == abi.NRLTB_E_ARG
+    assert lib.nrltb_ctx_create(None, 0) == abi.NRLTB_E_ARG
+    assert lib.nrltb_nparams(2) == 330 and lib.nrltb_nparams(1) == 97

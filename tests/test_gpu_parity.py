@@ -1,0 +1,216 @@
+"""GPU path (through the C ABI) against the oracle and the ex1 goldens.
+
+Tolerances (FP64 form): eigenvalues 1e-10 Ry, E_F 1e-9 Ry, E_total 1e-8 Ry/atom,
+pressure 1e-3 kbar = 6.8e-9 Ry/bohr^3; integer pair lists and their order exact.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from nrltb import KMesh, Opts, synth
+
+pytestmark = pytest.mark.gpu
+
+KBAR = 1.0 / 147105.08      # Ry/bohr^3 per kbar
+P_TOL = 1e-3 * KBAR
+
+
+def _sub(km, idx):
+    idx = np.asarray(idx)
+    w = km.w[idx] / km.w[idx].sum()
+    return KMesh(km.k[idx], w)
+
+
+def _structs(ex1):
+    out = [(ex1.structures[i][2], ex1.params) for i in (0, 7, 9, 17)]
+    for name in ("fcc1", "bcc32", "fcc128", "b2_216"):
+        st, par, km, _ = synth.CONFIGS[name]()
+        out.append((st, par))
+    return out
+
+
+def test_search2_bit_exact(ctx, ex1):
+    for st, par in _structs(ex1):
+        g, gk, gd = ctx.search2(st, par)
+        o, ok, od = oracle.search2(st, par)
+        assert len(g["dist"]) == len(o["dist"])
+        for key in ("dlv", "jkind", "jatm"):
+            assert np.array_equal(g[key], o[key]), key
+        assert np.array_equal(g["dist"], o["dist"])       # same ops, no contraction
+        assert np.array_equal(g["tt"], o["tt"])
+        np.testing.assert_allclose(g["screen"], o["screen"], rtol=1e-14, atol=0)
+        np.testing.assert_allclose(g["dscrn"], o["dscrn"], rtol=1e-13, atol=1e-300)
+        assert gk == ok and gd == od
+
+
+def test_search2_carried_flag(ctx, ex1):
+    st, par = ex1.structures[0][2], ex1.params
+    for kin in (0, 1):
+        g, gk, _ = ctx.search2(st, par, kneigh_in=kin)
+        o, ok, _ = oracle.search2(st, par, kneigh_in=kin)
+        assert len(g["dist"]) == len(o["dist"]) and gk == ok
+
+
+def test_search2_empty_pair_list(ctx):
+    from nrltb import Params, Structure
+    _, par, _, _ = synth.fcc1()
+    tiny = Params(par.kinds, par.kbas, par.valence, np.array([1.0]), np.array([0.5]), par.param)
+    plv = np.eye(3) * 10.0
+    st = Structure(np.array([1], np.int32), np.zeros((1, 3)), plv, (1, 1, 1), 1000.0)
+    g, _, _ = ctx.search2(st, tiny)
+    assert len(g["dist"]) == 0
+
+
+def test_setpar_matches_oracle(ctx, ex1):
+    for st, par in _structs(ex1):
+        pairs, _, _ = oracle.search2(st, par)
+        o = oracle.setpar(st, par, pairs, deriv=True)
+        g = ctx.setpar(st, par, pairs, deriv=True)
+        for key in ("hop", "over", "dhop", "dover"):
+            scale = max(np.abs(o[key]).max(), 1e-300)
+            np.testing.assert_allclose(g[key], o[key], rtol=1e-13, atol=1e-15 * scale, err_msg=key)
+        for key in ("den", "paros", "dparos"):
+            np.testing.assert_allclose(g[key], o[key], rtol=1e-12, atol=1e-15, err_msg=key)
+
+
+@pytest.mark.parametrize("which", [0, 1])
+def test_setham_matches_oracle(ctx, ex1, which):
+    cases = [(ex1.structures[0][2], ex1.params, ex1.structures[0][3]),
+             (ex1.structures[17][2], ex1.params, ex1.structures[17][3])]
+    st, par, km, _ = synth.bcc32()
+    cases.append((st, par, _sub(km, [0, 5, 63])))
+    st, par, km, _ = synth.fcc128()
+    cases.append((st, par, _sub(km, [4])))
+    st, par, km, _ = synth.b2_216()
+    cases.append((st, par, _sub(km, [3])))
+    for st, par, km in cases:
+        gh, gs = ctx.setham(st, par, km, which)
+        oh, os_ = oracle.setham(st, par, km, which)
+        for g, o in ((gh, oh), (gs, os_)):
+            scale = max(np.abs(o).max(), 1e-300)
+            assert np.abs(g - o).max() <= 1e-13 * scale + 1e-300
+
+
+def _check_eigs(ctx, H, S, tol=1e-10):
+    ge, gz, gst = ctx.diag(H, S)
+    oe, _, ost = oracle.diag(H, S, vectors=False)
+    assert (gst == 0).all() and (ost == 0).all()
+    assert np.abs(ge - oe).max() <= tol, np.abs(ge - oe).max()
+    for k in range(H.shape[0]):
+        Z = gz[k]
+        res = H[k] @ Z - (S[k] @ Z) * ge[k][None, :]
+        assert np.abs(res).max() < 1e-10 * max(1.0, np.abs(H[k]).max())
+        G = Z.conj().T @ S[k] @ Z
+        assert np.abs(G - np.eye(len(G))).max() < 1e-10
+    return ge
+
+
+def test_diag_fp64_small(ctx, ex1):
+    st, par, km = ex1.structures[0][2], ex1.params, ex1.structures[0][3]
+    H, S = oracle.setham(st, par, km)
+    _check_eigs(ctx, H, S)
+
+
+def test_diag_fp64_n288(ctx):
+    st, par, km, _ = synth.bcc32()
+    H, S = oracle.setham(st, par, _sub(km, [0, 21]))
+    _check_eigs(ctx, H, S)
+
+
+def test_diag_fp64_n1152(ctx):
+    st, par, km, _ = synth.fcc128()
+    H, S = oracle.setham(st, par, _sub(km, [13]))
+    _check_eigs(ctx, H, S)
+
+
+def test_diag_degenerate_and_tiny(ctx):
+    # exactly degenerate spectrum (block-diagonal copies) and a 1x1 problem
+    rng = np.random.default_rng(5)
+    A = rng.normal(size=(6, 6)) + 1j * rng.normal(size=(6, 6))
+    A = A + A.conj().T
+    H = np.zeros((1, 18, 18), complex)
+    for b in range(3):
+        H[0, 6 * b:6 * b + 6, 6 * b:6 * b + 6] = A
+    S = np.eye(18)[None].astype(complex)
+    _check_eigs(ctx, H, S)
+    H1 = np.array([[[2.5 + 0j]]])
+    S1 = np.array([[[1.25 + 0j]]])
+    ge, gz, _ = ctx.diag(H1, S1)
+    assert ge[0, 0] == pytest.approx(2.0, abs=1e-15)
+
+
+def test_diag_overlap_not_positive_definite(ctx):
+    # a host-made failure: indefinite S is reported per k, nothing faults
+    H = np.diag([1.0, 2.0, 3.0]).astype(complex)[None]
+    S = np.diag([1.0, -0.5, 1.0]).astype(complex)[None]
+    _, _, st = ctx.diag(H, S)
+    assert st[0] == 1
+
+
+def test_fermi_matches_oracle(ctx):
+    rng = np.random.default_rng(3)
+    eig = np.sort(rng.uniform(-1, 1, (27, 40)), axis=1)
+    w = np.full(27, 1 / 27)
+    for zfill, tkb in ((31.0, 0.005), (40.0, 0.01), (2.0, 0.001)):
+        ef_g = ctx.fermi(eig, w, tkb, zfill, tol=1e-12)
+        ef_o = oracle.fermi(eig, w, tkb, zfill, tol=1e-12)
+        assert ef_g == pytest.approx(ef_o, abs=1e-11)
+
+
+@pytest.mark.parametrize("idx", [0, 4, 8, 9, 13, 17])
+def test_bande_ex1_against_skout(ctx, ex1, ex1_gold, idx):
+    _, _, st, km = ex1.structures[idx]
+    r = ctx.bande(st, ex1.params, km, Opts(mode=4, tkb=ex1.tkb, eigcut=ex1.eigcut))
+    assert r.npairs == ex1_gold["npairs"][idx]
+    assert r.efermi == pytest.approx(ex1_gold["efermi"][idx], abs=1e-10)
+    assert r.e_total == pytest.approx(ex1_gold["e_total"][idx], abs=1e-10)
+    assert r.pressure == pytest.approx(ex1_gold["pressure"][idx], abs=1e-11)
+    assert r.fermi_shift == pytest.approx(ex1_gold["fermi_shift"][idx], abs=1e-11)
+
+
+def _compare_bande(ctx, st, par, km, tkb, nthreads=0, mode=4):
+    opts = Opts(mode=mode, tkb=tkb, eigcut=1e3, fermi_tol=1e-11)
+    g = ctx.bande(st, par, km, opts)
+    o = oracle.bande(st, par, km, opts, nthreads=nthreads)
+    assert g.npairs == o.npairs and g.nv == o.nv
+    assert np.abs(g.eig - o.eig).max() <= 1e-10
+    assert abs(g.efermi - o.efermi) <= 1e-9
+    assert abs(g.e_total - o.e_total) / st.natoms <= 1e-8
+    if mode == 4:
+        assert abs(g.pressure - o.pressure) <= P_TOL
+        # group sums of deig are invariant under rotations inside degenerate groups
+        for k in range(km.nk):
+            e = o.eig[k]
+            grp = np.concatenate([[0], np.cumsum(np.abs(np.diff(e)) > 1e-8)])
+            for gid in np.unique(grp):
+                m = grp == gid
+                assert abs(g.deig[k][m].sum() - o.deig[k][m].sum()) <= 1e-9 * max(1, m.sum())
+    return g, o
+
+
+def test_bande_fcc1_full_mesh(ctx):
+    st, par, km, o = synth.fcc1()
+    _compare_bande(ctx, st, par, km, o["tkb"])
+
+
+def test_bande_bcc32_subset(ctx):
+    st, par, km, o = synth.bcc32()
+    _compare_bande(ctx, st, par, _sub(km, [0, 9, 18, 27, 36, 45, 54, 63]), o["tkb"])
+
+
+def test_bande_mode3_energy_only(ctx, ex1):
+    _, _, st, km = ex1.structures[2]
+    _compare_bande(ctx, st, ex1.params, km, ex1.tkb, mode=3)
+
+
+def test_bande_nonpositive_overlap_kpoints(ctx):
+    # A parameter draw whose S(k) is indefinite at some k (made on the host, no
+    # device fault): those k carry the eigenvalues of S and no pressure terms,
+    # as diag.f:429-455 and bande.f:997-1003 leave them, and are counted.
+    st, _, km, _ = synth.fcc1()
+    par = synth.make_params([9], [11.0], 11)
+    sub = _sub(km, [0, 340, 471, 900, 1727])
+    g, o = _compare_bande(ctx, st, par, sub, 0.005)
+    assert o.nonphysical_k >= 2
+    assert g.nonphysical_k == o.nonphysical_k
+    assert np.array_equal(g.k_status, o.k_status)

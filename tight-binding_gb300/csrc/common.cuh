@@ -1,0 +1,91 @@
+// common.cuh -- shared helpers of the GB300 NRL tight-binding library:
+// complex arithmetic on interleaved (re, im) pairs, launch accounting and
+// error propagation into the context.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+
+namespace nrltb {
+
+// ---- complex arithmetic on float2 / double2 --------------------------------
+template <typename T> struct cplx;
+template <> struct cplx<float> { typedef float2 t; };
+template <> struct cplx<double> { typedef double2 t; };
+
+__host__ __device__ __forceinline__ double2 mk(double r, double i) { return make_double2(r, i); }
+__host__ __device__ __forceinline__ float2 mk(float r, float i) { return make_float2(r, i); }
+template <typename T> __host__ __device__ __forceinline__ typename cplx<T>::t cmk(T r, T i) { return mk(r, i); }
+
+template <typename C> __host__ __device__ __forceinline__ C cadd(C a, C b) { C r; r.x = a.x + b.x; r.y = a.y + b.y; return r; }
+template <typename C> __host__ __device__ __forceinline__ C csub(C a, C b) { C r; r.x = a.x - b.x; r.y = a.y - b.y; return r; }
+template <typename C> __host__ __device__ __forceinline__ C cmul(C a, C b)
+{
+    C r;
+    r.x = a.x * b.x - a.y * b.y;
+    r.y = a.x * b.y + a.y * b.x;
+    return r;
+}
+// conj(a) * b
+template <typename C> __host__ __device__ __forceinline__ C cmulc(C a, C b)
+{
+    C r;
+    r.x = a.x * b.x + a.y * b.y;
+    r.y = a.x * b.y - a.y * b.x;
+    return r;
+}
+template <typename C> __host__ __device__ __forceinline__ C cconj(C a) { a.y = -a.y; return a; }
+template <typename C, typename T> __host__ __device__ __forceinline__ C cscale(C a, T s) { a.x *= s; a.y *= s; return a; }
+// acc += a * b (complex FMA in four real FMAs)
+template <typename C> __device__ __forceinline__ void cfma(C &acc, C a, C b)
+{
+    acc.x = fma(a.x, b.x, acc.x);
+    acc.x = fma(-a.y, b.y, acc.x);
+    acc.y = fma(a.x, b.y, acc.y);
+    acc.y = fma(a.y, b.x, acc.y);
+}
+// acc += conj(a) * b
+template <typename C> __device__ __forceinline__ void cfmac(C &acc, C a, C b)
+{
+    acc.x = fma(a.x, b.x, acc.x);
+    acc.x = fma(a.y, b.y, acc.x);
+    acc.y = fma(a.x, b.y, acc.y);
+    acc.y = fma(-a.y, b.x, acc.y);
+}
+
+template <typename T> __device__ __forceinline__ T warp_sum(T v)
+{
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Block-wide sum of one value; every thread gets the result.  `sh` needs
+// blockDim.x / 32 entries.
+template <typename T> __device__ __forceinline__ T block_sum(T v, T *sh)
+{
+    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    v = warp_sum(v);
+    __syncthreads();
+    if (lane == 0) sh[wid] = v;
+    __syncthreads();
+    T t = (threadIdx.x < nw) ? sh[threadIdx.x] : T(0);
+    if (wid == 0) t = warp_sum(t);
+    if (threadIdx.x == 0) sh[0] = t;
+    __syncthreads();
+    T r = sh[0];
+    __syncthreads();
+    return r;
+}
+
+__host__ __device__ inline int cdiv(long a, long b) { return (int)((a + b - 1) / b); }
+
+// Launch accounting: every kernel launch of the library goes through LAUNCH so
+// that the context can report how many device kernels a call issued.
+extern thread_local long long *g_launch_counter;
+#define NRLTB_LAUNCH(kernel, grid, block, smem, stream, ...)                 \
+    do {                                                                     \
+        kernel<<<(grid), (block), (smem), (stream)>>>(__VA_ARGS__);          \
+        if (::nrltb::g_launch_counter) ++*::nrltb::g_launch_counter;         \
+    } while (0)
+
+}  // namespace nrltb

@@ -1,0 +1,733 @@
+// eig.cu -- batched generalized Hermitian eigensolver (see eig.cuh for the plan).
+#include <algorithm>
+#include <cfloat>
+#include "eig.cuh"
+
+namespace nrltb {
+
+template <typename T> __host__ __device__ inline T eps_of();
+template <> __host__ __device__ inline float eps_of<float>() { return FLT_EPSILON * 0.5f; }
+template <> __host__ __device__ inline double eps_of<double>() { return DBL_EPSILON * 0.5; }
+
+static inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+template <typename T> size_t eig_work_bytes(int n, int batch)
+{
+    EigWork<T> w;
+    eig_work_carve<T>(w, nullptr, n, batch);
+    return (size_t)w.status + sizeof(int) * (size_t)batch;  // carve from 0 gives the size
+}
+
+template <typename T> void eig_work_carve(EigWork<T> &w, void *base, int n, int batch)
+{
+    typedef typename cplx<T>::t C2;
+    size_t off = 0;
+    char *b = (char *)base;
+    auto take = [&](size_t bytes) { void *p = b + off; off = align256(off + bytes); return p; };
+    const size_t nn = (size_t)n * n, nb = (size_t)batch;
+    const int ncta = cdiv(n, EIG_ROWS) + 1;
+    w.n = n; w.batch = batch; w.ld = n; w.mstride = (long)nn;
+    w.L = (C2 *)take(sizeof(C2) * nn * nb);
+    w.Wi = (C2 *)take(sizeof(C2) * nn * nb);
+    w.A = (C2 *)take(sizeof(C2) * nn * nb);
+    w.Y = (C2 *)take(sizeof(C2) * nn * nb);
+    w.V = (C2 *)take(sizeof(C2) * nn * nb);
+    w.Wp = (C2 *)take(sizeof(C2) * n * EIG_NB * nb);
+    w.wq = (C2 *)take(sizeof(C2) * n * nb);
+    w.col = (C2 *)take(sizeof(C2) * n * nb);
+    w.tau = (C2 *)take(sizeof(C2) * n * nb);
+    w.pp = (C2 *)take(sizeof(C2) * 2 * EIG_NB * nb);
+    w.part = (C2 *)take(sizeof(C2) * (2 * EIG_NB + 2) * ncta * nb);
+    w.sc = (C2 *)take(sizeof(C2) * 4 * nb);
+    w.Tt = (C2 *)take(sizeof(C2) * EIG_NB * (size_t)std::max(n, 2 * EIG_NB) * nb);
+    w.Xt = (C2 *)take(sizeof(C2) * EIG_NB * (size_t)n * nb);
+    w.d = (double *)take(sizeof(double) * n * nb);
+    w.e = (double *)take(sizeof(double) * n * nb);
+    w.lam = (double *)take(sizeof(double) * n * nb);
+    w.ylu = (double *)take(sizeof(double) * 5 * nn * nb);
+    w.yvec = (double *)take(sizeof(double) * nn * nb);
+    w.perm = (int *)take(sizeof(int) * 4 * n * nb);
+    w.counter = (unsigned *)take(sizeof(unsigned) * nb);
+    w.status = (int *)take(sizeof(int) * nb);
+    if (!base) w.status = (int *)(uintptr_t)off;  // size query
+}
+
+// ---------------------------------------------------------------------------
+template <typename C2>
+__global__ void k_convert_h(const double2 *__restrict__ src, C2 *__restrict__ dst, long count)
+{
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < count; i += (long)gridDim.x * blockDim.x) {
+        double2 v = src[i];
+        C2 o;
+        o.x = v.x; o.y = v.y;
+        dst[i] = o;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Diagonal block: Cholesky L_jj L_jj^H = S_jj and its inverse, in shared memory.
+template <typename T>
+__global__ void __launch_bounds__(256) k_potrf_diag(EigWork<T> w, int j0, int jb)
+{
+    typedef typename cplx<T>::t C2;
+    __shared__ C2 a[EIG_NB][EIG_NB + 1];   // a[c][r]
+    __shared__ C2 x[EIG_NB][EIG_NB + 1];   // inverse, x[c][r]
+    __shared__ int bad;
+    const int b = blockIdx.x, tid = threadIdx.x;
+    C2 *L = w.L + b * w.mstride + j0 + (long)j0 * w.ld;
+    C2 *Wi = w.Wi + b * w.mstride + j0 + (long)j0 * w.ld;
+    for (int e = tid; e < jb * jb; e += blockDim.x) {
+        int r = e % jb, c = e / jb;
+        a[c][r] = L[r + (long)c * w.ld];
+    }
+    if (tid == 0) bad = 0;
+    __syncthreads();
+    for (int k = 0; k < jb; ++k) {
+        if (tid == 0) {
+            T piv = a[k][k].x;
+            if (!(piv > T(0))) { bad = 1; piv = T(1); }
+            a[k][k] = cmk<T>(sqrt(piv), T(0));
+        }
+        __syncthreads();
+        T inv = T(1) / a[k][k].x;
+        for (int r = k + 1 + tid; r < jb; r += blockDim.x) a[k][r] = cscale(a[k][r], inv);
+        __syncthreads();
+        for (int e = tid; e < jb * jb; e += blockDim.x) {
+            int r = e % jb, c = e / jb;
+            if (c > k && r >= c) a[c][r] = csub(a[c][r], cmul(a[k][r], cconj(a[k][c])));
+        }
+        __syncthreads();
+    }
+    // inverse of the lower-triangular block, one column per thread
+    if (tid < jb) {
+        int c = tid;
+        for (int r = 0; r < c; ++r) x[c][r] = cmk<T>(0, 0);
+        x[c][c] = cmk<T>(T(1) / a[c][c].x, T(0));
+        for (int r = c + 1; r < jb; ++r) {
+            C2 s = cmk<T>(0, 0);
+            for (int k = c; k < r; ++k) s = cadd(s, cmul(a[k][r], x[c][k]));
+            x[c][r] = cscale(s, -T(1) / a[r][r].x);
+        }
+    }
+    __syncthreads();
+    for (int e = tid; e < jb * jb; e += blockDim.x) {
+        int r = e % jb, c = e / jb;
+        C2 z = cmk<T>(0, 0);
+        L[r + (long)c * w.ld] = (r >= c) ? a[c][r] : z;
+        Wi[r + (long)c * w.ld] = (r >= c) ? x[c][r] : z;
+    }
+    if (tid == 0 && bad) w.status[b] = 1;
+}
+
+// ---------------------------------------------------------------------------
+// Tridiagonalisation, column i of the panel starting at j0 (c = i - j0).
+// KA: finalize W[:, c-1]; update column i; reflector (last CTA).
+template <typename T>
+__global__ void __launch_bounds__(EIG_ROWS) k_tri_colupd(EigWork<T> w, int i, int j0, int ncta)
+{
+    typedef typename cplx<T>::t C2;
+    __shared__ C2 vi[EIG_NB], wi[EIG_NB];
+    __shared__ T red[EIG_ROWS / 32];
+    __shared__ unsigned ticket;
+    const int b = blockIdx.y, n = w.n, c = i - j0, tid = threadIdx.x;
+    const long ld = w.ld;
+    C2 *A = w.A + b * w.mstride, *V = w.V + b * w.mstride;
+    C2 *Wp = w.Wp + (long)b * n * EIG_NB, *wq = w.wq + (long)b * n, *col = w.col + (long)b * n;
+    const C2 alpha_prev = w.sc[b * 4 + 1];
+    // row i of the panel's V and W (W[i, c-1] recomputed from w', never read from Wp)
+    if (tid < c) {
+        vi[tid] = V[i + (long)(j0 + tid) * ld];
+        if (tid < c - 1) wi[tid] = Wp[i + (long)tid * n];
+        else wi[tid] = cadd(wq[i], cmul(alpha_prev, V[i + (long)(i - 1) * ld]));
+    }
+    __syncthreads();
+    const int r = i + blockIdx.x * EIG_ROWS + tid;
+    T nrm2 = T(0);
+    if (r < n) {
+        C2 wlast = cmk<T>(0, 0);
+        if (c > 0) {
+            wlast = cadd(wq[r], cmul(alpha_prev, V[r + (long)(i - 1) * ld]));
+            Wp[r + (long)(c - 1) * n] = wlast;
+        }
+        C2 a = A[r + (long)i * ld];
+        for (int j = 0; j < c; ++j) {
+            C2 vrj = V[r + (long)(j0 + j) * ld];
+            C2 wrj = (j < c - 1) ? Wp[r + (long)j * n] : wlast;
+            a = csub(a, cmul(vrj, cconj(wi[j])));
+            a = csub(a, cmul(wrj, cconj(vi[j])));
+        }
+        col[r] = a;
+        if (r == i) w.d[(long)b * n + i] = (double)a.x;
+        if (r >= i + 2) nrm2 = a.x * a.x + a.y * a.y;
+    }
+    __threadfence();   // col[] is read by the last CTA
+    nrm2 = block_sum(nrm2, red);
+    if (tid == 0) {
+        C2 p; p.x = nrm2; p.y = T(0);
+        w.part[((long)b * ncta + blockIdx.x) * (2 * EIG_NB + 2)] = p;
+        __threadfence();
+        ticket = atomicAdd(&w.counter[b], 1u);
+    }
+    __syncthreads();
+    if (ticket != (unsigned)(ncta - 1) || tid != 0) return;
+    // last CTA: Householder reflector (zlarfg) from col[i+1:]
+    __threadfence();
+    T xn2 = T(0);
+    for (int q = 0; q < ncta; ++q) xn2 += __ldcg(&w.part[((long)b * ncta + q) * (2 * EIG_NB + 2)].x);
+    C2 tau = cmk<T>(0, 0), scale = cmk<T>(0, 0);
+    double beta = 0.0;
+    if (i + 1 < n) {
+        C2 al;
+        al.x = __ldcg(&col[i + 1].x);
+        al.y = __ldcg(&col[i + 1].y);
+        T xnorm = sqrt(xn2);
+        if (xnorm == T(0) && al.y == T(0)) {
+            beta = (double)al.x;
+        } else {
+            T bb = sqrt(al.x * al.x + al.y * al.y + xnorm * xnorm);
+            bb = (al.x >= T(0)) ? -bb : bb;
+            tau = cmk<T>((bb - al.x) / bb, -al.y / bb);
+            C2 den = cmk<T>(al.x - bb, al.y);         // 1 / (alpha - beta)
+            T dd = den.x * den.x + den.y * den.y;
+            scale = cmk<T>(den.x / dd, -den.y / dd);
+            beta = (double)bb;
+        }
+        w.e[(long)b * n + i] = beta;
+    }
+    w.tau[(long)b * n + i] = tau;
+    w.sc[b * 4 + 0] = scale;
+    w.counter[b] = 0;
+}
+
+// KB: v = scaled column; p1 = W^H v, p2 = V^H v over the panel's previous columns.
+template <typename T>
+__global__ void __launch_bounds__(EIG_ROWS) k_tri_vdots(EigWork<T> w, int i, int j0, int ncta)
+{
+    typedef typename cplx<T>::t C2;
+    __shared__ C2 sv[EIG_ROWS];
+    __shared__ unsigned ticket;
+    const int b = blockIdx.y, n = w.n, c = i - j0, tid = threadIdx.x;
+    const long ld = w.ld;
+    C2 *V = w.V + b * w.mstride, *Wp = w.Wp + (long)b * n * EIG_NB, *col = w.col + (long)b * n;
+    const C2 scale = w.sc[b * 4 + 0];
+    const int r = i + 1 + blockIdx.x * EIG_ROWS + tid;
+    C2 v = cmk<T>(0, 0);
+    if (r < n) {
+        v = (r == i + 1) ? cmk<T>(1, 0) : cmul(col[r], scale);
+        V[r + (long)i * ld] = v;
+    }
+    if (blockIdx.x == 0)
+        for (int q = tid; q <= i; q += EIG_ROWS) V[q + (long)i * ld] = cmk<T>(0, 0);
+    sv[tid] = v;
+    __syncthreads();
+    // partial dots: thread j < c sums W[:, j]^H v, thread EIG_NB + j sums V[:, j0+j]^H v
+    C2 *part = w.part + ((long)b * ncta + blockIdx.x) * (2 * EIG_NB + 2);
+    if (tid < 2 * EIG_NB) {
+        int j = tid % EIG_NB;
+        bool isV = tid >= EIG_NB;
+        C2 s = cmk<T>(0, 0);
+        if (j < c) {
+            int r0 = i + 1 + blockIdx.x * EIG_ROWS;
+            for (int q = 0; q < EIG_ROWS && r0 + q < n; ++q) {
+                C2 m = isV ? V[r0 + q + (long)(j0 + j) * ld] : Wp[r0 + q + (long)j * n];
+                cfmac(s, m, sv[q]);
+            }
+        }
+        part[tid] = s;
+        __threadfence();
+    }
+    __syncthreads();
+    if (tid == 0) {
+        ticket = atomicAdd(&w.counter[b], 1u);
+    }
+    __syncthreads();
+    if (ticket != (unsigned)(ncta - 1)) return;
+    __threadfence();
+    if (tid < 2 * EIG_NB) {
+        C2 s = cmk<T>(0, 0);
+        for (int q = 0; q < ncta; ++q) {
+            const C2 *p = w.part + ((long)b * ncta + q) * (2 * EIG_NB + 2) + tid;
+            s.x += __ldcg(&p->x);
+            s.y += __ldcg(&p->y);
+        }
+        w.pp[b * 2 * EIG_NB + tid] = s;
+    }
+    __syncthreads();
+    if (tid == 0) w.counter[b] = 0;
+}
+
+// KC: y = A[i+1:, i+1:] v with A stored in its lower triangle.  32-row blocks,
+// 32 x 32 tiles through shared memory, 8 column slices per row.
+template <typename T>
+__global__ void __launch_bounds__(256) k_tri_hemv(EigWork<T> w, int i)
+{
+    typedef typename cplx<T>::t C2;
+    __shared__ C2 tile[32][33];
+    __shared__ C2 vs[32];
+    __shared__ C2 red[8][33];
+    const int b = blockIdx.y, n = w.n, tid = threadIdx.x;
+    const long ld = w.ld;
+    const C2 *A = w.A + b * w.mstride, *V = w.V + b * w.mstride;
+    const int base = i + 1, m = n - base;
+    const int rb = blockIdx.x, r0 = base + 32 * rb;
+    const int tr = tid & 31, tc = tid >> 5;
+    C2 acc = cmk<T>(0, 0);
+    const int ntile = cdiv(m, 32);
+    for (int t = 0; t < ntile; ++t) {
+        const int s0 = base + 32 * t;
+        __syncthreads();
+        if (tid < 32) vs[tid] = (s0 + tid < n) ? V[s0 + tid + (long)i * ld] : cmk<T>(0, 0);
+        if (t <= rb) {
+            // tile[rr][ss] = A[r0+rr, s0+ss], coalesced along rr
+            for (int e = tid; e < 1024; e += 256) {
+                int rr = e & 31, ss = e >> 5;
+                int rg = r0 + rr, sg = s0 + ss;
+                tile[rr][ss] = (rg < n && sg < n && sg <= rg) ? A[rg + (long)sg * ld] : cmk<T>(0, 0);
+            }
+        } else {
+            // tile[rr][ss] = conj(A[s0+ss, r0+rr]), coalesced along ss
+            for (int e = tid; e < 1024; e += 256) {
+                int ss = e & 31, rr = e >> 5;
+                int rg = r0 + rr, sg = s0 + ss;
+                tile[rr][ss] = (rg < n && sg < n) ? cconj(A[sg + (long)rg * ld]) : cmk<T>(0, 0);
+            }
+        }
+        __syncthreads();
+        if (t == rb) {
+            // diagonal tile: only the lower half was loaded; mirror it
+            for (int e = tid; e < 1024; e += 256) {
+                int rr = e & 31, ss = e >> 5;
+                if (ss > rr) tile[rr][ss] = cconj(tile[ss][rr]);
+            }
+            __syncthreads();
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            int ss = tc + 8 * q;
+            cfma(acc, tile[tr][ss], vs[ss]);
+        }
+    }
+    red[tc][tr] = acc;
+    __syncthreads();
+    if (tid < 32) {
+        C2 s = red[0][tid];
+        for (int q = 1; q < 8; ++q) s = cadd(s, red[q][tid]);
+        int rg = r0 + tid;
+        if (rg < n) w.col[(long)b * n + rg] = s;
+    }
+}
+
+// KD: w' = tau (y - V p1 - W p2); alpha = -tau/2 (w'^H v) (last CTA).
+template <typename T>
+__global__ void __launch_bounds__(EIG_ROWS) k_tri_wupd(EigWork<T> w, int i, int j0, int ncta)
+{
+    typedef typename cplx<T>::t C2;
+    __shared__ C2 p1[EIG_NB], p2[EIG_NB];
+    __shared__ T red[EIG_ROWS / 32];
+    __shared__ unsigned ticket;
+    const int b = blockIdx.y, n = w.n, c = i - j0, tid = threadIdx.x;
+    const long ld = w.ld;
+    const C2 *V = w.V + b * w.mstride, *Wp = w.Wp + (long)b * n * EIG_NB;
+    C2 *wq = w.wq + (long)b * n;
+    const C2 *y = w.col + (long)b * n;
+    const C2 tau = w.tau[(long)b * n + i];
+    if (tid < c) {
+        p1[tid] = w.pp[b * 2 * EIG_NB + tid];
+        p2[tid] = w.pp[b * 2 * EIG_NB + EIG_NB + tid];
+    }
+    __syncthreads();
+    const int r = i + 1 + blockIdx.x * EIG_ROWS + tid;
+    T dre = T(0), dim = T(0);
+    if (r < n) {
+        C2 s = y[r];
+        for (int j = 0; j < c; ++j) {
+            s = csub(s, cmul(V[r + (long)(j0 + j) * ld], p1[j]));
+            s = csub(s, cmul(Wp[r + (long)j * n], p2[j]));
+        }
+        s = cmul(tau, s);
+        wq[r] = s;
+        C2 v = V[r + (long)i * ld];
+        dre = s.x * v.x + s.y * v.y;      // conj(w') v
+        dim = s.x * v.y - s.y * v.x;
+    }
+    if (blockIdx.x == 0)
+        for (int q = tid; q <= i; q += EIG_ROWS) wq[q] = cmk<T>(0, 0);
+    dre = block_sum(dre, red);
+    dim = block_sum(dim, red);
+    if (tid == 0) {
+        C2 p; p.x = dre; p.y = dim;
+        w.part[((long)b * ncta + blockIdx.x) * (2 * EIG_NB + 2) + 2 * EIG_NB] = p;
+        __threadfence();
+        ticket = atomicAdd(&w.counter[b], 1u);
+    }
+    __syncthreads();
+    if (ticket != (unsigned)(ncta - 1) || tid != 0) return;
+    __threadfence();
+    C2 dot = cmk<T>(0, 0);
+    for (int q = 0; q < ncta; ++q) {
+        const C2 *p = w.part + ((long)b * ncta + q) * (2 * EIG_NB + 2) + 2 * EIG_NB;
+        dot.x += __ldcg(&p->x);
+        dot.y += __ldcg(&p->y);
+    }
+    w.sc[b * 4 + 1] = cscale(cmul(tau, dot), T(-0.5));
+    w.counter[b] = 0;
+}
+
+// W[:, c] = w' + alpha v for the panel's last column.
+template <typename T>
+__global__ void k_tri_wfinal(EigWork<T> w, int i, int c)
+{
+    typedef typename cplx<T>::t C2;
+    const int b = blockIdx.y, n = w.n;
+    const C2 alpha = w.sc[b * 4 + 1];
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+        C2 v = (r > i) ? w.V[b * w.mstride + r + (long)i * w.ld] : cmk<T>(0, 0);
+        C2 q = (r > i) ? w.wq[(long)b * n + r] : cmk<T>(0, 0);
+        w.Wp[(long)b * n * EIG_NB + r + (long)c * n] = cadd(q, cmul(alpha, v));
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Tridiagonal eigenvalues: Sturm-count bisection inside each unreduced block.
+__device__ inline void find_block(const double *d, const double *e, int n, int r, int &b0, int &b1)
+{
+    const double ulp = DBL_EPSILON;
+    auto split = [&](int k) {   // negligible e[k]: split between rows k and k+1
+        return fabs(d[k] * d[k + 1]) * ulp * ulp + DBL_MIN >= e[k] * e[k];
+    };
+    b0 = r;
+    while (b0 > 0 && !split(b0 - 1)) --b0;
+    b1 = r;
+    while (b1 < n - 1 && !split(b1)) ++b1;
+}
+
+template <typename TB> __device__ inline TB tiny_of();
+template <> __device__ inline float tiny_of<float>() { return FLT_MIN; }
+template <> __device__ inline double tiny_of<double>() { return DBL_MIN; }
+
+// One thread per (matrix, row r): eigenvalue number r - b0 of r's block.
+template <typename TB>
+__global__ void k_tri_bisect(const double *dd, const double *ee, double *lamloc, int *blk, int n)
+{
+    const int b = blockIdx.y;
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    const double *d = dd + (long)b * n, *e = ee + (long)b * n;
+    int b0, b1;
+    find_block(d, e, n, r, b0, b1);
+    double tnorm = 0, lo = 1e300, hi = -1e300, emax2 = 0;
+    for (int k = b0; k <= b1; ++k) {
+        double off = (k > b0 ? fabs(e[k - 1]) : 0.0) + (k < b1 ? fabs(e[k]) : 0.0);
+        lo = fmin(lo, d[k] - off);
+        hi = fmax(hi, d[k] + off);
+        tnorm = fmax(tnorm, fabs(d[k]) + off);
+        if (k < b1) emax2 = fmax(emax2, e[k] * e[k]);
+    }
+    const TB eps = eps_of<TB>();
+    const TB pivmin = tiny_of<TB>() * TB(fmax(1.0, emax2));
+    const TB atol = eps * TB(tnorm);
+    const int j = r - b0;
+    TB a = TB(lo) - TB(2) * atol - pivmin, z = TB(hi) + TB(2) * atol + pivmin;
+    for (int it = 0; it < 256; ++it) {
+        const TB mid = TB(0.5) * (a + z);
+        const TB tol = fmax(atol, TB(2) * eps * fmax(fabs(a), fabs(z))) + pivmin;
+        if (!(z - a > tol) || mid == a || mid == z) break;
+        int cnt = 0;
+        TB q = TB(d[b0]) - mid;
+        if (fabs(q) < pivmin) q = -pivmin;
+        cnt += (q < TB(0));
+        for (int k = b0 + 1; k <= b1; ++k) {
+            const TB ek = TB(e[k - 1]);
+            q = TB(d[k]) - mid - ek * ek / q;
+            if (fabs(q) < pivmin) q = -pivmin;
+            cnt += (q < TB(0));
+        }
+        if (cnt <= j) a = mid; else z = mid;
+    }
+    lamloc[(long)b * n + r] = (double)(TB(0.5) * (a + z));
+    blk[((long)b * n + r) * 2 + 0] = b0;
+    blk[((long)b * n + r) * 2 + 1] = b1;
+}
+
+// Global ascending order: rank of (lamloc[r], r).
+__global__ void k_tri_rank(const double *lamloc, int *rank, double *lam, int n)
+{
+    const int b = blockIdx.y;
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    const double *L = lamloc + (long)b * n;
+    double v = L[r];
+    int cnt = 0;
+    for (int s = 0; s < n; ++s) {
+        double u = L[s];
+        cnt += (u < v) || (u == v && s < r);
+    }
+    rank[(long)b * n + r] = cnt;
+    lam[(long)b * n + cnt] = v;
+}
+
+__device__ inline double hash_unit(unsigned a, unsigned b)
+{
+    unsigned h = a * 0x9E3779B1u ^ (b + 0x7F4A7C15u) * 0x85EBCA77u;
+    h ^= h >> 15; h *= 0x2C1B3C6Du; h ^= h >> 12; h *= 0x297A2D39u; h ^= h >> 15;
+    return (double)(h & 0xFFFFFF) / (double)0x800000 - 1.0;   // [-1, 1)
+}
+
+// Tridiagonal eigenvectors by inverse iteration (FP64).  One thread per
+// cluster of close eigenvalues inside an unreduced block; members of a cluster
+// are re-orthogonalised against the previous members after every solve.
+__global__ void k_tri_invit(const double *dd, const double *ee, const double *lamloc, const int *blk,
+                            const int *rank, double *yvec, double *scratch, int n, double ctol)
+{
+    const int b = blockIdx.y;
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    const double *d = dd + (long)b * n, *e = ee + (long)b * n, *L = lamloc + (long)b * n;
+    const int b0 = blk[((long)b * n + r) * 2], b1 = blk[((long)b * n + r) * 2 + 1];
+    const int len = b1 - b0 + 1;
+    double tnorm = 0;
+    for (int k = b0; k <= b1; ++k)
+        tnorm = fmax(tnorm, fabs(d[k]) + (k > b0 ? fabs(e[k - 1]) : 0.0) + (k < b1 ? fabs(e[k]) : 0.0));
+    const double gap = ctol * fmax(tnorm, DBL_MIN);
+    // only the first member of a cluster works
+    if (r > b0 && L[r] - L[r - 1] < gap) return;
+    int rend = r;
+    while (rend < b1 && L[rend + 1] - L[rend] < gap) ++rend;
+    double *Y = yvec + (long)b * n * n;
+    double *S = scratch + ((long)b * n + r) * 5 * (long)n;
+    double *dl = S, *dg = S + n, *du = S + 2 * n, *du2 = S + 3 * n, *x = S + 4 * n;   // x: pivot flags
+    const double tiny = DBL_EPSILON * fmax(tnorm, DBL_MIN);
+    for (int m = r; m <= rend; ++m) {
+        const double lam = L[m];
+        // factor T_block - lam I = P L U (dgttrf)
+        for (int k = 0; k < len; ++k) {
+            dg[k] = d[b0 + k] - lam;
+            if (k < len - 1) { dl[k] = e[b0 + k]; du[k] = e[b0 + k]; du2[k] = 0.0; }
+        }
+        for (int k = 0; k < len - 1; ++k) {
+            if (fabs(dg[k]) >= fabs(dl[k])) {
+                double f = (dg[k] != 0.0) ? dl[k] / dg[k] : 0.0;
+                dl[k] = f;
+                dg[k + 1] = dg[k + 1] - f * du[k];
+                x[k] = 0.0;     // no interchange
+            } else {
+                double f = dg[k] / dl[k];
+                dg[k] = dl[k];
+                dl[k] = f;
+                double t = du[k];
+                du[k] = dg[k + 1];
+                dg[k + 1] = t - f * dg[k + 1];
+                if (k < len - 2) { du2[k] = du[k + 1]; du[k + 1] = -f * du[k + 1]; }
+                x[k] = 1.0;     // interchange
+            }
+        }
+        for (int k = 0; k < len; ++k)
+            if (fabs(dg[k]) < tiny) dg[k] = (dg[k] < 0.0) ? -tiny : tiny;
+        // the solution vector lives in Y's column for this eigenvalue
+        double *z = Y + (long)rank[(long)b * n + m] * n;
+        for (int k = 0; k < n; ++k) z[k] = 0.0;
+        double *v = z + b0;
+        for (int k = 0; k < len; ++k) v[k] = hash_unit((unsigned)(b * 7919 + m), (unsigned)k);
+        for (int it = 0; it < 3; ++it) {
+            // solve: apply P and L
+            for (int k = 0; k < len - 1; ++k) {
+                if (x[k] == 0.0) {
+                    v[k + 1] = v[k + 1] - dl[k] * v[k];
+                } else {
+                    double t = v[k];
+                    v[k] = v[k + 1];
+                    v[k + 1] = t - dl[k] * v[k + 1];
+                }
+            }
+            // U back-substitution
+            v[len - 1] = v[len - 1] / dg[len - 1];
+            if (len > 1) v[len - 2] = (v[len - 2] - du[len - 2] * v[len - 1]) / dg[len - 2];
+            for (int k = len - 3; k >= 0; --k) v[k] = (v[k] - du[k] * v[k + 1] - du2[k] * v[k + 2]) / dg[k];
+            // re-orthogonalise against earlier cluster members
+            for (int p = r; p < m; ++p) {
+                const double *zp = Y + (long)rank[(long)b * n + p] * n + b0;
+                double s = 0;
+                for (int k = 0; k < len; ++k) s += zp[k] * v[k];
+                for (int k = 0; k < len; ++k) v[k] -= s * zp[k];
+            }
+            double nrm = 0;
+            for (int k = 0; k < len; ++k) nrm += v[k] * v[k];
+            nrm = sqrt(nrm);
+            double inv = (nrm > 0) ? 1.0 / nrm : 0.0;
+            for (int k = 0; k < len; ++k) v[k] *= inv;
+        }
+        // sign convention: largest component positive
+        int kmax = 0;
+        for (int k = 1; k < len; ++k) if (fabs(v[k]) > fabs(v[kmax])) kmax = k;
+        if (v[kmax] < 0) for (int k = 0; k < len; ++k) v[k] = -v[k];
+    }
+}
+
+// real eigenvector matrix -> complex working precision
+template <typename C2>
+__global__ void k_real_to_cplx(const double *y, C2 *z, long count)
+{
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < count; i += (long)gridDim.x * blockDim.x) {
+        C2 o;
+        o.x = y[i]; o.y = 0;
+        z[i] = o;
+    }
+}
+
+// compact-WY T factor of one panel: T[0:c, c] = -tau_c T[0:c,0:c] G[0:c, c], T[c][c] = tau_c
+template <typename T>
+__global__ void k_larft(const typename cplx<T>::t *G, typename cplx<T>::t *Tm, const typename cplx<T>::t *tau,
+                        int n, int j0, int jb)
+{
+    typedef typename cplx<T>::t C2;
+    __shared__ C2 t[EIG_NB][EIG_NB + 1];   // t[col][row]
+    __shared__ C2 g[EIG_NB][EIG_NB + 1];
+    const int b = blockIdx.x, tid = threadIdx.x;
+    const C2 *Gb = G + (long)b * EIG_NB * EIG_NB;
+    for (int e = tid; e < jb * jb; e += blockDim.x) {
+        int rr = e % jb, cc = e / jb;
+        g[cc][rr] = Gb[rr + cc * EIG_NB];
+        t[cc][rr] = cmk<T>(0, 0);
+    }
+    __syncthreads();
+    for (int c = 0; c < jb; ++c) {
+        C2 tc = tau[(long)b * n + j0 + c];
+        // thread r < c: t[c][r] = -tau_c * sum_{k=r}^{c-1} t[k][r] g[c][k]
+        C2 s = cmk<T>(0, 0);
+        if (tid < c)
+            for (int k = tid; k < c; ++k) cfma(s, t[k][tid], g[c][k]);
+        __syncthreads();
+        if (tid < c) t[c][tid] = cscale(cmul(tc, s), T(-1));
+        if (tid == c) t[c][c] = tc;
+        __syncthreads();
+    }
+    C2 *Tb = Tm + (long)b * EIG_NB * EIG_NB;
+    for (int e = tid; e < jb * jb; e += blockDim.x) {
+        int rr = e % jb, cc = e / jb;
+        Tb[rr + cc * EIG_NB] = t[cc][rr];
+    }
+}
+
+__global__ void k_fill_int(int *p, int v, int count)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < count) p[i] = v;
+}
+
+// ---------------------------------------------------------------------------
+template <typename T>
+void eig_solve(cudaStream_t s, EigWork<T> &w, const double2 *H, const double2 *S, double *eig,
+               typename cplx<T>::t *X, bool vectors)
+{
+    typedef typename cplx<T>::t C2;
+    const int n = w.n, B = w.batch;
+    const long ld = w.ld, ms = w.mstride;
+    const C2 one = cmk<T>(1, 0), mone = cmk<T>(-1, 0), zero = cmk<T>(0, 0);
+    const long cnt = (long)n * n * B;
+    cudaMemsetAsync(w.status, 0, sizeof(int) * B, s);
+    cudaMemsetAsync(w.counter, 0, sizeof(unsigned) * B, s);
+    cudaMemsetAsync(w.sc, 0, sizeof(C2) * 4 * B, s);
+    // 0. inputs in working precision: S -> L, H -> A (A is free until step 3)
+    NRLTB_LAUNCH(k_convert_h<C2>, 1184, 256, 0, s, S, w.L, cnt);
+    NRLTB_LAUNCH(k_convert_h<C2>, 1184, 256, 0, s, H, w.A, cnt);
+    // 1. Cholesky S = L L^H
+    for (int j0 = 0; j0 < n; j0 += EIG_NB) {
+        const int jb = std::min(EIG_NB, n - j0), rem = n - j0 - jb;
+        NRLTB_LAUNCH(k_potrf_diag<T>, B, 256, 0, s, w, j0, jb);
+        if (rem > 0) {
+            C2 *P = w.L + (j0 + jb) + (long)j0 * ld;
+            zgemm<T>(s, rem, jb, jb, B, one, P, ld, ms, 0, w.Wi + j0 + (long)j0 * ld, ld, ms, 1, zero, P, ld, ms,
+                     0, 1, 0);
+            zgemm<T>(s, rem, rem, jb, B, mone, P, ld, ms, 0, P, ld, ms, 1, one,
+                     w.L + (j0 + jb) + (long)(j0 + jb) * ld, ld, ms, 0, 0, 1);
+        }
+    }
+    // 2. Wi = L^{-1}, bottom-up blocked (diagonal blocks already inverted)
+    {
+        int jlast = ((n - 1) / EIG_NB) * EIG_NB;
+        for (int j0 = jlast; j0 >= 0; j0 -= EIG_NB) {
+            const int jb = std::min(EIG_NB, n - j0), rem = n - j0 - jb;
+            if (rem <= 0) continue;
+            const long ldx = n;
+            zgemm<T>(s, rem, jb, rem, B, one, w.Wi + (long)(j0 + jb) * (ld + 1), ld, ms, 0,
+                     w.L + (j0 + jb) + (long)j0 * ld, ld, ms, 0, zero, w.Xt, ldx, (long)EIG_NB * n, 1, 0, 0);
+            zgemm<T>(s, rem, jb, jb, B, mone, w.Xt, ldx, (long)EIG_NB * n, 0, w.Wi + (long)j0 * (ld + 1), ld, ms, 0,
+                     zero, w.Wi + (j0 + jb) + (long)j0 * ld, ld, ms, 0, 2, 0);
+        }
+    }
+    // 3. A = Wi H Wi^H (lower tiles)
+    zgemm<T>(s, n, n, n, B, one, w.A, ld, ms, 0, w.Wi, ld, ms, 1, zero, w.Y, ld, ms, 0, 1, 0);
+    zgemm<T>(s, n, n, n, B, one, w.Wi, ld, ms, 0, w.Y, ld, ms, 0, zero, w.A, ld, ms, 1, 0, 1);
+    // 4. tridiagonalisation
+    const int ncta = cdiv(n, EIG_ROWS);
+    for (int j0 = 0; j0 < n; j0 += EIG_NB) {
+        const int jb = std::min(EIG_NB, n - j0);
+        for (int c = 0; c < jb; ++c) {
+            const int i = j0 + c;
+            const int nA = cdiv(n - i, EIG_ROWS);
+            NRLTB_LAUNCH(k_tri_colupd<T>, dim3(nA, B), EIG_ROWS, 0, s, w, i, j0, nA);
+            if (i == n - 1) break;
+            const int nB = cdiv(n - i - 1, EIG_ROWS);
+            NRLTB_LAUNCH(k_tri_vdots<T>, dim3(nB, B), EIG_ROWS, 0, s, w, i, j0, nB);
+            NRLTB_LAUNCH(k_tri_hemv<T>, dim3(cdiv(n - i - 1, 32), B), 256, 0, s, w, i);
+            NRLTB_LAUNCH(k_tri_wupd<T>, dim3(nB, B), EIG_ROWS, 0, s, w, i, j0, nB);
+        }
+        const int last = std::min(j0 + jb - 1, n - 2);
+        if (last < j0) break;
+        NRLTB_LAUNCH(k_tri_wfinal<T>, dim3(cdiv(n, 256), B), 256, 0, s, w, last, last - j0);
+        const int t0 = j0 + jb, rem = n - t0;
+        if (rem > 0) {
+            C2 *Vp = w.V + t0 + (long)j0 * ld, *Wpp = w.Wp + t0;
+            C2 *At = w.A + (long)t0 * (ld + 1);
+            zgemm<T>(s, rem, rem, jb, B, mone, Vp, ld, ms, 0, Wpp, n, (long)n * EIG_NB, 1, one, At, ld, ms, 0, 0, 1);
+            zgemm<T>(s, rem, rem, jb, B, mone, Wpp, n, (long)n * EIG_NB, 0, Vp, ld, ms, 1, one, At, ld, ms, 0, 0, 1);
+        }
+        (void)ncta;
+    }
+    // 5. tridiagonal eigenproblem (FP64 inverse iteration; bisection in T)
+    double *lamloc = (double *)w.Xt;   // free at this point: n doubles per matrix fit
+    int *blk = w.perm, *rank = w.perm + 2 * (long)n * B;
+    {
+        dim3 g(cdiv(n, 128), B);
+        NRLTB_LAUNCH(k_tri_bisect<T>, g, 128, 0, s, w.d, w.e, lamloc, blk, n);
+        NRLTB_LAUNCH(k_tri_rank, g, 128, 0, s, lamloc, rank, w.lam, n);
+        cudaMemcpyAsync(eig, w.lam, sizeof(double) * n * B, cudaMemcpyDeviceToDevice, s);
+    }
+    if (!vectors) return;
+    {
+        dim3 g(cdiv(n, 64), B);
+        const double ctol = (sizeof(T) == 8) ? 1e-9 : 1e-5;
+        NRLTB_LAUNCH(k_tri_invit, g, 64, 0, s, w.d, w.e, lamloc, blk, rank, w.yvec, w.ylu, n, ctol);
+        NRLTB_LAUNCH(k_real_to_cplx<C2>, 1184, 256, 0, s, w.yvec, w.Y, cnt);
+    }
+    // 6. Z = Q Y, panels applied last to first; then X = Wi^H Z
+    {
+        const int jlast = ((n - 2) / EIG_NB) * EIG_NB;
+        for (int j0 = (n >= 2 ? jlast : -1); j0 >= 0; j0 -= EIG_NB) {
+            const int jb = std::min(EIG_NB, n - 1 - j0);
+            if (jb <= 0) continue;
+            C2 *Vp = w.V + (long)j0 * ld;                    // n x jb, zero above the unit diagonal
+            C2 *G = w.Tt, *Tf = w.Tt + (long)EIG_NB * EIG_NB * B;
+            // G = Vp^H Vp, T factor, Xt = Vp^H Z, Xt = T Xt, Z -= Vp Xt
+            zgemm<T>(s, jb, jb, n, B, one, Vp, ld, ms, 1, Vp, ld, ms, 0, zero, G, EIG_NB, (long)EIG_NB * EIG_NB);
+            NRLTB_LAUNCH(k_larft<T>, B, 64, 0, s, G, Tf, w.tau, n, j0, jb);
+            zgemm<T>(s, jb, n, n, B, one, Vp, ld, ms, 1, w.Y, ld, ms, 0, zero, w.Xt, EIG_NB, (long)EIG_NB * n);
+            C2 *X2 = w.Wp;   // jb x n per matrix (Wp is n x EIG_NB = same size)
+            zgemm<T>(s, jb, n, jb, B, one, Tf, EIG_NB, (long)EIG_NB * EIG_NB, 0, w.Xt, EIG_NB, (long)EIG_NB * n, 0,
+                     zero, X2, EIG_NB, (long)EIG_NB * n, 2, 0, 0);
+            zgemm<T>(s, n, n, jb, B, mone, Vp, ld, ms, 0, X2, EIG_NB, (long)EIG_NB * n, 0, one, w.Y, ld, ms);
+        }
+        zgemm<T>(s, n, n, n, B, one, w.Wi, ld, ms, 1, w.Y, ld, ms, 0, zero, X, ld, ms, 2, 0, 0);
+    }
+}
+
+template size_t eig_work_bytes<double>(int, int);
+template size_t eig_work_bytes<float>(int, int);
+template void eig_work_carve<double>(EigWork<double> &, void *, int, int);
+template void eig_work_carve<float>(EigWork<float> &, void *, int, int);
+template void eig_solve<double>(cudaStream_t, EigWork<double> &, const double2 *, const double2 *, double *,
+                                double2 *, bool);
+template void eig_solve<float>(cudaStream_t, EigWork<float> &, const double2 *, const double2 *, double *,
+                               float2 *, bool);
+
+}  // namespace nrltb

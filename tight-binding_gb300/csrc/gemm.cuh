@@ -1,0 +1,161 @@
+// gemm.cuh -- batched complex GEMM for the eigensolver's blocked updates.
+//
+//   C[b] = alpha * op(A[b]) * op(B[b]) + beta * C[b],   op in {N, C = conj-transpose}
+//
+// Column-major interleaved complex storage (LAPACK layout), any m, n, k.
+// Triangular structure is exploited by trimming each tile's k range:
+//   triA = 1: op(A) lower (k <= m), 2: op(A) upper (k >= m)
+//   triB = 1: op(B) upper (k <= n), 2: op(B) lower (k >= n)
+// and elements outside the triangle are read as zero, so the other half of a
+// triangular operand may hold anything.  triC = 1 (2) computes only the tiles
+// that touch the lower (upper) triangle of C.
+//
+// SIMT register-tiled kernel: a BM x BN tile per CTA, BK-deep k slices staged
+// through shared memory, TM x TN complex outputs per thread.
+#pragma once
+#include "common.cuh"
+
+namespace nrltb {
+
+template <typename T> struct GemmArgs {
+    typedef typename cplx<T>::t C2;
+    int m, n, k, batch;
+    const C2 *A; long lda, sA; int opA;
+    const C2 *B; long ldb, sB; int opB;
+    C2 *C; long ldc, sC;
+    C2 alpha, beta;
+    int triA, triB, triC;
+};
+
+template <typename T, int BM, int BN, int BK, int TM, int TN>
+__global__ void __launch_bounds__((BM / TM) * (BN / TN))
+zgemm_kernel(GemmArgs<T> g)
+{
+    typedef typename cplx<T>::t C2;
+    constexpr int NT = (BM / TM) * (BN / TN);
+    __shared__ C2 As[BK][BM + 1];
+    __shared__ C2 Bs[BK][BN + 1];
+    const int b = blockIdx.z;
+    const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
+    if (g.triC == 1 && m0 + BM - 1 < n0) return;
+    if (g.triC == 2 && n0 + BN - 1 < m0) return;
+    const C2 *A = g.A + b * g.sA;
+    const C2 *B = g.B + b * g.sB;
+    C2 *Cm = g.C + b * g.sC;
+    int kbeg = 0, kend = g.k;
+    if (g.triA == 1) kend = min(kend, m0 + BM);
+    if (g.triA == 2) kbeg = max(kbeg, m0);
+    if (g.triB == 1) kend = min(kend, n0 + BN);
+    if (g.triB == 2) kbeg = max(kbeg, n0);
+    kbeg = (kbeg / BK) * BK;
+
+    const int tid = threadIdx.x;
+    const int tx = tid % (BM / TM), ty = tid / (BM / TM);
+    C2 acc[TM][TN];
+#pragma unroll
+    for (int i = 0; i < TM; ++i)
+#pragma unroll
+        for (int j = 0; j < TN; ++j) acc[i][j] = cmk<T>(0, 0);
+
+    for (int k0 = kbeg; k0 < kend; k0 += BK) {
+        // ---- stage op(A)[m0:m0+BM, k0:k0+BK] as As[kk][i] ----
+        if (g.opA == 0) {
+            for (int e = tid; e < BM * BK; e += NT) {
+                int i = e % BM, kk = e / BM;
+                int m = m0 + i, k = k0 + kk;
+                C2 v = cmk<T>(0, 0);
+                bool ok = m < g.m && k < kend;
+                if (g.triA == 1) ok = ok && k <= m;
+                if (g.triA == 2) ok = ok && k >= m;
+                if (ok) v = A[m + (long)k * g.lda];
+                As[kk][i] = v;
+            }
+        } else {
+            for (int e = tid; e < BM * BK; e += NT) {
+                int kk = e % BK, i = e / BK;
+                int m = m0 + i, k = k0 + kk;
+                C2 v = cmk<T>(0, 0);
+                bool ok = m < g.m && k < kend;
+                if (g.triA == 1) ok = ok && k <= m;
+                if (g.triA == 2) ok = ok && k >= m;
+                if (ok) v = cconj(A[k + (long)m * g.lda]);
+                As[kk][i] = v;
+            }
+        }
+        // ---- stage op(B)[k0:k0+BK, n0:n0+BN] as Bs[kk][j] ----
+        if (g.opB == 0) {
+            for (int e = tid; e < BN * BK; e += NT) {
+                int kk = e % BK, j = e / BK;
+                int n = n0 + j, k = k0 + kk;
+                C2 v = cmk<T>(0, 0);
+                bool ok = n < g.n && k < kend;
+                if (g.triB == 1) ok = ok && k <= n;
+                if (g.triB == 2) ok = ok && k >= n;
+                if (ok) v = B[k + (long)n * g.ldb];
+                Bs[kk][j] = v;
+            }
+        } else {
+            for (int e = tid; e < BN * BK; e += NT) {
+                int j = e % BN, kk = e / BN;
+                int n = n0 + j, k = k0 + kk;
+                C2 v = cmk<T>(0, 0);
+                bool ok = n < g.n && k < kend;
+                if (g.triB == 1) ok = ok && k <= n;
+                if (g.triB == 2) ok = ok && k >= n;
+                if (ok) v = cconj(B[n + (long)k * g.ldb]);
+                Bs[kk][j] = v;
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kk = 0; kk < BK; ++kk) {
+            C2 a[TM], bb[TN];
+#pragma unroll
+            for (int i = 0; i < TM; ++i) a[i] = As[kk][tx + i * (BM / TM)];
+#pragma unroll
+            for (int j = 0; j < TN; ++j) bb[j] = Bs[kk][ty + j * (BN / TN)];
+#pragma unroll
+            for (int i = 0; i < TM; ++i)
+#pragma unroll
+                for (int j = 0; j < TN; ++j) cfma(acc[i][j], a[i], bb[j]);
+        }
+        __syncthreads();
+    }
+    const bool beta0 = (g.beta.x == T(0) && g.beta.y == T(0));
+#pragma unroll
+    for (int i = 0; i < TM; ++i) {
+        int m = m0 + tx + i * (BM / TM);
+        if (m >= g.m) continue;
+#pragma unroll
+        for (int j = 0; j < TN; ++j) {
+            int n = n0 + ty + j * (BN / TN);
+            if (n >= g.n) continue;
+            C2 *c = Cm + m + (long)n * g.ldc;
+            C2 v = cmul(g.alpha, acc[i][j]);
+            if (!beta0) v = cadd(v, cmul(g.beta, *c));
+            *c = v;
+        }
+    }
+}
+
+template <typename T>
+void zgemm(cudaStream_t s, int m, int n, int k, int batch, typename cplx<T>::t alpha,
+           const typename cplx<T>::t *A, long lda, long sA, int opA,
+           const typename cplx<T>::t *B, long ldb, long sB, int opB,
+           typename cplx<T>::t beta, typename cplx<T>::t *C, long ldc, long sC,
+           int triA = 0, int triB = 0, int triC = 0)
+{
+    if (m <= 0 || n <= 0 || batch <= 0) return;
+    GemmArgs<T> g;
+    g.m = m; g.n = n; g.k = k; g.batch = batch;
+    g.A = A; g.lda = lda; g.sA = sA; g.opA = opA;
+    g.B = B; g.ldb = ldb; g.sB = sB; g.opB = opB;
+    g.C = C; g.ldc = ldc; g.sC = sC;
+    g.alpha = alpha; g.beta = beta;
+    g.triA = triA; g.triB = triB; g.triC = triC;
+    constexpr int BM = 64, BN = 64, BK = 8, TM = 4, TN = 4;
+    dim3 grid(cdiv(m, BM), cdiv(n, BN), batch);
+    NRLTB_LAUNCH((zgemm_kernel<T, BM, BN, BK, TM, TN>), grid, (BM / TM) * (BN / TN), 0, s, g);
+}
+
+}  // namespace nrltb

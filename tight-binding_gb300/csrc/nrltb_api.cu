@@ -1,0 +1,839 @@
+// nrltb_api.cu -- the C ABI of include/nrltb.h.
+//
+// One context = one CUDA device + one stream + grow-only device buffers.  The
+// per-structure path (nrltb_run) is:
+//   search2 -> setpar(+setparv) -> SK blocks -> for each k chunk:
+//     Bloch H, S -> eigensolve -> (mode 4) Bloch dH, dS -> Hellmann-Feynman
+//   -> Fermi level, E(T), P(T)
+// all on the device; the host only reads the pair count (one 16-byte copy) to
+// size the pair arrays.  There is no CPU fallback: every entry point fails with
+// NRLTB_E_NODEVICE / NRLTB_E_CUDA when the device path cannot run.
+#include <cstdarg>
+#include <cstring>
+#include <string>
+#include <vector>
+#include <algorithm>
+#include "nrltb.h"
+#include "common.cuh"
+#include "eig.cuh"
+#include "setup.cuh"
+#include "sums.cuh"
+#include "refine.cuh"
+
+namespace nrltb {
+thread_local long long *g_launch_counter = nullptr;
+}
+using namespace nrltb;
+
+static thread_local char g_err[512] = "";
+static void set_err(const char *fmt, ...)
+{
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof g_err, fmt, ap);
+    va_end(ap);
+}
+
+#define CK(call)                                                                      \
+    do {                                                                              \
+        cudaError_t e_ = (call);                                                      \
+        if (e_ != cudaSuccess) {                                                      \
+            set_err("%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
+            return NRLTB_E_CUDA;                                                      \
+        }                                                                             \
+    } while (0)
+#define CKL()                                                                         \
+    do {                                                                              \
+        cudaError_t e_ = cudaGetLastError();                                          \
+        if (e_ != cudaSuccess) {                                                      \
+            set_err("kernel launch failed: %s (%s:%d)", cudaGetErrorString(e_), __FILE__, __LINE__); \
+            return NRLTB_E_CUDA;                                                      \
+        }                                                                             \
+    } while (0)
+#define RET(x) do { int r_ = (x); if (r_ != NRLTB_OK) return r_; } while (0)
+
+struct DBuf {
+    void *p = nullptr;
+    size_t cap = 0;
+    int ensure(size_t bytes)
+    {
+        if (bytes <= cap) return NRLTB_OK;
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+        size_t want = std::max<size_t>(bytes, 256);
+        cudaError_t e = cudaMalloc(&p, want);
+        if (e != cudaSuccess) {
+            set_err("cudaMalloc(%zu) failed: %s", want, cudaGetErrorString(e));
+            p = nullptr;
+            return NRLTB_E_NOMEM;
+        }
+        cap = want;
+        return NRLTB_OK;
+    }
+    template <typename T> T *as() const { return (T *)p; }
+    void release() { if (p) cudaFree(p); p = nullptr; cap = 0; }
+};
+
+// host copy of one staged problem
+struct Staged {
+    bool valid = false;
+    int natoms = 0, kinds = 0, jsover = 1, nltype = 0, nv = 0, nk = 0;
+    std::vector<int> kkind, kbas, ksk, orb_atom;
+    std::vector<double> posn, posq, dnn, screenl, param, valence, kq, kw;
+    double plv[3][3];
+    int nd[3];
+    double volume = 0, zfill = 0;
+    nrltb_opts opt;
+};
+
+struct nrltb_ctx {
+    int device = 0;
+    cudaStream_t own = nullptr, stream = nullptr;
+    long long launches = 0;
+    Staged st;
+    // device inputs
+    DBuf d_kkind, d_posn, d_posq, d_kbas, d_dnn, d_screenl, d_param, d_kq, d_kw, d_ksk, d_orb;
+    // search2
+    DBuf d_code, d_blk, d_misc;
+    DBuf d_pairs;
+    int npairs = 0, kneigh_out = 0;
+    double dismin = 0;
+    // setpar / SK
+    DBuf d_sk, d_seg, d_ph;
+    // k-chunk matrices and solver
+    DBuf d_H, d_S, d_X, d_work, d_ref, d_hf, d_np;
+    std::vector<std::pair<int, int>> nonpd;   // (k, chunk) of k points whose S is not positive definite
+    // results
+    DBuf d_eig, d_deig, d_ncut, d_status, d_fjob, d_fout;
+    FermiOut fout;
+    int ran = 0;
+};
+
+static DevPairs pairs_view(nrltb_ctx *c, int cap)
+{
+    DevPairs p;
+    char *b = c->d_pairs.as<char>();
+    size_t o = 0;
+    auto take = [&](size_t bytes) { void *q = b + o; o += (bytes + 255) & ~size_t(255); return q; };
+    p.tt = (double *)take(sizeof(double) * 3 * (size_t)cap);
+    p.dlv = (int *)take(sizeof(int) * 3 * (size_t)cap);
+    p.dist = (double *)take(sizeof(double) * (size_t)cap);
+    p.screen = (double *)take(sizeof(double) * (size_t)cap);
+    p.dscrn = (double *)take(sizeof(double) * (size_t)cap);
+    p.jkind = (int *)take(sizeof(int) * 2 * (size_t)cap);
+    p.jatm = (int *)take(sizeof(int) * 2 * (size_t)cap);
+    return p;
+}
+static size_t pairs_bytes(int cap) { return (size_t)cap * (3 * 8 + 3 * 4 + 3 * 8 + 2 * 4 + 2 * 4) + 7 * 256; }
+
+static DevSK sk_view(nrltb_ctx *c, int P, int natoms, int kinds)
+{
+    DevSK s;
+    char *b = c->d_sk.as<char>();
+    size_t o = 0;
+    auto take = [&](size_t bytes) { void *q = b + o; o += (bytes + 255) & ~size_t(255); return q; };
+    s.hop = (double *)take(sizeof(double) * 14 * (size_t)P);
+    s.over = (double *)take(sizeof(double) * 14 * (size_t)P);
+    s.dhop = (double *)take(sizeof(double) * 14 * (size_t)P);
+    s.dover = (double *)take(sizeof(double) * 14 * (size_t)P);
+    s.dent = (double *)take(sizeof(double) * 2 * (size_t)P);
+    s.vdent = (double *)take(sizeof(double) * 2 * (size_t)P);
+    s.den = (double *)take(sizeof(double) * (size_t)natoms * kinds);
+    s.paros = (double *)take(sizeof(double) * 4 * (size_t)natoms);
+    s.dparos = (double *)take(sizeof(double) * 4 * (size_t)natoms);
+    s.E = (double *)take(sizeof(double) * 4 * 81 * (size_t)P);
+    return s;
+}
+static size_t sk_bytes(int P, int natoms, int kinds)
+{
+    return sizeof(double) * ((size_t)P * (56 + 4 + 4 * 81) + (size_t)natoms * (kinds + 8)) + 12 * 256;
+}
+
+static DevStructure dev_structure(nrltb_ctx *c)
+{
+    DevStructure S;
+    S.natoms = c->st.natoms;
+    S.kkind = c->d_kkind.as<int>();
+    S.posn = c->d_posn.as<double>();
+    S.posq = c->d_posq.as<double>();
+    memcpy(S.plv, c->st.plv, sizeof S.plv);
+    memcpy(S.nd, c->st.nd, sizeof S.nd);
+    S.volume = c->st.volume;
+    return S;
+}
+static DevParams dev_params(nrltb_ctx *c)
+{
+    DevParams P;
+    P.kinds = c->st.kinds;
+    P.jsover = c->st.jsover;
+    P.nltype = c->st.nltype;
+    P.kbas = c->d_kbas.as<int>();
+    P.dnn = c->d_dnn.as<double>();
+    P.screenl = c->d_screenl.as<double>();
+    P.param = c->d_param.as<double>();
+    return P;
+}
+
+template <typename T> static int upload(DBuf &b, const std::vector<T> &v, cudaStream_t s)
+{
+    RET(b.ensure(sizeof(T) * std::max<size_t>(v.size(), 1)));
+    if (!v.empty()) CK(cudaMemcpyAsync(b.p, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice, s));
+    return NRLTB_OK;
+}
+
+// ---- validation and staging ----------------------------------------------
+static int check_inputs(const nrltb_structure *st, const nrltb_params *par)
+{
+    if (!st || !par || !st->kkind || !st->posn || !par->kbas || !par->dnn || !par->screenl || !par->param) {
+        set_err("null structure or parameter pointer");
+        return NRLTB_E_ARG;
+    }
+    if (st->natoms < 1 || par->kinds < 1 || par->kinds > NRLTB_MAX_KINDS) {
+        set_err("natoms=%d kinds=%d out of range", st->natoms, par->kinds);
+        return NRLTB_E_ARG;
+    }
+    for (int i = 0; i < 3; ++i)
+        if (st->nd[i] < 0 || st->nd[i] > 64) { set_err("search box nd out of range"); return NRLTB_E_ARG; }
+    for (int i = 0; i < st->natoms; ++i)
+        if (st->kkind[i] < 1 || st->kkind[i] > par->kinds) { set_err("atom %d has kind %d", i + 1, st->kkind[i]); return NRLTB_E_ARG; }
+    for (int k = 0; k < par->kinds; ++k)
+        if (!(par->kbas[k] == 1 || par->kbas[k] == 4 || par->kbas[k] == 9)) {
+            set_err("kbas(%d)=%d: only s, sp3 and spd bases", k + 1, par->kbas[k]);
+            return NRLTB_E_UNSUPPORTED;
+        }
+    if (par->nltype != 0 && par->nltype != 1 && par->nltype != 2 && par->nltype != 3 && par->nltype != 90000) {
+        set_err("nltype %d", par->nltype);
+        return NRLTB_E_ARG;
+    }
+    return NRLTB_OK;
+}
+
+static int stage_host(nrltb_ctx *c, const nrltb_structure *st, const nrltb_params *par, const nrltb_kmesh *km,
+                      const nrltb_opts *opt)
+{
+    RET(check_inputs(st, par));
+    Staged &S = c->st;
+    S.valid = false;
+    S.natoms = st->natoms;
+    S.kinds = par->kinds;
+    S.jsover = par->jsover ? 1 : 0;
+    S.nltype = par->nltype;
+    S.kkind.assign(st->kkind, st->kkind + st->natoms);
+    S.posn.assign(st->posn, st->posn + 3 * st->natoms);
+    if (st->posq) S.posq.assign(st->posq, st->posq + 3 * st->natoms);
+    else S.posq.assign(3 * st->natoms, 0.0);
+    S.kbas.assign(par->kbas, par->kbas + par->kinds);
+    int nint = par->kinds * (par->kinds + 1) / 2;
+    S.dnn.assign(par->dnn, par->dnn + nint);
+    S.screenl.assign(par->screenl, par->screenl + nint);
+    S.param.assign(par->param, par->param + par->kinds * (29 + 68 * par->kinds));
+    S.valence.assign(par->valence ? par->valence : nullptr, par->valence ? par->valence + par->kinds : nullptr);
+    memcpy(S.plv, st->plv, sizeof S.plv);
+    memcpy(S.nd, st->nd, sizeof S.nd);
+    S.volume = st->volume;
+    S.ksk.resize(st->natoms);
+    S.orb_atom.clear();
+    int nv = 0;
+    double zfill = st->zcharge;
+    for (int i = 0; i < st->natoms; ++i) {
+        S.ksk[i] = nv;
+        int kb = par->kbas[st->kkind[i] - 1];
+        for (int q = 0; q < kb; ++q) S.orb_atom.push_back(i);
+        nv += kb;
+        if (par->valence) zfill += par->valence[st->kkind[i] - 1];
+    }
+    S.nv = nv;
+    S.zfill = zfill;
+    if (km) {
+        if (km->nk < 1 || !km->k || !km->w) { set_err("empty k list"); return NRLTB_E_ARG; }
+        S.nk = km->nk;
+        S.kq.assign(km->k, km->k + 3 * km->nk);
+        S.kw.assign(km->w, km->w + km->nk);
+    } else {
+        S.nk = 0;
+        S.kq.clear();
+        S.kw.clear();
+    }
+    if (opt) S.opt = *opt;
+    else { memset(&S.opt, 0, sizeof S.opt); S.opt.mode = 3; }
+    cudaStream_t s = c->stream;
+    RET(upload(c->d_kkind, S.kkind, s));
+    RET(upload(c->d_posn, S.posn, s));
+    RET(upload(c->d_posq, S.posq, s));
+    RET(upload(c->d_kbas, S.kbas, s));
+    RET(upload(c->d_dnn, S.dnn, s));
+    RET(upload(c->d_screenl, S.screenl, s));
+    RET(upload(c->d_param, S.param, s));
+    RET(upload(c->d_ksk, S.ksk, s));
+    RET(upload(c->d_orb, S.orb_atom, s));
+    if (km) {
+        RET(upload(c->d_kq, S.kq, s));
+        RET(upload(c->d_kw, S.kw, s));
+    }
+    S.valid = true;
+    return NRLTB_OK;
+}
+
+// ---- stages on the device -------------------------------------------------
+static int run_search2(nrltb_ctx *c, int kneigh_in)
+{
+    cudaStream_t s = c->stream;
+    const Staged &S = c->st;
+    const long box = (long)(2 * S.nd[0] + 1) * (2 * S.nd[1] + 1) * (2 * S.nd[2] + 1);
+    const long ncand = (long)S.natoms * S.natoms * box;
+    if (ncand > (1L << 31)) { set_err("search box too large (%ld candidates)", ncand); return NRLTB_E_ARG; }
+    const int nblk = cdiv(ncand, SEARCH_BLOCK);
+    RET(c->d_code.ensure((size_t)ncand));
+    RET(c->d_blk.ensure(sizeof(int) * (size_t)(nblk + 1)));
+    RET(c->d_misc.ensure(64));
+    int *misc = c->d_misc.as<int>();      // [0] ties [1] total [2] kneigh_out, [4..5] dismin bits
+    unsigned long long *dmin = (unsigned long long *)(misc + 4);
+    CK(cudaMemsetAsync(misc, 0, 16, s));
+    const unsigned long long inf = 0x7FF0000000000000ull;
+    CK(cudaMemcpyAsync(dmin, &inf, 8, cudaMemcpyHostToDevice, s));
+    DevStructure DS = dev_structure(c);
+    DevParams DP = dev_params(c);
+    NRLTB_LAUNCH(k_search_eval, std::min(cdiv(ncand, 256), 152 * 16), 256, 0, s, DS, DP, ncand,
+                 c->d_code.as<unsigned char>(), misc, dmin);
+    CKL();
+    int host_misc[6];
+    CK(cudaMemcpyAsync(host_misc, misc, sizeof host_misc, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    const int ties = host_misc[0];
+    NRLTB_LAUNCH(k_search_ties, 1, 1, 0, s, c->d_code.as<unsigned char>(), ncand, kneigh_in, misc + 2, ties > 0);
+    NRLTB_LAUNCH(k_search_count, nblk, SEARCH_BLOCK, 0, s, c->d_code.as<unsigned char>(), ncand, c->d_blk.as<int>());
+    NRLTB_LAUNCH(k_scan_small, 1, 1024, 0, s, c->d_blk.as<int>(), nblk, misc + 1);
+    CKL();
+    CK(cudaMemcpyAsync(host_misc, misc, sizeof host_misc, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    const int total = host_misc[1];
+    c->kneigh_out = host_misc[2];
+    unsigned long long bits;
+    memcpy(&bits, host_misc + 4, 8);
+    double dmin2;
+    memcpy(&dmin2, &bits, 8);
+    c->dismin = (bits == inf) ? sqrt(1e10) : sqrt(dmin2);
+    c->npairs = total;
+    RET(c->d_pairs.ensure(pairs_bytes(std::max(total, 1))));
+    DevPairs P = pairs_view(c, std::max(total, 1));
+    NRLTB_LAUNCH(k_search_scatter, nblk, SEARCH_BLOCK, 0, s, DS, DP, c->d_code.as<unsigned char>(), ncand,
+                 c->d_blk.as<int>(), P, total);
+    CKL();
+    return NRLTB_OK;
+}
+
+static int run_setpar(nrltb_ctx *c, int deriv)
+{
+    cudaStream_t s = c->stream;
+    const Staged &S = c->st;
+    const int P = std::max(c->npairs, 1);
+    RET(c->d_sk.ensure(sk_bytes(P, S.natoms, S.kinds)));
+    DevSK sk = sk_view(c, P, S.natoms, S.kinds);
+    DevPairs pr = pairs_view(c, P);
+    DevStructure DS = dev_structure(c);
+    DevParams DP = dev_params(c);
+    if (c->npairs > 0) NRLTB_LAUNCH(k_setpar_pairs, cdiv(c->npairs, 128), 128, 0, s, DS, DP, pr, c->npairs, sk, deriv);
+    NRLTB_LAUNCH(k_setpar_atoms, cdiv(S.natoms, 64), 64, 0, s, DS, DP, pr, c->npairs, sk, deriv);
+    CKL();
+    return NRLTB_OK;
+}
+
+static int run_skblocks(nrltb_ctx *c, int nwhich)
+{
+    cudaStream_t s = c->stream;
+    const Staged &S = c->st;
+    const int P = std::max(c->npairs, 1);
+    DevSK sk = sk_view(c, P, S.natoms, S.kinds);
+    DevPairs pr = pairs_view(c, P);
+    if (c->npairs > 0)
+        NRLTB_LAUNCH(k_sk_blocks, cdiv((long)c->npairs * nwhich, 128), 128, 0, s, pr, c->npairs, sk, nwhich);
+    RET(c->d_seg.ensure(sizeof(int2) * (size_t)S.natoms * S.natoms));
+    CK(cudaMemsetAsync(c->d_seg.p, 0, sizeof(int2) * (size_t)S.natoms * S.natoms, s));
+    if (c->npairs > 0)
+        NRLTB_LAUNCH(k_segments, cdiv(c->npairs, 256), 256, 0, s, pr, c->npairs, S.natoms, c->d_seg.as<int2>());
+    CKL();
+    return NRLTB_OK;
+}
+
+// dense matrices of k points [k0, k0+nk) into H, S (which0 0: H/S, 2: dH/dS)
+static int run_bloch(nrltb_ctx *c, int k0, int nk, int which0, double2 *M1, double2 *M2)
+{
+    cudaStream_t s = c->stream;
+    const Staged &S = c->st;
+    const int P = std::max(c->npairs, 1), nv = S.nv;
+    RET(c->d_ph.ensure(sizeof(double2) * (size_t)P * nk));
+    DevSK sk = sk_view(c, P, S.natoms, S.kinds);
+    DevPairs pr = pairs_view(c, P);
+    DevStructure DS = dev_structure(c);
+    DevParams DP = dev_params(c);
+    if (c->npairs > 0)
+        NRLTB_LAUNCH(k_phases, cdiv((long)c->npairs * nk, 256), 256, 0, s, DS, pr, c->npairs,
+                     c->d_kq.as<double>() + 3 * (long)k0, nk, c->d_ph.as<double2>());
+    NRLTB_LAUNCH(k_bloch_build, cdiv((long)nv * nv, 256), 256, 0, s, DS, DP, pr, c->npairs, sk, c->d_seg.as<int2>(),
+                 c->d_orb.as<int>(), c->d_ksk.as<int>(), c->d_ph.as<double2>(), nk, nv, which0, M1, M2, S.jsover);
+    CKL();
+    return NRLTB_OK;
+}
+
+// The FP64 eigenvectors sit after the FP32 staging area of d_X, at a 256-byte
+// aligned offset (double2 accesses need 16-byte alignment).
+static size_t zoff(size_t nn, int nk) { return (sizeof(float2) * nn * nk + 255) & ~size_t(255); }
+
+static size_t per_k_bytes(int nv, int prec)
+{
+    size_t nn = (size_t)nv * nv;
+    size_t w = (prec == NRLTB_PREC_FP64) ? eig_work_bytes<double>(nv, 1) : eig_work_bytes<float>(nv, 1);
+    size_t x = (prec == NRLTB_PREC_FP64) ? 16 * nn : 8 * nn;
+    size_t ref = (prec == NRLTB_PREC_FP64) ? 0 : refine_work_bytes(nv, 1);
+    return 32 * nn + w + x + ref + hf_scratch_bytes(nv, 1) + 64 * (size_t)nv;
+}
+
+static int choose_chunk(int nv, int nk, int prec)
+{
+    size_t free_b = 0, total_b = 0;
+    cudaMemGetInfo(&free_b, &total_b);
+    size_t budget = std::min<size_t>(free_b / 2, (size_t)48 << 30);
+    size_t per = per_k_bytes(nv, prec);
+    long c = (long)(budget / std::max<size_t>(per, 1));
+    c = std::max(1L, std::min<long>(c, nk));
+    return (int)c;
+}
+
+// eigensolve of nkc matrices in H, S; eigenvalues into eig (ld nv), vectors into Z (FP64, optional)
+static int run_solve(nrltb_ctx *c, int nv, int nkc, int prec, const double2 *H, const double2 *S, double *eig,
+                     double2 *Zout, int *status, bool vectors)
+{
+    cudaStream_t s = c->stream;
+    if (prec == NRLTB_PREC_FP64) {
+        RET(c->d_work.ensure(eig_work_bytes<double>(nv, nkc)));
+        EigWork<double> w;
+        eig_work_carve<double>(w, c->d_work.p, nv, nkc);
+        eig_solve<double>(s, w, H, S, eig, Zout, vectors);
+        CKL();
+        CK(cudaMemcpyAsync(status, w.status, sizeof(int) * nkc, cudaMemcpyDeviceToDevice, s));
+    } else {
+        if (!refine_available()) { set_err("mixed-precision form not built"); return NRLTB_E_UNSUPPORTED; }
+        RET(c->d_work.ensure(eig_work_bytes<float>(nv, nkc)));
+        RET(c->d_X.ensure(sizeof(float2) * (size_t)nv * nv * nkc));
+        EigWork<float> w;
+        eig_work_carve<float>(w, c->d_work.p, nv, nkc);
+        eig_solve<float>(s, w, H, S, eig, c->d_X.as<float2>(), true);
+        CKL();
+        CK(cudaMemcpyAsync(status, w.status, sizeof(int) * nkc, cudaMemcpyDeviceToDevice, s));
+        RET(c->d_ref.ensure(refine_work_bytes(nv, nkc)));
+        RefineWork rw;
+        refine_work_carve(rw, c->d_ref.p, nv, nkc);
+        refine_eigen(s, rw, H, S, c->d_X.as<float2>(), eig, Zout, status);
+        CKL();
+    }
+    return NRLTB_OK;
+}
+
+__global__ void k_identity(double2 *M, int n, int batch)
+{
+    const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (t >= (long)n * n * batch) return;
+    const long e = t % ((long)n * n);
+    const int r = (int)(e % n), col = (int)(e / n);
+    M[t] = make_double2(r == col ? 1.0 : 0.0, 0.0);
+}
+
+// k points whose overlap is not positive definite get the eigenvalues of S in
+// place of band energies, as diag.f:429-455 leaves them in esk, and take no part
+// in the perturbation (bande.f:997-1003).
+static int fix_nonpd(nrltb_ctx *c, int nv, const std::vector<int> &bad, const double2 *S, double *eig)
+{
+    cudaStream_t s = c->stream;
+    const int nb = (int)bad.size();
+    const size_t nn = (size_t)nv * nv;
+    const size_t mat = (sizeof(double2) * nn * nb + 255) & ~size_t(255);
+    RET(c->d_np.ensure(2 * mat + sizeof(double) * (size_t)nv * nb));
+    double2 *Hp = c->d_np.as<double2>(), *Sp = (double2 *)(c->d_np.as<char>() + mat);
+    double *ep = (double *)(c->d_np.as<char>() + 2 * mat);
+    for (int j = 0; j < nb; ++j)
+        CK(cudaMemcpyAsync(Hp + nn * j, S + nn * bad[j], sizeof(double2) * nn, cudaMemcpyDeviceToDevice, s));
+    NRLTB_LAUNCH(k_identity, cdiv((long)nn * nb, 256), 256, 0, s, Sp, nv, nb);
+    RET(c->d_work.ensure(eig_work_bytes<double>(nv, nb)));
+    EigWork<double> w;
+    eig_work_carve<double>(w, c->d_work.p, nv, nb);
+    eig_solve<double>(s, w, Hp, Sp, ep, nullptr, false);
+    CKL();
+    for (int j = 0; j < nb; ++j)
+        CK(cudaMemcpyAsync(eig + (size_t)nv * bad[j], ep + (size_t)nv * j, sizeof(double) * nv,
+                           cudaMemcpyDeviceToDevice, s));
+    return NRLTB_OK;
+}
+
+static int run_all(nrltb_ctx *c)
+{
+    if (!c->st.valid) { set_err("nothing staged"); return NRLTB_E_ARG; }
+    const Staged &S = c->st;
+    const nrltb_opts &o = S.opt;
+    if (!(o.mode == 3 || o.mode == 4)) { set_err("mode %d: only modes 3 and 4", o.mode); return NRLTB_E_UNSUPPORTED; }
+    if (!(o.precision == NRLTB_PREC_FP64 || o.precision == NRLTB_PREC_MIXED)) { set_err("precision"); return NRLTB_E_ARG; }
+    if (S.nk < 1) { set_err("no k points"); return NRLTB_E_ARG; }
+    const int lpress = (o.mode == 4);
+    cudaStream_t s = c->stream;
+    long long *prev = g_launch_counter;
+    g_launch_counter = &c->launches;
+    int rc = NRLTB_OK;
+    c->nonpd.clear();
+    do {
+        if ((rc = run_search2(c, o.kneigh_in))) break;
+        if ((rc = run_setpar(c, lpress))) break;
+        if ((rc = run_skblocks(c, lpress ? 4 : 2))) break;
+        const int nv = S.nv, nk = S.nk;
+        if ((rc = c->d_eig.ensure(sizeof(double) * (size_t)nv * nk))) break;
+        if ((rc = c->d_deig.ensure(sizeof(double) * (size_t)nv * nk))) break;
+        if ((rc = c->d_ncut.ensure(sizeof(int) * (size_t)nk))) break;
+        if ((rc = c->d_status.ensure(sizeof(int) * (size_t)nk))) break;
+        const int chunk = choose_chunk(nv, nk, o.precision);
+        const size_t nn = (size_t)nv * nv;
+        if ((rc = c->d_H.ensure(sizeof(double2) * nn * chunk))) break;
+        if ((rc = c->d_S.ensure(sizeof(double2) * nn * chunk))) break;
+        if ((rc = c->d_X.ensure(zoff(nn, chunk) + sizeof(double2) * nn * chunk))) break;
+        for (int k0 = 0; k0 < nk && rc == NRLTB_OK; k0 += chunk) {
+            const int nkc = std::min(chunk, nk - k0);
+            double *eig = c->d_eig.as<double>() + (size_t)k0 * nv;
+            int *status = c->d_status.as<int>() + k0;
+            if ((rc = run_bloch(c, k0, nkc, 0, c->d_H.as<double2>(), c->d_S.as<double2>()))) break;
+            double2 *Z = nullptr;
+            if (lpress) {
+                // FP64 eigenvectors live after the FP32 staging area of d_X
+                Z = (double2 *)(c->d_X.as<char>() + zoff(nn, chunk));
+            }
+            if ((rc = run_solve(c, nv, nkc, o.precision, c->d_H.as<double2>(), c->d_S.as<double2>(), eig, Z, status,
+                                lpress != 0)))
+                break;
+            std::vector<int> hst(nkc), bad;
+            if (cudaMemcpyAsync(hst.data(), status, sizeof(int) * nkc, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+                cudaStreamSynchronize(s) != cudaSuccess) { set_err("status readback failed"); rc = NRLTB_E_CUDA; break; }
+            for (int k = 0; k < nkc; ++k) if (hst[k] == NRLTB_K_S_NOT_PD) bad.push_back(k);
+            if (!bad.empty()) {
+                if ((rc = fix_nonpd(c, nv, bad, c->d_S.as<double2>(), eig))) break;
+                for (int k : bad) c->nonpd.push_back(std::make_pair(k0 + k, 0));
+            }
+            if (lpress) {
+                if ((rc = run_bloch(c, k0, nkc, 2, c->d_H.as<double2>(), c->d_S.as<double2>()))) break;
+                if ((rc = c->d_hf.ensure(hf_scratch_bytes(nv, nkc)))) break;
+                if ((rc = run_hf(s, nv, nkc, o.precision, c->d_H.as<double2>(), c->d_S.as<double2>(), Z, eig,
+                                 c->d_deig.as<double>() + (size_t)k0 * nv, c->d_hf.p, nullptr)))
+                    { set_err("hf failed"); break; }
+                CKL();
+            }
+        }
+        if (rc) break;
+        if (lpress) {
+            NRLTB_LAUNCH(k_ncut, cdiv(nk, 128), 128, 0, s, c->d_eig.as<double>(), nv, nv, nk, o.eigcut,
+                         c->d_ncut.as<int>());
+            for (auto &kc : c->nonpd) {
+                cudaMemsetAsync(c->d_ncut.as<int>() + kc.first, 0, sizeof(int), s);
+                cudaMemsetAsync(c->d_deig.as<double>() + (size_t)kc.first * nv, 0, sizeof(double) * nv, s);
+            }
+        }
+        FermiJob job;
+        job.eig = c->d_eig.as<double>();
+        job.deig = c->d_deig.as<double>();
+        job.w = c->d_kw.as<double>();
+        job.ncut = c->d_ncut.as<int>();
+        job.nv = nv; job.nk = nk; job.ldk = nv; job.lpress = lpress;
+        job.tkb = o.tkb; job.zfill = S.zfill; job.tol = (o.fermi_tol > 0) ? o.fermi_tol : 1e-8;
+        if ((rc = c->d_fout.ensure(sizeof(FermiOut)))) break;
+        if ((rc = c->d_fjob.ensure(sizeof(FermiJob)))) break;
+        job.out = c->d_fout.as<FermiOut>();
+        cudaError_t e = cudaMemcpyAsync(c->d_fjob.p, &job, sizeof job, cudaMemcpyHostToDevice, s);
+        if (e != cudaSuccess) { set_err("copy: %s", cudaGetErrorString(e)); rc = NRLTB_E_CUDA; break; }
+        NRLTB_LAUNCH(k_fermi_sums, 1, 1024, 0, s, c->d_fjob.as<FermiJob>());
+        e = cudaGetLastError();
+        if (e != cudaSuccess) { set_err("fermi: %s", cudaGetErrorString(e)); rc = NRLTB_E_CUDA; break; }
+        c->ran = 1;
+    } while (0);
+    g_launch_counter = prev;
+    return rc;
+}
+
+static int fetch(nrltb_ctx *c, nrltb_result *res)
+{
+    if (!c->ran) { set_err("nothing run"); return NRLTB_E_ARG; }
+    cudaStream_t s = c->stream;
+    const Staged &S = c->st;
+    const int nv = S.nv, nk = S.nk;
+    CK(cudaMemcpyAsync(&c->fout, c->d_fout.p, sizeof(FermiOut), cudaMemcpyDeviceToHost, s));
+    std::vector<int> status(nk);
+    CK(cudaMemcpyAsync(status.data(), c->d_status.p, sizeof(int) * nk, cudaMemcpyDeviceToHost, s));
+    if (res->eig) CK(cudaMemcpyAsync(res->eig, c->d_eig.p, sizeof(double) * (size_t)nv * nk, cudaMemcpyDeviceToHost, s));
+    if (res->deig) {
+        if (S.opt.mode == 4)
+            CK(cudaMemcpyAsync(res->deig, c->d_deig.p, sizeof(double) * (size_t)nv * nk, cudaMemcpyDeviceToHost, s));
+        else memset(res->deig, 0, sizeof(double) * (size_t)nv * nk);
+    }
+    if (res->ncut) {
+        if (S.opt.mode == 4) CK(cudaMemcpyAsync(res->ncut, c->d_ncut.p, sizeof(int) * nk, cudaMemcpyDeviceToHost, s));
+        else for (int k = 0; k < nk; ++k) res->ncut[k] = nv;
+    }
+    CK(cudaStreamSynchronize(s));
+    res->efermi = c->fout.efermi;
+    res->e_total = c->fout.e_total;
+    res->pressure = c->fout.pressure;
+    res->fermi_shift = c->fout.fermi_shift;
+    res->dismin = c->dismin;
+    res->npairs = c->npairs;
+    res->nv = nv;
+    res->nk = nk;
+    res->kneigh_out = c->kneigh_out;
+    int bad = 0;
+    for (int k = 0; k < nk; ++k) bad += (status[k] == NRLTB_K_S_NOT_PD);
+    res->nonphysical_k = bad;
+    if (res->k_status) memcpy(res->k_status, status.data(), sizeof(int) * nk);
+    return NRLTB_OK;
+}
+
+// ---- exported ABI -----------------------------------------------------------
+extern "C" {
+
+int nrltb_abi_version(void) { return NRLTB_ABI_VERSION; }
+const char *nrltb_last_error(void) { return g_err; }
+
+int nrltb_ctx_create(nrltb_ctx **out, int device)
+{
+    if (!out) { set_err("null out"); return NRLTB_E_ARG; }
+    *out = nullptr;
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev <= 0) {
+        set_err("no CUDA device: %s", e != cudaSuccess ? cudaGetErrorString(e) : "count 0");
+        return NRLTB_E_NODEVICE;
+    }
+    if (device < 0 || device >= ndev) { set_err("device %d of %d", device, ndev); return NRLTB_E_ARG; }
+    CK(cudaSetDevice(device));
+    nrltb_ctx *c = new nrltb_ctx();
+    c->device = device;
+    e = cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking);
+    if (e != cudaSuccess) { set_err("stream: %s", cudaGetErrorString(e)); delete c; return NRLTB_E_CUDA; }
+    c->stream = c->own;
+    *out = c;
+    return NRLTB_OK;
+}
+
+int nrltb_ctx_destroy(nrltb_ctx *c)
+{
+    if (!c) return NRLTB_OK;
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->stream);
+    DBuf *bufs[] = {&c->d_kkind, &c->d_posn, &c->d_posq, &c->d_kbas, &c->d_dnn, &c->d_screenl, &c->d_param,
+                    &c->d_kq, &c->d_kw, &c->d_ksk, &c->d_orb, &c->d_code, &c->d_blk, &c->d_misc, &c->d_pairs,
+                    &c->d_sk, &c->d_seg, &c->d_ph, &c->d_H, &c->d_S, &c->d_X, &c->d_work, &c->d_ref, &c->d_hf, &c->d_np,
+                    &c->d_eig, &c->d_deig, &c->d_ncut, &c->d_status, &c->d_fjob, &c->d_fout};
+    for (DBuf *b : bufs) b->release();
+    if (c->own) cudaStreamDestroy(c->own);
+    delete c;
+    return NRLTB_OK;
+}
+
+int nrltb_ctx_set_stream(nrltb_ctx *c, void *stream)
+{
+    if (!c) return NRLTB_E_ARG;
+    c->stream = stream ? (cudaStream_t)stream : c->own;
+    return NRLTB_OK;
+}
+
+long long nrltb_ctx_launch_count(const nrltb_ctx *c) { return c ? c->launches : 0; }
+
+int nrltb_stage(nrltb_ctx *c, const nrltb_structure *st, const nrltb_params *par, const nrltb_kmesh *km,
+                const nrltb_opts *opt)
+{
+    if (!c || !km || !opt) { set_err("null argument"); return NRLTB_E_ARG; }
+    CK(cudaSetDevice(c->device));
+    c->ran = 0;
+    return stage_host(c, st, par, km, opt);
+}
+
+int nrltb_run(nrltb_ctx *c)
+{
+    if (!c) return NRLTB_E_ARG;
+    CK(cudaSetDevice(c->device));
+    return run_all(c);
+}
+
+int nrltb_fetch(nrltb_ctx *c, nrltb_result *res)
+{
+    if (!c || !res) return NRLTB_E_ARG;
+    CK(cudaSetDevice(c->device));
+    return fetch(c, res);
+}
+
+int nrltb_bande(nrltb_ctx *c, const nrltb_structure *st, const nrltb_params *par, const nrltb_kmesh *km,
+                const nrltb_opts *opt, nrltb_result *res)
+{
+    RET(nrltb_stage(c, st, par, km, opt));
+    RET(nrltb_run(c));
+    return nrltb_fetch(c, res);
+}
+
+int nrltb_bande_batch(nrltb_ctx *c, int nstruct, const nrltb_structure *st, const nrltb_params *par,
+                      const nrltb_kmesh *km, const nrltb_opts *opt, nrltb_result *res)
+{
+    if (!c || nstruct < 0 || (nstruct > 0 && (!st || !par || !km || !opt || !res))) return NRLTB_E_ARG;
+    for (int i = 0; i < nstruct; ++i) RET(nrltb_bande(c, st + i, par + i, km + i, opt + i, res + i));
+    return NRLTB_OK;
+}
+
+int nrltb_search2(nrltb_ctx *c, const nrltb_structure *st, const nrltb_params *par, int kneigh_in,
+                  nrltb_pairs *out, int *kneigh_out, double *dismin)
+{
+    if (!c || !out) return NRLTB_E_ARG;
+    CK(cudaSetDevice(c->device));
+    RET(stage_host(c, st, par, nullptr, nullptr));
+    long long *prev = g_launch_counter;
+    g_launch_counter = &c->launches;
+    int rc = run_search2(c, kneigh_in);
+    g_launch_counter = prev;
+    RET(rc);
+    out->npairs = c->npairs;
+    if (kneigh_out) *kneigh_out = c->kneigh_out;
+    if (dismin) *dismin = c->dismin;
+    if (c->npairs > out->capacity) { set_err("pair capacity %d < %d", out->capacity, c->npairs); return NRLTB_E_CAPACITY; }
+    const int P = c->npairs;
+    DevPairs pr = pairs_view(c, std::max(P, 1));
+    cudaStream_t s = c->stream;
+    CK(cudaMemcpyAsync(out->tt, pr.tt, sizeof(double) * 3 * P, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(out->dlv, pr.dlv, sizeof(int) * 3 * P, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(out->dist, pr.dist, sizeof(double) * P, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(out->screen, pr.screen, sizeof(double) * P, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(out->dscrn, pr.dscrn, sizeof(double) * P, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(out->jkind, pr.jkind, sizeof(int) * 2 * P, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(out->jatm, pr.jatm, sizeof(int) * 2 * P, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    return NRLTB_OK;
+}
+
+int nrltb_setpar(nrltb_ctx *c, const nrltb_structure *st, const nrltb_params *par, const nrltb_pairs *pairs,
+                 double *hop, double *over, double *paros, double *den, double *dhop, double *dover, double *dparos)
+{
+    if (!c || !pairs || !hop || !over || !paros || !den) return NRLTB_E_ARG;
+    CK(cudaSetDevice(c->device));
+    RET(stage_host(c, st, par, nullptr, nullptr));
+    cudaStream_t s = c->stream;
+    const int P = pairs->npairs;
+    c->npairs = P;
+    RET(c->d_pairs.ensure(pairs_bytes(std::max(P, 1))));
+    DevPairs pr = pairs_view(c, std::max(P, 1));
+    CK(cudaMemcpyAsync(pr.tt, pairs->tt, sizeof(double) * 3 * P, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(pr.dlv, pairs->dlv, sizeof(int) * 3 * P, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(pr.dist, pairs->dist, sizeof(double) * P, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(pr.screen, pairs->screen, sizeof(double) * P, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(pr.dscrn, pairs->dscrn, sizeof(double) * P, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(pr.jkind, pairs->jkind, sizeof(int) * 2 * P, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(pr.jatm, pairs->jatm, sizeof(int) * 2 * P, cudaMemcpyHostToDevice, s));
+    const int deriv = (dhop && dover && dparos) ? 1 : 0;
+    long long *prev = g_launch_counter;
+    g_launch_counter = &c->launches;
+    int rc = run_setpar(c, deriv);
+    g_launch_counter = prev;
+    RET(rc);
+    DevSK sk = sk_view(c, std::max(P, 1), st->natoms, par->kinds);
+    CK(cudaMemcpyAsync(hop, sk.hop, sizeof(double) * 14 * P, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(over, sk.over, sizeof(double) * 14 * P, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(paros, sk.paros, sizeof(double) * 4 * st->natoms, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(den, sk.den, sizeof(double) * st->natoms * par->kinds, cudaMemcpyDeviceToHost, s));
+    if (deriv) {
+        CK(cudaMemcpyAsync(dhop, sk.dhop, sizeof(double) * 14 * P, cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(dover, sk.dover, sizeof(double) * 14 * P, cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(dparos, sk.dparos, sizeof(double) * 4 * st->natoms, cudaMemcpyDeviceToHost, s));
+    }
+    CK(cudaStreamSynchronize(s));
+    return NRLTB_OK;
+}
+
+int nrltb_setham(nrltb_ctx *c, const nrltb_structure *st, const nrltb_params *par, const nrltb_kmesh *km,
+                 int which, double *hmat, double *smat)
+{
+    if (!c || !km || !hmat || !smat || (which != 0 && which != 1)) return NRLTB_E_ARG;
+    CK(cudaSetDevice(c->device));
+    nrltb_opts o;
+    memset(&o, 0, sizeof o);
+    o.mode = which ? 4 : 3;
+    RET(stage_host(c, st, par, km, &o));
+    long long *prev = g_launch_counter;
+    g_launch_counter = &c->launches;
+    int rc = run_search2(c, 0);
+    if (!rc) rc = run_setpar(c, which);
+    if (!rc) rc = run_skblocks(c, which ? 4 : 2);
+    const int nv = c->st.nv, nk = c->st.nk;
+    const size_t nn = (size_t)nv * nv;
+    if (!rc) rc = c->d_H.ensure(sizeof(double2) * nn * nk);
+    if (!rc) rc = c->d_S.ensure(sizeof(double2) * nn * nk);
+    if (!rc) rc = run_bloch(c, 0, nk, which ? 2 : 0, c->d_H.as<double2>(), c->d_S.as<double2>());
+    g_launch_counter = prev;
+    RET(rc);
+    cudaStream_t s = c->stream;
+    CK(cudaMemcpyAsync(hmat, c->d_H.p, sizeof(double2) * nn * nk, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(smat, c->d_S.p, sizeof(double2) * nn * nk, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    return NRLTB_OK;
+}
+
+int nrltb_diag(nrltb_ctx *c, int nv, int nk, const double *hmat, const double *smat, int precision, double *eig,
+               double *z, int *k_status)
+{
+    if (!c || nv < 1 || nk < 1 || !hmat || !smat || !eig) return NRLTB_E_ARG;
+    if (!(precision == NRLTB_PREC_FP64 || precision == NRLTB_PREC_MIXED)) return NRLTB_E_ARG;
+    CK(cudaSetDevice(c->device));
+    cudaStream_t s = c->stream;
+    const size_t nn = (size_t)nv * nv;
+    RET(c->d_H.ensure(sizeof(double2) * nn * nk));
+    RET(c->d_S.ensure(sizeof(double2) * nn * nk));
+    RET(c->d_eig.ensure(sizeof(double) * (size_t)nv * nk));
+    RET(c->d_status.ensure(sizeof(int) * (size_t)nk));
+    RET(c->d_X.ensure(zoff(nn, nk) + sizeof(double2) * nn * nk));
+    CK(cudaMemcpyAsync(c->d_H.p, hmat, sizeof(double2) * nn * nk, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(c->d_S.p, smat, sizeof(double2) * nn * nk, cudaMemcpyHostToDevice, s));
+    double2 *Z = (double2 *)(c->d_X.as<char>() + zoff(nn, nk));
+    long long *prev = g_launch_counter;
+    g_launch_counter = &c->launches;
+    int rc = run_solve(c, nv, nk, precision, c->d_H.as<double2>(), c->d_S.as<double2>(), c->d_eig.as<double>(),
+                       Z, c->d_status.as<int>(), z != nullptr);
+    g_launch_counter = prev;
+    RET(rc);
+    CK(cudaMemcpyAsync(eig, c->d_eig.p, sizeof(double) * (size_t)nv * nk, cudaMemcpyDeviceToHost, s));
+    if (z) CK(cudaMemcpyAsync(z, Z, sizeof(double2) * nn * nk, cudaMemcpyDeviceToHost, s));
+    if (k_status) CK(cudaMemcpyAsync(k_status, c->d_status.p, sizeof(int) * nk, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    return NRLTB_OK;
+}
+
+int nrltb_fermi(nrltb_ctx *c, int nv, int nk, const double *eig, const double *w, double tkb, double zfill,
+                double tol, double *efermi)
+{
+    if (!c || nv < 1 || nk < 1 || !eig || !w || !efermi) return NRLTB_E_ARG;
+    if (!(zfill > 0)) { set_err("zfill <= 0: no Fermi level (fermi.f:165)"); return NRLTB_E_ARG; }
+    CK(cudaSetDevice(c->device));
+    cudaStream_t s = c->stream;
+    RET(c->d_eig.ensure(sizeof(double) * (size_t)nv * nk));
+    RET(c->d_kw.ensure(sizeof(double) * nk));
+    RET(c->d_fout.ensure(sizeof(FermiOut)));
+    RET(c->d_fjob.ensure(sizeof(FermiJob)));
+    CK(cudaMemcpyAsync(c->d_eig.p, eig, sizeof(double) * (size_t)nv * nk, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(c->d_kw.p, w, sizeof(double) * nk, cudaMemcpyHostToDevice, s));
+    FermiJob job;
+    memset(&job, 0, sizeof job);
+    job.eig = c->d_eig.as<double>();
+    job.w = c->d_kw.as<double>();
+    job.nv = nv; job.nk = nk; job.ldk = nv; job.lpress = 0;
+    job.tkb = tkb; job.zfill = zfill; job.tol = tol > 0 ? tol : 1e-8;
+    job.out = c->d_fout.as<FermiOut>();
+    CK(cudaMemcpyAsync(c->d_fjob.p, &job, sizeof job, cudaMemcpyHostToDevice, s));
+    long long *prev = g_launch_counter;
+    g_launch_counter = &c->launches;
+    NRLTB_LAUNCH(k_fermi_sums, 1, 1024, 0, s, c->d_fjob.as<FermiJob>());
+    g_launch_counter = prev;
+    CKL();
+    FermiOut o;
+    CK(cudaMemcpyAsync(&o, c->d_fout.p, sizeof o, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    *efermi = o.efermi;
+    return NRLTB_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,36 @@
+// refine.cuh -- mixed-precision form: FP64-accurate refinement of FP32
+// eigenpairs, and the Hellmann-Feynman products of both forms.
+#pragma once
+#include "common.cuh"
+
+namespace nrltb {
+
+struct RefineWork {
+    int n, batch;
+    double2 *YH, *YS;       // H X, S X
+    double2 *T, *R;         // X^H H X, X^H S X
+    double2 *U;             // cluster rotations / update matrix
+    float2 *Ef;             // FP32 update matrix
+    float2 *Xr;             // rotated FP32 vectors
+    float2 *XE;             // X E (FP32)
+    double *lam;            // refined eigenvalues
+    int *cl;                // cluster id per eigenvalue
+};
+
+bool refine_available();
+size_t refine_work_bytes(int n, int batch);
+void refine_work_carve(RefineWork &w, void *base, int n, int batch);
+// H, S FP64; X FP32 eigenvectors from the FP32 solve (S-orthonormal to FP32
+// accuracy); writes refined eigenvalues (ascending) and, if Z != NULL, FP64
+// eigenvectors.  status[k] gets NRLTB_K_NOT_CONVERGED when a cluster exceeds the
+// handled size.
+void refine_eigen(cudaStream_t s, RefineWork &w, const double2 *H, const double2 *S, const float2 *X,
+                  double *eig, double2 *Z, int *status);
+
+// Hellmann-Feynman shifts deig = diag(Z^H dH Z) - eig * diag(Z^H dS Z) for nkc
+// matrices; scratch must hold 2 n^2 nkc double2.
+int run_hf(cudaStream_t s, int n, int nkc, int prec, const double2 *dH, const double2 *dS, const double2 *Z,
+           const double *eig, double *deig, void *scratch, void *unused);
+size_t hf_scratch_bytes(int n, int nkc);
+
+}  // namespace nrltb

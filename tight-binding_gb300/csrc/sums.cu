@@ -1,0 +1,187 @@
+// sums.cu -- Fermi level, band energy, pressure (fermi.f, bande.f sums) and the
+// Hellmann-Feynman eigenvalue derivatives (perturb.f).
+//
+// k_fermi_sums: one CTA per structure.  The MPI_ALLREDUCE of every Newton step
+// (fermi.f:365-376) and the final MPI_REDUCEs (bande.f:1255-1331) become block
+// reductions; the iteration itself is the reference's: start at the middle of
+// the band-nfill / nfill+1 edges, Newton steps clamped to the bracket, bisection
+// when dN/dmu is small, stop when |N - zfill| < tol or the bracket closes.
+// Occupations are exactly 1 below mu - 20 kT and 0 above mu + 20 kT.
+#include "sums.cuh"
+
+namespace nrltb {
+
+__device__ inline double block_sum_d(double v, double *sh) { return block_sum<double>(v, sh); }
+__device__ inline double block_max_d(double v, double *sh)
+{
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    __syncthreads();
+    if (lane == 0) sh[wid] = v;
+    __syncthreads();
+    double t = (threadIdx.x < nw) ? sh[threadIdx.x] : -1e308;
+    if (wid == 0) for (int o = 16; o > 0; o >>= 1) t = fmax(t, __shfl_xor_sync(0xffffffffu, t, o));
+    if (threadIdx.x == 0) sh[0] = t;
+    __syncthreads();
+    double r = sh[0];
+    __syncthreads();
+    return r;
+}
+
+__global__ void __launch_bounds__(1024) k_fermi_sums(FermiJob *jobs)
+{
+    __shared__ double sh[32];
+    FermiJob J = jobs[blockIdx.x];
+    const int nv = J.nv, nk = J.nk, tid = threadIdx.x, nt = blockDim.x;
+    const long tot = (long)nv * nk;
+    const double el = 2.0, nearz = 1e-5, tkb = J.tkb, zfill = J.zfill, tol = J.tol;
+    const double beta = (tkb < nearz) ? 1.0 / nearz : 1.0 / tkb;
+    const int nfill = (int)(zfill / el + nearz);
+    const bool linst = fabs(zfill / el - (double)nfill) < tol;
+    // bounds (fermi.f:197-261)
+    double stl = -1e308, sth = 1e308, mul = 1e308, muh = -1e308;
+    for (long q = tid; q < tot; q += nt) {
+        const int k = (int)(q / nv), i = (int)(q % nv);
+        const double e = J.eig[(long)k * J.ldk + i];
+        if (i == nfill - 1) stl = fmax(stl, e);
+        if (i == nfill) sth = fmin(sth, e);
+        muh = fmax(muh, e);
+        mul = fmin(mul, e);
+    }
+    double stlow = block_max_d(stl, sh), sthigh = -block_max_d(-sth, sh);
+    double muhigh = block_max_d(muh, sh), mulow = -block_max_d(-mul, sh);
+    if (nfill >= nv) sthigh = J.eig[nv - 1];
+    double mu;
+    int it = 0;
+    if (linst && (sthigh - stlow > 20.0 * tkb)) {
+        mu = 0.5 * (stlow + sthigh);
+    } else {
+        mu = 0.5 * (stlow + sthigh);
+        for (it = 1; it <= 10000; ++it) {
+            const double mum20 = mu - tkb * 20.0, mup20 = mu + tkb * 20.0, btmu = -beta * mu;
+            double ns = 0, dns = 0;
+            for (long q = tid; q < tot; q += nt) {
+                const int k = (int)(q / nv), i = (int)(q % nv);
+                const double e = J.eig[(long)k * J.ldk + i];
+                const double wk = J.w[k];
+                if (e < mum20) ns += wk;
+                else if (e < mup20) {
+                    const double ex = exp(beta * e + btmu);
+                    const double f = 1.0 / (1.0 + ex);
+                    ns += wk * f;
+                    dns += wk * (ex * f * f);
+                }
+            }
+            double nsum = el * block_sum_d(ns, sh);
+            double dnsum = beta * el * block_sum_d(dns, sh);
+            if (fabs(nsum - zfill) < tol) break;
+            if (nsum < zfill) mulow = mu; else muhigh = mu;
+            double mu1;
+            if (dnsum < tol) mu1 = 0.5 * (mulow + muhigh);
+            else {
+                mu1 = mu + (zfill - nsum) / dnsum;
+                if (mu1 > muhigh) mu1 = 0.5 * (mu + muhigh);
+                else if (mu1 < mulow) mu1 = 0.5 * (mu + mulow);
+            }
+            if (muhigh - mulow > tol) mu = mu1;
+            else break;
+        }
+    }
+    // energy and pressure sums (bande.f:1162-1330)
+    const double tkbi = (tkb < 1e-5) ? 1e5 : 1.0 / tkb;
+    const double efp = mu + 20.0 * tkb, efm = mu - 20.0 * tkb;
+    double es = 0, d1 = 0, d2 = 0, d3 = 0, dfb = 0, dfe = 0;
+    for (long q = tid; q < tot; q += nt) {
+        const int k = (int)(q / nv), i = (int)(q % nv);
+        const int lim = J.lpress ? J.ncut[k] : nv;
+        if (i >= lim) continue;
+        const double e = J.eig[(long)k * J.ldk + i];
+        if (!(e < efp)) continue;
+        const double wt = 2.0 * J.w[k], ewt = wt * e;
+        const double de = J.lpress ? J.deig[(long)k * J.ldk + i] : 0.0;
+        if (e < efm) {
+            es += ewt;
+            d1 += wt * de;
+        } else {
+            const double x = e - mu;
+            const double fbe = 1.0 / (1.0 + exp(tkbi * x));
+            es += ewt * fbe;
+            if (J.lpress) {
+                const double dfbe = -tkbi * fbe * (1.0 / (1.0 + exp(tkbi * (-x))));
+                dfb += dfbe * wt;
+                d3 += dfbe * ewt;
+                const double dewt = wt * de;
+                d1 += dewt * fbe;
+                dfe += dfbe * dewt;
+                d2 += dfbe * ewt * de;
+            }
+        }
+    }
+    es = block_sum_d(es, sh);
+    d1 = block_sum_d(d1, sh);
+    d2 = block_sum_d(d2, sh);
+    d3 = block_sum_d(d3, sh);
+    dfb = block_sum_d(dfb, sh);
+    dfe = block_sum_d(dfe, sh);
+    if (tid == 0) {
+        FermiOut o;
+        o.efermi = mu;
+        o.e_total = es;
+        o.fermi_shift = 0;
+        o.pressure = 0;
+        if (J.lpress) {
+            const double dfermi = (fabs(dfb) > 1e-10) ? dfe / dfb : 0.0;
+            o.fermi_shift = dfermi;
+            o.pressure = -(d1 + (d2 - dfermi * d3));
+        }
+        o.iterations = it;
+        J.out[0] = o;
+    }
+}
+
+// ncut[k] = number of eigenvalues <= eigcut (perturb.f:87-95)
+__global__ void k_ncut(const double *eig, int ldk, int nv, int nk, double eigcut, int *ncut)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nk) return;
+    int c = 0;
+    while (c < nv && !(eig[(long)k * ldk + c] > eigcut)) ++c;
+    ncut[k] = c;
+}
+
+// Hellmann-Feynman shifts from P = triu(dH) Z and Q = triu(dS) Z:
+//   z^H M z = 2 Re(z^H triu(M) z) - sum_i M_ii |z_i|^2
+//   deig_n = z_n^H dH z_n - e_n z_n^H dS z_n
+// One warp per (column n, matrix).
+template <typename C2>
+__global__ void k_hf_dots(const C2 *Z, const C2 *Pm, const C2 *Qm, const double2 *dH, const double2 *dS,
+                          const double *eig, double *deig, int n, int batch)
+{
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (warp >= n * batch) return;
+    const int b = warp / n, col = warp % n;
+    const long off = (long)b * n * n + (long)col * n;
+    double sp = 0, sq = 0, dh = 0, ds = 0;
+    for (int i = lane; i < n; i += 32) {
+        const C2 z = Z[off + i], p = Pm[off + i], q = Qm[off + i];
+        sp += (double)z.x * p.x + (double)z.y * p.y;
+        sq += (double)z.x * q.x + (double)z.y * q.y;
+        const double a2 = (double)z.x * z.x + (double)z.y * z.y;
+        dh += dH[(long)b * n * n + (long)i * (n + 1)].x * a2;
+        ds += dS[(long)b * n * n + (long)i * (n + 1)].x * a2;
+    }
+    sp = warp_sum(sp); sq = warp_sum(sq); dh = warp_sum(dh); ds = warp_sum(ds);
+    if (lane == 0) {
+        const double e = eig[(long)b * n + col];
+        deig[(long)b * n + col] = (2.0 * sp - dh) - e * (2.0 * sq - ds);
+    }
+}
+
+void launch_hf_dots(cudaStream_t s, const double2 *Z, const double2 *P, const double2 *Q, const double2 *dH,
+                    const double2 *dS, const double *eig, double *deig, int n, int batch)
+{
+    const long warps = (long)n * batch;
+    NRLTB_LAUNCH(k_hf_dots<double2>, cdiv(warps * 32, 256), 256, 0, s, Z, P, Q, dH, dS, eig, deig, n, batch);
+}
+
+}  // namespace nrltb
