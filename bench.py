@@ -1,0 +1,295 @@
+"""Benchmark: k-point H/S build + eigensolves per second on one GB300.
+
+Workload (the configuration the metric is quoted on): fcc128, a 128-atom fcc
+supercell with seeded 0.1 bohr displacements, spd basis (N = 1152), 3x3x3
+Monkhorst-Pack mesh (27 k), mode 4.  One step = one full per-structure k loop
+(the reference's bande call plus the search2 before it): neighbour list, SK
+tables, H(k) and S(k), generalized eigensolve with vectors, dH/dV and dS/dV,
+Hellmann-Feynman shifts, Fermi level, E(T) and P(T) for all 27 k.  k-point
+solves/s = 27 / step time.
+
+  value    device-resident: inputs staged in HBM before the timed region
+           (nrltb_stage), K steps of nrltb_run timed with CUDA events on the
+           library's stream.
+  e2e      the same step through the reference-facing call nrltb_bande with
+           host buffers (input upload and result download inside the region).
+  --impl reference
+           the reference algorithm on the host cores: the C restatement in
+           oracle/ (the Fortran reference cannot be compiled here), one k per
+           thread on all host threads, single-threaded LAPACK zhpgv per k.
+
+The step's working set (H, S, dH, dS and the solver workspace for 27 k) is
+several GB, far larger than L2, so no L2 flush is needed between steps.
+"""
+import os
+
+os.environ.setdefault("OPENBLAS_NUM_THREADS", "1")    # one LAPACK thread per k (before numpy)
+
+import argparse
+import json
+import subprocess
+import sys
+import tempfile
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(REPO, "tight-binding_gb300"))
+
+METRIC = "k-point H/S build+eigensolves/s at N=1152, mixed vs FP64 on GB300 at 1e-9 Ry"
+UNIT = "k-point solves/s"
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def workload(name):
+    from nrltb import synth
+    st, par, km, o = synth.CONFIGS[name]()
+    return st, par, km, o
+
+
+def workload_desc(name, st, par, km):
+    return (f"{name}: {st.natoms}-atom supercell, N={par.nv(st)}, {km.nk} k, mode 4 "
+            f"(H/S/dH/dS build, eigensolve with vectors, Hellmann-Feynman, E_F, E, P)")
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons during a region."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+        return self
+
+    def __exit__(self, *a):
+        if self.p:
+            self.p.terminate()
+            try:
+                self.p.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.p.kill()
+
+    def summary(self):
+        import statistics
+        self.f.flush()
+        rows = []
+        with open(self.f.name) as fh:
+            for line in fh:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.f.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "samples": len(rows), "reasons": reasons}
+
+
+def cpu_sample(st, par, km, mode, nthreads, nk_sample):
+    """Oracle (reference algorithm) on the first nk_sample k points, all threads."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle
+    from nrltb import KMesh, Opts
+    sub = KMesh(km.k[:nk_sample], km.w[:nk_sample] / km.w[:nk_sample].sum())
+    opts = Opts(mode=mode, tkb=0.005, eigcut=1e3)
+    t0 = time.perf_counter()
+    oracle.bande(st, par, sub, opts, nthreads=nthreads)
+    return time.perf_counter() - t0
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    st, par, km, o = workload(args.config)
+    ncores = os.cpu_count() or 1
+    nks = min(km.nk, ncores)
+    times = []
+    for i in range(args.warmup + args.steps):
+        t = cpu_sample(st, par, km, 4, ncores, nks)
+        if i >= args.warmup:
+            times.append(t)
+    mean = sum(times) / len(times)
+    value = nks / mean
+    sample = (f"{nks} of the {km.nk} k points per step (one per host thread), mode 4: setham + "
+              f"zhpgv with vectors + sethamv + perturb, then Fermi/E/P")
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference",
+            "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": mean * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded structure and parameters)",
+            "config": {"workload": workload_desc(args.config, st, par, km), "host_cores": ncores},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": ncores, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--config", default="fcc128")
+    ap.add_argument("--precision", default="auto", choices=["auto", "fp64", "mixed"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import numpy as np
+    import torch
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from nrltb import Context, Opts, abi
+    ctx = Context(local)
+    lib = ctx.lib
+    st, par, km, o = workload(args.config)
+    nk = km.nk
+    prec = {"fp64": abi.PREC_FP64, "mixed": abi.PREC_MIXED}.get(args.precision)
+    if prec is None:
+        prec = abi.PREC_MIXED if _mixed_available(ctx, st, par, km) else abi.PREC_FP64
+    opts = Opts(mode=4, precision=prec, tkb=o["tkb"], eigcut=1e3, fermi_tol=1e-11)
+
+    stream = torch.cuda.Stream(local)
+    ctx.set_stream(stream.cuda_stream)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if ws > 1:
+            torch.distributed.barrier()
+            torch.cuda.synchronize()
+
+    def max_over_ranks(x):
+        if ws == 1:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        return float(t.item())
+
+    # ---- device-resident value ----
+    ctx.stage(st, par, km, opts)
+    for _ in range(args.warmup):
+        ctx.run()
+    barrier()
+    l0 = ctx.launch_count()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        barrier()
+        e0.record(stream)
+        for _ in range(args.steps):
+            ctx.run()
+        e1.record(stream)
+        barrier()
+    launches_value = ctx.launch_count() - l0
+    ms_dev = e0.elapsed_time(e1) / args.steps
+    ms_dev = max_over_ranks(ms_dev)
+    clocks = clk.summary()
+    res = ctx.fetch()
+    value = ws * nk / (ms_dev * 1e-3)
+
+    # ---- end to end through nrltb_bande with host buffers ----
+    for _ in range(2):
+        ctx.bande(st, par, km, opts)
+    barrier()
+    l1 = ctx.launch_count()
+    t0 = time.perf_counter()
+    e0.record(stream)
+    for _ in range(args.steps):
+        r = ctx.bande(st, par, km, opts)
+    e1.record(stream)
+    barrier()
+    ms_e2e = max_over_ranks((time.perf_counter() - t0) * 1e3 / args.steps)
+    launches_e2e = ctx.launch_count() - l1
+    e2e_value = ws * nk / (ms_e2e * 1e-3)
+    h2d = (st.kkind.nbytes + st.posn.nbytes + st.posq.nbytes + par.kbas.nbytes + par.dnn.nbytes +
+           par.screenl.nbytes + par.param.nbytes + km.k.nbytes + km.w.nbytes + 8 * 3 * st.natoms)
+    d2h = r.eig.nbytes + r.deig.nbytes + r.ncut.nbytes + r.k_status.nbytes + 64
+
+    # ---- roofline of the dominant kernel (batched complex GEMM of the solver) ----
+    n = par.nv(st)
+    gprec = 0 if prec == abi.PREC_FP64 else 1
+    ms_g, fl_g = np.zeros(1), np.zeros(1)
+    lib.nrltb_bench_zgemm(ctx.h, gprec, n, nk, 3, ms_g.ctypes.data_as(abi._dp), fl_g.ctypes.data_as(abi._dp))
+    peak = np.zeros(1)
+    lib.nrltb_bench_peak(ctx.h, gprec, peak.ctypes.data_as(abi._dp))
+    achieved = fl_g[0] / (ms_g[0] * 1e-3) / 1e12
+    roofline = {"bound": "tensor", "pipe": "fp64-fma" if gprec == 0 else "fp32-fma",
+                "kernel": "zgemm_kernel (batched complex GEMM, n=%d x %d matrices)" % (n, nk),
+                "achieved": achieved, "peak": float(peak[0]), "unit": "TFLOP/s",
+                "frac": achieved / float(peak[0]) if peak[0] > 0 else None, "traffic": None,
+                "peak_source": "live FMA-pipe microbenchmark on this GPU (MEASURED_PEAKS.json has "
+                               "no FP64/FP32-SIMT figure; GB300 has no FP64 tensor path)"}
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_dev, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if prec == abi.PREC_FP64 else "f32+f64",
+            "data": "synthetic (seeded structure and parameters, no public dataset)",
+            "config": {"workload": workload_desc(args.config, st, par, km),
+                       "precision": "fp64" if prec == abi.PREC_FP64 else "mixed",
+                       "l2": "inputs larger than L2 (H,S,dH,dS + workspace of 27 k are GBs)",
+                       "E_F": res.efermi, "E_total": res.e_total, "P": res.pressure},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h), "ms_per_step": ms_e2e},
+            "gpu_launches": int(launches_value),
+            "gpu_launches_e2e": int(launches_e2e),
+            "clocks": clocks, "roofline": roofline}
+
+    if rank == 0 and not args.no_cpu_baseline:
+        ncores = os.cpu_count() or 1
+        nks = min(nk, ncores)
+        t = cpu_sample(st, par, km, 4, ncores, nks)
+        line["cpu_baseline"] = {"value": nks / t, "unit": UNIT, "cores": ncores, "kind": "port",
+                                "sample": f"{nks} of {nk} k points, one per host thread, mode 4 "
+                                          f"(setham + zhpgv with vectors + sethamv + perturb + Fermi/E/P)"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def _mixed_available(ctx, st, par, km):
+    from nrltb import abi
+    import ctypes as C
+    import numpy as np
+    # a 1x1 probe: the mixed form reports NRLTB_E_UNSUPPORTED when it is not built
+    H = np.array([[[2.0 + 0j]]])
+    S = np.array([[[1.0 + 0j]]])
+    eig = np.zeros((1, 1))
+    stv = np.zeros(1, np.int32)
+    rc = ctx.lib.nrltb_diag(ctx.h, 1, 1, H.ctypes.data_as(abi._dp), S.ctypes.data_as(abi._dp), abi.PREC_MIXED,
+                            eig.ctypes.data_as(abi._dp), None, stv.ctypes.data_as(C.POINTER(C.c_int)))
+    return rc == 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -16,7 +16,7 @@ def _declared(header):
 def test_library_builds_and_exports_all_symbols():
     build.build_all()
     lib = ctypes.CDLL(abi.GPU_LIB)
-    names = _declared("nrltb.h") | _declared("nrltb_input.h")
+    names = _declared("nrltb.h") | _declared("nrltb_input.h") | _declared("nrltb_bench.h")
     assert len(names) >= 20
     missing = [n for n in names if not hasattr(lib, n)]
     assert not missing, missing

@@ -640,6 +640,13 @@ int nrltb_ctx_set_stream(nrltb_ctx *c, void *stream)
 
 long long nrltb_ctx_launch_count(const nrltb_ctx *c) { return c ? c->launches : 0; }
 
+// stream of a context, for the measurement hooks in bench_hooks.cu
+cudaStream_t nrltb_ctx_stream_internal(nrltb_ctx *c)
+{
+    cudaSetDevice(c->device);
+    return c->stream;
+}
+
 int nrltb_stage(nrltb_ctx *c, const nrltb_structure *st, const nrltb_params *par, const nrltb_kmesh *km,
                 const nrltb_opts *opt)
 {

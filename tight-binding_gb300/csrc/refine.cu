@@ -1,25 +1,47 @@
-// refine.cu -- mixed-precision refinement and Hellmann-Feynman products.
+// refine.cu -- mixed-precision form: FP64-accurate refinement of FP32 eigenpairs
+// of H x = lambda S x, and the Hellmann-Feynman products of both forms.
+//
+// Given FP32 eigenvectors X (S-orthonormal to FP32 accuracy) of FP64 H, S:
+//   1. T = X^H H X, R = X^H S X in double-float arithmetic (dfgemm.cuh).
+//   2. Clusters: eigenvalue estimates T_jj / R_jj closer than delta (a fraction
+//      of the spectral span) are grouped; each cluster's block (T_c, R_c) is
+//      solved exactly (Cholesky + complex Jacobi, FP64), giving a rotation U_c
+//      (Rayleigh-Ritz inside the cluster).
+//   3. With T' = U^H T U, R' = U^H R U (U block diagonal), one Newton-type
+//      correction of the whole basis (Ogita-Aishima): for i, j in different
+//      clusters E_ij = (T'_ij - l_j R'_ij) / (l_j - l_i), E_jj = (1 - R'_jj)/2,
+//      and the eigenvalue with its second-order term
+//        l_j + sum_{i not in c(j)} |T'_ij - l_j R'_ij|^2 / (l_j - l_i).
+//   4. Z = X U (I + E) in FP64 (X U in FP64, the small X U E in FP32), columns
+//      reordered by ascending eigenvalue.
+// One step takes FP32-level eigenpairs (errors ~1e-6 Ry) to eigenvalue errors
+// far below 1e-9 Ry; the remaining error is third order in the FP32 error.
+#include <cfloat>
 #include "refine.cuh"
 #include "gemm.cuh"
+#include "dfgemm.cuh"
 #include "sums.cuh"
 #include "nrltb.h"
 
 namespace nrltb {
 
+constexpr int REF_CMAX = 16;            // largest cluster solved exactly
+constexpr double REF_DELTA_REL = 5e-5;  // cluster threshold, fraction of the spectral span
+
 static inline size_t al256(size_t x) { return (x + 255) & ~size_t(255); }
 
-bool refine_available() { return false; }
+bool refine_available() { return true; }
 
 size_t refine_work_bytes(int n, int batch)
 {
     RefineWork w;
     refine_work_carve(w, nullptr, n, batch);
-    return (size_t)(uintptr_t)w.cl + sizeof(int) * (size_t)n * batch + 256;
+    return (size_t)(uintptr_t)w.cl + 256;
 }
 
 void refine_work_carve(RefineWork &w, void *base, int n, int batch)
 {
-    size_t off = 0, nn = (size_t)n * n * batch;
+    size_t off = 0, nn = (size_t)n * n * batch, nb = (size_t)n * batch;
     char *b = (char *)base;
     auto take = [&](size_t bytes) { void *p = b + off; off = al256(off + bytes); return p; };
     w.n = n; w.batch = batch;
@@ -27,19 +49,374 @@ void refine_work_carve(RefineWork &w, void *base, int n, int batch)
     w.YS = (double2 *)take(sizeof(double2) * nn);
     w.T = (double2 *)take(sizeof(double2) * nn);
     w.R = (double2 *)take(sizeof(double2) * nn);
-    w.U = (double2 *)take(sizeof(double2) * nn);
+    w.U = (double2 *)take(sizeof(double2) * nb * REF_CMAX);       // per column: coefficients on its cluster
     w.Ef = (float2 *)take(sizeof(float2) * nn);
     w.Xr = (float2 *)take(sizeof(float2) * nn);
     w.XE = (float2 *)take(sizeof(float2) * nn);
-    w.lam = (double *)take(sizeof(double) * (size_t)n * batch);
-    w.cl = (int *)take(sizeof(int) * (size_t)n * batch);
+    w.lam = (double *)take(sizeof(double) * nb * 3);               // l1 | R'_jj | delta
+    w.cl = (int *)take(sizeof(int) * nb * 4);                      // ord | pos0 | size | rank
     if (!base) w.cl = (int *)(uintptr_t)off;
+}
+
+// ---- 2. clusters: one CTA per matrix ----------------------------------------
+__global__ void __launch_bounds__(1024) k_ref_clusters(RefineWork w, int *status)
+{
+    __shared__ double red[32];
+    const int b = blockIdx.x, n = w.n, tid = threadIdx.x, nw = blockDim.x >> 5;
+    const double2 *T = w.T + (long)b * n * n, *R = w.R + (long)b * n * n;
+    double *l1 = w.lam + (long)b * n;
+    int *ord = w.cl + (long)b * n, *pos0 = w.cl + (long)n * w.batch + (long)b * n;
+    int *csz = w.cl + (long)2 * n * w.batch + (long)b * n;
+    double lo = 1e300, hi = -1e300;
+    for (int j = tid; j < n; j += blockDim.x) {
+        const double v = T[j + (long)j * n].x / R[j + (long)j * n].x;
+        l1[j] = v;
+        lo = fmin(lo, v);
+        hi = fmax(hi, v);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        lo = fmin(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+        hi = fmax(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+    }
+    if ((tid & 31) == 0) red[tid >> 5] = lo;
+    __syncthreads();
+    if (tid == 0) { double m = red[0]; for (int q = 1; q < nw; ++q) m = fmin(m, red[q]); red[0] = m; }
+    __syncthreads();
+    lo = red[0];
+    __syncthreads();
+    if ((tid & 31) == 0) red[tid >> 5] = hi;
+    __syncthreads();
+    if (tid == 0) { double m = red[0]; for (int q = 1; q < nw; ++q) m = fmax(m, red[q]); red[0] = m; }
+    __syncthreads();
+    hi = red[0];
+    // rank sort of the estimates (ties by index)
+    for (int j = tid; j < n; j += blockDim.x) {
+        const double v = l1[j];
+        int r = 0;
+        for (int q = 0; q < n; ++q) {
+            const double u = l1[q];
+            r += (u < v) || (u == v && q < j);
+        }
+        ord[r] = j;
+    }
+    __syncthreads();
+    if (tid == 0) {
+        // clusters: runs of sorted estimates closer than delta; a run longer than
+        // REF_CMAX is cut at its largest internal gap, recursively.  Cutting a
+        // gap below 1e-7 of the span would separate numerically coincident
+        // eigenvalues and is reported.
+        const double span = fmax(hi - lo, 1e-300);
+        const double delta = REF_DELTA_REL * span;
+        w.lam[(long)2 * n * w.batch + (long)b * n] = delta;
+        int forced = 0, p0 = 0;
+        for (int p = 1; p <= n; ++p) {
+            if (p < n && l1[ord[p]] - l1[ord[p - 1]] < delta) continue;
+            // run [p0, p): split until every piece fits
+            int stk[64][2], sp = 0;
+            stk[sp][0] = p0; stk[sp][1] = p; ++sp;
+            while (sp > 0) {
+                --sp;
+                const int a = stk[sp][0], e = stk[sp][1];
+                if (e - a <= REF_CMAX || sp >= 62) {
+                    for (int q = a; q < e; ++q) { pos0[ord[q]] = a; csz[ord[q]] = e - a; }
+                    if (e - a > REF_CMAX) forced = 1;
+                    continue;
+                }
+                int cut = a + 1;
+                double best = -1.0;
+                for (int q = a + 1; q < e; ++q) {
+                    const double g = l1[ord[q]] - l1[ord[q - 1]];
+                    if (g > best) { best = g; cut = q; }
+                }
+                if (best < 1e-7 * span) forced = 1;
+                stk[sp][0] = a; stk[sp][1] = cut; ++sp;
+                stk[sp][0] = cut; stk[sp][1] = e; ++sp;
+            }
+            p0 = p;
+        }
+        if (forced) status[b] = NRLTB_K_NOT_CONVERGED;
+    }
+}
+
+// ---- 2b. Rayleigh-Ritz inside each cluster: one warp per cluster ------------
+// Column j's rotation is stored as w.U[j*CMAX + a]: its coefficient on the
+// cluster's a-th member (sorted position pos0 + a).
+__global__ void __launch_bounds__(32) k_ref_rr(RefineWork w)
+{
+    __shared__ double2 A[REF_CMAX][REF_CMAX + 1];   // A[col][row]
+    __shared__ double2 Bm[REF_CMAX][REF_CMAX + 1];
+    __shared__ double2 Vv[REF_CMAX][REF_CMAX + 1];
+    const int b = blockIdx.y, p = blockIdx.x, n = w.n, lane = threadIdx.x;
+    const int *ord = w.cl + (long)b * n, *pos0 = w.cl + (long)n * w.batch + (long)b * n;
+    const int *csz = w.cl + (long)2 * n * w.batch + (long)b * n;
+    const int j0 = ord[p];
+    if (pos0[j0] != p) return;                       // not the first member of its cluster
+    const int c = csz[j0];
+    double2 *U = w.U + (long)b * n * REF_CMAX;
+    if (c == 1) {
+        if (lane == 0) U[(long)j0 * REF_CMAX] = make_double2(1.0, 0.0);
+        return;
+    }
+    const double2 *T = w.T + (long)b * n * n, *R = w.R + (long)b * n * n;
+    for (int e = lane; e < c * c; e += 32) {
+        const int r = e % c, q = e / c;
+        const int gr = ord[p + r], gq = ord[p + q];
+        A[q][r] = T[gr + (long)gq * n];
+        Bm[q][r] = R[gr + (long)gq * n];
+    }
+    __syncwarp();
+    if (lane == 0) {
+        // Cholesky Bm = L L^H (lower, in place; Bm[q][r] = element (r, q))
+        for (int k = 0; k < c; ++k) {
+            double piv = Bm[k][k].x;
+            for (int q = 0; q < k; ++q) piv -= Bm[q][k].x * Bm[q][k].x + Bm[q][k].y * Bm[q][k].y;
+            piv = sqrt(fmax(piv, 1e-300));
+            Bm[k][k] = make_double2(piv, 0.0);
+            for (int r = k + 1; r < c; ++r) {
+                double2 s = Bm[k][r];
+                for (int q = 0; q < k; ++q) s = csub(s, cmul(Bm[q][r], cconj(Bm[q][k])));
+                Bm[k][r] = cscale(s, 1.0 / piv);
+            }
+        }
+        // A <- L^{-1} A (columns), then A <- A L^{-H} (rows)
+        for (int q = 0; q < c; ++q)
+            for (int r = 0; r < c; ++r) {
+                double2 s = A[q][r];
+                for (int t = 0; t < r; ++t) s = csub(s, cmul(Bm[t][r], A[q][t]));
+                A[q][r] = cscale(s, 1.0 / Bm[r][r].x);
+            }
+        for (int r = 0; r < c; ++r)
+            for (int q = 0; q < c; ++q) {
+                double2 s = A[q][r];
+                for (int t = 0; t < q; ++t) s = csub(s, cmul(A[t][r], cconj(Bm[t][q])));
+                A[q][r] = cscale(s, 1.0 / Bm[q][q].x);
+            }
+        for (int q = 0; q < c; ++q)
+            for (int r = 0; r < c; ++r) Vv[q][r] = make_double2(r == q ? 1.0 : 0.0, 0.0);
+    }
+    __syncwarp();
+    // cyclic complex Jacobi on the Hermitian A, accumulating V
+    for (int sweep = 0; sweep < 30; ++sweep) {
+        double off = 0, dsum = 0;
+        for (int e = lane; e < c * c; e += 32) {
+            const int r = e % c, q = e / c;
+            if (r != q) off += A[q][r].x * A[q][r].x + A[q][r].y * A[q][r].y;
+            else dsum += A[q][r].x * A[q][r].x;
+        }
+        off = warp_sum(off);
+        dsum = warp_sum(dsum);
+        if (!(off > 1e-32 * dsum)) break;
+        for (int pp = 0; pp < c - 1; ++pp)
+            for (int qq = pp + 1; qq < c; ++qq) {
+                __syncwarp();
+                const double2 g = A[qq][pp];            // element (pp, qq)
+                const double ag = sqrt(g.x * g.x + g.y * g.y);
+                if (!(ag > 1e-300)) continue;
+                const double app = A[pp][pp].x, aqq = A[qq][qq].x;
+                const double tau = (aqq - app) / (2.0 * ag);
+                const double t = (tau >= 0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
+                const double cs = 1.0 / sqrt(1.0 + t * t), sn = t * cs;
+                // J = diag(1, e^{-i phi}) [[cs, sn], [-sn, cs]], g = |g| e^{i phi}
+                const double2 phc = make_double2(g.x / ag, -g.y / ag), ph = cconj(phc);
+                __syncwarp();
+                for (int r = lane; r < c; r += 32) {     // A J and V J (columns pp, qq)
+                    const double2 ap = A[pp][r], aq = cmul(A[qq][r], phc);
+                    A[pp][r] = csub(cscale(ap, cs), cscale(aq, sn));
+                    A[qq][r] = cadd(cscale(ap, sn), cscale(aq, cs));
+                    const double2 vp = Vv[pp][r], vq = cmul(Vv[qq][r], phc);
+                    Vv[pp][r] = csub(cscale(vp, cs), cscale(vq, sn));
+                    Vv[qq][r] = cadd(cscale(vp, sn), cscale(vq, cs));
+                }
+                __syncwarp();
+                for (int q = lane; q < c; q += 32) {     // J^H A (rows pp, qq)
+                    const double2 ap = A[q][pp], aq = cmul(A[q][qq], ph);
+                    A[q][pp] = csub(cscale(ap, cs), cscale(aq, sn));
+                    A[q][qq] = cadd(cscale(ap, sn), cscale(aq, cs));
+                }
+                __syncwarp();
+                if (lane == 0) {
+                    A[qq][pp] = make_double2(0, 0);
+                    A[pp][qq] = make_double2(0, 0);
+                    A[pp][pp].y = 0;
+                    A[qq][qq].y = 0;
+                }
+            }
+        __syncwarp();
+    }
+    __syncwarp();
+    // eigenvectors of the pencil: x = L^{-H} y
+    if (lane == 0) {
+        for (int q = 0; q < c; ++q)
+            for (int r = c - 1; r >= 0; --r) {
+                double2 s = Vv[q][r];
+                for (int t = r + 1; t < c; ++t) s = csub(s, cmul(cconj(Bm[r][t]), Vv[q][t]));
+                Vv[q][r] = cscale(s, 1.0 / Bm[r][r].x);
+            }
+    }
+    __syncwarp();
+    for (int e = lane; e < c * c; e += 32) {
+        const int a = e % c, q = e / c;
+        U[(long)ord[p + q] * REF_CMAX + a] = Vv[q][a];
+    }
+}
+
+// element (i, j) of U^H M U for the block-diagonal cluster rotation U
+__device__ __forceinline__ double2 rotated(const double2 *M, const double2 *U, const int *ord, const int *pos0,
+                                           const int *csz, int n, int i, int j)
+{
+    const int pi = pos0[i], ci = csz[i], pj = pos0[j], cj = csz[j];
+    if (ci == 1 && cj == 1) return M[i + (long)j * n];
+    double2 s = make_double2(0, 0);
+    for (int a = 0; a < ci; ++a) {
+        const int ga = (ci == 1) ? i : ord[pi + a];
+        const double2 ua = (ci == 1) ? make_double2(1, 0) : cconj(U[(long)i * REF_CMAX + a]);
+        double2 t = make_double2(0, 0);
+        for (int bb = 0; bb < cj; ++bb) {
+            const int gb = (cj == 1) ? j : ord[pj + bb];
+            const double2 ub = (cj == 1) ? make_double2(1, 0) : U[(long)j * REF_CMAX + bb];
+            t = cadd(t, cmul(M[ga + (long)gb * n], ub));
+        }
+        s = cadd(s, cmul(ua, t));
+    }
+    return s;
+}
+
+#define REF_VIEWS                                                              \
+    const int *ord = w.cl + (long)b * n, *pos0 = w.cl + (long)n * w.batch + (long)b * n; \
+    const int *csz = w.cl + (long)2 * n * w.batch + (long)b * n;               \
+    const double2 *U = w.U + (long)b * n * REF_CMAX;
+
+// 3a. l_j = T'_jj / R'_jj (thread per j)
+__global__ void k_ref_lambda(RefineWork w)
+{
+    const int b = blockIdx.y, n = w.n;
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    const long mo = (long)b * n * n;
+    REF_VIEWS
+    const double t = rotated(w.T + mo, U, ord, pos0, csz, n, j, j).x;
+    const double r = rotated(w.R + mo, U, ord, pos0, csz, n, j, j).x;
+    w.lam[(long)b * n + j] = t / r;
+    w.lam[(long)n * w.batch + (long)b * n + j] = r;
+}
+
+// 3b. E column j and the second-order eigenvalue term (warp per column)
+__global__ void k_ref_update(RefineWork w, double *l2out)
+{
+    const int warp = (int)((blockIdx.x * (long)blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+    const int n = w.n;
+    if (warp >= n * w.batch) return;
+    const int b = warp / n, j = warp % n;
+    const long mo = (long)b * n * n;
+    REF_VIEWS
+    const double *l1 = w.lam + (long)b * n;
+    const double lj = l1[j], rjj = w.lam[(long)n * w.batch + (long)b * n + j];
+    double corr = 0;
+    float2 *E = w.Ef + mo + (long)j * n;
+    for (int i = lane; i < n; i += 32) {
+        float2 e;
+        if (i == j) {
+            e = make_float2((float)(0.5 * (1.0 - rjj)), 0.f);
+        } else if (pos0[i] == pos0[j]) {
+            e = make_float2(0.f, 0.f);
+        } else {
+            const double2 t = rotated(w.T + mo, U, ord, pos0, csz, n, i, j);
+            const double2 r = rotated(w.R + mo, U, ord, pos0, csz, n, i, j);
+            const double2 num = make_double2(t.x - lj * r.x, t.y - lj * r.y);
+            const double den = lj - l1[i];
+            e = make_float2((float)(num.x / den), (float)(num.y / den));
+            corr += (num.x * num.x + num.y * num.y) / den;
+        }
+        E[i] = e;
+    }
+    corr = warp_sum(corr);
+    if (lane == 0) l2out[(long)b * n + j] = lj + corr;
+}
+
+// 4a. X U in FP64 (into YH) and FP32 (into Xr); thread per element
+__global__ void k_ref_rotate(RefineWork w, const float2 *X)
+{
+    const int n = w.n;
+    const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    const long nn = (long)n * n;
+    if (t >= nn * w.batch) return;
+    const int b = (int)(t / nn);
+    const long e = t - b * nn;
+    const int r = (int)(e % n), j = (int)(e / n);
+    REF_VIEWS
+    const float2 *Xb = X + b * nn;
+    double2 v;
+    if (csz[j] == 1) {
+        const float2 x = Xb[r + (long)j * n];
+        v = make_double2(x.x, x.y);
+    } else {
+        v = make_double2(0, 0);
+        for (int a = 0; a < csz[j]; ++a) {
+            const float2 x = Xb[r + (long)ord[pos0[j] + a] * n];
+            v = cadd(v, cmul(make_double2(x.x, x.y), U[(long)j * REF_CMAX + a]));
+        }
+    }
+    (void)ord;
+    w.YH[t] = v;
+    w.Xr[t] = make_float2((float)v.x, (float)v.y);
+}
+
+// 4b. ascending order of the refined eigenvalues
+__global__ void k_ref_rank(RefineWork w, const double *l2, double *eig)
+{
+    const int b = blockIdx.y, n = w.n;
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    const double *L = l2 + (long)b * n;
+    const double v = L[j];
+    int r = 0;
+    for (int q = 0; q < n; ++q) {
+        const double u = L[q];
+        r += (u < v) || (u == v && q < j);
+    }
+    w.cl[(long)3 * n * w.batch + (long)b * n + j] = r;
+    eig[(long)b * n + r] = v;
+}
+
+// 4c. Z[:, rank(j)] = (X U)[:, j] + (X U E)[:, j]
+__global__ void k_ref_finish(RefineWork w, double2 *Z)
+{
+    const int n = w.n;
+    const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    const long nn = (long)n * n;
+    if (t >= nn * w.batch) return;
+    const int b = (int)(t / nn);
+    const long e = t - b * nn;
+    const int r = (int)(e % n), j = (int)(e / n);
+    const int dst = w.cl[(long)3 * n * w.batch + (long)b * n + j];
+    const double2 x = w.YH[t];
+    const float2 d = w.XE[t];
+    Z[b * nn + r + (long)dst * n] = make_double2(x.x + (double)d.x, x.y + (double)d.y);
 }
 
 void refine_eigen(cudaStream_t s, RefineWork &w, const double2 *H, const double2 *S, const float2 *X,
                   double *eig, double2 *Z, int *status)
 {
-    (void)s; (void)w; (void)H; (void)S; (void)X; (void)eig; (void)Z; (void)status;
+    const int n = w.n, B = w.batch;
+    const long nn = (long)n * n;
+    // 1. T = X^H (H X), R = X^H (S X)
+    dfgemm<double2, float2>(s, n, n, n, B, H, n, nn, 0, X, n, nn, 0, w.YH, n, nn);
+    dfgemm<double2, float2>(s, n, n, n, B, S, n, nn, 0, X, n, nn, 0, w.YS, n, nn);
+    dfgemm<float2, double2>(s, n, n, n, B, X, n, nn, 1, w.YH, n, nn, 0, w.T, n, nn);
+    dfgemm<float2, double2>(s, n, n, n, B, X, n, nn, 1, w.YS, n, nn, 0, w.R, n, nn);
+    // 2. clusters and their Rayleigh-Ritz rotations
+    NRLTB_LAUNCH(k_ref_clusters, B, 1024, 0, s, w, status);
+    NRLTB_LAUNCH(k_ref_rr, dim3(n, B), 32, 0, s, w);
+    // 3. eigenvalue estimates, correction matrix and second-order eigenvalues
+    NRLTB_LAUNCH(k_ref_lambda, dim3(cdiv(n, 128), B), 128, 0, s, w);
+    double *l2 = (double *)w.YS;   // YS is free once R is formed
+    NRLTB_LAUNCH(k_ref_update, cdiv((long)n * B * 32, 256), 256, 0, s, w, l2);
+    // 4. Z = X U + (X U) E, reordered
+    NRLTB_LAUNCH(k_ref_rotate, cdiv(nn * B, 256), 256, 0, s, w, X);
+    const float2 onef = make_float2(1.f, 0.f), zerof = make_float2(0.f, 0.f);
+    zgemm<float>(s, n, n, n, B, onef, w.Xr, n, nn, 0, w.Ef, n, nn, 0, zerof, w.XE, n, nn);
+    NRLTB_LAUNCH(k_ref_rank, dim3(cdiv(n, 128), B), 128, 0, s, w, l2, eig);
+    if (Z) NRLTB_LAUNCH(k_ref_finish, cdiv(nn * B, 256), 256, 0, s, w, Z);
 }
 
 size_t hf_scratch_bytes(int n, int nkc) { return 2 * sizeof(double2) * (size_t)n * n * nkc + 512; }
@@ -47,14 +424,19 @@ size_t hf_scratch_bytes(int n, int nkc) { return 2 * sizeof(double2) * (size_t)n
 int run_hf(cudaStream_t s, int n, int nkc, int prec, const double2 *dH, const double2 *dS, const double2 *Z,
            const double *eig, double *deig, void *scratch, void *unused)
 {
-    (void)unused; (void)prec;
+    (void)unused;
     const long nn = (long)n * n;
     double2 *P = (double2 *)scratch;
     double2 *Q = (double2 *)((char *)scratch + al256(sizeof(double2) * nn * nkc));
-    const double2 one = make_double2(1, 0), zero = make_double2(0, 0);
-    // P = triu(dH) Z, Q = triu(dS) Z
-    zgemm<double>(s, n, n, n, nkc, one, dH, n, nn, 0, Z, n, nn, 0, zero, P, n, nn, 2, 0, 0);
-    zgemm<double>(s, n, n, n, nkc, one, dS, n, nn, 0, Z, n, nn, 0, zero, Q, n, nn, 2, 0, 0);
+    if (prec == NRLTB_PREC_FP64) {
+        const double2 one = make_double2(1, 0), zero = make_double2(0, 0);
+        // P = triu(dH) Z, Q = triu(dS) Z
+        zgemm<double>(s, n, n, n, nkc, one, dH, n, nn, 0, Z, n, nn, 0, zero, P, n, nn, 2, 0, 0);
+        zgemm<double>(s, n, n, n, nkc, one, dS, n, nn, 0, Z, n, nn, 0, zero, Q, n, nn, 2, 0, 0);
+    } else {
+        dfgemm<double2, double2>(s, n, n, n, nkc, dH, n, nn, 0, Z, n, nn, 0, P, n, nn, 0.0, 2, 0);
+        dfgemm<double2, double2>(s, n, n, n, nkc, dS, n, nn, 0, Z, n, nn, 0, Q, n, nn, 0.0, 2, 0);
+    }
     launch_hf_dots(s, Z, P, Q, dH, dS, eig, deig, n, nkc);
     return cudaGetLastError() == cudaSuccess ? NRLTB_OK : NRLTB_E_CUDA;
 }

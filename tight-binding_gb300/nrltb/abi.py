@@ -100,6 +100,9 @@ GPU_SYMBOLS = [
     ("nrltb_diag", C.c_int, [_vp, C.c_int, C.c_int, _dp, _dp, C.c_int, _dp, _dp, _ip]),
     ("nrltb_fermi", C.c_int, [_vp, C.c_int, C.c_int, _dp, _dp, C.c_double, C.c_double,
                               C.c_double, _dp]),
+    # measurement hooks (include/nrltb_bench.h)
+    ("nrltb_bench_peak", C.c_int, [_vp, C.c_int, _dp]),
+    ("nrltb_bench_zgemm", C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_int, _dp, _dp]),
 ]
 
 HOST_SYMBOLS = [
