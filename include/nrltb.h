@@ -172,6 +172,34 @@ int nrltb_diag(nrltb_ctx *ctx, int nv, int nk, const double *hmat, const double 
 int nrltb_fermi(nrltb_ctx *ctx, int nv, int nk, const double *eig, const double *w,
                 double tkb, double zfill, double tol, double *efermi);
 
+/* ---- neighbour list without allocation ----------------------------------
+ * No counterpart in the reference.  nrltb_search2 above sizes its buffers with
+ * cudaMalloc; this variant is for callers that cannot allocate device memory
+ * at call time -- codes whose own allocator already owns the GPU (a framework's
+ * caching pool, an arena reserved at start-up), or whose pipeline must not be
+ * stalled by the device-wide synchronisation a cudaMalloc/cudaFree can cause.
+ * It performs no allocation: positions, kinds and the pair arrays are the
+ * caller's device buffers (pair arrays of `capacity` entries, laid out as in
+ * nrltb_pairs), and its scratch is a fixed device array of
+ * NRLTB_NOALLOC_SCRATCH_BYTES that every GPU which loads the library keeps
+ * until the process exits.  Search boxes with more than
+ * NRLTB_NOALLOC_MAX_CANDIDATES candidate images (natoms^2 (2nd1+1)(2nd2+1)
+ * (2nd3+1)) are rejected with NRLTB_E_CAPACITY.  The first call on a device
+ * looks the scratch array up on that device; make that first call before any
+ * stream capture.  All calls share the one array, so calls that overlap on the
+ * GPU (different streams or host threads) race; serialise them.  The call runs
+ * on `stream` (NULL = legacy default stream) and returns when the results are
+ * written; *npairs gets the full pair count even when it exceeds capacity
+ * (then NRLTB_E_CAPACITY is returned and only the first `capacity` pairs
+ * are written). */
+#define NRLTB_NOALLOC_MAX_CANDIDATES 16777216L
+#define NRLTB_NOALLOC_SCRATCH_BYTES 16844288UL
+int nrltb_search2_noalloc(int device, void *stream, int natoms, const int *d_kkind, const double *d_posn,
+                          const double plv[3][3], const int nd[3], int kinds, const double *dnn,
+                          const double *screenl, int kneigh_in, int capacity, double *d_tt, int *d_dlv,
+                          double *d_dist, double *d_screen, double *d_dscrn, int *d_jkind, int *d_jatm,
+                          int *npairs, int *kneigh_out, double *dismin);
+
 #ifdef __cplusplus
 }
 #endif

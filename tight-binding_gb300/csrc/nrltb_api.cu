@@ -34,6 +34,9 @@ static void set_err(const char *fmt, ...)
     va_end(ap);
 }
 
+// error text for entry points defined in other files (nrltb_last_error)
+void nrltb_internal_set_error(const char *msg) { snprintf(g_err, sizeof g_err, "%s", msg); }
+
 #define CK(call)                                                                      \
     do {                                                                              \
         cudaError_t e_ = (call);                                                      \

@@ -100,6 +100,8 @@ GPU_SYMBOLS = [
     ("nrltb_diag", C.c_int, [_vp, C.c_int, C.c_int, _dp, _dp, C.c_int, _dp, _dp, _ip]),
     ("nrltb_fermi", C.c_int, [_vp, C.c_int, C.c_int, _dp, _dp, C.c_double, C.c_double,
                               C.c_double, _dp]),
+    ("nrltb_search2_noalloc", C.c_int, [C.c_int, _vp, C.c_int, _vp, _vp, _dp, _ip, C.c_int, _dp, _dp,
+                                        C.c_int, C.c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _ip, _ip, _dp]),
     # measurement hooks (include/nrltb_bench.h)
     ("nrltb_bench_peak", C.c_int, [_vp, C.c_int, _dp]),
     ("nrltb_bench_zgemm", C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_int, _dp, _dp]),
