@@ -30,6 +30,12 @@ constexpr double REF_DELTA_REL = 5e-5;  // cluster threshold, fraction of the sp
 
 static inline size_t al256(size_t x) { return (x + 255) & ~size_t(255); }
 
+// element (i, j) of a Hermitian matrix stored in its upper triangle
+__device__ __forceinline__ double2 herm_up(const double2 *M, int n, int i, int j)
+{
+    return (i <= j) ? M[i + (long)j * n] : cconj(M[j + (long)i * n]);
+}
+
 bool refine_available() { return true; }
 
 size_t refine_work_bytes(int n, int batch)
@@ -161,8 +167,8 @@ __global__ void __launch_bounds__(32) k_ref_rr(RefineWork w)
     for (int e = lane; e < c * c; e += 32) {
         const int r = e % c, q = e / c;
         const int gr = ord[p + r], gq = ord[p + q];
-        A[q][r] = T[gr + (long)gq * n];
-        Bm[q][r] = R[gr + (long)gq * n];
+        A[q][r] = herm_up(T, n, gr, gq);
+        Bm[q][r] = herm_up(R, n, gr, gq);
     }
     __syncwarp();
     if (lane == 0) {
@@ -260,12 +266,19 @@ __global__ void __launch_bounds__(32) k_ref_rr(RefineWork w)
     }
 }
 
+// element (i, j) of a Hermitian matrix of which only the upper triangle (and
+// whole diagonal tiles) is stored
+__device__ __forceinline__ double2 herm(const double2 *M, int n, int i, int j)
+{
+    return (i <= j) ? M[i + (long)j * n] : cconj(M[j + (long)i * n]);
+}
+
 // element (i, j) of U^H M U for the block-diagonal cluster rotation U
 __device__ __forceinline__ double2 rotated(const double2 *M, const double2 *U, const int *ord, const int *pos0,
                                            const int *csz, int n, int i, int j)
 {
     const int pi = pos0[i], ci = csz[i], pj = pos0[j], cj = csz[j];
-    if (ci == 1 && cj == 1) return M[i + (long)j * n];
+    if (ci == 1 && cj == 1) return herm(M, n, i, j);
     double2 s = make_double2(0, 0);
     for (int a = 0; a < ci; ++a) {
         const int ga = (ci == 1) ? i : ord[pi + a];
@@ -274,7 +287,7 @@ __device__ __forceinline__ double2 rotated(const double2 *M, const double2 *U, c
         for (int bb = 0; bb < cj; ++bb) {
             const int gb = (cj == 1) ? j : ord[pj + bb];
             const double2 ub = (cj == 1) ? make_double2(1, 0) : U[(long)j * REF_CMAX + bb];
-            t = cadd(t, cmul(M[ga + (long)gb * n], ub));
+            t = cadd(t, cmul(herm(M, n, ga, gb), ub));
         }
         s = cadd(s, cmul(ua, t));
     }
@@ -402,8 +415,9 @@ void refine_eigen(cudaStream_t s, RefineWork &w, const double2 *H, const double2
     // 1. T = X^H (H X), R = X^H (S X)
     dfgemm<double2, float2>(s, n, n, n, B, H, n, nn, 0, X, n, nn, 0, w.YH, n, nn);
     dfgemm<double2, float2>(s, n, n, n, B, S, n, nn, 0, X, n, nn, 0, w.YS, n, nn);
-    dfgemm<float2, double2>(s, n, n, n, B, X, n, nn, 1, w.YH, n, nn, 0, w.T, n, nn);
-    dfgemm<float2, double2>(s, n, n, n, B, X, n, nn, 1, w.YS, n, nn, 0, w.R, n, nn);
+    // T and R are Hermitian: only the tiles touching the upper triangle are formed
+    dfgemm<float2, double2>(s, n, n, n, B, X, n, nn, 1, w.YH, n, nn, 0, w.T, n, nn, 0.0, 0, 2);
+    dfgemm<float2, double2>(s, n, n, n, B, X, n, nn, 1, w.YS, n, nn, 0, w.R, n, nn, 0.0, 0, 2);
     // 2. clusters and their Rayleigh-Ritz rotations
     NRLTB_LAUNCH(k_ref_clusters, B, 1024, 0, s, w, status);
     NRLTB_LAUNCH(k_ref_rr, dim3(n, B), 32, 0, s, w);
@@ -419,7 +433,47 @@ void refine_eigen(cudaStream_t s, RefineWork &w, const double2 *H, const double2
     if (Z) NRLTB_LAUNCH(k_ref_finish, cdiv(nn * B, 256), 256, 0, s, w, Z);
 }
 
-size_t hf_scratch_bytes(int n, int nkc) { return 2 * sizeof(double2) * (size_t)n * n * nkc + 512; }
+size_t hf_scratch_bytes(int n, int nkc)
+{
+    // FP64 form: P, Q (2 n^2 double2); mixed form: dH, dS, Z, P as float2 (4 n^2 float2)
+    return 2 * sizeof(double2) * (size_t)n * n * nkc + 512;
+}
+
+__global__ void k_to_f32(const double2 *src, float2 *dst, long count)
+{
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < count; i += (long)gridDim.x * blockDim.x) {
+        const double2 v = src[i];
+        dst[i] = make_float2((float)v.x, (float)v.y);
+    }
+}
+void launch_to_f32(cudaStream_t s, const double2 *src, float2 *dst, long count)
+{
+    NRLTB_LAUNCH(k_to_f32, 1184, 256, 0, s, src, dst, count);
+}
+
+// deig_n = Re(z_n^H P_n) - e_n Re(z_n^H Q_n), FP32 inputs, FP64 sums; warp per column
+__global__ void k_hf_dots32(const float2 *Z, const float2 *P, const float2 *Q, const double *eig, double *deig,
+                            int n, int batch)
+{
+    const int warp = (int)((blockIdx.x * (long)blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+    if (warp >= n * batch) return;
+    const int b = warp / n, col = warp % n;
+    const long off = (long)b * n * n + (long)col * n;
+    double sp = 0, sq = 0;
+    for (int i = lane; i < n; i += 32) {
+        const float2 z = Z[off + i], p = P[off + i], q = Q[off + i];
+        sp += (double)z.x * p.x + (double)z.y * p.y;
+        sq += (double)z.x * q.x + (double)z.y * q.y;
+    }
+    sp = warp_sum(sp);
+    sq = warp_sum(sq);
+    if (lane == 0) deig[(long)b * n + col] = sp - eig[(long)b * n + col] * sq;
+}
+void launch_hf_dots32(cudaStream_t s, const float2 *Z, const float2 *P, const float2 *Q, const double *eig,
+                      double *deig, int n, int batch)
+{
+    NRLTB_LAUNCH(k_hf_dots32, cdiv((long)n * batch * 32, 256), 256, 0, s, Z, P, Q, eig, deig, n, batch);
+}
 
 int run_hf(cudaStream_t s, int n, int nkc, int prec, const double2 *dH, const double2 *dS, const double2 *Z,
            const double *eig, double *deig, void *scratch, void *unused)
@@ -433,11 +487,23 @@ int run_hf(cudaStream_t s, int n, int nkc, int prec, const double2 *dH, const do
         // P = triu(dH) Z, Q = triu(dS) Z
         zgemm<double>(s, n, n, n, nkc, one, dH, n, nn, 0, Z, n, nn, 0, zero, P, n, nn, 2, 0, 0);
         zgemm<double>(s, n, n, n, nkc, one, dS, n, nn, 0, Z, n, nn, 0, zero, Q, n, nn, 2, 0, 0);
+        launch_hf_dots(s, Z, P, Q, dH, dS, eig, deig, n, nkc);
     } else {
-        dfgemm<double2, double2>(s, n, n, n, nkc, dH, n, nn, 0, Z, n, nn, 0, P, n, nn, 0.0, 2, 0);
-        dfgemm<double2, double2>(s, n, n, n, nkc, dS, n, nn, 0, Z, n, nn, 0, Q, n, nn, 0.0, 2, 0);
+        // Mixed form: the products in FP32 (full, no triangle trick, so no
+        // cancellation against the diagonal); their error in P is ~1e-11
+        // Ry/bohr^3 per k, far below the 1e-3 kbar (6.8e-9) tolerance.  The
+        // scratch holds dH32 | dS32 | Z32 | P32 (4 n^2 float2 = 2 n^2 double2);
+        // dS Z overwrites dH32 once dH Z is formed.
+        float2 *h32 = (float2 *)scratch, *s32 = h32 + nn * nkc, *z32 = s32 + nn * nkc;
+        float2 *p32 = z32 + nn * nkc;
+        launch_to_f32(s, dH, h32, nn * nkc);
+        launch_to_f32(s, dS, s32, nn * nkc);
+        launch_to_f32(s, Z, z32, nn * nkc);
+        const float2 one = make_float2(1.f, 0.f), zero = make_float2(0.f, 0.f);
+        zgemm<float>(s, n, n, n, nkc, one, h32, n, nn, 0, z32, n, nn, 0, zero, p32, n, nn);
+        zgemm<float>(s, n, n, n, nkc, one, s32, n, nn, 0, z32, n, nn, 0, zero, h32, n, nn);   // dS Z over dH32
+        launch_hf_dots32(s, z32, p32, h32, eig, deig, n, nkc);
     }
-    launch_hf_dots(s, Z, P, Q, dH, dS, eig, deig, n, nkc);
     return cudaGetLastError() == cudaSuccess ? NRLTB_OK : NRLTB_E_CUDA;
 }
 
