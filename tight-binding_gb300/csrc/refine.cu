@@ -1,17 +1,21 @@
 // refine.cu -- mixed-precision form: FP64-accurate refinement of FP32 eigenpairs
 // of H x = lambda S x, and the Hellmann-Feynman products of both forms.
 //
-// Given FP32 eigenvectors X (S-orthonormal to FP32 accuracy) of FP64 H, S:
-//   1. T = X^H H X, R = X^H S X in double-float arithmetic (dfgemm.cuh).
-//   2. Clusters: eigenvalue estimates T_jj / R_jj closer than delta (a fraction
-//      of the spectral span) are grouped; each cluster's block (T_c, R_c) is
-//      solved exactly (Cholesky + complex Jacobi, FP64), giving a rotation U_c
+// Given FP32 eigenvectors X (S-orthonormal to FP32 accuracy) and eigenvalue
+// estimates l~ of FP64 H, S:
+//   1. Y_H = H X, Y_S = S X in double-float arithmetic (dfgemm.cuh), and the
+//      residuals r_j = Y_H[:, j] - l~_j Y_S[:, j] in FP64.  The residuals are
+//      small (~1e-6), so G = X^H r (G_ij = T_ij - l~_j R_ij with T = X^H H X,
+//      R = X^H S X) is accurate to ~1e-13 even as an FP32 GEMM; only the
+//      diagonals T_jj, R_jj and the cluster blocks below need FP64 dot products.
+//   2. Clusters: estimates T_jj / R_jj closer than delta (a fraction of the
+//      spectral span) are grouped; each cluster's block (T_c, R_c) is solved
+//      exactly (Cholesky + complex Jacobi, FP64), giving a rotation U_c
 //      (Rayleigh-Ritz inside the cluster).
-//   3. With T' = U^H T U, R' = U^H R U (U block diagonal), one Newton-type
-//      correction of the whole basis (Ogita-Aishima): for i, j in different
-//      clusters E_ij = (T'_ij - l_j R'_ij) / (l_j - l_i), E_jj = (1 - R'_jj)/2,
-//      and the eigenvalue with its second-order term
-//        l_j + sum_{i not in c(j)} |T'_ij - l_j R'_ij|^2 / (l_j - l_i).
+//   3. With G' = U^H G U (U block diagonal), one Newton-type correction of the
+//      whole basis (Ogita-Aishima): for i, j in different clusters
+//      E_ij = G'_ij / (l_j - l_i), E_jj = (1 - R'_jj) / 2, and the eigenvalue
+//      with its second-order term  l_j + sum_{i not in c(j)} |G'_ij|^2 / (l_j - l_i).
 //   4. Z = X U (I + E) in FP64 (X U in FP64, the small X U E in FP32), columns
 //      reordered by ascending eigenvalue.
 // One step takes FP32-level eigenpairs (errors ~1e-6 Ry) to eigenvalue errors
@@ -30,12 +34,6 @@ constexpr double REF_DELTA_REL = 5e-5;  // cluster threshold, fraction of the sp
 
 static inline size_t al256(size_t x) { return (x + 255) & ~size_t(255); }
 
-// element (i, j) of a Hermitian matrix stored in its upper triangle
-__device__ __forceinline__ double2 herm_up(const double2 *M, int n, int i, int j)
-{
-    return (i <= j) ? M[i + (long)j * n] : cconj(M[j + (long)i * n]);
-}
-
 bool refine_available() { return true; }
 
 size_t refine_work_bytes(int n, int batch)
@@ -51,17 +49,53 @@ void refine_work_carve(RefineWork &w, void *base, int n, int batch)
     char *b = (char *)base;
     auto take = [&](size_t bytes) { void *p = b + off; off = al256(off + bytes); return p; };
     w.n = n; w.batch = batch;
-    w.YH = (double2 *)take(sizeof(double2) * nn);
-    w.YS = (double2 *)take(sizeof(double2) * nn);
-    w.T = (double2 *)take(sizeof(double2) * nn);
-    w.R = (double2 *)take(sizeof(double2) * nn);
+    w.YH = (double2 *)take(sizeof(double2) * nn);                  // H X, later X U in FP64
+    w.YS = (double2 *)take(sizeof(double2) * nn);                  // S X, later the corrected eigenvalues
+    w.G = (float2 *)take(sizeof(float2) * nn);                     // X^H r
     w.U = (double2 *)take(sizeof(double2) * nb * REF_CMAX);       // per column: coefficients on its cluster
-    w.Ef = (float2 *)take(sizeof(float2) * nn);
+    w.Ef = (float2 *)take(sizeof(float2) * nn);                    // residuals r, later E
     w.Xr = (float2 *)take(sizeof(float2) * nn);
     w.XE = (float2 *)take(sizeof(float2) * nn);
-    w.lam = (double *)take(sizeof(double) * nb * 3);               // l1 | R'_jj | delta
+    w.lam = (double *)take(sizeof(double) * nb * 4);               // l | R'_jj | T_jj | R_jj
     w.cl = (int *)take(sizeof(int) * nb * 4);                      // ord | pos0 | size | rank
     if (!base) w.cl = (int *)(uintptr_t)off;
+}
+
+// ---- 1. residuals and accurate diagonals -----------------------------------
+__global__ void k_ref_resid(RefineWork w, const double *lt)
+{
+    const int n = w.n;
+    const long nn = (long)n * n;
+    const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (t >= nn * w.batch) return;
+    const int b = (int)(t / nn), j = (int)((t - b * nn) / n);
+    const double l = lt[(long)b * n + j];
+    const double2 yh = w.YH[t], ys = w.YS[t];
+    w.Ef[t] = make_float2((float)(yh.x - l * ys.x), (float)(yh.y - l * ys.y));
+}
+
+// T_jj = x_j^H (H x_j), R_jj = x_j^H (S x_j) in FP64; warp per column
+__global__ void k_ref_diag(RefineWork w, const float2 *X)
+{
+    const int warp = (int)((blockIdx.x * (long)blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+    const int n = w.n;
+    if (warp >= n * w.batch) return;
+    const int b = warp / n, j = warp % n;
+    const long off = (long)b * n * n + (long)j * n;
+    double t = 0, r = 0;
+    for (int i = lane; i < n; i += 32) {
+        const float2 x = X[off + i];
+        const double2 yh = w.YH[off + i], ys = w.YS[off + i];
+        t += (double)x.x * yh.x + (double)x.y * yh.y;
+        r += (double)x.x * ys.x + (double)x.y * ys.y;
+    }
+    t = warp_sum(t);
+    r = warp_sum(r);
+    if (lane == 0) {
+        const long nb = (long)n * w.batch;
+        w.lam[2 * nb + (long)b * n + j] = t;
+        w.lam[3 * nb + (long)b * n + j] = r;
+    }
 }
 
 // ---- 2. clusters: one CTA per matrix ----------------------------------------
@@ -69,14 +103,16 @@ __global__ void __launch_bounds__(1024) k_ref_clusters(RefineWork w, int *status
 {
     __shared__ double red[32];
     const int b = blockIdx.x, n = w.n, tid = threadIdx.x, nw = blockDim.x >> 5;
-    const double2 *T = w.T + (long)b * n * n, *R = w.R + (long)b * n * n;
-    double *l1 = w.lam + (long)b * n;
-    int *ord = w.cl + (long)b * n, *pos0 = w.cl + (long)n * w.batch + (long)b * n;
-    int *csz = w.cl + (long)2 * n * w.batch + (long)b * n;
+    const long nb = (long)n * w.batch;
+    double *l1 = w.lam + (long)b * n, *r1 = w.lam + nb + (long)b * n;
+    const double *tjj = w.lam + 2 * nb + (long)b * n, *rjj = w.lam + 3 * nb + (long)b * n;
+    int *ord = w.cl + (long)b * n, *pos0 = w.cl + nb + (long)b * n;
+    int *csz = w.cl + 2 * nb + (long)b * n;
     double lo = 1e300, hi = -1e300;
     for (int j = tid; j < n; j += blockDim.x) {
-        const double v = T[j + (long)j * n].x / R[j + (long)j * n].x;
+        const double v = tjj[j] / rjj[j];
         l1[j] = v;
+        r1[j] = rjj[j];
         lo = fmin(lo, v);
         hi = fmax(hi, v);
     }
@@ -113,11 +149,9 @@ __global__ void __launch_bounds__(1024) k_ref_clusters(RefineWork w, int *status
         // eigenvalues and is reported.
         const double span = fmax(hi - lo, 1e-300);
         const double delta = REF_DELTA_REL * span;
-        w.lam[(long)2 * n * w.batch + (long)b * n] = delta;
         int forced = 0, p0 = 0;
         for (int p = 1; p <= n; ++p) {
             if (p < n && l1[ord[p]] - l1[ord[p - 1]] < delta) continue;
-            // run [p0, p): split until every piece fits
             int stk[64][2], sp = 0;
             stk[sp][0] = p0; stk[sp][1] = p; ++sp;
             while (sp > 0) {
@@ -145,16 +179,19 @@ __global__ void __launch_bounds__(1024) k_ref_clusters(RefineWork w, int *status
 }
 
 // ---- 2b. Rayleigh-Ritz inside each cluster: one warp per cluster ------------
-// Column j's rotation is stored as w.U[j*CMAX + a]: its coefficient on the
-// cluster's a-th member (sorted position pos0 + a).
-__global__ void __launch_bounds__(32) k_ref_rr(RefineWork w)
+// The cluster block T_ab = x_a^H (H x_b), R_ab = x_a^H (S x_b) is formed with
+// FP64 dot products.  Column j's rotation is stored as w.U[j*CMAX + a], its
+// coefficient on the cluster's a-th member (sorted position pos0 + a); the
+// members' eigenvalues replace the estimates and their R'_jj becomes 1.
+__global__ void __launch_bounds__(32) k_ref_rr(RefineWork w, const float2 *X)
 {
     __shared__ double2 A[REF_CMAX][REF_CMAX + 1];   // A[col][row]
     __shared__ double2 Bm[REF_CMAX][REF_CMAX + 1];
     __shared__ double2 Vv[REF_CMAX][REF_CMAX + 1];
     const int b = blockIdx.y, p = blockIdx.x, n = w.n, lane = threadIdx.x;
-    const int *ord = w.cl + (long)b * n, *pos0 = w.cl + (long)n * w.batch + (long)b * n;
-    const int *csz = w.cl + (long)2 * n * w.batch + (long)b * n;
+    const long nb = (long)n * w.batch;
+    const int *ord = w.cl + (long)b * n, *pos0 = w.cl + nb + (long)b * n;
+    const int *csz = w.cl + 2 * nb + (long)b * n;
     const int j0 = ord[p];
     if (pos0[j0] != p) return;                       // not the first member of its cluster
     const int c = csz[j0];
@@ -163,15 +200,30 @@ __global__ void __launch_bounds__(32) k_ref_rr(RefineWork w)
         if (lane == 0) U[(long)j0 * REF_CMAX] = make_double2(1.0, 0.0);
         return;
     }
-    const double2 *T = w.T + (long)b * n * n, *R = w.R + (long)b * n * n;
-    for (int e = lane; e < c * c; e += 32) {
-        const int r = e % c, q = e / c;
-        const int gr = ord[p + r], gq = ord[p + q];
-        A[q][r] = herm_up(T, n, gr, gq);
-        Bm[q][r] = herm_up(R, n, gr, gq);
-    }
+    const long mo = (long)b * n * n;
+    for (int q = 0; q < c; ++q)
+        for (int r = 0; r < c; ++r) {
+            const int gr = ord[p + r], gq = ord[p + q];
+            double2 t = make_double2(0, 0), u = make_double2(0, 0);
+            for (int i = lane; i < n; i += 32) {
+                const float2 xf = X[mo + (long)gr * n + i];
+                const double2 x = make_double2(xf.x, xf.y);
+                t = cadd(t, cmulc(x, w.YH[mo + (long)gq * n + i]));
+                u = cadd(u, cmulc(x, w.YS[mo + (long)gq * n + i]));
+            }
+            t.x = warp_sum(t.x); t.y = warp_sum(t.y);
+            u.x = warp_sum(u.x); u.y = warp_sum(u.y);
+            if (lane == 0) { A[q][r] = t; Bm[q][r] = u; }
+        }
     __syncwarp();
     if (lane == 0) {
+        // Hermitian by construction up to rounding: symmetrise
+        for (int q = 0; q < c; ++q)
+            for (int r = q; r < c; ++r) {
+                const double2 a = cscale(cadd(A[q][r], cconj(A[r][q])), 0.5), bm = cscale(cadd(Bm[q][r], cconj(Bm[r][q])), 0.5);
+                A[q][r] = a; A[r][q] = cconj(a);
+                Bm[q][r] = bm; Bm[r][q] = cconj(bm);
+            }
         // Cholesky Bm = L L^H (lower, in place; Bm[q][r] = element (r, q))
         for (int k = 0; k < c; ++k) {
             double piv = Bm[k][k].x;
@@ -179,23 +231,23 @@ __global__ void __launch_bounds__(32) k_ref_rr(RefineWork w)
             piv = sqrt(fmax(piv, 1e-300));
             Bm[k][k] = make_double2(piv, 0.0);
             for (int r = k + 1; r < c; ++r) {
-                double2 s = Bm[k][r];
-                for (int q = 0; q < k; ++q) s = csub(s, cmul(Bm[q][r], cconj(Bm[q][k])));
-                Bm[k][r] = cscale(s, 1.0 / piv);
+                double2 s2 = Bm[k][r];
+                for (int q = 0; q < k; ++q) s2 = csub(s2, cmul(Bm[q][r], cconj(Bm[q][k])));
+                Bm[k][r] = cscale(s2, 1.0 / piv);
             }
         }
         // A <- L^{-1} A (columns), then A <- A L^{-H} (rows)
         for (int q = 0; q < c; ++q)
             for (int r = 0; r < c; ++r) {
-                double2 s = A[q][r];
-                for (int t = 0; t < r; ++t) s = csub(s, cmul(Bm[t][r], A[q][t]));
-                A[q][r] = cscale(s, 1.0 / Bm[r][r].x);
+                double2 s2 = A[q][r];
+                for (int t = 0; t < r; ++t) s2 = csub(s2, cmul(Bm[t][r], A[q][t]));
+                A[q][r] = cscale(s2, 1.0 / Bm[r][r].x);
             }
         for (int r = 0; r < c; ++r)
             for (int q = 0; q < c; ++q) {
-                double2 s = A[q][r];
-                for (int t = 0; t < q; ++t) s = csub(s, cmul(A[t][r], cconj(Bm[t][q])));
-                A[q][r] = cscale(s, 1.0 / Bm[q][q].x);
+                double2 s2 = A[q][r];
+                for (int t = 0; t < q; ++t) s2 = csub(s2, cmul(A[t][r], cconj(Bm[t][q])));
+                A[q][r] = cscale(s2, 1.0 / Bm[q][q].x);
             }
         for (int q = 0; q < c; ++q)
             for (int r = 0; r < c; ++r) Vv[q][r] = make_double2(r == q ? 1.0 : 0.0, 0.0);
@@ -203,15 +255,15 @@ __global__ void __launch_bounds__(32) k_ref_rr(RefineWork w)
     __syncwarp();
     // cyclic complex Jacobi on the Hermitian A, accumulating V
     for (int sweep = 0; sweep < 30; ++sweep) {
-        double off = 0, dsum = 0;
+        double offd = 0, dsum = 0;
         for (int e = lane; e < c * c; e += 32) {
             const int r = e % c, q = e / c;
-            if (r != q) off += A[q][r].x * A[q][r].x + A[q][r].y * A[q][r].y;
+            if (r != q) offd += A[q][r].x * A[q][r].x + A[q][r].y * A[q][r].y;
             else dsum += A[q][r].x * A[q][r].x;
         }
-        off = warp_sum(off);
+        offd = warp_sum(offd);
         dsum = warp_sum(dsum);
-        if (!(off > 1e-32 * dsum)) break;
+        if (!(offd > 1e-32 * dsum)) break;
         for (int pp = 0; pp < c - 1; ++pp)
             for (int qq = pp + 1; qq < c; ++qq) {
                 __syncwarp();
@@ -254,9 +306,9 @@ __global__ void __launch_bounds__(32) k_ref_rr(RefineWork w)
     if (lane == 0) {
         for (int q = 0; q < c; ++q)
             for (int r = c - 1; r >= 0; --r) {
-                double2 s = Vv[q][r];
-                for (int t = r + 1; t < c; ++t) s = csub(s, cmul(cconj(Bm[r][t]), Vv[q][t]));
-                Vv[q][r] = cscale(s, 1.0 / Bm[r][r].x);
+                double2 s2 = Vv[q][r];
+                for (int t = r + 1; t < c; ++t) s2 = csub(s2, cmul(cconj(Bm[r][t]), Vv[q][t]));
+                Vv[q][r] = cscale(s2, 1.0 / Bm[r][r].x);
             }
     }
     __syncwarp();
@@ -264,56 +316,45 @@ __global__ void __launch_bounds__(32) k_ref_rr(RefineWork w)
         const int a = e % c, q = e / c;
         U[(long)ord[p + q] * REF_CMAX + a] = Vv[q][a];
     }
+    for (int q = lane; q < c; q += 32) {
+        const int j = ord[p + q];
+        w.lam[(long)b * n + j] = A[q][q].x;        // Rayleigh-Ritz eigenvalue
+        w.lam[nb + (long)b * n + j] = 1.0;         // R'_jj
+    }
 }
 
-// element (i, j) of a Hermitian matrix of which only the upper triangle (and
-// whole diagonal tiles) is stored
-__device__ __forceinline__ double2 herm(const double2 *M, int n, int i, int j)
-{
-    return (i <= j) ? M[i + (long)j * n] : cconj(M[j + (long)i * n]);
-}
+#define REF_VIEWS                                                              \
+    const long nb = (long)n * w.batch;                                         \
+    const int *ord = w.cl + (long)b * n, *pos0 = w.cl + nb + (long)b * n;      \
+    const int *csz = w.cl + 2 * nb + (long)b * n;                              \
+    const double2 *U = w.U + (long)b * n * REF_CMAX;
 
-// element (i, j) of U^H M U for the block-diagonal cluster rotation U
-__device__ __forceinline__ double2 rotated(const double2 *M, const double2 *U, const int *ord, const int *pos0,
-                                           const int *csz, int n, int i, int j)
+// element (i, j) of G' = U^H G U for the block-diagonal cluster rotation U
+__device__ __forceinline__ double2 rotated_g(const float2 *G, const double2 *U, const int *ord, const int *pos0,
+                                             const int *csz, int n, int i, int j)
 {
-    const int pi = pos0[i], ci = csz[i], pj = pos0[j], cj = csz[j];
-    if (ci == 1 && cj == 1) return herm(M, n, i, j);
+    const int ci = csz[i], cj = csz[j];
+    if (ci == 1 && cj == 1) {
+        const float2 g = G[i + (long)j * n];
+        return make_double2(g.x, g.y);
+    }
     double2 s = make_double2(0, 0);
     for (int a = 0; a < ci; ++a) {
-        const int ga = (ci == 1) ? i : ord[pi + a];
+        const int ga = (ci == 1) ? i : ord[pos0[i] + a];
         const double2 ua = (ci == 1) ? make_double2(1, 0) : cconj(U[(long)i * REF_CMAX + a]);
         double2 t = make_double2(0, 0);
         for (int bb = 0; bb < cj; ++bb) {
-            const int gb = (cj == 1) ? j : ord[pj + bb];
+            const int gb = (cj == 1) ? j : ord[pos0[j] + bb];
             const double2 ub = (cj == 1) ? make_double2(1, 0) : U[(long)j * REF_CMAX + bb];
-            t = cadd(t, cmul(herm(M, n, ga, gb), ub));
+            const float2 g = G[ga + (long)gb * n];
+            t = cadd(t, cmul(make_double2(g.x, g.y), ub));
         }
         s = cadd(s, cmul(ua, t));
     }
     return s;
 }
 
-#define REF_VIEWS                                                              \
-    const int *ord = w.cl + (long)b * n, *pos0 = w.cl + (long)n * w.batch + (long)b * n; \
-    const int *csz = w.cl + (long)2 * n * w.batch + (long)b * n;               \
-    const double2 *U = w.U + (long)b * n * REF_CMAX;
-
-// 3a. l_j = T'_jj / R'_jj (thread per j)
-__global__ void k_ref_lambda(RefineWork w)
-{
-    const int b = blockIdx.y, n = w.n;
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= n) return;
-    const long mo = (long)b * n * n;
-    REF_VIEWS
-    const double t = rotated(w.T + mo, U, ord, pos0, csz, n, j, j).x;
-    const double r = rotated(w.R + mo, U, ord, pos0, csz, n, j, j).x;
-    w.lam[(long)b * n + j] = t / r;
-    w.lam[(long)n * w.batch + (long)b * n + j] = r;
-}
-
-// 3b. E column j and the second-order eigenvalue term (warp per column)
+// 3. E column j and the second-order eigenvalue term (warp per column)
 __global__ void k_ref_update(RefineWork w, double *l2out)
 {
     const int warp = (int)((blockIdx.x * (long)blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
@@ -323,9 +364,10 @@ __global__ void k_ref_update(RefineWork w, double *l2out)
     const long mo = (long)b * n * n;
     REF_VIEWS
     const double *l1 = w.lam + (long)b * n;
-    const double lj = l1[j], rjj = w.lam[(long)n * w.batch + (long)b * n + j];
+    const double lj = l1[j], rjj = w.lam[nb + (long)b * n + j];
     double corr = 0;
     float2 *E = w.Ef + mo + (long)j * n;
+    const float2 *G = w.G + mo;
     for (int i = lane; i < n; i += 32) {
         float2 e;
         if (i == j) {
@@ -333,12 +375,10 @@ __global__ void k_ref_update(RefineWork w, double *l2out)
         } else if (pos0[i] == pos0[j]) {
             e = make_float2(0.f, 0.f);
         } else {
-            const double2 t = rotated(w.T + mo, U, ord, pos0, csz, n, i, j);
-            const double2 r = rotated(w.R + mo, U, ord, pos0, csz, n, i, j);
-            const double2 num = make_double2(t.x - lj * r.x, t.y - lj * r.y);
+            const double2 g = rotated_g(G, U, ord, pos0, csz, n, i, j);
             const double den = lj - l1[i];
-            e = make_float2((float)(num.x / den), (float)(num.y / den));
-            corr += (num.x * num.x + num.y * num.y) / den;
+            e = make_float2((float)(g.x / den), (float)(g.y / den));
+            corr += (g.x * g.x + g.y * g.y) / den;
         }
         E[i] = e;
     }
@@ -369,7 +409,6 @@ __global__ void k_ref_rotate(RefineWork w, const float2 *X)
             v = cadd(v, cmul(make_double2(x.x, x.y), U[(long)j * REF_CMAX + a]));
         }
     }
-    (void)ord;
     w.YH[t] = v;
     w.Xr[t] = make_float2((float)v.x, (float)v.y);
 }
@@ -412,22 +451,21 @@ void refine_eigen(cudaStream_t s, RefineWork &w, const double2 *H, const double2
 {
     const int n = w.n, B = w.batch;
     const long nn = (long)n * n;
-    // 1. T = X^H (H X), R = X^H (S X)
+    const float2 onef = make_float2(1.f, 0.f), zerof = make_float2(0.f, 0.f);
+    // 1. H X, S X (double-float), residuals, G = X^H r (FP32), accurate diagonals
     dfgemm<double2, float2>(s, n, n, n, B, H, n, nn, 0, X, n, nn, 0, w.YH, n, nn);
     dfgemm<double2, float2>(s, n, n, n, B, S, n, nn, 0, X, n, nn, 0, w.YS, n, nn);
-    // T and R are Hermitian: only the tiles touching the upper triangle are formed
-    dfgemm<float2, double2>(s, n, n, n, B, X, n, nn, 1, w.YH, n, nn, 0, w.T, n, nn, 0.0, 0, 2);
-    dfgemm<float2, double2>(s, n, n, n, B, X, n, nn, 1, w.YS, n, nn, 0, w.R, n, nn, 0.0, 0, 2);
+    NRLTB_LAUNCH(k_ref_resid, cdiv(nn * B, 256), 256, 0, s, w, eig);
+    zgemm<float>(s, n, n, n, B, onef, X, n, nn, 1, w.Ef, n, nn, 0, zerof, w.G, n, nn);
+    NRLTB_LAUNCH(k_ref_diag, cdiv((long)n * B * 32, 256), 256, 0, s, w, X);
     // 2. clusters and their Rayleigh-Ritz rotations
     NRLTB_LAUNCH(k_ref_clusters, B, 1024, 0, s, w, status);
-    NRLTB_LAUNCH(k_ref_rr, dim3(n, B), 32, 0, s, w);
-    // 3. eigenvalue estimates, correction matrix and second-order eigenvalues
-    NRLTB_LAUNCH(k_ref_lambda, dim3(cdiv(n, 128), B), 128, 0, s, w);
-    double *l2 = (double *)w.YS;   // YS is free once R is formed
+    NRLTB_LAUNCH(k_ref_rr, dim3(n, B), 32, 0, s, w, X);
+    // 3. correction matrix and second-order eigenvalues (YS is free: it holds them)
+    double *l2 = (double *)w.YS;
     NRLTB_LAUNCH(k_ref_update, cdiv((long)n * B * 32, 256), 256, 0, s, w, l2);
     // 4. Z = X U + (X U) E, reordered
     NRLTB_LAUNCH(k_ref_rotate, cdiv(nn * B, 256), 256, 0, s, w, X);
-    const float2 onef = make_float2(1.f, 0.f), zerof = make_float2(0.f, 0.f);
     zgemm<float>(s, n, n, n, B, onef, w.Xr, n, nn, 0, w.Ef, n, nn, 0, zerof, w.XE, n, nn);
     NRLTB_LAUNCH(k_ref_rank, dim3(cdiv(n, 128), B), 128, 0, s, w, l2, eig);
     if (Z) NRLTB_LAUNCH(k_ref_finish, cdiv(nn * B, 256), 256, 0, s, w, Z);

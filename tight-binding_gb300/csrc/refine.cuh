@@ -8,8 +8,8 @@ namespace nrltb {
 struct RefineWork {
     int n, batch;
     double2 *YH, *YS;       // H X, S X
-    double2 *T, *R;         // X^H H X, X^H S X
-    double2 *U;             // cluster rotations / update matrix
+    float2 *G;              // X^H r, r the residuals H x_j - l_j S x_j
+    double2 *U;             // cluster rotations
     float2 *Ef;             // FP32 update matrix
     float2 *Xr;             // rotated FP32 vectors
     float2 *XE;             // X E (FP32)
