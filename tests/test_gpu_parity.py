@@ -214,3 +214,28 @@ def test_bande_nonpositive_overlap_kpoints(ctx):
     assert o.nonphysical_k >= 2
     assert g.nonphysical_k == o.nonphysical_k
     assert np.array_equal(g.k_status, o.k_status)
+
+
+def test_host_driver_ex1_skeng(tmp_path, ex1_gold):
+    # the C driver (static.f's structure loop) over the ex1 SKIN reproduces the
+    # reference's SKENG to its printed 9 decimals
+    import os
+    import shutil
+    import subprocess
+    from conftest import GOLDEN
+    from nrltb import build
+    src = os.path.join(GOLDEN, "ex1")
+    for f in os.listdir(src):
+        shutil.copy(os.path.join(src, f), tmp_path / f)
+    r = subprocess.run([build.DRIVER, "SKIN"], cwd=tmp_path, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    lines = (tmp_path / "SKENG").read_text().splitlines()
+    assert len(lines) == 18
+    for line, gold, label in zip(lines, ex1_gold["skeng"], ex1_gold["labels"]):
+        assert line[:20].split() == label.split()
+        vals = [float(x) for x in line[20:].split()]
+        assert abs(vals[0] - gold[0]) <= 5e-7
+        for v, g in zip(vals[1:], gold[1:]):
+            assert abs(v - g) <= 1.01e-9
+    out = (tmp_path / "SKOUT").read_text()
+    assert out.count("Number of pairs =") == 18

@@ -1,0 +1,134 @@
+/*
+ * nrltb_static.c -- the C host driver: the structure loop of the reference's
+ * "static" program (static.f:919-1259) on top of the GPU k-point path.
+ *
+ *   nrltb_static [--precision fp64|mixed] [--device N] [--fermi-tol T] [SKIN]
+ *
+ * Reads the SKIN file (default ./SKIN) and the parameter and k-point files it
+ * names with the C readers (nrltb_input.h), then for every structure calls
+ * nrltb_bande -- the drop-in for search2 + bande (static.f:1114, 1218) -- and
+ * appends one line to SKENG in the reference's format (static.f:1238-1254) and
+ * a summary block to SKOUT (bande.f:1405-1476 wording).  Output files go to the
+ * current directory, as in the reference.  search2's carried kneigh flag
+ * passes from one structure to the next as the reference's common block does.
+ */
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include "nrltb.h"
+#include "nrltb_input.h"
+
+static void usage(void)
+{
+    fprintf(stderr, "usage: nrltb_static [--precision fp64|mixed] [--device N] [--fermi-tol T] [SKIN]\n");
+}
+
+int main(int argc, char **argv)
+{
+    const char *skin_path = "SKIN";
+    int precision = NRLTB_PREC_FP64, device = 0;
+    double fermi_tol = 0.0;
+    for (int i = 1; i < argc; ++i) {
+        if (!strcmp(argv[i], "--precision") && i + 1 < argc) {
+            ++i;
+            if (!strcmp(argv[i], "fp64")) precision = NRLTB_PREC_FP64;
+            else if (!strcmp(argv[i], "mixed")) precision = NRLTB_PREC_MIXED;
+            else { usage(); return 2; }
+        } else if (!strcmp(argv[i], "--device") && i + 1 < argc) {
+            device = atoi(argv[++i]);
+        } else if (!strcmp(argv[i], "--fermi-tol") && i + 1 < argc) {
+            fermi_tol = atof(argv[++i]);
+        } else if (argv[i][0] == '-') {
+            usage();
+            return 2;
+        } else {
+            skin_path = argv[i];
+        }
+    }
+    nrltb_skin *skin = NULL;
+    int rc = nrltb_skin_open(skin_path, &skin);
+    if (rc != NRLTB_OK) {
+        fprintf(stderr, "nrltb_static: cannot read %s (error %d)\n", skin_path, rc);
+        return 1;
+    }
+    int mode;
+    double tkb, eigcut;
+    nrltb_params par;
+    nrltb_skin_info(skin, &mode, &tkb, &eigcut, &par);
+    if (mode != 3 && mode != 4) {
+        fprintf(stderr, "nrltb_static: Mode=%d is not built (modes 3 and 4 are)\n", mode);
+        nrltb_skin_close(skin);
+        return 1;
+    }
+    nrltb_ctx *ctx = NULL;
+    rc = nrltb_ctx_create(&ctx, device);
+    if (rc != NRLTB_OK) {
+        fprintf(stderr, "nrltb_static: no GPU context: %s\n", nrltb_last_error());
+        nrltb_skin_close(skin);
+        return 1;
+    }
+    FILE *skout = fopen("SKOUT", "w"), *skeng = fopen("SKENG", "w");
+    if (!skout || !skeng) {
+        fprintf(stderr, "nrltb_static: cannot write SKOUT/SKENG\n");
+        return 1;
+    }
+    fprintf(skout, " mode=%12d\n", mode);
+    fprintf(skout, "  temp. broad. (ryd): %.17G  eigenvalue cutoff = %.17G\n", tkb, eigcut);
+    fprintf(skout, " precision form: %s\n", precision == NRLTB_PREC_FP64 ? "FP64" : "mixed (FP32 + FP64 refinement)");
+    int kneigh = 0, jstruc = 0, status = 0;
+    for (;;) {
+        nrltb_structure st;
+        nrltb_kmesh km;
+        char title[72], label[24];
+        rc = nrltb_skin_next(skin, &st, &km, title, label);
+        if (rc == NRLTB_E_EOF) break;
+        if (rc != NRLTB_OK) {
+            fprintf(stderr, "nrltb_static: SKIN error %d near line %d\n", rc, nrltb_skin_error_line(skin));
+            status = 1;
+            break;
+        }
+        ++jstruc;
+        nrltb_opts opt;
+        memset(&opt, 0, sizeof opt);
+        opt.mode = mode;
+        opt.precision = precision;
+        opt.tkb = tkb;
+        opt.eigcut = eigcut;
+        opt.fermi_tol = fermi_tol;
+        opt.kneigh_in = kneigh;
+        nrltb_result res;
+        memset(&res, 0, sizeof res);
+        rc = nrltb_bande(ctx, &st, &par, &km, &opt, &res);
+        if (rc != NRLTB_OK) {
+            fprintf(stderr, "nrltb_static: structure %d: %s\n", jstruc, nrltb_last_error());
+            status = 1;
+            break;
+        }
+        kneigh = res.kneigh_out;
+        fprintf(skout, "-------------------------------\n\nstructure %5d\n\n%s\n\n", jstruc, title);
+        fprintf(skout, " Minimum distance this configuration = %.17G\n", res.dismin);
+        fprintf(skout, "Number of pairs = %6d\n", res.npairs);
+        fprintf(skout, " Secular equation size = %12d\n", res.nv);
+        fprintf(skout, " Volume= %.17G\n", st.volume);
+        if (res.nonphysical_k)
+            fprintf(skout, " Found non-physical overlap at %d k-points\n", res.nonphysical_k);
+        fprintf(skout, " Temperature = %.17G\n", tkb);
+        fprintf(skout, " EFermi = %.17G\n", res.efermi);
+        fprintf(skout, " E(T) = %.17G\n", res.e_total);
+        if (mode == 4) {
+            fprintf(skout, " Fermi level shift: %.17G\n", res.fermi_shift);
+            fprintf(skout, " P(T) = %.17G\n", res.pressure);
+            fprintf(skeng, "%-20.20s%12.6f%15.9f%15.9f%15.9f\n", label, st.volume, res.efermi, res.e_total,
+                    res.pressure);
+        } else {
+            fprintf(skeng, "%-20.20s%12.6f%15.9f%15.9f\n", label, st.volume, res.efermi, res.e_total);
+        }
+        fflush(skeng);
+        fflush(skout);
+    }
+    fclose(skout);
+    fclose(skeng);
+    nrltb_ctx_destroy(ctx);
+    nrltb_skin_close(skin);
+    return status;
+}
