@@ -15,10 +15,35 @@ extern "C" {
 int nrltb_bench_peak(nrltb_ctx *ctx, int kind, double *tflops);
 
 /* One batched complex GEMM launch of the eigensolver's kernel (C = A B, n x n x n,
- * `batch` matrices), precision 0 = FP64, 1 = FP32; averaged over `reps` launches
- * after a warm-up.  flops_per_launch = 8 n^3 batch. */
+ * `batch` matrices): precision 0 = FP64 (SIMT FMA pipe), 1 = FP32 (tensor cores,
+ * 3xTF32), 2 = FP32 on the SIMT FMA pipe (for comparison); averaged over `reps`
+ * launches after a warm-up.  flops_per_launch = 8 n^3 batch. */
 int nrltb_bench_zgemm(nrltb_ctx *ctx, int precision, int n, int batch, int reps,
                       double *ms_per_launch, double *flops_per_launch);
+
+/* One FP64-accurate product Y = A X of the mixed form's refinement (A FP64
+ * Hermitian, X FP32, both n x n complex, `batch` matrices): method 0 = the
+ * double-float SIMT GEMM, 1 = the bf16 tensor-core digit product.  Averaged
+ * over `reps` pairs of launches (H X and S X) after a warm-up;
+ * flops_per_launch = 8 n^3 batch for one product. */
+int nrltb_bench_refprod(nrltb_ctx *ctx, int method, int n, int batch, int reps,
+                        double *ms_per_launch, double *flops_per_launch);
+
+/* The same product on caller data, for accuracy checks: host arrays A
+ * (batch x n x n complex FP64, column-major, interleaved re/im, Hermitian),
+ * X (batch x n x n complex FP32; method 1 rounds it in place to the digits
+ * it uses) and Y (batch x n x n complex FP64, out). */
+int nrltb_bench_refprod_run(nrltb_ctx *ctx, int method, int n, int batch, const double *A, float *X,
+                            double *Y);
+
+/* One FP32 complex GEMM of the eigensolver's kernel on caller data, for
+ * accuracy checks: C = alpha op(A) op(B) + beta C with the kernel's op and
+ * triangle flags (gemm.cuh), one matrix; method 1 = tensor cores, 2 = SIMT.
+ * A, B, C are host arrays (column-major complex FP32, leading dimensions
+ * lda, ldb, ldc); alpha, beta are {re, im}. */
+int nrltb_bench_cgemm_run(nrltb_ctx *ctx, int method, int m, int n, int k, int opA, int opB, int triA,
+                          int triB, int triC, const float alpha[2], const float beta[2], const float *A,
+                          int lda, const float *B, int ldb, float *C, int ldc);
 
 #ifdef __cplusplus
 }

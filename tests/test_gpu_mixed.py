@@ -102,3 +102,59 @@ def test_mixed_bande_ex1_against_skout(ctx, ex1, ex1_gold):
         assert r.efermi == pytest.approx(ex1_gold["efermi"][idx], abs=1e-9)
         assert r.e_total == pytest.approx(ex1_gold["e_total"][idx], abs=1e-9)
         assert r.pressure == pytest.approx(ex1_gold["pressure"][idx], abs=P_TOL)
+
+
+def _refprod(ctx, method, A, X):
+    """Y = A X through the refinement's product (nrltb_bench_refprod_run)."""
+    import ctypes as C
+    A = np.ascontiguousarray(A.transpose(0, 2, 1), dtype=np.complex128)    # column-major per matrix
+    Xc = np.ascontiguousarray(X.transpose(0, 2, 1), dtype=np.complex64)
+    Y = np.zeros_like(A)
+    b, n = A.shape[0], A.shape[1]
+    rc = ctx.lib.nrltb_bench_refprod_run(ctx.h, method, n, b, A.ctypes.data_as(C.c_void_p),
+                                         Xc.ctypes.data_as(C.c_void_p), Y.ctypes.data_as(C.c_void_p))
+    assert rc == 0, ctx.lib.nrltb_last_error()
+    return Y.transpose(0, 2, 1), Xc.transpose(0, 2, 1)
+
+
+@pytest.mark.parametrize("method", [0, 1])
+def test_refinement_product_accuracy(ctx, method):
+    """H X against an extended-precision product of the X the method used.
+    Double-float SIMT (method 0): componentwise, the error grows like n 2^-48
+    |A||X| (its low part accumulates in plain FP32).  Tensor-core digits
+    (method 1): exact per 64-wide chunk; the error is the cut of A after 6
+    digits and the dropped digit levels, a fixed-point error per term of at
+    most 2^-43 of (largest component in row m of A) x (largest component in
+    column n of X)."""
+    rng = np.random.default_rng(5)
+    b, n = 2, 200
+    # Hermitian A with H-like structure: O(1) diagonal, decaying off-diagonals
+    # spanning many binades, some exact zeros
+    A = rng.standard_normal((b, n, n)) + 1j * rng.standard_normal((b, n, n))
+    i = np.arange(n)
+    A *= np.exp(-np.abs(i[:, None] - i[None, :]) / 15.0)[None]
+    A[:, 50:60, 100:120] = 0
+    A = 0.5 * (A + A.conj().transpose(0, 2, 1))
+    # FP32 X with columns of very different scale and a decaying tail
+    X = (rng.standard_normal((b, n, n)) + 1j * rng.standard_normal((b, n, n))) * \
+        np.logspace(-3, 1, n)[None, None, :] * np.exp(-i / 40.0)[None, :, None]
+    X = X.astype(np.complex64)
+    Y, Xu = _refprod(ctx, method, A, X)
+    # the rounded X stays within 2^-23 of each column's largest element (half a
+    # unit of 2^(e-23), 2^(e-1) <= colmax < 2^e)
+    colmax = np.maximum(np.abs(X.real), np.abs(X.imag)).max(axis=1, keepdims=True)
+    dx = np.maximum(np.abs(Xu.real - X.real), np.abs(Xu.imag - X.imag))
+    assert (dx <= colmax * 2.0 ** -23).all()
+    if method == 0:
+        assert (Xu == X).all()
+    ref = np.matmul(A.astype(np.clongdouble), Xu.astype(np.clongdouble))
+    err = np.abs((Y.astype(np.clongdouble) - ref).astype(np.complex128))
+    comp = np.matmul(np.abs(A), np.abs(Xu.astype(np.complex128)))
+    amax = np.maximum(np.abs(A.real), np.abs(A.imag)).max(axis=2)
+    xmax = np.maximum(np.abs(Xu.real), np.abs(Xu.imag)).max(axis=1).astype(np.float64)
+    fixed = n * amax[:, :, None] * xmax[:, None, :]
+    r_comp, r_fixed = (err / comp).max(), (err / fixed).max()
+    if method == 0:
+        assert r_comp <= n * 2.0 ** -46, (r_comp, r_fixed)
+    else:
+        assert r_fixed <= 2.0 ** -43, (r_comp, r_fixed)

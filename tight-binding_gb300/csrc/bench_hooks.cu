@@ -4,6 +4,8 @@
 #include "nrltb_bench.h"
 #include "common.cuh"
 #include "gemm.cuh"
+#include "dfgemm.cuh"
+#include "ozaki.cuh"
 
 using namespace nrltb;
 
@@ -60,7 +62,18 @@ extern "C" int nrltb_bench_peak(nrltb_ctx *ctx, int kind, double *tflops)
     return NRLTB_OK;
 }
 
-template <typename T>
+template <typename T, bool SIMT>
+static void one_gemm(cudaStream_t s, int n, int batch, const typename cplx<T>::t *A, const typename cplx<T>::t *B,
+                     typename cplx<T>::t *C)
+{
+    typedef typename cplx<T>::t C2;
+    const C2 one = cmk<T>(1, 0), zero = cmk<T>(0, 0);
+    const long st = (long)n * n;
+    if (SIMT) zgemm_simt<T>(s, n, n, n, batch, one, A, n, st, 0, B, n, st, 0, zero, C, n, st);
+    else zgemm<T>(s, n, n, n, batch, one, A, n, st, 0, B, n, st, 0, zero, C, n, st);
+}
+
+template <typename T, bool SIMT>
 static int time_gemm(cudaStream_t s, int n, int batch, int reps, double *ms)
 {
     typedef typename cplx<T>::t C2;
@@ -71,14 +84,12 @@ static int time_gemm(cudaStream_t s, int n, int batch, int reps, double *ms)
     if (cudaMalloc(&C, sizeof(C2) * nn) != cudaSuccess) { cudaFree(A); cudaFree(B); return NRLTB_E_NOMEM; }
     cudaMemsetAsync(A, 0, sizeof(C2) * nn, s);
     cudaMemsetAsync(B, 0, sizeof(C2) * nn, s);
-    const C2 one = cmk<T>(1, 0), zero = cmk<T>(0, 0);
-    const long st = (long)n * n;
-    zgemm<T>(s, n, n, n, batch, one, A, n, st, 0, B, n, st, 0, zero, C, n, st);
+    one_gemm<T, SIMT>(s, n, batch, A, B, C);
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     cudaEventRecord(e0, s);
-    for (int r = 0; r < reps; ++r) zgemm<T>(s, n, n, n, batch, one, A, n, st, 0, B, n, st, 0, zero, C, n, st);
+    for (int r = 0; r < reps; ++r) one_gemm<T, SIMT>(s, n, batch, A, B, C);
     cudaEventRecord(e1, s);
     cudaEventSynchronize(e1);
     float t = 0;
@@ -95,8 +106,124 @@ extern "C" int nrltb_bench_zgemm(nrltb_ctx *ctx, int precision, int n, int batch
 {
     if (!ctx || n < 1 || batch < 1 || reps < 1 || !ms_per_launch || !flops_per_launch) return NRLTB_E_ARG;
     cudaStream_t s = nrltb_ctx_stream_internal(ctx);
-    int rc = precision == 0 ? time_gemm<double>(s, n, batch, reps, ms_per_launch)
-                            : time_gemm<float>(s, n, batch, reps, ms_per_launch);
+    if (precision < 0 || precision > 2) return NRLTB_E_ARG;
+    int rc = precision == 0   ? time_gemm<double, true>(s, n, batch, reps, ms_per_launch)
+             : precision == 1 ? time_gemm<float, false>(s, n, batch, reps, ms_per_launch)
+                              : time_gemm<float, true>(s, n, batch, reps, ms_per_launch);
     *flops_per_launch = 8.0 * n * (double)n * n * batch;
     return rc;
+}
+
+// the refinement product Y = A X by either method; `work` holds ozaki_work_bytes
+static void refprod(cudaStream_t s, int method, int n, int batch, const double2 *A, float2 *X, double2 *Y,
+                    void *work)
+{
+    const long nn = (long)n * n;
+    if (method == 0) {
+        dfgemm<double2, float2>(s, n, n, n, batch, A, n, nn, 0, X, n, nn, 0, Y, n, nn);
+    } else {
+        const OzakiX ox = ozaki_prepare_x(s, X, n, batch, work);
+        ozaki_gemm(s, ox, A, Y);
+    }
+}
+
+struct DevBufs {
+    void *p[4] = {nullptr, nullptr, nullptr, nullptr};
+    ~DevBufs() { for (void *q : p) if (q) cudaFree(q); }
+};
+
+extern "C" int nrltb_bench_refprod(nrltb_ctx *ctx, int method, int n, int batch, int reps, double *ms_per_launch,
+                                   double *flops_per_launch)
+{
+    if (!ctx || (method != 0 && method != 1) || n < 1 || batch < 1 || reps < 1 || !ms_per_launch ||
+        !flops_per_launch)
+        return NRLTB_E_ARG;
+    cudaStream_t s = nrltb_ctx_stream_internal(ctx);
+    const size_t nn = (size_t)n * n * batch;
+    DevBufs d;
+    if (cudaMalloc(&d.p[0], sizeof(double2) * nn) != cudaSuccess ||
+        cudaMalloc(&d.p[1], sizeof(double2) * nn) != cudaSuccess ||
+        cudaMalloc(&d.p[2], sizeof(float2) * nn) != cudaSuccess ||
+        cudaMalloc(&d.p[3], ozaki_work_bytes(n, batch)) != cudaSuccess)
+        return NRLTB_E_NOMEM;
+    double2 *A = (double2 *)d.p[0], *Y = (double2 *)d.p[1];
+    float2 *X = (float2 *)d.p[2];
+    cudaMemsetAsync(A, 0, sizeof(double2) * nn, s);
+    cudaMemsetAsync(X, 0, sizeof(float2) * nn, s);
+    refprod(s, method, n, batch, A, X, Y, d.p[3]);
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, s);
+    for (int r = 0; r < reps; ++r) {
+        refprod(s, method, n, batch, A, X, Y, d.p[3]);
+        refprod(s, method, n, batch, A, X, Y, d.p[3]);
+    }
+    cudaEventRecord(e1, s);
+    cudaEventSynchronize(e1);
+    float t = 0;
+    cudaEventElapsedTime(&t, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    *ms_per_launch = t / (2.0 * reps);
+    *flops_per_launch = 8.0 * n * (double)n * n * batch;
+    return cudaGetLastError() == cudaSuccess ? NRLTB_OK : NRLTB_E_CUDA;
+}
+
+extern "C" int nrltb_bench_refprod_run(nrltb_ctx *ctx, int method, int n, int batch, const double *A, float *X,
+                                       double *Y)
+{
+    if (!ctx || (method != 0 && method != 1) || n < 1 || batch < 1 || !A || !X || !Y) return NRLTB_E_ARG;
+    cudaStream_t s = nrltb_ctx_stream_internal(ctx);
+    const size_t nn = (size_t)n * n * batch;
+    DevBufs d;
+    if (cudaMalloc(&d.p[0], sizeof(double2) * nn) != cudaSuccess ||
+        cudaMalloc(&d.p[1], sizeof(double2) * nn) != cudaSuccess ||
+        cudaMalloc(&d.p[2], sizeof(float2) * nn) != cudaSuccess ||
+        cudaMalloc(&d.p[3], ozaki_work_bytes(n, batch)) != cudaSuccess)
+        return NRLTB_E_NOMEM;
+    if (cudaMemcpyAsync(d.p[0], A, sizeof(double2) * nn, cudaMemcpyHostToDevice, s) != cudaSuccess ||
+        cudaMemcpyAsync(d.p[2], X, sizeof(float2) * nn, cudaMemcpyHostToDevice, s) != cudaSuccess)
+        return NRLTB_E_CUDA;
+    refprod(s, method, n, batch, (const double2 *)d.p[0], (float2 *)d.p[2], (double2 *)d.p[1], d.p[3]);
+    if (cudaMemcpyAsync(Y, d.p[1], sizeof(double2) * nn, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaMemcpyAsync(X, d.p[2], sizeof(float2) * nn, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess)
+        return NRLTB_E_CUDA;
+    return cudaGetLastError() == cudaSuccess ? NRLTB_OK : NRLTB_E_CUDA;
+}
+
+extern "C" int nrltb_bench_cgemm_run(nrltb_ctx *ctx, int method, int m, int n, int k, int opA, int opB, int triA,
+                                     int triB, int triC, const float alpha[2], const float beta[2], const float *A,
+                                     int lda, const float *B, int ldb, float *C, int ldc)
+{
+    if (!ctx || (method != 1 && method != 2) || m < 1 || n < 1 || k < 1 || !alpha || !beta || !A || !B || !C)
+        return NRLTB_E_ARG;
+    if (opA < 0 || opA > 1 || opB < 0 || opB > 1 || triA < 0 || triA > 2 || triB < 0 || triB > 2 || triC < 0 ||
+        triC > 2)
+        return NRLTB_E_ARG;
+    const long ra = opA ? k : m, ca = opA ? m : k, rb = opB ? n : k, cb = opB ? k : n;
+    if (lda < ra || ldb < rb || ldc < m) return NRLTB_E_ARG;
+    const size_t na = (size_t)lda * ca, nb = (size_t)ldb * cb, nc = (size_t)ldc * n;
+    cudaStream_t s = nrltb_ctx_stream_internal(ctx);
+    DevBufs d;
+    if (cudaMalloc(&d.p[0], sizeof(float2) * na) != cudaSuccess ||
+        cudaMalloc(&d.p[1], sizeof(float2) * nb) != cudaSuccess ||
+        cudaMalloc(&d.p[2], sizeof(float2) * nc) != cudaSuccess)
+        return NRLTB_E_NOMEM;
+    if (cudaMemcpyAsync(d.p[0], A, sizeof(float2) * na, cudaMemcpyHostToDevice, s) != cudaSuccess ||
+        cudaMemcpyAsync(d.p[1], B, sizeof(float2) * nb, cudaMemcpyHostToDevice, s) != cudaSuccess ||
+        cudaMemcpyAsync(d.p[2], C, sizeof(float2) * nc, cudaMemcpyHostToDevice, s) != cudaSuccess)
+        return NRLTB_E_CUDA;
+    const float2 al = make_float2(alpha[0], alpha[1]), be = make_float2(beta[0], beta[1]);
+    const float2 *dA = (const float2 *)d.p[0], *dB = (const float2 *)d.p[1];
+    float2 *dC = (float2 *)d.p[2];
+    if (method == 1)
+        zgemm<float>(s, m, n, k, 1, al, dA, lda, 0, opA, dB, ldb, 0, opB, be, dC, ldc, 0, triA, triB, triC);
+    else
+        zgemm_simt<float>(s, m, n, k, 1, al, dA, lda, 0, opA, dB, ldb, 0, opB, be, dC, ldc, 0, triA, triB, triC);
+    if (cudaMemcpyAsync(C, dC, sizeof(float2) * nc, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess)
+        return NRLTB_E_CUDA;
+    return cudaGetLastError() == cudaSuccess ? NRLTB_OK : NRLTB_E_CUDA;
 }

@@ -11,7 +11,8 @@
 // that touch the lower (upper) triangle of C.
 //
 // SIMT register-tiled kernel: a BM x BN tile per CTA, BK-deep k slices staged
-// through shared memory, TM x TN complex outputs per thread.
+// through shared memory, TM x TN complex outputs per thread.  FP64 runs here
+// (GB300 has no FP64 tensor path); FP32 goes to the tensor cores (gemm_tc.cu).
 #pragma once
 #include "common.cuh"
 
@@ -138,6 +139,43 @@ zgemm_kernel(GemmArgs<T> g)
     }
 }
 
+// FP32 on the tensor cores (gemm_tc.cu)
+void zgemm_tc_launch(cudaStream_t s, const GemmArgs<float> &g);
+
+template <typename T>
+GemmArgs<T> gemm_args(int m, int n, int k, int batch, typename cplx<T>::t alpha,
+                      const typename cplx<T>::t *A, long lda, long sA, int opA,
+                      const typename cplx<T>::t *B, long ldb, long sB, int opB,
+                      typename cplx<T>::t beta, typename cplx<T>::t *C, long ldc, long sC,
+                      int triA, int triB, int triC)
+{
+    GemmArgs<T> g;
+    g.m = m; g.n = n; g.k = k; g.batch = batch;
+    g.A = A; g.lda = lda; g.sA = sA; g.opA = opA;
+    g.B = B; g.ldb = ldb; g.sB = sB; g.opB = opB;
+    g.C = C; g.ldc = ldc; g.sC = sC;
+    g.alpha = alpha; g.beta = beta;
+    g.triA = triA; g.triB = triB; g.triC = triC;
+    return g;
+}
+
+// the SIMT kernel in either precision
+template <typename T>
+void zgemm_simt(cudaStream_t s, int m, int n, int k, int batch, typename cplx<T>::t alpha,
+                const typename cplx<T>::t *A, long lda, long sA, int opA,
+                const typename cplx<T>::t *B, long ldb, long sB, int opB,
+                typename cplx<T>::t beta, typename cplx<T>::t *C, long ldc, long sC,
+                int triA = 0, int triB = 0, int triC = 0)
+{
+    if (m <= 0 || n <= 0 || batch <= 0) return;
+    const GemmArgs<T> g = gemm_args<T>(m, n, k, batch, alpha, A, lda, sA, opA, B, ldb, sB, opB, beta, C, ldc, sC,
+                                       triA, triB, triC);
+    constexpr int BM = 64, BN = 64, BK = 8, TM = 4, TN = 4;
+    dim3 grid(cdiv(m, BM), cdiv(n, BN), batch);
+    NRLTB_LAUNCH((zgemm_kernel<T, BM, BN, BK, TM, TN>), grid, (BM / TM) * (BN / TN), 0, s, g);
+}
+
+// FP64: SIMT FMA pipe; FP32: tensor cores (3xTF32, FP32-class accuracy)
 template <typename T>
 void zgemm(cudaStream_t s, int m, int n, int k, int batch, typename cplx<T>::t alpha,
            const typename cplx<T>::t *A, long lda, long sA, int opA,
@@ -146,16 +184,19 @@ void zgemm(cudaStream_t s, int m, int n, int k, int batch, typename cplx<T>::t a
            int triA = 0, int triB = 0, int triC = 0)
 {
     if (m <= 0 || n <= 0 || batch <= 0) return;
-    GemmArgs<T> g;
-    g.m = m; g.n = n; g.k = k; g.batch = batch;
-    g.A = A; g.lda = lda; g.sA = sA; g.opA = opA;
-    g.B = B; g.ldb = ldb; g.sB = sB; g.opB = opB;
-    g.C = C; g.ldc = ldc; g.sC = sC;
-    g.alpha = alpha; g.beta = beta;
-    g.triA = triA; g.triB = triB; g.triC = triC;
-    constexpr int BM = 64, BN = 64, BK = 8, TM = 4, TN = 4;
-    dim3 grid(cdiv(m, BM), cdiv(n, BN), batch);
-    NRLTB_LAUNCH((zgemm_kernel<T, BM, BN, BK, TM, TN>), grid, (BM / TM) * (BN / TN), 0, s, g);
+    // tensor cores only where a 128 x 64 tile is well filled and the k loop is long
+    if constexpr (sizeof(T) == 4) {
+        if (m < 128 || n < 64 || k < 128) {
+            zgemm_simt<T>(s, m, n, k, batch, alpha, A, lda, sA, opA, B, ldb, sB, opB, beta, C, ldc, sC, triA, triB,
+                          triC);
+            return;
+        }
+        zgemm_tc_launch(s, gemm_args<T>(m, n, k, batch, alpha, A, lda, sA, opA, B, ldb, sB, opB, beta, C, ldc, sC,
+                                        triA, triB, triC));
+    } else {
+        zgemm_simt<T>(s, m, n, k, batch, alpha, A, lda, sA, opA, B, ldb, sB, opB, beta, C, ldc, sC, triA, triB,
+                      triC);
+    }
 }
 
 }  // namespace nrltb

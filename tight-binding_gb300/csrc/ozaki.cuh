@@ -1,0 +1,23 @@
+// ozaki.cuh -- FP64-accurate products Y = A X (A FP64 Hermitian, X FP32) on the
+// bf16 tensor cores by exact digit splitting (ozaki.cu).
+#pragma once
+#include <cuda_bf16.h>
+#include "common.cuh"
+
+namespace nrltb {
+
+struct OzakiX {
+    __nv_bfloat16 *DA, *DX;    // digit planes of A (reused for each A) and of X
+    int *exA, *exX;            // per-row (A) and per-column (X) binary exponents
+    int n, np, batch;          // order, order padded to the 64-wide tile, matrices
+};
+
+size_t ozaki_work_bytes(int n, int batch);
+// Rounds X in place to its 3-digit representation (a change of at most 2^-23
+// of each column's largest element) and splits it; work holds
+// ozaki_work_bytes(n, batch) bytes, 256-byte aligned.
+OzakiX ozaki_prepare_x(cudaStream_t s, float2 *X, int n, int batch, void *work);
+// Y = A X for the batch, A column-major n x n Hermitian (both triangles stored)
+void ozaki_gemm(cudaStream_t s, const OzakiX &ox, const double2 *A, double2 *Y);
+
+}  // namespace nrltb

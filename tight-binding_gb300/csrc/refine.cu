@@ -3,7 +3,10 @@
 //
 // Given FP32 eigenvectors X (S-orthonormal to FP32 accuracy) and eigenvalue
 // estimates l~ of FP64 H, S:
-//   1. Y_H = H X, Y_S = S X in double-float arithmetic (dfgemm.cuh), and the
+//   1. Y_H = H X, Y_S = S X to FP64 accuracy on the bf16 tensor cores
+//      (exact digit splitting, ozaki.cuh; X is first rounded to 24 bits below
+//      each column's largest element so that the products are exact for the
+//      X used by every later step), and the
 //      residuals r_j = Y_H[:, j] - l~_j Y_S[:, j] in FP64.  The residuals are
 //      small (~1e-6), so G = X^H r (G_ij = T_ij - l~_j R_ij with T = X^H H X,
 //      R = X^H S X) is accurate to ~1e-13 even as an FP32 GEMM; only the
@@ -23,7 +26,7 @@
 #include <cfloat>
 #include "refine.cuh"
 #include "gemm.cuh"
-#include "dfgemm.cuh"
+#include "ozaki.cuh"
 #include "sums.cuh"
 #include "nrltb.h"
 
@@ -56,6 +59,7 @@ void refine_work_carve(RefineWork &w, void *base, int n, int batch)
     w.Ef = (float2 *)take(sizeof(float2) * nn);                    // residuals r, later E
     w.Xr = (float2 *)take(sizeof(float2) * nn);
     w.XE = (float2 *)take(sizeof(float2) * nn);
+    w.oz = take(ozaki_work_bytes(n, batch));
     w.lam = (double *)take(sizeof(double) * nb * 4);               // l | R'_jj | T_jj | R_jj
     w.cl = (int *)take(sizeof(int) * nb * 4);                      // ord | pos0 | size | rank
     if (!base) w.cl = (int *)(uintptr_t)off;
@@ -446,15 +450,17 @@ __global__ void k_ref_finish(RefineWork w, double2 *Z)
     Z[b * nn + r + (long)dst * n] = make_double2(x.x + (double)d.x, x.y + (double)d.y);
 }
 
-void refine_eigen(cudaStream_t s, RefineWork &w, const double2 *H, const double2 *S, const float2 *X,
+void refine_eigen(cudaStream_t s, RefineWork &w, const double2 *H, const double2 *S, float2 *X,
                   double *eig, double2 *Z, int *status)
 {
     const int n = w.n, B = w.batch;
     const long nn = (long)n * n;
     const float2 onef = make_float2(1.f, 0.f), zerof = make_float2(0.f, 0.f);
-    // 1. H X, S X (double-float), residuals, G = X^H r (FP32), accurate diagonals
-    dfgemm<double2, float2>(s, n, n, n, B, H, n, nn, 0, X, n, nn, 0, w.YH, n, nn);
-    dfgemm<double2, float2>(s, n, n, n, B, S, n, nn, 0, X, n, nn, 0, w.YS, n, nn);
+    // 1. H X, S X (tensor cores, FP64-accurate), residuals, G = X^H r (FP32),
+    //    accurate diagonals
+    const OzakiX ox = ozaki_prepare_x(s, X, n, B, w.oz);
+    ozaki_gemm(s, ox, H, w.YH);
+    ozaki_gemm(s, ox, S, w.YS);
     NRLTB_LAUNCH(k_ref_resid, cdiv(nn * B, 256), 256, 0, s, w, eig);
     zgemm<float>(s, n, n, n, B, onef, X, n, nn, 1, w.Ef, n, nn, 0, zerof, w.G, n, nn);
     NRLTB_LAUNCH(k_ref_diag, cdiv((long)n * B * 32, 256), 256, 0, s, w, X);
@@ -538,8 +544,11 @@ int run_hf(cudaStream_t s, int n, int nkc, int prec, const double2 *dH, const do
         launch_to_f32(s, dS, s32, nn * nkc);
         launch_to_f32(s, Z, z32, nn * nkc);
         const float2 one = make_float2(1.f, 0.f), zero = make_float2(0.f, 0.f);
-        zgemm<float>(s, n, n, n, nkc, one, h32, n, nn, 0, z32, n, nn, 0, zero, p32, n, nn);
-        zgemm<float>(s, n, n, n, nkc, one, s32, n, nn, 0, z32, n, nn, 0, zero, h32, n, nn);   // dS Z over dH32
+        // SIMT FMA pipe, not the tensor cores: the MMA accumulator's rounding
+        // is biased toward zero, and a relative bias of ~1e-6 in P shifts the
+        // pressure coherently by ~1e-7 Ry/bohr^3
+        zgemm_simt<float>(s, n, n, n, nkc, one, h32, n, nn, 0, z32, n, nn, 0, zero, p32, n, nn);
+        zgemm_simt<float>(s, n, n, n, nkc, one, s32, n, nn, 0, z32, n, nn, 0, zero, h32, n, nn);   // dS Z over dH32
         launch_hf_dots32(s, z32, p32, h32, eig, deig, n, nkc);
     }
     return cudaGetLastError() == cudaSuccess ? NRLTB_OK : NRLTB_E_CUDA;

@@ -15,6 +15,7 @@ struct RefineWork {
     float2 *XE;             // X E (FP32)
     double *lam;            // refined eigenvalues
     int *cl;                // cluster id per eigenvalue
+    void *oz;               // digit planes of the tensor-core products (ozaki.cuh)
 };
 
 bool refine_available();
@@ -24,7 +25,8 @@ void refine_work_carve(RefineWork &w, void *base, int n, int batch);
 // accuracy); writes refined eigenvalues (ascending) and, if Z != NULL, FP64
 // eigenvectors.  status[k] gets NRLTB_K_NOT_CONVERGED when a cluster exceeds the
 // handled size.
-void refine_eigen(cudaStream_t s, RefineWork &w, const double2 *H, const double2 *S, const float2 *X,
+// X is rounded in place to the representation the tensor-core products use.
+void refine_eigen(cudaStream_t s, RefineWork &w, const double2 *H, const double2 *S, float2 *X,
                   double *eig, double2 *Z, int *status);
 
 // Hellmann-Feynman shifts deig = diag(Z^H dH Z) - eig * diag(Z^H dS Z) for nkc

@@ -105,6 +105,10 @@ GPU_SYMBOLS = [
     # measurement hooks (include/nrltb_bench.h)
     ("nrltb_bench_peak", C.c_int, [_vp, C.c_int, _dp]),
     ("nrltb_bench_zgemm", C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_int, _dp, _dp]),
+    ("nrltb_bench_refprod", C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_int, _dp, _dp]),
+    ("nrltb_bench_refprod_run", C.c_int, [_vp, C.c_int, C.c_int, C.c_int, _vp, _vp, _vp]),
+    ("nrltb_bench_cgemm_run", C.c_int, [_vp] + [C.c_int] * 9 + [_vp, _vp, _vp, C.c_int, _vp, C.c_int, _vp,
+                                                                  C.c_int]),
 ]
 
 HOST_SYMBOLS = [
