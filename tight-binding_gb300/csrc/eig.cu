@@ -2,6 +2,7 @@
 #include <algorithm>
 #include <cfloat>
 #include "eig.cuh"
+#include "tri_panel.cuh"
 
 namespace nrltb {
 
@@ -39,12 +40,14 @@ template <typename T> void eig_work_carve(EigWork<T> &w, void *base, int n, int 
     w.pp = (C2 *)take(sizeof(C2) * 2 * EIG_NB * nb);
     w.part = (C2 *)take(sizeof(C2) * (2 * EIG_NB + 2) * ncta * nb);
     w.sc = (C2 *)take(sizeof(C2) * 4 * nb);
-    w.Tt = (C2 *)take(sizeof(C2) * EIG_NB * (size_t)std::max(n, 2 * EIG_NB) * nb);
+    const size_t nbw = (size_t)std::min(EIG_WY, n);
+    w.Tt = (C2 *)take(sizeof(C2) * std::max(EIG_NB * (size_t)std::max(n, 2 * EIG_NB), 2 * nbw * nbw) * nb);
     w.Xt = (C2 *)take(sizeof(C2) * EIG_NB * (size_t)n * nb);
     w.d = (double *)take(sizeof(double) * n * nb);
     w.e = (double *)take(sizeof(double) * n * nb);
     w.lam = (double *)take(sizeof(double) * n * nb);
-    w.ylu = (double *)take(sizeof(double) * 5 * nn * nb);
+    // inverse iteration: 6 arrays of n per thread slot, 64 cdiv(n, 64) slots per matrix
+    w.ylu = (double *)take(sizeof(double) * 6 * (size_t)n * (64 * (size_t)cdiv(n, 64)) * nb);
     w.yvec = (double *)take(sizeof(double) * nn * nb);
     w.perm = (int *)take(sizeof(int) * 4 * n * nb);
     w.counter = (unsigned *)take(sizeof(unsigned) * nb);
@@ -473,11 +476,30 @@ __device__ inline double hash_unit(unsigned a, unsigned b)
     return (double)(h & 0xFFFFFF) / (double)0x800000 - 1.0;   // [-1, 1)
 }
 
-// Tridiagonal eigenvectors by inverse iteration (FP64).  One thread per
-// cluster of close eigenvalues inside an unreduced block; members of a cluster
-// are re-orthogonalised against the previous members after every solve.
+// An array of one thread whose elements are `st` apart (thread-interleaved
+// scratch: a warp's accesses to the same element index are coalesced).
+template <typename TB> struct Strided {
+    TB *p;
+    long st;
+    __device__ Strided(TB *p_, long st_) : p(p_), st(st_) {}
+    __device__ TB &operator[](long k) const { return p[k * st]; }
+    __device__ Strided operator+(long k) const { return Strided(p + k * st, st); }
+};
+
+// Tridiagonal eigenvectors by inverse iteration in TB arithmetic (FP64 for
+// the FP64 form, FP32 for the FP32 solve of the mixed form), one thread per
+// eigenvalue (dstein's dgttrf/dgtts2 steps, 3 iterations from a pseudo-random
+// start), written to the eigenvalue's column of Y.  Members of a cluster of
+// close eigenvalues iterate independently; k_tri_cluster_orth then
+// orthonormalises each cluster.  An exactly degenerate cluster's iterates are
+// independent random combinations inside its invariant subspace, and a member
+// separated by g from the others keeps only ~eps ||T|| / g of their
+// directions, so orthonormalising after the iteration spans the same subspace
+// as re-orthogonalising during it.  Scratch: 6 arrays of n TB per thread,
+// interleaved across the launch's threads.
+template <typename TB>
 __global__ void k_tri_invit(const double *dd, const double *ee, const double *lamloc, const int *blk,
-                            const int *rank, double *yvec, double *scratch, int n, double ctol)
+                            const int *rank, double *yvec, TB *scratch, int n)
 {
     const int b = blockIdx.y;
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
@@ -488,78 +510,128 @@ __global__ void k_tri_invit(const double *dd, const double *ee, const double *la
     double tnorm = 0;
     for (int k = b0; k <= b1; ++k)
         tnorm = fmax(tnorm, fabs(d[k]) + (k > b0 ? fabs(e[k - 1]) : 0.0) + (k < b1 ? fabs(e[k]) : 0.0));
+    // thread-interleaved scratch: element k of array a at S[(a n + k) NT]
+    const long NT = (long)gridDim.y * gridDim.x * blockDim.x;
+    Strided<TB> S(scratch + ((long)blockIdx.y * gridDim.x + blockIdx.x) * blockDim.x + threadIdx.x, NT);
+    // multipliers, 1 / pivots, first and second super-diagonals of U, pivot flags, iterate
+    Strided<TB> DL = S, RG = S + n, DU = S + 2 * n, DU2 = S + 3 * n, PV = S + 4 * n, v = S + 5 * n;
+    const TB tiny = eps_of<TB>() * TB(2) * TB(fmax(tnorm, (double)tiny_of<TB>()));
+    const TB lam = TB(L[r]);
+    auto pivot = [&](TB g) { return (fabs(g) < tiny) ? ((g < TB(0)) ? -tiny : tiny) : g; };
+    // factor T_block - lam I = P L U (dgttrf), the running row carried in registers
+    {
+        TB dcur = TB(d[b0]) - lam, ducur = (len > 1) ? TB(e[b0]) : TB(0);
+        for (int k = 0; k < len - 1; ++k) {
+            const TB dlk = TB(e[b0 + k]);
+            TB dnext = TB(d[b0 + k + 1]) - lam;
+            TB dunext = (k < len - 2) ? TB(e[b0 + k + 1]) : TB(0);
+            if (fabs(dcur) >= fabs(dlk)) {
+                const TB f = (dcur != TB(0)) ? dlk / dcur : TB(0);
+                DL[k] = f; RG[k] = TB(1) / pivot(dcur); DU[k] = ducur; DU2[k] = TB(0); PV[k] = TB(0);
+                dnext -= f * ducur;
+            } else {
+                const TB f = dcur / dlk;
+                DL[k] = f; RG[k] = TB(1) / pivot(dlk); DU[k] = dnext; DU2[k] = dunext; PV[k] = TB(1);
+                dnext = ducur - f * dnext;
+                dunext = -f * dunext;
+            }
+            dcur = dnext;
+            ducur = dunext;
+        }
+        RG[len - 1] = TB(1) / pivot(dcur);
+    }
+    for (int k = 0; k < len; ++k) v[k] = TB(hash_unit((unsigned)(b * 7919 + r), (unsigned)k));
+    for (int it = 0; it < 3; ++it) {
+        // solve: apply P and L (running element in a register)
+        TB vc = v[0];
+        for (int k = 0; k < len - 1; ++k) {
+            const TB vn = v[k + 1], f = DL[k];
+            if (PV[k] == TB(0)) { v[k] = vc; vc = vn - f * vc; }
+            else { v[k] = vn; vc = vc - f * vn; }
+        }
+        v[len - 1] = vc;
+        // U back-substitution (the two following elements in registers)
+        TB x1 = v[len - 1] * RG[len - 1], x2 = TB(0);
+        v[len - 1] = x1;
+        for (int k = len - 2; k >= 0; --k) {
+            const TB xk = (v[k] - DU[k] * x1 - DU2[k] * x2) * RG[k];
+            v[k] = xk;
+            x2 = x1;
+            x1 = xk;
+        }
+        TB nrm = 0;
+        for (int k = 0; k < len; ++k) nrm += v[k] * v[k];
+        nrm = sqrt(nrm);
+        const TB inv = (nrm > TB(0)) ? TB(1) / nrm : TB(0);
+        for (int k = 0; k < len; ++k) v[k] *= inv;
+    }
+    // sign convention: largest component positive
+    int kmax = 0;
+    TB vmax = TB(-1);
+    for (int k = 0; k < len; ++k) {
+        const TB a = fabs(v[k]);
+        if (a > vmax) { vmax = a; kmax = k; }
+    }
+    const double sg = (v[kmax] < TB(0)) ? -1.0 : 1.0;
+    double *z = yvec + (long)b * n * n + (long)rank[(long)b * n + r] * n;
+    for (int k = 0; k < n; ++k) z[k] = (k >= b0 && k <= b1) ? sg * (double)v[k - b0] : 0.0;
+}
+
+// Orthonormalise each cluster of eigenvalues closer than ctol ||T|| (within
+// an unreduced block) by modified Gram-Schmidt, twice; one warp per
+// eigenvalue, the warp of a cluster's first member does the work.
+__global__ void __launch_bounds__(256) k_tri_cluster_orth(const double *dd, const double *ee, const double *lamloc,
+                                                          const int *blk, const int *rank, double *yvec, int n,
+                                                          double ctol)
+{
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int b = blockIdx.y, r = blockIdx.x * 8 + warp;
+    if (r >= n) return;   // warp-uniform
+    const double *d = dd + (long)b * n, *e = ee + (long)b * n, *L = lamloc + (long)b * n;
+    const int b0 = blk[((long)b * n + r) * 2], b1 = blk[((long)b * n + r) * 2 + 1];
+    const int len = b1 - b0 + 1;
+    double tnorm = 0;
+    for (int k = b0 + lane; k <= b1; k += 32)
+        tnorm = fmax(tnorm, fabs(d[k]) + (k > b0 ? fabs(e[k - 1]) : 0.0) + (k < b1 ? fabs(e[k]) : 0.0));
+    for (int o = 16; o > 0; o >>= 1) tnorm = fmax(tnorm, __shfl_xor_sync(0xffffffffu, tnorm, o));
     const double gap = ctol * fmax(tnorm, DBL_MIN);
-    // only the first member of a cluster works
-    if (r > b0 && L[r] - L[r - 1] < gap) return;
+    if (r > b0 && L[r] - L[r - 1] < gap) return;   // not the first member
     int rend = r;
     while (rend < b1 && L[rend + 1] - L[rend] < gap) ++rend;
+    if (rend == r) return;
     double *Y = yvec + (long)b * n * n;
-    double *S = scratch + ((long)b * n + r) * 5 * (long)n;
-    double *dl = S, *dg = S + n, *du = S + 2 * n, *du2 = S + 3 * n, *x = S + 4 * n;   // x: pivot flags
-    const double tiny = DBL_EPSILON * fmax(tnorm, DBL_MIN);
     for (int m = r; m <= rend; ++m) {
-        const double lam = L[m];
-        // factor T_block - lam I = P L U (dgttrf)
-        for (int k = 0; k < len; ++k) {
-            dg[k] = d[b0 + k] - lam;
-            if (k < len - 1) { dl[k] = e[b0 + k]; du[k] = e[b0 + k]; du2[k] = 0.0; }
-        }
-        for (int k = 0; k < len - 1; ++k) {
-            if (fabs(dg[k]) >= fabs(dl[k])) {
-                double f = (dg[k] != 0.0) ? dl[k] / dg[k] : 0.0;
-                dl[k] = f;
-                dg[k + 1] = dg[k + 1] - f * du[k];
-                x[k] = 0.0;     // no interchange
-            } else {
-                double f = dg[k] / dl[k];
-                dg[k] = dl[k];
-                dl[k] = f;
-                double t = du[k];
-                du[k] = dg[k + 1];
-                dg[k + 1] = t - f * dg[k + 1];
-                if (k < len - 2) { du2[k] = du[k + 1]; du[k + 1] = -f * du[k + 1]; }
-                x[k] = 1.0;     // interchange
-            }
-        }
-        for (int k = 0; k < len; ++k)
-            if (fabs(dg[k]) < tiny) dg[k] = (dg[k] < 0.0) ? -tiny : tiny;
-        // the solution vector lives in Y's column for this eigenvalue
-        double *z = Y + (long)rank[(long)b * n + m] * n;
-        for (int k = 0; k < n; ++k) z[k] = 0.0;
-        double *v = z + b0;
-        for (int k = 0; k < len; ++k) v[k] = hash_unit((unsigned)(b * 7919 + m), (unsigned)k);
-        for (int it = 0; it < 3; ++it) {
-            // solve: apply P and L
-            for (int k = 0; k < len - 1; ++k) {
-                if (x[k] == 0.0) {
-                    v[k + 1] = v[k + 1] - dl[k] * v[k];
-                } else {
-                    double t = v[k];
-                    v[k] = v[k + 1];
-                    v[k + 1] = t - dl[k] * v[k + 1];
-                }
-            }
-            // U back-substitution
-            v[len - 1] = v[len - 1] / dg[len - 1];
-            if (len > 1) v[len - 2] = (v[len - 2] - du[len - 2] * v[len - 1]) / dg[len - 2];
-            for (int k = len - 3; k >= 0; --k) v[k] = (v[k] - du[k] * v[k + 1] - du2[k] * v[k + 2]) / dg[k];
-            // re-orthogonalise against earlier cluster members
+        double *v = Y + (long)rank[(long)b * n + m] * n + b0;
+        for (int pass = 0; pass < 2; ++pass) {
             for (int p = r; p < m; ++p) {
                 const double *zp = Y + (long)rank[(long)b * n + p] * n + b0;
-                double s = 0;
-                for (int k = 0; k < len; ++k) s += zp[k] * v[k];
-                for (int k = 0; k < len; ++k) v[k] -= s * zp[k];
+                double sdot = 0;
+                for (int k = lane; k < len; k += 32) sdot += zp[k] * v[k];
+                sdot = warp_sum(sdot);
+                for (int k = lane; k < len; k += 32) v[k] -= sdot * zp[k];
+                __syncwarp();
             }
-            double nrm = 0;
-            for (int k = 0; k < len; ++k) nrm += v[k] * v[k];
-            nrm = sqrt(nrm);
-            double inv = (nrm > 0) ? 1.0 / nrm : 0.0;
-            for (int k = 0; k < len; ++k) v[k] *= inv;
         }
-        // sign convention: largest component positive
+        double nrm = 0;
+        for (int k = lane; k < len; k += 32) nrm += v[k] * v[k];
+        nrm = sqrt(warp_sum(nrm));
+        const double inv = (nrm > 0) ? 1.0 / nrm : 0.0;
+        // sign convention: the first largest component positive
+        double vmax = -1.0;
         int kmax = 0;
-        for (int k = 1; k < len; ++k) if (fabs(v[k]) > fabs(v[kmax])) kmax = k;
-        if (v[kmax] < 0) for (int k = 0; k < len; ++k) v[k] = -v[k];
+        for (int k = lane; k < len; k += 32) {
+            const double a = fabs(v[k]);
+            if (a > vmax) { vmax = a; kmax = k; }
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            const double ov = __shfl_xor_sync(0xffffffffu, vmax, o);
+            const int ok = __shfl_xor_sync(0xffffffffu, kmax, o);
+            if (ov > vmax || (ov == vmax && ok < kmax)) { vmax = ov; kmax = ok; }
+        }
+        const double sg = (v[kmax] < 0) ? -inv : inv;
+        __syncwarp();
+        for (int k = lane; k < len; k += 32) v[k] *= sg;
+        __syncwarp();
     }
 }
 
@@ -574,37 +646,31 @@ __global__ void k_real_to_cplx(const double *y, C2 *z, long count)
     }
 }
 
-// compact-WY T factor of one panel: T[0:c, c] = -tau_c T[0:c,0:c] G[0:c, c], T[c][c] = tau_c
+// compact-WY T factor of a block of jb <= EIG_WY reflectors (G = Vb^H Vb and T
+// column-major nbw x nbw per matrix, in global memory): column by column,
+// T[0:c, c] = -tau_c T[0:c, 0:c] G[0:c, c], T[c, c] = tau_c (LAPACK's larft,
+// forward columnwise).  One CTA of EIG_WY threads per matrix, thread = row.
 template <typename T>
-__global__ void k_larft(const typename cplx<T>::t *G, typename cplx<T>::t *Tm, const typename cplx<T>::t *tau,
-                        int n, int j0, int jb)
+__global__ void __launch_bounds__(EIG_WY) k_larft_wy(const typename cplx<T>::t *G, typename cplx<T>::t *Tm,
+                                                     const typename cplx<T>::t *tau, int n, int j0, int jb, int nbw)
 {
     typedef typename cplx<T>::t C2;
-    __shared__ C2 t[EIG_NB][EIG_NB + 1];   // t[col][row]
-    __shared__ C2 g[EIG_NB][EIG_NB + 1];
-    const int b = blockIdx.x, tid = threadIdx.x;
-    const C2 *Gb = G + (long)b * EIG_NB * EIG_NB;
-    for (int e = tid; e < jb * jb; e += blockDim.x) {
-        int rr = e % jb, cc = e / jb;
-        g[cc][rr] = Gb[rr + cc * EIG_NB];
-        t[cc][rr] = cmk<T>(0, 0);
-    }
-    __syncthreads();
+    __shared__ C2 g[EIG_WY];
+    const int b = blockIdx.x, r = threadIdx.x;
+    const C2 *Gb = G + (long)b * nbw * nbw;
+    C2 *Tb = Tm + (long)b * nbw * nbw;
     for (int c = 0; c < jb; ++c) {
-        C2 tc = tau[(long)b * n + j0 + c];
-        // thread r < c: t[c][r] = -tau_c * sum_{k=r}^{c-1} t[k][r] g[c][k]
-        C2 s = cmk<T>(0, 0);
-        if (tid < c)
-            for (int k = tid; k < c; ++k) cfma(s, t[k][tid], g[c][k]);
+        if (r < c) g[r] = Gb[r + (long)c * nbw];
         __syncthreads();
-        if (tid < c) t[c][tid] = cscale(cmul(tc, s), T(-1));
-        if (tid == c) t[c][c] = tc;
+        const C2 tc = tau[(long)b * n + j0 + c];
+        if (r < c) {
+            C2 acc = cmk<T>(0, 0);
+            for (int k = r; k < c; ++k) cfma(acc, Tb[r + (long)k * nbw], g[k]);
+            Tb[r + (long)c * nbw] = cscale(cmul(tc, acc), T(-1));
+        } else if (r == c) {
+            Tb[c + (long)c * nbw] = tc;
+        }
         __syncthreads();
-    }
-    C2 *Tb = Tm + (long)b * EIG_NB * EIG_NB;
-    for (int e = tid; e < jb * jb; e += blockDim.x) {
-        int rr = e % jb, cc = e / jb;
-        Tb[rr + cc * EIG_NB] = t[cc][rr];
     }
 }
 
@@ -658,23 +724,28 @@ void eig_solve(cudaStream_t s, EigWork<T> &w, const double2 *H, const double2 *S
     // 3. A = Wi H Wi^H (lower tiles)
     zgemm<T>(s, n, n, n, B, one, w.A, ld, ms, 0, w.Wi, ld, ms, 1, zero, w.Y, ld, ms, 0, 1, 0);
     zgemm<T>(s, n, n, n, B, one, w.Wi, ld, ms, 0, w.Y, ld, ms, 0, zero, w.A, ld, ms, 1, 0, 1);
-    // 4. tridiagonalisation
-    const int ncta = cdiv(n, EIG_ROWS);
+    // 4. tridiagonalisation: one cluster launch per panel (tri_panel.cuh); the
+    //    per-column launch chain below is the path for devices or sizes where
+    //    such a cluster cannot be scheduled
+    bool clusters = true;
     for (int j0 = 0; j0 < n; j0 += EIG_NB) {
         const int jb = std::min(EIG_NB, n - j0);
-        for (int c = 0; c < jb; ++c) {
-            const int i = j0 + c;
-            const int nA = cdiv(n - i, EIG_ROWS);
-            NRLTB_LAUNCH(k_tri_colupd<T>, dim3(nA, B), EIG_ROWS, 0, s, w, i, j0, nA);
-            if (i == n - 1) break;
-            const int nB = cdiv(n - i - 1, EIG_ROWS);
-            NRLTB_LAUNCH(k_tri_vdots<T>, dim3(nB, B), EIG_ROWS, 0, s, w, i, j0, nB);
-            NRLTB_LAUNCH(k_tri_hemv<T>, dim3(cdiv(n - i - 1, 32), B), 256, 0, s, w, i);
-            NRLTB_LAUNCH(k_tri_wupd<T>, dim3(nB, B), EIG_ROWS, 0, s, w, i, j0, nB);
+        if (clusters) clusters = tri_panel_launch<T>(s, w, j0, jb);
+        if (!clusters) {
+            for (int c = 0; c < jb; ++c) {
+                const int i = j0 + c;
+                const int nA = cdiv(n - i, EIG_ROWS);
+                NRLTB_LAUNCH(k_tri_colupd<T>, dim3(nA, B), EIG_ROWS, 0, s, w, i, j0, nA);
+                if (i == n - 1) break;
+                const int nB = cdiv(n - i - 1, EIG_ROWS);
+                NRLTB_LAUNCH(k_tri_vdots<T>, dim3(nB, B), EIG_ROWS, 0, s, w, i, j0, nB);
+                NRLTB_LAUNCH(k_tri_hemv<T>, dim3(cdiv(n - i - 1, 32), B), 256, 0, s, w, i);
+                NRLTB_LAUNCH(k_tri_wupd<T>, dim3(nB, B), EIG_ROWS, 0, s, w, i, j0, nB);
+            }
+            const int last = std::min(j0 + jb - 1, n - 2);
+            if (last >= j0) NRLTB_LAUNCH(k_tri_wfinal<T>, dim3(cdiv(n, 256), B), 256, 0, s, w, last, last - j0);
         }
-        const int last = std::min(j0 + jb - 1, n - 2);
-        if (last < j0) break;
-        NRLTB_LAUNCH(k_tri_wfinal<T>, dim3(cdiv(n, 256), B), 256, 0, s, w, last, last - j0);
+        if (std::min(j0 + jb - 1, n - 2) < j0) break;
         const int t0 = j0 + jb, rem = n - t0;
         if (rem > 0) {
             C2 *Vp = w.V + t0 + (long)j0 * ld, *Wpp = w.Wp + t0;
@@ -682,7 +753,6 @@ void eig_solve(cudaStream_t s, EigWork<T> &w, const double2 *H, const double2 *S
             zgemm<T>(s, rem, rem, jb, B, mone, Vp, ld, ms, 0, Wpp, n, (long)n * EIG_NB, 1, one, At, ld, ms, 0, 0, 1);
             zgemm<T>(s, rem, rem, jb, B, mone, Wpp, n, (long)n * EIG_NB, 0, Vp, ld, ms, 1, one, At, ld, ms, 0, 0, 1);
         }
-        (void)ncta;
     }
     // 5. tridiagonal eigenproblem (FP64 inverse iteration; bisection in T)
     double *lamloc = (double *)w.Xt;   // free at this point: n doubles per matrix fit
@@ -695,27 +765,34 @@ void eig_solve(cudaStream_t s, EigWork<T> &w, const double2 *H, const double2 *S
     }
     if (!vectors) return;
     {
-        dim3 g(cdiv(n, 64), B);
-        const double ctol = (sizeof(T) == 8) ? 1e-9 : 1e-5;
-        NRLTB_LAUNCH(k_tri_invit, g, 64, 0, s, w.d, w.e, lamloc, blk, rank, w.yvec, w.ylu, n, ctol);
+        // eigenvalues closer than ctol ||T|| are orthonormalised as one cluster
+        // (LAPACK's dstein uses 1e-3 ||T||; outside a cluster the vectors'
+        // overlap is ~ eps ||T|| / gap <= 1e-11 for FP64)
+        const double ctol = 1e-5;
+        // 64 threads per CTA: cdiv(n, 64) * 64 * B thread slots <= the scratch carve's 64 cdiv(n, 64) n B
+        NRLTB_LAUNCH(k_tri_invit<T>, dim3(cdiv(n, 64), B), 64, 0, s, w.d, w.e, lamloc, blk, rank, w.yvec,
+                     (T *)w.ylu, n);
+        NRLTB_LAUNCH(k_tri_cluster_orth, dim3(cdiv(n, 8), B), 256, 0, s, w.d, w.e, lamloc, blk, rank, w.yvec, n,
+                     ctol);
         NRLTB_LAUNCH(k_real_to_cplx<C2>, 1184, 256, 0, s, w.yvec, w.Y, cnt);
     }
-    // 6. Z = Q Y, panels applied last to first; then X = Wi^H Z
+    // 6. Z = Q Y: blocks of EIG_WY reflectors applied last to first as
+    //    Y[j0+1:, :] -= Vb (Tb (Vb^H Y[j0+1:, :])), Vb = V[j0+1:, j0:j0+jb] (the
+    //    reflectors of the block vanish above row j0+1); then X = Wi^H Z.
+    //    A (free after step 4) holds Vb^H Y, L (free after step 2) holds Tb Vb^H Y.
     {
-        const int jlast = ((n - 2) / EIG_NB) * EIG_NB;
-        for (int j0 = (n >= 2 ? jlast : -1); j0 >= 0; j0 -= EIG_NB) {
-            const int jb = std::min(EIG_NB, n - 1 - j0);
-            if (jb <= 0) continue;
-            C2 *Vp = w.V + (long)j0 * ld;                    // n x jb, zero above the unit diagonal
-            C2 *G = w.Tt, *Tf = w.Tt + (long)EIG_NB * EIG_NB * B;
-            // G = Vp^H Vp, T factor, Xt = Vp^H Z, Xt = T Xt, Z -= Vp Xt
-            zgemm<T>(s, jb, jb, n, B, one, Vp, ld, ms, 1, Vp, ld, ms, 0, zero, G, EIG_NB, (long)EIG_NB * EIG_NB);
-            NRLTB_LAUNCH(k_larft<T>, B, 64, 0, s, G, Tf, w.tau, n, j0, jb);
-            zgemm<T>(s, jb, n, n, B, one, Vp, ld, ms, 1, w.Y, ld, ms, 0, zero, w.Xt, EIG_NB, (long)EIG_NB * n);
-            C2 *X2 = w.Wp;   // jb x n per matrix (Wp is n x EIG_NB = same size)
-            zgemm<T>(s, jb, n, jb, B, one, Tf, EIG_NB, (long)EIG_NB * EIG_NB, 0, w.Xt, EIG_NB, (long)EIG_NB * n, 0,
-                     zero, X2, EIG_NB, (long)EIG_NB * n, 2, 0, 0);
-            zgemm<T>(s, n, n, jb, B, mone, Vp, ld, ms, 0, X2, EIG_NB, (long)EIG_NB * n, 0, one, w.Y, ld, ms);
+        const int nbw = std::min(EIG_WY, n), nref = n - 1;
+        C2 *G = w.Tt, *Tf = w.Tt + (long)nbw * nbw * B;
+        const long sG = (long)nbw * nbw, sX = (long)nbw * n;
+        for (int j0 = (nref >= 1 ? ((nref - 1) / nbw) * nbw : -1); j0 >= 0; j0 -= nbw) {
+            const int jb = std::min(nbw, nref - j0), mb = n - j0 - 1;
+            const C2 *Vb = w.V + (j0 + 1) + (long)j0 * ld;
+            C2 *Yb = w.Y + (j0 + 1);
+            zgemm<T>(s, jb, jb, mb, B, one, Vb, ld, ms, 1, Vb, ld, ms, 0, zero, G, nbw, sG);
+            NRLTB_LAUNCH(k_larft_wy<T>, B, EIG_WY, 0, s, G, Tf, w.tau, n, j0, jb, nbw);
+            zgemm<T>(s, jb, n, mb, B, one, Vb, ld, ms, 1, Yb, ld, ms, 0, zero, w.A, nbw, sX);
+            zgemm<T>(s, jb, n, jb, B, one, Tf, nbw, sG, 0, w.A, nbw, sX, 0, zero, w.L, nbw, sX, 2, 0, 0);
+            zgemm<T>(s, mb, n, jb, B, mone, Vb, ld, ms, 0, w.L, nbw, sX, 0, one, Yb, ld, ms);
         }
         zgemm<T>(s, n, n, n, B, one, w.Wi, ld, ms, 1, w.Y, ld, ms, 0, zero, X, ld, ms, 2, 0, 0);
     }

@@ -13,10 +13,11 @@
 //      column update, reflector, lower-triangle Hermitian mat-vec and w update;
 //      per panel a rank-2nb trailing update as two GEMMs.
 //   5. T (real symmetric) eigenvalues by Sturm-count bisection per unreduced
-//      block; eigenvectors by inverse iteration with re-orthogonalisation inside
-//      clusters of close eigenvalues (dstein's scheme), in FP64.
-//   6. X = W^H Q Y: blocked compact-WY application of the reflectors and a
-//      triangular GEMM.
+//      block; eigenvectors by inverse iteration (dstein's factorisation and
+//      solves) in FP64, each cluster of close eigenvalues orthonormalised
+//      afterwards.
+//   6. X = W^H Q Y: compact-WY application of the reflectors in blocks of
+//      EIG_WY (rows above each block skipped) and a triangular GEMM.
 // Every stage runs on all matrices of the batch at once (grid.z / grid.y =
 // matrix).  Non-positive-definite S is reported per matrix (status 1), as
 // diag.f:429-455 does with ioverr, without stopping the batch.
@@ -28,6 +29,7 @@ namespace nrltb {
 
 constexpr int EIG_NB = 32;          // panel width (Cholesky, inverse, tridiagonal)
 constexpr int EIG_ROWS = 128;       // rows per CTA in the column kernels
+constexpr int EIG_WY = 128;         // reflectors per block of the back-transform
 
 // Device workspace for one batch of `batch` matrices of order n.
 template <typename T> struct EigWork {
@@ -50,7 +52,7 @@ template <typename T> struct EigWork {
     C2 *Xt;                         // EIG_NB x n per matrix
     double *d, *e;                  // tridiagonal, n per matrix
     double *lam;                    // eigenvalues, n per matrix (ascending)
-    double *ylu;                    // inverse-iteration scratch, 5 n per thread-slot
+    double *ylu;                    // inverse-iteration scratch, 5 n per thread
     double *yvec;                   // real eigenvectors of T, n x n per matrix
     int *perm;                      // eigenvalue -> block bookkeeping, 3 n per matrix
     unsigned *counter;              // per-matrix ticket counters (last-CTA pattern)

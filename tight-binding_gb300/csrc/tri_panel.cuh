@@ -1,0 +1,421 @@
+// tri_panel.cuh -- one panel (up to EIG_NB columns) of the blocked Householder
+// tridiagonalisation A = Q T Q^H, with one thread-block cluster per matrix.
+//
+// The per-column chain of zhetrd/zlatrd (column update, reflector, Hermitian
+// mat-vec y = A v of the trailing matrix, w = tau (y - V p1 - W p2),
+// alpha = -tau/2 w^H v) is latency bound when each step is its own launch.
+// Here the CL CTAs of a cluster own the matrix rows in 32-row tiles (tile t
+// belongs to CTA t mod CL) and run every column of the panel in one launch,
+// with three cluster barriers per column.  The cluster-wide sums (|x|^2 of
+// the reflector, W^H v / V^H v, w^H v) are per-CTA partials in shared memory,
+// read by every CTA through distributed shared memory in rank order, so all
+// CTAs derive identical scalars without a further barrier and the result does
+// not depend on scheduling.
+//
+// The mat-vec reads only A's lower triangle: for an own row tile R and a
+// column tile S > R, the lower tile (S, R) is read (coalesced) and its
+// conjugate transpose applied with a warp butterfly (transpose-reduce), so a
+// CTA forms the whole y of its own rows without cross-CTA traffic.
+//
+// The CTA keeps its own rows of the panel's V and W columns (and of w') in
+// shared memory, so the per-column updates read no global memory but the
+// current column of A, row i and the mat-vec tiles.
+//
+// Every CTA executes the same sequence of barriers: control flow that
+// encloses a barrier depends only on kernel arguments.
+#pragma once
+#include <cooperative_groups.h>
+#include "eig.cuh"
+
+namespace nrltb {
+
+constexpr int TP_THREADS = 256, TP_WARPS = TP_THREADS / 32;
+constexpr int TP_CL = 8;   // CTAs per cluster (portable size)
+
+// values per lane of one butterfly (16: two CTAs of 256 threads fit an SM)
+template <typename T> struct TpNV { static constexpr int v = 16; };
+
+// Transpose-reduce over the warp: lane l holds x[0..NV); afterwards x[0] of
+// lane l is sum over all lanes of x[u] with u = l >> (5 - log2 NV) (lanes that
+// share u hold the same total).
+template <int NV, typename C2>
+__device__ __forceinline__ void tp_butterfly(C2 (&x)[NV], int lane)
+{
+    int o = 16;
+#pragma unroll
+    for (int m = NV; m > 1; m >>= 1, o >>= 1) {
+        const bool up = (lane & o) != 0;
+#pragma unroll
+        for (int u = 0; u < m / 2; ++u) {
+            C2 send = up ? x[u] : x[u + m / 2];
+            C2 keep = up ? x[u + m / 2] : x[u];
+            keep.x += __shfl_xor_sync(0xffffffffu, send.x, o);
+            keep.y += __shfl_xor_sync(0xffffffffu, send.y, o);
+            x[u] = keep;
+        }
+    }
+    for (; o > 0; o >>= 1) {
+        x[0].x += __shfl_xor_sync(0xffffffffu, x[0].x, o);
+        x[0].y += __shfl_xor_sync(0xffffffffu, x[0].y, o);
+    }
+}
+
+template <typename T> struct TpSmem {
+    typedef typename cplx<T>::t C2;
+    C2 *vfull;      // v of the current column, all rows (32 T_)
+    C2 *acol;       // own rows: updated column, then v (32 nown)
+    C2 *ypart;      // per warp: partial y of the own rows (TP_WARPS x 32 nown)
+    C2 *Vs, *Ws;    // own rows of the panel's V and W columns (EIG_NB x 32 nown each)
+    C2 *wqs;        // own rows of w' of the previous column (32 nown)
+    C2 *wi, *vi;    // row i of the panel's W and V
+    C2 *p1, *p2;    // W^H v, V^H v (cluster sums)
+    C2 *pw;         // per-warp partials of W^H v | V^H v (TP_WARPS x 64)
+    C2 *p12part;    // this CTA's W^H v | V^H v (64)
+    C2 *a0;         // element i+1 of the updated column (owner CTA)
+    C2 *dotpart;    // this CTA's w^H v
+    T *normpart;    // this CTA's |x|^2
+    T *red;         // block_sum scratch
+};
+
+inline size_t tp_smem_bytes(int n, int csize, size_t c2)
+{
+    const int T_ = cdiv(n, 32), nown = cdiv(T_, TP_CL);
+    (void)csize;
+    return c2 * (32 * (size_t)T_ + 32 * (size_t)nown * (2 + TP_WARPS + 2 * EIG_NB) + 4 * 32 + TP_WARPS * 64 + 64 +
+                 2) +
+           2 * 16 * (TP_WARPS + 1) + 64;
+}
+
+template <typename T>
+__device__ __forceinline__ TpSmem<T> tp_carve(unsigned char *base, int n)
+{
+    typedef typename cplx<T>::t C2;
+    const int T_ = cdiv(n, 32), nown = cdiv(T_, TP_CL);
+    TpSmem<T> s;
+    C2 *p = (C2 *)base;
+    s.vfull = p; p += 32 * T_;
+    s.acol = p; p += 32 * nown;
+    s.ypart = p; p += 32 * nown * TP_WARPS;
+    s.Vs = p; p += 32 * nown * EIG_NB;
+    s.Ws = p; p += 32 * nown * EIG_NB;
+    s.wqs = p; p += 32 * nown;
+    s.wi = p; p += 32;
+    s.vi = p; p += 32;
+    s.p1 = p; p += 32;
+    s.p2 = p; p += 32;
+    s.pw = p; p += TP_WARPS * 64;
+    s.p12part = p; p += 64;
+    s.a0 = p; p += 1;
+    s.dotpart = p; p += 1;
+    T *q = (T *)p;
+    s.normpart = q; q += 2;
+    s.red = q;
+    return s;
+}
+
+// one 32 x 32 tile of the trailing mat-vec for own row tile R (own ordinal k)
+// and column tile S; contributions go to this warp's ypart slots of tile R
+template <typename T>
+__device__ __forceinline__ void tp_tile(const typename cplx<T>::t *A, long ld, int n, int lo, int R, int S,
+                                        const typename cplx<T>::t *vfull, typename cplx<T>::t *yp, int lane)
+{
+    typedef typename cplx<T>::t C2;
+    constexpr int NV = TpNV<T>::v;
+    const bool trans = S > R, diag = S == R;
+    const int rowt = trans ? S : R, colt = trans ? R : S;
+    const int r = 32 * rowt + lane;
+    const bool rv = r >= lo && r < n;
+    const C2 vr = vfull[r];
+    C2 yr = cmk<T>(0, 0);
+#pragma unroll 1
+    for (int h = 0; h < 32 / NV; ++h) {
+        C2 x[NV];
+#pragma unroll
+        for (int u = 0; u < NV; ++u) {
+            const int s = 32 * colt + h * NV + u;
+            const bool ok = rv && s >= lo && s < n && (!diag || s <= r);
+            C2 a = cmk<T>(0, 0);
+            if (ok) a = A[r + (long)s * ld];
+            if (!trans) cfma(yr, a, vfull[s]);
+            x[u] = cmk<T>(0, 0);
+            if (trans || (diag && s < r)) cfmac(x[u], a, vr);   // conj(a) v_r
+        }
+        if (trans || diag) {   // warp-uniform
+            tp_butterfly<NV>(x, lane);
+            constexpr int sh = (NV == 32) ? 0 : (NV == 16 ? 1 : 2);
+            if ((lane & ((1 << sh) - 1)) == 0) {
+                C2 &dst = yp[h * NV + (lane >> sh)];
+                dst = cadd(dst, x[0]);
+            }
+        }
+    }
+    if (!trans) yp[lane] = cadd(yp[lane], yr);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(TP_THREADS, 2) k_tri_panel(EigWork<T> w, int j0, int jb)
+{
+    typedef typename cplx<T>::t C2;
+    namespace cg = cooperative_groups;
+    constexpr int CL = TP_CL, NV = TpNV<T>::v;
+    extern __shared__ __align__(16) unsigned char tp_raw[];
+    cg::cluster_group cluster = cg::this_cluster();
+    const int q = (int)cluster.block_rank();
+    const int b = blockIdx.y, n = w.n, tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const long ld = w.ld;
+    const C2 *A = w.A + b * w.mstride;
+    C2 *V = w.V + b * w.mstride;
+    C2 *Wp = w.Wp + (long)b * n * EIG_NB, *wq = w.wq + (long)b * n;
+    const int T_ = cdiv(n, 32);
+    const int nown = (q < T_) ? (T_ - 1 - q) / CL + 1 : 0;
+    TpSmem<T> sm = tp_carve<T>(tp_raw, n);
+    const int ns = 32 * cdiv(T_, CL);   // row stride of Vs, Ws
+    const C2 zero = cmk<T>(0, 0);
+
+    C2 tau = zero, alpha = zero;
+    int c = 0;
+    for (; c < jb; ++c) {
+        const int i = j0 + c;
+        // ---- A: alpha of the previous column; row i of V, W; update column i ----
+        if (c > 0) {
+            C2 dot = zero;
+            for (int rk = 0; rk < CL; ++rk) dot = cadd(dot, *cluster.map_shared_rank(sm.dotpart, rk));
+            alpha = cscale(cmul(tau, dot), T(-0.5));
+        }
+        if (tid < c) {
+            sm.vi[tid] = V[i + (long)(j0 + tid) * ld];
+            sm.wi[tid] = (tid < c - 1) ? Wp[i + (long)tid * n] : cadd(wq[i], cmul(alpha, V[i + (long)(i - 1) * ld]));
+        }
+        __syncthreads();
+        T nrm2 = T(0);
+        for (int k = warp; k < nown; k += TP_WARPS) {
+            const int r = 32 * (q + CL * k) + lane;
+            if (r < i || r >= n) continue;
+            C2 wl = zero;
+            const int slot = 32 * k + lane;
+            if (c > 0) {
+                wl = cadd(sm.wqs[slot], cmul(alpha, sm.Vs[(c - 1) * ns + slot]));
+                Wp[r + (long)(c - 1) * n] = wl;
+                sm.Ws[(c - 1) * ns + slot] = wl;
+            }
+            C2 a = A[r + (long)i * ld];
+            // eight panel columns per round: their loads are issued together
+            for (int j8 = 0; j8 < c; j8 += 8) {
+                C2 vv[8], ww[8];
+#pragma unroll
+                for (int u = 0; u < 8; ++u) {
+                    const int j = j8 + u;
+                    vv[u] = zero;
+                    ww[u] = zero;
+                    if (j < c) {
+                        vv[u] = sm.Vs[j * ns + slot];
+                        ww[u] = sm.Ws[j * ns + slot];
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < 8; ++u)
+                    if (j8 + u < c) {
+                        a = csub(a, cmul(vv[u], cconj(sm.wi[j8 + u])));
+                        a = csub(a, cmul(ww[u], cconj(sm.vi[j8 + u])));
+                    }
+            }
+            sm.acol[32 * k + lane] = a;
+            if (r == i) w.d[(long)b * n + i] = (double)a.x;
+            if (r == i + 1) *sm.a0 = a;
+            if (r >= i + 2) nrm2 += a.x * a.x + a.y * a.y;
+        }
+        nrm2 = block_sum(nrm2, sm.red);
+        if (tid == 0) *sm.normpart = nrm2;
+        if (i == n - 1) break;   // last column of the matrix: d only (uniform)
+        cluster.sync();   // #1
+
+        // ---- B: reflector (every CTA, same order); v; partial W^H v, V^H v ----
+        T xn2 = T(0);
+        for (int rk = 0; rk < CL; ++rk) xn2 += *cluster.map_shared_rank(sm.normpart, rk);
+        const C2 al = *cluster.map_shared_rank(sm.a0, ((i + 1) / 32) % CL);
+        C2 scale = zero;
+        double beta;
+        tau = zero;
+        {
+            const T xnorm = sqrt(xn2);
+            if (xnorm == T(0) && al.y == T(0)) {
+                beta = (double)al.x;
+            } else {
+                T bb = sqrt(al.x * al.x + al.y * al.y + xnorm * xnorm);
+                bb = (al.x >= T(0)) ? -bb : bb;
+                tau = cmk<T>((bb - al.x) / bb, -al.y / bb);
+                const C2 den = cmk<T>(al.x - bb, al.y);   // 1 / (alpha - beta)
+                const T dd = den.x * den.x + den.y * den.y;
+                scale = cmk<T>(den.x / dd, -den.y / dd);
+                beta = (double)bb;
+            }
+        }
+        if (q == 0 && tid == 0) {
+            w.e[(long)b * n + i] = beta;
+            w.tau[(long)b * n + i] = tau;
+        }
+        if (q == 0)
+            for (int qq = tid; qq <= i; qq += TP_THREADS) V[qq + (long)i * ld] = zero;
+        for (int e = tid; e < TP_WARPS * 64; e += TP_THREADS) sm.pw[e] = zero;
+        __syncthreads();
+        for (int k = warp; k < nown; k += TP_WARPS) {
+            const int r = 32 * (q + CL * k) + lane;
+            const bool valid = r >= i + 1 && r < n;
+            C2 v = zero;
+            if (valid) {
+                v = (r == i + 1) ? cmk<T>(1, 0) : cmul(sm.acol[32 * k + lane], scale);
+                V[r + (long)i * ld] = v;
+            }
+            sm.acol[32 * k + lane] = v;
+            sm.Vs[c * ns + 32 * k + lane] = v;
+            // W^H v and V^H v over this warp's rows: column j in butterfly slot j
+#pragma unroll 1
+            for (int part = 0; part < 2; ++part) {
+#pragma unroll 1
+                for (int h = 0; h < 32 / NV; ++h) {
+                    C2 x[NV];
+#pragma unroll
+                    for (int u = 0; u < NV; ++u) {
+                        const int j = h * NV + u;
+                        x[u] = zero;
+                        if (valid && j < c) {
+                            const C2 m = part ? sm.Vs[j * ns + 32 * k + lane] : sm.Ws[j * ns + 32 * k + lane];
+                            cfmac(x[u], m, v);
+                        }
+                    }
+                    tp_butterfly<NV>(x, lane);
+                    constexpr int sh = (NV == 32) ? 0 : 1;
+                    if ((lane & ((1 << sh) - 1)) == 0) {
+                        C2 &dst = sm.pw[warp * 64 + part * 32 + h * NV + (lane >> sh)];
+                        dst = cadd(dst, x[0]);
+                    }
+                }
+            }
+        }
+        __syncthreads();
+        if (tid < 64) {
+            C2 s = zero;
+            for (int ww = 0; ww < TP_WARPS; ++ww) s = cadd(s, sm.pw[ww * 64 + tid]);
+            sm.p12part[tid] = s;
+        }
+        cluster.sync();   // #2
+
+        // ---- C: cluster sums p1, p2; full v; trailing mat-vec for own rows ----
+        if (tid < 64) {
+            C2 s = zero;
+            for (int rk = 0; rk < CL; ++rk) s = cadd(s, cluster.map_shared_rank(sm.p12part, rk)[tid]);
+            if (tid < 32) sm.p1[tid] = s; else sm.p2[tid - 32] = s;
+        }
+        for (int s = tid; s < 32 * T_; s += TP_THREADS)
+            sm.vfull[s] = (s >= i + 1 && s < n) ? V[s + (long)i * ld] : zero;
+        for (int e = tid; e < 32 * nown * TP_WARPS; e += TP_THREADS) sm.ypart[e] = zero;
+        __syncthreads();
+        {
+            const int tb = (i + 1) / 32, ncol = T_ - tb;
+            int k0 = 0;
+            while (k0 < nown && q + CL * k0 < tb) ++k0;
+            const int nitems = (nown - k0) * ncol;
+            C2 *yw = sm.ypart + warp * 32 * nown;
+            for (int it = warp; it < nitems; it += TP_WARPS) {
+                const int k = k0 + it / ncol, S = tb + it % ncol;
+                tp_tile<T>(A, ld, n, i + 1, q + CL * k, S, sm.vfull, yw + 32 * k, lane);
+            }
+        }
+        __syncthreads();
+
+        // ---- D: w' = tau (y - V p1 - W p2) for own rows; partial w'^H v ----
+        C2 dot = zero;
+        for (int k = warp; k < nown; k += TP_WARPS) {
+            const int r = 32 * (q + CL * k) + lane;
+            if (r < i + 1 || r >= n) continue;
+            C2 y = zero;
+            for (int ww = 0; ww < TP_WARPS; ++ww) y = cadd(y, sm.ypart[ww * 32 * nown + 32 * k + lane]);
+            for (int j8 = 0; j8 < c; j8 += 8) {
+                C2 vv[8], ww[8];
+#pragma unroll
+                for (int u = 0; u < 8; ++u) {
+                    const int j = j8 + u;
+                    vv[u] = zero;
+                    ww[u] = zero;
+                    if (j < c) {
+                        vv[u] = sm.Vs[j * ns + 32 * k + lane];
+                        ww[u] = sm.Ws[j * ns + 32 * k + lane];
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < 8; ++u)
+                    if (j8 + u < c) {
+                        y = csub(y, cmul(vv[u], sm.p1[j8 + u]));
+                        y = csub(y, cmul(ww[u], sm.p2[j8 + u]));
+                    }
+            }
+            y = cmul(tau, y);
+            wq[r] = y;
+            sm.wqs[32 * k + lane] = y;
+            cfmac(dot, y, sm.acol[32 * k + lane]);   // conj(w') v
+        }
+        if (q == 0)
+            for (int qq = tid; qq <= i; qq += TP_THREADS) wq[qq] = zero;
+        dot.x = block_sum(dot.x, sm.red);
+        dot.y = block_sum(dot.y, sm.red);
+        if (tid == 0) *sm.dotpart = dot;
+        cluster.sync();   // #3
+    }
+    // W[:, last] = w' + alpha v of the panel's last reflected column
+    if (c == jb) {
+        const int i = j0 + jb - 1;
+        C2 dot = zero;
+        for (int rk = 0; rk < CL; ++rk) dot = cadd(dot, *cluster.map_shared_rank(sm.dotpart, rk));
+        alpha = cscale(cmul(tau, dot), T(-0.5));
+        for (int k = warp; k < nown; k += TP_WARPS) {
+            const int r = 32 * (q + CL * k) + lane;
+            if (r >= n) continue;
+            const C2 v = (r > i) ? sm.Vs[(jb - 1) * ns + 32 * k + lane] : zero;
+            const C2 qv = (r > i) ? sm.wqs[32 * k + lane] : zero;
+            Wp[r + (long)(jb - 1) * n] = cadd(qv, cmul(alpha, v));
+        }
+    }
+    cluster.sync();   // no CTA leaves while others may read its shared memory
+}
+
+// Launches the panel kernel with cluster dimension TP_CL; returns false if a
+// cluster of this size and shared memory cannot be scheduled on the device.
+template <typename T>
+bool tri_panel_launch(cudaStream_t s, const EigWork<T> &w, int j0, int jb)
+{
+    // FP64: the mat-vec is bound by the FP64 pipe, which the per-column launch
+    // chain (every SM on every column) uses better than 8 CTAs per matrix
+    if (sizeof(T) == 8) return false;
+    const size_t smem = tp_smem_bytes(w.n, 0, sizeof(typename cplx<T>::t));
+    if (smem > 200 * 1024) return false;
+    static thread_local int checked_dev = -1;
+    static thread_local bool ok_dev = false;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = TP_CL;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3(TP_CL, w.batch, 1);
+    cfg.blockDim = dim3(TP_THREADS, 1, 1);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    if (cudaFuncSetAttribute(k_tri_panel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+        return false;
+    if (checked_dev != dev) {
+        int nclusters = 0;
+        ok_dev = cudaOccupancyMaxActiveClusters(&nclusters, k_tri_panel<T>, &cfg) == cudaSuccess && nclusters > 0;
+        checked_dev = dev;
+        cudaGetLastError();
+    }
+    if (!ok_dev) return false;
+    if (cudaLaunchKernelEx(&cfg, k_tri_panel<T>, w, j0, jb) != cudaSuccess) return false;
+    if (g_launch_counter) ++*g_launch_counter;
+    return true;
+}
+
+}  // namespace nrltb
