@@ -8,15 +8,17 @@
 // largest element, far below the FP32 eigensolver's own error), so the
 // products are formed for exactly the X every later step uses.
 // Every digit is an integer that bf16 holds exactly and every digit product is
-// <= 2^14.  For a 64-wide k chunk the sum over the (at most 3) digit pairs of
-// one weight 256^-(L+2), L = s + t, and over the two real products of a
-// complex component stays below 2^24, so the tensor core's FP32 accumulation
-// of one level and one chunk is exact.  Each chunk's level sums are folded,
+// <= 2^14.  A complex product takes three real ones (p1 = Ar Xr, p2 = Ai Xi,
+// p3 = (Ar + Ai)(Xr + Xi), digit sums <= 256 are exact in bf16 too).  For a
+// 64-wide k chunk each sum over the (at most 3) digit pairs of one weight
+// 256^-(L+2), L = s + t, stays below 2^24 (p3: 64 * 3 * 2^16), so the tensor
+// core's FP32 accumulation of one level and one chunk is exact, and so are
+// re = p1 - p2 and im = p3 - (p1 + p2) (both below 2^23 in magnitude).  Each chunk's level sums are folded,
 // scaled by 256^-(L+2), into a double-float (FP32 pair) accumulator.  Levels
 // L <= 5 are kept (15 digit pairs); the dropped ones and the 6-digit cut of A
 // are below 2^-48 of |A row| |X column| per term, the accuracy of the
-// double-float SIMT product this replaces.  15 digit pairs x 4 real products
-// = 60 bf16 MMAs per complex multiply-add, issued as mma.sync.m16n8k16.
+// double-float SIMT product this replaces.  15 digit pairs x 3 real products
+// = 45 bf16 MMAs per complex multiply-add, issued as mma.sync.m16n8k16.
 //
 // Because A is Hermitian, its row scale equals its column scale and row m is
 // the conjugate of column m, so both are read with coalesced column accesses.
@@ -148,7 +150,14 @@ __device__ __forceinline__ void mma_bf16(float c[4], const unsigned a[4], const 
                  : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
 }
 
-__device__ __forceinline__ unsigned neg_bf16x2(unsigned v) { return v ^ 0x80008000u; }
+// sum of two packed pairs of bf16 digits: exact, the sums are integers of
+// magnitude <= 256
+__device__ __forceinline__ unsigned add_bf16x2(unsigned a, unsigned b)
+{
+    __nv_bfloat162 x = *reinterpret_cast<__nv_bfloat162 *>(&a), y = *reinterpret_cast<__nv_bfloat162 *>(&b);
+    __nv_bfloat162 z = __hadd2(x, y);
+    return *reinterpret_cast<unsigned *>(&z);
+}
 
 // (hi, lo) += v, v exact in FP64's sense once scaled by a power of two
 __device__ __forceinline__ void df_add(float &hi, float &lo, float v)
@@ -198,13 +207,15 @@ k_oz_gemm(const __nv_bfloat16 *DA, const __nv_bfloat16 *DX, const int *exA, cons
         __syncthreads();
 #pragma unroll 1
         for (int L = 0; L <= OZ_SA - 1; ++L) {
-            float cr[2][2][4], ci[2][2][4];
+            // level sums: p1 = Ar Xr, p2 = Ai Xi, p3 = (Ar + Ai)(Xr + Xi) (three real
+            // products per complex one); re = p1 - p2, im = p3 - p1 - p2
+            float p1[2][2][4], p2[2][2][4], p3[2][2][4];
 #pragma unroll
             for (int a = 0; a < 2; ++a)
 #pragma unroll
                 for (int c = 0; c < 2; ++c)
 #pragma unroll
-                    for (int q = 0; q < 4; ++q) cr[a][c][q] = ci[a][c][q] = 0.f;
+                    for (int q = 0; q < 4; ++q) p1[a][c][q] = p2[a][c][q] = p3[a][c][q] = 0.f;
 #pragma unroll 1
             for (int t = 0; t < OZ_SB; ++t) {
                 const int s = L - t;
@@ -217,7 +228,7 @@ k_oz_gemm(const __nv_bfloat16 *DA, const __nv_bfloat16 *DX, const int *exA, cons
 #pragma unroll
                 for (int kk = 0; kk < OZ_T; kk += 16) {
                     const int kw = kk / 2;
-                    unsigned ar[2][4], ai[2][4], an[2][4];
+                    unsigned ar[2][4], ai[2][4], as[2][4];
 #pragma unroll
                     for (int a = 0; a < 2; ++a) {
                         const int r0 = wm + a * 16 + g;
@@ -230,9 +241,9 @@ k_oz_gemm(const __nv_bfloat16 *DA, const __nv_bfloat16 *DX, const int *exA, cons
                         ai[a][2] = Ai[r0 * W + kw + 4 + tq];
                         ai[a][3] = Ai[(r0 + 8) * W + kw + 4 + tq];
 #pragma unroll
-                        for (int q = 0; q < 4; ++q) an[a][q] = neg_bf16x2(ai[a][q]);
+                        for (int q = 0; q < 4; ++q) as[a][q] = add_bf16x2(ar[a][q], ai[a][q]);
                     }
-                    unsigned br[2][2], bi[2][2];
+                    unsigned br[2][2], bi[2][2], bs[2][2];
 #pragma unroll
                     for (int c = 0; c < 2; ++c) {
                         const int c0 = wn + c * 8 + g;
@@ -240,22 +251,22 @@ k_oz_gemm(const __nv_bfloat16 *DA, const __nv_bfloat16 *DX, const int *exA, cons
                         br[c][1] = Xr[c0 * W + kw + 4 + tq];
                         bi[c][0] = Xi[c0 * W + kw + tq];
                         bi[c][1] = Xi[c0 * W + kw + 4 + tq];
+                        bs[c][0] = add_bf16x2(br[c][0], bi[c][0]);
+                        bs[c][1] = add_bf16x2(br[c][1], bi[c][1]);
                     }
-                    // two rounds over the 8 accumulators, so no MMA waits on the one before it
+                    // three rounds over the 12 accumulators: no MMA waits on the one before it
 #pragma unroll
                     for (int c = 0; c < 2; ++c)
 #pragma unroll
-                        for (int a = 0; a < 2; ++a) {
-                            mma_bf16(cr[a][c], ar[a], br[c]);   // re += Ar Xr
-                            mma_bf16(ci[a][c], ar[a], bi[c]);   // im += Ar Xi
-                        }
+                        for (int a = 0; a < 2; ++a) mma_bf16(p1[a][c], ar[a], br[c]);
 #pragma unroll
                     for (int c = 0; c < 2; ++c)
 #pragma unroll
-                        for (int a = 0; a < 2; ++a) {
-                            mma_bf16(cr[a][c], an[a], bi[c]);   // re -= Ai Xi
-                            mma_bf16(ci[a][c], ai[a], br[c]);   // im += Ai Xr
-                        }
+                        for (int a = 0; a < 2; ++a) mma_bf16(p2[a][c], ai[a], bi[c]);
+#pragma unroll
+                    for (int c = 0; c < 2; ++c)
+#pragma unroll
+                        for (int a = 0; a < 2; ++a) mma_bf16(p3[a][c], as[a], bs[c]);
                 }
             }
             // fold this level of this chunk: exact integers scaled by 256^-(L+2)
@@ -266,8 +277,10 @@ k_oz_gemm(const __nv_bfloat16 *DA, const __nv_bfloat16 *DX, const int *exA, cons
                 for (int c = 0; c < 2; ++c)
 #pragma unroll
                     for (int q = 0; q < 4; ++q) {
-                        df_add(hr[a][c][q], lr[a][c][q], cr[a][c][q] * w);
-                        df_add(hi_[a][c][q], li[a][c][q], ci[a][c][q] * w);
+                        const float re = p1[a][c][q] - p2[a][c][q];
+                        const float im = p3[a][c][q] - (p1[a][c][q] + p2[a][c][q]);
+                        df_add(hr[a][c][q], lr[a][c][q], re * w);
+                        df_add(hi_[a][c][q], li[a][c][q], im * w);
                     }
         }
     }

@@ -182,17 +182,17 @@ __global__ void __launch_bounds__(1024) k_ref_clusters(RefineWork w, int *status
     }
 }
 
-// ---- 2b. Rayleigh-Ritz inside each cluster: one warp per cluster ------------
+// ---- 2b. Rayleigh-Ritz inside each cluster: one CTA per cluster -------------
 // The cluster block T_ab = x_a^H (H x_b), R_ab = x_a^H (S x_b) is formed with
-// FP64 dot products.  Column j's rotation is stored as w.U[j*CMAX + a], its
+// FP64 dot products (a thread per entry); one warp then solves the pencil.  Column j's rotation is stored as w.U[j*CMAX + a], its
 // coefficient on the cluster's a-th member (sorted position pos0 + a); the
 // members' eigenvalues replace the estimates and their R'_jj becomes 1.
-__global__ void __launch_bounds__(32) k_ref_rr(RefineWork w, const float2 *X)
+__global__ void __launch_bounds__(REF_CMAX * REF_CMAX) k_ref_rr(RefineWork w, const float2 *X)
 {
     __shared__ double2 A[REF_CMAX][REF_CMAX + 1];   // A[col][row]
     __shared__ double2 Bm[REF_CMAX][REF_CMAX + 1];
     __shared__ double2 Vv[REF_CMAX][REF_CMAX + 1];
-    const int b = blockIdx.y, p = blockIdx.x, n = w.n, lane = threadIdx.x;
+    const int b = blockIdx.y, p = blockIdx.x, n = w.n, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const long nb = (long)n * w.batch;
     const int *ord = w.cl + (long)b * n, *pos0 = w.cl + nb + (long)b * n;
     const int *csz = w.cl + 2 * nb + (long)b * n;
@@ -201,24 +201,29 @@ __global__ void __launch_bounds__(32) k_ref_rr(RefineWork w, const float2 *X)
     const int c = csz[j0];
     double2 *U = w.U + (long)b * n * REF_CMAX;
     if (c == 1) {
-        if (lane == 0) U[(long)j0 * REF_CMAX] = make_double2(1.0, 0.0);
+        if (tid == 0) U[(long)j0 * REF_CMAX] = make_double2(1.0, 0.0);
         return;
     }
     const long mo = (long)b * n * n;
-    for (int q = 0; q < c; ++q)
-        for (int r = 0; r < c; ++r) {
-            const int gr = ord[p + r], gq = ord[p + q];
-            double2 t = make_double2(0, 0), u = make_double2(0, 0);
-            for (int i = lane; i < n; i += 32) {
-                const float2 xf = X[mo + (long)gr * n + i];
-                const double2 x = make_double2(xf.x, xf.y);
-                t = cadd(t, cmulc(x, w.YH[mo + (long)gq * n + i]));
-                u = cadd(u, cmulc(x, w.YS[mo + (long)gq * n + i]));
-            }
-            t.x = warp_sum(t.x); t.y = warp_sum(t.y);
-            u.x = warp_sum(u.x); u.y = warp_sum(u.y);
-            if (lane == 0) { A[q][r] = t; Bm[q][r] = u; }
+    // T_rq = x_r^H (H x_q), R_rq = x_r^H (S x_q) in FP64, one thread per (q, r)
+    // pair: the FP64 work of a large cluster is spread over the SM's four
+    // sub-partitions
+    if (tid < c * c) {
+        const int q = tid / c, r = tid % c;
+        const float2 *xr = X + mo + (long)ord[p + r] * n;
+        const double2 *hq = w.YH + mo + (long)ord[p + q] * n, *sq = w.YS + mo + (long)ord[p + q] * n;
+        double2 t = make_double2(0, 0), u = make_double2(0, 0);
+        for (int i = 0; i < n; ++i) {
+            const float2 xf = xr[i];
+            const double2 x = make_double2(xf.x, xf.y);
+            t = cadd(t, cmulc(x, hq[i]));
+            u = cadd(u, cmulc(x, sq[i]));
         }
+        A[q][r] = t;
+        Bm[q][r] = u;
+    }
+    __syncthreads();
+    if (warp != 0) return;
     __syncwarp();
     if (lane == 0) {
         // Hermitian by construction up to rounding: symmetrise
@@ -333,32 +338,39 @@ __global__ void __launch_bounds__(32) k_ref_rr(RefineWork w, const float2 *X)
     const int *csz = w.cl + 2 * nb + (long)b * n;                              \
     const double2 *U = w.U + (long)b * n * REF_CMAX;
 
-// element (i, j) of G' = U^H G U for the block-diagonal cluster rotation U
-__device__ __forceinline__ double2 rotated_g(const float2 *G, const double2 *U, const int *ord, const int *pos0,
-                                             const int *csz, int n, int i, int j)
+// element (i, j) of G' = U^H G U for the block-diagonal cluster rotation U,
+// in FP32 (G itself is an FP32 product; its entries are residual-sized)
+__device__ __forceinline__ float2 rotated_g(const float2 *G, const double2 *U, const int *ord, const int *pos0,
+                                            const int *csz, int n, int i, int j)
 {
     const int ci = csz[i], cj = csz[j];
-    if (ci == 1 && cj == 1) {
-        const float2 g = G[i + (long)j * n];
-        return make_double2(g.x, g.y);
-    }
-    double2 s = make_double2(0, 0);
+    if (ci == 1 && cj == 1) return G[i + (long)j * n];
+    float2 s = make_float2(0.f, 0.f);
     for (int a = 0; a < ci; ++a) {
         const int ga = (ci == 1) ? i : ord[pos0[i] + a];
-        const double2 ua = (ci == 1) ? make_double2(1, 0) : cconj(U[(long)i * REF_CMAX + a]);
-        double2 t = make_double2(0, 0);
+        float2 ua = make_float2(1.f, 0.f);
+        if (ci > 1) {
+            const double2 u = U[(long)i * REF_CMAX + a];
+            ua = make_float2((float)u.x, (float)-u.y);
+        }
+        float2 t = make_float2(0.f, 0.f);
         for (int bb = 0; bb < cj; ++bb) {
             const int gb = (cj == 1) ? j : ord[pos0[j] + bb];
-            const double2 ub = (cj == 1) ? make_double2(1, 0) : U[(long)j * REF_CMAX + bb];
-            const float2 g = G[ga + (long)gb * n];
-            t = cadd(t, cmul(make_double2(g.x, g.y), ub));
+            float2 ub = make_float2(1.f, 0.f);
+            if (cj > 1) {
+                const double2 u = U[(long)j * REF_CMAX + bb];
+                ub = make_float2((float)u.x, (float)u.y);
+            }
+            cfma(t, G[ga + (long)gb * n], ub);
         }
-        s = cadd(s, cmul(ua, t));
+        cfma(s, ua, t);
     }
     return s;
 }
 
-// 3. E column j and the second-order eigenvalue term (warp per column)
+// 3. E column j and the second-order eigenvalue term (warp per column).  The
+// gaps l_j - l_i are formed in FP64; E and the second-order terms (products of
+// residual-sized FP32 entries) in FP32.
 __global__ void k_ref_update(RefineWork w, double *l2out)
 {
     const int warp = (int)((blockIdx.x * (long)blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
@@ -369,25 +381,26 @@ __global__ void k_ref_update(RefineWork w, double *l2out)
     REF_VIEWS
     const double *l1 = w.lam + (long)b * n;
     const double lj = l1[j], rjj = w.lam[nb + (long)b * n + j];
-    double corr = 0;
+    const int pj = pos0[j];
+    float corr = 0.f;
     float2 *E = w.Ef + mo + (long)j * n;
     const float2 *G = w.G + mo;
     for (int i = lane; i < n; i += 32) {
         float2 e;
         if (i == j) {
             e = make_float2((float)(0.5 * (1.0 - rjj)), 0.f);
-        } else if (pos0[i] == pos0[j]) {
+        } else if (pos0[i] == pj) {
             e = make_float2(0.f, 0.f);
         } else {
-            const double2 g = rotated_g(G, U, ord, pos0, csz, n, i, j);
-            const double den = lj - l1[i];
-            e = make_float2((float)(g.x / den), (float)(g.y / den));
-            corr += (g.x * g.x + g.y * g.y) / den;
+            const float2 g = rotated_g(G, U, ord, pos0, csz, n, i, j);
+            const float rden = 1.f / (float)(lj - l1[i]);
+            e = make_float2(g.x * rden, g.y * rden);
+            corr += (g.x * g.x + g.y * g.y) * rden;
         }
         E[i] = e;
     }
     corr = warp_sum(corr);
-    if (lane == 0) l2out[(long)b * n + j] = lj + corr;
+    if (lane == 0) l2out[(long)b * n + j] = lj + (double)corr;
 }
 
 // 4a. X U in FP64 (into YH) and FP32 (into Xr); thread per element
@@ -466,7 +479,7 @@ void refine_eigen(cudaStream_t s, RefineWork &w, const double2 *H, const double2
     NRLTB_LAUNCH(k_ref_diag, cdiv((long)n * B * 32, 256), 256, 0, s, w, X);
     // 2. clusters and their Rayleigh-Ritz rotations
     NRLTB_LAUNCH(k_ref_clusters, B, 1024, 0, s, w, status);
-    NRLTB_LAUNCH(k_ref_rr, dim3(n, B), 32, 0, s, w, X);
+    NRLTB_LAUNCH(k_ref_rr, dim3(n, B), REF_CMAX * REF_CMAX, 0, s, w, X);
     // 3. correction matrix and second-order eigenvalues (YS is free: it holds them)
     double *l2 = (double *)w.YS;
     NRLTB_LAUNCH(k_ref_update, cdiv((long)n * B * 32, 256), 256, 0, s, w, l2);
