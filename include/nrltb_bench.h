@@ -10,8 +10,10 @@
 extern "C" {
 #endif
 
-/* Peak of the FMA pipe on this GPU: kind 0 = FP64 (DFMA), 1 = FP32 (FFMA).
- * Independent FMA chains on every SM; returns TFLOP/s (2 flops per FMA). */
+/* Peak of one instruction pipe on this GPU: kind 0 = FP64 FMA, 1 = FP32 FMA
+ * (2 flops per FMA), 2 = mma.sync bf16 m16n8k16, 3 = mma.sync tf32 m16n8k8
+ * (FP32 accumulate; 2 m n k flops per MMA).  Independent chains on every SM;
+ * returns TFLOP/s. */
 int nrltb_bench_peak(nrltb_ctx *ctx, int kind, double *tflops);
 
 /* One batched complex GEMM launch of the eigensolver's kernel (C = A B, n x n x n,
@@ -44,6 +46,17 @@ int nrltb_bench_refprod_run(nrltb_ctx *ctx, int method, int n, int batch, const 
 int nrltb_bench_cgemm_run(nrltb_ctx *ctx, int method, int m, int n, int k, int opA, int opB, int triA,
                           int triB, int triC, const float alpha[2], const float beta[2], const float *A,
                           int lda, const float *B, int ldb, float *C, int ldc);
+
+/* Kernel-class timing of the context's own calls: with on = 1 every later
+ * launch of a timed class (0 = FP32 tensor-core GEMM, 1 = SIMT GEMM, 2 = the
+ * refinement's tensor-core digit product, 3 = the tridiagonalisation panel
+ * kernel) is bracketed by CUDA events on the launching stream and tagged with
+ * its algorithmic work (flops: 8 per complex multiply-add a GEMM needs, zeros
+ * of triangular operands and a skipped triangle of C excluded; bytes: the
+ * trailing lower triangles a panel reads).  Turning it on clears
+ * the records; stats synchronizes the stream and sums one class. */
+int nrltb_bench_kernel_timing(nrltb_ctx *ctx, int on);
+int nrltb_bench_kernel_stats(nrltb_ctx *ctx, int cls, double *ms, double *work, int *launches);
 
 #ifdef __cplusplus
 }

@@ -28,17 +28,48 @@ __global__ void k_fma_peak(T *out, int iters, T a, T b)
     if (s == T(-1.2345)) out[0] = s;   // keeps the chains alive
 }
 
+// 8 independent accumulators per warp, back-to-back mma.sync (kind 2: bf16
+// m16n8k16, kind 3: tf32 m16n8k8; FP32 accumulate)
+template <int KIND>
+__global__ void k_mma_peak(float *out, int iters)
+{
+    float c[8][4];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) c[i][0] = c[i][1] = c[i][2] = c[i][3] = 0.f;
+    const unsigned a0 = 0x3f803f80u ^ threadIdx.x, b0 = 0x3f803f80u ^ (threadIdx.x << 1);
+    const unsigned a[4] = {a0, a0 ^ 1u, a0 ^ 2u, a0 ^ 3u}, b[2] = {b0, b0 ^ 1u};
+    for (int it = 0; it < iters; ++it) {
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            if (KIND == 2)
+                asm volatile("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
+                             "{%8,%9}, {%0,%1,%2,%3};"
+                             : "+f"(c[i][0]), "+f"(c[i][1]), "+f"(c[i][2]), "+f"(c[i][3])
+                             : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+            else
+                asm volatile("mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
+                             "{%8,%9}, {%0,%1,%2,%3};"
+                             : "+f"(c[i][0]), "+f"(c[i][1]), "+f"(c[i][2]), "+f"(c[i][3])
+                             : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+        }
+    }
+    float s = 0.f;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) s += c[i][0] + c[i][1] + c[i][2] + c[i][3];
+    if (s == -1.2345f) out[0] = s;
+}
+
 extern "C" int nrltb_bench_peak(nrltb_ctx *ctx, int kind, double *tflops)
 {
-    if (!ctx || !tflops || (kind != 0 && kind != 1)) return NRLTB_E_ARG;
+    if (!ctx || !tflops || kind < 0 || kind > 3) return NRLTB_E_ARG;
     cudaStream_t s = nrltb_ctx_stream_internal(ctx);
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     void *buf = nullptr;
     if (cudaMalloc(&buf, 64) != cudaSuccess) return NRLTB_E_NOMEM;
-    const int threads = 512, blocks = sms * 4;
-    const int iters = (kind == 0) ? 64 : 4096;
+    const int threads = (kind >= 2) ? 256 : 512, blocks = sms * 4;
+    const int iters = (kind == 0) ? 64 : (kind == 1 ? 4096 : 2048);
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
@@ -46,7 +77,9 @@ extern "C" int nrltb_bench_peak(nrltb_ctx *ctx, int kind, double *tflops)
     for (int rep = 0; rep < 4; ++rep) {
         cudaEventRecord(e0, s);
         if (kind == 0) k_fma_peak<double><<<blocks, threads, 0, s>>>((double *)buf, iters, 0.999999, 1e-7);
-        else k_fma_peak<float><<<blocks, threads, 0, s>>>((float *)buf, iters, 0.9999f, 1e-4f);
+        else if (kind == 1) k_fma_peak<float><<<blocks, threads, 0, s>>>((float *)buf, iters, 0.9999f, 1e-4f);
+        else if (kind == 2) k_mma_peak<2><<<blocks, threads, 0, s>>>((float *)buf, iters);
+        else k_mma_peak<3><<<blocks, threads, 0, s>>>((float *)buf, iters);
         cudaEventRecord(e1, s);
         cudaEventSynchronize(e1);
         float ms = 0;
@@ -57,7 +90,8 @@ extern "C" int nrltb_bench_peak(nrltb_ctx *ctx, int kind, double *tflops)
     cudaEventDestroy(e1);
     cudaFree(buf);
     if (cudaGetLastError() != cudaSuccess) return NRLTB_E_CUDA;
-    const double flops = 2.0 * 8 * 16 * (double)iters * threads * blocks;
+    double flops = 2.0 * 8 * 16 * (double)iters * threads * blocks;
+    if (kind >= 2) flops = (kind == 2 ? 4096.0 : 2048.0) * 8 * (double)iters * (threads / 32) * blocks;
     *tflops = flops / (best * 1e-3) / 1e12;
     return NRLTB_OK;
 }

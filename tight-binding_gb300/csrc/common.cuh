@@ -82,6 +82,47 @@ __host__ __device__ inline int cdiv(long a, long b) { return (int)((a + b - 1) /
 // Launch accounting: every kernel launch of the library goes through LAUNCH so
 // that the context can report how many device kernels a call issued.
 extern thread_local long long *g_launch_counter;
+
+// Kernel-class timing (off unless a context enables it): CUDA events on the
+// launching stream around each launch of a timed class, with the launch's
+// algorithmic work (flops or bytes), summed by nrltb_bench_kernel_stats.
+enum KClass { KC_GEMM_TC = 0, KC_GEMM_SIMT = 1, KC_DIGIT_GEMM = 2, KC_TRI_PANEL = 3, KC_COUNT = 4 };
+struct KTimer {
+    bool on = false;
+    struct Rec { int cls; cudaEvent_t a, b; double work; };
+    Rec recs[4096];
+    int nrec = 0;
+    cudaEvent_t pool[8192];
+    int npool = 0, used = 0;
+    cudaEvent_t next()
+    {
+        if (used == npool) {
+            if (npool == 8192) return nullptr;
+            if (cudaEventCreate(&pool[npool]) != cudaSuccess) return nullptr;
+            ++npool;
+        }
+        return pool[used++];
+    }
+};
+extern thread_local KTimer *g_ktimer;
+// record the start of a timed launch; returns the event or null (timing off)
+inline cudaEvent_t kt_begin(cudaStream_t s)
+{
+    KTimer *k = g_ktimer;
+    if (!k || !k->on || k->nrec == 4096) return nullptr;
+    cudaEvent_t e = k->next();
+    if (e) cudaEventRecord(e, s);
+    return e;
+}
+inline void kt_end(cudaEvent_t a, cudaStream_t s, int cls, double work)
+{
+    KTimer *k = g_ktimer;
+    if (!a || !k) return;
+    cudaEvent_t b = k->next();
+    if (!b) return;
+    cudaEventRecord(b, s);
+    k->recs[k->nrec++] = {cls, a, b, work};
+}
 #define NRLTB_LAUNCH(kernel, grid, block, smem, stream, ...)                 \
     do {                                                                     \
         kernel<<<(grid), (block), (smem), (stream)>>>(__VA_ARGS__);          \

@@ -14,6 +14,7 @@
 // through shared memory, TM x TN complex outputs per thread.  FP64 runs here
 // (GB300 has no FP64 tensor path); FP32 goes to the tensor cores (gemm_tc.cu).
 #pragma once
+#include <algorithm>
 #include "common.cuh"
 
 namespace nrltb {
@@ -142,6 +143,38 @@ zgemm_kernel(GemmArgs<T> g)
 // FP32 on the tensor cores (gemm_tc.cu)
 void zgemm_tc_launch(cudaStream_t s, const GemmArgs<float> &g);
 
+// complex multiply-adds a GEMM with these triangle flags needs (the zeros of a
+// triangular operand and the skipped triangle of C excluded); for the
+// kernel-class timing, evaluated only while it is on
+inline double gemm_useful_macs(int m, int n, int k, int triA, int triB, int triC)
+{
+    auto krange = [&](int i, int j) {
+        int lo = 0, hi = k;
+        if (triA == 1) hi = std::min(hi, i + 1);
+        if (triA == 2) lo = std::max(lo, i);
+        if (triB == 1) hi = std::min(hi, j + 1);
+        if (triB == 2) lo = std::max(lo, j);
+        return (double)std::max(hi - lo, 0);
+    };
+    if (!triA && !triB && !triC) return (double)m * n * k;
+    double sum = 0;
+    if (!triB && !triC) {
+        for (int i = 0; i < m; ++i) sum += krange(i, 0);
+        return sum * n;
+    }
+    if (!triA && !triC) {
+        for (int j = 0; j < n; ++j) sum += krange(0, j);
+        return sum * m;
+    }
+    for (int i = 0; i < m; ++i)
+        for (int j = 0; j < n; ++j) {
+            if (triC == 1 && j > i) continue;
+            if (triC == 2 && j < i) continue;
+            sum += krange(i, j);
+        }
+    return sum;
+}
+
 template <typename T>
 GemmArgs<T> gemm_args(int m, int n, int k, int batch, typename cplx<T>::t alpha,
                       const typename cplx<T>::t *A, long lda, long sA, int opA,
@@ -172,7 +205,9 @@ void zgemm_simt(cudaStream_t s, int m, int n, int k, int batch, typename cplx<T>
                                        triA, triB, triC);
     constexpr int BM = 64, BN = 64, BK = 8, TM = 4, TN = 4;
     dim3 grid(cdiv(m, BM), cdiv(n, BN), batch);
+    cudaEvent_t ev = kt_begin(s);
     NRLTB_LAUNCH((zgemm_kernel<T, BM, BN, BK, TM, TN>), grid, (BM / TM) * (BN / TN), 0, s, g);
+    if (ev) kt_end(ev, s, KC_GEMM_SIMT, 8.0 * gemm_useful_macs(m, n, k, triA, triB, triC) * batch);
 }
 
 // FP64: SIMT FMA pipe; FP32: tensor cores (3xTF32, FP32-class accuracy)
@@ -191,8 +226,10 @@ void zgemm(cudaStream_t s, int m, int n, int k, int batch, typename cplx<T>::t a
                           triC);
             return;
         }
+        cudaEvent_t ev = kt_begin(s);
         zgemm_tc_launch(s, gemm_args<T>(m, n, k, batch, alpha, A, lda, sA, opA, B, ldb, sB, opB, beta, C, ldc, sC,
                                         triA, triB, triC));
+        if (ev) kt_end(ev, s, KC_GEMM_TC, 8.0 * gemm_useful_macs(m, n, k, triA, triB, triC) * batch);
     } else {
         zgemm_simt<T>(s, m, n, k, batch, alpha, A, lda, sA, opA, B, ldb, sB, opB, beta, C, ldc, sC, triA, triB,
                       triC);

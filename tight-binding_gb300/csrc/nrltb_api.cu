@@ -13,7 +13,9 @@
 #include <string>
 #include <vector>
 #include <algorithm>
+#include <new>
 #include "nrltb.h"
+#include "nrltb_bench.h"
 #include "common.cuh"
 #include "eig.cuh"
 #include "setup.cuh"
@@ -22,6 +24,7 @@
 
 namespace nrltb {
 thread_local long long *g_launch_counter = nullptr;
+thread_local KTimer *g_ktimer = nullptr;
 }
 using namespace nrltb;
 
@@ -94,6 +97,7 @@ struct nrltb_ctx {
     int device = 0;
     cudaStream_t own = nullptr, stream = nullptr;
     long long launches = 0;
+    KTimer *kt = nullptr;   // kernel-class timing (measurement hooks)
     Staged st;
     // device inputs
     DBuf d_kkind, d_posn, d_posq, d_kbas, d_dnn, d_screenl, d_param, d_kq, d_kw, d_ksk, d_orb;
@@ -479,7 +483,9 @@ static int run_all(nrltb_ctx *c)
     const int lpress = (o.mode == 4);
     cudaStream_t s = c->stream;
     long long *prev = g_launch_counter;
+    KTimer *prev_kt = g_ktimer;
     g_launch_counter = &c->launches;
+    g_ktimer = c->kt;
     int rc = NRLTB_OK;
     c->nonpd.clear();
     do {
@@ -553,6 +559,7 @@ static int run_all(nrltb_ctx *c)
         c->ran = 1;
     } while (0);
     g_launch_counter = prev;
+    g_ktimer = prev_kt;
     return rc;
 }
 
@@ -629,8 +636,51 @@ int nrltb_ctx_destroy(nrltb_ctx *c)
                     &c->d_sk, &c->d_seg, &c->d_ph, &c->d_H, &c->d_S, &c->d_X, &c->d_work, &c->d_ref, &c->d_hf, &c->d_np,
                     &c->d_eig, &c->d_deig, &c->d_ncut, &c->d_status, &c->d_fjob, &c->d_fout};
     for (DBuf *b : bufs) b->release();
+    if (c->kt) {
+        for (int i = 0; i < c->kt->npool; ++i) cudaEventDestroy(c->kt->pool[i]);
+        delete c->kt;
+    }
     if (c->own) cudaStreamDestroy(c->own);
     delete c;
+    return NRLTB_OK;
+}
+
+// ---- kernel-class timing (include/nrltb_bench.h) ----------------------------
+extern "C" int nrltb_bench_kernel_timing(nrltb_ctx *c, int on)
+{
+    if (!c) return NRLTB_E_ARG;
+    if (on) {
+        if (!c->kt) c->kt = new (std::nothrow) KTimer();
+        if (!c->kt) return NRLTB_E_NOMEM;
+        cudaSetDevice(c->device);
+        cudaStreamSynchronize(c->stream);
+        c->kt->nrec = 0;
+        c->kt->used = 0;
+        c->kt->on = true;
+    } else if (c->kt) {
+        c->kt->on = false;
+    }
+    return NRLTB_OK;
+}
+
+extern "C" int nrltb_bench_kernel_stats(nrltb_ctx *c, int cls, double *ms, double *work, int *launches)
+{
+    if (!c || cls < 0 || cls >= KC_COUNT || !ms || !work || !launches) return NRLTB_E_ARG;
+    *ms = 0;
+    *work = 0;
+    *launches = 0;
+    if (!c->kt) return NRLTB_OK;
+    cudaSetDevice(c->device);
+    if (cudaStreamSynchronize(c->stream) != cudaSuccess) return NRLTB_E_CUDA;
+    for (int i = 0; i < c->kt->nrec; ++i) {
+        const KTimer::Rec &r = c->kt->recs[i];
+        if (r.cls != cls) continue;
+        float t = 0;
+        if (cudaEventElapsedTime(&t, r.a, r.b) != cudaSuccess) return NRLTB_E_CUDA;
+        *ms += t;
+        *work += r.work;
+        ++*launches;
+    }
     return NRLTB_OK;
 }
 
@@ -696,9 +746,12 @@ int nrltb_search2(nrltb_ctx *c, const nrltb_structure *st, const nrltb_params *p
     CK(cudaSetDevice(c->device));
     RET(stage_host(c, st, par, nullptr, nullptr));
     long long *prev = g_launch_counter;
+    KTimer *prev_kt = g_ktimer;
     g_launch_counter = &c->launches;
+    g_ktimer = c->kt;
     int rc = run_search2(c, kneigh_in);
     g_launch_counter = prev;
+    g_ktimer = prev_kt;
     RET(rc);
     out->npairs = c->npairs;
     if (kneigh_out) *kneigh_out = c->kneigh_out;
@@ -738,9 +791,12 @@ int nrltb_setpar(nrltb_ctx *c, const nrltb_structure *st, const nrltb_params *pa
     CK(cudaMemcpyAsync(pr.jatm, pairs->jatm, sizeof(int) * 2 * P, cudaMemcpyHostToDevice, s));
     const int deriv = (dhop && dover && dparos) ? 1 : 0;
     long long *prev = g_launch_counter;
+    KTimer *prev_kt = g_ktimer;
     g_launch_counter = &c->launches;
+    g_ktimer = c->kt;
     int rc = run_setpar(c, deriv);
     g_launch_counter = prev;
+    g_ktimer = prev_kt;
     RET(rc);
     DevSK sk = sk_view(c, std::max(P, 1), st->natoms, par->kinds);
     CK(cudaMemcpyAsync(hop, sk.hop, sizeof(double) * 14 * P, cudaMemcpyDeviceToHost, s));
@@ -766,7 +822,9 @@ int nrltb_setham(nrltb_ctx *c, const nrltb_structure *st, const nrltb_params *pa
     o.mode = which ? 4 : 3;
     RET(stage_host(c, st, par, km, &o));
     long long *prev = g_launch_counter;
+    KTimer *prev_kt = g_ktimer;
     g_launch_counter = &c->launches;
+    g_ktimer = c->kt;
     int rc = run_search2(c, 0);
     if (!rc) rc = run_setpar(c, which);
     if (!rc) rc = run_skblocks(c, which ? 4 : 2);
@@ -776,6 +834,7 @@ int nrltb_setham(nrltb_ctx *c, const nrltb_structure *st, const nrltb_params *pa
     if (!rc) rc = c->d_S.ensure(sizeof(double2) * nn * nk);
     if (!rc) rc = run_bloch(c, 0, nk, which ? 2 : 0, c->d_H.as<double2>(), c->d_S.as<double2>());
     g_launch_counter = prev;
+    g_ktimer = prev_kt;
     RET(rc);
     cudaStream_t s = c->stream;
     CK(cudaMemcpyAsync(hmat, c->d_H.p, sizeof(double2) * nn * nk, cudaMemcpyDeviceToHost, s));
@@ -801,10 +860,13 @@ int nrltb_diag(nrltb_ctx *c, int nv, int nk, const double *hmat, const double *s
     CK(cudaMemcpyAsync(c->d_S.p, smat, sizeof(double2) * nn * nk, cudaMemcpyHostToDevice, s));
     double2 *Z = (double2 *)(c->d_X.as<char>() + zoff(nn, nk));
     long long *prev = g_launch_counter;
+    KTimer *prev_kt = g_ktimer;
     g_launch_counter = &c->launches;
+    g_ktimer = c->kt;
     int rc = run_solve(c, nv, nk, precision, c->d_H.as<double2>(), c->d_S.as<double2>(), c->d_eig.as<double>(),
                        Z, c->d_status.as<int>(), z != nullptr);
     g_launch_counter = prev;
+    g_ktimer = prev_kt;
     RET(rc);
     CK(cudaMemcpyAsync(eig, c->d_eig.p, sizeof(double) * (size_t)nv * nk, cudaMemcpyDeviceToHost, s));
     if (z) CK(cudaMemcpyAsync(z, Z, sizeof(double2) * nn * nk, cudaMemcpyDeviceToHost, s));
@@ -835,9 +897,12 @@ int nrltb_fermi(nrltb_ctx *c, int nv, int nk, const double *eig, const double *w
     job.out = c->d_fout.as<FermiOut>();
     CK(cudaMemcpyAsync(c->d_fjob.p, &job, sizeof job, cudaMemcpyHostToDevice, s));
     long long *prev = g_launch_counter;
+    KTimer *prev_kt = g_ktimer;
     g_launch_counter = &c->launches;
+    g_ktimer = c->kt;
     NRLTB_LAUNCH(k_fermi_sums, 1, 1024, 0, s, c->d_fjob.as<FermiJob>());
     g_launch_counter = prev;
+    g_ktimer = prev_kt;
     CKL();
     FermiOut o;
     CK(cudaMemcpyAsync(&o, c->d_fout.p, sizeof o, cudaMemcpyDeviceToHost, s));

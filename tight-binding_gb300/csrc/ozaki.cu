@@ -326,7 +326,9 @@ void ozaki_gemm(cudaStream_t s, const OzakiX &ox, const double2 *A, double2 *Y)
     const int smem = (OZ_SA + OZ_SB) * 2 * OZ_T * OZ_KP * (int)sizeof(__nv_bfloat16);
     cudaFuncSetAttribute(k_oz_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     dim3 grid(np / OZ_T, np / OZ_T, batch);
+    cudaEvent_t ev = kt_begin(s);
     NRLTB_LAUNCH(k_oz_gemm, grid, OZ_THREADS, smem, s, ox.DA, ox.DX, ox.exA, ox.exX, Y, n, np, batch);
+    kt_end(ev, s, KC_DIGIT_GEMM, 8.0 * n * (double)n * n * batch);
 }
 
 }  // namespace nrltb

@@ -413,8 +413,16 @@ bool tri_panel_launch(cudaStream_t s, const EigWork<T> &w, int j0, int jb)
         cudaGetLastError();
     }
     if (!ok_dev) return false;
+    cudaEvent_t ev = kt_begin(s);
     if (cudaLaunchKernelEx(&cfg, k_tri_panel<T>, w, j0, jb) != cudaSuccess) return false;
     if (g_launch_counter) ++*g_launch_counter;
+    // algorithmic bytes: the lower triangle of each column's trailing matrix, read once
+    double bytes = 0;
+    for (int c = 0; c < jb; ++c) {
+        const double m = w.n - (j0 + c) - 1;
+        bytes += 0.5 * m * (m + 1) * sizeof(typename cplx<T>::t);
+    }
+    kt_end(ev, s, KC_TRI_PANEL, bytes * w.batch);
     return true;
 }
 

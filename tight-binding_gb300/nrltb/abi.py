@@ -107,6 +107,8 @@ GPU_SYMBOLS = [
     ("nrltb_bench_zgemm", C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_int, _dp, _dp]),
     ("nrltb_bench_refprod", C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_int, _dp, _dp]),
     ("nrltb_bench_refprod_run", C.c_int, [_vp, C.c_int, C.c_int, C.c_int, _vp, _vp, _vp]),
+    ("nrltb_bench_kernel_timing", C.c_int, [_vp, C.c_int]),
+    ("nrltb_bench_kernel_stats", C.c_int, [_vp, C.c_int, _dp, _dp, C.POINTER(C.c_int)]),
     ("nrltb_bench_cgemm_run", C.c_int, [_vp] + [C.c_int] * 9 + [_vp, _vp, _vp, C.c_int, _vp, C.c_int, _vp,
                                                                   C.c_int]),
 ]
