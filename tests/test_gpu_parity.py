@@ -239,3 +239,68 @@ def test_host_driver_ex1_skeng(tmp_path, ex1_gold):
             assert abs(v - g) <= 1.01e-9
     out = (tmp_path / "SKOUT").read_text()
     assert out.count("Number of pairs =") == 18
+
+
+def test_pressure_matches_energy_derivative_b2_216(ctx):
+    """The two-species N=1404 configuration (8 Gamma-centred k, kT = 0.01): the
+    Hellmann-Feynman pressure against -dE/dV from E(T) at V0 (1 +- h),
+    (1 +- 2h), h = 0.25% (five-point difference), uniform scaling of the cell
+    and the atoms.  FP64 form.  The pair cut-off is raised from 16.5 to 24
+    bohr for this check: at 16.5 the screened integrals are still ~1e-5 Ry, so
+    the pairs that cross the cut-off as the cell scales make E(V) jump (a
+    ~3e-5 relative offset of the difference quotient, present in the
+    reference model too; ~8e-7 at 20 bohr); at 24 bohr the jumps are below
+    1e-13 Ry."""
+    from dataclasses import replace
+    from nrltb import Structure
+    st0, par0, km, o = synth.b2_216()
+    par = replace(par0, dnn=np.full_like(par0.dnn, 24.0))
+
+    def scaled(eps):
+        s = (1.0 + eps) ** (1.0 / 3.0)
+        plv = st0.plv * s
+        return Structure(st0.kkind, st0.posn * s, plv, synth.search_box(plv, 24.0), st0.volume * (1.0 + eps))
+
+    st = scaled(0.0)
+    opts4 = Opts(mode=4, tkb=o["tkb"], eigcut=1e3, fermi_tol=1e-12)
+    opts3 = Opts(mode=3, tkb=o["tkb"], eigcut=1e3, fermi_tol=1e-12)
+    r0 = ctx.bande(st, par, km, opts4, want_eig=False)
+
+    def energy(eps):
+        return ctx.bande(scaled(eps), par, km, opts3, want_eig=False).e_total
+
+    h = 0.0025
+    e1p, e1m, e2p, e2m = energy(h), energy(-h), energy(2 * h), energy(-2 * h)
+    dedv = (8.0 * (e1p - e1m) - (e2p - e2m)) / (12.0 * h * st.volume)
+    assert abs(-dedv - r0.pressure) <= P_TOL, (-dedv, r0.pressure)
+
+
+def test_bande_batch_matches_single_calls(ctx):
+    """nrltb_bande_batch over a mixed list of structures (spd and sp3, 4-64
+    atoms, 2^3..5^3 meshes) returns what one nrltb_bande call per structure
+    returns, bit for bit, and a small member agrees with the oracle."""
+    import ctypes as C
+    from nrltb import abi
+    from nrltb.api import new_result, result_from_c
+    items = synth.batch256(count=12)
+    opts = [Opts(mode=4, tkb=o["tkb"], eigcut=1e3, fermi_tol=1e-12) for (_, _, _, o) in items]
+    single = [ctx.bande(st, par, km, op) for (st, par, km, _), op in zip(items, opts)]
+    n = len(items)
+    cs = (abi.Structure_ * n)(*[it[0].to_c() for it in items])
+    cp = (abi.Params_ * n)(*[it[1].to_c() for it in items])
+    ck = (abi.KMesh_ * n)(*[it[2].to_c() for it in items])
+    co = (abi.Opts_ * n)(*[op.to_c() for op in opts])
+    made = [new_result(it[1].nv(it[0]), it[2].nk) for it in items]
+    cr = (abi.Result_ * n)(*[m[0] for m in made])
+    rc = ctx.lib.nrltb_bande_batch(ctx.h, n, cs, cp, ck, co, cr)
+    assert rc == 0, ctx.lib.nrltb_last_error()
+    for i in range(n):
+        b = result_from_c(cr[i], made[i][1])
+        a = single[i]
+        assert b.efermi == a.efermi and b.e_total == a.e_total and b.pressure == a.pressure
+        assert np.array_equal(b.eig, a.eig) and np.array_equal(b.deig, a.deig)
+    small = min(range(n), key=lambda i: items[i][1].nv(items[i][0]) * items[i][2].nk)
+    st, par, km, _ = items[small]
+    ref = oracle.bande(st, par, km, opts[small])
+    assert abs(single[small].efermi - ref.efermi) <= 1e-9
+    assert np.abs(single[small].eig - ref.eig).max() <= 1e-10

@@ -13,7 +13,10 @@
 #include <string>
 #include <vector>
 #include <algorithm>
+#include <atomic>
+#include <mutex>
 #include <new>
+#include <thread>
 #include "nrltb.h"
 #include "nrltb_bench.h"
 #include "common.cuh"
@@ -98,6 +101,7 @@ struct nrltb_ctx {
     cudaStream_t own = nullptr, stream = nullptr;
     long long launches = 0;
     KTimer *kt = nullptr;   // kernel-class timing (measurement hooks)
+    std::vector<nrltb_ctx *> workers;   // nrltb_bande_batch: one context and stream per host worker
     Staged st;
     // device inputs
     DBuf d_kkind, d_posn, d_posq, d_kbas, d_dnn, d_screenl, d_param, d_kq, d_kw, d_ksk, d_orb;
@@ -640,6 +644,7 @@ int nrltb_ctx_destroy(nrltb_ctx *c)
         for (int i = 0; i < c->kt->npool; ++i) cudaEventDestroy(c->kt->pool[i]);
         delete c->kt;
     }
+    for (nrltb_ctx *w : c->workers) nrltb_ctx_destroy(w);
     if (c->own) cudaStreamDestroy(c->own);
     delete c;
     return NRLTB_OK;
@@ -731,11 +736,59 @@ int nrltb_bande(nrltb_ctx *c, const nrltb_structure *st, const nrltb_params *par
     return nrltb_fetch(c, res);
 }
 
+// Structures are independent: BATCH_WORKERS host threads, each with its own
+// context (workspace) and stream, take structures from a shared counter, so
+// the GPU overlaps the small structures' launch-latency-bound solves.  Each
+// structure's result is the one nrltb_bande gives for it alone (every kernel
+// works per matrix and the k sums have a fixed order).
+constexpr int BATCH_WORKERS = 4;
+
 int nrltb_bande_batch(nrltb_ctx *c, int nstruct, const nrltb_structure *st, const nrltb_params *par,
                       const nrltb_kmesh *km, const nrltb_opts *opt, nrltb_result *res)
 {
     if (!c || nstruct < 0 || (nstruct > 0 && (!st || !par || !km || !opt || !res))) return NRLTB_E_ARG;
-    for (int i = 0; i < nstruct; ++i) RET(nrltb_bande(c, st + i, par + i, km + i, opt + i, res + i));
+    const int W = std::min(BATCH_WORKERS, nstruct);
+    if (W <= 1) {
+        for (int i = 0; i < nstruct; ++i) RET(nrltb_bande(c, st + i, par + i, km + i, opt + i, res + i));
+        return NRLTB_OK;
+    }
+    CK(cudaSetDevice(c->device));
+    CK(cudaStreamSynchronize(c->stream));   // work the caller queued comes first
+    while ((int)c->workers.size() < W) {
+        nrltb_ctx *w = nullptr;
+        RET(nrltb_ctx_create(&w, c->device));
+        c->workers.push_back(w);
+    }
+    std::atomic<int> next(0), failed(0);
+    std::mutex mu;
+    int first_rc = NRLTB_OK;
+    std::string first_msg;
+    std::vector<long long> before(W);
+    for (int i = 0; i < W; ++i) before[i] = c->workers[i]->launches;
+    auto body = [&](int wi) {
+        nrltb_ctx *wc = c->workers[wi];
+        for (;;) {
+            const int i = next.fetch_add(1);
+            if (i >= nstruct || failed.load()) return;
+            const int rc = nrltb_bande(wc, st + i, par + i, km + i, opt + i, res + i);
+            if (rc != NRLTB_OK) {
+                std::lock_guard<std::mutex> g(mu);
+                if (!failed.exchange(1)) {
+                    first_rc = rc;
+                    first_msg = std::string(nrltb_last_error()) + " (structure " + std::to_string(i) + ")";
+                }
+                return;
+            }
+        }
+    };
+    std::vector<std::thread> th;
+    for (int wi = 0; wi < W; ++wi) th.emplace_back(body, wi);
+    for (std::thread &t : th) t.join();
+    for (int i = 0; i < W; ++i) c->launches += c->workers[i]->launches - before[i];
+    if (failed.load()) {
+        set_err("%s", first_msg.c_str());
+        return first_rc;
+    }
     return NRLTB_OK;
 }
 

@@ -404,8 +404,10 @@ bool tri_panel_launch(cudaStream_t s, const EigWork<T> &w, int j0, int jb)
     cfg.stream = s;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    if (cudaFuncSetAttribute(k_tri_panel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    if (cudaFuncSetAttribute(k_tri_panel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+        cudaGetLastError();   // not sticky: the per-column path takes over
         return false;
+    }
     if (checked_dev != dev) {
         int nclusters = 0;
         ok_dev = cudaOccupancyMaxActiveClusters(&nclusters, k_tri_panel<T>, &cfg) == cudaSuccess && nclusters > 0;
@@ -414,7 +416,10 @@ bool tri_panel_launch(cudaStream_t s, const EigWork<T> &w, int j0, int jb)
     }
     if (!ok_dev) return false;
     cudaEvent_t ev = kt_begin(s);
-    if (cudaLaunchKernelEx(&cfg, k_tri_panel<T>, w, j0, jb) != cudaSuccess) return false;
+    if (cudaLaunchKernelEx(&cfg, k_tri_panel<T>, w, j0, jb) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
     if (g_launch_counter) ++*g_launch_counter;
     // algorithmic bytes: the lower triangle of each column's trailing matrix, read once
     double bytes = 0;
