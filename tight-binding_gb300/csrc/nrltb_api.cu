@@ -345,7 +345,7 @@ static int run_setpar(nrltb_ctx *c, int deriv)
     DevStructure DS = dev_structure(c);
     DevParams DP = dev_params(c);
     if (c->npairs > 0) NRLTB_LAUNCH(k_setpar_pairs, cdiv(c->npairs, 128), 128, 0, s, DS, DP, pr, c->npairs, sk, deriv);
-    NRLTB_LAUNCH(k_setpar_atoms, cdiv(S.natoms, 64), 64, 0, s, DS, DP, pr, c->npairs, sk, deriv);
+    NRLTB_LAUNCH(k_setpar_atoms, cdiv((long)S.natoms * 32, 256), 256, 0, s, DS, DP, pr, c->npairs, sk, deriv);
     CKL();
     return NRLTB_OK;
 }

@@ -508,30 +508,6 @@ void launch_to_f32(cudaStream_t s, const double2 *src, float2 *dst, long count)
     NRLTB_LAUNCH(k_to_f32, 1184, 256, 0, s, src, dst, count);
 }
 
-// deig_n = Re(z_n^H P_n) - e_n Re(z_n^H Q_n), FP32 inputs, FP64 sums; warp per column
-__global__ void k_hf_dots32(const float2 *Z, const float2 *P, const float2 *Q, const double *eig, double *deig,
-                            int n, int batch)
-{
-    const int warp = (int)((blockIdx.x * (long)blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
-    if (warp >= n * batch) return;
-    const int b = warp / n, col = warp % n;
-    const long off = (long)b * n * n + (long)col * n;
-    double sp = 0, sq = 0;
-    for (int i = lane; i < n; i += 32) {
-        const float2 z = Z[off + i], p = P[off + i], q = Q[off + i];
-        sp += (double)z.x * p.x + (double)z.y * p.y;
-        sq += (double)z.x * q.x + (double)z.y * q.y;
-    }
-    sp = warp_sum(sp);
-    sq = warp_sum(sq);
-    if (lane == 0) deig[(long)b * n + col] = sp - eig[(long)b * n + col] * sq;
-}
-void launch_hf_dots32(cudaStream_t s, const float2 *Z, const float2 *P, const float2 *Q, const double *eig,
-                      double *deig, int n, int batch)
-{
-    NRLTB_LAUNCH(k_hf_dots32, cdiv((long)n * batch * 32, 256), 256, 0, s, Z, P, Q, eig, deig, n, batch);
-}
-
 int run_hf(cudaStream_t s, int n, int nkc, int prec, const double2 *dH, const double2 *dS, const double2 *Z,
            const double *eig, double *deig, void *scratch, void *unused)
 {
@@ -546,23 +522,24 @@ int run_hf(cudaStream_t s, int n, int nkc, int prec, const double2 *dH, const do
         zgemm<double>(s, n, n, n, nkc, one, dS, n, nn, 0, Z, n, nn, 0, zero, Q, n, nn, 2, 0, 0);
         launch_hf_dots(s, Z, P, Q, dH, dS, eig, deig, n, nkc);
     } else {
-        // Mixed form: the products in FP32 (full, no triangle trick, so no
-        // cancellation against the diagonal); their error in P is ~1e-11
-        // Ry/bohr^3 per k, far below the 1e-3 kbar (6.8e-9) tolerance.  The
-        // scratch holds dH32 | dS32 | Z32 | P32 (4 n^2 float2 = 2 n^2 double2);
-        // dS Z overwrites dH32 once dH Z is formed.
+        // Mixed form: P = triu(dH) Z, Q = triu(dS) Z in FP32 on the FMA pipe
+        // (not the tensor cores: the MMA accumulator's rounding is biased
+        // toward zero, and a relative bias of ~1e-6 in P shifts the pressure
+        // coherently by ~1e-7 Ry/bohr^3), then
+        // deig = 2 Re(z^H P) - sum dH_ii |z_i|^2 - e (2 Re(z^H Q) - sum dS_ii |z_i|^2)
+        // with FP64 sums; the pressure error stays ~1e-10 Ry/bohr^3 per k
+        // against the 1e-3 kbar (6.8e-9) tolerance.  The scratch holds
+        // dH32 | dS32 | Z32 | P32 (4 n^2 float2 = 2 n^2 double2); dS Z
+        // overwrites dH32 once dH Z is formed.
         float2 *h32 = (float2 *)scratch, *s32 = h32 + nn * nkc, *z32 = s32 + nn * nkc;
         float2 *p32 = z32 + nn * nkc;
         launch_to_f32(s, dH, h32, nn * nkc);
         launch_to_f32(s, dS, s32, nn * nkc);
         launch_to_f32(s, Z, z32, nn * nkc);
         const float2 one = make_float2(1.f, 0.f), zero = make_float2(0.f, 0.f);
-        // SIMT FMA pipe, not the tensor cores: the MMA accumulator's rounding
-        // is biased toward zero, and a relative bias of ~1e-6 in P shifts the
-        // pressure coherently by ~1e-7 Ry/bohr^3
-        zgemm_simt<float>(s, n, n, n, nkc, one, h32, n, nn, 0, z32, n, nn, 0, zero, p32, n, nn);
-        zgemm_simt<float>(s, n, n, n, nkc, one, s32, n, nn, 0, z32, n, nn, 0, zero, h32, n, nn);   // dS Z over dH32
-        launch_hf_dots32(s, z32, p32, h32, eig, deig, n, nkc);
+        zgemm_simt<float>(s, n, n, n, nkc, one, h32, n, nn, 0, z32, n, nn, 0, zero, p32, n, nn, 2, 0, 0);
+        zgemm_simt<float>(s, n, n, n, nkc, one, s32, n, nn, 0, z32, n, nn, 0, zero, h32, n, nn, 2, 0, 0);
+        launch_hf_dots32_tri(s, z32, p32, h32, dH, dS, eig, deig, n, nkc);
     }
     return cudaGetLastError() == cudaSuccess ? NRLTB_OK : NRLTB_E_CUDA;
 }

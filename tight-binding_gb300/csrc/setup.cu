@@ -301,27 +301,40 @@ __global__ void k_setpar_pairs(DevStructure S, DevParams P, DevPairs pr, int npa
 }
 
 // Per-atom densities in pair order, then the on-site polynomials (setpar.f:735-884)
-// and their volume derivatives (setparv.f:730-886).
+// and their volume derivatives (setparv.f:730-886).  One warp per atom: the
+// lanes scan 32 pairs at a time and the matching pairs are added in pair order
+// (the reference's summation order), every lane keeping the same sums.
 __global__ void k_setpar_atoms(DevStructure S, DevParams P, DevPairs pr, int npairs, DevSK sk, int deriv)
 {
-    const int a = blockIdx.x * blockDim.x + threadIdx.x;
-    if (a >= S.natoms) return;
+    const int a = (int)((blockIdx.x * (long)blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+    if (a >= S.natoms) return;   // warp-uniform
     const int kinds = P.kinds;
     double den[NRLTB_MAX_KINDS], vden[NRLTB_MAX_KINDS];
     for (int k = 0; k < kinds; ++k) { den[k] = 0; vden[k] = 0; }
-    for (int p = 0; p < npairs; ++p) {
-        const int iat = pr.jatm[2 * p] - 1, jat = pr.jatm[2 * p + 1] - 1;
-        if (iat == a) {
-            const int k2 = pr.jkind[2 * p + 1];
-            den[k2 - 1] += sk.dent[2 * (long)p];
-            vden[k2 - 1] += sk.vdent[2 * (long)p];
+    for (int p0 = 0; p0 < npairs; p0 += 32) {
+        const int p = p0 + lane;
+        int iat = -1, jat = -1, kk = 0;
+        double d1 = 0, v1 = 0;
+        bool m1 = false, m2 = false;
+        if (p < npairs) {
+            iat = pr.jatm[2 * p] - 1;
+            jat = pr.jatm[2 * p + 1] - 1;
+            m1 = iat == a;
+            m2 = jat == a && iat != a;
+            if (m1) { kk = pr.jkind[2 * p + 1]; d1 = sk.dent[2 * (long)p]; v1 = sk.vdent[2 * (long)p]; }
+            else if (m2) { kk = pr.jkind[2 * p]; d1 = sk.dent[2 * (long)p + 1]; v1 = sk.vdent[2 * (long)p + 1]; }
         }
-        if (jat == a && iat != a) {
-            const int k1 = pr.jkind[2 * p];
-            den[k1 - 1] += sk.dent[2 * (long)p + 1];
-            vden[k1 - 1] += sk.vdent[2 * (long)p + 1];
+        unsigned hits = __ballot_sync(0xffffffffu, m1 || m2);
+        while (hits) {   // in pair order
+            const int l = __ffs(hits) - 1;
+            hits &= hits - 1;
+            const int k = __shfl_sync(0xffffffffu, kk, l);
+            const double d = __shfl_sync(0xffffffffu, d1, l), v = __shfl_sync(0xffffffffu, v1, l);
+            den[k - 1] += d;
+            vden[k - 1] += v;
         }
     }
+    if (lane != 0) return;
     const double *Pm = P.param - 1;
     const int jk1 = S.kkind[a];
     for (int k = 0; k < kinds; ++k) sk.den[(long)a * kinds + k] = den[k];

@@ -184,4 +184,11 @@ void launch_hf_dots(cudaStream_t s, const double2 *Z, const double2 *P, const do
     NRLTB_LAUNCH(k_hf_dots<double2>, cdiv(warps * 32, 256), 256, 0, s, Z, P, Q, dH, dS, eig, deig, n, batch);
 }
 
+void launch_hf_dots32_tri(cudaStream_t s, const float2 *Z, const float2 *P, const float2 *Q, const double2 *dH,
+                          const double2 *dS, const double *eig, double *deig, int n, int batch)
+{
+    const long warps = (long)n * batch;
+    NRLTB_LAUNCH(k_hf_dots<float2>, cdiv(warps * 32, 256), 256, 0, s, Z, P, Q, dH, dS, eig, deig, n, batch);
+}
+
 }  // namespace nrltb
