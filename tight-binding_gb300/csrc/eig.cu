@@ -42,7 +42,7 @@ template <typename T> void eig_work_carve(EigWork<T> &w, void *base, int n, int 
     w.sc = (C2 *)take(sizeof(C2) * 4 * nb);
     const size_t nbw = (size_t)std::min(EIG_WY, n);
     w.Tt = (C2 *)take(sizeof(C2) * std::max(EIG_NB * (size_t)std::max(n, 2 * EIG_NB), 2 * nbw * nbw) * nb);
-    w.Xt = (C2 *)take(sizeof(C2) * EIG_NB * (size_t)n * nb);
+    w.Xt = (C2 *)take(sizeof(C2) * std::max(EIG_NB, (int)nbw) * (size_t)n * nb);
     w.d = (double *)take(sizeof(double) * n * nb);
     w.e = (double *)take(sizeof(double) * n * nb);
     w.lam = (double *)take(sizeof(double) * n * nb);
@@ -721,8 +721,14 @@ void eig_solve(cudaStream_t s, EigWork<T> &w, const double2 *H, const double2 *S
                      zero, w.Wi + (j0 + jb) + (long)j0 * ld, ld, ms, 0, 2, 0);
         }
     }
-    // 3. A = Wi H Wi^H (lower tiles)
-    zgemm<T>(s, n, n, n, B, one, w.A, ld, ms, 0, w.Wi, ld, ms, 1, zero, w.Y, ld, ms, 0, 1, 0);
+    // 3. A = Wi H Wi^H (lower tiles); FP32: Wi^H formed explicitly in L (free
+    //    after step 2) so that both tensor-core GEMMs stream stored operands
+    if (sizeof(T) == 4) {
+        conj_transpose<T>(s, w.Wi, w.L, n, B);
+        zgemm<T>(s, n, n, n, B, one, w.A, ld, ms, 0, w.L, ld, ms, 0, zero, w.Y, ld, ms, 0, 1, 0);
+    } else {
+        zgemm<T>(s, n, n, n, B, one, w.A, ld, ms, 0, w.Wi, ld, ms, 1, zero, w.Y, ld, ms, 0, 1, 0);
+    }
     zgemm<T>(s, n, n, n, B, one, w.Wi, ld, ms, 0, w.Y, ld, ms, 0, zero, w.A, ld, ms, 1, 0, 1);
     // 4. tridiagonalisation: one cluster launch per panel (tri_panel.cuh); the
     //    per-column launch chain below is the path for devices or sizes where
@@ -790,11 +796,25 @@ void eig_solve(cudaStream_t s, EigWork<T> &w, const double2 *H, const double2 *S
             C2 *Yb = w.Y + (j0 + 1);
             zgemm<T>(s, jb, jb, mb, B, one, Vb, ld, ms, 1, Vb, ld, ms, 0, zero, G, nbw, sG);
             NRLTB_LAUNCH(k_larft_wy<T>, B, EIG_WY, 0, s, G, Tf, w.tau, n, j0, jb, nbw);
-            zgemm<T>(s, jb, n, mb, B, one, Vb, ld, ms, 1, Yb, ld, ms, 0, zero, w.A, nbw, sX);
+            if (sizeof(T) == 4) {
+                // Vb^H formed explicitly in Xt: the tensor-core GEMM streams an A
+                // operand in its stored orientation twice as fast
+                conj_transpose<T>(s, Vb, ld, ms, w.Xt, nbw, sX, mb, jb, B);
+                zgemm<T>(s, jb, n, mb, B, one, w.Xt, nbw, sX, 0, Yb, ld, ms, 0, zero, w.A, nbw, sX);
+            } else {
+                zgemm<T>(s, jb, n, mb, B, one, Vb, ld, ms, 1, Yb, ld, ms, 0, zero, w.A, nbw, sX);
+            }
             zgemm<T>(s, jb, n, jb, B, one, Tf, nbw, sG, 0, w.A, nbw, sX, 0, zero, w.L, nbw, sX, 2, 0, 0);
             zgemm<T>(s, mb, n, jb, B, mone, Vb, ld, ms, 0, w.L, nbw, sX, 0, one, Yb, ld, ms);
         }
-        zgemm<T>(s, n, n, n, B, one, w.Wi, ld, ms, 1, w.Y, ld, ms, 0, zero, X, ld, ms, 2, 0, 0);
+        if (sizeof(T) == 4) {
+            // Wi^H formed explicitly in L (free again): the tensor-core GEMM
+            // streams an A operand in its stored orientation twice as fast
+            conj_transpose<T>(s, w.Wi, w.L, n, B);
+            zgemm<T>(s, n, n, n, B, one, w.L, ld, ms, 0, w.Y, ld, ms, 0, zero, X, ld, ms, 2, 0, 0);
+        } else {
+            zgemm<T>(s, n, n, n, B, one, w.Wi, ld, ms, 1, w.Y, ld, ms, 0, zero, X, ld, ms, 2, 0, 0);
+        }
     }
 }
 

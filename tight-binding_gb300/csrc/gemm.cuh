@@ -143,6 +143,43 @@ zgemm_kernel(GemmArgs<T> g)
 // FP32 on the tensor cores (gemm_tc.cu)
 void zgemm_tc_launch(cudaStream_t s, const GemmArgs<float> &g);
 
+// dst = src^H for `batch` rows x cols matrices (src leading dimension lds,
+// stride ss; dst leading dimension ldd, stride ds), 32 x 32 tiles through
+// shared memory so both sides are coalesced
+template <typename C2>
+__global__ void k_conj_transpose(const C2 *src, long lds, long ss, C2 *dst, long ldd, long ds, int rows, int cols)
+{
+    __shared__ C2 t[32][33];
+    const C2 *S = src + blockIdx.z * ss;
+    C2 *D = dst + blockIdx.z * ds;
+    const int c0 = blockIdx.x * 32, r0 = blockIdx.y * 32;
+    for (int q = threadIdx.y; q < 32; q += blockDim.y) {
+        const int r = r0 + threadIdx.x, c = c0 + q;
+        if (r < rows && c < cols) t[q][threadIdx.x] = S[r + (long)c * lds];
+    }
+    __syncthreads();
+    for (int q = threadIdx.y; q < 32; q += blockDim.y) {
+        const int c = c0 + threadIdx.x, r = r0 + q;   // D(c, r) = conj(S(r, c))
+        if (r < rows && c < cols) {
+            C2 v = t[threadIdx.x][q];
+            v.y = -v.y;
+            D[c + (long)r * ldd] = v;
+        }
+    }
+}
+template <typename T>
+void conj_transpose(cudaStream_t s, const typename cplx<T>::t *src, long lds, long ss, typename cplx<T>::t *dst,
+                    long ldd, long ds, int rows, int cols, int batch)
+{
+    NRLTB_LAUNCH(k_conj_transpose<typename cplx<T>::t>, dim3(cdiv(cols, 32), cdiv(rows, 32), batch), dim3(32, 8), 0,
+                 s, src, lds, ss, dst, ldd, ds, rows, cols);
+}
+template <typename T>
+void conj_transpose(cudaStream_t s, const typename cplx<T>::t *src, typename cplx<T>::t *dst, int n, int batch)
+{
+    conj_transpose<T>(s, src, n, (long)n * n, dst, n, (long)n * n, n, n, batch);
+}
+
 // complex multiply-adds a GEMM with these triangle flags needs (the zeros of a
 // triangular operand and the skipped triangle of C excluded); for the
 // kernel-class timing, evaluated only while it is on
@@ -220,6 +257,7 @@ void zgemm(cudaStream_t s, int m, int n, int k, int batch, typename cplx<T>::t a
 {
     if (m <= 0 || n <= 0 || batch <= 0) return;
     // tensor cores only where a 128 x 64 tile is well filled and the k loop is long
+    // (rank-32 panel updates run faster on the FMA pipe)
     if constexpr (sizeof(T) == 4) {
         if (m < 128 || n < 64 || k < 128) {
             zgemm_simt<T>(s, m, n, k, batch, alpha, A, lda, sA, opA, B, ldb, sB, opB, beta, C, ldc, sC, triA, triB,

@@ -17,7 +17,7 @@
 namespace nrltb {
 
 constexpr int TC_BM = 128, TC_BN = 64, TC_BK = 16;
-constexpr int TC_LDA = TC_BM + 4, TC_LDB = TC_BN + 4;   // == 4 mod 16: conflict-free fragment loads
+constexpr int TC_LDA = TC_BM + 4, TC_LDB = TC_BN + 4;   // [k][row] strides == 4 mod 16: conflict-free fragment loads
 constexpr int TC_THREADS = 256;
 constexpr int TC_AE = TC_BM * TC_BK / TC_THREADS;       // staged A elements per thread (8)
 constexpr int TC_BE = TC_BN * TC_BK / TC_THREADS;       // staged B elements per thread (4)
@@ -75,10 +75,25 @@ __device__ __forceinline__ void tc_b_pos(int opB, int e, int &kk, int &j)
     if (opB == 0) { kk = e % TC_BK; j = e / TC_BK; } else { j = e % TC_BN; kk = e / TC_BN; }
 }
 
+// Shared-memory layouts: an operand staged k-fastest (op(A) = A^H, op(B) = B,
+// so that its global reads are coalesced) is kept [row][k] with a row stride of
+// TC_LDK = 20 complex, otherwise [k][row]; both give conflict-free stores and
+// fragment loads.
+constexpr int TC_LDK = TC_BK + 4;
+template <int KM>   // KM = 1: [row][k]
+struct TcTile {
+    float2 *p;
+    int ld;   // [k][row] row stride
+    __device__ float2 &at(int k, int row) const { return KM ? p[row * TC_LDK + k] : p[k * ld + row]; }
+};
+
+template <int TA, int TB>
 __global__ void __launch_bounds__(TC_THREADS) zgemm_tc_kernel(GemmArgs<float> g)
 {
-    __shared__ float2 As[TC_BK][TC_LDA];
-    __shared__ float2 Bs[TC_BK][TC_LDB];
+    __shared__ float2 As_[TA ? TC_BM * TC_LDK : TC_BK * TC_LDA];
+    __shared__ float2 Bs_[TB ? TC_BN * TC_LDK : TC_BK * TC_LDB];
+    const TcTile<TA> As{As_, TC_LDA};
+    const TcTile<TB> Bs{Bs_, TC_LDB};
     const int b = blockIdx.z;
     const int m0 = blockIdx.x * TC_BM, n0 = blockIdx.y * TC_BN;
     if (g.triC == 1 && m0 + TC_BM - 1 < n0) return;
@@ -126,13 +141,13 @@ __global__ void __launch_bounds__(TC_THREADS) zgemm_tc_kernel(GemmArgs<float> g)
         for (int u = 0; u < TC_AE; ++u) {
             int i, kk;
             tc_a_pos(g.opA, tid + u * TC_THREADS, i, kk);
-            As[kk][i] = ra[u];
+            As.at(kk, i) = ra[u];
         }
 #pragma unroll
         for (int u = 0; u < TC_BE; ++u) {
             int kk, j;
             tc_b_pos(g.opB, tid + u * TC_THREADS, kk, j);
-            Bs[kk][j] = rb[u];
+            Bs.at(kk, j) = rb[u];
         }
         __syncthreads();
         if (k0 + TC_BK < kend) fetch(k0 + TC_BK);
@@ -144,7 +159,7 @@ __global__ void __launch_bounds__(TC_THREADS) zgemm_tc_kernel(GemmArgs<float> g)
             for (int c = 0; c < 4; ++c)
 #pragma unroll
                 for (int h = 0; h < 2; ++h) {
-                    const float2 v = Bs[ks + tq + 4 * h][wn + c * 8 + gq];
+                    const float2 v = Bs.at(ks + tq + 4 * h, wn + c * 8 + gq);
                     tf32_split(v.x, brh[c][h], brl[c][h]);
                     tf32_split(v.y, bih[c][h], bil[c][h]);
                 }
@@ -155,7 +170,7 @@ __global__ void __launch_bounds__(TC_THREADS) zgemm_tc_kernel(GemmArgs<float> g)
 #pragma unroll
                 for (int q = 0; q < 4; ++q) {
                     const int r = wm + a * 16 + gq + 8 * (q & 1), kq = ks + tq + 4 * (q >> 1);
-                    const float2 v = As[kq][r];
+                    const float2 v = As.at(kq, r);
                     tf32_split(v.x, arh[q], arl[q]);
                     tf32_split(v.y, aih[q], ail[q]);
                     anh[q] = aih[q] ^ 0x80000000u;
@@ -197,7 +212,11 @@ __global__ void __launch_bounds__(TC_THREADS) zgemm_tc_kernel(GemmArgs<float> g)
 void zgemm_tc_launch(cudaStream_t s, const GemmArgs<float> &g)
 {
     dim3 grid(cdiv(g.m, TC_BM), cdiv(g.n, TC_BN), g.batch);
-    NRLTB_LAUNCH(zgemm_tc_kernel, grid, TC_THREADS, 0, s, g);
+    const bool ta = g.opA == 1, tb = g.opB == 0;
+    if (ta && tb) NRLTB_LAUNCH((zgemm_tc_kernel<1, 1>), grid, TC_THREADS, 0, s, g);
+    else if (ta) NRLTB_LAUNCH((zgemm_tc_kernel<1, 0>), grid, TC_THREADS, 0, s, g);
+    else if (tb) NRLTB_LAUNCH((zgemm_tc_kernel<0, 1>), grid, TC_THREADS, 0, s, g);
+    else NRLTB_LAUNCH((zgemm_tc_kernel<0, 0>), grid, TC_THREADS, 0, s, g);
 }
 
 }  // namespace nrltb

@@ -475,7 +475,10 @@ void refine_eigen(cudaStream_t s, RefineWork &w, const double2 *H, const double2
     ozaki_gemm(s, ox, H, w.YH);
     ozaki_gemm(s, ox, S, w.YS);
     NRLTB_LAUNCH(k_ref_resid, cdiv(nn * B, 256), 256, 0, s, w, eig);
-    zgemm<float>(s, n, n, n, B, onef, X, n, nn, 1, w.Ef, n, nn, 0, zerof, w.G, n, nn);
+    // X^H formed explicitly (Xr is free until step 4): the tensor-core GEMM
+    // streams an A operand in its stored orientation twice as fast
+    conj_transpose<float>(s, X, w.Xr, n, B);
+    zgemm<float>(s, n, n, n, B, onef, w.Xr, n, nn, 0, w.Ef, n, nn, 0, zerof, w.G, n, nn);
     NRLTB_LAUNCH(k_ref_diag, cdiv((long)n * B * 32, 256), 256, 0, s, w, X);
     // 2. clusters and their Rayleigh-Ritz rotations
     NRLTB_LAUNCH(k_ref_clusters, B, 1024, 0, s, w, status);
