@@ -240,10 +240,16 @@ void zgemm_simt(cudaStream_t s, int m, int n, int k, int batch, typename cplx<T>
     if (m <= 0 || n <= 0 || batch <= 0) return;
     const GemmArgs<T> g = gemm_args<T>(m, n, k, batch, alpha, A, lda, sA, opA, B, ldb, sB, opB, beta, C, ldc, sC,
                                        triA, triB, triC);
-    constexpr int BM = 64, BN = 64, BK = 8, TM = 4, TN = 4;
+    constexpr int BM = 64, BN = 64, TM = 4, TN = 4;
     dim3 grid(cdiv(m, BM), cdiv(n, BN), batch);
     cudaEvent_t ev = kt_begin(s);
-    NRLTB_LAUNCH((zgemm_kernel<T, BM, BN, BK, TM, TN>), grid, (BM / TM) * (BN / TN), 0, s, g);
+    // short k (the rank-32 panel updates): the whole k range in one or two
+    // shared-memory stages instead of four to eight
+    constexpr int BKS = sizeof(T) == 4 ? 32 : 16;
+    if (k <= 64)
+        NRLTB_LAUNCH((zgemm_kernel<T, BM, BN, BKS, TM, TN>), grid, (BM / TM) * (BN / TN), 0, s, g);
+    else
+        NRLTB_LAUNCH((zgemm_kernel<T, BM, BN, 8, TM, TN>), grid, (BM / TM) * (BN / TN), 0, s, g);
     if (ev) kt_end(ev, s, KC_GEMM_SIMT, 8.0 * gemm_useful_macs(m, n, k, triA, triB, triC) * batch);
 }
 
