@@ -113,34 +113,61 @@ __device__ __forceinline__ TpSmem<T> tp_carve(unsigned char *base, int n)
     return s;
 }
 
-// one 32 x 32 tile of the trailing mat-vec for own row tile R (own ordinal k)
-// and column tile S; contributions go to this warp's ypart slots of tile R
+// The trailing mat-vec for own row tile R over column tiles [s_lo, s_hi), one
+// warp: y_R += A_RS v_S for S < R (lane = row), for S > R the lower tile (S, R)
+// is read by rows and its conjugate transpose applied: the lanes' products are
+// summed over all S of the strip in registers and reduced across lanes once per
+// half tile (butterfly), and the diagonal tile combines both.  Tiles inside
+// [lo, n) in both directions take an unmasked path.  Contributions are added to
+// this warp's ypart slots of tile R.
 template <typename T>
-__device__ __forceinline__ void tp_tile(const typename cplx<T>::t *A, long ld, int n, int lo, int R, int S,
-                                        const typename cplx<T>::t *vfull, typename cplx<T>::t *yp, int lane)
+__device__ __forceinline__ void tp_strip(const typename cplx<T>::t *A, long ld, int n, int lo, int R, int s_lo,
+                                         int s_hi, const typename cplx<T>::t *vfull, typename cplx<T>::t *yp,
+                                         int lane)
 {
     typedef typename cplx<T>::t C2;
     constexpr int NV = TpNV<T>::v;
-    const bool trans = S > R, diag = S == R;
-    const int rowt = trans ? S : R, colt = trans ? R : S;
-    const int r = 32 * rowt + lane;
-    const bool rv = r >= lo && r < n;
-    const C2 vr = vfull[r];
     C2 yr = cmk<T>(0, 0);
+    const bool has_upper = s_hi - 1 >= R;   // trans or diagonal tiles in the strip (warp-uniform)
 #pragma unroll 1
     for (int h = 0; h < 32 / NV; ++h) {
         C2 x[NV];
 #pragma unroll
-        for (int u = 0; u < NV; ++u) {
-            const int s = 32 * colt + h * NV + u;
-            const bool ok = rv && s >= lo && s < n && (!diag || s <= r);
-            C2 a = cmk<T>(0, 0);
-            if (ok) a = A[r + (long)s * ld];
-            if (!trans) cfma(yr, a, vfull[s]);
-            x[u] = cmk<T>(0, 0);
-            if (trans || (diag && s < r)) cfmac(x[u], a, vr);   // conj(a) v_r
+        for (int u = 0; u < NV; ++u) x[u] = cmk<T>(0, 0);
+#pragma unroll 1
+        for (int S = s_lo; S < s_hi; ++S) {
+            const bool trans = S > R, diag = S == R;
+            const int rowt = trans ? S : R, colt = trans ? R : S;
+            const int r = 32 * rowt + lane, c0 = 32 * colt + h * NV;
+            const C2 vr = vfull[r];
+            const bool interior = !diag && 32 * rowt >= lo && 32 * rowt + 31 < n && c0 >= lo && c0 + NV <= n;
+            C2 a[NV];
+            if (interior) {
+#pragma unroll
+                for (int u = 0; u < NV; ++u) a[u] = A[r + (long)(c0 + u) * ld];
+            } else {
+                const bool rv = r >= lo && r < n;
+#pragma unroll
+                for (int u = 0; u < NV; ++u) {
+                    const int sc = c0 + u;
+                    a[u] = cmk<T>(0, 0);
+                    if (rv && sc >= lo && sc < n && (!diag || sc <= r)) a[u] = A[r + (long)sc * ld];
+                }
+            }
+            if (!trans) {
+#pragma unroll
+                for (int u = 0; u < NV; ++u) cfma(yr, a[u], vfull[c0 + u]);
+            }
+            if (trans) {
+#pragma unroll
+                for (int u = 0; u < NV; ++u) cfmac(x[u], a[u], vr);   // conj(a) v_r
+            } else if (diag) {
+#pragma unroll
+                for (int u = 0; u < NV; ++u)
+                    if (c0 + u < r) cfmac(x[u], a[u], vr);
+            }
         }
-        if (trans || diag) {   // warp-uniform
+        if (has_upper) {
             tp_butterfly<NV>(x, lane);
             constexpr int sh = (NV == 32) ? 0 : (NV == 16 ? 1 : 2);
             if ((lane & ((1 << sh) - 1)) == 0) {
@@ -149,7 +176,7 @@ __device__ __forceinline__ void tp_tile(const typename cplx<T>::t *A, long ld, i
             }
         }
     }
-    if (!trans) yp[lane] = cadd(yp[lane], yr);
+    yp[lane] = cadd(yp[lane], yr);
 }
 
 template <typename T>
@@ -311,14 +338,14 @@ __global__ void __launch_bounds__(TP_THREADS, 2) k_tri_panel(EigWork<T> w, int j
         for (int e = tid; e < 32 * nown * TP_WARPS; e += TP_THREADS) sm.ypart[e] = zero;
         __syncthreads();
         {
+            // each own row tile's column tiles are cut into TP_WARPS contiguous strips
             const int tb = (i + 1) / 32, ncol = T_ - tb;
-            int k0 = 0;
-            while (k0 < nown && q + CL * k0 < tb) ++k0;
-            const int nitems = (nown - k0) * ncol;
             C2 *yw = sm.ypart + warp * 32 * nown;
-            for (int it = warp; it < nitems; it += TP_WARPS) {
-                const int k = k0 + it / ncol, S = tb + it % ncol;
-                tp_tile<T>(A, ld, n, i + 1, q + CL * k, S, sm.vfull, yw + 32 * k, lane);
+            const int s_lo = tb + (warp * ncol) / TP_WARPS, s_hi = tb + ((warp + 1) * ncol) / TP_WARPS;
+            for (int k = 0; k < nown; ++k) {
+                const int R = q + CL * k;
+                if (R < tb || s_lo >= s_hi) continue;
+                tp_strip<T>(A, ld, n, i + 1, R, s_lo, s_hi, sm.vfull, yw + 32 * k, lane);
             }
         }
         __syncthreads();
