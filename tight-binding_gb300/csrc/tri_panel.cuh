@@ -251,8 +251,15 @@ __global__ void __launch_bounds__(TP_THREADS, 2) k_tri_panel(EigWork<T> w, int j
             if (r == i + 1) *sm.a0 = a;
             if (r >= i + 2) nrm2 += a.x * a.x + a.y * a.y;
         }
-        nrm2 = block_sum(nrm2, sm.red);
-        if (tid == 0) *sm.normpart = nrm2;
+        // CTA sum with one barrier: warp sums, then thread 0 adds them in warp order
+        nrm2 = warp_sum(nrm2);
+        if (lane == 0) sm.red[warp] = nrm2;
+        __syncthreads();
+        if (tid == 0) {
+            T t = T(0);
+            for (int ww = 0; ww < TP_WARPS; ++ww) t += sm.red[ww];
+            *sm.normpart = t;
+        }
         if (i == n - 1) break;   // last column of the matrix: d only (uniform)
         cluster.sync();   // #1
 
@@ -283,8 +290,9 @@ __global__ void __launch_bounds__(TP_THREADS, 2) k_tri_panel(EigWork<T> w, int j
         }
         if (q == 0)
             for (int qq = tid; qq <= i; qq += TP_THREADS) V[qq + (long)i * ld] = zero;
-        for (int e = tid; e < TP_WARPS * 64; e += TP_THREADS) sm.pw[e] = zero;
-        __syncthreads();
+        // this warp's W^H v | V^H v slots: cleared by the warp itself
+        for (int e = lane; e < 64; e += 32) sm.pw[warp * 64 + e] = zero;
+        __syncwarp();
         for (int k = warp; k < nown; k += TP_WARPS) {
             const int r = 32 * (q + CL * k) + lane;
             const bool valid = r >= i + 1 && r < n;
@@ -383,9 +391,15 @@ __global__ void __launch_bounds__(TP_THREADS, 2) k_tri_panel(EigWork<T> w, int j
         }
         if (q == 0)
             for (int qq = tid; qq <= i; qq += TP_THREADS) wq[qq] = zero;
-        dot.x = block_sum(dot.x, sm.red);
-        dot.y = block_sum(dot.y, sm.red);
-        if (tid == 0) *sm.dotpart = dot;
+        dot.x = warp_sum(dot.x);
+        dot.y = warp_sum(dot.y);
+        if (lane == 0) { sm.red[2 * warp] = dot.x; sm.red[2 * warp + 1] = dot.y; }
+        __syncthreads();
+        if (tid == 0) {
+            C2 t = zero;
+            for (int ww = 0; ww < TP_WARPS; ++ww) { t.x += sm.red[2 * ww]; t.y += sm.red[2 * ww + 1]; }
+            *sm.dotpart = t;
+        }
         cluster.sync();   // #3
     }
     // W[:, last] = w' + alpha v of the panel's last reflected column
