@@ -431,21 +431,54 @@ __global__ void k_tri_bisect(const double *dd, const double *ee, double *lamloc,
     const TB atol = eps * TB(tnorm);
     const int j = r - b0;
     TB a = TB(lo) - TB(2) * atol - pivmin, z = TB(hi) + TB(2) * atol + pivmin;
-    for (int it = 0; it < 256; ++it) {
-        const TB mid = TB(0.5) * (a + z);
-        const TB tol = fmax(atol, TB(2) * eps * fmax(fabs(a), fabs(z))) + pivmin;
-        if (!(z - a > tol) || mid == a || mid == z) break;
+    // Sturm count: eigenvalues of the block below x
+    auto count = [&](TB x) {
         int cnt = 0;
-        TB q = TB(d[b0]) - mid;
+        TB q = TB(d[b0]) - x;
         if (fabs(q) < pivmin) q = -pivmin;
         cnt += (q < TB(0));
         for (int k = b0 + 1; k <= b1; ++k) {
             const TB ek = TB(e[k - 1]);
-            q = TB(d[k]) - mid - ek * ek / q;
+            q = TB(d[k]) - x - ek * ek / q;
             if (fabs(q) < pivmin) q = -pivmin;
             cnt += (q < TB(0));
         }
-        if (cnt <= j) a = mid; else z = mid;
+        return cnt;
+    };
+    if (sizeof(TB) == 4) {
+        // FP32 (latency bound): quadsection, three independent Sturm chains per pass
+        for (int it = 0; it < 128; ++it) {
+            const TB h = TB(0.25) * (z - a);
+            const TB m1 = a + h, m2 = TB(0.5) * (a + z), m3 = z - h;
+            const TB tol = fmax(atol, TB(2) * eps * fmax(fabs(a), fabs(z))) + pivmin;
+            if (!(z - a > tol) || m1 == a || m3 == z || !(m1 < m2) || !(m2 < m3)) break;
+            int c1 = 0, c2 = 0, c3 = 0;
+            TB q1 = TB(d[b0]) - m1, q2 = TB(d[b0]) - m2, q3 = TB(d[b0]) - m3;
+            if (fabs(q1) < pivmin) q1 = -pivmin;
+            if (fabs(q2) < pivmin) q2 = -pivmin;
+            if (fabs(q3) < pivmin) q3 = -pivmin;
+            c1 += (q1 < TB(0)); c2 += (q2 < TB(0)); c3 += (q3 < TB(0));
+            for (int k = b0 + 1; k <= b1; ++k) {
+                const TB dk = TB(d[k]), ek = TB(e[k - 1]), e2 = ek * ek;
+                q1 = dk - m1 - e2 / q1;
+                q2 = dk - m2 - e2 / q2;
+                q3 = dk - m3 - e2 / q3;
+                if (fabs(q1) < pivmin) q1 = -pivmin;
+                if (fabs(q2) < pivmin) q2 = -pivmin;
+                if (fabs(q3) < pivmin) q3 = -pivmin;
+                c1 += (q1 < TB(0)); c2 += (q2 < TB(0)); c3 += (q3 < TB(0));
+            }
+            if (c3 <= j) a = m3;
+            else if (c2 <= j) { a = m2; z = m3; }
+            else if (c1 <= j) { a = m1; z = m2; }
+            else z = m1;
+        }
+    }
+    for (int it = 0; it < 256; ++it) {   // bisection (FP64; FP32 finishes here)
+        const TB mid = TB(0.5) * (a + z);
+        const TB tol = fmax(atol, TB(2) * eps * fmax(fabs(a), fabs(z))) + pivmin;
+        if (!(z - a > tol) || mid == a || mid == z) break;
+        if (count(mid) <= j) a = mid; else z = mid;
     }
     lamloc[(long)b * n + r] = (double)(TB(0.5) * (a + z));
     blk[((long)b * n + r) * 2 + 0] = b0;
@@ -489,7 +522,7 @@ template <typename TB> struct Strided {
 // Tridiagonal eigenvectors by inverse iteration in TB arithmetic (FP64 for
 // the FP64 form, FP32 for the FP32 solve of the mixed form), one thread per
 // eigenvalue (dstein's dgttrf/dgtts2 steps, 3 iterations from a pseudo-random
-// start), written to the eigenvalue's column of Y.  Members of a cluster of
+// start in FP64, 2 in FP32), written to the eigenvalue's column of Y.  Members of a cluster of
 // close eigenvalues iterate independently; k_tri_cluster_orth then
 // orthonormalises each cluster.  An exactly degenerate cluster's iterates are
 // independent random combinations inside its invariant subspace, and a member
@@ -541,7 +574,10 @@ __global__ void k_tri_invit(const double *dd, const double *ee, const double *la
         RG[len - 1] = TB(1) / pivot(dcur);
     }
     for (int k = 0; k < len; ++k) v[k] = TB(hash_unit((unsigned)(b * 7919 + r), (unsigned)k));
-    for (int it = 0; it < 3; ++it) {
+    // dstein's one converging solve and two extra (FP64); the FP32 solve of the
+    // mixed form is refined afterwards, so one extra suffices there
+    const int iters = sizeof(TB) == 8 ? 3 : 2;
+    for (int it = 0; it < iters; ++it) {
         // solve: apply P and L (running element in a register)
         TB vc = v[0];
         for (int k = 0; k < len - 1; ++k) {
@@ -647,31 +683,39 @@ __global__ void k_real_to_cplx(const double *y, C2 *z, long count)
 }
 
 // compact-WY T factor of a block of jb <= EIG_WY reflectors (G = Vb^H Vb and T
-// column-major nbw x nbw per matrix, in global memory): column by column,
+// column-major nbw x nbw per matrix): column by column,
 // T[0:c, c] = -tau_c T[0:c, 0:c] G[0:c, c], T[c, c] = tau_c (LAPACK's larft,
-// forward columnwise).  One CTA of EIG_WY threads per matrix, thread = row.
-template <typename T>
+// forward columnwise).  One CTA of EIG_WY threads per matrix, thread = row;
+// T is built in shared memory when it fits (FP32: 128 x 129 complex = 132 KB,
+// dynamic), else in global memory.
+template <typename T, bool SMEM>
 __global__ void __launch_bounds__(EIG_WY) k_larft_wy(const typename cplx<T>::t *G, typename cplx<T>::t *Tm,
                                                      const typename cplx<T>::t *tau, int n, int j0, int jb, int nbw)
 {
     typedef typename cplx<T>::t C2;
     __shared__ C2 g[EIG_WY];
+    extern __shared__ __align__(16) unsigned char larft_smem[];
     const int b = blockIdx.x, r = threadIdx.x;
     const C2 *Gb = G + (long)b * nbw * nbw;
     C2 *Tb = Tm + (long)b * nbw * nbw;
+    const int lt = SMEM ? EIG_WY + 1 : nbw;   // column stride of the working T
+    C2 *Tw = SMEM ? (C2 *)larft_smem : Tb;
     for (int c = 0; c < jb; ++c) {
         if (r < c) g[r] = Gb[r + (long)c * nbw];
         __syncthreads();
         const C2 tc = tau[(long)b * n + j0 + c];
         if (r < c) {
             C2 acc = cmk<T>(0, 0);
-            for (int k = r; k < c; ++k) cfma(acc, Tb[r + (long)k * nbw], g[k]);
-            Tb[r + (long)c * nbw] = cscale(cmul(tc, acc), T(-1));
+            for (int k = r; k < c; ++k) cfma(acc, Tw[r + (long)k * lt], g[k]);
+            Tw[r + (long)c * lt] = cscale(cmul(tc, acc), T(-1));
         } else if (r == c) {
-            Tb[c + (long)c * nbw] = tc;
+            Tw[c + (long)c * lt] = tc;
         }
         __syncthreads();
     }
+    if (SMEM)
+        for (int c = 0; c < jb; ++c)
+            if (r <= c) Tb[r + (long)c * nbw] = Tw[r + (long)c * lt];
 }
 
 __global__ void k_fill_int(int *p, int v, int count)
@@ -795,7 +839,13 @@ void eig_solve(cudaStream_t s, EigWork<T> &w, const double2 *H, const double2 *S
             const C2 *Vb = w.V + (j0 + 1) + (long)j0 * ld;
             C2 *Yb = w.Y + (j0 + 1);
             zgemm<T>(s, jb, jb, mb, B, one, Vb, ld, ms, 1, Vb, ld, ms, 0, zero, G, nbw, sG);
-            NRLTB_LAUNCH(k_larft_wy<T>, B, EIG_WY, 0, s, G, Tf, w.tau, n, j0, jb, nbw);
+            if (sizeof(T) == 4) {
+                const int sm = (int)(sizeof(C2) * EIG_WY * (EIG_WY + 1));
+                cudaFuncSetAttribute(k_larft_wy<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+                NRLTB_LAUNCH((k_larft_wy<T, true>), B, EIG_WY, sm, s, G, Tf, w.tau, n, j0, jb, nbw);
+            } else {
+                NRLTB_LAUNCH((k_larft_wy<T, false>), B, EIG_WY, 0, s, G, Tf, w.tau, n, j0, jb, nbw);
+            }
             if (sizeof(T) == 4) {
                 // Vb^H formed explicitly in Xt: the tensor-core GEMM streams an A
                 // operand in its stored orientation twice as fast
