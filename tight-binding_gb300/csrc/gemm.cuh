@@ -262,7 +262,7 @@ void zgemm(cudaStream_t s, int m, int n, int k, int batch, typename cplx<T>::t a
            int triA = 0, int triB = 0, int triC = 0)
 {
     if (m <= 0 || n <= 0 || batch <= 0) return;
-    // tensor cores only where a 128 x 64 tile is well filled and the k loop is long
+    // tensor cores only for large m, n and a long k loop
     // (rank-32 panel updates run faster on the FMA pipe)
     if constexpr (sizeof(T) == 4) {
         if (m < 128 || n < 64 || k < 128) {

@@ -8,15 +8,16 @@
 // dropped l_a l_b is 2^-22 relative) at tensor-core rates.  A complex
 // multiply-add is four real products: 12 MMAs.
 //
-// CTA tile 128 x 64 (8 warps, warp tile 32 x 32), 16-deep k slices staged
-// through shared memory; the next slice is fetched into registers while the
-// tensor cores work on the current one.
+// CTA tile 64 x 64 (8 warps, warp tile 32 x 16, two CTAs per SM), 16-deep k
+// slices staged through shared memory; the next slice is fetched into
+// registers while the tensor cores work on the current one.
 #include "common.cuh"
 #include "gemm.cuh"
 
 namespace nrltb {
 
-constexpr int TC_BM = 128, TC_BN = 64, TC_BK = 16;
+constexpr int TC_BM = 64, TC_BN = 64, TC_BK = 16;
+constexpr int TC_NT = 2;                                  // n8 tiles per warp (warp tile 32 x 16)
 constexpr int TC_LDA = TC_BM + 4, TC_LDB = TC_BN + 4;   // [k][row] strides == 4 mod 16: conflict-free fragment loads
 constexpr int TC_THREADS = 256;
 constexpr int TC_AE = TC_BM * TC_BK / TC_THREADS;       // staged A elements per thread (8)
@@ -88,7 +89,7 @@ struct TcTile {
 };
 
 template <int TA, int TB>
-__global__ void __launch_bounds__(TC_THREADS) zgemm_tc_kernel(GemmArgs<float> g)
+__global__ void __launch_bounds__(TC_THREADS, 2) zgemm_tc_kernel(GemmArgs<float> g)
 {
     __shared__ float2 As_[TA ? TC_BM * TC_LDK : TC_BK * TC_LDA];
     __shared__ float2 Bs_[TB ? TC_BN * TC_LDK : TC_BK * TC_LDB];
@@ -109,13 +110,13 @@ __global__ void __launch_bounds__(TC_THREADS) zgemm_tc_kernel(GemmArgs<float> g)
     kbeg = (kbeg / TC_BK) * TC_BK;
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int wm = (warp & 3) * 32, wn = (warp >> 2) * 32;
+    const int wm = (warp & 1) * 32, wn = (warp >> 1) * (8 * TC_NT);
     const int gq = lane >> 2, tq = lane & 3;
-    float accr[2][4][4], acci[2][4][4];
+    float accr[2][TC_NT][4], acci[2][TC_NT][4];
 #pragma unroll
     for (int a = 0; a < 2; ++a)
 #pragma unroll
-        for (int c = 0; c < 4; ++c)
+        for (int c = 0; c < TC_NT; ++c)
 #pragma unroll
             for (int q = 0; q < 4; ++q) accr[a][c][q] = acci[a][c][q] = 0.f;
 
@@ -154,9 +155,9 @@ __global__ void __launch_bounds__(TC_THREADS) zgemm_tc_kernel(GemmArgs<float> g)
 #pragma unroll
         for (int ks = 0; ks < TC_BK; ks += 8) {
             // B fragments (k8 x n8) of the warp's 4 column tiles: head/tail of re, im
-            unsigned brh[4][2], brl[4][2], bih[4][2], bil[4][2];
+            unsigned brh[TC_NT][2], brl[TC_NT][2], bih[TC_NT][2], bil[TC_NT][2];
 #pragma unroll
-            for (int c = 0; c < 4; ++c)
+            for (int c = 0; c < TC_NT; ++c)
 #pragma unroll
                 for (int h = 0; h < 2; ++h) {
                     const float2 v = Bs.at(ks + tq + 4 * h, wn + c * 8 + gq);
@@ -178,17 +179,17 @@ __global__ void __launch_bounds__(TC_THREADS) zgemm_tc_kernel(GemmArgs<float> g)
                 }
                 // small terms first, then the head products; 8 independent chains per round
 #pragma unroll
-                for (int c = 0; c < 4; ++c) { mma_tf32(accr[a][c], arl, brh[c]); mma_tf32(acci[a][c], arl, bih[c]); }
+                for (int c = 0; c < TC_NT; ++c) { mma_tf32(accr[a][c], arl, brh[c]); mma_tf32(acci[a][c], arl, bih[c]); }
 #pragma unroll
-                for (int c = 0; c < 4; ++c) { mma_tf32(accr[a][c], arh, brl[c]); mma_tf32(acci[a][c], arh, bil[c]); }
+                for (int c = 0; c < TC_NT; ++c) { mma_tf32(accr[a][c], arh, brl[c]); mma_tf32(acci[a][c], arh, bil[c]); }
 #pragma unroll
-                for (int c = 0; c < 4; ++c) { mma_tf32(accr[a][c], anl, bih[c]); mma_tf32(acci[a][c], ail, brh[c]); }
+                for (int c = 0; c < TC_NT; ++c) { mma_tf32(accr[a][c], anl, bih[c]); mma_tf32(acci[a][c], ail, brh[c]); }
 #pragma unroll
-                for (int c = 0; c < 4; ++c) { mma_tf32(accr[a][c], anh, bil[c]); mma_tf32(acci[a][c], aih, brl[c]); }
+                for (int c = 0; c < TC_NT; ++c) { mma_tf32(accr[a][c], anh, bil[c]); mma_tf32(acci[a][c], aih, brl[c]); }
 #pragma unroll
-                for (int c = 0; c < 4; ++c) { mma_tf32(accr[a][c], arh, brh[c]); mma_tf32(acci[a][c], arh, bih[c]); }
+                for (int c = 0; c < TC_NT; ++c) { mma_tf32(accr[a][c], arh, brh[c]); mma_tf32(acci[a][c], arh, bih[c]); }
 #pragma unroll
-                for (int c = 0; c < 4; ++c) { mma_tf32(accr[a][c], anh, bih[c]); mma_tf32(acci[a][c], aih, brh[c]); }
+                for (int c = 0; c < TC_NT; ++c) { mma_tf32(accr[a][c], anh, bih[c]); mma_tf32(acci[a][c], aih, brh[c]); }
             }
         }
     }
@@ -196,7 +197,7 @@ __global__ void __launch_bounds__(TC_THREADS) zgemm_tc_kernel(GemmArgs<float> g)
 #pragma unroll
     for (int a = 0; a < 2; ++a)
 #pragma unroll
-        for (int c = 0; c < 4; ++c)
+        for (int c = 0; c < TC_NT; ++c)
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
                 const int m = m0 + wm + a * 16 + gq + (q >= 2 ? 8 : 0);
