@@ -269,19 +269,36 @@ k_oz_gemm(const __nv_bfloat16 *DA, const __nv_bfloat16 *DX, const int *exA, cons
                         for (int a = 0; a < 2; ++a) mma_bf16(p3[a][c], as[a], bs[c]);
                 }
             }
-            // fold this level of this chunk: exact integers scaled by 256^-(L+2)
+            // fold this level of this chunk: exact integers scaled by 256^-(L+2).
+            // Levels 0-2 by an exact two-sum into (hi, lo); from level 3 on the
+            // contribution (< 2^-17 of the unit scale) goes straight into lo,
+            // whose own rounding (2^-24 |lo|) already bounds the pair's error.
             const float w = ldexpf(1.0f, -8 * (L + 2));
+            if (L < 3) {
 #pragma unroll
-            for (int a = 0; a < 2; ++a)
+                for (int a = 0; a < 2; ++a)
 #pragma unroll
-                for (int c = 0; c < 2; ++c)
+                    for (int c = 0; c < 2; ++c)
 #pragma unroll
-                    for (int q = 0; q < 4; ++q) {
-                        const float re = p1[a][c][q] - p2[a][c][q];
-                        const float im = p3[a][c][q] - (p1[a][c][q] + p2[a][c][q]);
-                        df_add(hr[a][c][q], lr[a][c][q], re * w);
-                        df_add(hi_[a][c][q], li[a][c][q], im * w);
-                    }
+                        for (int q = 0; q < 4; ++q) {
+                            const float re = p1[a][c][q] - p2[a][c][q];
+                            const float im = p3[a][c][q] - (p1[a][c][q] + p2[a][c][q]);
+                            df_add(hr[a][c][q], lr[a][c][q], re * w);
+                            df_add(hi_[a][c][q], li[a][c][q], im * w);
+                        }
+            } else {
+#pragma unroll
+                for (int a = 0; a < 2; ++a)
+#pragma unroll
+                    for (int c = 0; c < 2; ++c)
+#pragma unroll
+                        for (int q = 0; q < 4; ++q) {
+                            const float re = p1[a][c][q] - p2[a][c][q];
+                            const float im = p3[a][c][q] - (p1[a][c][q] + p2[a][c][q]);
+                            lr[a][c][q] = fmaf(re, w, lr[a][c][q]);
+                            li[a][c][q] = fmaf(im, w, li[a][c][q]);
+                        }
+            }
         }
     }
     // scale by 2^(e_m + 1) 2^(f_n + 1) and store
