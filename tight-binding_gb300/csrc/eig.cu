@@ -718,6 +718,56 @@ __global__ void __launch_bounds__(EIG_WY) k_larft_wy(const typename cplx<T>::t *
             if (r <= c) Tb[r + (long)c * nbw] = Tw[r + (long)c * lt];
 }
 
+// Join the inverted 32 x 32 diagonal blocks of L pairwise: for the 64-block at
+// j0 = 64 t, W(j0+32.., j0..) = -W11 L10 W00 (W00, W11 the blocks' inverses,
+// lower triangular; L10 the 32 x 32 block of L below W00).  One CTA per
+// (pair, matrix); the three 32 x 32 blocks in shared memory.
+template <typename T>
+__global__ void __launch_bounds__(256) k_inv_pair(EigWork<T> w)
+{
+    typedef typename cplx<T>::t C2;
+    __shared__ C2 a0[32][32], b1[32][32], lt[32][32];   // [col][row]
+    const int b = blockIdx.y, n = w.n, tid = threadIdx.x;
+    const int j0 = 2 * EIG_NB * blockIdx.x, j1 = j0 + EIG_NB;
+    if (j1 >= n) return;
+    const int m1 = min(EIG_NB, n - j1);
+    const long ld = w.ld;
+    const C2 *Wi = w.Wi + b * w.mstride, *L = w.L + b * w.mstride;
+    C2 *Wo = w.Wi + b * w.mstride;
+    const C2 z = cmk<T>(0, 0);
+    for (int e = tid; e < 1024; e += 256) {
+        const int r = e & 31, c = e >> 5;
+        a0[c][r] = (r >= c) ? Wi[(j0 + r) + (long)(j0 + c) * ld] : z;
+        b1[c][r] = (r >= c && r < m1) ? Wi[(j1 + r) + (long)(j1 + c) * ld] : z;
+        lt[c][r] = (r < m1) ? L[(j1 + r) + (long)(j0 + c) * ld] : z;
+    }
+    __syncthreads();
+    // T1 = W11 L10 (W11 lower: k <= r), four entries per thread
+    C2 t1[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+        const int e = tid + 256 * u, r = e & 31, c = e >> 5;
+        C2 acc = z;
+        for (int k = 0; k <= r; ++k) cfma(acc, b1[k][r], lt[c][k]);
+        t1[u] = acc;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+        const int e = tid + 256 * u;
+        lt[e >> 5][e & 31] = t1[u];
+    }
+    __syncthreads();
+    // W10 = -T1 W00 (W00 lower: k >= c)
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+        const int e = tid + 256 * u, r = e & 31, c = e >> 5;
+        C2 acc = z;
+        for (int k = c; k < 32; ++k) cfma(acc, lt[k][r], a0[c][k]);
+        if (r < m1) Wo[(j1 + r) + (long)(j0 + c) * ld] = cscale(acc, T(-1));
+    }
+}
+
 __global__ void k_fill_int(int *p, int v, int count)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -752,16 +802,22 @@ void eig_solve(cudaStream_t s, EigWork<T> &w, const double2 *H, const double2 *S
                      w.L + (j0 + jb) + (long)(j0 + jb) * ld, ld, ms, 0, 0, 1);
         }
     }
-    // 2. Wi = L^{-1}, bottom-up blocked (diagonal blocks already inverted)
+    // 2. Wi = L^{-1}, bottom-up blocked: the 32 x 32 diagonal blocks are already
+    //    inverted; pairs of them are joined into 64 x 64 diagonal inverses, then
+    //    the 64-wide block columns are filled from the bottom (GEMMs with n = 64,
+    //    wide enough for the tensor-core tile)
     {
-        int jlast = ((n - 1) / EIG_NB) * EIG_NB;
-        for (int j0 = jlast; j0 >= 0; j0 -= EIG_NB) {
-            const int jb = std::min(EIG_NB, n - j0), rem = n - j0 - jb;
+        const int npair = cdiv(n, 2 * EIG_NB);
+        NRLTB_LAUNCH(k_inv_pair<T>, dim3(npair, B), 256, 0, s, w);
+        constexpr int NB2 = 2 * EIG_NB;
+        int jlast = ((n - 1) / NB2) * NB2;
+        for (int j0 = jlast; j0 >= 0; j0 -= NB2) {
+            const int jb = std::min(NB2, n - j0), rem = n - j0 - jb;
             if (rem <= 0) continue;
             const long ldx = n;
             zgemm<T>(s, rem, jb, rem, B, one, w.Wi + (long)(j0 + jb) * (ld + 1), ld, ms, 0,
-                     w.L + (j0 + jb) + (long)j0 * ld, ld, ms, 0, zero, w.Xt, ldx, (long)EIG_NB * n, 1, 0, 0);
-            zgemm<T>(s, rem, jb, jb, B, mone, w.Xt, ldx, (long)EIG_NB * n, 0, w.Wi + (long)j0 * (ld + 1), ld, ms, 0,
+                     w.L + (j0 + jb) + (long)j0 * ld, ld, ms, 0, zero, w.Xt, ldx, (long)NB2 * n, 1, 0, 0);
+            zgemm<T>(s, rem, jb, jb, B, mone, w.Xt, ldx, (long)NB2 * n, 0, w.Wi + (long)j0 * (ld + 1), ld, ms, 0,
                      zero, w.Wi + (j0 + jb) + (long)j0 * ld, ld, ms, 0, 2, 0);
         }
     }

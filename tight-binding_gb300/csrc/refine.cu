@@ -208,8 +208,11 @@ __global__ void __launch_bounds__(REF_CMAX * REF_CMAX) k_ref_rr(RefineWork w, co
     // T_rq = x_r^H (H x_q), R_rq = x_r^H (S x_q) in FP64, one thread per (q, r)
     // pair: the FP64 work of a large cluster is spread over the SM's four
     // sub-partitions
-    if (tid < c * c) {
-        const int q = tid / c, r = tid % c;
+    // (Hermitian blocks: only r <= q is formed, the other triangle is its conjugate)
+    if (tid < c * (c + 1) / 2) {
+        int q = 0, rem = tid;
+        while (rem > q) { rem -= q + 1; ++q; }
+        const int r = rem;
         const float2 *xr = X + mo + (long)ord[p + r] * n;
         const double2 *hq = w.YH + mo + (long)ord[p + q] * n, *sq = w.YS + mo + (long)ord[p + q] * n;
         double2 t = make_double2(0, 0), u = make_double2(0, 0);
@@ -221,6 +224,8 @@ __global__ void __launch_bounds__(REF_CMAX * REF_CMAX) k_ref_rr(RefineWork w, co
         }
         A[q][r] = t;
         Bm[q][r] = u;
+        A[r][q] = cconj(t);
+        Bm[r][q] = cconj(u);
     }
     __syncthreads();
     if (warp != 0) return;
