@@ -33,7 +33,9 @@ template <typename T> void eig_work_carve(EigWork<T> &w, void *base, int n, int 
     w.A = (C2 *)take(sizeof(C2) * nn * nb);
     w.Y = (C2 *)take(sizeof(C2) * nn * nb);
     w.V = (C2 *)take(sizeof(C2) * nn * nb);
-    w.Wp = (C2 *)take(sizeof(C2) * n * EIG_NB * nb);
+    w.VW = (C2 *)take(sizeof(C2) * n * 3 * EIG_NB * nb);
+    w.wps = (long)n * 3 * EIG_NB;
+    w.Wp = w.VW + (long)n * EIG_NB;
     w.wq = (C2 *)take(sizeof(C2) * n * nb);
     w.col = (C2 *)take(sizeof(C2) * n * nb);
     w.tau = (C2 *)take(sizeof(C2) * n * nb);
@@ -135,7 +137,7 @@ __global__ void __launch_bounds__(EIG_ROWS) k_tri_colupd(EigWork<T> w, int i, in
     const int b = blockIdx.y, n = w.n, c = i - j0, tid = threadIdx.x;
     const long ld = w.ld;
     C2 *A = w.A + b * w.mstride, *V = w.V + b * w.mstride;
-    C2 *Wp = w.Wp + (long)b * n * EIG_NB, *wq = w.wq + (long)b * n, *col = w.col + (long)b * n;
+    C2 *Wp = w.Wp + (long)b * w.wps, *wq = w.wq + (long)b * n, *col = w.col + (long)b * n;
     const C2 alpha_prev = w.sc[b * 4 + 1];
     // row i of the panel's V and W (W[i, c-1] recomputed from w', never read from Wp)
     if (tid < c) {
@@ -211,7 +213,7 @@ __global__ void __launch_bounds__(EIG_ROWS) k_tri_vdots(EigWork<T> w, int i, int
     __shared__ unsigned ticket;
     const int b = blockIdx.y, n = w.n, c = i - j0, tid = threadIdx.x;
     const long ld = w.ld;
-    C2 *V = w.V + b * w.mstride, *Wp = w.Wp + (long)b * n * EIG_NB, *col = w.col + (long)b * n;
+    C2 *V = w.V + b * w.mstride, *Wp = w.Wp + (long)b * w.wps, *col = w.col + (long)b * n;
     const C2 scale = w.sc[b * 4 + 0];
     const int r = i + 1 + blockIdx.x * EIG_ROWS + tid;
     C2 v = cmk<T>(0, 0);
@@ -330,7 +332,7 @@ __global__ void __launch_bounds__(EIG_ROWS) k_tri_wupd(EigWork<T> w, int i, int 
     __shared__ unsigned ticket;
     const int b = blockIdx.y, n = w.n, c = i - j0, tid = threadIdx.x;
     const long ld = w.ld;
-    const C2 *V = w.V + b * w.mstride, *Wp = w.Wp + (long)b * n * EIG_NB;
+    const C2 *V = w.V + b * w.mstride, *Wp = w.Wp + (long)b * w.wps;
     C2 *wq = w.wq + (long)b * n;
     const C2 *y = w.col + (long)b * n;
     const C2 tau = w.tau[(long)b * n + i];
@@ -386,7 +388,7 @@ __global__ void k_tri_wfinal(EigWork<T> w, int i, int c)
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
         C2 v = (r > i) ? w.V[b * w.mstride + r + (long)i * w.ld] : cmk<T>(0, 0);
         C2 q = (r > i) ? w.wq[(long)b * n + r] : cmk<T>(0, 0);
-        w.Wp[(long)b * n * EIG_NB + r + (long)c * n] = cadd(q, cmul(alpha, v));
+        w.Wp[(long)b * w.wps + r + (long)c * n] = cadd(q, cmul(alpha, v));
     }
 }
 
@@ -407,6 +409,11 @@ __device__ inline void find_block(const double *d, const double *e, int n, int r
 template <typename TB> __device__ inline TB tiny_of();
 template <> __device__ inline float tiny_of<float>() { return FLT_MIN; }
 template <> __device__ inline double tiny_of<double>() { return DBL_MIN; }
+// Quotient in the tridiagonal recurrences: FP32 takes the reciprocal-based
+// quotient (2 ulp; |b| stays below 2^126 there), FP64 the IEEE one.  The FP32
+// eigenpairs are refined to FP64 accuracy afterwards.
+__device__ inline float tri_div(float a, float b) { return __fdividef(a, b); }
+__device__ inline double tri_div(double a, double b) { return a / b; }
 
 // One thread per (matrix, row r): eigenvalue number r - b0 of r's block.
 template <typename TB>
@@ -446,32 +453,50 @@ __global__ void k_tri_bisect(const double *dd, const double *ee, double *lamloc,
         return cnt;
     };
     if (sizeof(TB) == 4) {
-        // FP32 (latency bound): quadsection, three independent Sturm chains per pass
-        for (int it = 0; it < 128; ++it) {
-            const TB h = TB(0.25) * (z - a);
-            const TB m1 = a + h, m2 = TB(0.5) * (a + z), m3 = z - h;
+        // FP32 (latency bound): octasection, seven independent Sturm chains per
+        // pass; the new interval lies between the last point counting <= j
+        // eigenvalues below it and the first counting more
+        constexpr int NP = 7;
+        for (int it = 0; it < 64; ++it) {
+            const TB h = TB(1.0 / (NP + 1)) * (z - a);
             const TB tol = fmax(atol, TB(2) * eps * fmax(fabs(a), fabs(z))) + pivmin;
-            if (!(z - a > tol) || m1 == a || m3 == z || !(m1 < m2) || !(m2 < m3)) break;
-            int c1 = 0, c2 = 0, c3 = 0;
-            TB q1 = TB(d[b0]) - m1, q2 = TB(d[b0]) - m2, q3 = TB(d[b0]) - m3;
-            if (fabs(q1) < pivmin) q1 = -pivmin;
-            if (fabs(q2) < pivmin) q2 = -pivmin;
-            if (fabs(q3) < pivmin) q3 = -pivmin;
-            c1 += (q1 < TB(0)); c2 += (q2 < TB(0)); c3 += (q3 < TB(0));
+            TB m[NP];
+            bool ok = z - a > tol;
+#pragma unroll
+            for (int i = 0; i < NP; ++i) m[i] = a + TB(i + 1) * h;
+            ok = ok && m[0] > a && m[NP - 1] < z;
+#pragma unroll
+            for (int i = 0; i + 1 < NP; ++i) ok = ok && m[i] < m[i + 1];
+            if (!ok) break;
+            TB q[NP];
+            int c[NP];
+            const TB d0 = TB(d[b0]);
+#pragma unroll
+            for (int i = 0; i < NP; ++i) {
+                q[i] = d0 - m[i];
+                if (fabs(q[i]) < pivmin) q[i] = -pivmin;
+                c[i] = q[i] < TB(0);
+            }
             for (int k = b0 + 1; k <= b1; ++k) {
                 const TB dk = TB(d[k]), ek = TB(e[k - 1]), e2 = ek * ek;
-                q1 = dk - m1 - e2 / q1;
-                q2 = dk - m2 - e2 / q2;
-                q3 = dk - m3 - e2 / q3;
-                if (fabs(q1) < pivmin) q1 = -pivmin;
-                if (fabs(q2) < pivmin) q2 = -pivmin;
-                if (fabs(q3) < pivmin) q3 = -pivmin;
-                c1 += (q1 < TB(0)); c2 += (q2 < TB(0)); c3 += (q3 < TB(0));
+#pragma unroll
+                for (int i = 0; i < NP; ++i) {
+                    q[i] = dk - m[i] - tri_div(e2, q[i]);
+                    if (fabs(q[i]) < pivmin) q[i] = -pivmin;
+                    c[i] += q[i] < TB(0);
+                }
             }
-            if (c3 <= j) a = m3;
-            else if (c2 <= j) { a = m2; z = m3; }
-            else if (c1 <= j) { a = m1; z = m2; }
-            else z = m1;
+            TB na = a, nz = z;
+            bool found = false;
+#pragma unroll
+            for (int i = 0; i < NP; ++i) {
+                if (!found) {
+                    if (c[i] <= j) na = m[i];
+                    else { nz = m[i]; found = true; }
+                }
+            }
+            a = na;
+            z = nz;
         }
     }
     for (int it = 0; it < 256; ++it) {   // bisection (FP64; FP32 finishes here)
@@ -559,19 +584,19 @@ __global__ void k_tri_invit(const double *dd, const double *ee, const double *la
             TB dnext = TB(d[b0 + k + 1]) - lam;
             TB dunext = (k < len - 2) ? TB(e[b0 + k + 1]) : TB(0);
             if (fabs(dcur) >= fabs(dlk)) {
-                const TB f = (dcur != TB(0)) ? dlk / dcur : TB(0);
-                DL[k] = f; RG[k] = TB(1) / pivot(dcur); DU[k] = ducur; DU2[k] = TB(0); PV[k] = TB(0);
+                const TB f = (dcur != TB(0)) ? tri_div(dlk, dcur) : TB(0);
+                DL[k] = f; RG[k] = tri_div(TB(1), pivot(dcur)); DU[k] = ducur; DU2[k] = TB(0); PV[k] = TB(0);
                 dnext -= f * ducur;
             } else {
-                const TB f = dcur / dlk;
-                DL[k] = f; RG[k] = TB(1) / pivot(dlk); DU[k] = dnext; DU2[k] = dunext; PV[k] = TB(1);
+                const TB f = tri_div(dcur, dlk);
+                DL[k] = f; RG[k] = tri_div(TB(1), pivot(dlk)); DU[k] = dnext; DU2[k] = dunext; PV[k] = TB(1);
                 dnext = ducur - f * dnext;
                 dunext = -f * dunext;
             }
             dcur = dnext;
             ducur = dunext;
         }
-        RG[len - 1] = TB(1) / pivot(dcur);
+        RG[len - 1] = tri_div(TB(1), pivot(dcur));
     }
     for (int k = 0; k < len; ++k) v[k] = TB(hash_unit((unsigned)(b * 7919 + r), (unsigned)k));
     // dstein's one converging solve and two extra (FP64); the FP32 solve of the
@@ -768,6 +793,21 @@ __global__ void __launch_bounds__(256) k_inv_pair(EigWork<T> w)
     }
 }
 
+// Rows t0.. of the panel's V columns j0..j0+jb into columns 0..jb and
+// 2 EIG_NB.. of VW (W sits in between), for the merged trailing update
+template <typename C2>
+__global__ void k_copy_vpanel(const C2 *V, long ld, long ms, C2 *VW, long ldw, long wps, int t0, int j0, int jb,
+                              int rem)
+{
+    const long e = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (e >= (long)rem * jb) return;
+    const int b = blockIdx.y, r = (int)(e % rem), c = (int)(e / rem);
+    const C2 v = V[b * ms + t0 + r + (long)(j0 + c) * ld];
+    C2 *o = VW + b * wps + t0 + r;
+    o[(long)c * ldw] = v;
+    o[(long)(2 * EIG_NB + c) * ldw] = v;
+}
+
 __global__ void k_fill_int(int *p, int v, int count)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -856,8 +896,16 @@ void eig_solve(cudaStream_t s, EigWork<T> &w, const double2 *H, const double2 *S
         if (rem > 0) {
             C2 *Vp = w.V + t0 + (long)j0 * ld, *Wpp = w.Wp + t0;
             C2 *At = w.A + (long)t0 * (ld + 1);
-            zgemm<T>(s, rem, rem, jb, B, mone, Vp, ld, ms, 0, Wpp, n, (long)n * EIG_NB, 1, one, At, ld, ms, 0, 0, 1);
-            zgemm<T>(s, rem, rem, jb, B, mone, Wpp, n, (long)n * EIG_NB, 0, Vp, ld, ms, 1, one, At, ld, ms, 0, 0, 1);
+            if (jb == EIG_NB) {
+                // A -= [Vp Wp] [Wp Vp]^H in one rank-64 update: Vp copied on both sides of W
+                NRLTB_LAUNCH(k_copy_vpanel<C2>, dim3(cdiv((long)rem * jb, 256), B), 256, 0, s, w.V, ld, ms, w.VW,
+                             (long)n, w.wps, t0, j0, jb, rem);
+                zgemm<T>(s, rem, rem, 2 * EIG_NB, B, mone, w.VW + t0, n, w.wps, 0, w.VW + t0 + (long)n * EIG_NB, n,
+                         w.wps, 1, one, At, ld, ms, 0, 0, 1);
+            } else {
+                zgemm<T>(s, rem, rem, jb, B, mone, Vp, ld, ms, 0, Wpp, n, w.wps, 1, one, At, ld, ms, 0, 0, 1);
+                zgemm<T>(s, rem, rem, jb, B, mone, Wpp, n, w.wps, 0, Vp, ld, ms, 1, one, At, ld, ms, 0, 0, 1);
+            }
         }
     }
     // 5. tridiagonal eigenproblem (FP64 inverse iteration; bisection in T)

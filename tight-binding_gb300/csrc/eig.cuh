@@ -41,7 +41,9 @@ template <typename T> struct EigWork {
     C2 *A;                          // reduced matrix, overwritten by tridiagonalisation
     C2 *Y;                          // scratch n x n (reduction product, then Q Y)
     C2 *V;                          // Householder vectors, column i in V[:, i]
-    C2 *Wp;                         // panel W, n x EIG_NB per matrix
+    C2 *Wp;                         // panel W, n x EIG_NB per matrix (matrix stride wps)
+    C2 *VW;                         // [V panel | W | V panel], n x 3 EIG_NB per matrix; Wp is its middle
+    long wps;                       // matrix stride of VW and Wp
     C2 *wq;                         // w' of the current column, n per matrix
     C2 *col;                        // current updated column, n per matrix
     C2 *tau;                        // n per matrix

@@ -192,7 +192,7 @@ __global__ void __launch_bounds__(TP_THREADS, 2) k_tri_panel(EigWork<T> w, int j
     const long ld = w.ld;
     const C2 *A = w.A + b * w.mstride;
     C2 *V = w.V + b * w.mstride;
-    C2 *Wp = w.Wp + (long)b * n * EIG_NB, *wq = w.wq + (long)b * n;
+    C2 *Wp = w.Wp + (long)b * w.wps, *wq = w.wq + (long)b * n;
     const int T_ = cdiv(n, 32);
     const int nown = (q < T_) ? (T_ - 1 - q) / CL + 1 : 0;
     TpSmem<T> sm = tp_carve<T>(tp_raw, n);
