@@ -40,12 +40,18 @@ int nrltb_bench_refprod_run(nrltb_ctx *ctx, int method, int n, int batch, const 
 
 /* One FP32 complex GEMM of the eigensolver's kernel on caller data, for
  * accuracy checks: C = alpha op(A) op(B) + beta C with the kernel's op and
- * triangle flags (gemm.cuh), one matrix; method 1 = tensor cores, 2 = SIMT.
+ * triangle flags (gemm.cuh), one matrix; method 1 = the library's dispatch,
+ * 2 = SIMT, 3 = the tcgen05 kernel (op A = op B = N only), 4 = the mma.sync
+ * tensor-core kernel.
  * A, B, C are host arrays (column-major complex FP32, leading dimensions
  * lda, ldb, ldc); alpha, beta are {re, im}. */
 int nrltb_bench_cgemm_run(nrltb_ctx *ctx, int method, int m, int n, int k, int opA, int opB, int triA,
                           int triB, int triC, const float alpha[2], const float beta[2], const float *A,
                           int lda, const float *B, int ldb, float *C, int ldc);
+
+/* Fault flag of the tcgen05 GEMM kernel: nonzero once a bounded barrier wait
+ * inside it ran out (the kernel then leaves C untouched); clear = 1 resets it. */
+int nrltb_bench_umma_fault(int clear);
 
 /* Kernel-class timing of the context's own calls: with on = 1 every later
  * launch of a timed class (0 = FP32 tensor-core GEMM, 1 = SIMT GEMM, 2 = the

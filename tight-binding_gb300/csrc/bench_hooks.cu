@@ -231,8 +231,9 @@ extern "C" int nrltb_bench_cgemm_run(nrltb_ctx *ctx, int method, int m, int n, i
                                      int triB, int triC, const float alpha[2], const float beta[2], const float *A,
                                      int lda, const float *B, int ldb, float *C, int ldc)
 {
-    if (!ctx || (method != 1 && method != 2) || m < 1 || n < 1 || k < 1 || !alpha || !beta || !A || !B || !C)
+    if (!ctx || method < 1 || method > 4 || m < 1 || n < 1 || k < 1 || !alpha || !beta || !A || !B || !C)
         return NRLTB_E_ARG;
+    if (method == 3 && (opA != 0 || opB != 0)) return NRLTB_E_ARG;
     if (opA < 0 || opA > 1 || opB < 0 || opB > 1 || triA < 0 || triA > 2 || triB < 0 || triB > 2 || triC < 0 ||
         triC > 2)
         return NRLTB_E_ARG;
@@ -252,12 +253,23 @@ extern "C" int nrltb_bench_cgemm_run(nrltb_ctx *ctx, int method, int m, int n, i
     const float2 al = make_float2(alpha[0], alpha[1]), be = make_float2(beta[0], beta[1]);
     const float2 *dA = (const float2 *)d.p[0], *dB = (const float2 *)d.p[1];
     float2 *dC = (float2 *)d.p[2];
+    const GemmArgs<float> g = gemm_args<float>(m, n, k, 1, al, dA, lda, 0, opA, dB, ldb, 0, opB, be, dC, ldc, 0,
+                                               triA, triB, triC);
     if (method == 1)
         zgemm<float>(s, m, n, k, 1, al, dA, lda, 0, opA, dB, ldb, 0, opB, be, dC, ldc, 0, triA, triB, triC);
-    else
+    else if (method == 2)
         zgemm_simt<float>(s, m, n, k, 1, al, dA, lda, 0, opA, dB, ldb, 0, opB, be, dC, ldc, 0, triA, triB, triC);
+    else if (method == 3)
+        zgemm_umma_launch(s, g);
+    else
+        zgemm_tc_launch(s, g);
     if (cudaMemcpyAsync(C, dC, sizeof(float2) * nc, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
         cudaStreamSynchronize(s) != cudaSuccess)
         return NRLTB_E_CUDA;
     return cudaGetLastError() == cudaSuccess ? NRLTB_OK : NRLTB_E_CUDA;
+}
+
+extern "C" int nrltb_bench_umma_fault(int clear)
+{
+    return (int)zgemm_umma_fault(clear != 0);
 }

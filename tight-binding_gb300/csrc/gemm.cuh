@@ -140,8 +140,13 @@ zgemm_kernel(GemmArgs<T> g)
     }
 }
 
-// FP32 on the tensor cores (gemm_tc.cu)
+// FP32 on the tensor cores: tcgen05 with tensor-memory accumulators for
+// untransposed operands (gemm_umma.cu), mma.sync otherwise (gemm_tc.cu)
 void zgemm_tc_launch(cudaStream_t s, const GemmArgs<float> &g);
+bool zgemm_umma_supported(const GemmArgs<float> &g);
+void zgemm_umma_launch(cudaStream_t s, const GemmArgs<float> &g);
+// fault flag of the tcgen05 kernel (a barrier wait that ran out); clear resets it
+unsigned zgemm_umma_fault(bool clear);
 
 // dst = src^H for `batch` rows x cols matrices (src leading dimension lds,
 // stride ss; dst leading dimension ldd, stride ds), 32 x 32 tiles through
@@ -271,8 +276,10 @@ void zgemm(cudaStream_t s, int m, int n, int k, int batch, typename cplx<T>::t a
             return;
         }
         cudaEvent_t ev = kt_begin(s);
-        zgemm_tc_launch(s, gemm_args<T>(m, n, k, batch, alpha, A, lda, sA, opA, B, ldb, sB, opB, beta, C, ldc, sC,
-                                        triA, triB, triC));
+        const GemmArgs<float> g = gemm_args<T>(m, n, k, batch, alpha, A, lda, sA, opA, B, ldb, sB, opB, beta, C,
+                                               ldc, sC, triA, triB, triC);
+        if (zgemm_umma_supported(g)) zgemm_umma_launch(s, g);
+        else zgemm_tc_launch(s, g);
         if (ev) kt_end(ev, s, KC_GEMM_TC, 8.0 * gemm_useful_macs(m, n, k, triA, triB, triC) * batch);
     } else {
         zgemm_simt<T>(s, m, n, k, batch, alpha, A, lda, sA, opA, B, ldb, sB, opB, beta, C, ldc, sC, triA, triB,

@@ -111,6 +111,7 @@ GPU_SYMBOLS = [
     ("nrltb_bench_kernel_stats", C.c_int, [_vp, C.c_int, _dp, _dp, C.POINTER(C.c_int)]),
     ("nrltb_bench_cgemm_run", C.c_int, [_vp] + [C.c_int] * 9 + [_vp, _vp, _vp, C.c_int, _vp, C.c_int, _vp,
                                                                   C.c_int]),
+    ("nrltb_bench_umma_fault", C.c_int, [C.c_int]),
 ]
 
 HOST_SYMBOLS = [

@@ -17,7 +17,7 @@ HOST = os.path.join(PKG_ROOT, "host")
 INCLUDE = os.path.join(REPO_ROOT, "include")
 OBJ = os.path.join(LIB_DIR, "obj")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["nrltb_api.cu", "eig.cu", "setup.cu", "sums.cu", "refine.cu", "ozaki.cu", "gemm_tc.cu", "bench_hooks.cu", "noalloc.cu"]
+CU_SOURCES = ["nrltb_api.cu", "eig.cu", "setup.cu", "sums.cu", "refine.cu", "ozaki.cu", "gemm_tc.cu", "gemm_umma.cu", "bench_hooks.cu", "noalloc.cu"]
 DRIVER = os.path.join(LIB_DIR, "nrltb_static")
 
 
