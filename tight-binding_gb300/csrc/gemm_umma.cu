@@ -5,17 +5,18 @@
 //
 // 3xTF32: each FP32 operand x is split into a TF32 head h = tf32(x) and tail
 // l = tf32(x - h); a real product is l_a h_b + h_a l_b + h_a h_b (the dropped
-// l_a l_b is 2^-22 relative).  Complex: the B tile is staged as three row
-// blocks [-Bi | Br | Bi] of 64 columns each, so that one M = 128, N = 128 MMA
-// gives Ar [Br | Bi] (columns 0-63 into Re, 64-127 into Im) and another
-// Ai [-Bi | Br]; both accumulate into one 128 x 128 FP32 tensor-memory tile
-// holding Re | Im of a 128 x 64 complex output tile.  Six MMAs per 8-deep k
-// step.
+// l_a l_b is 2^-22 relative).  Complex: the B tile is staged as the row
+// blocks [Br | Bi] (64 columns each), and two M = 128, N = 128 accumulators in
+// tensor memory take P = Ar [Br | Bi] and Q = Ai [Br | Bi]; the epilogue forms
+// Re = P[:, j] - Q[:, 64 + j], Im = P[:, 64 + j] + Q[:, j] for a 128 x 64
+// complex output tile.  Six MMAs per 8-deep k step.
 //
-// CTA: 256 threads; all stage operands (global -> registers -> head/tail
+// CTA: 256 threads, two CTAs per SM (96 KB stage each, 256 tensor-memory
+// columns each); all threads stage operands (global -> registers -> head/tail
 // split -> 128-byte-swizzled K-major shared-memory tiles), thread 0 issues the
-// MMAs and commits them to a shared-memory barrier per stage; two 32-deep
-// stages, the next slice's global loads in flight while the tensor cores work.
+// MMAs and commits them to a shared-memory barrier; the next 32-deep slice's
+// global loads are in flight while the tensor cores work, and the other CTA
+// on the SM fills the tensor pipe while this one stages or stores.
 // Epilogue: each warp reads 32 rows x 32 complex columns of tensor memory.
 // Every barrier wait is bounded (about two seconds); on expiry the kernel
 // records a fault flag and leaves without touching C.
@@ -29,10 +30,10 @@ namespace {
 constexpr int UM_BM = 128, UM_BN = 64, UM_BK = 32;
 constexpr int UM_THREADS = 256;
 constexpr int UM_APL = UM_BM * 128;          // one A plane: 128 rows x 32 TF32 (128 B)
-constexpr int UM_BPL = 3 * UM_BN * 128;      // one B plane: rows -Bi | Br | Bi
+constexpr int UM_BPL = 2 * UM_BN * 128;      // one B plane: rows Br | Bi
 constexpr int UM_STAGE = 4 * UM_APL + 2 * UM_BPL;   // A: re h, re l, im h, im l; B: h, l
-constexpr int UM_SMEM = 2 * UM_STAGE + 1024 + 64;   // two stages, alignment slack, barriers
-constexpr uint32_t UM_TMEM_COLS = 128;
+constexpr int UM_SMEM = UM_STAGE + 1024 + 64;        // one stage, alignment slack, barrier
+constexpr uint32_t UM_TMEM_COLS = 256;               // P | Q
 constexpr unsigned long long UM_WAIT_NS = 2000000000ull;
 
 // instruction descriptor, kind::tf32: D f32 (bits 4-5 = 1), A and B tf32
@@ -122,17 +123,15 @@ __device__ __forceinline__ uint32_t um_swz(int r, int g)
     return (uint32_t)((r >> 3) * 1024 + (r & 7) * 128 + ((g ^ (r & 7)) << 4));
 }
 
-// heads and tails of four values into two planes (flip = negate)
-__device__ __forceinline__ void um_put4(unsigned char *ph, unsigned char *pl, uint32_t off, const float x[4],
-                                        bool flip)
+// heads and tails of four values into two planes
+__device__ __forceinline__ void um_put4(unsigned char *ph, unsigned char *pl, uint32_t off, const float x[4])
 {
     uint4 h, l;
     uint32_t hh[4], ll[4];
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
-        const float v = flip ? -x[j] : x[j];
-        hh[j] = um_tf32(v);
-        ll[j] = um_tf32(v - __uint_as_float(hh[j]));
+        hh[j] = um_tf32(x[j]);
+        ll[j] = um_tf32(x[j] - __uint_as_float(hh[j]));
     }
     h = make_uint4(hh[0], hh[1], hh[2], hh[3]);
     l = make_uint4(ll[0], ll[1], ll[2], ll[3]);
@@ -140,7 +139,7 @@ __device__ __forceinline__ void um_put4(unsigned char *ph, unsigned char *pl, ui
     *(uint4 *)(pl + off) = l;
 }
 
-__global__ void __launch_bounds__(UM_THREADS, 1) zgemm_umma_kernel(GemmArgs<float> g)
+__global__ void __launch_bounds__(UM_THREADS, 2) zgemm_umma_kernel(GemmArgs<float> g)
 {
     extern __shared__ __align__(16) unsigned char um_raw[];
     const int b = blockIdx.z;
@@ -161,9 +160,9 @@ __global__ void __launch_bounds__(UM_THREADS, 1) zgemm_umma_kernel(GemmArgs<floa
     // 1024-aligned tiles (the swizzle pattern follows address bits 4-9)
     const uint32_t raw_s = um_smem_addr(um_raw);
     unsigned char *base = um_raw + (((raw_s + 1023u) & ~1023u) - raw_s);
-    uint64_t *bars = (uint64_t *)(base + 2 * UM_STAGE);
-    uint32_t *tslot = (uint32_t *)(bars + 2);
-    const uint32_t bar0 = um_smem_addr(bars);   // stage s: bar0 + 8 s
+    uint64_t *bar = (uint64_t *)(base + UM_STAGE);
+    uint32_t *tslot = (uint32_t *)(bar + 1);
+    const uint32_t bar0 = um_smem_addr(bar);
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     if (warp == 0) {
@@ -173,7 +172,6 @@ __global__ void __launch_bounds__(UM_THREADS, 1) zgemm_umma_kernel(GemmArgs<floa
     }
     if (tid == 0) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(bar0) : "memory");
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(bar0 + 8) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -215,8 +213,8 @@ __global__ void __launch_bounds__(UM_THREADS, 1) zgemm_umma_kernel(GemmArgs<floa
             float re[4], im[4];
 #pragma unroll
             for (int j = 0; j < 4; ++j) { re[j] = ra[4 * u + j].x; im[j] = ra[4 * u + j].y; }
-            um_put4(st, st + UM_APL, off, re, false);
-            um_put4(st + 2 * UM_APL, st + 3 * UM_APL, off, im, false);
+            um_put4(st, st + UM_APL, off, re);
+            um_put4(st + 2 * UM_APL, st + 3 * UM_APL, off, im);
         }
         unsigned char *bh = st + 4 * UM_APL, *bl = bh + UM_BPL;
 #pragma unroll
@@ -225,58 +223,56 @@ __global__ void __launch_bounds__(UM_THREADS, 1) zgemm_umma_kernel(GemmArgs<floa
             float re[4], im[4];
 #pragma unroll
             for (int j = 0; j < 4; ++j) { re[j] = rb[4 * u + j].x; im[j] = rb[4 * u + j].y; }
-            um_put4(bh, bl, um_swz(UM_BN + rb_n, gk), re, false);
-            um_put4(bh, bl, um_swz(2 * UM_BN + rb_n, gk), im, false);
-            um_put4(bh, bl, um_swz(rb_n, gk), im, true);
+            um_put4(bh, bl, um_swz(rb_n, gk), re);
+            um_put4(bh, bl, um_swz(UM_BN + rb_n, gk), im);
         }
     };
 
     bool fail = false;
     if (nk > 0) fetch(kbeg);
     for (int c = 0; c < nk; ++c) {
-        const int s = c & 1;
-        if (c >= 2) {
-            // the MMAs of chunk c - 2 have finished reading stage s
+        if (c >= 1) {
+            // the MMAs of chunk c - 1 have finished reading the stage
             int ok = 1;
-            if (tid == 0) ok = um_wait(bar0 + 8 * s, ((c - 2) >> 1) & 1);
+            if (tid == 0) ok = um_wait(bar0, (c - 1) & 1);
             if (__syncthreads_or(!ok)) { fail = true; break; }
         }
-        store(base + s * UM_STAGE);
+        store(base);
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         __syncthreads();
         if (c + 1 < nk) fetch(kbeg + (c + 1) * UM_BK);
         if (tid == 0) {
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const uint32_t sa = um_smem_addr(base + s * UM_STAGE);
+            const uint32_t sa = um_smem_addr(base);
             const uint32_t sb = sa + 4 * UM_APL;
+            const uint32_t tp = tmem, tq = tmem + 128;
 #pragma unroll
             for (int ks = 0; ks < UM_BK / 8; ++ks) {
                 const uint32_t ko = 32u * ks;
                 const uint64_t arh = um_desc(sa + ko), arl = um_desc(sa + UM_APL + ko);
                 const uint64_t aih = um_desc(sa + 2 * UM_APL + ko), ail = um_desc(sa + 3 * UM_APL + ko);
-                // [Br | Bi] = rows 64-191, [-Bi | Br] = rows 0-127
-                const uint64_t ph = um_desc(sb + UM_BN * 128 + ko), pl = um_desc(sb + UM_BPL + UM_BN * 128 + ko);
-                const uint64_t qh = um_desc(sb + ko), ql = um_desc(sb + UM_BPL + ko);
-                um_mma(tmem, arl, ph, (c > 0 || ks > 0) ? 1u : 0u);
-                um_mma(tmem, arh, pl, 1u);
-                um_mma(tmem, ail, qh, 1u);
-                um_mma(tmem, aih, ql, 1u);
-                um_mma(tmem, arh, ph, 1u);
-                um_mma(tmem, aih, qh, 1u);
+                const uint64_t bh = um_desc(sb + ko), bl = um_desc(sb + UM_BPL + ko);
+                const uint32_t acc = (c > 0 || ks > 0) ? 1u : 0u;
+                um_mma(tp, arl, bh, acc);
+                um_mma(tq, ail, bh, acc);
+                um_mma(tp, arh, bl, 1u);
+                um_mma(tq, aih, bl, 1u);
+                um_mma(tp, arh, bh, 1u);
+                um_mma(tq, aih, bh, 1u);
             }
             asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
-                         :: "r"(bar0 + 8 * s) : "memory");
+                         :: "r"(bar0) : "memory");
         }
     }
     if (!fail && nk > 0) {
         int ok = 1;
-        if (tid == 0) ok = um_wait(bar0 + 8 * ((nk - 1) & 1), ((nk - 1) >> 1) & 1);
+        if (tid == 0) ok = um_wait(bar0, (nk - 1) & 1);
         if (__syncthreads_or(!ok)) fail = true;
     }
     if (fail) {
         if (tid == 0) atomicOr(&g_umma_fault, 1u);
         // give MMAs still in flight a second bounded wait before the memory is released
-        if (tid == 0 && nk > 0) um_wait(bar0 + 8 * ((nk - 1) & 1), ((nk - 1) >> 1) & 1);
+        if (tid == 0 && nk > 0) um_wait(bar0, (nk - 1) & 1);
     } else {
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         const int q = warp & 3, h = warp >> 2;
@@ -287,9 +283,19 @@ __global__ void __launch_bounds__(UM_THREADS, 1) zgemm_umma_kernel(GemmArgs<floa
         for (int cc = 0; cc < 32; cc += 16) {
             float re[16], im[16];
             if (nk > 0) {
-                um_ld16(trow + (uint32_t)(32 * h + cc), re);
-                um_ld16(trow + (uint32_t)(UM_BN + 32 * h + cc), im);
+                // Re = P[:, j] - Q[:, 64 + j], Im = P[:, 64 + j] + Q[:, j]
+                float t[16];
+                const uint32_t col = (uint32_t)(32 * h + cc);
+                um_ld16(trow + col, re);
+                um_ld16(trow + 128 + UM_BN + col, t);
                 asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+                for (int j = 0; j < 16; ++j) re[j] -= t[j];
+                um_ld16(trow + UM_BN + col, im);
+                um_ld16(trow + 128 + col, t);
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+                for (int j = 0; j < 16; ++j) im[j] += t[j];
             } else {
 #pragma unroll
                 for (int j = 0; j < 16; ++j) re[j] = im[j] = 0.f;
