@@ -49,8 +49,10 @@ int nrltb_bench_cgemm_run(nrltb_ctx *ctx, int method, int m, int n, int k, int o
                           int triB, int triC, const float alpha[2], const float beta[2], const float *A,
                           int lda, const float *B, int ldb, float *C, int ldc);
 
-/* Fault flag of the tcgen05 GEMM kernel: nonzero once a bounded barrier wait
- * inside it ran out (the kernel then leaves C untouched); clear = 1 resets it. */
+/* Fault flags of the tcgen05 kernels: bit 0 the FP32 GEMM, bit 1 the
+ * refinement's digit product; a bit is set once a bounded barrier wait inside
+ * that kernel ran out (the kernel then leaves its output untouched).
+ * clear = 1 resets both. */
 int nrltb_bench_umma_fault(int clear);
 
 /* Kernel-class timing of the context's own calls: with on = 1 every later

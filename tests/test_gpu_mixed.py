@@ -117,8 +117,8 @@ def _refprod(ctx, method, A, X):
     return Y.transpose(0, 2, 1), Xc.transpose(0, 2, 1)
 
 
-@pytest.mark.parametrize("method", [0, 1])
-def test_refinement_product_accuracy(ctx, method):
+@pytest.mark.parametrize("method,n", [(0, 200), (1, 200), (1, 300)])
+def test_refinement_product_accuracy(ctx, method, n):
     """H X against an extended-precision product of the X the method used.
     Double-float SIMT (method 0): componentwise, the error grows like n 2^-48
     |A||X| (its low part accumulates in plain FP32).  Tensor-core digits
@@ -127,7 +127,8 @@ def test_refinement_product_accuracy(ctx, method):
     most 2^-43 of (largest component in row m of A) x (largest component in
     column n of X)."""
     rng = np.random.default_rng(5)
-    b, n = 2, 200
+    b = 2
+    ctx.lib.nrltb_bench_umma_fault(1)
     # Hermitian A with H-like structure: O(1) diagonal, decaying off-diagonals
     # spanning many binades, some exact zeros
     A = rng.standard_normal((b, n, n)) + 1j * rng.standard_normal((b, n, n))
@@ -158,3 +159,4 @@ def test_refinement_product_accuracy(ctx, method):
         assert r_comp <= n * 2.0 ** -46, (r_comp, r_fixed)
     else:
         assert r_fixed <= 2.0 ** -43, (r_comp, r_fixed)
+    assert ctx.lib.nrltb_bench_umma_fault(0) == 0

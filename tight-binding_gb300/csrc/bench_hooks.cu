@@ -271,5 +271,5 @@ extern "C" int nrltb_bench_cgemm_run(nrltb_ctx *ctx, int method, int m, int n, i
 
 extern "C" int nrltb_bench_umma_fault(int clear)
 {
-    return (int)zgemm_umma_fault(clear != 0);
+    return (int)(zgemm_umma_fault(clear != 0) | (ozaki_fault(clear != 0) << 1));
 }

@@ -8,40 +8,74 @@
 // largest element, far below the FP32 eigensolver's own error), so the
 // products are formed for exactly the X every later step uses.
 // Every digit is an integer that bf16 holds exactly and every digit product is
-// <= 2^14.  A complex product takes three real ones (p1 = Ar Xr, p2 = Ai Xi,
-// p3 = (Ar + Ai)(Xr + Xi), digit sums <= 256 are exact in bf16 too).  For a
-// 64-wide k chunk each sum over the (at most 3) digit pairs of one weight
-// 256^-(L+2), L = s + t, stays below 2^24 (p3: 64 * 3 * 2^16), so the tensor
-// core's FP32 accumulation of one level and one chunk is exact, and so are
-// re = p1 - p2 and im = p3 - (p1 + p2) (both below 2^23 in magnitude).  Each chunk's level sums are folded,
+// <= 2^14.  A complex digit product takes four real ones.  For a 64-wide k
+// chunk each sum over the (at most 3) digit pairs of one weight 256^-(L+2),
+// L = s + t, stays below 2^21.6, so the tensor core's FP32 accumulation of one
+// level and one chunk is exact, and so are re = Xr Ar - Xi Ai and
+// im = Xr Ai + Xi Ar (below 2^22.6).  Each chunk's level sums are folded,
 // scaled by 256^-(L+2), into a double-float (FP32 pair) accumulator.  Levels
 // L <= 5 are kept (15 digit pairs); the dropped ones and the 6-digit cut of A
-// are below 2^-48 of |A row| |X column| per term, the accuracy of the
-// double-float SIMT product this replaces.  15 digit pairs x 3 real products
-// = 45 bf16 MMAs per complex multiply-add, issued as mma.sync.m16n8k16.
+// are below 2^-48 of |A row| |X column| per term.
+//
+// Tensor cores: tcgen05.mma kind::f16 (bf16 digits, FP32 accumulators in
+// tensor memory).  One CTA computes a 32 x 128 tile of Y as its transpose:
+// the MMA's M = 128 rows are columns j of X (their digit tiles Xr_t, Xi_t),
+// its N = 64 columns the digit rows [Ar_s | Ai_s] of 32 rows i of A, so
+// P = Xr_t [Ar_s | Ai_s] and Q = Xi_t [Ar_s | Ai_s] give
+// Re Y_ij = P[j, i] - Q[j, 32 + i] and Im Y_ij = P[j, 32 + i] + Q[j, i].
+// Digits are written pre-tiled in the 128-byte-swizzled K-major layout the
+// MMA reads, so each tile is one bulk asynchronous copy (cp.async.bulk with
+// a transaction-count barrier).  Warp roles: one producer thread (copies),
+// one MMA thread, eight fold warps (tensor memory -> registers, double-float
+// accumulation, output).  Within a chunk the A digit planes s = 0..5 stream
+// through a ring while the chunk's X digits stay resident; plane s feeds
+// levels s, s+1, s+2, and level s is complete after it, so four 128-column
+// tensor-memory level buffers let the fold of one level overlap the MMAs of
+// the next three.  Every barrier wait is bounded (about two seconds); on
+// expiry the CTA records a fault flag and leaves Y untouched.
 //
 // Because A is Hermitian, its row scale equals its column scale and row m is
 // the conjugate of column m, so both are read with coalesced column accesses.
+#include <cstdint>
 #include "common.cuh"
 #include "ozaki.cuh"
 
 namespace nrltb {
 
 constexpr int OZ_SA = 6, OZ_SB = 3;       // digits of A (FP64) and X (FP32)
-constexpr int OZ_T = 64;                  // CTA tile (m, n) and k chunk
-constexpr int OZ_KP = OZ_T + 8;           // padded k stride in smem (bf16 units): 36 words
-constexpr int OZ_THREADS = 256;           // 8 warps: 2 (m) x 4 (n), warp tile 32 x 16
+constexpr int OZ_MX = 128;                // columns of X (and of Y) per CTA: tensor-memory lanes
+constexpr int OZ_NA_ROWS = 32;            // rows of A (and of Y) per CTA
+constexpr int OZ_BK = 64;                 // k chunk: one 128-byte swizzled row of bf16
+constexpr int OZ_PAD = 128;               // n padded to a multiple of this (rows, columns, k)
+constexpr int OZ_XBLK = 2 * OZ_MX * 128;          // X digit block (one t): Xr_t | Xi_t tiles, 32 KB
+constexpr int OZ_ABLK = 2 * OZ_NA_ROWS * 128;     // A digit block (one s): Ar_s | Ai_s rows, 8 KB
+constexpr int OZ_XSTAGE = OZ_SB * OZ_XBLK;        // a chunk's X digits, 96 KB
+constexpr int OZ_NXS = 2;                 // X chunk stages
+constexpr int OZ_NAS = 4;                 // A blocks in flight
+constexpr int OZ_NBUF = 4;                // tensor-memory level buffers, 128 columns each
+constexpr int OZ_FOLD_WARPS = 8;
+constexpr int OZ_THREADS = 32 * (OZ_FOLD_WARPS + 2);   // + producer warp + MMA warp
+constexpr int OZ_NBAR = 2 * OZ_NXS + 2 * OZ_NAS + 2 * OZ_NBUF;
+constexpr int OZ_SMEM = OZ_NXS * OZ_XSTAGE + OZ_NAS * OZ_ABLK + 1024 + 8 * OZ_NBAR + 16;
+constexpr uint32_t OZ_TMEM_COLS = 512;
+constexpr unsigned long long OZ_WAIT_NS = 2000000000ull;
+// instruction descriptor, kind::f16: D f32 (bits 4-5 = 1), A and B bf16
+// (bits 7-9, 10-12 = 1), both K-major, N >> 3 at bits 17-22, M >> 4 at 24-28
+constexpr uint32_t OZ_IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(64 >> 3) << 17) |
+                              ((uint32_t)(OZ_MX >> 4) << 24);
 
 static inline size_t al256(size_t x) { return (x + 255) & ~size_t(255); }
-static inline int pad64(int n) { return (n + OZ_T - 1) / OZ_T * OZ_T; }
+static inline int padn(int n) { return (n + OZ_PAD - 1) / OZ_PAD * OZ_PAD; }
 
 size_t ozaki_work_bytes(int n, int batch)
 {
-    const size_t np = (size_t)pad64(n), nb = (size_t)batch;
-    return al256(sizeof(__nv_bfloat16) * np * np * nb * 2 * OZ_SA)   // A digits [s][re|im][b][m][k]
-         + al256(sizeof(__nv_bfloat16) * np * np * nb * 2 * OZ_SB)   // X digits [t][re|im][b][n][k]
+    const size_t np = (size_t)padn(n), nb = (size_t)batch;
+    return al256(sizeof(__nv_bfloat16) * np * np * nb * 2 * OZ_SA)   // A digit blocks
+         + al256(sizeof(__nv_bfloat16) * np * np * nb * 2 * OZ_SB)   // X digit blocks
          + 2 * al256(sizeof(int) * np * nb) + 256;                    // exponents
 }
+
+__device__ unsigned g_oz_fault;
 
 // column exponents: e_j = smallest e with |M_kj| < 2^e for all k (re and im)
 template <typename C2>
@@ -85,78 +119,187 @@ __device__ __forceinline__ void digits_of(long long U, float d[ND])
     d[0] = (float)U;
 }
 
-// A digits, written row-major per (m, k): D[s][c][b][m][k], c = 0 re, 1 im.
-// A is Hermitian: A_mk = conj(A_km) is read down column m (coalesced).
-// U = rint(A_mk 2^(47 - e_m)) (|U| <= 2^47, one rounding at 2^-48 of 2^(e_m+1))
-// is cut into OZ_SA = 6 digits with integer arithmetic.
-__global__ void k_oz_digits_a(const double2 *A, int n, int np, const int *ex, __nv_bfloat16 *D, int batch)
+// byte offset of the 16-byte chunk holding k = 8 g .. 8 g + 7 of row r in a
+// 128-byte-swizzled K-major tile (chunk index XOR row mod 8)
+__device__ __forceinline__ uint32_t oz_swz(int r, int g)
 {
-    const long npp = (long)np * np;
-    const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
-    if (t >= npp * batch) return;
-    const int b = (int)(t / npp);
-    const long e = t - b * npp;
-    const int m = (int)(e / np), k = (int)(e % np);      // row-major: k fastest
-    double2 v = make_double2(0.0, 0.0);
-    if (m < n && k < n) {
-        v = A[(long)b * n * n + k + (long)m * n];
-        v.y = -v.y;
-    }
-    const double sc = pow2d(47 - ex[(long)b * np + m]);
-    float dr[OZ_SA], di[OZ_SA];
-    digits_of<OZ_SA>(__double2ll_rn(v.x * sc), dr);
-    digits_of<OZ_SA>(__double2ll_rn(v.y * sc), di);
+    return (uint32_t)((r >> 3) * 1024 + (r & 7) * 128 + ((g ^ (r & 7)) << 4));
+}
+
+__device__ __forceinline__ uint4 oz_pack8(const float d[8])
+{
+    uint32_t w[4];
 #pragma unroll
-    for (int s = 0; s < OZ_SA; ++s) {
-        D[(((long)s * 2 + 0) * batch + b) * npp + e] = __float2bfloat16_rn(dr[s]);
-        D[(((long)s * 2 + 1) * batch + b) * npp + e] = __float2bfloat16_rn(di[s]);
+    for (int j = 0; j < 4; ++j) {
+        __nv_bfloat162 p = __floats2bfloat162_rn(d[2 * j], d[2 * j + 1]);   // low half: element 2 j
+        w[j] = *reinterpret_cast<uint32_t *>(&p);
+    }
+    return make_uint4(w[0], w[1], w[2], w[3]);
+}
+
+// A digits.  Thread: row i, 8 consecutive k.  A is Hermitian: A_ik = conj(A_ki)
+// is read down column i (coalesced).  U = rint(A_ik 2^(47 - e_i))
+// (|U| <= 2^47, one rounding at 2^-48 of 2^(e_i+1)) is cut into 6 digits.
+// Layout: blocks [b][i / 32][k / 64][s] of 8 KB = [Ar_s | Ai_s], 32 rows each.
+__global__ void k_oz_digits_a(const double2 *A, int n, int np, const int *ex, unsigned char *D, int batch)
+{
+    const int kg8 = np / 8;
+    const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (t >= (long)batch * np * kg8) return;
+    const int b = (int)(t / ((long)np * kg8));
+    const long e = t - (long)b * np * kg8;
+    const int i = (int)(e / kg8), kq = (int)(e % kg8), k0 = 8 * kq;
+    const double sc = pow2d(47 - ex[(long)b * np + i]);
+    float dr[OZ_SA][8], di[OZ_SA][8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+        const int k = k0 + u;
+        double2 v = make_double2(0.0, 0.0);
+        if (i < n && k < n) {
+            v = A[(long)b * n * n + k + (long)i * n];
+            v.y = -v.y;
+        }
+        float xr[OZ_SA], xi[OZ_SA];
+        digits_of<OZ_SA>(__double2ll_rn(v.x * sc), xr);
+        digits_of<OZ_SA>(__double2ll_rn(v.y * sc), xi);
+#pragma unroll
+        for (int q = 0; q < OZ_SA; ++q) { dr[q][u] = xr[q]; di[q][u] = xi[q]; }
+    }
+    const int KC = np / OZ_BK;
+    unsigned char *blk = D + ((((long)b * (np / OZ_NA_ROWS) + i / OZ_NA_ROWS) * KC + k0 / OZ_BK) * OZ_SA) * OZ_ABLK;
+    const uint32_t off = oz_swz(i % OZ_NA_ROWS, (k0 % OZ_BK) / 8);
+#pragma unroll
+    for (int q = 0; q < OZ_SA; ++q) {
+        *(uint4 *)(blk + (long)q * OZ_ABLK + off) = oz_pack8(dr[q]);
+        *(uint4 *)(blk + (long)q * OZ_ABLK + OZ_NA_ROWS * 128 + off) = oz_pack8(di[q]);
     }
 }
 
-// X digits, stored per (n, k): D[t][c][b][n][k] (k fastest), X column-major FP32.
-// U = rint(X_kn 2^(23 - f_n)) (|U| <= 2^23) is cut into OZ_SB = 3 digits and X
-// itself is overwritten with U 2^(f_n - 23), the value its digits represent
-// (exact in FP32).
-__global__ void k_oz_digits_x(float2 *X, int n, int np, const int *ex, __nv_bfloat16 *D, int batch)
+// X digits.  Thread: column j, 8 consecutive k (X column-major FP32).
+// U = rint(X_kj 2^(23 - f_j)) (|U| <= 2^23) is cut into 3 digits and X itself
+// is overwritten with U 2^(f_j - 23), the value its digits represent (exact in
+// FP32).  Layout: blocks [b][j / 128][k / 64][t] of 32 KB = [Xr_t | Xi_t],
+// 128 rows each.
+__global__ void k_oz_digits_x(float2 *X, int n, int np, const int *ex, unsigned char *D, int batch)
 {
-    const long npp = (long)np * np;
+    const int kg8 = np / 8;
     const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
-    if (t >= npp * batch) return;
-    const int b = (int)(t / npp);
-    const long e = t - b * npp;
-    const int j = (int)(e / np), k = (int)(e % np);
-    const bool in = j < n && k < n;
-    const long xi = (long)b * n * n + k + (long)j * n;
-    float2 v = make_float2(0.f, 0.f);
-    if (in) v = X[xi];
+    if (t >= (long)batch * np * kg8) return;
+    const int b = (int)(t / ((long)np * kg8));
+    const long e = t - (long)b * np * kg8;
+    const int j = (int)(e / kg8), kq = (int)(e % kg8), k0 = 8 * kq;
     const int fj = ex[(long)b * np + j];
-    const int ur = __float2int_rn(v.x * pow2f(23 - fj)), ui = __float2int_rn(v.y * pow2f(23 - fj));
-    float dr[OZ_SB], di[OZ_SB];
-    digits_of<OZ_SB>(ur, dr);
-    digits_of<OZ_SB>(ui, di);
+    float dr[OZ_SB][8], di[OZ_SB][8];
 #pragma unroll
-    for (int s = 0; s < OZ_SB; ++s) {
-        D[(((long)s * 2 + 0) * batch + b) * npp + e] = __float2bfloat16_rn(dr[s]);
-        D[(((long)s * 2 + 1) * batch + b) * npp + e] = __float2bfloat16_rn(di[s]);
+    for (int u = 0; u < 8; ++u) {
+        const int k = k0 + u;
+        const bool in = j < n && k < n;
+        const long xi = (long)b * n * n + k + (long)j * n;
+        float2 v = make_float2(0.f, 0.f);
+        if (in) v = X[xi];
+        const int ur = __float2int_rn(v.x * pow2f(23 - fj)), ui = __float2int_rn(v.y * pow2f(23 - fj));
+        float xr[OZ_SB], xm[OZ_SB];
+        digits_of<OZ_SB>(ur, xr);
+        digits_of<OZ_SB>(ui, xm);
+#pragma unroll
+        for (int q = 0; q < OZ_SB; ++q) { dr[q][u] = xr[q]; di[q][u] = xm[q]; }
+        if (in) X[xi] = make_float2((float)ur * pow2f(fj - 23), (float)ui * pow2f(fj - 23));
     }
-    if (in) X[xi] = make_float2((float)ur * pow2f(fj - 23), (float)ui * pow2f(fj - 23));
+    const int KC = np / OZ_BK;
+    unsigned char *blk = D + ((((long)b * (np / OZ_MX) + j / OZ_MX) * KC + k0 / OZ_BK) * OZ_SB) * OZ_XBLK;
+    const uint32_t off = oz_swz(j % OZ_MX, (k0 % OZ_BK) / 8);
+#pragma unroll
+    for (int q = 0; q < OZ_SB; ++q) {
+        *(uint4 *)(blk + (long)q * OZ_XBLK + off) = oz_pack8(dr[q]);
+        *(uint4 *)(blk + (long)q * OZ_XBLK + OZ_MX * 128 + off) = oz_pack8(di[q]);
+    }
 }
 
-__device__ __forceinline__ void mma_bf16(float c[4], const unsigned a[4], const unsigned b[2])
+// ---------------------------------------------------------------------------
+// tcgen05 / barrier helpers
+__device__ __forceinline__ uint32_t oz_saddr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups
+// 1024 B apart, descriptor version 1 (bits 46-48)
+__device__ __forceinline__ uint64_t oz_desc(uint32_t saddr)
 {
-    asm volatile("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-                 "{%0,%1,%2,%3};"
-                 : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
-                 : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+    uint64_t d = (uint64_t)((saddr & 0x3FFFFu) >> 4);
+    d |= (uint64_t)1 << 16;
+    d |= (uint64_t)(1024 >> 4) << 32;
+    d |= (uint64_t)1 << 46;
+    d |= (uint64_t)2 << 61;
+    return d;
 }
 
-// sum of two packed pairs of bf16 digits: exact, the sums are integers of
-// magnitude <= 256
-__device__ __forceinline__ unsigned add_bf16x2(unsigned a, unsigned b)
+__device__ __forceinline__ void oz_mma(uint32_t tmem, uint64_t da, uint64_t db, uint32_t acc)
 {
-    __nv_bfloat162 x = *reinterpret_cast<__nv_bfloat162 *>(&a), y = *reinterpret_cast<__nv_bfloat162 *>(&b);
-    __nv_bfloat162 z = __hadd2(x, y);
-    return *reinterpret_cast<unsigned *>(&z);
+    asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                 "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n"
+                 :: "r"(tmem), "l"(da), "l"(db), "r"(OZ_IDESC), "r"(acc));
+}
+
+__device__ __forceinline__ void oz_commit(uint32_t bar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" :: "r"(bar)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool oz_test(uint32_t bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile("{\n\t.reg .pred p;\n\tmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                 "selp.u32 %0, 1, 0, p;\n\t}\n"
+                 : "=r"(ok) : "r"(bar), "r"(parity) : "memory");
+    return ok != 0;
+}
+
+__device__ __forceinline__ unsigned long long oz_ns()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// wait for the phase of the given parity, at most OZ_WAIT_NS or until another
+// role has given up (abort flag)
+__device__ bool oz_wait(uint32_t bar, uint32_t parity, volatile int *abort)
+{
+    if (oz_test(bar, parity)) return true;
+    const unsigned long long t0 = oz_ns();
+    for (;;) {
+        __nanosleep(32);
+        if (oz_test(bar, parity)) return true;
+        if (*abort || oz_ns() - t0 > OZ_WAIT_NS) return false;
+    }
+}
+
+__device__ __forceinline__ void oz_expect(uint32_t bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" :: "r"(bar), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void oz_bulk(uint32_t dst, const void *src, uint32_t bytes, uint32_t bar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 :: "r"(dst), "l"(src), "r"(bytes), "r"(bar) : "memory");
+}
+
+__device__ __forceinline__ void oz_arrive(uint32_t bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" :: "r"(bar) : "memory");
+}
+
+__device__ __forceinline__ void oz_ld16(uint32_t taddr, float v[16])
+{
+    uint32_t r[16];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+                 "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+                   "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+                   "=r"(r[14]), "=r"(r[15])
+                 : "r"(taddr));
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
 // (hi, lo) += v, v exact in FP64's sense once scaled by a power of two
@@ -167,161 +310,198 @@ __device__ __forceinline__ void df_add(float &hi, float &lo, float v)
     hi = s;
 }
 
-// One CTA: a 64 x 64 tile of Y for one matrix.  Shared memory holds, for one
-// 64-wide k chunk, all digits of the A rows and X columns of the tile.
+// One CTA: rows i0..i0+31 of Y (A rows) x columns j0..j0+127 (X columns) of
+// one matrix, as the transpose tile in tensor memory (see the file header).
 __global__ void __launch_bounds__(OZ_THREADS, 1)
-k_oz_gemm(const __nv_bfloat16 *DA, const __nv_bfloat16 *DX, const int *exA, const int *exX, double2 *Y,
-          int n, int np, int batch)
+k_oz_gemm(const unsigned char *DA, const unsigned char *DX, const int *exA, const int *exX, double2 *Y, int n,
+          int np, int batch)
 {
-    extern __shared__ __align__(16) unsigned char smem[];
-    // sA[s][c][64 rows][OZ_KP], sX[t][c][64 cols][OZ_KP]  (bf16)
-    __nv_bfloat16 *sA = (__nv_bfloat16 *)smem;
-    __nv_bfloat16 *sX = sA + OZ_SA * 2 * OZ_T * OZ_KP;
-    const int b = blockIdx.z, m0 = blockIdx.y * OZ_T, n0 = blockIdx.x * OZ_T;
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int wm = (warp >> 2) * 32, wn = (warp & 3) * 16;     // warp tile origin
-    const int g = lane >> 2, tq = lane & 3;
-    const long npp = (long)np * np;
-    // double-float accumulators: [mt 2][nt 2][frag 4] x (re, im) x (hi, lo)
-    float hr[2][2][4], lr[2][2][4], hi_[2][2][4], li[2][2][4];
-#pragma unroll
-    for (int a = 0; a < 2; ++a)
-#pragma unroll
-        for (int c = 0; c < 2; ++c)
-#pragma unroll
-            for (int q = 0; q < 4; ++q) hr[a][c][q] = lr[a][c][q] = hi_[a][c][q] = li[a][c][q] = 0.f;
+    extern __shared__ __align__(16) unsigned char oz_raw[];
+    const int it = blockIdx.x, jt = blockIdx.y, b = blockIdx.z;
+    const int KC = np / OZ_BK;
+    const uint32_t raw_s = oz_saddr(oz_raw);
+    unsigned char *base = oz_raw + (((raw_s + 1023u) & ~1023u) - raw_s);
+    unsigned char *sX = base;                                   // OZ_NXS x 96 KB
+    unsigned char *sA = base + OZ_NXS * OZ_XSTAGE;              // OZ_NAS x 8 KB
+    uint64_t *bars = (uint64_t *)(sA + OZ_NAS * OZ_ABLK);
+    uint32_t *tslot = (uint32_t *)(bars + OZ_NBAR);
+    volatile int *abort = (volatile int *)(tslot + 1);
+    const uint32_t bar0 = oz_saddr(bars);
+    // barrier addresses: X full/empty, A full/empty, level full/empty
+    auto full_x = [&](int q) { return bar0 + 8u * q; };
+    auto empty_x = [&](int q) { return bar0 + 8u * (OZ_NXS + q); };
+    auto full_a = [&](int q) { return bar0 + 8u * (2 * OZ_NXS + q); };
+    auto empty_a = [&](int q) { return bar0 + 8u * (2 * OZ_NXS + OZ_NAS + q); };
+    auto tfull = [&](int q) { return bar0 + 8u * (2 * OZ_NXS + 2 * OZ_NAS + q); };
+    auto tempty = [&](int q) { return bar0 + 8u * (2 * OZ_NXS + 2 * OZ_NAS + OZ_NBUF + q); };
 
-    for (int k0 = 0; k0 < np; k0 += OZ_T) {
-        __syncthreads();
-        // stage the chunk: 16-byte vectors (8 bf16) along k
-        for (int v = tid; v < OZ_SA * 2 * OZ_T * (OZ_T / 8); v += OZ_THREADS) {
-            const int kv = v % (OZ_T / 8), r = (v / (OZ_T / 8)) % OZ_T, sc = v / (OZ_T / 8 * OZ_T);
-            const uint4 d = *(const uint4 *)(DA + ((long)sc * batch + b) * npp + (long)(m0 + r) * np + k0 + kv * 8);
-            *(uint4 *)(sA + ((long)sc * OZ_T + r) * OZ_KP + kv * 8) = d;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+                     :: "r"(oz_saddr(tslot)), "r"(OZ_TMEM_COLS) : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid == 0) {
+        for (int q = 0; q < OZ_NBAR; ++q) {
+            const bool fold = q >= 2 * OZ_NXS + 2 * OZ_NAS + OZ_NBUF;   // level-empty: one arrive per fold warp
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(bar0 + 8u * q),
+                         "r"(fold ? OZ_FOLD_WARPS : 1) : "memory");
         }
-        for (int v = tid; v < OZ_SB * 2 * OZ_T * (OZ_T / 8); v += OZ_THREADS) {
-            const int kv = v % (OZ_T / 8), r = (v / (OZ_T / 8)) % OZ_T, sc = v / (OZ_T / 8 * OZ_T);
-            const uint4 d = *(const uint4 *)(DX + ((long)sc * batch + b) * npp + (long)(n0 + r) * np + k0 + kv * 8);
-            *(uint4 *)(sX + ((long)sc * OZ_T + r) * OZ_KP + kv * 8) = d;
-        }
-        __syncthreads();
-#pragma unroll 1
-        for (int L = 0; L <= OZ_SA - 1; ++L) {
-            // level sums: p1 = Ar Xr, p2 = Ai Xi, p3 = (Ar + Ai)(Xr + Xi) (three real
-            // products per complex one); re = p1 - p2, im = p3 - p1 - p2
-            float p1[2][2][4], p2[2][2][4], p3[2][2][4];
-#pragma unroll
-            for (int a = 0; a < 2; ++a)
-#pragma unroll
-                for (int c = 0; c < 2; ++c)
-#pragma unroll
-                    for (int q = 0; q < 4; ++q) p1[a][c][q] = p2[a][c][q] = p3[a][c][q] = 0.f;
-#pragma unroll 1
-            for (int t = 0; t < OZ_SB; ++t) {
-                const int s = L - t;
-                if (s < 0 || s >= OZ_SA) continue;
-                const unsigned *Ar = (const unsigned *)(sA + ((long)(s * 2 + 0) * OZ_T) * OZ_KP);
-                const unsigned *Ai = (const unsigned *)(sA + ((long)(s * 2 + 1) * OZ_T) * OZ_KP);
-                const unsigned *Xr = (const unsigned *)(sX + ((long)(t * 2 + 0) * OZ_T) * OZ_KP);
-                const unsigned *Xi = (const unsigned *)(sX + ((long)(t * 2 + 1) * OZ_T) * OZ_KP);
-                constexpr int W = OZ_KP / 2;   // row stride in 32-bit words
-#pragma unroll
-                for (int kk = 0; kk < OZ_T; kk += 16) {
-                    const int kw = kk / 2;
-                    unsigned ar[2][4], ai[2][4], as[2][4];
-#pragma unroll
-                    for (int a = 0; a < 2; ++a) {
-                        const int r0 = wm + a * 16 + g;
-                        ar[a][0] = Ar[r0 * W + kw + tq];
-                        ar[a][1] = Ar[(r0 + 8) * W + kw + tq];
-                        ar[a][2] = Ar[r0 * W + kw + 4 + tq];
-                        ar[a][3] = Ar[(r0 + 8) * W + kw + 4 + tq];
-                        ai[a][0] = Ai[r0 * W + kw + tq];
-                        ai[a][1] = Ai[(r0 + 8) * W + kw + tq];
-                        ai[a][2] = Ai[r0 * W + kw + 4 + tq];
-                        ai[a][3] = Ai[(r0 + 8) * W + kw + 4 + tq];
-#pragma unroll
-                        for (int q = 0; q < 4; ++q) as[a][q] = add_bf16x2(ar[a][q], ai[a][q]);
-                    }
-                    unsigned br[2][2], bi[2][2], bs[2][2];
-#pragma unroll
-                    for (int c = 0; c < 2; ++c) {
-                        const int c0 = wn + c * 8 + g;
-                        br[c][0] = Xr[c0 * W + kw + tq];
-                        br[c][1] = Xr[c0 * W + kw + 4 + tq];
-                        bi[c][0] = Xi[c0 * W + kw + tq];
-                        bi[c][1] = Xi[c0 * W + kw + 4 + tq];
-                        bs[c][0] = add_bf16x2(br[c][0], bi[c][0]);
-                        bs[c][1] = add_bf16x2(br[c][1], bi[c][1]);
-                    }
-                    // three rounds over the 12 accumulators: no MMA waits on the one before it
-#pragma unroll
-                    for (int c = 0; c < 2; ++c)
-#pragma unroll
-                        for (int a = 0; a < 2; ++a) mma_bf16(p1[a][c], ar[a], br[c]);
-#pragma unroll
-                    for (int c = 0; c < 2; ++c)
-#pragma unroll
-                        for (int a = 0; a < 2; ++a) mma_bf16(p2[a][c], ai[a], bi[c]);
-#pragma unroll
-                    for (int c = 0; c < 2; ++c)
-#pragma unroll
-                        for (int a = 0; a < 2; ++a) mma_bf16(p3[a][c], as[a], bs[c]);
+        *abort = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *tslot;
+
+    const unsigned char *gX = DX + (((long)b * (np / OZ_MX) + jt) * KC) * OZ_SB * OZ_XBLK;
+    const unsigned char *gA = DA + (((long)b * (np / OZ_NA_ROWS) + it) * KC) * OZ_SA * OZ_ABLK;
+
+    if (warp == OZ_FOLD_WARPS) {
+        // ---- producer: bulk copies of the pre-swizzled digit tiles ----
+        if (lane == 0) {
+            bool ok = true;
+            for (int kc = 0; kc < KC && ok; ++kc) {
+                const int jx = kc % OZ_NXS, ux = kc / OZ_NXS;
+                if (ux > 0 && !(ok = oz_wait(empty_x(jx), (ux - 1) & 1, abort))) break;
+                oz_expect(full_x(jx), OZ_XSTAGE);
+                for (int q = 0; q < OZ_SB; ++q)
+                    oz_bulk(oz_saddr(sX + jx * OZ_XSTAGE + q * OZ_XBLK), gX + ((long)kc * OZ_SB + q) * OZ_XBLK,
+                            OZ_XBLK, full_x(jx));
+                for (int sdig = 0; sdig < OZ_SA; ++sdig) {
+                    const int qa = kc * OZ_SA + sdig, ia = qa % OZ_NAS, ua = qa / OZ_NAS;
+                    if (ua > 0 && !(ok = oz_wait(empty_a(ia), (ua - 1) & 1, abort))) break;
+                    oz_expect(full_a(ia), OZ_ABLK);
+                    oz_bulk(oz_saddr(sA + ia * OZ_ABLK), gA + (long)qa * OZ_ABLK, OZ_ABLK, full_a(ia));
                 }
             }
-            // fold this level of this chunk: exact integers scaled by 256^-(L+2).
-            // Levels 0-2 by an exact two-sum into (hi, lo); from level 3 on the
-            // contribution (< 2^-17 of the unit scale) goes straight into lo,
-            // whose own rounding (2^-24 |lo|) already bounds the pair's error.
-            const float w = ldexpf(1.0f, -8 * (L + 2));
-            if (L < 3) {
-#pragma unroll
-                for (int a = 0; a < 2; ++a)
-#pragma unroll
-                    for (int c = 0; c < 2; ++c)
-#pragma unroll
-                        for (int q = 0; q < 4; ++q) {
-                            const float re = p1[a][c][q] - p2[a][c][q];
-                            const float im = p3[a][c][q] - (p1[a][c][q] + p2[a][c][q]);
-                            df_add(hr[a][c][q], lr[a][c][q], re * w);
-                            df_add(hi_[a][c][q], li[a][c][q], im * w);
+            if (!ok) { *abort = 1; atomicOr(&g_oz_fault, 1u); }
+        }
+    } else if (warp == OZ_FOLD_WARPS + 1) {
+        // ---- MMA issue: plane-major within each chunk ----
+        if (lane == 0) {
+            bool ok = true;
+            const uint32_t sx0 = oz_saddr(sX), sa0 = oz_saddr(sA);
+            for (int kc = 0; kc < KC && ok; ++kc) {
+                const int jx = kc % OZ_NXS, ux = kc / OZ_NXS;
+                if (!(ok = oz_wait(full_x(jx), ux & 1, abort))) break;
+                for (int sdig = 0; sdig < OZ_SA; ++sdig) {
+                    const int qa = kc * OZ_SA + sdig, ia = qa % OZ_NAS, ua = qa / OZ_NAS;
+                    if (!(ok = oz_wait(full_a(ia), ua & 1, abort))) break;
+                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                    for (int tdig = 0; tdig < OZ_SB; ++tdig) {
+                        const int L = sdig + tdig;
+                        if (L > OZ_SA - 1) break;
+                        const int ql = kc * OZ_SA + L, buf = ql % OZ_NBUF;
+                        const bool first = sdig == (L > 2 ? L - 2 : 0);
+                        if (first && ql >= OZ_NBUF) {
+                            // the fold of level ql - 4 has emptied this buffer
+                            if (!(ok = oz_wait(tempty(buf), ((ql - OZ_NBUF) / OZ_NBUF) & 1, abort))) break;
+                            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
                         }
-            } else {
+                        const uint32_t xr = sx0 + jx * OZ_XSTAGE + tdig * OZ_XBLK, xi = xr + OZ_MX * 128;
+                        const uint32_t ab = sa0 + ia * OZ_ABLK;
+                        const uint32_t tP = tmem + 128u * buf, tQ = tP + 64u;
 #pragma unroll
-                for (int a = 0; a < 2; ++a)
-#pragma unroll
-                    for (int c = 0; c < 2; ++c)
-#pragma unroll
-                        for (int q = 0; q < 4; ++q) {
-                            const float re = p1[a][c][q] - p2[a][c][q];
-                            const float im = p3[a][c][q] - (p1[a][c][q] + p2[a][c][q]);
-                            lr[a][c][q] = fmaf(re, w, lr[a][c][q]);
-                            li[a][c][q] = fmaf(im, w, li[a][c][q]);
+                        for (int ks = 0; ks < OZ_BK / 16; ++ks) {
+                            const uint32_t ko = 32u * ks;
+                            const uint64_t db = oz_desc(ab + ko);
+                            const uint32_t acc = (first && ks == 0) ? 0u : 1u;
+                            oz_mma(tP, oz_desc(xr + ko), db, acc);
+                            oz_mma(tQ, oz_desc(xi + ko), db, acc);
                         }
+                    }
+                    if (!ok) break;
+                    oz_commit(empty_a(ia));
+                    oz_commit(tfull((kc * OZ_SA + sdig) % OZ_NBUF));   // level sdig of this chunk is complete
+                }
+                if (!ok) break;
+                oz_commit(empty_x(jx));
+            }
+            if (ok && KC > 0) {
+                // the last commit has landed: every MMA of the CTA has finished
+                const int jx = (KC - 1) % OZ_NXS, ux = (KC - 1) / OZ_NXS;
+                ok = oz_wait(empty_x(jx), ux & 1, abort);
+            }
+            if (!ok) { *abort = 1; atomicOr(&g_oz_fault, 1u); }
+        }
+    } else {
+        // ---- fold warps: level sums -> double-float accumulators -> Y ----
+        const int q4 = warp & 3, h = warp >> 2;
+        const uint32_t trow = tmem + ((uint32_t)(32 * q4) << 16);
+        float hr[16], lr[16], hi[16], li[16];
+#pragma unroll
+        for (int c = 0; c < 16; ++c) hr[c] = lr[c] = hi[c] = li[c] = 0.f;
+        bool ok = true;
+        for (int kc = 0; kc < KC && ok; ++kc) {
+#pragma unroll 1
+            for (int L = 0; L < OZ_SA; ++L) {
+                const int ql = kc * OZ_SA + L, buf = ql % OZ_NBUF;
+                ok = __all_sync(0xffffffffu, oz_wait(tfull(buf), (ql / OZ_NBUF) & 1, abort));
+                if (!ok) break;
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                float pre[16], pim[16], qre[16], qim[16];
+                const uint32_t c0 = trow + 128u * buf + 16u * h;
+                oz_ld16(c0, pre);         // Xr Ar
+                oz_ld16(c0 + 32u, pim);   // Xr Ai
+                oz_ld16(c0 + 64u, qre);   // Xi Ar
+                oz_ld16(c0 + 96u, qim);   // Xi Ai
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+                __syncwarp();
+                if (lane == 0) oz_arrive(tempty(buf));
+                const float w = ldexpf(1.0f, -8 * (L + 2));
+                if (L < 3) {
+                    // levels 0-2: exact two-sum into (hi, lo)
+#pragma unroll
+                    for (int c = 0; c < 16; ++c) {
+                        df_add(hr[c], lr[c], (pre[c] - qim[c]) * w);
+                        df_add(hi[c], li[c], (pim[c] + qre[c]) * w);
+                    }
+                } else {
+                    // from level 3 on the contribution (< 2^-17 of the unit scale) goes
+                    // straight into lo, whose own rounding already bounds the pair's error
+#pragma unroll
+                    for (int c = 0; c < 16; ++c) {
+                        lr[c] = fmaf(pre[c] - qim[c], w, lr[c]);
+                        li[c] = fmaf(pim[c] + qre[c], w, li[c]);
+                    }
+                }
+            }
+        }
+        if (!ok && lane == 0) { *abort = 1; atomicOr(&g_oz_fault, 1u); }
+        if (ok) {
+            // Y[i, j], j = this thread's X column, i = 16 consecutive A rows:
+            // scale by 2^(e_i + 1) 2^(f_j + 1)
+            const int j = jt * OZ_MX + 32 * q4 + lane;
+            if (j < n) {
+                const int fj = exX[(long)b * np + j];
+                double2 *yc = Y + (long)b * n * n + (long)j * n;
+#pragma unroll
+                for (int c = 0; c < 16; ++c) {
+                    const int i = it * OZ_NA_ROWS + 16 * h + c;
+                    if (i >= n) break;
+                    const int sh = exA[(long)b * np + i] + fj + 2;
+                    yc[i] = make_double2(ldexp((double)hr[c] + (double)lr[c], sh),
+                                         ldexp((double)hi[c] + (double)li[c], sh));
+                }
             }
         }
     }
-    // scale by 2^(e_m + 1) 2^(f_n + 1) and store
-#pragma unroll
-    for (int a = 0; a < 2; ++a)
-#pragma unroll
-        for (int c = 0; c < 2; ++c)
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                const int m = m0 + wm + a * 16 + g + (q >= 2 ? 8 : 0);
-                const int nn = n0 + wn + c * 8 + tq * 2 + (q & 1);
-                if (m >= n || nn >= n) continue;
-                const int sh = exA[(long)b * np + m] + exX[(long)b * np + nn] + 2;
-                const double re = ldexp((double)hr[a][c][q] + (double)lr[a][c][q], sh);
-                const double im = ldexp((double)hi_[a][c][q] + (double)li[a][c][q], sh);
-                Y[(long)b * n * n + m + (long)nn * n] = make_double2(re, im);
-            }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tmem), "r"(OZ_TMEM_COLS)
+                     : "memory");
+    }
 }
 
 OzakiX ozaki_prepare_x(cudaStream_t s, float2 *X, int n, int batch, void *work)
 {
     OzakiX ox;
-    const int np = pad64(n);
+    const int np = padn(n);
     const size_t npp = (size_t)np * np;
     char *w = (char *)work;
     ox.DA = (__nv_bfloat16 *)w;
@@ -330,7 +510,8 @@ OzakiX ozaki_prepare_x(cudaStream_t s, float2 *X, int n, int batch, void *work)
     ox.exX = (int *)((char *)ox.exA + al256(sizeof(int) * (size_t)np * batch));
     ox.n = n; ox.np = np; ox.batch = batch;
     NRLTB_LAUNCH(k_oz_colexp<float2>, cdiv((long)np * batch * 32, 256), 256, 0, s, X, n, np, ox.exX, batch);
-    NRLTB_LAUNCH(k_oz_digits_x, cdiv((long)npp * batch, 256), 256, 0, s, X, n, np, ox.exX, ox.DX, batch);
+    NRLTB_LAUNCH(k_oz_digits_x, cdiv((long)npp / 8 * batch, 256), 256, 0, s, X, n, np, ox.exX,
+                 (unsigned char *)ox.DX, batch);
     return ox;
 }
 
@@ -339,13 +520,29 @@ void ozaki_gemm(cudaStream_t s, const OzakiX &ox, const double2 *A, double2 *Y)
     const int n = ox.n, np = ox.np, batch = ox.batch;
     const size_t npp = (size_t)np * np;
     NRLTB_LAUNCH(k_oz_colexp<double2>, cdiv((long)np * batch * 32, 256), 256, 0, s, A, n, np, ox.exA, batch);
-    NRLTB_LAUNCH(k_oz_digits_a, cdiv((long)npp * batch, 256), 256, 0, s, A, n, np, ox.exA, ox.DA, batch);
-    const int smem = (OZ_SA + OZ_SB) * 2 * OZ_T * OZ_KP * (int)sizeof(__nv_bfloat16);
-    cudaFuncSetAttribute(k_oz_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    dim3 grid(np / OZ_T, np / OZ_T, batch);
+    NRLTB_LAUNCH(k_oz_digits_a, cdiv((long)npp / 8 * batch, 256), 256, 0, s, A, n, np, ox.exA,
+                 (unsigned char *)ox.DA, batch);
+    static const bool attr = [] {
+        cudaFuncSetAttribute(k_oz_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, OZ_SMEM);
+        return true;
+    }();
+    (void)attr;
+    dim3 grid(np / OZ_NA_ROWS, np / OZ_MX, batch);
     cudaEvent_t ev = kt_begin(s);
-    NRLTB_LAUNCH(k_oz_gemm, grid, OZ_THREADS, smem, s, ox.DA, ox.DX, ox.exA, ox.exX, Y, n, np, batch);
+    NRLTB_LAUNCH(k_oz_gemm, grid, OZ_THREADS, OZ_SMEM, s, (const unsigned char *)ox.DA,
+                 (const unsigned char *)ox.DX, ox.exA, ox.exX, Y, n, np, batch);
     kt_end(ev, s, KC_DIGIT_GEMM, 8.0 * n * (double)n * n * batch);
+}
+
+unsigned ozaki_fault(bool clear)
+{
+    unsigned v = 0;
+    cudaMemcpyFromSymbol(&v, g_oz_fault, sizeof(v));
+    if (clear) {
+        const unsigned z = 0;
+        cudaMemcpyToSymbol(g_oz_fault, &z, sizeof(z));
+    }
+    return v;
 }
 
 }  // namespace nrltb

@@ -9,7 +9,7 @@ namespace nrltb {
 struct OzakiX {
     __nv_bfloat16 *DA, *DX;    // digit planes of A (reused for each A) and of X
     int *exA, *exX;            // per-row (A) and per-column (X) binary exponents
-    int n, np, batch;          // order, order padded to the 64-wide tile, matrices
+    int n, np, batch;          // order, order padded to a multiple of 128, matrices
 };
 
 size_t ozaki_work_bytes(int n, int batch);
@@ -19,5 +19,7 @@ size_t ozaki_work_bytes(int n, int batch);
 OzakiX ozaki_prepare_x(cudaStream_t s, float2 *X, int n, int batch, void *work);
 // Y = A X for the batch, A column-major n x n Hermitian (both triangles stored)
 void ozaki_gemm(cudaStream_t s, const OzakiX &ox, const double2 *A, double2 *Y);
+// fault flag of the product kernel (a barrier wait that ran out); clear resets it
+unsigned ozaki_fault(bool clear);
 
 }  // namespace nrltb
