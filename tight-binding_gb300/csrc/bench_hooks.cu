@@ -8,6 +8,7 @@
 #include "ozaki.cuh"
 
 using namespace nrltb;
+void nrltb_internal_set_error(const char *msg);
 
 struct nrltb_ctx;
 extern "C" cudaStream_t nrltb_ctx_stream_internal(nrltb_ctx *c);
@@ -220,11 +221,15 @@ extern "C" int nrltb_bench_refprod_run(nrltb_ctx *ctx, int method, int n, int ba
         cudaMemcpyAsync(d.p[2], X, sizeof(float2) * nn, cudaMemcpyHostToDevice, s) != cudaSuccess)
         return NRLTB_E_CUDA;
     refprod(s, method, n, batch, (const double2 *)d.p[0], (float2 *)d.p[2], (double2 *)d.p[1], d.p[3]);
-    if (cudaMemcpyAsync(Y, d.p[1], sizeof(double2) * nn, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-        cudaMemcpyAsync(X, d.p[2], sizeof(float2) * nn, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-        cudaStreamSynchronize(s) != cudaSuccess)
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(Y, d.p[1], sizeof(double2) * nn, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(X, d.p[2], sizeof(float2) * nn, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+        nrltb_internal_set_error(cudaGetErrorString(e));
         return NRLTB_E_CUDA;
-    return cudaGetLastError() == cudaSuccess ? NRLTB_OK : NRLTB_E_CUDA;
+    }
+    return NRLTB_OK;
 }
 
 extern "C" int nrltb_bench_cgemm_run(nrltb_ctx *ctx, int method, int m, int n, int k, int opA, int opB, int triA,

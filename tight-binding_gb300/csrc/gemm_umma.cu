@@ -68,12 +68,14 @@ __device__ __forceinline__ void um_mma(uint32_t tmem, uint64_t da, uint64_t db, 
                  :: "r"(tmem), "l"(da), "l"(db), "r"(UM_IDESC), "r"(acc));
 }
 
+// one bounded hardware wait (the thread is suspended until the phase completes
+// or about a microsecond passes)
 __device__ __forceinline__ bool um_test(uint32_t bar, uint32_t parity)
 {
     uint32_t ok;
-    asm volatile("{\n\t.reg .pred p;\n\tmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+    asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
                  "selp.u32 %0, 1, 0, p;\n\t}\n"
-                 : "=r"(ok) : "r"(bar), "r"(parity) : "memory");
+                 : "=r"(ok) : "r"(bar), "r"(parity), "r"(1000u) : "memory");
     return ok != 0;
 }
 
@@ -90,7 +92,6 @@ __device__ bool um_wait(uint32_t bar, uint32_t parity)
     if (um_test(bar, parity)) return true;
     const unsigned long long t0 = um_clock_ns();
     for (;;) {
-        __nanosleep(64);
         if (um_test(bar, parity)) return true;
         if (um_clock_ns() - t0 > UM_WAIT_NS) return false;
     }

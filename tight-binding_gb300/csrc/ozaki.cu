@@ -18,21 +18,21 @@
 // are below 2^-48 of |A row| |X column| per term.
 //
 // Tensor cores: tcgen05.mma kind::f16 (bf16 digits, FP32 accumulators in
-// tensor memory).  One CTA computes a 32 x 128 tile of Y as its transpose:
-// the MMA's M = 128 rows are columns j of X (their digit tiles Xr_t, Xi_t),
-// its N = 64 columns the digit rows [Ar_s | Ai_s] of 32 rows i of A, so
-// P = Xr_t [Ar_s | Ai_s] and Q = Xi_t [Ar_s | Ai_s] give
-// Re Y_ij = P[j, i] - Q[j, 32 + i] and Im Y_ij = P[j, 32 + i] + Q[j, i].
-// Digits are written pre-tiled in the 128-byte-swizzled K-major layout the
-// MMA reads, so each tile is one bulk asynchronous copy (cp.async.bulk with
-// a transaction-count barrier).  Warp roles: one producer thread (copies),
-// one MMA thread, eight fold warps (tensor memory -> registers, double-float
-// accumulation, output).  Within a chunk the A digit planes s = 0..5 stream
-// through a ring while the chunk's X digits stay resident; plane s feeds
-// levels s, s+1, s+2, and level s is complete after it, so four 128-column
-// tensor-memory level buffers let the fold of one level overlap the MMAs of
-// the next three.  Every barrier wait is bounded (about two seconds); on
-// expiry the CTA records a fault flag and leaves Y untouched.
+// tensor memory).  One CTA computes a 128 x 64 tile of Y: the MMA's M = 128
+// rows are rows i of A (digit tiles Ar_s, Ai_s), its N = 128 columns come
+// from the digit rows [-Xi_t | Xr_t | Xi_t] of 64 columns j of X, so that
+// Ar_s [Xr_t | Xi_t] + Ai_s [-Xi_t | Xr_t] accumulates [Re | Im] of a digit
+// pair's product in one 128-column accumulator.  Digits are written pre-tiled
+// in the 128-byte-swizzled K-major layout the MMA reads, so each tile is one
+// bulk asynchronous copy (cp.async.bulk with a transaction-count barrier).
+// Warp roles: one producer thread (copies), one MMA thread, sixteen fold warps
+// (tensor memory -> registers, double-float accumulation, output).  Within a
+// chunk the A digit planes s = 0..5 stream through a ring while the chunk's X
+// digits stay resident; plane s takes the digit pairs (s, 0), (s, 1), (s, 2),
+// so level L is first touched at plane max(0, L - 2) and complete after plane
+// L, and four 128-column tensor-memory level buffers let the folds run behind
+// the MMAs.  Every barrier wait is bounded (about two seconds); on expiry the
+// CTA records a fault flag and leaves Y untouched.
 //
 // Because A is Hermitian, its row scale equals its column scale and row m is
 // the conjugate of column m, so both are read with coalesced column accesses.
@@ -43,17 +43,17 @@
 namespace nrltb {
 
 constexpr int OZ_SA = 6, OZ_SB = 3;       // digits of A (FP64) and X (FP32)
-constexpr int OZ_MX = 128;                // columns of X (and of Y) per CTA: tensor-memory lanes
-constexpr int OZ_NA_ROWS = 32;            // rows of A (and of Y) per CTA
+constexpr int OZ_MA = 128;                // rows of A (and of Y) per CTA: tensor-memory lanes
+constexpr int OZ_NX = 64;                 // columns of X (and of Y) per CTA
 constexpr int OZ_BK = 64;                 // k chunk: one 128-byte swizzled row of bf16
 constexpr int OZ_PAD = 128;               // n padded to a multiple of this (rows, columns, k)
-constexpr int OZ_XBLK = 2 * OZ_MX * 128;          // X digit block (one t): Xr_t | Xi_t tiles, 32 KB
-constexpr int OZ_ABLK = 2 * OZ_NA_ROWS * 128;     // A digit block (one s): Ar_s | Ai_s rows, 8 KB
-constexpr int OZ_XSTAGE = OZ_SB * OZ_XBLK;        // a chunk's X digits, 96 KB
+constexpr int OZ_ABLK = 2 * OZ_MA * 128;          // A digit block (one s): Ar_s | Ai_s tiles, 32 KB
+constexpr int OZ_XBLK = 3 * OZ_NX * 128;          // X digit block (one t): -Xi_t | Xr_t | Xi_t, 24 KB
+constexpr int OZ_XSTAGE = OZ_SB * OZ_XBLK;        // a chunk's X digits, 72 KB
 constexpr int OZ_NXS = 2;                 // X chunk stages
-constexpr int OZ_NAS = 4;                 // A blocks in flight
+constexpr int OZ_NAS = 2;                 // A blocks in flight
 constexpr int OZ_NBUF = 4;                // tensor-memory level buffers, 128 columns each
-constexpr int OZ_FOLD_WARPS = 8;
+constexpr int OZ_FOLD_WARPS = 16;         // 4 per 32-lane quarter, 16 columns each
 constexpr int OZ_THREADS = 32 * (OZ_FOLD_WARPS + 2);   // + producer warp + MMA warp
 constexpr int OZ_NBAR = 2 * OZ_NXS + 2 * OZ_NAS + 2 * OZ_NBUF;
 constexpr int OZ_SMEM = OZ_NXS * OZ_XSTAGE + OZ_NAS * OZ_ABLK + 1024 + 8 * OZ_NBAR + 16;
@@ -61,8 +61,8 @@ constexpr uint32_t OZ_TMEM_COLS = 512;
 constexpr unsigned long long OZ_WAIT_NS = 2000000000ull;
 // instruction descriptor, kind::f16: D f32 (bits 4-5 = 1), A and B bf16
 // (bits 7-9, 10-12 = 1), both K-major, N >> 3 at bits 17-22, M >> 4 at 24-28
-constexpr uint32_t OZ_IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(64 >> 3) << 17) |
-                              ((uint32_t)(OZ_MX >> 4) << 24);
+constexpr uint32_t OZ_IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(128 >> 3) << 17) |
+                              ((uint32_t)(OZ_MA >> 4) << 24);
 
 static inline size_t al256(size_t x) { return (x + 255) & ~size_t(255); }
 static inline int padn(int n) { return (n + OZ_PAD - 1) / OZ_PAD * OZ_PAD; }
@@ -70,8 +70,8 @@ static inline int padn(int n) { return (n + OZ_PAD - 1) / OZ_PAD * OZ_PAD; }
 size_t ozaki_work_bytes(int n, int batch)
 {
     const size_t np = (size_t)padn(n), nb = (size_t)batch;
-    return al256(sizeof(__nv_bfloat16) * np * np * nb * 2 * OZ_SA)   // A digit blocks
-         + al256(sizeof(__nv_bfloat16) * np * np * nb * 2 * OZ_SB)   // X digit blocks
+    return al256(sizeof(__nv_bfloat16) * np * np * nb * 2 * OZ_SA)   // A digit blocks: Ar, Ai
+         + al256(sizeof(__nv_bfloat16) * np * np * nb * 3 * OZ_SB)   // X digit blocks: -Xi, Xr, Xi
          + 2 * al256(sizeof(int) * np * nb) + 256;                    // exponents
 }
 
@@ -140,7 +140,7 @@ __device__ __forceinline__ uint4 oz_pack8(const float d[8])
 // A digits.  Thread: row i, 8 consecutive k.  A is Hermitian: A_ik = conj(A_ki)
 // is read down column i (coalesced).  U = rint(A_ik 2^(47 - e_i))
 // (|U| <= 2^47, one rounding at 2^-48 of 2^(e_i+1)) is cut into 6 digits.
-// Layout: blocks [b][i / 32][k / 64][s] of 8 KB = [Ar_s | Ai_s], 32 rows each.
+// Layout: blocks [b][i / 128][k / 64][s] of 32 KB = [Ar_s | Ai_s], 128 rows each.
 __global__ void k_oz_digits_a(const double2 *A, int n, int np, const int *ex, unsigned char *D, int batch)
 {
     const int kg8 = np / 8;
@@ -166,20 +166,20 @@ __global__ void k_oz_digits_a(const double2 *A, int n, int np, const int *ex, un
         for (int q = 0; q < OZ_SA; ++q) { dr[q][u] = xr[q]; di[q][u] = xi[q]; }
     }
     const int KC = np / OZ_BK;
-    unsigned char *blk = D + ((((long)b * (np / OZ_NA_ROWS) + i / OZ_NA_ROWS) * KC + k0 / OZ_BK) * OZ_SA) * OZ_ABLK;
-    const uint32_t off = oz_swz(i % OZ_NA_ROWS, (k0 % OZ_BK) / 8);
+    unsigned char *blk = D + ((((long)b * (np / OZ_MA) + i / OZ_MA) * KC + k0 / OZ_BK) * OZ_SA) * OZ_ABLK;
+    const uint32_t off = oz_swz(i % OZ_MA, (k0 % OZ_BK) / 8);
 #pragma unroll
     for (int q = 0; q < OZ_SA; ++q) {
         *(uint4 *)(blk + (long)q * OZ_ABLK + off) = oz_pack8(dr[q]);
-        *(uint4 *)(blk + (long)q * OZ_ABLK + OZ_NA_ROWS * 128 + off) = oz_pack8(di[q]);
+        *(uint4 *)(blk + (long)q * OZ_ABLK + OZ_MA * 128 + off) = oz_pack8(di[q]);
     }
 }
 
 // X digits.  Thread: column j, 8 consecutive k (X column-major FP32).
 // U = rint(X_kj 2^(23 - f_j)) (|U| <= 2^23) is cut into 3 digits and X itself
 // is overwritten with U 2^(f_j - 23), the value its digits represent (exact in
-// FP32).  Layout: blocks [b][j / 128][k / 64][t] of 32 KB = [Xr_t | Xi_t],
-// 128 rows each.
+// FP32).  Layout: blocks [b][j / 64][k / 64][t] of 24 KB = [-Xi_t | Xr_t | Xi_t],
+// 64 rows each (negated digits are exact integers of the same range).
 __global__ void k_oz_digits_x(float2 *X, int n, int np, const int *ex, unsigned char *D, int batch)
 {
     const int kg8 = np / 8;
@@ -189,7 +189,7 @@ __global__ void k_oz_digits_x(float2 *X, int n, int np, const int *ex, unsigned 
     const long e = t - (long)b * np * kg8;
     const int j = (int)(e / kg8), kq = (int)(e % kg8), k0 = 8 * kq;
     const int fj = ex[(long)b * np + j];
-    float dr[OZ_SB][8], di[OZ_SB][8];
+    float dr[OZ_SB][8], di[OZ_SB][8], dn[OZ_SB][8];
 #pragma unroll
     for (int u = 0; u < 8; ++u) {
         const int k = k0 + u;
@@ -202,16 +202,18 @@ __global__ void k_oz_digits_x(float2 *X, int n, int np, const int *ex, unsigned 
         digits_of<OZ_SB>(ur, xr);
         digits_of<OZ_SB>(ui, xm);
 #pragma unroll
-        for (int q = 0; q < OZ_SB; ++q) { dr[q][u] = xr[q]; di[q][u] = xm[q]; }
+        for (int q = 0; q < OZ_SB; ++q) { dr[q][u] = xr[q]; di[q][u] = xm[q]; dn[q][u] = -xm[q]; }
         if (in) X[xi] = make_float2((float)ur * pow2f(fj - 23), (float)ui * pow2f(fj - 23));
     }
     const int KC = np / OZ_BK;
-    unsigned char *blk = D + ((((long)b * (np / OZ_MX) + j / OZ_MX) * KC + k0 / OZ_BK) * OZ_SB) * OZ_XBLK;
-    const uint32_t off = oz_swz(j % OZ_MX, (k0 % OZ_BK) / 8);
+    unsigned char *blk = D + ((((long)b * (np / OZ_NX) + j / OZ_NX) * KC + k0 / OZ_BK) * OZ_SB) * OZ_XBLK;
+    const uint32_t off = oz_swz(j % OZ_NX, (k0 % OZ_BK) / 8);
 #pragma unroll
     for (int q = 0; q < OZ_SB; ++q) {
-        *(uint4 *)(blk + (long)q * OZ_XBLK + off) = oz_pack8(dr[q]);
-        *(uint4 *)(blk + (long)q * OZ_XBLK + OZ_MX * 128 + off) = oz_pack8(di[q]);
+        unsigned char *bq = blk + (long)q * OZ_XBLK;
+        *(uint4 *)(bq + off) = oz_pack8(dn[q]);
+        *(uint4 *)(bq + OZ_NX * 128 + off) = oz_pack8(dr[q]);
+        *(uint4 *)(bq + 2 * OZ_NX * 128 + off) = oz_pack8(di[q]);
     }
 }
 
@@ -244,12 +246,14 @@ __device__ __forceinline__ void oz_commit(uint32_t bar)
                  : "memory");
 }
 
-__device__ __forceinline__ bool oz_test(uint32_t bar, uint32_t parity)
+// one bounded hardware wait (the thread is suspended until the phase completes
+// or about a microsecond passes)
+__device__ __forceinline__ bool oz_try(uint32_t bar, uint32_t parity)
 {
     uint32_t ok;
-    asm volatile("{\n\t.reg .pred p;\n\tmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+    asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
                  "selp.u32 %0, 1, 0, p;\n\t}\n"
-                 : "=r"(ok) : "r"(bar), "r"(parity) : "memory");
+                 : "=r"(ok) : "r"(bar), "r"(parity), "r"(1000u) : "memory");
     return ok != 0;
 }
 
@@ -262,13 +266,12 @@ __device__ __forceinline__ unsigned long long oz_ns()
 
 // wait for the phase of the given parity, at most OZ_WAIT_NS or until another
 // role has given up (abort flag)
-__device__ bool oz_wait(uint32_t bar, uint32_t parity, volatile int *abort)
+__device__ __forceinline__ bool oz_wait(uint32_t bar, uint32_t parity, volatile int *abort)
 {
-    if (oz_test(bar, parity)) return true;
+    if (oz_try(bar, parity)) return true;
     const unsigned long long t0 = oz_ns();
     for (;;) {
-        __nanosleep(32);
-        if (oz_test(bar, parity)) return true;
+        if (oz_try(bar, parity)) return true;
         if (*abort || oz_ns() - t0 > OZ_WAIT_NS) return false;
     }
 }
@@ -289,17 +292,13 @@ __device__ __forceinline__ void oz_arrive(uint32_t bar)
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" :: "r"(bar) : "memory");
 }
 
-__device__ __forceinline__ void oz_ld16(uint32_t taddr, float v[16])
+__device__ __forceinline__ void oz_ld4(uint32_t taddr, float v[4])
 {
-    uint32_t r[16];
-    asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 "
-                 "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-                   "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
-                   "=r"(r[14]), "=r"(r[15])
-                 : "r"(taddr));
+    uint32_t r[4];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]) : "r"(taddr));
 #pragma unroll
-    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+    for (int i = 0; i < 4; ++i) v[i] = __uint_as_float(r[i]);
 }
 
 // (hi, lo) += v, v exact in FP64's sense once scaled by a power of two
@@ -310,19 +309,21 @@ __device__ __forceinline__ void df_add(float &hi, float &lo, float v)
     hi = s;
 }
 
-// One CTA: rows i0..i0+31 of Y (A rows) x columns j0..j0+127 (X columns) of
-// one matrix, as the transpose tile in tensor memory (see the file header).
-__global__ void __launch_bounds__(OZ_THREADS, 1)
+// One CTA: rows i0..i0+127 of Y (A rows) x columns j0..j0+63 (X columns) of
+// one matrix (see the file header).
+// 18 warps: at most 5 per SM sub-partition, whose 16K registers allow 96
+// registers a thread
+__global__ void __maxnreg__(96)
 k_oz_gemm(const unsigned char *DA, const unsigned char *DX, const int *exA, const int *exX, double2 *Y, int n,
           int np, int batch)
 {
     extern __shared__ __align__(16) unsigned char oz_raw[];
-    const int it = blockIdx.x, jt = blockIdx.y, b = blockIdx.z;
+    const int jt = blockIdx.x, it = blockIdx.y, b = blockIdx.z;
     const int KC = np / OZ_BK;
     const uint32_t raw_s = oz_saddr(oz_raw);
     unsigned char *base = oz_raw + (((raw_s + 1023u) & ~1023u) - raw_s);
-    unsigned char *sX = base;                                   // OZ_NXS x 96 KB
-    unsigned char *sA = base + OZ_NXS * OZ_XSTAGE;              // OZ_NAS x 8 KB
+    unsigned char *sX = base;                                   // OZ_NXS x 72 KB
+    unsigned char *sA = base + OZ_NXS * OZ_XSTAGE;              // OZ_NAS x 32 KB
     uint64_t *bars = (uint64_t *)(sA + OZ_NAS * OZ_ABLK);
     uint32_t *tslot = (uint32_t *)(bars + OZ_NBAR);
     volatile int *abort = (volatile int *)(tslot + 1);
@@ -355,8 +356,8 @@ k_oz_gemm(const unsigned char *DA, const unsigned char *DX, const int *exA, cons
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = *tslot;
 
-    const unsigned char *gX = DX + (((long)b * (np / OZ_MX) + jt) * KC) * OZ_SB * OZ_XBLK;
-    const unsigned char *gA = DA + (((long)b * (np / OZ_NA_ROWS) + it) * KC) * OZ_SA * OZ_ABLK;
+    const unsigned char *gX = DX + (((long)b * (np / OZ_NX) + jt) * KC) * OZ_SB * OZ_XBLK;
+    const unsigned char *gA = DA + (((long)b * (np / OZ_MA) + it) * KC) * OZ_SA * OZ_ABLK;
 
     if (warp == OZ_FOLD_WARPS) {
         // ---- producer: bulk copies of the pre-swizzled digit tiles ----
@@ -379,7 +380,7 @@ k_oz_gemm(const unsigned char *DA, const unsigned char *DX, const int *exA, cons
             if (!ok) { *abort = 1; atomicOr(&g_oz_fault, 1u); }
         }
     } else if (warp == OZ_FOLD_WARPS + 1) {
-        // ---- MMA issue: plane-major within each chunk ----
+        // ---- MMA issue: plane s takes the digit pairs (s, 0), (s, 1), (s, 2) ----
         if (lane == 0) {
             bool ok = true;
             const uint32_t sx0 = oz_saddr(sX), sa0 = oz_saddr(sA);
@@ -390,6 +391,7 @@ k_oz_gemm(const unsigned char *DA, const unsigned char *DX, const int *exA, cons
                     const int qa = kc * OZ_SA + sdig, ia = qa % OZ_NAS, ua = qa / OZ_NAS;
                     if (!(ok = oz_wait(full_a(ia), ua & 1, abort))) break;
                     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                    const uint32_t ar = sa0 + ia * OZ_ABLK, ai = ar + OZ_MA * 128;
                     for (int tdig = 0; tdig < OZ_SB; ++tdig) {
                         const int L = sdig + tdig;
                         if (L > OZ_SA - 1) break;
@@ -400,16 +402,14 @@ k_oz_gemm(const unsigned char *DA, const unsigned char *DX, const int *exA, cons
                             if (!(ok = oz_wait(tempty(buf), ((ql - OZ_NBUF) / OZ_NBUF) & 1, abort))) break;
                             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
                         }
-                        const uint32_t xr = sx0 + jx * OZ_XSTAGE + tdig * OZ_XBLK, xi = xr + OZ_MX * 128;
-                        const uint32_t ab = sa0 + ia * OZ_ABLK;
-                        const uint32_t tP = tmem + 128u * buf, tQ = tP + 64u;
+                        // X block rows: [-Xi | Xr | Xi]; w1 = [Xr | Xi], w2 = [-Xi | Xr]
+                        const uint32_t w2 = sx0 + jx * OZ_XSTAGE + tdig * OZ_XBLK, w1 = w2 + OZ_NX * 128;
+                        const uint32_t tl = tmem + 128u * buf;
 #pragma unroll
                         for (int ks = 0; ks < OZ_BK / 16; ++ks) {
                             const uint32_t ko = 32u * ks;
-                            const uint64_t db = oz_desc(ab + ko);
-                            const uint32_t acc = (first && ks == 0) ? 0u : 1u;
-                            oz_mma(tP, oz_desc(xr + ko), db, acc);
-                            oz_mma(tQ, oz_desc(xi + ko), db, acc);
+                            oz_mma(tl, oz_desc(ar + ko), oz_desc(w1 + ko), (first && ks == 0) ? 0u : 1u);
+                            oz_mma(tl, oz_desc(ai + ko), oz_desc(w2 + ko), 1u);
                         }
                     }
                     if (!ok) break;
@@ -441,50 +441,55 @@ k_oz_gemm(const unsigned char *DA, const unsigned char *DX, const int *exA, cons
                 ok = __all_sync(0xffffffffu, oz_wait(tfull(buf), (ql / OZ_NBUF) & 1, abort));
                 if (!ok) break;
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                float pre[16], pim[16], qre[16], qim[16];
-                const uint32_t c0 = trow + 128u * buf + 16u * h;
-                oz_ld16(c0, pre);         // Xr Ar
-                oz_ld16(c0 + 32u, pim);   // Xr Ai
-                oz_ld16(c0 + 64u, qre);   // Xi Ar
-                oz_ld16(c0 + 96u, qim);   // Xi Ai
-                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-                asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-                __syncwarp();
-                if (lane == 0) oz_arrive(tempty(buf));
                 const float w = ldexpf(1.0f, -8 * (L + 2));
-                if (L < 3) {
-                    // levels 0-2: exact two-sum into (hi, lo)
+                // four groups of 4 columns (fewer live registers); the buffer is
+                // released once all are in registers
 #pragma unroll
-                    for (int c = 0; c < 16; ++c) {
-                        df_add(hr[c], lr[c], (pre[c] - qim[c]) * w);
-                        df_add(hi[c], li[c], (pim[c] + qre[c]) * w);
+                for (int hf = 0; hf < 4; ++hf) {
+                    float re[4], im[4];
+                    const uint32_t c0 = trow + 128u * buf + 16u * h + 4u * hf;
+                    oz_ld4(c0, re);           // Ar Xr - Ai Xi
+                    oz_ld4(c0 + 64u, im);     // Ar Xi + Ai Xr
+                    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                    if (hf == 3) {
+                        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+                        __syncwarp();
+                        if (lane == 0) oz_arrive(tempty(buf));
                     }
-                } else {
-                    // from level 3 on the contribution (< 2^-17 of the unit scale) goes
-                    // straight into lo, whose own rounding already bounds the pair's error
+                    if (L < 3) {
+                        // levels 0-2: exact two-sum into (hi, lo)
 #pragma unroll
-                    for (int c = 0; c < 16; ++c) {
-                        lr[c] = fmaf(pre[c] - qim[c], w, lr[c]);
-                        li[c] = fmaf(pim[c] + qre[c], w, li[c]);
+                        for (int c = 0; c < 4; ++c) {
+                            df_add(hr[4 * hf + c], lr[4 * hf + c], re[c] * w);
+                            df_add(hi[4 * hf + c], li[4 * hf + c], im[c] * w);
+                        }
+                    } else {
+                        // from level 3 on the contribution (< 2^-17 of the unit scale) goes
+                        // straight into lo, whose own rounding already bounds the pair's error
+#pragma unroll
+                        for (int c = 0; c < 4; ++c) {
+                            lr[4 * hf + c] = fmaf(re[c], w, lr[4 * hf + c]);
+                            li[4 * hf + c] = fmaf(im[c], w, li[4 * hf + c]);
+                        }
                     }
                 }
             }
         }
         if (!ok && lane == 0) { *abort = 1; atomicOr(&g_oz_fault, 1u); }
         if (ok) {
-            // Y[i, j], j = this thread's X column, i = 16 consecutive A rows:
+            // Y[i, j], i = this thread's A row, j = 16 consecutive X columns:
             // scale by 2^(e_i + 1) 2^(f_j + 1)
-            const int j = jt * OZ_MX + 32 * q4 + lane;
-            if (j < n) {
-                const int fj = exX[(long)b * np + j];
-                double2 *yc = Y + (long)b * n * n + (long)j * n;
+            const int i = it * OZ_MA + 32 * q4 + lane;
+            if (i < n) {
+                const int ei = exA[(long)b * np + i];
+                double2 *yb = Y + (long)b * n * n + i;
 #pragma unroll
                 for (int c = 0; c < 16; ++c) {
-                    const int i = it * OZ_NA_ROWS + 16 * h + c;
-                    if (i >= n) break;
-                    const int sh = exA[(long)b * np + i] + fj + 2;
-                    yc[i] = make_double2(ldexp((double)hr[c] + (double)lr[c], sh),
-                                         ldexp((double)hi[c] + (double)li[c], sh));
+                    const int j = jt * OZ_NX + 16 * h + c;
+                    if (j >= n) break;
+                    const double sc = pow2d(ei + exX[(long)b * np + j] + 2);   // exact power of two
+                    yb[(long)j * n] = make_double2(((double)hr[c] + (double)lr[c]) * sc,
+                                                   ((double)hi[c] + (double)li[c]) * sc);
                 }
             }
         }
@@ -506,7 +511,7 @@ OzakiX ozaki_prepare_x(cudaStream_t s, float2 *X, int n, int batch, void *work)
     char *w = (char *)work;
     ox.DA = (__nv_bfloat16 *)w;
     ox.DX = (__nv_bfloat16 *)(w + al256(sizeof(__nv_bfloat16) * npp * batch * 2 * OZ_SA));
-    ox.exA = (int *)((char *)ox.DX + al256(sizeof(__nv_bfloat16) * npp * batch * 2 * OZ_SB));
+    ox.exA = (int *)((char *)ox.DX + al256(sizeof(__nv_bfloat16) * npp * batch * 3 * OZ_SB));
     ox.exX = (int *)((char *)ox.exA + al256(sizeof(int) * (size_t)np * batch));
     ox.n = n; ox.np = np; ox.batch = batch;
     NRLTB_LAUNCH(k_oz_colexp<float2>, cdiv((long)np * batch * 32, 256), 256, 0, s, X, n, np, ox.exX, batch);
@@ -527,7 +532,7 @@ void ozaki_gemm(cudaStream_t s, const OzakiX &ox, const double2 *A, double2 *Y)
         return true;
     }();
     (void)attr;
-    dim3 grid(np / OZ_NA_ROWS, np / OZ_MX, batch);
+    dim3 grid(np / OZ_NX, np / OZ_MA, batch);
     cudaEvent_t ev = kt_begin(s);
     NRLTB_LAUNCH(k_oz_gemm, grid, OZ_THREADS, OZ_SMEM, s, (const unsigned char *)ox.DA,
                  (const unsigned char *)ox.DX, ox.exA, ox.exX, Y, n, np, batch);
