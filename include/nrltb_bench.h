@@ -25,7 +25,9 @@ int nrltb_bench_zgemm(nrltb_ctx *ctx, int precision, int n, int batch, int reps,
 
 /* One FP64-accurate product Y = A X of the mixed form's refinement (A FP64
  * Hermitian, X FP32, both n x n complex, `batch` matrices): method 0 = the
- * double-float SIMT GEMM, 1 = the bf16 tensor-core digit product.  Averaged
+ * double-float SIMT GEMM, 1 = the bf16 tensor-core digit product, 2 = the
+ * same with A rounded to 3 digits (the mixed form's Hellmann-Feynman
+ * products, FP32-class accuracy).  Averaged
  * over `reps` pairs of launches (H X and S X) after a warm-up;
  * flops_per_launch = 8 n^3 batch for one product. */
 int nrltb_bench_refprod(nrltb_ctx *ctx, int method, int n, int batch, int reps,
@@ -33,8 +35,8 @@ int nrltb_bench_refprod(nrltb_ctx *ctx, int method, int n, int batch, int reps,
 
 /* The same product on caller data, for accuracy checks: host arrays A
  * (batch x n x n complex FP64, column-major, interleaved re/im, Hermitian),
- * X (batch x n x n complex FP32; method 1 rounds it in place to the digits
- * it uses) and Y (batch x n x n complex FP64, out). */
+ * X (batch x n x n complex FP32; methods 1 and 2 round it in place to the
+ * digits they use) and Y (batch x n x n complex FP64, out). */
 int nrltb_bench_refprod_run(nrltb_ctx *ctx, int method, int n, int batch, const double *A, float *X,
                             double *Y);
 

@@ -158,7 +158,7 @@ static void refprod(cudaStream_t s, int method, int n, int batch, const double2 
         dfgemm<double2, float2>(s, n, n, n, batch, A, n, nn, 0, X, n, nn, 0, Y, n, nn);
     } else {
         const OzakiX ox = ozaki_prepare_x(s, X, n, batch, work);
-        ozaki_gemm(s, ox, A, Y);
+        ozaki_gemm(s, ox, A, Y, method == 2 ? 3 : 6);
     }
 }
 
@@ -170,7 +170,7 @@ struct DevBufs {
 extern "C" int nrltb_bench_refprod(nrltb_ctx *ctx, int method, int n, int batch, int reps, double *ms_per_launch,
                                    double *flops_per_launch)
 {
-    if (!ctx || (method != 0 && method != 1) || n < 1 || batch < 1 || reps < 1 || !ms_per_launch ||
+    if (!ctx || method < 0 || method > 2 || n < 1 || batch < 1 || reps < 1 || !ms_per_launch ||
         !flops_per_launch)
         return NRLTB_E_ARG;
     cudaStream_t s = nrltb_ctx_stream_internal(ctx);
@@ -208,7 +208,7 @@ extern "C" int nrltb_bench_refprod(nrltb_ctx *ctx, int method, int n, int batch,
 extern "C" int nrltb_bench_refprod_run(nrltb_ctx *ctx, int method, int n, int batch, const double *A, float *X,
                                        double *Y)
 {
-    if (!ctx || (method != 0 && method != 1) || n < 1 || batch < 1 || !A || !X || !Y) return NRLTB_E_ARG;
+    if (!ctx || method < 0 || method > 2 || n < 1 || batch < 1 || !A || !X || !Y) return NRLTB_E_ARG;
     cudaStream_t s = nrltb_ctx_stream_internal(ctx);
     const size_t nn = (size_t)n * n * batch;
     DevBufs d;

@@ -138,9 +138,11 @@ __device__ __forceinline__ uint4 oz_pack8(const float d[8])
 }
 
 // A digits.  Thread: row i, 8 consecutive k.  A is Hermitian: A_ik = conj(A_ki)
-// is read down column i (coalesced).  U = rint(A_ik 2^(47 - e_i))
-// (|U| <= 2^47, one rounding at 2^-48 of 2^(e_i+1)) is cut into 6 digits.
-// Layout: blocks [b][i / 128][k / 64][s] of 32 KB = [Ar_s | Ai_s], 128 rows each.
+// is read down column i (coalesced).  U = rint(A_ik 2^(8 SA - 1 - e_i))
+// (|U| <= 2^(8 SA - 1), one rounding at 2^-(8 SA) of 2^(e_i+1)) is cut into SA
+// digits.  Layout: blocks [b][i / 128][k / 64][s] of 32 KB = [Ar_s | Ai_s],
+// 128 rows each.
+template <int SA>
 __global__ void k_oz_digits_a(const double2 *A, int n, int np, const int *ex, unsigned char *D, int batch)
 {
     const int kg8 = np / 8;
@@ -149,8 +151,8 @@ __global__ void k_oz_digits_a(const double2 *A, int n, int np, const int *ex, un
     const int b = (int)(t / ((long)np * kg8));
     const long e = t - (long)b * np * kg8;
     const int i = (int)(e / kg8), kq = (int)(e % kg8), k0 = 8 * kq;
-    const double sc = pow2d(47 - ex[(long)b * np + i]);
-    float dr[OZ_SA][8], di[OZ_SA][8];
+    const double sc = pow2d(8 * SA - 1 - ex[(long)b * np + i]);
+    float dr[SA][8], di[SA][8];
 #pragma unroll
     for (int u = 0; u < 8; ++u) {
         const int k = k0 + u;
@@ -159,17 +161,17 @@ __global__ void k_oz_digits_a(const double2 *A, int n, int np, const int *ex, un
             v = A[(long)b * n * n + k + (long)i * n];
             v.y = -v.y;
         }
-        float xr[OZ_SA], xi[OZ_SA];
-        digits_of<OZ_SA>(__double2ll_rn(v.x * sc), xr);
-        digits_of<OZ_SA>(__double2ll_rn(v.y * sc), xi);
+        float xr[SA], xi[SA];
+        digits_of<SA>(__double2ll_rn(v.x * sc), xr);
+        digits_of<SA>(__double2ll_rn(v.y * sc), xi);
 #pragma unroll
-        for (int q = 0; q < OZ_SA; ++q) { dr[q][u] = xr[q]; di[q][u] = xi[q]; }
+        for (int q = 0; q < SA; ++q) { dr[q][u] = xr[q]; di[q][u] = xi[q]; }
     }
     const int KC = np / OZ_BK;
-    unsigned char *blk = D + ((((long)b * (np / OZ_MA) + i / OZ_MA) * KC + k0 / OZ_BK) * OZ_SA) * OZ_ABLK;
+    unsigned char *blk = D + ((((long)b * (np / OZ_MA) + i / OZ_MA) * KC + k0 / OZ_BK) * SA) * OZ_ABLK;
     const uint32_t off = oz_swz(i % OZ_MA, (k0 % OZ_BK) / 8);
 #pragma unroll
-    for (int q = 0; q < OZ_SA; ++q) {
+    for (int q = 0; q < SA; ++q) {
         *(uint4 *)(blk + (long)q * OZ_ABLK + off) = oz_pack8(dr[q]);
         *(uint4 *)(blk + (long)q * OZ_ABLK + OZ_MA * 128 + off) = oz_pack8(di[q]);
     }
@@ -313,6 +315,7 @@ __device__ __forceinline__ void df_add(float &hi, float &lo, float v)
 // one matrix (see the file header).
 // 18 warps: at most 5 per SM sub-partition, whose 16K registers allow 96
 // registers a thread
+template <int SA>
 __global__ void __maxnreg__(96)
 k_oz_gemm(const unsigned char *DA, const unsigned char *DX, const int *exA, const int *exX, double2 *Y, int n,
           int np, int batch)
@@ -357,7 +360,9 @@ k_oz_gemm(const unsigned char *DA, const unsigned char *DX, const int *exA, cons
     const uint32_t tmem = *tslot;
 
     const unsigned char *gX = DX + (((long)b * (np / OZ_NX) + jt) * KC) * OZ_SB * OZ_XBLK;
-    const unsigned char *gA = DA + (((long)b * (np / OZ_MA) + it) * KC) * OZ_SA * OZ_ABLK;
+    const unsigned char *gA = DA + (((long)b * (np / OZ_MA) + it) * KC) * SA * OZ_ABLK;
+    // digit levels L = s + t kept per chunk: L <= 5 of 6 x 3 digits, all of 3 x 3
+    constexpr int NL = SA == 6 ? 6 : SA + OZ_SB - 1;
 
     if (warp == OZ_FOLD_WARPS) {
         // ---- producer: bulk copies of the pre-swizzled digit tiles ----
@@ -370,8 +375,8 @@ k_oz_gemm(const unsigned char *DA, const unsigned char *DX, const int *exA, cons
                 for (int q = 0; q < OZ_SB; ++q)
                     oz_bulk(oz_saddr(sX + jx * OZ_XSTAGE + q * OZ_XBLK), gX + ((long)kc * OZ_SB + q) * OZ_XBLK,
                             OZ_XBLK, full_x(jx));
-                for (int sdig = 0; sdig < OZ_SA; ++sdig) {
-                    const int qa = kc * OZ_SA + sdig, ia = qa % OZ_NAS, ua = qa / OZ_NAS;
+                for (int sdig = 0; sdig < SA; ++sdig) {
+                    const int qa = kc * SA + sdig, ia = qa % OZ_NAS, ua = qa / OZ_NAS;
                     if (ua > 0 && !(ok = oz_wait(empty_a(ia), (ua - 1) & 1, abort))) break;
                     oz_expect(full_a(ia), OZ_ABLK);
                     oz_bulk(oz_saddr(sA + ia * OZ_ABLK), gA + (long)qa * OZ_ABLK, OZ_ABLK, full_a(ia));
@@ -387,15 +392,15 @@ k_oz_gemm(const unsigned char *DA, const unsigned char *DX, const int *exA, cons
             for (int kc = 0; kc < KC && ok; ++kc) {
                 const int jx = kc % OZ_NXS, ux = kc / OZ_NXS;
                 if (!(ok = oz_wait(full_x(jx), ux & 1, abort))) break;
-                for (int sdig = 0; sdig < OZ_SA; ++sdig) {
-                    const int qa = kc * OZ_SA + sdig, ia = qa % OZ_NAS, ua = qa / OZ_NAS;
+                for (int sdig = 0; sdig < SA; ++sdig) {
+                    const int qa = kc * SA + sdig, ia = qa % OZ_NAS, ua = qa / OZ_NAS;
                     if (!(ok = oz_wait(full_a(ia), ua & 1, abort))) break;
                     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
                     const uint32_t ar = sa0 + ia * OZ_ABLK, ai = ar + OZ_MA * 128;
                     for (int tdig = 0; tdig < OZ_SB; ++tdig) {
                         const int L = sdig + tdig;
-                        if (L > OZ_SA - 1) break;
-                        const int ql = kc * OZ_SA + L, buf = ql % OZ_NBUF;
+                        if (L > NL - 1) break;
+                        const int ql = kc * NL + L, buf = ql % OZ_NBUF;
                         const bool first = sdig == (L > 2 ? L - 2 : 0);
                         if (first && ql >= OZ_NBUF) {
                             // the fold of level ql - 4 has emptied this buffer
@@ -414,7 +419,9 @@ k_oz_gemm(const unsigned char *DA, const unsigned char *DX, const int *exA, cons
                     }
                     if (!ok) break;
                     oz_commit(empty_a(ia));
-                    oz_commit(tfull((kc * OZ_SA + sdig) % OZ_NBUF));   // level sdig of this chunk is complete
+                    // level sdig of this chunk is complete; after the last plane, all remaining ones
+                    for (int L = sdig; L < (sdig == SA - 1 ? NL : sdig + 1); ++L)
+                        oz_commit(tfull((kc * NL + L) % OZ_NBUF));
                 }
                 if (!ok) break;
                 oz_commit(empty_x(jx));
@@ -436,8 +443,8 @@ k_oz_gemm(const unsigned char *DA, const unsigned char *DX, const int *exA, cons
         bool ok = true;
         for (int kc = 0; kc < KC && ok; ++kc) {
 #pragma unroll 1
-            for (int L = 0; L < OZ_SA; ++L) {
-                const int ql = kc * OZ_SA + L, buf = ql % OZ_NBUF;
+            for (int L = 0; L < NL; ++L) {
+                const int ql = kc * NL + L, buf = ql % OZ_NBUF;
                 ok = __all_sync(0xffffffffu, oz_wait(tfull(buf), (ql / OZ_NBUF) & 1, abort));
                 if (!ok) break;
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -520,23 +527,29 @@ OzakiX ozaki_prepare_x(cudaStream_t s, float2 *X, int n, int batch, void *work)
     return ox;
 }
 
-void ozaki_gemm(cudaStream_t s, const OzakiX &ox, const double2 *A, double2 *Y)
+template <int SA> static void ozaki_gemm_sa(cudaStream_t s, const OzakiX &ox, const double2 *A, double2 *Y)
 {
     const int n = ox.n, np = ox.np, batch = ox.batch;
     const size_t npp = (size_t)np * np;
     NRLTB_LAUNCH(k_oz_colexp<double2>, cdiv((long)np * batch * 32, 256), 256, 0, s, A, n, np, ox.exA, batch);
-    NRLTB_LAUNCH(k_oz_digits_a, cdiv((long)npp / 8 * batch, 256), 256, 0, s, A, n, np, ox.exA,
+    NRLTB_LAUNCH(k_oz_digits_a<SA>, cdiv((long)npp / 8 * batch, 256), 256, 0, s, A, n, np, ox.exA,
                  (unsigned char *)ox.DA, batch);
     static const bool attr = [] {
-        cudaFuncSetAttribute(k_oz_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, OZ_SMEM);
+        cudaFuncSetAttribute(k_oz_gemm<SA>, cudaFuncAttributeMaxDynamicSharedMemorySize, OZ_SMEM);
         return true;
     }();
     (void)attr;
     dim3 grid(np / OZ_NX, np / OZ_MA, batch);
     cudaEvent_t ev = kt_begin(s);
-    NRLTB_LAUNCH(k_oz_gemm, grid, OZ_THREADS, OZ_SMEM, s, (const unsigned char *)ox.DA,
+    NRLTB_LAUNCH(k_oz_gemm<SA>, grid, OZ_THREADS, OZ_SMEM, s, (const unsigned char *)ox.DA,
                  (const unsigned char *)ox.DX, ox.exA, ox.exX, Y, n, np, batch);
     kt_end(ev, s, KC_DIGIT_GEMM, 8.0 * n * (double)n * n * batch);
+}
+
+void ozaki_gemm(cudaStream_t s, const OzakiX &ox, const double2 *A, double2 *Y, int adigits)
+{
+    if (adigits == 3) ozaki_gemm_sa<3>(s, ox, A, Y);
+    else ozaki_gemm_sa<6>(s, ox, A, Y);
 }
 
 unsigned ozaki_fault(bool clear)

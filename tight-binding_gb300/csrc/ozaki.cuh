@@ -17,8 +17,11 @@ size_t ozaki_work_bytes(int n, int batch);
 // of each column's largest element) and splits it; work holds
 // ozaki_work_bytes(n, batch) bytes, 256-byte aligned.
 OzakiX ozaki_prepare_x(cudaStream_t s, float2 *X, int n, int batch, void *work);
-// Y = A X for the batch, A column-major n x n Hermitian (both triangles stored)
-void ozaki_gemm(cudaStream_t s, const OzakiX &ox, const double2 *A, double2 *Y);
+// Y = A X for the batch, A column-major n x n Hermitian (both triangles stored).
+// adigits = 6: A cut after 48 bits, digit levels up to 5 (FP64-accurate);
+// adigits = 3: A rounded to 24 bits of its row scale, all 9 digit pairs
+// (the exact product of the rounded A and X, FP32-class accuracy).
+void ozaki_gemm(cudaStream_t s, const OzakiX &ox, const double2 *A, double2 *Y, int adigits = 6);
 // fault flag of the product kernel (a barrier wait that ran out); clear resets it
 unsigned ozaki_fault(bool clear);
 

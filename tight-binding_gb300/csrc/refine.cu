@@ -500,8 +500,10 @@ void refine_eigen(cudaStream_t s, RefineWork &w, const double2 *H, const double2
 
 size_t hf_scratch_bytes(int n, int nkc)
 {
-    // FP64 form: P, Q (2 n^2 double2); mixed form: dH, dS, Z, P as float2 (4 n^2 float2)
-    return 2 * sizeof(double2) * (size_t)n * n * nkc + 512;
+    // FP64 form: P, Q (2 n^2 double2); mixed form: P, Q, Z as float2 and the
+    // digit planes of the tensor-core products
+    const size_t nn = (size_t)n * n * nkc;
+    return al256(2 * sizeof(double2) * nn) + al256(sizeof(float2) * nn) + ozaki_work_bytes(n, nkc) + 512;
 }
 
 __global__ void k_to_f32(const double2 *src, float2 *dst, long count)
@@ -530,24 +532,22 @@ int run_hf(cudaStream_t s, int n, int nkc, int prec, const double2 *dH, const do
         zgemm<double>(s, n, n, n, nkc, one, dS, n, nn, 0, Z, n, nn, 0, zero, Q, n, nn, 2, 0, 0);
         launch_hf_dots(s, Z, P, Q, dH, dS, eig, deig, n, nkc);
     } else {
-        // Mixed form: P = triu(dH) Z, Q = triu(dS) Z in FP32 on the FMA pipe
-        // (not the tensor cores: the MMA accumulator's rounding is biased
-        // toward zero, and a relative bias of ~1e-6 in P shifts the pressure
-        // coherently by ~1e-7 Ry/bohr^3), then
-        // deig = 2 Re(z^H P) - sum dH_ii |z_i|^2 - e (2 Re(z^H Q) - sum dS_ii |z_i|^2)
-        // with FP64 sums; the pressure error stays ~1e-10 Ry/bohr^3 per k
-        // against the 1e-3 kbar (6.8e-9) tolerance.  The scratch holds
-        // dH32 | dS32 | Z32 | P32 (4 n^2 float2 = 2 n^2 double2); dS Z
-        // overwrites dH32 once dH Z is formed.
-        float2 *h32 = (float2 *)scratch, *s32 = h32 + nn * nkc, *z32 = s32 + nn * nkc;
-        float2 *p32 = z32 + nn * nkc;
-        launch_to_f32(s, dH, h32, nn * nkc);
-        launch_to_f32(s, dS, s32, nn * nkc);
+        // Mixed form: P = dH Z', Q = dS Z' by the tensor-core digit product with
+        // dH, dS rounded to 24 bits of their row scale (3 digits) and Z' = Z
+        // rounded to 24 bits of its column scale, every digit pair kept: the
+        // exact product of the rounded operands, so no accumulation bias (a
+        // biased FP32 accumulation, as in the tensor cores' own, of ~1e-6
+        // relative in P shifts the pressure coherently by ~1e-7 Ry/bohr^3);
+        // then deig = Re(z^H P) - e Re(z^H Q) with FP64 Z and sums.  The
+        // pressure error stays ~1e-10 Ry/bohr^3 per k against the 1e-3 kbar
+        // (6.8e-9) tolerance.
+        float2 *z32 = (float2 *)((char *)Q + al256(sizeof(double2) * nn * nkc));
+        void *oz = (char *)z32 + al256(sizeof(float2) * nn * nkc);
         launch_to_f32(s, Z, z32, nn * nkc);
-        const float2 one = make_float2(1.f, 0.f), zero = make_float2(0.f, 0.f);
-        zgemm_simt<float>(s, n, n, n, nkc, one, h32, n, nn, 0, z32, n, nn, 0, zero, p32, n, nn, 2, 0, 0);
-        zgemm_simt<float>(s, n, n, n, nkc, one, s32, n, nn, 0, z32, n, nn, 0, zero, h32, n, nn, 2, 0, 0);
-        launch_hf_dots32_tri(s, z32, p32, h32, dH, dS, eig, deig, n, nkc);
+        const OzakiX ox = ozaki_prepare_x(s, z32, n, nkc, oz);
+        ozaki_gemm(s, ox, dH, P, 3);
+        ozaki_gemm(s, ox, dS, Q, 3);
+        launch_hf_dots_full(s, Z, P, Q, eig, deig, n, nkc);
     }
     return cudaGetLastError() == cudaSuccess ? NRLTB_OK : NRLTB_E_CUDA;
 }

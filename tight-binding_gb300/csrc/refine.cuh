@@ -30,7 +30,7 @@ void refine_eigen(cudaStream_t s, RefineWork &w, const double2 *H, const double2
                   double *eig, double2 *Z, int *status);
 
 // Hellmann-Feynman shifts deig = diag(Z^H dH Z) - eig * diag(Z^H dS Z) for nkc
-// matrices; scratch must hold 2 n^2 nkc double2.
+// matrices; scratch must hold hf_scratch_bytes(n, nkc), 256-byte aligned.
 int run_hf(cudaStream_t s, int n, int nkc, int prec, const double2 *dH, const double2 *dS, const double2 *Z,
            const double *eig, double *deig, void *scratch, void *unused);
 size_t hf_scratch_bytes(int n, int nkc);

@@ -152,8 +152,9 @@ __global__ void k_ncut(const double *eig, int ldk, int nv, int nk, double eigcut
 // Hellmann-Feynman shifts from P = triu(dH) Z and Q = triu(dS) Z:
 //   z^H M z = 2 Re(z^H triu(M) z) - sum_i M_ii |z_i|^2
 //   deig_n = z_n^H dH z_n - e_n z_n^H dS z_n
-// One warp per (column n, matrix).
-template <typename C2>
+// or, FULL, from the full products P = dH Z, Q = dS Z (deig_n = Re z_n^H P_n -
+// e_n Re z_n^H Q_n).  One warp per (column n, matrix).
+template <typename C2, bool FULL = false>
 __global__ void k_hf_dots(const C2 *Z, const C2 *Pm, const C2 *Qm, const double2 *dH, const double2 *dS,
                           const double *eig, double *deig, int n, int batch)
 {
@@ -166,14 +167,17 @@ __global__ void k_hf_dots(const C2 *Z, const C2 *Pm, const C2 *Qm, const double2
         const C2 z = Z[off + i], p = Pm[off + i], q = Qm[off + i];
         sp += (double)z.x * p.x + (double)z.y * p.y;
         sq += (double)z.x * q.x + (double)z.y * q.y;
-        const double a2 = (double)z.x * z.x + (double)z.y * z.y;
-        dh += dH[(long)b * n * n + (long)i * (n + 1)].x * a2;
-        ds += dS[(long)b * n * n + (long)i * (n + 1)].x * a2;
+        if (!FULL) {
+            const double a2 = (double)z.x * z.x + (double)z.y * z.y;
+            dh += dH[(long)b * n * n + (long)i * (n + 1)].x * a2;
+            ds += dS[(long)b * n * n + (long)i * (n + 1)].x * a2;
+        }
     }
-    sp = warp_sum(sp); sq = warp_sum(sq); dh = warp_sum(dh); ds = warp_sum(ds);
+    sp = warp_sum(sp); sq = warp_sum(sq);
+    if (!FULL) { dh = warp_sum(dh); ds = warp_sum(ds); }
     if (lane == 0) {
         const double e = eig[(long)b * n + col];
-        deig[(long)b * n + col] = (2.0 * sp - dh) - e * (2.0 * sq - ds);
+        deig[(long)b * n + col] = FULL ? sp - e * sq : (2.0 * sp - dh) - e * (2.0 * sq - ds);
     }
 }
 
@@ -184,11 +188,12 @@ void launch_hf_dots(cudaStream_t s, const double2 *Z, const double2 *P, const do
     NRLTB_LAUNCH(k_hf_dots<double2>, cdiv(warps * 32, 256), 256, 0, s, Z, P, Q, dH, dS, eig, deig, n, batch);
 }
 
-void launch_hf_dots32_tri(cudaStream_t s, const float2 *Z, const float2 *P, const float2 *Q, const double2 *dH,
-                          const double2 *dS, const double *eig, double *deig, int n, int batch)
+void launch_hf_dots_full(cudaStream_t s, const double2 *Z, const double2 *P, const double2 *Q, const double *eig,
+                         double *deig, int n, int batch)
 {
     const long warps = (long)n * batch;
-    NRLTB_LAUNCH(k_hf_dots<float2>, cdiv(warps * 32, 256), 256, 0, s, Z, P, Q, dH, dS, eig, deig, n, batch);
+    NRLTB_LAUNCH((k_hf_dots<double2, true>), cdiv(warps * 32, 256), 256, 0, s, Z, P, Q, nullptr, nullptr, eig,
+                 deig, n, batch);
 }
 
 }  // namespace nrltb

@@ -23,8 +23,8 @@ __global__ void k_fermi_sums(FermiJob *jobs);
 __global__ void k_ncut(const double *eig, int ldk, int nv, int nk, double eigcut, int *ncut);
 void launch_hf_dots(cudaStream_t s, const double2 *Z, const double2 *P, const double2 *Q, const double2 *dH,
                     const double2 *dS, const double *eig, double *deig, int n, int batch);
-// the same from FP32 Z, P = triu(dH) Z, Q = triu(dS) Z (FP64 sums and diagonals)
-void launch_hf_dots32_tri(cudaStream_t s, const float2 *Z, const float2 *P, const float2 *Q, const double2 *dH,
-                          const double2 *dS, const double *eig, double *deig, int n, int batch);
+// the same from the full products P = dH Z, Q = dS Z
+void launch_hf_dots_full(cudaStream_t s, const double2 *Z, const double2 *P, const double2 *Q, const double *eig,
+                         double *deig, int n, int batch);
 
 }  // namespace nrltb
