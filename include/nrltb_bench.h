@@ -43,7 +43,7 @@ int nrltb_bench_refprod_run(nrltb_ctx *ctx, int method, int n, int batch, const 
 /* One FP32 complex GEMM of the eigensolver's kernel on caller data, for
  * accuracy checks: C = alpha op(A) op(B) + beta C with the kernel's op and
  * triangle flags (gemm.cuh), one matrix; method 1 = the library's dispatch,
- * 2 = SIMT, 3 = the tcgen05 kernel (op A = op B = N only), 4 = the mma.sync
+ * 2 = SIMT, 3 = the tcgen05 kernel (op A = N only), 4 = the mma.sync
  * tensor-core kernel.
  * A, B, C are host arrays (column-major complex FP32, leading dimensions
  * lda, ldb, ldc); alpha, beta are {re, im}. */

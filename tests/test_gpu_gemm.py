@@ -5,7 +5,7 @@ the solver uses, on ragged sizes.  Bound: 2^-20 (|alpha| |op(A)| |op(B)| +
 kernels (3xTF32 with FP32 accumulation in the tensor cores; both the tcgen05
 and the mma.sync kernel measure 1.3e-6 at k = 333); elements whose bound is 0
 must be exact.  Methods: 1 the library's dispatch, 2 SIMT, 3 the tcgen05
-kernel (untransposed operands), 4 the mma.sync tensor-core kernel."""
+kernel (op(A) = A), 4 the mma.sync tensor-core kernel."""
 import ctypes as C
 
 import numpy as np
@@ -68,12 +68,16 @@ CASES = [
     (200, 200, 32, 1, 0, 0, 0, 2),
     (33, 1, 250, 1, 0, 0, 0, 0),
     (1, 1, 1, 0, 0, 0, 0, 0),
-    # several 128 x 64 tiles and 32-deep k slices (both shared-memory stages)
+    # several 128 x 64 tiles and 32-deep k slices
     (300, 200, 333, 0, 0, 0, 0, 0),
     (256, 130, 256, 0, 0, 2, 0, 0),
     (256, 256, 200, 0, 0, 0, 2, 1),
     (257, 100, 161, 0, 0, 1, 0, 0),
     (129, 65, 1, 0, 0, 0, 0, 0),
+    # rank-32 / 64 updates with op(B) = B^H (Cholesky and tridiagonal trailing updates)
+    (300, 300, 64, 0, 1, 0, 0, 1),
+    (256, 200, 32, 0, 1, 0, 0, 0),
+    (260, 130, 96, 0, 1, 0, 1, 0),
 ]
 
 
@@ -81,8 +85,8 @@ CASES = [
 @pytest.mark.parametrize("method", [1, 2, 3, 4])
 def test_cgemm_forms(ctx, case, method):
     m, n, k, opA, opB, triA, triB, triC = case
-    if method == 3 and (opA or opB):
-        pytest.skip("the tcgen05 kernel takes untransposed operands")
+    if method == 3 and opA:
+        pytest.skip("the tcgen05 kernel takes op(A) = A")
     ctx.lib.nrltb_bench_umma_fault(1)
     for alpha, beta, seed in ((1 + 0j, 0j, 1), (-0.5 + 0.25j, 1 + 0j, 2)):
         r = _run(ctx, method, m, n, k, opA, opB, triA, triB, triC, alpha, beta, seed)

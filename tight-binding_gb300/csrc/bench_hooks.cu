@@ -238,7 +238,7 @@ extern "C" int nrltb_bench_cgemm_run(nrltb_ctx *ctx, int method, int m, int n, i
 {
     if (!ctx || method < 1 || method > 4 || m < 1 || n < 1 || k < 1 || !alpha || !beta || !A || !B || !C)
         return NRLTB_E_ARG;
-    if (method == 3 && (opA != 0 || opB != 0)) return NRLTB_E_ARG;
+    if (method == 3 && opA != 0) return NRLTB_E_ARG;
     if (opA < 0 || opA > 1 || opB < 0 || opB > 1 || triA < 0 || triA > 2 || triB < 0 || triB > 2 || triC < 0 ||
         triC > 2)
         return NRLTB_E_ARG;

@@ -141,7 +141,7 @@ zgemm_kernel(GemmArgs<T> g)
 }
 
 // FP32 on the tensor cores: tcgen05 with tensor-memory accumulators for
-// untransposed operands (gemm_umma.cu), mma.sync otherwise (gemm_tc.cu)
+// op(A) = A (gemm_umma.cu), mma.sync otherwise (gemm_tc.cu)
 void zgemm_tc_launch(cudaStream_t s, const GemmArgs<float> &g);
 bool zgemm_umma_supported(const GemmArgs<float> &g);
 void zgemm_umma_launch(cudaStream_t s, const GemmArgs<float> &g);
@@ -267,18 +267,19 @@ void zgemm(cudaStream_t s, int m, int n, int k, int batch, typename cplx<T>::t a
            int triA = 0, int triB = 0, int triC = 0)
 {
     if (m <= 0 || n <= 0 || batch <= 0) return;
-    // tensor cores only for large m, n and a long k loop
-    // (rank-32 panel updates run faster on the FMA pipe)
+    // tensor cores for m >= 128, n >= 64: tcgen05 (op(A) = A) from k = 32,
+    // mma.sync (op(A) = A^H) from k = 128; the rest on the FMA pipe
     if constexpr (sizeof(T) == 4) {
-        if (m < 128 || n < 64 || k < 128) {
+        const GemmArgs<float> g = gemm_args<T>(m, n, k, batch, alpha, A, lda, sA, opA, B, ldb, sB, opB, beta, C,
+                                               ldc, sC, triA, triB, triC);
+        const bool umma = zgemm_umma_supported(g);
+        if (m < 128 || n < 64 || k < (umma ? 32 : 128)) {
             zgemm_simt<T>(s, m, n, k, batch, alpha, A, lda, sA, opA, B, ldb, sB, opB, beta, C, ldc, sC, triA, triB,
                           triC);
             return;
         }
         cudaEvent_t ev = kt_begin(s);
-        const GemmArgs<float> g = gemm_args<T>(m, n, k, batch, alpha, A, lda, sA, opA, B, ldb, sB, opB, beta, C,
-                                               ldc, sC, triA, triB, triC);
-        if (zgemm_umma_supported(g)) zgemm_umma_launch(s, g);
+        if (umma) zgemm_umma_launch(s, g);
         else zgemm_tc_launch(s, g);
         if (ev) kt_end(ev, s, KC_GEMM_TC, 8.0 * gemm_useful_macs(m, n, k, triA, triB, triC) * batch);
     } else {

@@ -1,7 +1,7 @@
 // gemm_umma.cu -- batched complex FP32 GEMM on the 5th-generation tensor cores
 // (tcgen05, TF32 operands from shared memory, FP32 accumulators in tensor
-// memory), for the forms C = alpha A B + beta C with both operands
-// untransposed (the eigensolver's large products).
+// memory), for the forms C = alpha A op(B) + beta C with op(B) = B or B^H (the
+// eigensolver's large products and its rank-32/64 panel updates).
 //
 // 3xTF32: each FP32 operand x is split into a TF32 head h = tf32(x) and tail
 // l = tf32(x - h); a real product is l_a h_b + h_a l_b + h_a h_b (the dropped
@@ -140,6 +140,7 @@ __device__ __forceinline__ void um_put4(unsigned char *ph, unsigned char *pl, ui
     *(uint4 *)(pl + off) = l;
 }
 
+template <int TB>   // 1: op(B) = B^H
 __global__ void __launch_bounds__(UM_THREADS, 2) zgemm_umma_kernel(GemmArgs<float> g)
 {
     extern __shared__ __align__(16) unsigned char um_raw[];
@@ -180,8 +181,11 @@ __global__ void __launch_bounds__(UM_THREADS, 2) zgemm_umma_kernel(GemmArgs<floa
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = *tslot;
 
-    // staging maps: A row ra_r, k groups (tid >> 7) + 2u; B column rb_n, k groups (tid & 3) + 4u
-    const int ra_r = tid & (UM_BM - 1), rb_n = tid >> 2;
+    // staging maps: A row ra_r, k groups (tid >> 7) + 2u; B column rb_n, k groups
+    // rb_g + 4u (B: four consecutive k of a column are contiguous; B^H: the
+    // threads of a warp walk consecutive columns)
+    const int ra_r = tid & (UM_BM - 1);
+    const int rb_n = TB ? (tid & (UM_BN - 1)) : (tid >> 2), rb_g = TB ? (tid >> 6) : (tid & 3);
     float2 ra[16], rb[8];
     auto fetch = [&](int k0) {
         const int m = m0 + ra_r;
@@ -200,11 +204,16 @@ __global__ void __launch_bounds__(UM_THREADS, 2) zgemm_umma_kernel(GemmArgs<floa
         for (int u = 0; u < 2; ++u)
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
-                const int k = k0 + 4 * ((tid & 3) + 4 * u) + j;
+                const int k = k0 + 4 * (rb_g + 4 * u) + j;
                 bool ok = n < g.n && k < kend;
                 if (g.triB == 1) ok = ok && k <= n;
                 if (g.triB == 2) ok = ok && k >= n;
-                rb[4 * u + j] = ok ? B[k + (long)n * g.ldb] : make_float2(0.f, 0.f);
+                float2 v = make_float2(0.f, 0.f);
+                if (ok) {
+                    if (TB) { v = B[n + (long)k * g.ldb]; v.y = -v.y; }
+                    else v = B[k + (long)n * g.ldb];
+                }
+                rb[4 * u + j] = v;
             }
     };
     auto store = [&](unsigned char *st) {
@@ -220,7 +229,7 @@ __global__ void __launch_bounds__(UM_THREADS, 2) zgemm_umma_kernel(GemmArgs<floa
         unsigned char *bh = st + 4 * UM_APL, *bl = bh + UM_BPL;
 #pragma unroll
         for (int u = 0; u < 2; ++u) {
-            const int gk = (tid & 3) + 4 * u;
+            const int gk = rb_g + 4 * u;
             float re[4], im[4];
 #pragma unroll
             for (int j = 0; j < 4; ++j) { re[j] = rb[4 * u + j].x; im[j] = rb[4 * u + j].y; }
@@ -325,18 +334,20 @@ __global__ void __launch_bounds__(UM_THREADS, 2) zgemm_umma_kernel(GemmArgs<floa
 
 bool zgemm_umma_supported(const GemmArgs<float> &g)
 {
-    return g.opA == 0 && g.opB == 0;
+    return g.opA == 0;
 }
 
 void zgemm_umma_launch(cudaStream_t s, const GemmArgs<float> &g)
 {
     static const bool attr = [] {
-        cudaFuncSetAttribute(zgemm_umma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, UM_SMEM);
+        cudaFuncSetAttribute(zgemm_umma_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, UM_SMEM);
+        cudaFuncSetAttribute(zgemm_umma_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, UM_SMEM);
         return true;
     }();
     (void)attr;
     dim3 grid(cdiv(g.m, UM_BM), cdiv(g.n, UM_BN), g.batch);
-    NRLTB_LAUNCH(zgemm_umma_kernel, grid, UM_THREADS, UM_SMEM, s, g);
+    if (g.opB) NRLTB_LAUNCH(zgemm_umma_kernel<1>, grid, UM_THREADS, UM_SMEM, s, g);
+    else NRLTB_LAUNCH(zgemm_umma_kernel<0>, grid, UM_THREADS, UM_SMEM, s, g);
 }
 
 unsigned zgemm_umma_fault(bool clear)
