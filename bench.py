@@ -147,10 +147,12 @@ def run_reference(args):
 
 
 KCLASSES = [  # (class id, name, bound, unit of work)
-    (0, "zgemm_tc_kernel: FP32 complex GEMM on the tensor cores (3xTF32 mma.sync)", "tensor", "flop"),
-    (1, "zgemm_kernel: complex GEMM on the FMA pipe (FP64 form; FP32 Hellmann-Feynman and k<128 shapes)",
+    (0, "zgemm_umma_kernel / zgemm_tc_kernel: FP32 complex GEMM on the tensor cores (3xTF32; tcgen05 with "
+        "tensor-memory accumulators for op(A) = A, mma.sync for op(A) = A^H)", "tensor", "flop"),
+    (1, "zgemm_kernel: complex GEMM on the FMA pipe (FP64 form; FP32 shapes below the tensor-core thresholds)",
      "fma", "flop"),
-    (2, "k_oz_gemm: FP64-accurate H X, S X from bf16 digit products (mma.sync)", "tensor", "flop"),
+    (2, "k_oz_gemm: bf16 digit products on tcgen05 (refinement H X, S X to FP64 accuracy; Hellmann-Feynman "
+        "dH Z, dS Z from 3-digit dH, dS)", "tensor", "flop"),
     (3, "k_tri_panel: tridiagonalisation panel (cluster per matrix, Hermitian mat-vec)", "hbm", "byte"),
 ]
 
