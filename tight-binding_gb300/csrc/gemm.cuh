@@ -12,7 +12,8 @@
 //
 // SIMT register-tiled kernel: a BM x BN tile per CTA, BK-deep k slices staged
 // through shared memory, TM x TN complex outputs per thread.  FP64 runs here
-// (GB300 has no FP64 tensor path); FP32 goes to the tensor cores (gemm_tc.cu).
+// (GB300 has no FP64 tensor path); FP32 goes to the tensor cores
+// (gemm_umma.cu, gemm_tc.cu).
 #pragma once
 #include <algorithm>
 #include "common.cuh"

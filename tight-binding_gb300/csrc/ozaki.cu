@@ -15,7 +15,9 @@
 // im = Xr Ai + Xi Ar (below 2^22.6).  Each chunk's level sums are folded,
 // scaled by 256^-(L+2), into a double-float (FP32 pair) accumulator.  Levels
 // L <= 5 are kept (15 digit pairs); the dropped ones and the 6-digit cut of A
-// are below 2^-48 of |A row| |X column| per term.
+// are below 2^-48 of |A row| |X column| per term.  A 3-digit form (A rounded to
+// 24 bits of its row scale, all 9 digit pairs, levels 0-4) gives the exact
+// product of the rounded operands for the Hellmann-Feynman products.
 //
 // Tensor cores: tcgen05.mma kind::f16 (bf16 digits, FP32 accumulators in
 // tensor memory).  One CTA computes a 128 x 64 tile of Y: the MMA's M = 128
