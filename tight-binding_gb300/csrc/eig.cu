@@ -416,13 +416,26 @@ __device__ inline float tri_div(float a, float b) { return __fdividef(a, b); }
 __device__ inline double tri_div(double a, double b) { return a / b; }
 
 // One thread per (matrix, row r): eigenvalue number r - b0 of r's block.
+// FP32: the matrix's d and e^2 in FP32 are staged once per CTA in shared
+// memory (2 n floats of dynamic shared memory), so the Sturm chains read them
+// without a conversion from FP64 per step (the values are the same).
 template <typename TB>
 __global__ void k_tri_bisect(const double *dd, const double *ee, double *lamloc, int *blk, int n)
 {
+    extern __shared__ float bis_s[];
     const int b = blockIdx.y;
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= n) return;
     const double *d = dd + (long)b * n, *e = ee + (long)b * n;
+    float *sd = bis_s, *se2 = bis_s + n;
+    if (sizeof(TB) == 4) {
+        for (int k = threadIdx.x; k < n; k += blockDim.x) {
+            sd[k] = (float)d[k];
+            const float ek = (float)e[k];
+            se2[k] = ek * ek;
+        }
+        __syncthreads();
+    }
+    if (r >= n) return;
     int b0, b1;
     find_block(d, e, n, r, b0, b1);
     double tnorm = 0, lo = 1e300, hi = -1e300, emax2 = 0;
@@ -470,7 +483,7 @@ __global__ void k_tri_bisect(const double *dd, const double *ee, double *lamloc,
             if (!ok) break;
             TB q[NP];
             int c[NP];
-            const TB d0 = TB(d[b0]);
+            const TB d0 = TB(sd[b0]);
 #pragma unroll
             for (int i = 0; i < NP; ++i) {
                 q[i] = d0 - m[i];
@@ -478,7 +491,7 @@ __global__ void k_tri_bisect(const double *dd, const double *ee, double *lamloc,
                 c[i] = q[i] < TB(0);
             }
             for (int k = b0 + 1; k <= b1; ++k) {
-                const TB dk = TB(d[k]), ek = TB(e[k - 1]), e2 = ek * ek;
+                const TB dk = TB(sd[k]), e2 = TB(se2[k - 1]);
 #pragma unroll
                 for (int i = 0; i < NP; ++i) {
                     q[i] = dk - m[i] - tri_div(e2, q[i]);
@@ -913,7 +926,10 @@ void eig_solve(cudaStream_t s, EigWork<T> &w, const double2 *H, const double2 *S
     int *blk = w.perm, *rank = w.perm + 2 * (long)n * B;
     {
         dim3 g(cdiv(n, 128), B);
-        NRLTB_LAUNCH(k_tri_bisect<T>, g, 128, 0, s, w.d, w.e, lamloc, blk, n);
+        const size_t bsm = sizeof(T) == 4 ? 2 * sizeof(float) * n : 0;
+        if (bsm > 48 * 1024)
+            cudaFuncSetAttribute(k_tri_bisect<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bsm);
+        NRLTB_LAUNCH(k_tri_bisect<T>, g, 128, bsm, s, w.d, w.e, lamloc, blk, n);
         NRLTB_LAUNCH(k_tri_rank, g, 128, 0, s, lamloc, rank, w.lam, n);
         cudaMemcpyAsync(eig, w.lam, sizeof(double) * n * B, cudaMemcpyDeviceToDevice, s);
     }
