@@ -141,7 +141,7 @@ __device__ __forceinline__ void um_put4(unsigned char *ph, unsigned char *pl, ui
 }
 
 template <int TB>   // 1: op(B) = B^H
-__global__ void __launch_bounds__(UM_THREADS, 2) zgemm_umma_kernel(GemmArgs<float> g)
+__global__ void __launch_bounds__(UM_THREADS, 2) zgemm_umma_kernel(GemmArgs<float> g, int va, int vb)
 {
     extern __shared__ __align__(16) unsigned char um_raw[];
     const int b = blockIdx.z;
@@ -181,27 +181,55 @@ __global__ void __launch_bounds__(UM_THREADS, 2) zgemm_umma_kernel(GemmArgs<floa
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = *tslot;
 
-    // staging maps: A row ra_r, k groups (tid >> 7) + 2u; B column rb_n, k groups
-    // rb_g + 4u (B: four consecutive k of a column are contiguous; B^H: the
+    // staging maps: A rows 2 ra_p and 2 ra_p + 1, k groups ra_g + 4u (a 16-byte
+    // load takes both rows of one k when va and the chunk is interior); B
+    // column rb_n, k groups rb_g + 4u (B: four consecutive k of a column are
+    // contiguous, two 16-byte loads when vb and the chunk is interior; B^H: the
     // threads of a warp walk consecutive columns)
-    const int ra_r = tid & (UM_BM - 1);
+    const int ra_p = tid & 63, ra_g = tid >> 6, ra_s = (ra_p >> 2) & 1;
     const int rb_n = TB ? (tid & (UM_BN - 1)) : (tid >> 2), rb_g = TB ? (tid >> 6) : (tid & 3);
-    float2 ra[16], rb[8];
+    float2 ra[16], rb[8];   // ra[8 u + 4 row + j]
     auto fetch = [&](int k0) {
-        const int m = m0 + ra_r;
-#pragma unroll
-        for (int u = 0; u < 4; ++u)
-#pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                const int k = k0 + 4 * ((tid >> 7) + 2 * u) + j;
-                bool ok = m < g.m && k < kend;
-                if (g.triA == 1) ok = ok && k <= m;
-                if (g.triA == 2) ok = ok && k >= m;
-                ra[4 * u + j] = ok ? A[m + (long)k * g.lda] : make_float2(0.f, 0.f);
-            }
-        const int n = n0 + rb_n;
+        const int mA = m0 + 2 * ra_p;
+        const bool ain = va && m0 + UM_BM <= g.m && k0 + UM_BK <= kend &&
+                         (g.triA == 0 || (g.triA == 1 && k0 + UM_BK - 1 <= m0) ||
+                          (g.triA == 2 && k0 >= m0 + UM_BM - 1));
 #pragma unroll
         for (int u = 0; u < 2; ++u)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int k = k0 + 4 * (ra_g + 4 * u) + j;
+                if (ain) {
+                    const float4 v = *reinterpret_cast<const float4 *>(A + mA + (long)k * g.lda);
+                    ra[8 * u + j] = make_float2(v.x, v.y);
+                    ra[8 * u + 4 + j] = make_float2(v.z, v.w);
+                } else {
+#pragma unroll
+                    for (int h = 0; h < 2; ++h) {
+                        const int m = mA + h;
+                        bool ok = m < g.m && k < kend;
+                        if (g.triA == 1) ok = ok && k <= m;
+                        if (g.triA == 2) ok = ok && k >= m;
+                        ra[8 * u + 4 * h + j] = ok ? A[m + (long)k * g.lda] : make_float2(0.f, 0.f);
+                    }
+                }
+            }
+        const int n = n0 + rb_n;
+        const bool bin = !TB && vb && n0 + UM_BN <= g.n && k0 + UM_BK <= kend &&
+                         (g.triB == 0 || (g.triB == 1 && k0 + UM_BK - 1 <= n0) ||
+                          (g.triB == 2 && k0 >= n0 + UM_BN - 1));
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            if (bin) {
+                const int k = k0 + 4 * (rb_g + 4 * u);
+                const float4 *q = reinterpret_cast<const float4 *>(B + k + (long)n * g.ldb);
+                const float4 v0 = q[0], v1 = q[1];
+                rb[4 * u + 0] = make_float2(v0.x, v0.y);
+                rb[4 * u + 1] = make_float2(v0.z, v0.w);
+                rb[4 * u + 2] = make_float2(v1.x, v1.y);
+                rb[4 * u + 3] = make_float2(v1.z, v1.w);
+                continue;
+            }
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
                 const int k = k0 + 4 * (rb_g + 4 * u) + j;
@@ -215,17 +243,28 @@ __global__ void __launch_bounds__(UM_THREADS, 2) zgemm_umma_kernel(GemmArgs<floa
                 }
                 rb[4 * u + j] = v;
             }
+        }
     };
     auto store = [&](unsigned char *st) {
+        // rows in the order 2 ra_p + ra_s, then the other: the eight row
+        // residues mod 8 of each eight threads keep the swizzled stores
+        // conflict-free
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            const uint32_t off = um_swz(ra_r, (tid >> 7) + 2 * u);
-            float re[4], im[4];
+        for (int u = 0; u < 2; ++u)
 #pragma unroll
-            for (int j = 0; j < 4; ++j) { re[j] = ra[4 * u + j].x; im[j] = ra[4 * u + j].y; }
-            um_put4(st, st + UM_APL, off, re);
-            um_put4(st + 2 * UM_APL, st + 3 * UM_APL, off, im);
-        }
+            for (int hh = 0; hh < 2; ++hh) {
+                const bool second = (hh ^ ra_s) != 0;
+                const uint32_t off = um_swz(2 * ra_p + (second ? 1 : 0), ra_g + 4 * u);
+                float re[4], im[4];
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const float2 v = second ? ra[8 * u + 4 + j] : ra[8 * u + j];   // register select
+                    re[j] = v.x;
+                    im[j] = v.y;
+                }
+                um_put4(st, st + UM_APL, off, re);
+                um_put4(st + 2 * UM_APL, st + 3 * UM_APL, off, im);
+            }
         unsigned char *bh = st + 4 * UM_APL, *bl = bh + UM_BPL;
 #pragma unroll
         for (int u = 0; u < 2; ++u) {
@@ -346,8 +385,12 @@ void zgemm_umma_launch(cudaStream_t s, const GemmArgs<float> &g)
     }();
     (void)attr;
     dim3 grid(cdiv(g.m, UM_BM), cdiv(g.n, UM_BN), g.batch);
-    if (g.opB) NRLTB_LAUNCH(zgemm_umma_kernel<1>, grid, UM_THREADS, UM_SMEM, s, g);
-    else NRLTB_LAUNCH(zgemm_umma_kernel<0>, grid, UM_THREADS, UM_SMEM, s, g);
+    // 16-byte loads need every element address of an even row (A) or even k (B)
+    // 16-byte aligned: an aligned base, even leading dimension and batch stride
+    const int va = ((uintptr_t)g.A % 16 == 0) && g.lda % 2 == 0 && g.sA % 2 == 0;
+    const int vb = ((uintptr_t)g.B % 16 == 0) && g.ldb % 2 == 0 && g.sB % 2 == 0;
+    if (g.opB) NRLTB_LAUNCH(zgemm_umma_kernel<1>, grid, UM_THREADS, UM_SMEM, s, g, va, vb);
+    else NRLTB_LAUNCH(zgemm_umma_kernel<0>, grid, UM_THREADS, UM_SMEM, s, g, va, vb);
 }
 
 unsigned zgemm_umma_fault(bool clear)
