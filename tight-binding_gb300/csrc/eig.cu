@@ -394,6 +394,15 @@ __global__ void k_tri_wfinal(EigWork<T> w, int i, int c)
 
 // ---------------------------------------------------------------------------
 // Tridiagonal eigenvalues: Sturm-count bisection inside each unreduced block.
+// the same from per-row split flags (split after row k) in shared memory
+__device__ inline void find_block_flags(const unsigned char *sp, int n, int r, int &b0, int &b1)
+{
+    b0 = r;
+    while (b0 > 0 && !sp[b0 - 1]) --b0;
+    b1 = r;
+    while (b1 < n - 1 && !sp[b1]) ++b1;
+}
+
 __device__ inline void find_block(const double *d, const double *e, int n, int r, int &b0, int &b1)
 {
     const double ulp = DBL_EPSILON;
@@ -416,9 +425,10 @@ __device__ inline float tri_div(float a, float b) { return __fdividef(a, b); }
 __device__ inline double tri_div(double a, double b) { return a / b; }
 
 // One thread per (matrix, row r): eigenvalue number r - b0 of r's block.
-// FP32: the matrix's d and e^2 in FP32 are staged once per CTA in shared
-// memory (2 n floats of dynamic shared memory), so the Sturm chains read them
-// without a conversion from FP64 per step (the values are the same).
+// FP32: the matrix's d and e^2 in FP32 and the split flags of find_block are
+// staged once per CTA in shared memory (2 n floats + n bytes of dynamic shared
+// memory), so the Sturm chains read them without a conversion from FP64 per
+// step and the block search needs no FP64 work (the values are the same).
 template <typename TB>
 __global__ void k_tri_bisect(const double *dd, const double *ee, double *lamloc, int *blk, int n)
 {
@@ -427,17 +437,21 @@ __global__ void k_tri_bisect(const double *dd, const double *ee, double *lamloc,
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     const double *d = dd + (long)b * n, *e = ee + (long)b * n;
     float *sd = bis_s, *se2 = bis_s + n;
+    unsigned char *ssp = (unsigned char *)(bis_s + 2 * n);
     if (sizeof(TB) == 4) {
         for (int k = threadIdx.x; k < n; k += blockDim.x) {
             sd[k] = (float)d[k];
             const float ek = (float)e[k];
             se2[k] = ek * ek;
+            // find_block's split test, once per row
+            ssp[k] = k < n - 1 && fabs(d[k] * d[k + 1]) * DBL_EPSILON * DBL_EPSILON + DBL_MIN >= e[k] * e[k];
         }
         __syncthreads();
     }
     if (r >= n) return;
     int b0, b1;
-    find_block(d, e, n, r, b0, b1);
+    if (sizeof(TB) == 4) find_block_flags(ssp, n, r, b0, b1);
+    else find_block(d, e, n, r, b0, b1);
     double tnorm = 0, lo = 1e300, hi = -1e300, emax2 = 0;
     for (int k = b0; k <= b1; ++k) {
         double off = (k > b0 ? fabs(e[k - 1]) : 0.0) + (k < b1 ? fabs(e[k]) : 0.0);
@@ -926,7 +940,7 @@ void eig_solve(cudaStream_t s, EigWork<T> &w, const double2 *H, const double2 *S
     int *blk = w.perm, *rank = w.perm + 2 * (long)n * B;
     {
         dim3 g(cdiv(n, 128), B);
-        const size_t bsm = sizeof(T) == 4 ? 2 * sizeof(float) * n : 0;
+        const size_t bsm = sizeof(T) == 4 ? 2 * sizeof(float) * n + n : 0;
         if (bsm > 48 * 1024)
             cudaFuncSetAttribute(k_tri_bisect<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bsm);
         NRLTB_LAUNCH(k_tri_bisect<T>, g, 128, bsm, s, w.d, w.e, lamloc, blk, n);

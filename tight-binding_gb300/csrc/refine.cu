@@ -135,7 +135,10 @@ __global__ void __launch_bounds__(1024) k_ref_clusters(RefineWork w, int *status
     if (tid == 0) { double m = red[0]; for (int q = 1; q < nw; ++q) m = fmax(m, red[q]); red[0] = m; }
     __syncthreads();
     hi = red[0];
-    // rank sort of the estimates (ties by index)
+    // rank sort of the estimates (ties by index); the sorted values go to a
+    // scratch copy (the first n doubles of this matrix's U, written only by the
+    // Rayleigh-Ritz step that follows) so the serial pass below streams them
+    double *srt = (double *)(w.U + (long)b * n * REF_CMAX);
     for (int j = tid; j < n; j += blockDim.x) {
         const double v = l1[j];
         int r = 0;
@@ -144,6 +147,7 @@ __global__ void __launch_bounds__(1024) k_ref_clusters(RefineWork w, int *status
             r += (u < v) || (u == v && q < j);
         }
         ord[r] = j;
+        srt[r] = v;
     }
     __syncthreads();
     if (tid == 0) {
@@ -155,7 +159,7 @@ __global__ void __launch_bounds__(1024) k_ref_clusters(RefineWork w, int *status
         const double delta = REF_DELTA_REL * span;
         int forced = 0, p0 = 0;
         for (int p = 1; p <= n; ++p) {
-            if (p < n && l1[ord[p]] - l1[ord[p - 1]] < delta) continue;
+            if (p < n && srt[p] - srt[p - 1] < delta) continue;
             int stk[64][2], sp = 0;
             stk[sp][0] = p0; stk[sp][1] = p; ++sp;
             while (sp > 0) {
@@ -169,7 +173,7 @@ __global__ void __launch_bounds__(1024) k_ref_clusters(RefineWork w, int *status
                 int cut = a + 1;
                 double best = -1.0;
                 for (int q = a + 1; q < e; ++q) {
-                    const double g = l1[ord[q]] - l1[ord[q - 1]];
+                    const double g = srt[q] - srt[q - 1];
                     if (g > best) { best = g; cut = q; }
                 }
                 if (best < 1e-7 * span) forced = 1;
