@@ -103,9 +103,21 @@ __global__ void k_ref_diag(RefineWork w, const float2 *X)
 }
 
 // ---- 2. clusters: one CTA per matrix ----------------------------------------
+// order-preserving 64-bit key of a double (not NaN; -0 and +0 share the key
+// of 0): key(u) < key(v) exactly when u < v
+__device__ __forceinline__ unsigned long long ord_key(double v)
+{
+    const long long bits = v == 0.0 ? 0ll : __double_as_longlong(v);
+    return bits >= 0 ? (unsigned long long)bits ^ 0x8000000000000000ull : ~(unsigned long long)bits;
+}
+
+// the rank sort takes its keys from shared memory up to this order
+constexpr int REF_KEYS_MAX = 24576;
+
 __global__ void __launch_bounds__(1024) k_ref_clusters(RefineWork w, int *status)
 {
     __shared__ double red[32];
+    extern __shared__ unsigned long long cl_keys[];
     const int b = blockIdx.x, n = w.n, tid = threadIdx.x, nw = blockDim.x >> 5;
     const long nb = (long)n * w.batch;
     double *l1 = w.lam + (long)b * n, *r1 = w.lam + nb + (long)b * n;
@@ -139,15 +151,31 @@ __global__ void __launch_bounds__(1024) k_ref_clusters(RefineWork w, int *status
     // scratch copy (the first n doubles of this matrix's U, written only by the
     // Rayleigh-Ritz step that follows) so the serial pass below streams them
     double *srt = (double *)(w.U + (long)b * n * REF_CMAX);
-    for (int j = tid; j < n; j += blockDim.x) {
-        const double v = l1[j];
-        int r = 0;
-        for (int q = 0; q < n; ++q) {
-            const double u = l1[q];
-            r += (u < v) || (u == v && q < j);
+    if (n <= REF_KEYS_MAX) {
+        // integer keys in shared memory: the n^2 comparisons stay off the FP64 pipe
+        for (int j = tid; j < n; j += blockDim.x) cl_keys[j] = ord_key(l1[j]);
+        __syncthreads();
+        for (int j = tid; j < n; j += blockDim.x) {
+            const unsigned long long kv = cl_keys[j];
+            int r = 0;
+            for (int q = 0; q < n; ++q) {
+                const unsigned long long ku = cl_keys[q];
+                r += (ku < kv) || (ku == kv && q < j);
+            }
+            ord[r] = j;
+            srt[r] = l1[j];
         }
-        ord[r] = j;
-        srt[r] = v;
+    } else {
+        for (int j = tid; j < n; j += blockDim.x) {
+            const double v = l1[j];
+            int r = 0;
+            for (int q = 0; q < n; ++q) {
+                const double u = l1[q];
+                r += (u < v) || (u == v && q < j);
+            }
+            ord[r] = j;
+            srt[r] = v;
+        }
     }
     __syncthreads();
     if (tid == 0) {
@@ -490,7 +518,9 @@ void refine_eigen(cudaStream_t s, RefineWork &w, const double2 *H, const double2
     zgemm<float>(s, n, n, n, B, onef, w.Xr, n, nn, 0, w.Ef, n, nn, 0, zerof, w.G, n, nn);
     NRLTB_LAUNCH(k_ref_diag, cdiv((long)n * B * 32, 256), 256, 0, s, w, X);
     // 2. clusters and their Rayleigh-Ritz rotations
-    NRLTB_LAUNCH(k_ref_clusters, B, 1024, 0, s, w, status);
+    const size_t csm = n <= REF_KEYS_MAX ? sizeof(unsigned long long) * n : 0;
+    if (csm > 48 * 1024) cudaFuncSetAttribute(k_ref_clusters, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)csm);
+    NRLTB_LAUNCH(k_ref_clusters, B, 1024, csm, s, w, status);
     NRLTB_LAUNCH(k_ref_rr, dim3(n, B), REF_CMAX * REF_CMAX, 0, s, w, X);
     // 3. correction matrix and second-order eigenvalues (YS is free: it holds them)
     double *l2 = (double *)w.YS;
