@@ -333,11 +333,14 @@ int nrltb_skin_info(const nrltb_skin *s, int *mode, double *tkb, double *eigcut,
 
 int nrltb_skin_error_line(const nrltb_skin *s) { return s ? s->errline : 0; }
 
-/* setlat.f:147-1000 for the lattice types 0, 1-5 and 7 (and their volume forms) */
+/* setlat.f:147-1000: lattice types 0-16 (and their volume forms, latnum < 0)
+ * and the elastic strain options 0, 1, +-2, +-21, +-3, 4, 5, 6.  alat[i][j]
+ * is the jth Cartesian component of the ith primitive vector (setlat.f's
+ * alat(i,j)). */
 static int read_setlat(lreader *r, double alat[3][3], double *vol)
 {
     long latnum = 0;
-    double a, b, c, v[9];
+    double a, b, c, v[9], theta, cellv;
     double scale[3] = {1, 1, 1};
     memset(alat, 0, sizeof(double) * 9);
     if (ld_ints(r, 1, &latnum)) return NRLTB_E_PARSE;
@@ -379,22 +382,150 @@ static int read_setlat(lreader *r, double alat[3][3], double *vol)
         else { a = pow(fabs(v[0]) / fabs(v[1]), third); c = v[1] * a; }
         alat[0][0] = a; alat[1][1] = a; alat[2][2] = c;
         break;
+    case 6:   /* body-centered tetragonal (setlat.f:347-371) */
+        if (ld_reals(r, 2, v)) return NRLTB_E_PARSE;
+        if (latnum > 0) { a = v[0]; c = v[1]; }
+        else { a = pow(2.0 * fabs(v[0]) / fabs(v[1]), third); c = v[1] * a; }
+        alat[0][0] = a; alat[1][1] = a;
+        alat[2][0] = half * a; alat[2][1] = half * a; alat[2][2] = half * c;
+        break;
     case 7:
         if (ld_reals(r, 3, v)) return NRLTB_E_PARSE;
         if (latnum > 0) { a = v[0]; b = v[1]; c = v[2]; }
         else { a = pow(fabs(v[0]) / fabs(v[1] * v[2]), third); b = v[1] * a; c = v[2] * a; }
         alat[0][0] = a; alat[1][1] = b; alat[2][2] = c;
         break;
+    case 8:   /* base-centered orthorhombic: (a/2, -b/2, 0), (a/2, b/2, 0), (0, 0, c) */
+        if (ld_reals(r, 3, v)) return NRLTB_E_PARSE;
+        if (latnum > 0) { a = v[0]; b = v[1]; c = v[2]; }
+        else { a = pow(fabs(2.0 * v[0]) / fabs(v[1] * v[2]), third); b = v[1] * a; c = v[2] * a; }
+        alat[0][0] = half * a; alat[1][0] = half * a;
+        alat[1][1] = half * b; alat[0][1] = -half * b;
+        alat[2][2] = c;
+        break;
+    case 9:   /* simple tetragonal with in-plane vectors along (110), (1-10) */
+    case 10:  /* face-centered tetragonal, the same in-plane vectors */
+        if (ld_reals(r, 2, v)) return NRLTB_E_PARSE;
+        if (latnum > 0) { a = v[0]; c = v[1]; }
+        else { a = pow(fabs((labs(latnum) == 9 ? 2.0 : 4.0) * v[0] / v[1]), third); c = v[1] * a; }
+        alat[0][0] = half * a; alat[0][1] = -half * a;
+        alat[1][0] = half * a; alat[1][1] = half * a;
+        if (labs(latnum) == 9) alat[2][2] = c;
+        else { alat[2][0] = half * a; alat[2][2] = half * c; }
+        break;
+    case 11:  /* fcc-like face-centered tetragonal */
+        if (ld_reals(r, 2, v)) return NRLTB_E_PARSE;
+        if (latnum > 0) { a = v[0]; c = v[1]; }
+        else { a = pow(4.0 * fabs(v[0]) / fabs(v[1]), third); c = v[1] * a; }
+        alat[1][0] = half * a; alat[2][0] = half * a;
+        alat[0][1] = half * a; alat[2][1] = half * a;
+        alat[0][2] = half * c; alat[1][2] = half * c;
+        break;
+    case 12:  /* rhombohedral (a, b, b), (b, a, b), (b, b, a); or V and the angle */
+        if (ld_reals(r, 2, v)) return NRLTB_E_PARSE;
+        if (latnum > 0) { a = v[0]; b = v[1]; }
+        else {
+            const double ct = cos(v[1]);   /* cosine of the angle between the vectors */
+            if (ct < -half) return NRLTB_E_PARSE;   /* setlat.f stops: angle too large */
+            const double bo = third * (sqrt((1.0 + 2.0 * ct) / (1.0 - ct)) - 1.0);
+            c = pow(fabs(v[0]) / (1.0 + 3.0 * bo), third);
+            a = c * (1.0 + bo);
+            b = c * bo;
+        }
+        for (int i = 0; i < 3; ++i) for (int j = 0; j < 3; ++j) alat[j][i] = (i == j) ? a : b;
+        break;
+    case 13:  /* bcc-like body-centered tetragonal */
+        if (ld_reals(r, 2, v)) return NRLTB_E_PARSE;
+        if (latnum > 0) { a = v[0]; c = v[1]; }
+        else { a = pow(2.0 * fabs(v[0]) / fabs(v[1]), third); c = v[1] * a; }
+        alat[0][0] = -half * a; alat[0][1] = half * a; alat[0][2] = half * c;
+        alat[1][0] = half * a; alat[1][1] = -half * a; alat[1][2] = half * c;
+        alat[2][0] = half * a; alat[2][1] = half * a; alat[2][2] = -half * c;
+        break;
+    case 14:  /* base-centered orthorhombic from a, c and the in-plane angle */
+        if (ld_reals(r, 3, v)) return NRLTB_E_PARSE;
+        theta = v[2];
+        if (latnum > 0) { a = v[0]; c = v[1]; }
+        else { a = pow(v[0] / (v[1] * sin(theta)), third); c = a * v[1]; }
+        theta = half * theta;
+        alat[0][0] = a * cos(theta); alat[0][1] = -a * sin(theta);
+        alat[1][0] = alat[0][0]; alat[1][1] = -alat[0][1];
+        alat[2][2] = c;
+        break;
+    case 15:  /* "magic strain" lattices around fcc: w (0, y, z), (x, 0, z), (x, y, 0) */
+    case 16:  /* ... around bcc: w (-x, y, z), (x, -y, z), (x, y, -z) */
+    {
+        if (ld_reals(r, 3, v)) return NRLTB_E_PARSE;
+        const int fcc_based = labs(latnum) == 15;
+        const double rm = v[1], tpi3 = 2.0 * 3.14159265358979323846 / 3.0;
+        theta = v[2];
+        if (latnum > 0) cellv = (fcc_based ? half : 0.25) * v[0] * v[0] * v[0];   /* from a_bcc or a_fcc */
+        else cellv = v[0];
+        const double w = pow((fcc_based ? half : 0.25) * cellv, third), sg = fcc_based ? -1.0 : 1.0;
+        const double x = w * exp(sg * rm * cos(theta + tpi3)), y = w * exp(sg * rm * cos(theta - tpi3));
+        const double z = w * exp(sg * rm * cos(theta));
+        if (fcc_based) {
+            alat[0][1] = y; alat[0][2] = z;
+            alat[1][0] = x; alat[1][2] = z;
+            alat[2][0] = x; alat[2][1] = y;
+        } else {
+            alat[0][0] = -x; alat[0][1] = y; alat[0][2] = z;
+            alat[1][0] = x; alat[1][1] = -y; alat[1][2] = z;
+            alat[2][0] = x; alat[2][1] = y; alat[2][2] = -z;
+        }
+        break;
+    }
     default:
         return NRLTB_E_UNSUPPORTED;
     }
-    /* elastic strains (setlat.f:862-978): only the explicit e_i form */
+    /* elastic strains (setlat.f:862-978): the explicit e_i or one of the
+     * one-parameter menus */
     long strain = 0;
     if (ld_ints(r, 1, &strain)) return NRLTB_E_PARSE;
     if (strain != 0) {
-        double e[6];
-        if (strain != 1) return NRLTB_E_UNSUPPORTED;
-        if (ld_reals(r, 6, e)) return NRLTB_E_PARSE;
+        double e[6] = {0, 0, 0, 0, 0, 0}, x, x2;
+        switch (strain) {
+        case 1:
+            if (ld_reals(r, 6, e)) return NRLTB_E_PARSE;
+            break;
+        case 2: case -2: case 21: case -21:
+            /* volume-conserving e1 = sqrt((1+x)/(1-x)) - 1, e2 = sqrt((1-x)/(1+x)) - 1, or
+             * e1 = x, e2 = -x, e3 = x^2/(1-x^2); +-2 read x^2, +-21 read x */
+            if (ld_reals(r, 1, &x)) return NRLTB_E_PARSE;
+            if (labs(strain) == 2) { x2 = x; x = sqrt(x2); } else x2 = x * x;
+            if (strain > 0) { e[0] = sqrt((1.0 + x) / (1.0 - x)) - 1.0; e[1] = sqrt((1.0 - x) / (1.0 + x)) - 1.0; }
+            else { e[0] = x; e[1] = -x; e[2] = x2 / (1.0 - x2); }
+            break;
+        case 3: case -3:   /* read x^2 = e6^2 */
+            if (ld_reals(r, 1, &x2)) return NRLTB_E_PARSE;
+            e[5] = sqrt(x2);
+            if (strain > 0) { e[0] = sqrt(1.0 + 0.25 * x2) - 1.0; e[1] = e[0]; }
+            else e[2] = x2 / (4.0 - x2);
+            break;
+        case 4:   /* c/a changed by 1 + x at constant volume */
+            if (ld_reals(r, 1, &x)) return NRLTB_E_PARSE;
+            e[0] = pow(1.0 + x, -third) - 1.0;
+            e[1] = e[0];
+            e[2] = pow(1.0 + x, 2.0 / 3.0) - 1.0;
+            break;
+        case 5:   /* [111] strain of the Cartesian unit vectors */
+            if (ld_reals(r, 1, &x)) return NRLTB_E_PARSE;
+            e[0] = (1.0 + x) * pow(1.0 + 3.0 * x, -third) - 1.0;
+            e[1] = e[0];
+            e[2] = e[0];
+            e[3] = 2.0 * x * pow(1.0 + 3.0 * x, -third);
+            e[4] = e[3];
+            e[5] = e[4];
+            break;
+        case 6:   /* hexagonal C44 strain: e4 = x, e3 = x^2/4 (x < 0 when x^2 is entered negative) */
+            if (ld_reals(r, 1, &x2)) return NRLTB_E_PARSE;
+            x = x2 < 0 ? -sqrt(fabs(x2)) : sqrt(x2);
+            e[3] = x;
+            e[2] = 0.25 * x * x;
+            break;
+        default:
+            return NRLTB_E_PARSE;   /* setlat.f: unknown strain type */
+        }
         double est[3][3] = {{1 + e[0], half * e[5], half * e[4]},
                             {half * e[5], 1 + e[1], half * e[3]},
                             {half * e[4], half * e[3], 1 + e[2]}};
