@@ -547,9 +547,304 @@ static int read_setlat(lreader *r, double alat[3][3], double *vol)
     return NRLTB_OK;
 }
 
-/* kptin.f:66-366 for the explicit-list (-1313 file, inline list) and path
- * (999) forms.  The mesh generator path (kptgen.f) is not restated. */
-static int read_kpoints(nrltb_skin *s)
+/* ---- k-point mesh generator (kptin.f:90-150, rdspgp.f, kptgen.f, mapk.f,
+ * gdot.f, hsort.f, matmlt.f).  Matrices are kept with the Fortran indices:
+ * m[i][j] is M(i+1, j+1); sums run in the Fortran routines' order. */
+static const double KG_TPI = 2.0 * 3.14159265358979323846;
+
+/* C = A B in matmlt.f's order: c(i,k) = a(i,j) b(j,k) + c(i,k), j ascending */
+static void kg_matmlt(const double a[3][3], const double b[3][3], double c[3][3])
+{
+    for (int i = 0; i < 3; ++i) for (int k = 0; k < 3; ++k) c[i][k] = 0.0;
+    for (int k = 0; k < 3; ++k)
+        for (int j = 0; j < 3; ++j) {
+            const double sv = b[j][k];
+            for (int i = 0; i < 3; ++i) c[i][k] = a[i][j] * sv + c[i][k];
+        }
+}
+
+/* gdot.f: a^T G b, inner sum over i first */
+static double kg_gdot(const double a[3], const double b[3], const double g[3][3])
+{
+    double d = 0.0;
+    for (int j = 0; j < 3; ++j) {
+        double sum = 0.0;
+        for (int i = 0; i < 3; ++i) sum = sum + a[i] * g[i][j];
+        d = d + sum * b[j];
+    }
+    return d;
+}
+
+/* hsort.f: heap sort of a[0..n-1] into the index list ind (1-based values) */
+static void kg_hsort(int n, const double *a, int *ind)
+{
+    for (int j = 1; j <= n; ++j) ind[j - 1] = j;
+    if (n <= 1) return;
+    int l = n / 2 + 1, ir = n, indxt;
+    double q;
+    for (;;) {
+        if (l > 1) {
+            l = l - 1;
+            indxt = ind[l - 1];
+            q = a[indxt - 1];
+        } else {
+            indxt = ind[ir - 1];
+            q = a[indxt - 1];
+            ind[ir - 1] = ind[0];
+            ir = ir - 1;
+            if (ir == 1) { ind[0] = indxt; return; }
+        }
+        int i = l, j = l + l;
+        while (j <= ir) {
+            if (j < ir && a[ind[j - 1] - 1] < a[ind[j] - 1]) j = j + 1;
+            if (q < a[ind[j - 1] - 1]) {
+                ind[i - 1] = ind[j - 1];
+                i = j;
+                j = j + j;
+            } else {
+                j = ir + 1;
+            }
+        }
+        ind[i - 1] = indxt;
+    }
+}
+
+/* kptin.f:94-136: AVEC(I,J) = PLV(J,I), the reciprocal vectors BVEC (column j
+ * = b_j) and the metric BIJ; returns the cell volume |A . B| */
+static double kg_recip(const double plv[3][3], double avec[3][3], double bvec[3][3], double bij[3][3])
+{
+    double A[9], B[9];
+    int l = 0;
+    for (int j = 0; j < 3; ++j)
+        for (int i = 0; i < 3; ++i) { avec[i][j] = plv[j][i]; A[l++] = avec[i][j]; }
+    B[0] = A[4] * A[8] - A[5] * A[7];
+    B[1] = A[5] * A[6] - A[3] * A[8];
+    B[2] = A[3] * A[7] - A[4] * A[6];
+    B[3] = A[7] * A[2] - A[8] * A[1];
+    B[4] = A[8] * A[0] - A[6] * A[2];
+    B[5] = A[6] * A[1] - A[7] * A[0];
+    B[6] = A[1] * A[5] - A[2] * A[4];
+    B[7] = A[2] * A[3] - A[0] * A[5];
+    B[8] = A[0] * A[4] - A[1] * A[3];
+    double ws = A[0] * B[0] + A[1] * B[1] + A[2] * B[2];
+    const double pre = KG_TPI / ws;
+    l = 0;
+    for (int j = 0; j < 3; ++j)
+        for (int i = 0; i < 3; ++i) bvec[i][j] = pre * B[l++];
+    for (int i = 0; i < 3; ++i) for (int j = 0; j < 3; ++j) bij[j][i] = 0.0;
+    for (int j = 0; j < 3; ++j)
+        for (int i = 0; i < 3; ++i)
+            for (int k = 0; k < 3; ++k) bij[i][j] = bvec[k][i] * bvec[k][j] + bij[i][j];
+    return fabs(ws);
+}
+
+/* rdspgp.f: the space group's rotations in reciprocal-lattice coordinates
+ * (RSPCT), from a file giving them in direct-lattice (ilat) or Cartesian
+ * coordinates; the non-primitive translations are not needed here */
+static int kg_spacegroup(const char *path, int ilat, int lattic, const double avec[3][3], const double bvec[3][3],
+                         int *nop, double (**rspct)[3][3])
+{
+    lreader g;
+    if (lr_open(&g, path)) return NRLTB_E_IO;
+    int rc = NRLTB_OK;
+    char fld[64];
+    double (*rc_t)[3][3] = NULL;
+    if (lr_next(&g)) { rc = NRLTB_E_PARSE; goto out; }
+    long n;
+    field(g.buf, 10, 5, fld);                        /* (A10,I5,5X,3F10.5) */
+    if (fmt_int(fld, 1, &n) || n <= 0) { rc = NRLTB_E_PARSE; goto out; }
+    double (*rspc)[3][3] = malloc(sizeof(double) * 9 * n);
+    rc_t = malloc(sizeof(double) * 9 * n);
+    const double tpiinv = 1.0 / KG_TPI;
+    double t[3][3], tinv[3][3], work[3][3];
+    if (ilat) {
+        /* (18F4.0): (((RSPDIR(I,J,K),J=1,3),I=1,3),K=1,NOP); RSPC = TINV RSPDIR T */
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) { t[i][j] = bvec[j][i] * tpiinv; tinv[i][j] = avec[i][j]; }
+        long got = 0, tot = 9 * n;
+        double *dir = malloc(sizeof(double) * tot);
+        while (got < tot) {
+            if (lr_next(&g)) { free(dir); free(rspc); rc = NRLTB_E_PARSE; goto out; }
+            for (int f = 0; f < 18 && got < tot; ++f) {
+                field(g.buf, 4 * f, 4, fld);
+                if (fmt_real(fld, 0, 1, &dir[got])) { free(dir); free(rspc); rc = NRLTB_E_PARSE; goto out; }
+                ++got;
+            }
+        }
+        for (long k = 0; k < n; ++k) {
+            double rd[3][3];
+            for (int i = 0; i < 3; ++i) for (int j = 0; j < 3; ++j) rd[i][j] = dir[9 * k + 3 * i + j];
+            kg_matmlt(rd, t, work);
+            kg_matmlt(tinv, work, rspc[k]);
+        }
+        free(dir);
+    } else {
+        /* (3D20.10) per row: ((RSPC(I,J,K),J=1,3),I=1,3) */
+        for (long k = 0; k < n; ++k)
+            for (int i = 0; i < 3; ++i) {
+                if (lr_next(&g)) { free(rspc); rc = NRLTB_E_PARSE; goto out; }
+                for (int j = 0; j < 3; ++j) {
+                    field(g.buf, 20 * j, 20, fld);
+                    if (fmt_real(fld, 10, 1, &rspc[k][i][j])) { free(rspc); rc = NRLTB_E_PARSE; goto out; }
+                }
+            }
+        if (lattic == 4) {   /* hexagonal: snap +-sqrt(3)/2 */
+            const double c32 = sqrt(3.0) / 2.0;
+            for (long k = 0; k < n; ++k)
+                for (int i = 0; i < 3; ++i)
+                    for (int j = 0; j < 3; ++j) {
+                        if (fabs(rspc[k][i][j] - c32) < 0.001) rspc[k][i][j] = c32;
+                        if (fabs(rspc[k][i][j] + c32) < 0.001) rspc[k][i][j] = -c32;
+                    }
+        }
+    }
+    /* RSPCT = T RSPC TINV with T(I,J) = AVEC(J,I)/2pi, TINV = BVEC */
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) { t[i][j] = avec[j][i] / KG_TPI; tinv[i][j] = bvec[i][j]; }
+    for (long k = 0; k < n; ++k) {
+        kg_matmlt(rspc[k], tinv, work);
+        kg_matmlt(t, work, rc_t[k]);
+    }
+    free(rspc);
+    *nop = (int)n;
+    *rspct = rc_t;
+    rc_t = NULL;
+out:
+    free(rc_t);
+    lr_close(&g);
+    return rc;
+}
+
+/* kptgen.f: the mesh of kdiv divisions (special points when lspec) reduced to
+ * the irreducible wedge: points shifted to the Wigner-Seitz cell, sorted by
+ * |k| (hsort), grouped in shells of radius within 1e-4, each merged with an
+ * earlier point of its shell that a rotation (plus a reciprocal lattice
+ * vector, or the time reversal k -> -k) maps onto it.  Returns the
+ * irreducible points (reciprocal-lattice coordinates) and weights. */
+static int kg_generate(const double plv[3][3], int lattic, int nop, double (*rspct)[3][3], int lspec,
+                       const long kpdiv[3], double **q_out, double **w_out, int *nk_out)
+{
+    double avec[3][3], bvec[3][3], bij[3][3];
+    const double wsvol = kg_recip(plv, avec, bvec, bij);
+    const int lbcc = lattic == 2, lhex = lattic == 4, ltet = lattic == 7 || lattic == 8 || lattic == 9;
+    double alat = 0.0;
+    if (lbcc) {   /* bcc: the mesh of the simple cubic cell */
+        alat = pow(2.0 * wsvol, 0.33333333333333333);
+        alat = 2.0 * KG_TPI / alat;
+    }
+    long kdiv1 = kpdiv[0], kdiv2 = kpdiv[1], kdiv3 = kpdiv[2], max1, max2, max3;
+    if (kdiv1 <= 0 || kdiv2 <= 0 || kdiv3 <= 0) return NRLTB_E_PARSE;
+    if (ltet) { kdiv1 = 2 * kdiv1; kdiv2 = 2 * kdiv2; }
+    if (lspec) {
+        if (lhex) {
+            max1 = kdiv1 + kdiv1 % 2;
+            max2 = max1;
+            if (kdiv1 != kdiv2) return NRLTB_E_PARSE;   /* kptgen.f stops: KDIV error for hex */
+        } else {
+            max1 = kdiv1 + 1;
+            max2 = kdiv2 + 1;
+        }
+        max3 = kdiv3 + 1;
+    } else {
+        max1 = kdiv1; max2 = kdiv2; max3 = kdiv3;
+    }
+    const long cnt = (max1 + 1) * (max2 + 1) * (max3 + 1);
+    double *rk = malloc(sizeof(double) * 3 * cnt), *rad = malloc(sizeof(double) * cnt);
+    char *lin = malloc(cnt);
+    int *index = malloc(sizeof(int) * cnt), *ist = malloc(sizeof(int) * (cnt + 2));
+    const double f1 = 0.5 / (double)kdiv1, f2 = 0.5 / (double)kdiv2, f3 = 0.5 / (double)kdiv3;
+    const double tpiinv = 1.0 / KG_TPI;
+    long nk = 0, kin = 0;
+    for (long ii = -max1; ii <= max1; ii += 2)
+        for (long jj = -max2; jj <= max2; jj += 2)
+            for (long kk = -max3; kk <= max3; kk += 2) {
+                double uk[3] = {f1 * (double)ii, f2 * (double)jj, f3 * (double)kk}, u[3];
+                if (lattic == 7 || lattic == 8 || lattic == 9) {
+                    uk[0] = (double)ii / (double)kdiv1;
+                    uk[1] = (double)jj / (double)kdiv2;
+                    if (lattic == 7) uk[2] = uk[2] + 0.5 * (uk[0] - uk[1]);
+                    else if (lattic == 8) uk[2] = uk[2] + 0.5 * uk[0];
+                    else uk[2] = uk[2] + 0.5 * (uk[0] + uk[1]);
+                }
+                u[0] = uk[0]; u[1] = uk[1]; u[2] = uk[2];
+                lin[nk] = ii <= kdiv1 && ii > -kdiv1 && jj <= kdiv2 && jj > -kdiv2 && kk <= kdiv3 && kk > -kdiv3;
+                if (lin[nk]) ++kin;
+                if (lbcc) {   /* Cartesian point -> reciprocal-lattice coordinates (mapk.f, inv = 1) */
+                    double uu[3];
+                    for (int j = 0; j < 3; ++j) uu[j] = uk[j] * alat;
+                    for (int j = 0; j < 3; ++j)
+                        u[j] = (uu[0] * avec[0][j] + uu[1] * avec[1][j] + uu[2] * avec[2][j]) * tpiinv;
+                }
+                /* the shortest equivalent vector, among shifts by -3..3 reciprocal vectors */
+                double r2 = 1e50, ut[3] = {0, 0, 0};
+                for (int i1 = -3; i1 <= 3; ++i1)
+                    for (int i2 = -3; i2 <= 3; ++i2)
+                        for (int i3 = -3; i3 <= 3; ++i3) {
+                            const double uu[3] = {u[0] + i1, u[1] + i2, u[2] + i3};
+                            const double rr = kg_gdot(uu, uu, bij);
+                            if (rr <= r2) { r2 = rr; ut[0] = uu[0]; ut[1] = uu[1]; ut[2] = uu[2]; }
+                        }
+                rk[3 * nk] = ut[0]; rk[3 * nk + 1] = ut[1]; rk[3 * nk + 2] = ut[2];
+                rad[nk] = r2;
+                ++nk;
+            }
+    kg_hsort((int)nk, rad, index);
+    double *srk = malloc(sizeof(double) * 3 * nk), *srad = malloc(sizeof(double) * nk);
+    for (long j = 0; j < nk; ++j) {
+        srad[j] = rad[index[j] - 1];
+        for (int c = 0; c < 3; ++c) srk[3 * j + c] = rk[3 * (index[j] - 1) + c];
+    }
+    const double f = 1.0 / (double)kin, toler = 1e-4;
+    double r2 = srad[0] + toler;
+    int nst = 1;
+    ist[0] = 1;
+    for (long j = 2; j <= nk; ++j)
+        if (srad[j - 1] > r2) { r2 = srad[j - 1] + toler; ist[nst++] = (int)j; }
+    ist[nst] = (int)nk + 1;
+    double *q = malloc(sizeof(double) * 3 * nk), *w = malloc(sizeof(double) * nk);
+    int novk = 0;
+    for (int sh = 0; sh < nst; ++sh) {
+        const int k1 = novk + 1;
+        for (int j = ist[sh]; j <= ist[sh + 1] - 1; ++j) {
+            int ieq = 0;
+            const double xx = srk[3 * (j - 1)], yy = srk[3 * (j - 1) + 1], zz = srk[3 * (j - 1) + 2];
+            for (int k = k1; k <= novk; ++k) {
+                const double *u = q + 3 * (k - 1);
+                for (int iox = 0; iox < nop; ++iox) {
+                    const double (*r)[3] = rspct[iox];
+                    for (int i1 = -1; i1 <= 1; ++i1) {
+                        const double x = r[0][0] * u[0] + r[0][1] * u[1] + r[0][2] * u[2] + (double)i1;
+                        for (int i2 = -1; i2 <= 1; ++i2) {
+                            const double y = r[1][0] * u[0] + r[1][1] * u[1] + r[1][2] * u[2] + (double)i2;
+                            for (int i3 = -1; i3 <= 1; ++i3) {
+                                const double z = r[2][0] * u[0] + r[2][1] * u[1] + r[2][2] * u[2] + (double)i3;
+                                if (fabs(x - xx) + fabs(y - yy) + fabs(z - zz) <= 1e-4) ieq = k;
+                                if (ieq == 0 && fabs(x + xx) + fabs(y + yy) + fabs(z + zz) <= 1e-4) ieq = k;
+                            }
+                        }
+                    }
+                }
+            }
+            const int inmesh = lin[index[j - 1] - 1];
+            if (ieq == 0) {
+                ++novk;
+                q[3 * (novk - 1)] = xx; q[3 * (novk - 1) + 1] = yy; q[3 * (novk - 1) + 2] = zz;
+                w[novk - 1] = inmesh ? f : 0.0;
+            } else if (inmesh) {
+                w[ieq - 1] = w[ieq - 1] + f;
+            }
+        }
+    }
+    free(rk); free(rad); free(lin); free(index); free(ist); free(srk); free(srad);
+    *q_out = q;
+    *w_out = w;
+    *nk_out = novk;
+    return NRLTB_OK;
+}
+
+/* kptin.f:66-366: the explicit-list (-1313 file, inline list), path (999) and
+ * generated-mesh (NKV <= 0, kptgen.f) forms */
+static int read_kpoints(nrltb_skin *s, const double plv[3][3])
 {
     lreader *r = &s->r;
     char fld[300];
@@ -558,17 +853,22 @@ static int read_kpoints(nrltb_skin *s)
     int newsym = (fld[0] == 'T' || fld[0] == 't');
     if (!newsym) return s->nk > 0 ? NRLTB_OK : NRLTB_E_PARSE;
     if (lr_next(r)) return NRLTB_E_PARSE;           /* (7x,I1) LATTIC */
+    long lattic = 0;
+    field(r->buf, 7, 1, fld);
+    if (fmt_int(fld, 1, &lattic)) return NRLTB_E_PARSE;
     if (lr_next(r)) return NRLTB_E_PARSE;           /* (A) space group file */
-    char sg[300], full[1400];
+    char sg[300], full[1400], sgpath[1400];
     field(r->buf, 0, 255, sg);
     rtrim(sg);
-    join_path(s->dir, sg, full, sizeof full);
+    join_path(s->dir, sg, sgpath, sizeof sgpath);
     {
-        FILE *f = fopen(full, "r");                  /* OPEN(25,...,STATUS='OLD') */
+        FILE *f = fopen(sgpath, "r");                /* OPEN(25,...,STATUS='OLD') */
         if (!f) return NRLTB_E_IO;
         fclose(f);
     }
     if (lr_next(r)) return NRLTB_E_PARSE;           /* (5x,L1) ILAT */
+    field(r->buf, 5, 1, fld);
+    const int ilat = (fld[0] == 'T' || fld[0] == 't');
     if (lr_next(r)) return NRLTB_E_PARSE;           /* (I5,2F10.6) NKV, SFK */
     long nkv;
     double sfk;
@@ -595,7 +895,65 @@ static int read_kpoints(nrltb_skin *s)
     }
     if (sfk <= 1e-6) sfk = 1.0;
     int rc = NRLTB_OK;
-    if (nkv <= 0) { rc = NRLTB_E_UNSUPPORTED; goto done; }
+    if (nkv <= 0) {
+        /* generated mesh: (6X,L1,8X,L1) LSPEC, LINFOK; (5I5) KPDIV1-3, KPST, KPEND */
+        if (lr_next(kio)) { rc = NRLTB_E_PARSE; goto done; }
+        field(kio->buf, 6, 1, fld);
+        const int lspec = (fld[0] == 'T' || fld[0] == 't');
+        field(kio->buf, 15, 1, fld);
+        const int linfok = (fld[0] == 'T' || fld[0] == 't');
+        if (lr_next(kio)) { rc = NRLTB_E_PARSE; goto done; }
+        long kp[5];
+        for (int i = 0; i < 5; ++i) {
+            field(kio->buf, 5 * i, 5, fld);
+            if (fmt_int(fld, 1, &kp[i])) { rc = NRLTB_E_PARSE; goto done; }
+        }
+        double avec[3][3], bvec[3][3], bij[3][3];
+        kg_recip(plv, avec, bvec, bij);
+        int nop = 0;
+        double (*rspct)[3][3] = NULL;
+        if ((rc = kg_spacegroup(sgpath, ilat, (int)lattic, avec, bvec, &nop, &rspct))) goto done;
+        double *q = NULL, *w = NULL;
+        int nk = 0;
+        rc = kg_generate(plv, (int)lattic, nop, rspct, lspec, kp, &q, &w, &nk);
+        free(rspct);
+        if (rc) goto done;
+        if (linfok) {   /* information-only points: weight 0 */
+            const long ninfo = -nkv;
+            q = realloc(q, sizeof(double) * 3 * (nk + ninfo));
+            w = realloc(w, sizeof(double) * (nk + ninfo));
+            for (long i = 0; i < ninfo; ++i) {
+                double v[3];
+                if (ld_reals(kio, 3, v)) { free(q); free(w); rc = NRLTB_E_PARSE; goto done; }
+                for (int j = 0; j < 3; ++j) q[3 * nk + j] = v[j] / sfk;
+                w[nk++] = 0.0;
+            }
+        }
+        double wsum = 0.0;
+        for (int i = 0; i < nk; ++i) wsum = wsum + w[i];
+        if (fabs(wsum - 1.0) > 1e-6) {
+            const double wi = 1.0 / wsum;
+            for (int i = 0; i < nk; ++i) w[i] = w[i] * wi;
+        }
+        long kpst = kp[3] <= 0 ? 1 : kp[3], kpend = kp[4] == 0 ? nk : kp[4];
+        if (kpst > 1 || kpend < nk) {   /* keep points KPST..KPEND, renormalised */
+            if (kpend > nk || kpst > kpend) { free(q); free(w); rc = NRLTB_E_PARSE; goto done; }
+            int m = 0;
+            wsum = 0.0;
+            for (long i = kpst; i <= kpend; ++i) {
+                w[m] = w[i - 1];
+                wsum = wsum + w[m];
+                for (int j = 0; j < 3; ++j) q[3 * m + j] = q[3 * (i - 1) + j];
+                ++m;
+            }
+            nk = m;
+            wsum = 1.0 / wsum;
+        }
+        for (int i = 0; i < nk; ++i) w[i] = w[i] * wsum;   /* kptin.f's final WGHTK*WGHTS */
+        free(s->kq); free(s->kw);
+        s->kq = q; s->kw = w; s->nk = nk;
+        goto done;
+    }
     if (nkv == 999) {
         /* path mode: segments of KD equally spaced points, weight 1 each */
         long kpdir;
@@ -742,7 +1100,7 @@ int nrltb_skin_next(nrltb_skin *s, nrltb_structure *st, nrltb_kmesh *km, char *t
     }
     free(shift);
     free(epsl);
-    rc = read_kpoints(s);
+    rc = read_kpoints(s, plv);
     if (rc) goto fail;
     memset(st, 0, sizeof *st);
     st->natoms = natoms;

@@ -62,7 +62,8 @@ def build_all(force=False, verbose=False):
     hsrc = os.path.join(HOST, "nrltb_input.c")
     ho = os.path.join(OBJ, "nrltb_input.o")
     if force or _stale(ho, [hsrc] + hdrs):
-        jobs.append(["gcc", "-std=gnu11", "-O2", "-fPIC", "-Wall", "-I", INCLUDE, "-c", hsrc, "-o", ho])
+        jobs.append(["gcc", "-std=gnu11", "-O2", "-ffp-contract=off", "-fPIC", "-Wall", "-I", INCLUDE, "-c", hsrc,
+                     "-o", ho])
     with cf.ThreadPoolExecutor(max_workers=min(8, max(1, os.cpu_count() or 1))) as ex:
         list(ex.map(_run, jobs))
     objs = [os.path.join(OBJ, s.replace(".cu", ".o")) for s in CU_SOURCES] + [ho]
