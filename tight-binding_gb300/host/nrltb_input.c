@@ -1043,7 +1043,7 @@ int nrltb_skin_next(nrltb_skin *s, nrltb_structure *st, nrltb_kmesh *km, char *t
     int *shift = calloc((size_t)natoms, sizeof(int));
     double *epsl = calloc(3 * (size_t)natoms, sizeof(double));
     if (lphonon) {
-        long nshift;
+        long nshift = 0;
         if (ld_ints(r, 1, &nshift) || nshift > natoms) { free(shift); free(epsl); goto fail; }
         for (long k = 0; k < nshift; ++k) {
             ldctx c = {r, NULL, 0};
