@@ -18,7 +18,7 @@
 extern "C" {
 #endif
 
-#define NRLTB_ABI_VERSION 1
+#define NRLTB_ABI_VERSION 2
 
 /* ---- return codes ------------------------------------------------------ */
 #define NRLTB_OK             0
@@ -82,7 +82,8 @@ typedef struct {
 } nrltb_kmesh;
 
 typedef struct {
-    int mode;              /* 3: E(T) only; 4: E(T) and P(T) (static.f modes)   */
+    int mode;              /* static.f modes: 3 E(T); 4 E(T), P(T); 1 and 2 the  */
+                           /* same plus Gillan's T -> 0 extrapolation           */
     int precision;         /* NRLTB_PREC_FP64 or NRLTB_PREC_MIXED               */
     double tkb;            /* Fermi broadening kT, Ry                           */
     double eigcut;         /* eigenvalue cutoff for the pressure sums, Ry       */
@@ -106,17 +107,26 @@ typedef struct {
 
 typedef struct {
     double efermi;         /* Fermi level, Ry                                   */
-    double e_total;        /* E(T) band energy per cell, Ry (SKENG earg1)       */
-    double pressure;       /* P(T) = -dE/dV, Ry/bohr^3 (SKENG earg2, mode 4)     */
+    double e_total;        /* E(T) band energy per cell, Ry                     */
+    double pressure;       /* P(T) = -dE/dV, Ry/bohr^3 (modes 2 and 4)          */
     double fermi_shift;    /* dE_F/dV term (bande.f:1440)                       */
     double dismin;         /* shortest pair distance (search2.f:226)            */
     int npairs, nv, nk;
     int kneigh_out;        /* search2's flag after this structure               */
     int nonphysical_k;     /* count of k with a non-PD overlap                  */
     double *eig;           /* optional out [nk][nv] ascending eigenvalues       */
-    double *deig;          /* optional out [nk][nv] dE_i/dV (mode 4)            */
-    int *ncut;             /* optional out [nk] states <= eigcut (mode 4)       */
+    double *deig;          /* optional out [nk][nv] dE_i/dV (modes 2 and 4)     */
+    int *ncut;             /* optional out [nk] states <= eigcut (modes 2, 4)   */
     int *k_status;         /* optional out [nk] NRLTB_K_*                       */
+    /* Gillan's free-energy extrapolation (bande.f:1409-1470), modes 1 and 2;
+     * 0 in modes 3 and 4 */
+    double entropy;        /* S(T), window states only (bande.f:1234)           */
+    double free_energy;    /* A(T) = E(T) - kT S(T)                             */
+    double entropy_shift;  /* -T dS/dV term (bande.f:1457), mode 2              */
+    /* bande's two outputs, as SKENG prints them (bande.f:96-123):
+     *   mode 1: E(0) = (E+A)/2, E(T)     mode 2: E(0), P(0) = P - shift/2
+     *   mode 3: E(T), 0                  mode 4: E(T), P(T)                  */
+    double earg1, earg2;
 } nrltb_result;
 
 typedef struct nrltb_ctx nrltb_ctx;

@@ -793,6 +793,8 @@ int oracle_bande(const nrltb_structure *st, const nrltb_params *par, const nrltb
 #define FB(x) (1.0 / (1.0 + exp(tkbi * (x))))
     double etol = 20.0 * tkb, efp = efermi + etol, efm = efermi - etol;
     double esum = 0, desum1 = 0, desum2 = 0, desum3 = 0, dfbsum = 0, dferm = 0;
+    double entropy = 0, dent1 = 0, dent2 = 0;
+    const int lentro = opt->mode < 3;
     const double sfac = 2.0;
     for (int k = 0; k < nk; ++k) {
         const double *e = esk + (size_t)k * nv, *de = desk + (size_t)k * nv;
@@ -807,6 +809,8 @@ int oracle_bande(const nrltb_structure *st, const nrltb_params *par, const nrltb
             } else {
                 double fbe = FB(e[i] - efermi);
                 esum = esum + ewt * fbe;
+                /* bande.f:1233-1242, 1313 */
+                if (lentro) entropy = entropy - wt * (fbe * log(fbe) + (1.0 - fbe) * log(1.0 - fbe));
                 if (lpress) {
                     double dfbe = -tkbi * FB(e[i] - efermi) * FB(-(e[i] - efermi));
                     dfbsum = dfbsum + dfbe * wt;
@@ -815,6 +819,11 @@ int oracle_bande(const nrltb_structure *st, const nrltb_params *par, const nrltb
                     desum1 = desum1 + dewt * fbe;
                     dferm = dferm + dfbe * dewt;
                     desum2 = desum2 + dfbe * ewt * de[i];
+                    if (lentro) {
+                        double con1 = dfbe * wt * (e[i] - efermi);
+                        dent1 = dent1 + con1 * de[i];
+                        dent2 = dent2 + con1;
+                    }
                 }
             }
         }
@@ -828,6 +837,22 @@ int oracle_bande(const nrltb_structure *st, const nrltb_params *par, const nrltb
         double dfermi = (fabs(dfbsum) > 1e-10) ? dferm / dfbsum : 0.0;
         res->fermi_shift = dfermi;
         res->pressure = -(desum1 + (desum2 - dfermi * desum3));
+    }
+    /* bande.f:1409-1476 */
+    res->entropy = res->free_energy = res->entropy_shift = 0;
+    res->earg1 = esum;
+    res->earg2 = lpress ? res->pressure : 0.0;
+    if (lentro) {
+        res->entropy = entropy;
+        res->free_energy = esum - tkb * entropy;
+        res->earg1 = 0.5 * (esum + res->free_energy);
+        res->earg2 = esum;
+        if (lpress) {
+            double pent = res->fermi_shift * dent2 - dent1;
+            double fpress = res->pressure - pent;
+            res->entropy_shift = pent;
+            res->earg2 = 0.5 * (res->pressure + fpress);
+        }
     }
     res->dismin = dismin;
     res->npairs = pr.npairs;

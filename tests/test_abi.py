@@ -24,7 +24,7 @@ def test_library_builds_and_exports_all_symbols():
 
 def test_abi_version_and_error_string():
     lib = abi.load_gpu()
-    assert lib.nrltb_abi_version() == 1
+    assert lib.nrltb_abi_version() == 2
     assert isinstance(lib.nrltb_last_error(), bytes)
 
 

@@ -3,8 +3,8 @@
 // One context = one CUDA device + one stream + grow-only device buffers.  The
 // per-structure path (nrltb_run) is:
 //   search2 -> setpar(+setparv) -> SK blocks -> for each k chunk:
-//     Bloch H, S -> eigensolve -> (mode 4) Bloch dH, dS -> Hellmann-Feynman
-//   -> Fermi level, E(T), P(T)
+//     Bloch H, S -> eigensolve -> (modes 2, 4) Bloch dH, dS -> Hellmann-Feynman
+//   -> Fermi level, E(T), P(T) (+ modes 1, 2: entropy S(T), E(0), P(0))
 // all on the device; the host only reads the pair count (one 16-byte copy) to
 // size the pair arrays.  There is no CPU fallback: every entry point fails with
 // NRLTB_E_NODEVICE / NRLTB_E_CUDA when the device path cannot run.
@@ -481,10 +481,11 @@ static int run_all(nrltb_ctx *c)
     if (!c->st.valid) { set_err("nothing staged"); return NRLTB_E_ARG; }
     const Staged &S = c->st;
     const nrltb_opts &o = S.opt;
-    if (!(o.mode == 3 || o.mode == 4)) { set_err("mode %d: only modes 3 and 4", o.mode); return NRLTB_E_UNSUPPORTED; }
+    if (o.mode < 1 || o.mode > 4) { set_err("mode %d: modes 1 to 4 are built", o.mode); return NRLTB_E_UNSUPPORTED; }
     if (!(o.precision == NRLTB_PREC_FP64 || o.precision == NRLTB_PREC_MIXED)) { set_err("precision"); return NRLTB_E_ARG; }
     if (S.nk < 1) { set_err("no k points"); return NRLTB_E_ARG; }
-    const int lpress = (o.mode == 4);
+    const int lpress = (o.mode == 2 || o.mode == 4);   // bande.f:726-730
+    const int lentro = (o.mode < 3);
     cudaStream_t s = c->stream;
     long long *prev = g_launch_counter;
     KTimer *prev_kt = g_ktimer;
@@ -551,6 +552,7 @@ static int run_all(nrltb_ctx *c)
         job.w = c->d_kw.as<double>();
         job.ncut = c->d_ncut.as<int>();
         job.nv = nv; job.nk = nk; job.ldk = nv; job.lpress = lpress;
+        job.lentro = lentro; job.pad = 0;
         job.tkb = o.tkb; job.zfill = S.zfill; job.tol = (o.fermi_tol > 0) ? o.fermi_tol : 1e-8;
         if ((rc = c->d_fout.ensure(sizeof(FermiOut)))) break;
         if ((rc = c->d_fjob.ensure(sizeof(FermiJob)))) break;
@@ -573,17 +575,18 @@ static int fetch(nrltb_ctx *c, nrltb_result *res)
     cudaStream_t s = c->stream;
     const Staged &S = c->st;
     const int nv = S.nv, nk = S.nk;
+    const int mode = S.opt.mode, lpress = (mode == 2 || mode == 4), lentro = (mode < 3);
     CK(cudaMemcpyAsync(&c->fout, c->d_fout.p, sizeof(FermiOut), cudaMemcpyDeviceToHost, s));
     std::vector<int> status(nk);
     CK(cudaMemcpyAsync(status.data(), c->d_status.p, sizeof(int) * nk, cudaMemcpyDeviceToHost, s));
     if (res->eig) CK(cudaMemcpyAsync(res->eig, c->d_eig.p, sizeof(double) * (size_t)nv * nk, cudaMemcpyDeviceToHost, s));
     if (res->deig) {
-        if (S.opt.mode == 4)
+        if (lpress)
             CK(cudaMemcpyAsync(res->deig, c->d_deig.p, sizeof(double) * (size_t)nv * nk, cudaMemcpyDeviceToHost, s));
         else memset(res->deig, 0, sizeof(double) * (size_t)nv * nk);
     }
     if (res->ncut) {
-        if (S.opt.mode == 4) CK(cudaMemcpyAsync(res->ncut, c->d_ncut.p, sizeof(int) * nk, cudaMemcpyDeviceToHost, s));
+        if (lpress) CK(cudaMemcpyAsync(res->ncut, c->d_ncut.p, sizeof(int) * nk, cudaMemcpyDeviceToHost, s));
         else for (int k = 0; k < nk; ++k) res->ncut[k] = nv;
     }
     CK(cudaStreamSynchronize(s));
@@ -591,6 +594,23 @@ static int fetch(nrltb_ctx *c, nrltb_result *res)
     res->e_total = c->fout.e_total;
     res->pressure = c->fout.pressure;
     res->fermi_shift = c->fout.fermi_shift;
+    // Gillan's extrapolation and bande's two outputs (bande.f:1409-1476)
+    const double esum = c->fout.e_total, press = c->fout.pressure;
+    res->entropy = res->free_energy = res->entropy_shift = 0;
+    res->earg1 = esum;
+    res->earg2 = lpress ? press : 0.0;
+    if (lentro) {
+        res->entropy = c->fout.entropy;
+        res->free_energy = esum - S.opt.tkb * c->fout.entropy;
+        res->earg1 = 0.5 * (esum + res->free_energy);
+        res->earg2 = esum;
+        if (lpress) {
+            const double pent = c->fout.fermi_shift * c->fout.dent2 - c->fout.dent1;
+            const double fpress = press - pent;
+            res->entropy_shift = pent;
+            res->earg2 = 0.5 * (press + fpress);
+        }
+    }
     res->dismin = c->dismin;
     res->npairs = c->npairs;
     res->nv = nv;
@@ -946,6 +966,7 @@ int nrltb_fermi(nrltb_ctx *c, int nv, int nk, const double *eig, const double *w
     job.eig = c->d_eig.as<double>();
     job.w = c->d_kw.as<double>();
     job.nv = nv; job.nk = nk; job.ldk = nv; job.lpress = 0;
+    job.lentro = 0; job.pad = 0;
     job.tkb = tkb; job.zfill = zfill; job.tol = tol > 0 ? tol : 1e-8;
     job.out = c->d_fout.as<FermiOut>();
     CK(cudaMemcpyAsync(c->d_fjob.p, &job, sizeof job, cudaMemcpyHostToDevice, s));

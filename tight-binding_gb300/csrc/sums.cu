@@ -6,7 +6,9 @@
 // reductions; the iteration itself is the reference's: start at the middle of
 // the band-nfill / nfill+1 edges, Newton steps clamped to the bracket, bisection
 // when dN/dmu is small, stop when |N - zfill| < tol or the bracket closes.
-// Occupations are exactly 1 below mu - 20 kT and 0 above mu + 20 kT.
+// Occupations are exactly 1 below mu - 20 kT and 0 above mu + 20 kT.  With
+// lentro (modes 1, 2) the same window also gives Gillan's entropy S(T) and its
+// two volume-derivative sums (bande.f:1189-1242).
 #include "sums.cuh"
 
 namespace nrltb {
@@ -90,7 +92,7 @@ __global__ void __launch_bounds__(1024) k_fermi_sums(FermiJob *jobs)
     // energy and pressure sums (bande.f:1162-1330)
     const double tkbi = (tkb < 1e-5) ? 1e5 : 1.0 / tkb;
     const double efp = mu + 20.0 * tkb, efm = mu - 20.0 * tkb;
-    double es = 0, d1 = 0, d2 = 0, d3 = 0, dfb = 0, dfe = 0;
+    double es = 0, d1 = 0, d2 = 0, d3 = 0, dfb = 0, dfe = 0, ent = 0, dn1 = 0, dn2 = 0;
     for (long q = tid; q < tot; q += nt) {
         const int k = (int)(q / nv), i = (int)(q % nv);
         const int lim = J.lpress ? J.ncut[k] : nv;
@@ -106,6 +108,8 @@ __global__ void __launch_bounds__(1024) k_fermi_sums(FermiJob *jobs)
             const double x = e - mu;
             const double fbe = 1.0 / (1.0 + exp(tkbi * x));
             es += ewt * fbe;
+            // Gillan entropy of the window states (bande.f:1233-1242, 1313)
+            if (J.lentro) ent -= wt * (fbe * log(fbe) + (1.0 - fbe) * log(1.0 - fbe));
             if (J.lpress) {
                 const double dfbe = -tkbi * fbe * (1.0 / (1.0 + exp(tkbi * (-x))));
                 dfb += dfbe * wt;
@@ -114,6 +118,11 @@ __global__ void __launch_bounds__(1024) k_fermi_sums(FermiJob *jobs)
                 d1 += dewt * fbe;
                 dfe += dfbe * dewt;
                 d2 += dfbe * ewt * de;
+                if (J.lentro) {
+                    const double con1 = dfbe * wt * x;
+                    dn1 += con1 * de;
+                    dn2 += con1;
+                }
             }
         }
     }
@@ -123,6 +132,11 @@ __global__ void __launch_bounds__(1024) k_fermi_sums(FermiJob *jobs)
     d3 = block_sum_d(d3, sh);
     dfb = block_sum_d(dfb, sh);
     dfe = block_sum_d(dfe, sh);
+    if (J.lentro) {
+        ent = block_sum_d(ent, sh);
+        dn1 = block_sum_d(dn1, sh);
+        dn2 = block_sum_d(dn2, sh);
+    }
     if (tid == 0) {
         FermiOut o;
         o.efermi = mu;
@@ -134,7 +148,11 @@ __global__ void __launch_bounds__(1024) k_fermi_sums(FermiJob *jobs)
             o.fermi_shift = dfermi;
             o.pressure = -(d1 + (d2 - dfermi * d3));
         }
+        o.entropy = ent;
+        o.dent1 = dn1;
+        o.dent2 = dn2;
         o.iterations = it;
+        o.pad = 0;
         J.out[0] = o;
     }
 }

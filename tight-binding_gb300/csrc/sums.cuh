@@ -6,6 +6,7 @@ namespace nrltb {
 
 struct FermiOut {
     double efermi, e_total, pressure, fermi_shift;
+    double entropy, dent1, dent2;   // Gillan sums (lentro), else 0
     int iterations, pad;
 };
 
@@ -15,6 +16,7 @@ struct FermiJob {
     const double *w;        // [nk]
     const int *ncut;        // [nk] (mode 4)
     int nv, nk, ldk, lpress;
+    int lentro, pad;        // entropy sums (modes 1, 2)
     double tkb, zfill, tol;
     FermiOut *out;
 };

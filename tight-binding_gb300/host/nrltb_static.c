@@ -55,8 +55,8 @@ int main(int argc, char **argv)
     double tkb, eigcut;
     nrltb_params par;
     nrltb_skin_info(skin, &mode, &tkb, &eigcut, &par);
-    if (mode != 3 && mode != 4) {
-        fprintf(stderr, "nrltb_static: Mode=%d is not built (modes 3 and 4 are)\n", mode);
+    if (mode < 1 || mode > 4) {
+        fprintf(stderr, "nrltb_static: Mode=%d is not built (modes 1 to 4 are)\n", mode);
         nrltb_skin_close(skin);
         return 1;
     }
@@ -115,14 +115,26 @@ int main(int argc, char **argv)
         fprintf(skout, " Temperature = %.17G\n", tkb);
         fprintf(skout, " EFermi = %.17G\n", res.efermi);
         fprintf(skout, " E(T) = %.17G\n", res.e_total);
-        if (mode == 4) {
+        if (mode < 3) {   /* bande.f:1409-1420 */
+            fprintf(skout, " S(T) = %.17G\n", res.entropy);
+            fprintf(skout, " A(T) = %.17G\n", res.free_energy);
+            fprintf(skout, " E(0) = %.17G + O[T**4]\n", res.earg1);
+        }
+        if (mode == 2 || mode == 4) {   /* bande.f:1430-1476 */
             fprintf(skout, " Fermi level shift: %.17G\n", res.fermi_shift);
             fprintf(skout, " P(T) = %.17G\n", res.pressure);
-            fprintf(skeng, "%-20.20s%12.6f%15.9f%15.9f%15.9f\n", label, st.volume, res.efermi, res.e_total,
-                    res.pressure);
-        } else {
-            fprintf(skeng, "%-20.20s%12.6f%15.9f%15.9f\n", label, st.volume, res.efermi, res.e_total);
+            if (mode == 2) {
+                fprintf(skout, " Entropy shift = %.17G\n", res.entropy_shift);
+                fprintf(skout, " P_A(T) = %.17G\n", res.pressure - res.entropy_shift);
+                fprintf(skout, " P(0) = %.17G + O[T**4]\n", res.earg2);
+            }
         }
+        /* static.f:1238-1245: E_F and bande's two outputs; mode 3 has one */
+        if (mode == 3)
+            fprintf(skeng, "%-20.20s%12.6f%15.9f%15.9f\n", label, st.volume, res.efermi, res.earg1);
+        else
+            fprintf(skeng, "%-20.20s%12.6f%15.9f%15.9f%15.9f\n", label, st.volume, res.efermi, res.earg1,
+                    res.earg2);
         fflush(skeng);
         fflush(skout);
     }

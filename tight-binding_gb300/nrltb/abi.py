@@ -70,7 +70,8 @@ class Result_(C.Structure):
                 ("fermi_shift", C.c_double), ("dismin", C.c_double), ("npairs", C.c_int),
                 ("nv", C.c_int), ("nk", C.c_int), ("kneigh_out", C.c_int),
                 ("nonphysical_k", C.c_int), ("eig", _dp), ("deig", _dp), ("ncut", _ip),
-                ("k_status", _ip)]
+                ("k_status", _ip), ("entropy", C.c_double), ("free_energy", C.c_double),
+                ("entropy_shift", C.c_double), ("earg1", C.c_double), ("earg2", C.c_double)]
 
 
 _vp = C.c_void_p

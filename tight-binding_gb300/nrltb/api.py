@@ -157,6 +157,11 @@ class Result:
     deig: np.ndarray = None
     ncut: np.ndarray = None
     k_status: np.ndarray = None
+    entropy: float = 0.0
+    free_energy: float = 0.0
+    entropy_shift: float = 0.0
+    earg1: float = 0.0
+    earg2: float = 0.0
 
 
 def new_result(nv, nk, want_eig=True, want_deig=True):
@@ -174,7 +179,9 @@ def new_result(nv, nk, want_eig=True, want_deig=True):
 
 def result_from_c(r, arrays):
     return Result(r.efermi, r.e_total, r.pressure, r.fermi_shift, r.dismin, r.npairs, r.nv,
-                  r.nk, r.kneigh_out, r.nonphysical_k, **arrays)
+                  r.nk, r.kneigh_out, r.nonphysical_k, **arrays, entropy=r.entropy,
+                  free_energy=r.free_energy, entropy_shift=r.entropy_shift, earg1=r.earg1,
+                  earg2=r.earg2)
 
 
 def new_pairs(capacity):
