@@ -721,6 +721,9 @@ out:
  * earlier point of its shell that a rotation (plus a reciprocal lattice
  * vector, or the time reversal k -> -k) maps onto it.  Returns the
  * irreducible points (reciprocal-lattice coordinates) and weights. */
+/* full-zone mesh points kg_generate accepts (about 161^3) */
+#define KG_MAX_POINTS 4194304L
+
 static int kg_generate(const double plv[3][3], int lattic, int nop, double (*rspct)[3][3], int lspec,
                        const long kpdiv[3], double **q_out, double **w_out, int *nk_out)
 {
@@ -748,10 +751,21 @@ static int kg_generate(const double plv[3][3], int lattic, int nop, double (*rsp
     } else {
         max1 = kdiv1; max2 = kdiv2; max3 = kdiv3;
     }
+    /* kptgen.f:141-145 stops when the full-zone mesh passes its array bound
+     * (2 nkd points); the bound here is KG_MAX_POINTS, checked before any work */
+    if (max1 >= KG_MAX_POINTS || max2 >= KG_MAX_POINTS || max3 >= KG_MAX_POINTS ||
+        (max1 + 1) * (max2 + 1) > KG_MAX_POINTS || (max1 + 1) * (max2 + 1) * (max3 + 1) > KG_MAX_POINTS)
+        return NRLTB_E_UNSUPPORTED;
     const long cnt = (max1 + 1) * (max2 + 1) * (max3 + 1);
     double *rk = malloc(sizeof(double) * 3 * cnt), *rad = malloc(sizeof(double) * cnt);
     char *lin = malloc(cnt);
     int *index = malloc(sizeof(int) * cnt), *ist = malloc(sizeof(int) * (cnt + 2));
+    double *srk = malloc(sizeof(double) * 3 * cnt), *srad = malloc(sizeof(double) * cnt);
+    double *q = malloc(sizeof(double) * 3 * cnt), *w = malloc(sizeof(double) * cnt);
+    if (!rk || !rad || !lin || !index || !ist || !srk || !srad || !q || !w) {
+        free(rk); free(rad); free(lin); free(index); free(ist); free(srk); free(srad); free(q); free(w);
+        return NRLTB_E_NOMEM;
+    }
     const double f1 = 0.5 / (double)kdiv1, f2 = 0.5 / (double)kdiv2, f3 = 0.5 / (double)kdiv3;
     const double tpiinv = 1.0 / KG_TPI;
     long nk = 0, kin = 0;
@@ -789,7 +803,6 @@ static int kg_generate(const double plv[3][3], int lattic, int nop, double (*rsp
                 ++nk;
             }
     kg_hsort((int)nk, rad, index);
-    double *srk = malloc(sizeof(double) * 3 * nk), *srad = malloc(sizeof(double) * nk);
     for (long j = 0; j < nk; ++j) {
         srad[j] = rad[index[j] - 1];
         for (int c = 0; c < 3; ++c) srk[3 * j + c] = rk[3 * (index[j] - 1) + c];
@@ -801,7 +814,6 @@ static int kg_generate(const double plv[3][3], int lattic, int nop, double (*rsp
     for (long j = 2; j <= nk; ++j)
         if (srad[j - 1] > r2) { r2 = srad[j - 1] + toler; ist[nst++] = (int)j; }
     ist[nst] = (int)nk + 1;
-    double *q = malloc(sizeof(double) * 3 * nk), *w = malloc(sizeof(double) * nk);
     int novk = 0;
     for (int sh = 0; sh < nst; ++sh) {
         const int k1 = novk + 1;
@@ -920,8 +932,12 @@ static int read_kpoints(nrltb_skin *s, const double plv[3][3])
         if (rc) goto done;
         if (linfok) {   /* information-only points: weight 0 */
             const long ninfo = -nkv;
-            q = realloc(q, sizeof(double) * 3 * (nk + ninfo));
-            w = realloc(w, sizeof(double) * (nk + ninfo));
+            if (ninfo > KG_MAX_POINTS) { free(q); free(w); rc = NRLTB_E_UNSUPPORTED; goto done; }
+            double *q2 = realloc(q, sizeof(double) * 3 * (nk + ninfo));
+            if (q2) q = q2;
+            double *w2 = q2 ? realloc(w, sizeof(double) * (nk + ninfo)) : NULL;
+            if (w2) w = w2;
+            if (!q2 || !w2) { free(q); free(w); rc = NRLTB_E_NOMEM; goto done; }
             for (long i = 0; i < ninfo; ++i) {
                 double v[3];
                 if (ld_reals(kio, 3, v)) { free(q); free(w); rc = NRLTB_E_PARSE; goto done; }
@@ -960,16 +976,23 @@ static int read_kpoints(nrltb_skin *s, const double plv[3][3])
         if (lr_next(kio)) { rc = NRLTB_E_PARSE; goto done; }
         field(kio->buf, 0, 5, fld);
         if (fmt_int(fld, !own, &kpdir)) { rc = NRLTB_E_PARSE; goto done; }
-        int cap = 1024, nk = 0;
+        long cap = 1024, nk = 0;
         double *q = malloc(sizeof(double) * 3 * cap), *w = malloc(sizeof(double) * cap);
+        if (!q || !w) { free(q); free(w); rc = NRLTB_E_NOMEM; goto done; }
         for (long d = 0; d < kpdir; ++d) {
             double v[7];
             if (ld_reals(kio, 7, v)) { free(q); free(w); rc = NRLTB_E_PARSE; goto done; }
+            if (!(v[0] > -1e9 && v[0] <= (double)KG_MAX_POINTS) || nk + (long)v[0] > KG_MAX_POINTS) {
+                free(q); free(w); rc = NRLTB_E_UNSUPPORTED; goto done;
+            }
             int kd = (int)v[0];
             if (nk + kd + 1 > cap) {
                 cap = 2 * (nk + kd + 1);
-                q = realloc(q, sizeof(double) * 3 * cap);
-                w = realloc(w, sizeof(double) * cap);
+                double *q2 = realloc(q, sizeof(double) * 3 * cap);
+                if (q2) q = q2;
+                double *w2 = q2 ? realloc(w, sizeof(double) * cap) : NULL;
+                if (w2) w = w2;
+                if (!q2 || !w2) { free(q); free(w); rc = NRLTB_E_NOMEM; goto done; }
             }
             double el[3];
             for (int i = 0; i < 3; ++i) el[i] = (v[4 + i] - v[1 + i]) / (double)(kd - 1);
@@ -980,11 +1003,13 @@ static int read_kpoints(nrltb_skin *s, const double plv[3][3])
                 w[nk++] = 1.0;
             }
         }
-        for (int i = 0; i < nk; ++i) w[i] = w[i] * (double)nk; /* WGHTS = NK here */
+        for (long i = 0; i < nk; ++i) w[i] = w[i] * (double)nk; /* WGHTS = NK here */
         free(s->kq); free(s->kw);
-        s->kq = q; s->kw = w; s->nk = nk;
+        s->kq = q; s->kw = w; s->nk = (int)nk;
     } else {
+        if (nkv > KG_MAX_POINTS) { rc = NRLTB_E_UNSUPPORTED; goto done; }
         double *q = malloc(sizeof(double) * 3 * nkv), *w = malloc(sizeof(double) * nkv);
+        if (!q || !w) { free(q); free(w); rc = NRLTB_E_NOMEM; goto done; }
         double wsum = 0;
         for (long i = 0; i < nkv; ++i) {
             double v[4];
