@@ -180,7 +180,8 @@ CONFIGS = {"fcc1": fcc1, "bcc32": bcc32, "fcc128": fcc128, "b2_216": b2_216}
 # ---- writers in the reference's file formats ---------------------------------
 def write_params(path, par, title="synthetic NRL parameters"):
     with open(path, "w") as f:
-        f.write("NN%05d\n" % par.nltype)
+        # first letter: N non-orthogonal, O orthogonal (S parameters read, ignored)
+        f.write("%sN%05d\n" % ("N" if par.jsover else "O", par.nltype))
         f.write(title[:79] + "\n")
         f.write("%d\n" % par.kinds)
         for i in range(par.dnn.size):
