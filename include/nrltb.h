@@ -56,6 +56,10 @@ typedef struct {
     int nd[3];             /* search box half-widths nd1..nd3 (input1.f:488)   */
     double volume;         /* cell volume, bohr^3 (setlat.f:997-1000)          */
     double zcharge;        /* electrons above the nominal valence (static.f)   */
+    const int *flip;       /* optional [natoms], jspins = 2 only: nonzero if the */
+                           /* atom's spin is flipped (input1.f:778-787 magdir 2),*/
+                           /* its density and on-site terms then take the other */
+                           /* spin's parameters (setpar.f:500-536, 806-867)      */
 } nrltb_structure;
 
 /*
@@ -71,7 +75,10 @@ typedef struct {
     const double *valence; /* [kinds] formal valence (s+p+d occupancy)          */
     const double *dnn;     /* [kinds(kinds+1)/2] cutoff radius per type, bohr   */
     const double *screenl; /* [kinds(kinds+1)/2] screening length per type      */
-    const double *param;   /* [kinds(29+68 kinds)] parameters in file order     */
+    const double *param;   /* [jspins][kinds(29+68 kinds)] parameters, file order*/
+    int jspins;            /* 1 (or 0) spin-restricted; 2 collinear spin-      */
+                           /* polarized ("M" files, input.f:157-229): one set  */
+                           /* per spin, one electron per band                 */
 } nrltb_params;
 
 /* Explicit k list in reciprocal-lattice coordinates (kptin.f -1313 path). */
@@ -113,11 +120,12 @@ typedef struct {
     double dismin;         /* shortest pair distance (search2.f:226)            */
     int npairs, nv, nk;
     int kneigh_out;        /* search2's flag after this structure               */
-    int nonphysical_k;     /* count of k with a non-PD overlap                  */
-    double *eig;           /* optional out [nk][nv] ascending eigenvalues       */
-    double *deig;          /* optional out [nk][nv] dE_i/dV (modes 2 and 4)     */
-    int *ncut;             /* optional out [nk] states <= eigcut (modes 2, 4)   */
-    int *k_status;         /* optional out [nk] NRLTB_K_*                       */
+    int nonphysical_k;     /* count of (spin, k) with a non-PD overlap          */
+    /* per-k outputs hold jspins blocks of nk rows, spin 1 first               */
+    double *eig;           /* optional out [jspins][nk][nv] ascending eigenvalues*/
+    double *deig;          /* optional out [jspins][nk][nv] dE_i/dV (modes 2, 4) */
+    int *ncut;             /* optional out [jspins][nk] states <= eigcut         */
+    int *k_status;         /* optional out [jspins][nk] NRLTB_K_*                */
     /* Gillan's free-energy extrapolation (bande.f:1409-1470), modes 1 and 2;
      * 0 in modes 3 and 4 */
     double entropy;        /* S(T), window states only (bande.f:1234)           */
@@ -127,6 +135,8 @@ typedef struct {
      *   mode 1: E(0) = (E+A)/2, E(T)     mode 2: E(0), P(0) = P - shift/2
      *   mode 3: E(T), 0                  mode 4: E(T), P(T)                  */
     double earg1, earg2;
+    double smag;           /* jspins = 2: spin-up minus spin-down electrons per */
+                           /* cell (bande.f:1336-1395), SKENG's last column; 0  */
 } nrltb_result;
 
 typedef struct nrltb_ctx nrltb_ctx;
@@ -165,6 +175,9 @@ int nrltb_run(nrltb_ctx *ctx);
 int nrltb_fetch(nrltb_ctx *ctx, nrltb_result *res);
 
 /* ---- stage entry points (one per reference routine) -------------------- */
+/* With jspins = 2 these compute spin channel 1 (jspin = 1 of setpar.f: the
+ * first parameter set, the second for flipped atoms' densities and on-site
+ * terms). */
 /* search2.f:1-240 */
 int nrltb_search2(nrltb_ctx *ctx, const nrltb_structure *st, const nrltb_params *par,
                   int kneigh_in, nrltb_pairs *out, int *kneigh_out, double *dismin);

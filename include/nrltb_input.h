@@ -25,15 +25,20 @@ int nrltb_skin_info(const nrltb_skin *s, int *mode, double *tkb, double *eigcut,
                     nrltb_params *par);
 /* Read the next structure: title, label, zcharge (static.f:938-950), input1.f,
  * setlat.f, the lattice-to-Cartesian step (static.f:1088-1103) and kptin.f.
- * Returns NRLTB_E_EOF after the last structure.  title must hold 71 chars and
- * label 21 (NUL included). */
+ * With the spin-flip flag T on the (2a1) line each atom line carries magdir
+ * and st->flip marks the atoms with magdir 2 (NULL when none is flipped); the
+ * non-collinear flags N, D, S give NRLTB_E_UNSUPPORTED.  Returns NRLTB_E_EOF
+ * after the last structure.  title must hold 71 chars and label 21 (NUL
+ * included). */
 int nrltb_skin_next(nrltb_skin *s, nrltb_structure *st, nrltb_kmesh *km,
                     char *title, char *label);
 /* Line number (1-based) of the SKIN file where the last error happened. */
 int nrltb_skin_error_line(const nrltb_skin *s);
 void nrltb_skin_close(nrltb_skin *s);
 
-/* Parameter file alone (input.f:137-359). */
+/* Parameter file alone (input.f:137-359).  A magnetic file ("M" as the header's
+ * second letter) holds one parameter set per spin: par->jspins = 2 and
+ * par->param has 2 nrltb_nparams(kinds) values. */
 typedef struct nrltb_parfile nrltb_parfile;
 int nrltb_parfile_read(const char *path, nrltb_parfile **out, nrltb_params *par);
 void nrltb_parfile_close(nrltb_parfile *p);

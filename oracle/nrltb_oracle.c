@@ -54,6 +54,8 @@ void oracle_set_lapack(void *zhpgv, void *zhpev)
 /* parameter index arithmetic (setpar.f:461, 567-578, 654-667, 852-856)    */
 /* all results are 1-based Fortran indices into param(...)                 */
 static int ip_density(int kind) { return (kind - 1) * 17 + 1; }
+/* parameters per spin set (input.f:275) */
+static int npards(int kinds) { return kinds * (29 + 68 * kinds); }
 static int ip_hop(int kinds, int jk1, int jk2)
 {
     int base = kinds * (1 + 4 * (3 * kinds + 1));
@@ -141,12 +143,25 @@ int oracle_search2(const nrltb_structure *st, const nrltb_params *par, int kneig
 }
 
 /* ---------------------------------------------------------------------- */
-/* setpar (src/setpar.f:399-884), collinear, jspin = 1, no spin flips      */
-int oracle_setpar(const nrltb_structure *st, const nrltb_params *par, const nrltb_pairs *pr,
-                  double *hop, double *over, double *paros, double *den)
+/* Spin channel js (0-based) of a parameter set: the channel's own set, and the
+ * set a flipped atom takes its density and on-site terms from (setpar.f:500-536,
+ * 806-867: jsfrm = 3 - jspin when flipos).  1-based views.                 */
+static const double *chan_params(const nrltb_params *par, int js)
+{
+    return par->param + (size_t)js * npards(par->kinds) - 1;
+}
+static const double *atom_params(const nrltb_structure *st, const nrltb_params *par, int js, int a)
+{
+    int flipped = par->jspins == 2 && st->flip && st->flip[a];
+    return chan_params(par, flipped ? 1 - js : js);
+}
+
+/* setpar (src/setpar.f:399-884), collinear, spin channel js */
+static int setpar_chan(const nrltb_structure *st, const nrltb_params *par, int js, const nrltb_pairs *pr,
+                       double *hop, double *over, double *paros, double *den)
 {
     const int kinds = par->kinds;
-    const double *P = par->param - 1; /* 1-based view */
+    const double *P = chan_params(par, js);
     const int realov = (par->nltype == 1 || par->nltype == 3);
     const int harrison = (par->nltype == 2 || par->nltype == 3);
     for (int i = 0; i < st->natoms * kinds; ++i) den[i] = 0.0;
@@ -154,12 +169,13 @@ int oracle_setpar(const nrltb_structure *st, const nrltb_params *par, const nrlt
         int iat = pr->jatm[2 * p] - 1, jat = pr->jatm[2 * p + 1] - 1;
         int k1 = pr->jkind[2 * p], k2 = pr->jkind[2 * p + 1];
         double dist = pr->dist[p], scr = pr->screen[p];
-        /* densities, setpar.f:500-536 */
-        double b = P[ip_density(k2)] * P[ip_density(k2)];
+        /* densities, setpar.f:500-536: the receiving atom's spin picks the set */
+        const double *Pi = atom_params(st, par, js, iat), *Pj = atom_params(st, par, js, jat);
+        double b = Pi[ip_density(k2)] * Pi[ip_density(k2)];
         double dent = exp(-b * dist) * scr;
         den[iat * kinds + (k2 - 1)] += dent;
         if (jat != iat) {
-            b = P[ip_density(k1)] * P[ip_density(k1)];
+            b = Pj[ip_density(k1)] * Pj[ip_density(k1)];
             dent = exp(-b * dist) * scr;
             den[jat * kinds + (k1 - 1)] += dent;
         }
@@ -206,9 +222,10 @@ int oracle_setpar(const nrltb_structure *st, const nrltb_params *par, const nrlt
             }
         }
     }
-    /* on-site terms, setpar.f:735-884 */
+    /* on-site terms, setpar.f:735-884, from the atom's own spin set */
     const double twtrd = 2.0 / 3.0;
     for (int iat = 0; iat < st->natoms; ++iat) {
+        P = atom_params(st, par, js, iat);
         int jk1 = st->kkind[iat];
         int ip = ip_density(jk1);
         double vm23 = pow(den[iat * kinds + jk1 - 1], twtrd);
@@ -231,12 +248,12 @@ int oracle_setpar(const nrltb_structure *st, const nrltb_params *par, const nrlt
     return NRLTB_OK;
 }
 
-/* setparv (src/setparv.f:426-886), collinear, jspin = 1 */
-int oracle_setparv(const nrltb_structure *st, const nrltb_params *par, const nrltb_pairs *pr,
-                   const double *den, double *dhop, double *dover, double *dparos)
+/* setparv (src/setparv.f:426-886), collinear, spin channel js */
+static int setparv_chan(const nrltb_structure *st, const nrltb_params *par, int js, const nrltb_pairs *pr,
+                        const double *den, double *dhop, double *dover, double *dparos)
 {
     const int kinds = par->kinds;
-    const double *P = par->param - 1;
+    const double *P = chan_params(par, js);
     const int realov = (par->nltype == 1 || par->nltype == 3);
     const int harrison = (par->nltype == 2 || par->nltype == 3);
     const double third = 1.0 / 3.0, twtrd = 2.0 / 3.0, threeh = 3.0 / 2.0;
@@ -247,11 +264,12 @@ int oracle_setparv(const nrltb_structure *st, const nrltb_params *par, const nrl
         int k1 = pr->jkind[2 * p], k2 = pr->jkind[2 * p + 1];
         double dist = pr->dist[p], scr = pr->screen[p], dsc = pr->dscrn[p];
         double vdist = third * dist / st->volume;
-        double b = P[ip_density(k2)] * P[ip_density(k2)];
+        const double *Pi = atom_params(st, par, js, iat), *Pj = atom_params(st, par, js, jat);
+        double b = Pi[ip_density(k2)] * Pi[ip_density(k2)];
         double dent = exp(-b * dist) * scr;
         vden[iat * kinds + k2 - 1] += (dsc - b) * dent * vdist;
         if (jat != iat) {
-            b = P[ip_density(k1)] * P[ip_density(k1)];
+            b = Pj[ip_density(k1)] * Pj[ip_density(k1)];
             dent = exp(-b * dist) * scr;
             vden[jat * kinds + k1 - 1] += (dsc - b) * dent * vdist;
         }
@@ -301,6 +319,7 @@ int oracle_setparv(const nrltb_structure *st, const nrltb_params *par, const nrl
         }
     }
     for (int iat = 0; iat < st->natoms; ++iat) {
+        P = atom_params(st, par, js, iat);
         int jk1 = st->kkind[iat];
         int ip = ip_density(jk1);
         double vm13 = pow(den[iat * kinds + jk1 - 1], third);
@@ -326,6 +345,18 @@ int oracle_setparv(const nrltb_structure *st, const nrltb_params *par, const nrl
     }
     free(vden);
     return NRLTB_OK;
+}
+
+/* The stage entry points compute spin channel 1. */
+int oracle_setpar(const nrltb_structure *st, const nrltb_params *par, const nrltb_pairs *pr,
+                  double *hop, double *over, double *paros, double *den)
+{
+    return setpar_chan(st, par, 0, pr, hop, over, paros, den);
+}
+int oracle_setparv(const nrltb_structure *st, const nrltb_params *par, const nrltb_pairs *pr,
+                   const double *den, double *dhop, double *dover, double *dparos)
+{
+    return setparv_chan(st, par, 0, pr, den, dhop, dover, dparos);
 }
 
 /* ---------------------------------------------------------------------- */
@@ -549,27 +580,37 @@ static int oracle_perturb(int n, const zc *dh, const zc *ds, const zc *z, const 
 
 /* ---------------------------------------------------------------------- */
 /* fermi (src/fermi.f:162-425); el = 2 (non-spin), eigen[k][nv] ascending   */
-double oracle_fermi(int nv, int nk, const double *eigen, const double *w, double tkb,
-                    double zfill, double tol, int *iterations)
+/* fermi.f:162-425 over nk rows of eigenvalues (spin channels stacked as
+ * rows, fermi.f's spin-then-k order), el electrons per band */
+double oracle_fermi_el(int nv, int nk, const double *eigen, const double *w, double tkb,
+                       double zfill, double tol, double el, int *iterations)
 {
-    const double nearz = 1e-5, el = 2.0;
+    const double nearz = 1e-5;
     if (tol <= 0) tol = 1e-8;
     int it = 0;
     double beta = (tkb < nearz) ? 1.0 / nearz : 1.0 / tkb;
     int nfill = (int)(zfill / el + nearz);
     int linst = fabs(zfill / el - (double)nfill) < tol;
+    /* fermi.f:197-223 reads bands nfill and nfill+1; where those lie outside
+     * the nv computed bands (nfill >= nv happens with one electron per band)
+     * the reference reads past them.  Here the indices are clamped to the
+     * computed bands and the insulator shortcut is not taken: only the
+     * starting point of the search changes. */
+    const int ilo = (nfill < nv ? nfill : nv) - 1 < 0 ? 0 : (nfill < nv ? nfill : nv) - 1;
+    const int ihi = nfill < nv - 1 ? nfill : nv - 1;
+    const int inrange = nfill >= 1 && nfill < nv;
     double muhigh = eigen[nv - 1], mulow = eigen[0];
-    double stlow = eigen[nfill - 1], sthigh = eigen[nfill < nv ? nfill : nv - 1];
+    double stlow = eigen[ilo], sthigh = eigen[ihi];
     for (int k = 0; k < nk; ++k) {
         const double *e = eigen + (size_t)k * nv;
-        if (e[nfill - 1] > stlow) stlow = e[nfill - 1];
-        if (nfill < nv && e[nfill] < sthigh) sthigh = e[nfill];
+        if (e[ilo] > stlow) stlow = e[ilo];
+        if (e[ihi] < sthigh) sthigh = e[ihi];
         for (int i = 0; i < nv; ++i) {
             if (e[i] > muhigh) muhigh = e[i];
             if (e[i] < mulow) mulow = e[i];
         }
     }
-    if (linst && (sthigh - stlow > 20.0 * tkb)) {
+    if (linst && inrange && (sthigh - stlow > 20.0 * tkb)) {
         if (iterations) *iterations = 0;
         return 0.5 * (stlow + sthigh);
     }
@@ -610,6 +651,12 @@ double oracle_fermi(int nv, int nk, const double *eigen, const double *w, double
     }
     if (iterations) *iterations = it;
     return mu;
+}
+
+double oracle_fermi(int nv, int nk, const double *eigen, const double *w, double tkb,
+                    double zfill, double tol, int *iterations)
+{
+    return oracle_fermi_el(nv, nk, eigen, w, tkb, zfill, tol, 2.0, iterations);
 }
 
 /* ---------------------------------------------------------------------- */
@@ -747,6 +794,11 @@ int oracle_bande(const nrltb_structure *st, const nrltb_params *par, const nrltb
                  const nrltb_opts *opt, nrltb_result *res, int nthreads)
 {
     if (!p_zhpgv || !p_zhpev) return NRLTB_E_ARG;
+    /* bande.f:711-730: spin channels, pressure and entropy switches */
+    const int nsp = (par->jspins == 2) ? 2 : 1;
+    if (nsp == 1 && st->flip)
+        for (int i = 0; i < st->natoms; ++i)
+            if (st->flip[i]) return NRLTB_E_ARG;   /* spin flips need two parameter sets */
     int lpress = (opt->mode == 2 || opt->mode == 4);
     int nv = 0;
     double zfill = st->zcharge;
@@ -761,45 +813,51 @@ int oracle_bande(const nrltb_structure *st, const nrltb_params *par, const nrltb
     double *hop = calloc(14 * P + 1, 8), *over = calloc(14 * P + 1, 8);
     double *paros = calloc(4 * (size_t)st->natoms, 8), *den = calloc((size_t)st->natoms * par->kinds, 8);
     double *dhop = calloc(14 * P + 1, 8), *dover = calloc(14 * P + 1, 8), *dparos = calloc(4 * (size_t)st->natoms, 8);
-    oracle_setpar(st, par, &pr, hop, over, paros, den);
-    if (lpress) oracle_setparv(st, par, &pr, den, dhop, dover, dparos);
-    int nk = km->nk;
-    double *esk = malloc(sizeof(double) * (size_t)nv * nk);
-    double *desk = calloc((size_t)nv * nk, sizeof(double));
-    int *ncut = calloc((size_t)nk, sizeof(int));
-    int *kst = calloc((size_t)nk, sizeof(int));
+    const int nk = km->nk, nrow = nsp * nk;   /* rows: spin 1's k points, then spin 2's */
+    double *esk = malloc(sizeof(double) * (size_t)nv * nrow);
+    double *desk = calloc((size_t)nv * nrow, sizeof(double));
+    double *wrow = malloc(sizeof(double) * (size_t)nrow);
+    int *ncut = calloc((size_t)nrow, sizeof(int));
+    int *kst = calloc((size_t)nrow, sizeof(int));
+    for (int r = 0; r < nrow; ++r) wrow[r] = km->w[r % nk];
     size_t np = (size_t)nv * (nv + 1) / 2;
 #ifdef _OPENMP
     if (nthreads > 0) omp_set_num_threads(nthreads);
 #endif
+    for (int js = 0; js < nsp; ++js) {   /* bande.f:816 */
+        setpar_chan(st, par, js, &pr, hop, over, paros, den);
+        if (lpress) setparv_chan(st, par, js, &pr, den, dhop, dover, dparos);
 #pragma omp parallel for schedule(dynamic, 1)
-    for (int k = 0; k < nk; ++k) {
-        zc *hp = malloc(sizeof(zc) * np), *sp = malloc(sizeof(zc) * np);
-        zc *z = lpress ? malloc(sizeof(zc) * (size_t)nv * nv) : NULL;
-        oracle_setham_packed(st, par, &pr, hop, over, paros, km->k + 3 * k, 0, hp, sp);
-        int ioverr = oracle_diag_packed(nv, lpress, par->jsover, hp, sp, esk + (size_t)k * nv, z);
-        kst[k] = ioverr ? NRLTB_K_S_NOT_PD : NRLTB_K_OK;
-        if (!ioverr && lpress) {
-            oracle_setham_packed(st, par, &pr, dhop, dover, dparos, km->k + 3 * k, 1, hp, sp);
-            if (!par->jsover) for (size_t i = 0; i < np; ++i) sp[i] = 0;
-            oracle_perturb(nv, hp, sp, z, esk + (size_t)k * nv, opt->eigcut, &ncut[k], desk + (size_t)k * nv);
+        for (int k = 0; k < nk; ++k) {
+            const int r = js * nk + k;
+            zc *hp = malloc(sizeof(zc) * np), *sp = malloc(sizeof(zc) * np);
+            zc *z = lpress ? malloc(sizeof(zc) * (size_t)nv * nv) : NULL;
+            oracle_setham_packed(st, par, &pr, hop, over, paros, km->k + 3 * k, 0, hp, sp);
+            int ioverr = oracle_diag_packed(nv, lpress, par->jsover, hp, sp, esk + (size_t)r * nv, z);
+            kst[r] = ioverr ? NRLTB_K_S_NOT_PD : NRLTB_K_OK;
+            if (!ioverr && lpress) {
+                oracle_setham_packed(st, par, &pr, dhop, dover, dparos, km->k + 3 * k, 1, hp, sp);
+                if (!par->jsover) for (size_t i = 0; i < np; ++i) sp[i] = 0;
+                oracle_perturb(nv, hp, sp, z, esk + (size_t)r * nv, opt->eigcut, &ncut[r], desk + (size_t)r * nv);
+            }
+            free(hp); free(sp); free(z);
         }
-        free(hp); free(sp); free(z);
     }
-    /* fermi.f, then the sums of bande.f:1162-1330 in the reference's k order */
+    /* fermi.f with el = sfac electrons per band (bande.f:1065-1080), then the
+     * sums of bande.f:1162-1330 in the reference's spin-then-k order */
+    const double sfac = (nsp == 2) ? 1.0 : 2.0;
     double tkb = opt->tkb;
-    double efermi = oracle_fermi(nv, nk, esk, km->w, tkb, zfill, opt->fermi_tol, NULL);
+    double efermi = oracle_fermi_el(nv, nrow, esk, wrow, tkb, zfill, opt->fermi_tol, sfac, NULL);
     double tkbi = (tkb < 1e-5) ? 1e5 : 1.0 / tkb;
 #define FB(x) (1.0 / (1.0 + exp(tkbi * (x))))
     double etol = 20.0 * tkb, efp = efermi + etol, efm = efermi - etol;
     double esum = 0, desum1 = 0, desum2 = 0, desum3 = 0, dfbsum = 0, dferm = 0;
     double entropy = 0, dent1 = 0, dent2 = 0;
     const int lentro = opt->mode < 3;
-    const double sfac = 2.0;
-    for (int k = 0; k < nk; ++k) {
-        const double *e = esk + (size_t)k * nv, *de = desk + (size_t)k * nv;
-        double wt = sfac * km->w[k];
-        int nlim = lpress ? ncut[k] : nv;
+    for (int r = 0; r < nrow; ++r) {
+        const double *e = esk + (size_t)r * nv, *de = desk + (size_t)r * nv;
+        double wt = sfac * wrow[r];
+        int nlim = lpress ? ncut[r] : nv;
         for (int i = 0; i < nlim; ++i) {
             if (!(e[i] < efp)) continue;
             double ewt = wt * e[i];
@@ -828,6 +886,22 @@ int oracle_bande(const nrltb_structure *st, const nrltb_params *par, const nrltb
             }
         }
     }
+    /* spin populations and moment, bande.f:1336-1395 (all nv states, weight
+     * without sfac, which is 1 here) */
+    double smag = 0.0;
+    if (nsp == 2) {
+        for (int js = 0; js < 2; ++js) {
+            double sptemp = 0.0;
+            for (int k = 0; k < nk; ++k) {
+                const double *e = esk + (size_t)(js * nk + k) * nv;
+                for (int i = 0; i < nv; ++i) {
+                    if (e[i] < efm) sptemp = sptemp + km->w[k];
+                    else if (e[i] < efp) sptemp = sptemp + km->w[k] * FB(e[i] - efermi);
+                }
+            }
+            smag = (js == 0) ? sptemp : smag - sptemp;
+        }
+    }
 #undef FB
     res->efermi = efermi;
     res->e_total = esum;
@@ -854,18 +928,19 @@ int oracle_bande(const nrltb_structure *st, const nrltb_params *par, const nrltb
             res->earg2 = 0.5 * (res->pressure + fpress);
         }
     }
+    res->smag = smag;
     res->dismin = dismin;
     res->npairs = pr.npairs;
     res->nv = nv;
     res->nk = nk;
     res->kneigh_out = kneigh_out;
     res->nonphysical_k = 0;
-    for (int k = 0; k < nk; ++k) res->nonphysical_k += (kst[k] != 0);
-    if (res->eig) memcpy(res->eig, esk, sizeof(double) * (size_t)nv * nk);
-    if (res->deig) memcpy(res->deig, desk, sizeof(double) * (size_t)nv * nk);
-    if (res->ncut) memcpy(res->ncut, ncut, sizeof(int) * (size_t)nk);
-    if (res->k_status) memcpy(res->k_status, kst, sizeof(int) * (size_t)nk);
-    free(esk); free(desk); free(ncut); free(kst);
+    for (int r = 0; r < nrow; ++r) res->nonphysical_k += (kst[r] != 0);
+    if (res->eig) memcpy(res->eig, esk, sizeof(double) * (size_t)nv * nrow);
+    if (res->deig) memcpy(res->deig, desk, sizeof(double) * (size_t)nv * nrow);
+    if (res->ncut) memcpy(res->ncut, ncut, sizeof(int) * (size_t)nrow);
+    if (res->k_status) memcpy(res->k_status, kst, sizeof(int) * (size_t)nrow);
+    free(esk); free(desk); free(wrow); free(ncut); free(kst);
     free(hop); free(over); free(paros); free(den); free(dhop); free(dover); free(dparos);
     free_pairs(&pr);
     return NRLTB_OK;

@@ -99,6 +99,7 @@ extern "C" int nrltb_search2_noalloc(int device, void *stream, int natoms, const
     memcpy(S.plv, plv, sizeof S.plv);
     memcpy(S.nd, nd, sizeof S.nd);
     S.volume = 0.0;
+    S.flip = nullptr;
     DevParams P;
     P.kinds = kinds;
     P.jsover = 1;
@@ -107,6 +108,7 @@ extern "C" int nrltb_search2_noalloc(int device, void *stream, int natoms, const
     P.dnn = ddnn;
     P.screenl = dscr;
     P.param = nullptr;
+    P.param_alt = nullptr;
     const int nblk = cdiv(ncand, SEARCH_BLOCK);
     k_search_eval<<<std::min(cdiv(ncand, 256), 152 * 16), 256, 0, s>>>(S, P, ncand, code, misc, dmin);
     int host_misc[6];

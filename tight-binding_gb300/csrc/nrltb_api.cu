@@ -88,7 +88,8 @@ struct DBuf {
 struct Staged {
     bool valid = false;
     int natoms = 0, kinds = 0, jsover = 1, nltype = 0, nv = 0, nk = 0;
-    std::vector<int> kkind, kbas, ksk, orb_atom;
+    int jspins = 1, anyflip = 0;   // spin channels; any atom spin-flipped
+    std::vector<int> kkind, kbas, ksk, orb_atom, flip;
     std::vector<double> posn, posq, dnn, screenl, param, valence, kq, kw;
     double plv[3][3];
     int nd[3];
@@ -104,7 +105,7 @@ struct nrltb_ctx {
     std::vector<nrltb_ctx *> workers;   // nrltb_bande_batch: one context and stream per host worker
     Staged st;
     // device inputs
-    DBuf d_kkind, d_posn, d_posq, d_kbas, d_dnn, d_screenl, d_param, d_kq, d_kw, d_ksk, d_orb;
+    DBuf d_kkind, d_posn, d_posq, d_kbas, d_dnn, d_screenl, d_param, d_kq, d_kw, d_ksk, d_orb, d_flip;
     // search2
     DBuf d_code, d_blk, d_misc;
     DBuf d_pairs;
@@ -171,9 +172,11 @@ static DevStructure dev_structure(nrltb_ctx *c)
     memcpy(S.plv, c->st.plv, sizeof S.plv);
     memcpy(S.nd, c->st.nd, sizeof S.nd);
     S.volume = c->st.volume;
+    S.flip = c->st.anyflip ? c->d_flip.as<int>() : nullptr;
     return S;
 }
-static DevParams dev_params(nrltb_ctx *c)
+// spin channel js: its own parameter set, and the other one for flipped atoms
+static DevParams dev_params(nrltb_ctx *c, int js = 0)
 {
     DevParams P;
     P.kinds = c->st.kinds;
@@ -182,7 +185,9 @@ static DevParams dev_params(nrltb_ctx *c)
     P.kbas = c->d_kbas.as<int>();
     P.dnn = c->d_dnn.as<double>();
     P.screenl = c->d_screenl.as<double>();
-    P.param = c->d_param.as<double>();
+    const size_t npards = (size_t)c->st.kinds * (29 + 68 * c->st.kinds);
+    P.param = c->d_param.as<double>() + (size_t)js * npards;
+    P.param_alt = (c->st.jspins == 2) ? c->d_param.as<double>() + (size_t)(1 - js) * npards : P.param;
     return P;
 }
 
@@ -217,6 +222,10 @@ static int check_inputs(const nrltb_structure *st, const nrltb_params *par)
         set_err("nltype %d", par->nltype);
         return NRLTB_E_ARG;
     }
+    if (par->jspins < 0 || par->jspins > 2) { set_err("jspins %d", par->jspins); return NRLTB_E_ARG; }
+    if (par->jspins != 2 && st->flip)
+        for (int i = 0; i < st->natoms; ++i)
+            if (st->flip[i]) { set_err("atom %d is spin-flipped but the parameters have one spin", i + 1); return NRLTB_E_ARG; }
     return NRLTB_OK;
 }
 
@@ -238,7 +247,12 @@ static int stage_host(nrltb_ctx *c, const nrltb_structure *st, const nrltb_param
     int nint = par->kinds * (par->kinds + 1) / 2;
     S.dnn.assign(par->dnn, par->dnn + nint);
     S.screenl.assign(par->screenl, par->screenl + nint);
-    S.param.assign(par->param, par->param + par->kinds * (29 + 68 * par->kinds));
+    S.jspins = (par->jspins == 2) ? 2 : 1;
+    S.param.assign(par->param, par->param + (size_t)S.jspins * par->kinds * (29 + 68 * par->kinds));
+    S.flip.assign(st->natoms, 0);
+    S.anyflip = 0;
+    if (st->flip && S.jspins == 2)
+        for (int i = 0; i < st->natoms; ++i) { S.flip[i] = st->flip[i] ? 1 : 0; S.anyflip |= S.flip[i]; }
     S.valence.assign(par->valence ? par->valence : nullptr, par->valence ? par->valence + par->kinds : nullptr);
     memcpy(S.plv, st->plv, sizeof S.plv);
     memcpy(S.nd, st->nd, sizeof S.nd);
@@ -261,6 +275,8 @@ static int stage_host(nrltb_ctx *c, const nrltb_structure *st, const nrltb_param
         S.nk = km->nk;
         S.kq.assign(km->k, km->k + 3 * km->nk);
         S.kw.assign(km->w, km->w + km->nk);
+        // one weight per row of the Fermi sums: every spin channel's k points
+        if (S.jspins == 2) S.kw.insert(S.kw.end(), km->w, km->w + km->nk);
     } else {
         S.nk = 0;
         S.kq.clear();
@@ -278,6 +294,7 @@ static int stage_host(nrltb_ctx *c, const nrltb_structure *st, const nrltb_param
     RET(upload(c->d_param, S.param, s));
     RET(upload(c->d_ksk, S.ksk, s));
     RET(upload(c->d_orb, S.orb_atom, s));
+    RET(upload(c->d_flip, S.flip, s));
     if (km) {
         RET(upload(c->d_kq, S.kq, s));
         RET(upload(c->d_kw, S.kw, s));
@@ -334,7 +351,7 @@ static int run_search2(nrltb_ctx *c, int kneigh_in)
     return NRLTB_OK;
 }
 
-static int run_setpar(nrltb_ctx *c, int deriv)
+static int run_setpar(nrltb_ctx *c, int deriv, int js = 0)
 {
     cudaStream_t s = c->stream;
     const Staged &S = c->st;
@@ -343,7 +360,7 @@ static int run_setpar(nrltb_ctx *c, int deriv)
     DevSK sk = sk_view(c, P, S.natoms, S.kinds);
     DevPairs pr = pairs_view(c, P);
     DevStructure DS = dev_structure(c);
-    DevParams DP = dev_params(c);
+    DevParams DP = dev_params(c, js);
     if (c->npairs > 0) NRLTB_LAUNCH(k_setpar_pairs, cdiv(c->npairs, 128), 128, 0, s, DS, DP, pr, c->npairs, sk, deriv);
     NRLTB_LAUNCH(k_setpar_atoms, cdiv((long)S.natoms * 32, 256), 256, 0, s, DS, DP, pr, c->npairs, sk, deriv);
     CKL();
@@ -495,51 +512,59 @@ static int run_all(nrltb_ctx *c)
     c->nonpd.clear();
     do {
         if ((rc = run_search2(c, o.kneigh_in))) break;
-        if ((rc = run_setpar(c, lpress))) break;
+        if ((rc = run_setpar(c, lpress, 0))) break;
         if ((rc = run_skblocks(c, lpress ? 4 : 2))) break;
-        const int nv = S.nv, nk = S.nk;
-        if ((rc = c->d_eig.ensure(sizeof(double) * (size_t)nv * nk))) break;
-        if ((rc = c->d_deig.ensure(sizeof(double) * (size_t)nv * nk))) break;
-        if ((rc = c->d_ncut.ensure(sizeof(int) * (size_t)nk))) break;
-        if ((rc = c->d_status.ensure(sizeof(int) * (size_t)nk))) break;
+        const int nv = S.nv, nk = S.nk, nsp = S.jspins, nrow = nsp * nk;
+        // per-k outputs: one block of nk rows per spin channel, spin 1 first
+        if ((rc = c->d_eig.ensure(sizeof(double) * (size_t)nv * nrow))) break;
+        if ((rc = c->d_deig.ensure(sizeof(double) * (size_t)nv * nrow))) break;
+        if ((rc = c->d_ncut.ensure(sizeof(int) * (size_t)nrow))) break;
+        if ((rc = c->d_status.ensure(sizeof(int) * (size_t)nrow))) break;
         const int chunk = choose_chunk(nv, nk, o.precision);
         const size_t nn = (size_t)nv * nv;
         if ((rc = c->d_H.ensure(sizeof(double2) * nn * chunk))) break;
         if ((rc = c->d_S.ensure(sizeof(double2) * nn * chunk))) break;
         if ((rc = c->d_X.ensure(zoff(nn, chunk) + sizeof(double2) * nn * chunk))) break;
-        for (int k0 = 0; k0 < nk && rc == NRLTB_OK; k0 += chunk) {
-            const int nkc = std::min(chunk, nk - k0);
-            double *eig = c->d_eig.as<double>() + (size_t)k0 * nv;
-            int *status = c->d_status.as<int>() + k0;
-            if ((rc = run_bloch(c, k0, nkc, 0, c->d_H.as<double2>(), c->d_S.as<double2>()))) break;
-            double2 *Z = nullptr;
-            if (lpress) {
-                // FP64 eigenvectors live after the FP32 staging area of d_X
-                Z = (double2 *)(c->d_X.as<char>() + zoff(nn, chunk));
+        for (int js = 0; js < nsp && rc == NRLTB_OK; ++js) {   // bande.f:816
+            if (js > 0) {   // the second spin channel's integrals replace the first's
+                if ((rc = run_setpar(c, lpress, js))) break;
+                if ((rc = run_skblocks(c, lpress ? 4 : 2))) break;
             }
-            if ((rc = run_solve(c, nv, nkc, o.precision, c->d_H.as<double2>(), c->d_S.as<double2>(), eig, Z, status,
-                                lpress != 0)))
-                break;
-            std::vector<int> hst(nkc), bad;
-            if (cudaMemcpyAsync(hst.data(), status, sizeof(int) * nkc, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-                cudaStreamSynchronize(s) != cudaSuccess) { set_err("status readback failed"); rc = NRLTB_E_CUDA; break; }
-            for (int k = 0; k < nkc; ++k) if (hst[k] == NRLTB_K_S_NOT_PD) bad.push_back(k);
-            if (!bad.empty()) {
-                if ((rc = fix_nonpd(c, nv, bad, c->d_S.as<double2>(), eig))) break;
-                for (int k : bad) c->nonpd.push_back(std::make_pair(k0 + k, 0));
-            }
-            if (lpress) {
-                if ((rc = run_bloch(c, k0, nkc, 2, c->d_H.as<double2>(), c->d_S.as<double2>()))) break;
-                if ((rc = c->d_hf.ensure(hf_scratch_bytes(nv, nkc)))) break;
-                if ((rc = run_hf(s, nv, nkc, o.precision, c->d_H.as<double2>(), c->d_S.as<double2>(), Z, eig,
-                                 c->d_deig.as<double>() + (size_t)k0 * nv, c->d_hf.p, nullptr)))
-                    { set_err("hf failed"); break; }
-                CKL();
+            for (int k0 = 0; k0 < nk && rc == NRLTB_OK; k0 += chunk) {
+                const int nkc = std::min(chunk, nk - k0);
+                const int r0 = js * nk + k0;   // first row of this chunk
+                double *eig = c->d_eig.as<double>() + (size_t)r0 * nv;
+                int *status = c->d_status.as<int>() + r0;
+                if ((rc = run_bloch(c, k0, nkc, 0, c->d_H.as<double2>(), c->d_S.as<double2>()))) break;
+                double2 *Z = nullptr;
+                if (lpress) {
+                    // FP64 eigenvectors live after the FP32 staging area of d_X
+                    Z = (double2 *)(c->d_X.as<char>() + zoff(nn, chunk));
+                }
+                if ((rc = run_solve(c, nv, nkc, o.precision, c->d_H.as<double2>(), c->d_S.as<double2>(), eig, Z,
+                                    status, lpress != 0)))
+                    break;
+                std::vector<int> hst(nkc), bad;
+                if (cudaMemcpyAsync(hst.data(), status, sizeof(int) * nkc, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+                    cudaStreamSynchronize(s) != cudaSuccess) { set_err("status readback failed"); rc = NRLTB_E_CUDA; break; }
+                for (int k = 0; k < nkc; ++k) if (hst[k] == NRLTB_K_S_NOT_PD) bad.push_back(k);
+                if (!bad.empty()) {
+                    if ((rc = fix_nonpd(c, nv, bad, c->d_S.as<double2>(), eig))) break;
+                    for (int k : bad) c->nonpd.push_back(std::make_pair(r0 + k, 0));
+                }
+                if (lpress) {
+                    if ((rc = run_bloch(c, k0, nkc, 2, c->d_H.as<double2>(), c->d_S.as<double2>()))) break;
+                    if ((rc = c->d_hf.ensure(hf_scratch_bytes(nv, nkc)))) break;
+                    if ((rc = run_hf(s, nv, nkc, o.precision, c->d_H.as<double2>(), c->d_S.as<double2>(), Z, eig,
+                                     c->d_deig.as<double>() + (size_t)r0 * nv, c->d_hf.p, nullptr)))
+                        { set_err("hf failed"); break; }
+                    CKL();
+                }
             }
         }
         if (rc) break;
         if (lpress) {
-            NRLTB_LAUNCH(k_ncut, cdiv(nk, 128), 128, 0, s, c->d_eig.as<double>(), nv, nv, nk, o.eigcut,
+            NRLTB_LAUNCH(k_ncut, cdiv(nrow, 128), 128, 0, s, c->d_eig.as<double>(), nv, nv, nrow, o.eigcut,
                          c->d_ncut.as<int>());
             for (auto &kc : c->nonpd) {
                 cudaMemsetAsync(c->d_ncut.as<int>() + kc.first, 0, sizeof(int), s);
@@ -551,8 +576,10 @@ static int run_all(nrltb_ctx *c)
         job.deig = c->d_deig.as<double>();
         job.w = c->d_kw.as<double>();
         job.ncut = c->d_ncut.as<int>();
-        job.nv = nv; job.nk = nk; job.ldk = nv; job.lpress = lpress;
-        job.lentro = lentro; job.pad = 0;
+        job.nv = nv; job.nk = nrow; job.ldk = nv; job.lpress = lpress;
+        job.lentro = lentro;
+        job.nks = (nsp == 2) ? nk : 0;
+        job.el = (nsp == 2) ? 1.0 : 2.0;   // electrons per band, bande.f:1065-1073
         job.tkb = o.tkb; job.zfill = S.zfill; job.tol = (o.fermi_tol > 0) ? o.fermi_tol : 1e-8;
         if ((rc = c->d_fout.ensure(sizeof(FermiOut)))) break;
         if ((rc = c->d_fjob.ensure(sizeof(FermiJob)))) break;
@@ -574,20 +601,20 @@ static int fetch(nrltb_ctx *c, nrltb_result *res)
     if (!c->ran) { set_err("nothing run"); return NRLTB_E_ARG; }
     cudaStream_t s = c->stream;
     const Staged &S = c->st;
-    const int nv = S.nv, nk = S.nk;
+    const int nv = S.nv, nk = S.nk, nrow = S.jspins * S.nk;
     const int mode = S.opt.mode, lpress = (mode == 2 || mode == 4), lentro = (mode < 3);
     CK(cudaMemcpyAsync(&c->fout, c->d_fout.p, sizeof(FermiOut), cudaMemcpyDeviceToHost, s));
-    std::vector<int> status(nk);
-    CK(cudaMemcpyAsync(status.data(), c->d_status.p, sizeof(int) * nk, cudaMemcpyDeviceToHost, s));
-    if (res->eig) CK(cudaMemcpyAsync(res->eig, c->d_eig.p, sizeof(double) * (size_t)nv * nk, cudaMemcpyDeviceToHost, s));
+    std::vector<int> status(nrow);
+    CK(cudaMemcpyAsync(status.data(), c->d_status.p, sizeof(int) * nrow, cudaMemcpyDeviceToHost, s));
+    if (res->eig) CK(cudaMemcpyAsync(res->eig, c->d_eig.p, sizeof(double) * (size_t)nv * nrow, cudaMemcpyDeviceToHost, s));
     if (res->deig) {
         if (lpress)
-            CK(cudaMemcpyAsync(res->deig, c->d_deig.p, sizeof(double) * (size_t)nv * nk, cudaMemcpyDeviceToHost, s));
-        else memset(res->deig, 0, sizeof(double) * (size_t)nv * nk);
+            CK(cudaMemcpyAsync(res->deig, c->d_deig.p, sizeof(double) * (size_t)nv * nrow, cudaMemcpyDeviceToHost, s));
+        else memset(res->deig, 0, sizeof(double) * (size_t)nv * nrow);
     }
     if (res->ncut) {
-        if (lpress) CK(cudaMemcpyAsync(res->ncut, c->d_ncut.p, sizeof(int) * nk, cudaMemcpyDeviceToHost, s));
-        else for (int k = 0; k < nk; ++k) res->ncut[k] = nv;
+        if (lpress) CK(cudaMemcpyAsync(res->ncut, c->d_ncut.p, sizeof(int) * nrow, cudaMemcpyDeviceToHost, s));
+        else for (int k = 0; k < nrow; ++k) res->ncut[k] = nv;
     }
     CK(cudaStreamSynchronize(s));
     res->efermi = c->fout.efermi;
@@ -611,15 +638,17 @@ static int fetch(nrltb_ctx *c, nrltb_result *res)
             res->earg2 = 0.5 * (press + fpress);
         }
     }
+    // magnetic moment, bande.f:1388-1392
+    res->smag = (S.jspins == 2) ? c->fout.spin_up - c->fout.spin_dn : 0.0;
     res->dismin = c->dismin;
     res->npairs = c->npairs;
     res->nv = nv;
     res->nk = nk;
     res->kneigh_out = c->kneigh_out;
     int bad = 0;
-    for (int k = 0; k < nk; ++k) bad += (status[k] == NRLTB_K_S_NOT_PD);
+    for (int k = 0; k < nrow; ++k) bad += (status[k] == NRLTB_K_S_NOT_PD);
     res->nonphysical_k = bad;
-    if (res->k_status) memcpy(res->k_status, status.data(), sizeof(int) * nk);
+    if (res->k_status) memcpy(res->k_status, status.data(), sizeof(int) * nrow);
     return NRLTB_OK;
 }
 
@@ -656,7 +685,7 @@ int nrltb_ctx_destroy(nrltb_ctx *c)
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
     DBuf *bufs[] = {&c->d_kkind, &c->d_posn, &c->d_posq, &c->d_kbas, &c->d_dnn, &c->d_screenl, &c->d_param,
-                    &c->d_kq, &c->d_kw, &c->d_ksk, &c->d_orb, &c->d_code, &c->d_blk, &c->d_misc, &c->d_pairs,
+                    &c->d_kq, &c->d_kw, &c->d_ksk, &c->d_orb, &c->d_flip, &c->d_code, &c->d_blk, &c->d_misc, &c->d_pairs,
                     &c->d_sk, &c->d_seg, &c->d_ph, &c->d_H, &c->d_S, &c->d_X, &c->d_work, &c->d_ref, &c->d_hf, &c->d_np,
                     &c->d_eig, &c->d_deig, &c->d_ncut, &c->d_status, &c->d_fjob, &c->d_fout};
     for (DBuf *b : bufs) b->release();
@@ -966,7 +995,7 @@ int nrltb_fermi(nrltb_ctx *c, int nv, int nk, const double *eig, const double *w
     job.eig = c->d_eig.as<double>();
     job.w = c->d_kw.as<double>();
     job.nv = nv; job.nk = nk; job.ldk = nv; job.lpress = 0;
-    job.lentro = 0; job.pad = 0;
+    job.lentro = 0; job.nks = 0; job.el = 2.0;
     job.tkb = tkb; job.zfill = zfill; job.tol = tol > 0 ? tol : 1e-8;
     job.out = c->d_fout.as<FermiOut>();
     CK(cudaMemcpyAsync(c->d_fjob.p, &job, sizeof job, cudaMemcpyHostToDevice, s));

@@ -219,12 +219,14 @@ __global__ void k_setpar_pairs(DevStructure S, DevParams P, DevPairs pr, int npa
     const int k1 = pr.jkind[2 * p], k2 = pr.jkind[2 * p + 1];
     const double dist = pr.dist[p], scr = pr.screen[p], dsc = pr.dscrn[p];
     const double vdist = (1.0 / 3.0) * dist / S.volume;
-    // density contributions (setpar.f:500-536, setparv.f:510-535)
-    double b2 = Pm[ip_density(k2)] * Pm[ip_density(k2)];
+    // density contributions (setpar.f:500-536, setparv.f:510-535); the
+    // receiving atom's spin picks the parameter set
+    const double *Pi = atom_params(S, P, pr.jatm[2 * p] - 1), *Pj = atom_params(S, P, pr.jatm[2 * p + 1] - 1);
+    double b2 = Pi[ip_density(k2)] * Pi[ip_density(k2)];
     double dent = exp(-b2 * dist) * scr;
     sk.dent[2 * (long)p] = dent;
     sk.vdent[2 * (long)p] = (dsc - b2) * dent * vdist;
-    double b1 = Pm[ip_density(k1)] * Pm[ip_density(k1)];
+    double b1 = Pj[ip_density(k1)] * Pj[ip_density(k1)];
     double dent1 = exp(-b1 * dist) * scr;
     sk.dent[2 * (long)p + 1] = dent1;
     sk.vdent[2 * (long)p + 1] = (dsc - b1) * dent1 * vdist;
@@ -335,7 +337,7 @@ __global__ void k_setpar_atoms(DevStructure S, DevParams P, DevPairs pr, int npa
         }
     }
     if (lane != 0) return;
-    const double *Pm = P.param - 1;
+    const double *Pm = atom_params(S, P, a);   // on-site terms from the atom's own spin set
     const int jk1 = S.kkind[a];
     for (int k = 0; k < kinds; ++k) sk.den[(long)a * kinds + k] = den[k];
     double paros[4], dparos[4];

@@ -15,13 +15,22 @@ struct DevStructure {
     double plv[3][3];
     int nd[3];
     double volume;
+    const int *flip;        // device [natoms], nonzero = spin flipped; nullptr = none
 };
 
 struct DevParams {
     int kinds, jsover, nltype;
     const int *kbas;        // device
-    const double *dnn, *screenl, *param;   // device
+    const double *dnn, *screenl, *param;   // device; param = this spin channel's set
+    const double *param_alt;               // the set flipped atoms' densities and on-site terms use
 };
+
+// parameter set (1-based view) for atom a's density and on-site terms
+// (setpar.f:500-536, 806-867: jsfrm = 3 - jspin for a flipped atom)
+__device__ __forceinline__ const double *atom_params(const DevStructure &S, const DevParams &P, int a)
+{
+    return ((S.flip && S.flip[a]) ? P.param_alt : P.param) - 1;
+}
 
 struct DevPairs {
     double *tt; int *dlv; double *dist, *screen, *dscrn; int *jkind, *jatm;

@@ -36,26 +36,30 @@ __global__ void __launch_bounds__(1024) k_fermi_sums(FermiJob *jobs)
     FermiJob J = jobs[blockIdx.x];
     const int nv = J.nv, nk = J.nk, tid = threadIdx.x, nt = blockDim.x;
     const long tot = (long)nv * nk;
-    const double el = 2.0, nearz = 1e-5, tkb = J.tkb, zfill = J.zfill, tol = J.tol;
+    const double el = J.el, nearz = 1e-5, tkb = J.tkb, zfill = J.zfill, tol = J.tol;
     const double beta = (tkb < nearz) ? 1.0 / nearz : 1.0 / tkb;
     const int nfill = (int)(zfill / el + nearz);
     const bool linst = fabs(zfill / el - (double)nfill) < tol;
-    // bounds (fermi.f:197-261)
+    // bounds (fermi.f:197-261) from bands nfill and nfill+1; where those lie
+    // outside the nv computed bands (nfill >= nv happens with one electron per
+    // band) the reference reads past them: here the band indices are clamped
+    // and the insulator shortcut is not taken, which moves only the start
+    const int ilo = max(min(nfill, nv) - 1, 0), ihi = min(nfill, nv - 1);
+    const bool inrange = nfill >= 1 && nfill < nv;
     double stl = -1e308, sth = 1e308, mul = 1e308, muh = -1e308;
     for (long q = tid; q < tot; q += nt) {
         const int k = (int)(q / nv), i = (int)(q % nv);
         const double e = J.eig[(long)k * J.ldk + i];
-        if (i == nfill - 1) stl = fmax(stl, e);
-        if (i == nfill) sth = fmin(sth, e);
+        if (i == ilo) stl = fmax(stl, e);
+        if (i == ihi) sth = fmin(sth, e);
         muh = fmax(muh, e);
         mul = fmin(mul, e);
     }
     double stlow = block_max_d(stl, sh), sthigh = -block_max_d(-sth, sh);
     double muhigh = block_max_d(muh, sh), mulow = -block_max_d(-mul, sh);
-    if (nfill >= nv) sthigh = J.eig[nv - 1];
     double mu;
     int it = 0;
-    if (linst && (sthigh - stlow > 20.0 * tkb)) {
+    if (linst && inrange && (sthigh - stlow > 20.0 * tkb)) {
         mu = 0.5 * (stlow + sthigh);
     } else {
         mu = 0.5 * (stlow + sthigh);
@@ -92,14 +96,20 @@ __global__ void __launch_bounds__(1024) k_fermi_sums(FermiJob *jobs)
     // energy and pressure sums (bande.f:1162-1330)
     const double tkbi = (tkb < 1e-5) ? 1e5 : 1.0 / tkb;
     const double efp = mu + 20.0 * tkb, efm = mu - 20.0 * tkb;
-    double es = 0, d1 = 0, d2 = 0, d3 = 0, dfb = 0, dfe = 0, ent = 0, dn1 = 0, dn2 = 0;
+    double es = 0, d1 = 0, d2 = 0, d3 = 0, dfb = 0, dfe = 0, ent = 0, dn1 = 0, dn2 = 0, sup = 0, sdn = 0;
     for (long q = tid; q < tot; q += nt) {
         const int k = (int)(q / nv), i = (int)(q % nv);
+        const double e = J.eig[(long)k * J.ldk + i];
+        // spin populations over all nv states (bande.f:1336-1395), weight w(k)
+        if (J.nks > 0 && e < efp) {
+            const double occ = (e < efm) ? J.w[k] : J.w[k] * (1.0 / (1.0 + exp(tkbi * (e - mu))));
+            if (k < J.nks) sup += occ;
+            else sdn += occ;
+        }
         const int lim = J.lpress ? J.ncut[k] : nv;
         if (i >= lim) continue;
-        const double e = J.eig[(long)k * J.ldk + i];
         if (!(e < efp)) continue;
-        const double wt = 2.0 * J.w[k], ewt = wt * e;
+        const double wt = J.el * J.w[k], ewt = wt * e;
         const double de = J.lpress ? J.deig[(long)k * J.ldk + i] : 0.0;
         if (e < efm) {
             es += ewt;
@@ -137,6 +147,10 @@ __global__ void __launch_bounds__(1024) k_fermi_sums(FermiJob *jobs)
         dn1 = block_sum_d(dn1, sh);
         dn2 = block_sum_d(dn2, sh);
     }
+    if (J.nks > 0) {
+        sup = block_sum_d(sup, sh);
+        sdn = block_sum_d(sdn, sh);
+    }
     if (tid == 0) {
         FermiOut o;
         o.efermi = mu;
@@ -151,6 +165,8 @@ __global__ void __launch_bounds__(1024) k_fermi_sums(FermiJob *jobs)
         o.entropy = ent;
         o.dent1 = dn1;
         o.dent2 = dn2;
+        o.spin_up = sup;
+        o.spin_dn = sdn;
         o.iterations = it;
         o.pad = 0;
         J.out[0] = o;

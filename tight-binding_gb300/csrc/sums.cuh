@@ -7,16 +7,19 @@ namespace nrltb {
 struct FermiOut {
     double efermi, e_total, pressure, fermi_shift;
     double entropy, dent1, dent2;   // Gillan sums (lentro), else 0
+    double spin_up, spin_dn;        // spin populations (nks > 0), else 0
     int iterations, pad;
 };
 
 struct FermiJob {
     const double *eig;      // [nk][ldk]
-    const double *deig;     // [nk][ldk] (mode 4)
-    const double *w;        // [nk]
-    const int *ncut;        // [nk] (mode 4)
-    int nv, nk, ldk, lpress;
-    int lentro, pad;        // entropy sums (modes 1, 2)
+    const double *deig;     // [nk][ldk] (modes 2, 4)
+    const double *w;        // [nk] weight of each row
+    const int *ncut;        // [nk] (modes 2, 4)
+    int nv, nk, ldk, lpress;   // nk rows: all spin channels' k points, spin 1 first
+    int lentro;             // entropy sums (modes 1, 2)
+    int nks;                // k points per spin channel when there are two, else 0
+    double el;              // electrons per band: 2 spin-restricted, 1 spin-polarized
     double tkb, zfill, tol;
     FermiOut *out;
 };

@@ -196,8 +196,7 @@ int nrltb_parfile_read(const char *path, nrltb_parfile **out, nrltb_params *par)
     if (fmt_int(fld, 0, &iv)) goto fail;
     p->nltype = (int)iv;
     p->jsover = !(ov == 'O' || ov == 'o');
-    p->jspins = (mag == 'M' || mag == 'm') ? 2 : 1;
-    if (p->jspins != 1) { rc = NRLTB_E_UNSUPPORTED; goto fail; }
+    p->jspins = (mag == 'M' || mag == 'm') ? 2 : 1;   /* input.f:213-229 */
     if (p->nltype != 90000 && (p->nltype > 3 || p->nltype < 0)) p->nltype = 0; /* input.f:239-242 */
     if (lr_next(&r)) goto fail;
     field(r.buf, 0, 79, p->title);
@@ -219,8 +218,10 @@ int nrltb_parfile_read(const char *path, nrltb_parfile **out, nrltb_params *par)
         if (ld_reals(&r, 3, occ)) goto fail;
         p->valence[i] = occ[0] + occ[1] + occ[2];
     }
-    int npards = nrltb_nparams(p->kinds);
+    /* one set per spin, read in sequence (input.f:327-358) */
+    int npards = nrltb_nparams(p->kinds) * p->jspins;
     p->param = (double *)calloc((size_t)npards, sizeof(double));
+    if (!p->param) { rc = NRLTB_E_NOMEM; goto fail; }
     p->nparam = npards;
     for (int i = 0; i < npards; ++i) {
         /* a short file leaves the remaining parameters zero (input.f:330-351) */
@@ -235,6 +236,7 @@ int nrltb_parfile_read(const char *path, nrltb_parfile **out, nrltb_params *par)
     par->dnn = p->dnn;
     par->screenl = p->screenl;
     par->param = p->param;
+    par->jspins = p->jspins;
     *out = p;
     return NRLTB_OK;
 fail:
@@ -261,7 +263,7 @@ struct nrltb_skin {
     nrltb_params par;
     /* current structure */
     int natoms;
-    int *kkind;
+    int *kkind, *flip;
     double *posn, *posq;
     /* k list, kept across structures (kptin.f `save nk`) */
     int nk;
@@ -1055,7 +1057,10 @@ int nrltb_skin_next(nrltb_skin *s, nrltb_structure *st, nrltb_kmesh *km, char *t
     if (lr_next(r)) goto fail;                     /* '(2a1)' lphonon, spin flag */
     char c1 = r->buf[0] ? r->buf[0] : ' ', c2 = (r->buf[0] && r->buf[1]) ? r->buf[1] : ' ';
     int lphonon = (c1 == 'T' || c1 == 't');
-    if (!(c2 == ' ' || c2 == 'F' || c2 == 'f')) { rc = NRLTB_E_UNSUPPORTED; goto fail; }
+    /* input1.f:535-546: T spin flips (a magdir per atom); N, D, S non-collinear
+     * runs (not built); anything else plain */
+    int spinflip = (c2 == 'T' || c2 == 't');
+    if (c2 == 'N' || c2 == 'n' || c2 == 'D' || c2 == 'd' || c2 == 'S' || c2 == 's') { rc = NRLTB_E_UNSUPPORTED; goto fail; }
     /* reciprocal vectors without 2 pi (input1.f:612-624) */
     double bvec[3][3];
     for (int i = 0; i < 3; ++i) {
@@ -1092,14 +1097,21 @@ int nrltb_skin_next(nrltb_skin *s, nrltb_structure *st, nrltb_kmesh *km, char *t
             }
         }
     }
-    free(s->kkind); free(s->posn); free(s->posq);
+    free(s->kkind); free(s->flip); free(s->posn); free(s->posq);
     s->natoms = natoms;
     s->kkind = malloc(sizeof(int) * natoms);
+    s->flip = calloc((size_t)natoms, sizeof(int));
     s->posn = malloc(sizeof(double) * 3 * natoms);
     s->posq = malloc(sizeof(double) * 3 * natoms);
+    if (!s->kkind || !s->flip || !s->posn || !s->posq) { free(shift); free(epsl); rc = NRLTB_E_NOMEM; goto fail; }
+    int anyflip = 0;
     for (int i = 0; i < natoms; ++i) {
-        double v[7];
-        if (ld_reals(r, 7, v)) { free(shift); free(epsl); goto fail; }
+        double v[8];
+        if (ld_reals(r, spinflip ? 8 : 7, v)) { free(shift); free(epsl); goto fail; }
+        if (spinflip) {   /* input1.f:778-787: magdir 2 flips the atom */
+            s->flip[i] = (v[7] == 2.0);
+            anyflip |= s->flip[i];
+        }
         int kind = (int)v[0];
         double p[3] = {v[1], v[2], v[3]};
         if (kind < 0) {
@@ -1132,6 +1144,7 @@ int nrltb_skin_next(nrltb_skin *s, nrltb_structure *st, nrltb_kmesh *km, char *t
     st->kkind = s->kkind;
     st->posn = s->posn;
     st->posq = s->posq;
+    st->flip = anyflip ? s->flip : NULL;
     memcpy(st->plv, plv, sizeof plv);
     memcpy(st->nd, nd, sizeof nd);
     st->volume = vol;
@@ -1150,6 +1163,6 @@ void nrltb_skin_close(nrltb_skin *s)
     if (!s) return;
     lr_close(&s->r);
     nrltb_parfile_close(s->pf);
-    free(s->kkind); free(s->posn); free(s->posq); free(s->kq); free(s->kw);
+    free(s->kkind); free(s->flip); free(s->posn); free(s->posq); free(s->kq); free(s->kw);
     free(s);
 }

@@ -129,12 +129,17 @@ int main(int argc, char **argv)
                 fprintf(skout, " P(0) = %.17G + O[T**4]\n", res.earg2);
             }
         }
-        /* static.f:1238-1245: E_F and bande's two outputs; mode 3 has one */
+        if (par.jspins == 2)   /* bande.f:1390-1394 */
+            fprintf(skout, "for a total magnetization of %10.5f electrons per unit cell.\n", res.smag);
+        /* static.f:1238-1254: E_F and bande's two outputs (mode 3 has one), then
+         * the moment for a collinear spin-polarized set */
+        char tail[32] = "";
+        if (par.jspins == 2) snprintf(tail, sizeof tail, "%10.6f", res.smag);
         if (mode == 3)
-            fprintf(skeng, "%-20.20s%12.6f%15.9f%15.9f\n", label, st.volume, res.efermi, res.earg1);
+            fprintf(skeng, "%-20.20s%12.6f%15.9f%15.9f%s\n", label, st.volume, res.efermi, res.earg1, tail);
         else
-            fprintf(skeng, "%-20.20s%12.6f%15.9f%15.9f%15.9f\n", label, st.volume, res.efermi, res.earg1,
-                    res.earg2);
+            fprintf(skeng, "%-20.20s%12.6f%15.9f%15.9f%15.9f%s\n", label, st.volume, res.efermi, res.earg1,
+                    res.earg2, tail);
         fflush(skeng);
         fflush(skout);
     }

@@ -41,13 +41,13 @@ _ip = C.POINTER(C.c_int)
 class Structure_(C.Structure):
     _fields_ = [("natoms", C.c_int), ("kkind", _ip), ("posn", _dp), ("posq", _dp),
                 ("plv", (C.c_double * 3) * 3), ("nd", C.c_int * 3),
-                ("volume", C.c_double), ("zcharge", C.c_double)]
+                ("volume", C.c_double), ("zcharge", C.c_double), ("flip", _ip)]
 
 
 class Params_(C.Structure):
     _fields_ = [("kinds", C.c_int), ("jsover", C.c_int), ("nltype", C.c_int),
                 ("kbas", _ip), ("valence", _dp), ("dnn", _dp), ("screenl", _dp),
-                ("param", _dp)]
+                ("param", _dp), ("jspins", C.c_int)]
 
 
 class KMesh_(C.Structure):
@@ -71,7 +71,8 @@ class Result_(C.Structure):
                 ("nv", C.c_int), ("nk", C.c_int), ("kneigh_out", C.c_int),
                 ("nonphysical_k", C.c_int), ("eig", _dp), ("deig", _dp), ("ncut", _ip),
                 ("k_status", _ip), ("entropy", C.c_double), ("free_energy", C.c_double),
-                ("entropy_shift", C.c_double), ("earg1", C.c_double), ("earg2", C.c_double)]
+                ("entropy_shift", C.c_double), ("earg1", C.c_double), ("earg2", C.c_double),
+                ("smag", C.c_double)]
 
 
 _vp = C.c_void_p

@@ -32,6 +32,7 @@ class Structure:
     volume: float
     zcharge: float = 0.0
     posq: np.ndarray = None      # (natoms, 3) phase offsets, default zero
+    flip: np.ndarray = None      # (natoms,) nonzero = spin flipped (two-spin sets only)
 
     def __post_init__(self):
         self.kkind = np.ascontiguousarray(self.kkind, dtype=np.int32)
@@ -40,6 +41,8 @@ class Structure:
         if self.posq is None:
             self.posq = np.zeros_like(self.posn)
         self.posq = np.ascontiguousarray(self.posq, dtype=np.float64).reshape(-1, 3)
+        if self.flip is not None:
+            self.flip = np.ascontiguousarray(self.flip, dtype=np.int32).reshape(-1)
 
     @property
     def natoms(self):
@@ -57,13 +60,15 @@ class Structure:
             s.nd[i] = int(self.nd[i])
         s.volume = float(self.volume)
         s.zcharge = float(self.zcharge)
+        s.flip = _iptr(self.flip)
         s._keep = (self,)
         return s
 
 
 @dataclass
 class Params:
-    """An NRL parameter set (input.f), spin-restricted."""
+    """An NRL parameter set (input.f): one set of kinds(29 + 68 kinds) values, or
+    two (jspins = 2, a collinear spin-polarized set, spin 1 first)."""
     kinds: int
     kbas: np.ndarray
     valence: np.ndarray
@@ -72,6 +77,7 @@ class Params:
     param: np.ndarray
     jsover: int = 1
     nltype: int = 0
+    jspins: int = 1
 
     def __post_init__(self):
         self.kbas = np.ascontiguousarray(self.kbas, dtype=np.int32)
@@ -79,7 +85,7 @@ class Params:
         self.dnn = np.ascontiguousarray(self.dnn, dtype=np.float64)
         self.screenl = np.ascontiguousarray(self.screenl, dtype=np.float64)
         self.param = np.ascontiguousarray(self.param, dtype=np.float64)
-        assert self.param.size == self.kinds * (29 + 68 * self.kinds)
+        assert self.param.size == self.jspins * self.kinds * (29 + 68 * self.kinds)
 
     def to_c(self):
         p = abi.Params_()
@@ -91,6 +97,7 @@ class Params:
         p.dnn = _dptr(self.dnn)
         p.screenl = _dptr(self.screenl)
         p.param = _dptr(self.param)
+        p.jspins = self.jspins
         p._keep = (self,)
         return p
 
@@ -162,12 +169,15 @@ class Result:
     entropy_shift: float = 0.0
     earg1: float = 0.0
     earg2: float = 0.0
+    smag: float = 0.0
 
 
-def new_result(nv, nk, want_eig=True, want_deig=True):
-    arrays = dict(eig=np.zeros((nk, nv)) if want_eig else None,
-                  deig=np.zeros((nk, nv)) if want_deig else None,
-                  ncut=np.zeros(nk, np.int32), k_status=np.zeros(nk, np.int32))
+def new_result(nv, nk, want_eig=True, want_deig=True, jspins=1):
+    """Result struct with per-k arrays of jspins * nk rows (spin 1's k points first)."""
+    nrow = max(jspins, 1) * nk
+    arrays = dict(eig=np.zeros((nrow, nv)) if want_eig else None,
+                  deig=np.zeros((nrow, nv)) if want_deig else None,
+                  ncut=np.zeros(nrow, np.int32), k_status=np.zeros(nrow, np.int32))
     r = abi.Result_()
     r.eig = _dptr(arrays["eig"])
     r.deig = _dptr(arrays["deig"])
@@ -181,7 +191,7 @@ def result_from_c(r, arrays):
     return Result(r.efermi, r.e_total, r.pressure, r.fermi_shift, r.dismin, r.npairs, r.nv,
                   r.nk, r.kneigh_out, r.nonphysical_k, **arrays, entropy=r.entropy,
                   free_energy=r.free_energy, entropy_shift=r.entropy_shift, earg1=r.earg1,
-                  earg2=r.earg2)
+                  earg2=r.earg2, smag=r.smag)
 
 
 def new_pairs(capacity):
@@ -235,12 +245,13 @@ def read_skin(path, lib=None):
         cp = abi.Params_()
         lib.nrltb_skin_info(h, C.byref(mode), C.byref(tkb), C.byref(eigcut), C.byref(cp))
         nint = cp.kinds * (cp.kinds + 1) // 2
-        npar = cp.kinds * (29 + 68 * cp.kinds)
+        npar = max(cp.jspins, 1) * cp.kinds * (29 + 68 * cp.kinds)
         params = Params(cp.kinds, np.ctypeslib.as_array(cp.kbas, (cp.kinds,)).copy(),
                         np.ctypeslib.as_array(cp.valence, (cp.kinds,)).copy(),
                         np.ctypeslib.as_array(cp.dnn, (nint,)).copy(),
                         np.ctypeslib.as_array(cp.screenl, (nint,)).copy(),
-                        np.ctypeslib.as_array(cp.param, (npar,)).copy(), cp.jsover, cp.nltype)
+                        np.ctypeslib.as_array(cp.param, (npar,)).copy(), cp.jsover, cp.nltype,
+                        max(cp.jspins, 1))
         out = SkinFile(mode.value, tkb.value, eigcut.value, params)
         while True:
             cs, ck = abi.Structure_(), abi.KMesh_()
@@ -255,7 +266,8 @@ def read_skin(path, lib=None):
                            np.ctypeslib.as_array(cs.posn, (n, 3)).copy(),
                            np.array([[cs.plv[i][j] for j in range(3)] for i in range(3)]),
                            tuple(cs.nd), cs.volume, cs.zcharge,
-                           np.ctypeslib.as_array(cs.posq, (n, 3)).copy())
+                           np.ctypeslib.as_array(cs.posq, (n, 3)).copy(),
+                           np.ctypeslib.as_array(cs.flip, (n,)).copy() if cs.flip else None)
             km = KMesh(np.ctypeslib.as_array(ck.k, (ck.nk, 3)).copy(),
                        np.ctypeslib.as_array(ck.w, (ck.nk,)).copy())
             out.structures.append((title.value.decode(), label.value.decode(), st, km))
@@ -302,14 +314,14 @@ class Context:
 
     def bande(self, st, par, km, opts, want_eig=True):
         nv, nk = par.nv(st), km.nk
-        r, arrays = new_result(nv, nk, want_eig, want_eig)
+        r, arrays = new_result(nv, nk, want_eig, want_eig, par.jspins)
         cs, cp, ck, co = st.to_c(), par.to_c(), km.to_c(), opts.to_c()
         self._check(self.lib.nrltb_bande(self.h, C.byref(cs), C.byref(cp), C.byref(ck),
                                          C.byref(co), C.byref(r)), "nrltb_bande")
         return result_from_c(r, arrays)
 
     def stage(self, st, par, km, opts):
-        self._staged = (st.to_c(), par.to_c(), km.to_c(), opts.to_c(), par.nv(st), km.nk)
+        self._staged = (st.to_c(), par.to_c(), km.to_c(), opts.to_c(), par.nv(st), km.nk, par.jspins)
         cs, cp, ck, co = self._staged[:4]
         self._check(self.lib.nrltb_stage(self.h, C.byref(cs), C.byref(cp), C.byref(ck),
                                          C.byref(co)), "nrltb_stage")
@@ -319,7 +331,7 @@ class Context:
 
     def fetch(self, want_eig=True):
         nv, nk = self._staged[4], self._staged[5]
-        r, arrays = new_result(nv, nk, want_eig, want_eig)
+        r, arrays = new_result(nv, nk, want_eig, want_eig, self._staged[6])
         self._check(self.lib.nrltb_fetch(self.h, C.byref(r)), "nrltb_fetch")
         return result_from_c(r, arrays)
 

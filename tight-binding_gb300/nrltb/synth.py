@@ -87,6 +87,22 @@ def make_params(kbas_list, valence_list, seed, dnn=16.5, screenl=0.5, s_scale=1.
                   np.full(nint, dnn), np.full(nint, screenl), p, 1, 0)
 
 
+def make_magnetic_params(kbas_list, valence_list, seed, split=0.08, dnn=16.5, screenl=0.5):
+    """A collinear spin-polarized set (jspins = 2): the spin-1 set drawn as
+    make_params does, the spin-2 set equal to it except for the on-site
+    polynomials' constant terms, raised by `split` Ry (an exchange splitting),
+    and the density parameters, scaled by 1.05."""
+    base = make_params(kbas_list, valence_list, seed, dnn=dnn, screenl=screenl)
+    p2 = base.param.copy()
+    for k in range(base.kinds):
+        ip = k * 17
+        p2[ip] *= 1.05
+        for o in range(4):
+            p2[ip + 1 + 4 * o] += split
+    return Params(base.kinds, base.kbas, base.valence, base.dnn, base.screenl,
+                  np.concatenate([base.param, p2]), 1, 0, 2)
+
+
 def search_box(plv, dnn):
     """Smallest search box nd that finds every image within dnn (search2.f)."""
     vol = abs(np.linalg.det(plv))
@@ -180,8 +196,9 @@ CONFIGS = {"fcc1": fcc1, "bcc32": bcc32, "fcc128": fcc128, "b2_216": b2_216}
 # ---- writers in the reference's file formats ---------------------------------
 def write_params(path, par, title="synthetic NRL parameters"):
     with open(path, "w") as f:
-        # first letter: N non-orthogonal, O orthogonal (S parameters read, ignored)
-        f.write("%sN%05d\n" % ("N" if par.jsover else "O", par.nltype))
+        # N non-orthogonal / O orthogonal (S parameters read, ignored); then N
+        # spin-restricted / M magnetic (one parameter set per spin)
+        f.write("%s%s%05d\n" % ("N" if par.jsover else "O", "M" if par.jspins == 2 else "N", par.nltype))
         f.write(title[:79] + "\n")
         f.write("%d\n" % par.kinds)
         for i in range(par.dnn.size):
@@ -216,7 +233,10 @@ def write_skin(dirname, entries, par, mode=4, tkb=0.005, eigcut=1e3):
             f.write("0\n")
             for v in st.plv:
                 f.write("%.17g %.17g %.17g\n" % tuple(v))
-            f.write("1 1 1\n0\n%d\n%d %d %d\nF\n" % ((st.natoms,) + tuple(st.nd)))
-            for kk, p, q in zip(st.kkind, st.posn, st.posq):
-                f.write("%d %.17g %.17g %.17g %.17g %.17g %.17g\n" % ((-int(kk),) + tuple(p) + tuple(q)))
+            flips = st.flip is not None
+            # (2a1) lphonon, spin flag: T means a magdir (1 up, 2 flipped) per atom
+            f.write("1 1 1\n0\n%d\n%d %d %d\n%s\n" % ((st.natoms,) + tuple(st.nd) + ("FT" if flips else "F",)))
+            for i, (kk, p, q) in enumerate(zip(st.kkind, st.posn, st.posq)):
+                f.write("%d %.17g %.17g %.17g %.17g %.17g %.17g" % ((-int(kk),) + tuple(p) + tuple(q)))
+                f.write(" %d\n" % (2 if st.flip[i] else 1) if flips else "\n")
             f.write("NEWSYM=T\nLATTIC=1\nsg\nILAT=F\n-1313\n%s\n" % kname)
