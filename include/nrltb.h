@@ -90,7 +90,9 @@ typedef struct {
 
 typedef struct {
     int mode;              /* static.f modes: 3 E(T); 4 E(T), P(T); 1 and 2 the  */
-                           /* same plus Gillan's T -> 0 extrapolation           */
+                           /* same plus Gillan's T -> 0 extrapolation; 5, 6, 10 */
+                           /* E(T) plus orbital charges (orbocc); 8, 9 E(T) for */
+                           /* eigenvalue files (7 is not a mode of the reference)*/
     int precision;         /* NRLTB_PREC_FP64 or NRLTB_PREC_MIXED               */
     double tkb;            /* Fermi broadening kT, Ry                           */
     double eigcut;         /* eigenvalue cutoff for the pressure sums, Ry       */
@@ -137,6 +139,10 @@ typedef struct {
     double earg1, earg2;
     double smag;           /* jspins = 2: spin-up minus spin-down electrons per */
                            /* cell (bande.f:1336-1395), SKENG's last column; 0  */
+    double *orbocc;        /* optional out [jspins][nk][nv][nv], modes 5, 6, 10: */
+                           /* [row][state n][orbital i] = |(S^1/2 z_n)_i|^2, the */
+                           /* Lowdin charges of diag.f:526-700; -1 at a k whose  */
+                           /* overlap is not positive definite                  */
 } nrltb_result;
 
 typedef struct nrltb_ctx nrltb_ctx;

@@ -46,6 +46,18 @@ void nrltb_parfile_close(nrltb_parfile *p);
 /* Number of parameters for `kinds` species: kinds(29 + 68 kinds) (input.f:275). */
 int nrltb_nparams(int kinds);
 
+/* Eigenvalue files (static.f:759-781, 1132-1145; bande.f:1568-1700): append one
+ * structure's records (append != 0) or start the file, for mode 6 or 10 (QLMT
+ * with per-atom s, p, d or per-orbital Lowdin charges of the states below
+ * eigcut; res->orbocc required), 9 (QLMT with every eigenvalue, no atoms) or 8
+ * (QAPW, eigenvalues per k point).  res holds nrltb_bande's per-k arrays for
+ * par->jspins spin blocks; km is the k list the structure was run on.  Mode 5
+ * is not written: the reference mixes formatted records into its unformatted
+ * QLMT and stops there. */
+int nrltb_qlmt_write(const char *path, int append, int mode, const nrltb_structure *st,
+                     const nrltb_params *par, const nrltb_kmesh *km, double eigcut,
+                     const nrltb_result *res);
+
 #ifdef __cplusplus
 }
 #endif

@@ -790,6 +790,43 @@ int oracle_diag_dense(int nv, int nk, const double *hd, const double *sd, double
 /* ---------------------------------------------------------------------- */
 /* bande (src/bande.f:816-1446) for one structure, k loop parallel over
  * threads (the reference's k data parallelism, one k per thread).          */
+/* diag.f:526-700: Lowdin charges |(U z_k)_i|^2 of every state k, U = S^1/2 formed
+ * from zhpev's eigenpairs of S as diag.f:603-614 forms it (U = 1 for an
+ * orthogonal set); sp is S packed upper, z the S-orthonormal eigenvectors
+ * (column k = state k); orb[k * n + i].                                     */
+static void oracle_lowdin(int n, int jsover, const zc *sp, const zc *z, double *orb)
+{
+    zc *u = calloc((size_t)n * n, sizeof(zc));
+    if (jsover) {
+        size_t np = (size_t)n * (n + 1) / 2;
+        zc *s1 = malloc(sizeof(zc) * np), *sv = malloc(sizeof(zc) * (size_t)n * n);
+        zc *work = malloc(sizeof(zc) * 2 * (size_t)n);
+        double *rwork = malloc(sizeof(double) * 3 * (size_t)n), *seig = malloc(sizeof(double) * n);
+        memcpy(s1, sp, sizeof(zc) * np);
+        char jobz = 'V', uplo = 'U';
+        int info = 0, ld = n;
+        p_zhpev(&jobz, &uplo, &n, s1, seig, sv, &ld, work, rwork, &info);
+        for (int i = 0; i < n; ++i) seig[i] = sqrt(seig[i]);
+        for (int i = 0; i < n; ++i)
+            for (int j = 0; j <= i; ++j) {
+                zc csum = 0;
+                for (int k = 0; k < n; ++k) csum = csum + seig[k] * sv[(size_t)k * n + i] * conj(sv[(size_t)k * n + j]);
+                u[(size_t)j * n + i] = csum;          /* u(i, j) */
+                u[(size_t)i * n + j] = conj(csum);    /* u(j, i) */
+            }
+        free(s1); free(sv); free(work); free(rwork); free(seig);
+    } else {
+        for (int i = 0; i < n; ++i) u[(size_t)i * n + i] = 1.0;
+    }
+    for (int k = 0; k < n; ++k)
+        for (int i = 0; i < n; ++i) {
+            zc csum = 0;
+            for (int m = 0; m < n; ++m) csum = csum + u[(size_t)m * n + i] * z[(size_t)k * n + m];
+            orb[(size_t)k * n + i] = creal(csum * conj(csum));
+        }
+    free(u);
+}
+
 int oracle_bande(const nrltb_structure *st, const nrltb_params *par, const nrltb_kmesh *km,
                  const nrltb_opts *opt, nrltb_result *res, int nthreads)
 {
@@ -800,6 +837,7 @@ int oracle_bande(const nrltb_structure *st, const nrltb_params *par, const nrltb
         for (int i = 0; i < st->natoms; ++i)
             if (st->flip[i]) return NRLTB_E_ARG;   /* spin flips need two parameter sets */
     int lpress = (opt->mode == 2 || opt->mode == 4);
+    const int lqlmt = (opt->mode == 5 || opt->mode == 6 || opt->mode == 10) && res->orbocc;
     int nv = 0;
     double zfill = st->zcharge;
     for (int i = 0; i < st->natoms; ++i) { nv += par->kbas[st->kkind[i] - 1]; zfill += par->valence[st->kkind[i] - 1]; }
@@ -831,10 +869,18 @@ int oracle_bande(const nrltb_structure *st, const nrltb_params *par, const nrltb
         for (int k = 0; k < nk; ++k) {
             const int r = js * nk + k;
             zc *hp = malloc(sizeof(zc) * np), *sp = malloc(sizeof(zc) * np);
-            zc *z = lpress ? malloc(sizeof(zc) * (size_t)nv * nv) : NULL;
+            zc *z = (lpress || lqlmt) ? malloc(sizeof(zc) * (size_t)nv * nv) : NULL;
+            zc *sc = lqlmt ? malloc(sizeof(zc) * np) : NULL;
             oracle_setham_packed(st, par, &pr, hop, over, paros, km->k + 3 * k, 0, hp, sp);
-            int ioverr = oracle_diag_packed(nv, lpress, par->jsover, hp, sp, esk + (size_t)r * nv, z);
+            if (sc) memcpy(sc, sp, sizeof(zc) * np);
+            int ioverr = oracle_diag_packed(nv, lpress || lqlmt, par->jsover, hp, sp, esk + (size_t)r * nv, z);
             kst[r] = ioverr ? NRLTB_K_S_NOT_PD : NRLTB_K_OK;
+            if (lqlmt) {
+                double *orb = res->orbocc + (size_t)r * nv * nv;
+                if (ioverr) for (size_t i = 0; i < (size_t)nv * nv; ++i) orb[i] = -1.0;
+                else oracle_lowdin(nv, par->jsover, sc, z, orb);
+            }
+            free(sc);
             if (!ioverr && lpress) {
                 oracle_setham_packed(st, par, &pr, dhop, dover, dparos, km->k + 3 * k, 1, hp, sp);
                 if (!par->jsover) for (size_t i = 0; i < np; ++i) sp[i] = 0;

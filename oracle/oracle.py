@@ -156,7 +156,7 @@ def bande(st, par, km, opts, nthreads=0):
     from nrltb import api
     lib = load()
     nv, nk = par.nv(st), km.nk
-    r, arrays = api.new_result(nv, nk, jspins=par.jspins)
+    r, arrays = api.new_result(nv, nk, jspins=par.jspins, want_orbocc=opts.mode in (5, 6, 10))
     cs, cp, ck, co = st.to_c(), par.to_c(), km.to_c(), opts.to_c()
     rc = lib.oracle_bande(_ref(cs), _ref(cp), _ref(ck), _ref(co), _ref(r), nthreads)
     assert rc == 0, rc

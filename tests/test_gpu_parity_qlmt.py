@@ -1,0 +1,115 @@
+"""Modes 5, 6, 10 (Lowdin orbital charges, diag.f:526-700) and the eigenvalue
+files of modes 6, 8, 9, 10 on the GPU path against the oracle.
+
+Charges are compared summed over each group of degenerate states (within a
+group any rotation of the eigenvectors is as good, and the per-state charges
+follow the rotation): 1e-9 in the FP64 form, 1e-8 in the mixed form.  A k point
+whose overlap is not positive definite carries -1 for every charge.  The host
+driver's QLMT and QAPW files are compared field by field with the same writer
+fed the oracle's results, on k points with no degenerate states, within two
+units of each field's last printed digit.
+"""
+import os
+import subprocess
+from dataclasses import replace
+
+import numpy as np
+import pytest
+
+import oracle
+from nrltb import KMesh, Opts, abi, build, read_skin, synth, write_qlmt
+
+pytestmark = pytest.mark.gpu
+
+
+def _groups(e):
+    return np.concatenate([[0], np.cumsum(np.diff(e) > 1e-8)])
+
+
+def _compare_charges(g, o, tol):
+    assert g.orbocc.shape == o.orbocc.shape
+    for row in range(o.orbocc.shape[0]):
+        if o.k_status[row] != 0:
+            assert (g.orbocc[row] == -1.0).all()
+            continue
+        grp = _groups(o.eig[row])
+        for gid in np.unique(grp):
+            m = grp == gid
+            assert np.abs(g.orbocc[row][m].sum(axis=0) - o.orbocc[row][m].sum(axis=0)).max() <= tol * m.sum()
+
+
+def _run(ctx, st, par, km, mode, precision, tkb=0.005):
+    g = ctx.bande(st, par, km, Opts(mode=mode, precision=precision, tkb=tkb, eigcut=1e3, fermi_tol=1e-11))
+    o = oracle.bande(st, par, km, Opts(mode=mode, tkb=tkb, eigcut=1e3, fermi_tol=1e-11))
+    etol = 1e-10 if precision == abi.PREC_FP64 else 1e-9
+    assert np.abs(g.eig - o.eig).max() <= etol
+    assert abs(g.e_total - o.e_total) / st.natoms <= 1e-8
+    assert np.abs(g.orbocc.sum(axis=2)[g.k_status == 0] - 1.0).max() <= 1e-9
+    _compare_charges(g, o, 1e-9 if precision == abi.PREC_FP64 else 1e-8)
+    return g, o
+
+
+@pytest.mark.parametrize("precision", [abi.PREC_FP64, abi.PREC_MIXED])
+@pytest.mark.parametrize("mode", [6, 10, 5])
+def test_charges_fcc1(ctx, mode, precision):
+    st, par, km, o = synth.fcc1()
+    idx = np.arange(0, km.nk, 61)
+    _run(ctx, st, par, KMesh(km.k[idx], km.w[idx] / km.w[idx].sum()), mode, precision, o["tkb"])
+
+
+@pytest.mark.parametrize("precision", [abi.PREC_FP64, abi.PREC_MIXED])
+def test_charges_bcc32(ctx, precision):
+    st, par, km, o = synth.bcc32()
+    idx = np.array([0, 21, 42, 63])
+    _run(ctx, st, par, KMesh(km.k[idx], km.w[idx] / km.w[idx].sum()), 6, precision, o["tkb"])
+
+
+def test_charges_orthogonal_and_spin(ctx):
+    st, par, km, o = synth.fcc1()
+    idx = np.arange(0, km.nk, 173)
+    sub = KMesh(km.k[idx], km.w[idx] / km.w[idx].sum())
+    _run(ctx, st, replace(par, jsover=0), sub, 10, abi.PREC_FP64, o["tkb"])
+    mag = synth.make_magnetic_params([9], [10.0], 7, split=0.08)
+    g, _ = _run(ctx, st, mag, sub, 6, abi.PREC_FP64, o["tkb"])
+    assert g.orbocc.shape[0] == 2 * sub.nk
+
+
+def test_charges_nonpositive_overlap(ctx):
+    st, _, km, _ = synth.fcc1()
+    par = synth.make_params([9], [11.0], 11)
+    sub = KMesh(km.k[[0, 340, 471, 900, 1727]], np.full(5, 0.2))
+    g, o = _run(ctx, st, par, sub, 6, abi.PREC_FP64)
+    assert (o.k_status != 0).sum() >= 2 and np.array_equal(g.k_status, o.k_status)
+
+
+def _fields(line):
+    return line.replace("D", "E").split()
+
+
+@pytest.mark.parametrize("mode", [6, 8, 9, 10])
+def test_host_driver_files(tmp_path, mode):
+    rng = np.random.default_rng(5)
+    st, par, _, o = synth.fcc1()
+    km = KMesh(rng.uniform(-0.5, 0.5, (6, 3)), np.full(6, 1 / 6))   # generic points: no degeneracy
+    sts = [(st, km), (replace(st, plv=st.plv * 1.02, posn=st.posn * 1.02, volume=st.volume * 1.02 ** 3), km)]
+    synth.write_skin(str(tmp_path), sts, par, mode=mode, tkb=o["tkb"], eigcut=0.5)
+    r = subprocess.run([build.DRIVER, "SKIN"], cwd=tmp_path, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    name = "QAPW" if mode == 8 else "QLMT"
+    got = (tmp_path / name).read_text().splitlines()
+    sk = read_skin(str(tmp_path / "SKIN"))
+    ref_path = str(tmp_path / "ref")
+    for j, (_, _, s, k) in enumerate(sk.structures):
+        res = oracle.bande(s, sk.params, k, Opts(mode=mode, tkb=sk.tkb, eigcut=sk.eigcut))
+        write_qlmt(ref_path, mode, s, sk.params, k, sk.eigcut, res, append=j > 0)
+    want = open(ref_path).read().splitlines()
+    assert len(got) == len(want)
+    for a, b in zip(got, want):
+        fa, fb = _fields(a), _fields(b)
+        assert len(fa) == len(fb), (a, b)
+        for x, y in zip(fa, fb):
+            if x == y:
+                continue
+            last = 10.0 ** -(len(x.split("E")[0].split(".")[1]) if "." in x else 0)
+            scale = 10.0 ** int(x.split("E")[1]) if "E" in x else 1.0
+            assert abs(float(x) - float(y)) <= 2 * last * scale, (a, b)

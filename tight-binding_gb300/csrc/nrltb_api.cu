@@ -114,10 +114,10 @@ struct nrltb_ctx {
     // setpar / SK
     DBuf d_sk, d_seg, d_ph;
     // k-chunk matrices and solver
-    DBuf d_H, d_S, d_X, d_work, d_ref, d_hf, d_np;
+    DBuf d_H, d_S, d_X, d_work, d_ref, d_hf, d_np, d_qw;
     std::vector<std::pair<int, int>> nonpd;   // (k, chunk) of k points whose S is not positive definite
     // results
-    DBuf d_eig, d_deig, d_ncut, d_status, d_fjob, d_fout;
+    DBuf d_eig, d_deig, d_ncut, d_status, d_fjob, d_fout, d_orbq;
     FermiOut fout;
     int ran = 0;
 };
@@ -417,12 +417,12 @@ static size_t per_k_bytes(int nv, int prec)
     return 32 * nn + w + x + ref + hf_scratch_bytes(nv, 1) + 64 * (size_t)nv;
 }
 
-static int choose_chunk(int nv, int nk, int prec)
+static int choose_chunk(int nv, int nk, int prec, size_t extra_per_k = 0)
 {
     size_t free_b = 0, total_b = 0;
     cudaMemGetInfo(&free_b, &total_b);
     size_t budget = std::min<size_t>(free_b / 2, (size_t)48 << 30);
-    size_t per = per_k_bytes(nv, prec);
+    size_t per = per_k_bytes(nv, prec) + extra_per_k;
     long c = (long)(budget / std::max<size_t>(per, 1));
     c = std::max(1L, std::min<long>(c, nk));
     return (int)c;
@@ -467,6 +467,68 @@ __global__ void k_identity(double2 *M, int n, int batch)
     M[t] = make_double2(r == col ? 1.0 : 0.0, 0.0);
 }
 
+// ---- Lowdin orbital charges (modes 5, 6, 10; diag.f:526-700) ----------------
+// With S = V diag(o) V^H the square root is U = V diag(o^1/2) V^H, and the charge
+// of orbital i in state n is |(U z_n)_i|^2 (z_n S-orthonormal, so each state's
+// charges sum to 1).  U z = V (diag(o^1/2) (V^H z)): two batched GEMMs.
+__global__ void k_lowdin_scale(double2 *Y, const double *o, int n, int batch)
+{
+    const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    const long nn = (long)n * n;
+    if (t >= nn * batch) return;
+    const long b = t / nn;
+    const int i = (int)((t - b * nn) % n);   // row of Y = V^H z (column-major)
+    const double r = sqrt(fmax(o[b * n + i], 0.0));
+    Y[t] = make_double2(Y[t].x * r, Y[t].y * r);
+}
+
+// orb[b][state][orbital] = |W(orbital, state)|^2, i.e. the same flat index as the
+// column-major W; -1 for every entry of a k whose overlap is not positive definite
+__global__ void k_lowdin_charges(const double2 *W, const int *status, double *orb, int n, int batch)
+{
+    const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    const long nn = (long)n * n;
+    if (t >= nn * batch) return;
+    const double2 w = W[t];
+    orb[t] = (status[t / nn] == NRLTB_K_S_NOT_PD) ? -1.0 : w.x * w.x + w.y * w.y;
+}
+
+static size_t lowdin_bytes_per_k(int nv) { return 3 * sizeof(double2) * (size_t)nv * nv + sizeof(double) * nv + 1024; }
+
+// charges of nkc k points: S their overlaps, Z their S-orthonormal eigenvectors
+static int run_lowdin(nrltb_ctx *c, int nv, int nkc, const double2 *S, const double2 *Z, const int *status,
+                      double *orb)
+{
+    cudaStream_t s = c->stream;
+    const size_t nn = (size_t)nv * nv;
+    const size_t mat = (sizeof(double2) * nn * nkc + 255) & ~size_t(255);
+    const long tot = (long)nn * nkc;
+    const double2 *W = Z;
+    if (c->st.jsover) {
+        RET(c->d_qw.ensure(3 * mat + sizeof(double) * (size_t)nv * nkc));
+        double2 *A = c->d_qw.as<double2>();
+        double2 *B = (double2 *)(c->d_qw.as<char>() + mat);
+        double2 *V = (double2 *)(c->d_qw.as<char>() + 2 * mat);
+        double *o = (double *)(c->d_qw.as<char>() + 3 * mat);
+        // eigen-decomposition of S (diag.f:545): S as the matrix, identity metric
+        CK(cudaMemcpyAsync(A, S, sizeof(double2) * nn * nkc, cudaMemcpyDeviceToDevice, s));
+        NRLTB_LAUNCH(k_identity, cdiv(tot, 256), 256, 0, s, B, nv, nkc);
+        RET(c->d_work.ensure(eig_work_bytes<double>(nv, nkc)));
+        EigWork<double> w;
+        eig_work_carve<double>(w, c->d_work.p, nv, nkc);
+        eig_solve<double>(s, w, A, B, o, V, true);
+        CKL();
+        const double2 one = make_double2(1, 0), zero = make_double2(0, 0);
+        zgemm<double>(s, nv, nv, nv, nkc, one, V, nv, (long)nn, 1, Z, nv, (long)nn, 0, zero, A, nv, (long)nn);
+        NRLTB_LAUNCH(k_lowdin_scale, cdiv(tot, 256), 256, 0, s, A, o, nv, nkc);
+        zgemm<double>(s, nv, nv, nv, nkc, one, V, nv, (long)nn, 0, A, nv, (long)nn, 0, zero, B, nv, (long)nn);
+        W = B;
+    }
+    NRLTB_LAUNCH(k_lowdin_charges, cdiv(tot, 256), 256, 0, s, W, status, orb, nv, nkc);
+    CKL();
+    return NRLTB_OK;
+}
+
 // k points whose overlap is not positive definite get the eigenvalues of S in
 // place of band energies, as diag.f:429-455 leaves them in esk, and take no part
 // in the perturbation (bande.f:997-1003).
@@ -498,11 +560,15 @@ static int run_all(nrltb_ctx *c)
     if (!c->st.valid) { set_err("nothing staged"); return NRLTB_E_ARG; }
     const Staged &S = c->st;
     const nrltb_opts &o = S.opt;
-    if (o.mode < 1 || o.mode > 4) { set_err("mode %d: modes 1 to 4 are built", o.mode); return NRLTB_E_UNSUPPORTED; }
+    if (o.mode < 1 || o.mode > 10 || o.mode == 7) {
+        set_err("mode %d: modes 1-6 and 8-10 are built (the reference has no mode 7)", o.mode);
+        return NRLTB_E_UNSUPPORTED;
+    }
     if (!(o.precision == NRLTB_PREC_FP64 || o.precision == NRLTB_PREC_MIXED)) { set_err("precision"); return NRLTB_E_ARG; }
     if (S.nk < 1) { set_err("no k points"); return NRLTB_E_ARG; }
     const int lpress = (o.mode == 2 || o.mode == 4);   // bande.f:726-730
     const int lentro = (o.mode < 3);
+    const int lqlmt = (o.mode == 5 || o.mode == 6 || o.mode == 10);   // orbital charges, diag.f:526
     cudaStream_t s = c->stream;
     long long *prev = g_launch_counter;
     KTimer *prev_kt = g_ktimer;
@@ -520,8 +586,9 @@ static int run_all(nrltb_ctx *c)
         if ((rc = c->d_deig.ensure(sizeof(double) * (size_t)nv * nrow))) break;
         if ((rc = c->d_ncut.ensure(sizeof(int) * (size_t)nrow))) break;
         if ((rc = c->d_status.ensure(sizeof(int) * (size_t)nrow))) break;
-        const int chunk = choose_chunk(nv, nk, o.precision);
+        const int chunk = choose_chunk(nv, nk, o.precision, lqlmt ? lowdin_bytes_per_k(nv) : 0);
         const size_t nn = (size_t)nv * nv;
+        if (lqlmt && (rc = c->d_orbq.ensure(sizeof(double) * nn * nrow))) break;
         if ((rc = c->d_H.ensure(sizeof(double2) * nn * chunk))) break;
         if ((rc = c->d_S.ensure(sizeof(double2) * nn * chunk))) break;
         if ((rc = c->d_X.ensure(zoff(nn, chunk) + sizeof(double2) * nn * chunk))) break;
@@ -537,12 +604,12 @@ static int run_all(nrltb_ctx *c)
                 int *status = c->d_status.as<int>() + r0;
                 if ((rc = run_bloch(c, k0, nkc, 0, c->d_H.as<double2>(), c->d_S.as<double2>()))) break;
                 double2 *Z = nullptr;
-                if (lpress) {
+                if (lpress || lqlmt) {
                     // FP64 eigenvectors live after the FP32 staging area of d_X
                     Z = (double2 *)(c->d_X.as<char>() + zoff(nn, chunk));
                 }
                 if ((rc = run_solve(c, nv, nkc, o.precision, c->d_H.as<double2>(), c->d_S.as<double2>(), eig, Z,
-                                    status, lpress != 0)))
+                                    status, (lpress || lqlmt) != 0)))
                     break;
                 std::vector<int> hst(nkc), bad;
                 if (cudaMemcpyAsync(hst.data(), status, sizeof(int) * nkc, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
@@ -552,6 +619,9 @@ static int run_all(nrltb_ctx *c)
                     if ((rc = fix_nonpd(c, nv, bad, c->d_S.as<double2>(), eig))) break;
                     for (int k : bad) c->nonpd.push_back(std::make_pair(r0 + k, 0));
                 }
+                if (lqlmt && (rc = run_lowdin(c, nv, nkc, c->d_S.as<double2>(), Z, status,
+                                              c->d_orbq.as<double>() + (size_t)r0 * nn)))
+                    break;
                 if (lpress) {
                     if ((rc = run_bloch(c, k0, nkc, 2, c->d_H.as<double2>(), c->d_S.as<double2>()))) break;
                     if ((rc = c->d_hf.ensure(hf_scratch_bytes(nv, nkc)))) break;
@@ -616,6 +686,9 @@ static int fetch(nrltb_ctx *c, nrltb_result *res)
         if (lpress) CK(cudaMemcpyAsync(res->ncut, c->d_ncut.p, sizeof(int) * nrow, cudaMemcpyDeviceToHost, s));
         else for (int k = 0; k < nrow; ++k) res->ncut[k] = nv;
     }
+    if (res->orbocc && (mode == 5 || mode == 6 || mode == 10))
+        CK(cudaMemcpyAsync(res->orbocc, c->d_orbq.p, sizeof(double) * (size_t)nv * nv * nrow, cudaMemcpyDeviceToHost,
+                           s));
     CK(cudaStreamSynchronize(s));
     res->efermi = c->fout.efermi;
     res->e_total = c->fout.e_total;
@@ -687,7 +760,8 @@ int nrltb_ctx_destroy(nrltb_ctx *c)
     DBuf *bufs[] = {&c->d_kkind, &c->d_posn, &c->d_posq, &c->d_kbas, &c->d_dnn, &c->d_screenl, &c->d_param,
                     &c->d_kq, &c->d_kw, &c->d_ksk, &c->d_orb, &c->d_flip, &c->d_code, &c->d_blk, &c->d_misc, &c->d_pairs,
                     &c->d_sk, &c->d_seg, &c->d_ph, &c->d_H, &c->d_S, &c->d_X, &c->d_work, &c->d_ref, &c->d_hf, &c->d_np,
-                    &c->d_eig, &c->d_deig, &c->d_ncut, &c->d_status, &c->d_fjob, &c->d_fout};
+                    &c->d_qw, &c->d_eig, &c->d_deig, &c->d_ncut, &c->d_status, &c->d_fjob, &c->d_fout,
+                    &c->d_orbq};
     for (DBuf *b : bufs) b->release();
     if (c->kt) {
         for (int i = 0; i < c->kt->npool; ++i) cudaEventDestroy(c->kt->pool[i]);

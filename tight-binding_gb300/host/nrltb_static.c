@@ -55,8 +55,10 @@ int main(int argc, char **argv)
     double tkb, eigcut;
     nrltb_params par;
     nrltb_skin_info(skin, &mode, &tkb, &eigcut, &par);
-    if (mode < 1 || mode > 4) {
-        fprintf(stderr, "nrltb_static: Mode=%d is not built (modes 1 to 4 are)\n", mode);
+    /* mode 7 stops the reference (static.f:732-743); its mode 5 writes formatted
+     * records into an unformatted QLMT and stops there (bande.f:1631-1640) */
+    if (mode < 1 || mode > 10 || mode == 5 || mode == 7) {
+        fprintf(stderr, "nrltb_static: Mode=%d is not built (modes 1-4, 6 and 8-10 are)\n", mode);
         nrltb_skin_close(skin);
         return 1;
     }
@@ -75,6 +77,9 @@ int main(int argc, char **argv)
     fprintf(skout, " mode=%12d\n", mode);
     fprintf(skout, "  temp. broad. (ryd): %.17G  eigenvalue cutoff = %.17G\n", tkb, eigcut);
     fprintf(skout, " precision form: %s\n", precision == NRLTB_PREC_FP64 ? "FP64" : "mixed (FP32 + FP64 refinement)");
+    /* static.f:759-781: QLMT for modes 6, 9, 10, QAPW for mode 8, one file for
+     * every structure */
+    const char *qfile = (mode == 8) ? "QAPW" : (mode == 6 || mode == 9 || mode == 10) ? "QLMT" : NULL;
     int kneigh = 0, jstruc = 0, status = 0;
     for (;;) {
         nrltb_structure st;
@@ -98,9 +103,31 @@ int main(int argc, char **argv)
         opt.kneigh_in = kneigh;
         nrltb_result res;
         memset(&res, 0, sizeof res);
+        const int nsp = (par.jspins == 2) ? 2 : 1;
+        size_t nv = 0;
+        for (int i = 0; i < st.natoms; ++i) nv += (size_t)par.kbas[st.kkind[i] - 1];
+        double *eigbuf = NULL, *orbbuf = NULL;
+        if (qfile) {
+            eigbuf = malloc(sizeof(double) * nv * (size_t)km.nk * nsp);
+            if (mode == 6 || mode == 10) orbbuf = malloc(sizeof(double) * nv * nv * (size_t)km.nk * nsp);
+            if (!eigbuf || ((mode == 6 || mode == 10) && !orbbuf)) {
+                fprintf(stderr, "nrltb_static: structure %d: out of host memory\n", jstruc);
+                free(eigbuf); free(orbbuf);
+                status = 1;
+                break;
+            }
+            res.eig = eigbuf;
+            res.orbocc = orbbuf;
+        }
         rc = nrltb_bande(ctx, &st, &par, &km, &opt, &res);
+        if (rc == NRLTB_OK && qfile) {
+            rc = nrltb_qlmt_write(qfile, jstruc > 1, mode, &st, &par, &km, eigcut, &res);
+            if (rc != NRLTB_OK) fprintf(stderr, "nrltb_static: cannot write %s (error %d)\n", qfile, rc);
+        }
+        free(eigbuf);
+        free(orbbuf);
         if (rc != NRLTB_OK) {
-            fprintf(stderr, "nrltb_static: structure %d: %s\n", jstruc, nrltb_last_error());
+            if (rc != NRLTB_E_IO) fprintf(stderr, "nrltb_static: structure %d: %s\n", jstruc, nrltb_last_error());
             status = 1;
             break;
         }
@@ -135,7 +162,7 @@ int main(int argc, char **argv)
          * the moment for a collinear spin-polarized set */
         char tail[32] = "";
         if (par.jspins == 2) snprintf(tail, sizeof tail, "%10.6f", res.smag);
-        if (mode == 3)
+        if (mode == 3 || mode > 4)
             fprintf(skeng, "%-20.20s%12.6f%15.9f%15.9f%s\n", label, st.volume, res.efermi, res.earg1, tail);
         else
             fprintf(skeng, "%-20.20s%12.6f%15.9f%15.9f%15.9f%s\n", label, st.volume, res.efermi, res.earg1,

@@ -7,4 +7,4 @@ builds it (``nrltb.build``) and generates the seeded synthetic workloads
 """
 from . import abi  # noqa: F401
 from .api import (Context, KMesh, NrltbError, Opts, Params, Result, SkinFile,  # noqa: F401
-                  Structure, read_skin)
+                  Structure, read_skin, write_qlmt)

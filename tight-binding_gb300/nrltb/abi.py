@@ -72,7 +72,7 @@ class Result_(C.Structure):
                 ("nonphysical_k", C.c_int), ("eig", _dp), ("deig", _dp), ("ncut", _ip),
                 ("k_status", _ip), ("entropy", C.c_double), ("free_energy", C.c_double),
                 ("entropy_shift", C.c_double), ("earg1", C.c_double), ("earg2", C.c_double),
-                ("smag", C.c_double)]
+                ("smag", C.c_double), ("orbocc", _dp)]
 
 
 _vp = C.c_void_p
@@ -125,6 +125,7 @@ HOST_SYMBOLS = [
     ("nrltb_parfile_read", C.c_int, [C.c_char_p, C.POINTER(_vp), _pp]),
     ("nrltb_parfile_close", None, [_vp]),
     ("nrltb_nparams", C.c_int, [C.c_int]),
+    ("nrltb_qlmt_write", C.c_int, [C.c_char_p, C.c_int, C.c_int, _sp, _pp, _kp, C.c_double, _rp]),
 ]
 
 _cache = {}

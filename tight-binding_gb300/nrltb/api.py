@@ -170,17 +170,21 @@ class Result:
     earg1: float = 0.0
     earg2: float = 0.0
     smag: float = 0.0
+    orbocc: np.ndarray = None   # (jspins*nk, nv states, nv orbitals), modes 5, 6, 10
 
 
-def new_result(nv, nk, want_eig=True, want_deig=True, jspins=1):
-    """Result struct with per-k arrays of jspins * nk rows (spin 1's k points first)."""
+def new_result(nv, nk, want_eig=True, want_deig=True, jspins=1, want_orbocc=False):
+    """Result struct with per-k arrays of jspins * nk rows (spin 1's k points
+    first); want_orbocc adds the (rows, states, orbitals) Lowdin charges."""
     nrow = max(jspins, 1) * nk
     arrays = dict(eig=np.zeros((nrow, nv)) if want_eig else None,
                   deig=np.zeros((nrow, nv)) if want_deig else None,
-                  ncut=np.zeros(nrow, np.int32), k_status=np.zeros(nrow, np.int32))
+                  ncut=np.zeros(nrow, np.int32), k_status=np.zeros(nrow, np.int32),
+                  orbocc=np.zeros((nrow, nv, nv)) if want_orbocc else None)
     r = abi.Result_()
     r.eig = _dptr(arrays["eig"])
     r.deig = _dptr(arrays["deig"])
+    r.orbocc = _dptr(arrays["orbocc"])
     r.ncut = _iptr(arrays["ncut"])
     r.k_status = _iptr(arrays["k_status"])
     r._keep = arrays
@@ -192,6 +196,25 @@ def result_from_c(r, arrays):
                   r.nk, r.kneigh_out, r.nonphysical_k, **arrays, entropy=r.entropy,
                   free_energy=r.free_energy, entropy_shift=r.entropy_shift, earg1=r.earg1,
                   earg2=r.earg2, smag=r.smag)
+
+
+def write_qlmt(path, mode, st, par, km, eigcut, result, append=False, lib=None):
+    """Append (or start) the QLMT / QAPW records of one structure through the C
+    writer nrltb_qlmt_write: result is a Result with eig (and orbocc in modes 6
+    and 10) for par.jspins spin blocks."""
+    lib = lib or abi.load_host()
+    keep = [np.ascontiguousarray(result.eig, dtype=np.float64)]
+    r = abi.Result_()
+    r.nv, r.nk = result.nv, result.nk
+    r.eig = _dptr(keep[0])
+    if result.orbocc is not None:
+        keep.append(np.ascontiguousarray(result.orbocc, dtype=np.float64))
+        r.orbocc = _dptr(keep[1])
+    cs, cp, ck = st.to_c(), par.to_c(), km.to_c()
+    rc = lib.nrltb_qlmt_write(os.fsencode(path), int(append), mode, C.byref(cs), C.byref(cp), C.byref(ck),
+                              float(eigcut), C.byref(r))
+    if rc != 0:
+        raise RuntimeError(f"nrltb_qlmt_write returned {rc}")
 
 
 def new_pairs(capacity):
@@ -312,9 +335,11 @@ class Context:
     def launch_count(self):
         return int(self.lib.nrltb_ctx_launch_count(self.h))
 
-    def bande(self, st, par, km, opts, want_eig=True):
+    def bande(self, st, par, km, opts, want_eig=True, want_orbocc=None):
         nv, nk = par.nv(st), km.nk
-        r, arrays = new_result(nv, nk, want_eig, want_eig, par.jspins)
+        if want_orbocc is None:
+            want_orbocc = opts.mode in (5, 6, 10)
+        r, arrays = new_result(nv, nk, want_eig, want_eig, par.jspins, want_orbocc)
         cs, cp, ck, co = st.to_c(), par.to_c(), km.to_c(), opts.to_c()
         self._check(self.lib.nrltb_bande(self.h, C.byref(cs), C.byref(cp), C.byref(ck),
                                          C.byref(co), C.byref(r)), "nrltb_bande")

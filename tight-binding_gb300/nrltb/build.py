@@ -17,6 +17,7 @@ HOST = os.path.join(PKG_ROOT, "host")
 INCLUDE = os.path.join(REPO_ROOT, "include")
 OBJ = os.path.join(LIB_DIR, "obj")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+HOST_SOURCES = ["nrltb_input.c", "nrltb_qlmt.c"]
 CU_SOURCES = ["nrltb_api.cu", "eig.cu", "setup.cu", "sums.cu", "refine.cu", "ozaki.cu", "gemm_tc.cu", "gemm_umma.cu", "bench_hooks.cu", "noalloc.cu"]
 DRIVER = os.path.join(LIB_DIR, "nrltb_static")
 
@@ -59,19 +60,22 @@ def build_all(force=False, verbose=False):
         o = os.path.join(OBJ, src.replace(".cu", ".o"))
         if force or _stale(o, [s] + hdrs):
             jobs.append([nvcc] + ARCH + cflags + ["-c", s, "-o", o])
-    hsrc = os.path.join(HOST, "nrltb_input.c")
-    ho = os.path.join(OBJ, "nrltb_input.o")
-    if force or _stale(ho, [hsrc] + hdrs):
-        jobs.append(["gcc", "-std=gnu11", "-O2", "-ffp-contract=off", "-fPIC", "-Wall", "-I", INCLUDE, "-c", hsrc,
-                     "-o", ho])
+    hos = []
+    for src in HOST_SOURCES:
+        hsrc = os.path.join(HOST, src)
+        ho = os.path.join(OBJ, src.replace(".c", ".o"))
+        hos.append(ho)
+        if force or _stale(ho, [hsrc] + hdrs):
+            jobs.append(["gcc", "-std=gnu11", "-O2", "-ffp-contract=off", "-fPIC", "-Wall", "-I", INCLUDE, "-c",
+                         hsrc, "-o", ho])
     with cf.ThreadPoolExecutor(max_workers=min(8, max(1, os.cpu_count() or 1))) as ex:
         list(ex.map(_run, jobs))
-    objs = [os.path.join(OBJ, s.replace(".cu", ".o")) for s in CU_SOURCES] + [ho]
+    objs = [os.path.join(OBJ, s.replace(".cu", ".o")) for s in CU_SOURCES] + hos
     if force or _stale(GPU_LIB, objs):
         _run([nvcc] + ARCH + ["-shared", "-o", GPU_LIB + ".tmp"] + objs + ["-lcudart"])
         os.replace(GPU_LIB + ".tmp", GPU_LIB)
-    if force or _stale(HOST_LIB, [ho]):
-        _run(["gcc", "-shared", "-o", HOST_LIB + ".tmp", ho, "-lm"])
+    if force or _stale(HOST_LIB, hos):
+        _run(["gcc", "-shared", "-o", HOST_LIB + ".tmp"] + hos + ["-lm"])
         os.replace(HOST_LIB + ".tmp", HOST_LIB)
     dsrc = os.path.join(HOST, "nrltb_static.c")
     if os.path.exists(dsrc) and (force or _stale(DRIVER, [dsrc, GPU_LIB] + hdrs)):
