@@ -60,6 +60,10 @@ typedef struct {
                            /* atom's spin is flipped (input1.f:778-787 magdir 2),*/
                            /* its density and on-site terms then take the other */
                            /* spin's parameters (setpar.f:500-536, 806-867)      */
+    const double *spinat;  /* optional [natoms][3] unit spin direction per atom:  */
+                           /* non-collinear spins (input1.f:754-771, flag N),    */
+                           /* jspins = 2 sets, a 2N x 2N problem; flips ignored. */
+                           /* The GPU path returns NRLTB_E_UNSUPPORTED for it    */
 } nrltb_structure;
 
 /*

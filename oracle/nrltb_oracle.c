@@ -250,7 +250,7 @@ static int setpar_chan(const nrltb_structure *st, const nrltb_params *par, int j
 
 /* setparv (src/setparv.f:426-886), collinear, spin channel js */
 static int setparv_chan(const nrltb_structure *st, const nrltb_params *par, int js, const nrltb_pairs *pr,
-                        const double *den, double *dhop, double *dover, double *dparos)
+                        const double *den, double *dhop, double *dover, double *dparos, double *vden_out)
 {
     const int kinds = par->kinds;
     const double *P = chan_params(par, js);
@@ -343,6 +343,7 @@ static int setparv_chan(const nrltb_structure *st, const nrltb_params *par, int 
             }
         }
     }
+    if (vden_out) memcpy(vden_out, vden, sizeof(double) * (size_t)st->natoms * kinds);
     free(vden);
     return NRLTB_OK;
 }
@@ -356,7 +357,7 @@ int oracle_setpar(const nrltb_structure *st, const nrltb_params *par, const nrlt
 int oracle_setparv(const nrltb_structure *st, const nrltb_params *par, const nrltb_pairs *pr,
                    const double *den, double *dhop, double *dover, double *dparos)
 {
-    return setparv_chan(st, par, 0, pr, den, dhop, dover, dparos);
+    return setparv_chan(st, par, 0, pr, den, dhop, dover, dparos, NULL);
 }
 
 /* ---------------------------------------------------------------------- */
@@ -790,6 +791,145 @@ int oracle_diag_dense(int nv, int nk, const double *hd, const double *sd, double
 /* ---------------------------------------------------------------------- */
 /* bande (src/bande.f:816-1446) for one structure, k loop parallel over
  * threads (the reference's k data parallelism, one k per thread).          */
+/* ---------------------------------------------------------------------- */
+/* Non-collinear spins (lnoncol).  The densities are those of the two
+ * parameter sets (setpar.f:466-490, setparv.f:466-496); the on-site terms are
+ * the average and half difference of the two sets' polynomials, rotated onto
+ * each atom's spin direction later (spinham.f, addspins.f).  Hopping and
+ * overlap integrals come from the first set.
+ *
+ * Cross-species on-site terms are restated as the reference has them, which
+ * differs from its collinear form: setpar.f:768-794 replaces (not adds) the
+ * average, takes 4 coefficients per orbital class with stride 4 and a full
+ * difference for spinos; setparv.f:771-795 replaces the derivatives, takes
+ * the first set's density derivative for both spins and a stride of 3.     */
+static void onsite_noncol(const nrltb_structure *st, const nrltb_params *par, const double *den1, const double *den2,
+                          const double *vden1, const double *vden2, double *paros, double *spinos, double *dparos,
+                          double *dspnos)
+{
+    const int kinds = par->kinds;
+    const double *P1 = chan_params(par, 0), *P2 = chan_params(par, 1);
+    const double third = 1.0 / 3.0, twtrd = 2.0 / 3.0, threeh = 1.5, half = 0.5;
+    for (int iat = 0; iat < st->natoms; ++iat) {
+        const int jk1 = st->kkind[iat];
+        const double *d1 = den1 + (size_t)iat * kinds, *d2 = den2 + (size_t)iat * kinds;
+        int ip = ip_density(jk1);
+        double vm23up = pow(d1[jk1 - 1], twtrd), vm23dn = pow(d2[jk1 - 1], twtrd);
+        for (int k = 0; k < 4; ++k) {
+            double pup = P1[ip + 1] + vm23up * (P1[ip + 2] + vm23up * (P1[ip + 3] + vm23up * P1[ip + 4]));
+            double pdn = P2[ip + 1] + vm23dn * (P2[ip + 2] + vm23dn * (P2[ip + 3] + vm23dn * P2[ip + 4]));
+            paros[4 * iat + k] = half * (pup + pdn);
+            spinos[4 * iat + k] = half * (pup - pdn);
+            ip += 4;
+        }
+        for (int jk2 = 1; jk2 <= kinds; ++jk2) {
+            if (jk2 == jk1 || !((d1[jk2 - 1] > d2[jk2 - 1] ? d1[jk2 - 1] : d2[jk2 - 1]) > 0.0)) continue;
+            vm23up = pow(d1[jk2 - 1], twtrd);
+            vm23dn = pow(d2[jk2 - 1], twtrd);
+            ip = ip_cross_onsite(kinds, jk1, jk2);
+            for (int k = 0; k < 4; ++k) {
+                double pup = P1[ip + 1] + vm23up * (P1[ip + 2] + vm23up * (P1[ip + 3] + vm23up * P1[ip + 4]));
+                double pdn = P2[ip + 1] + vm23dn * (P2[ip + 2] + vm23dn * (P2[ip + 3] + vm23dn * P2[ip + 4]));
+                paros[4 * iat + k] = half * (pup + pdn);
+                spinos[4 * iat + k] = pup - pdn;
+                ip += 4;
+            }
+        }
+        if (!dparos) continue;
+        const double *v1 = vden1 + (size_t)iat * kinds, *v2 = vden2 + (size_t)iat * kinds;
+        ip = ip_density(jk1);
+        double vm13up = pow(d1[jk1 - 1], third), vm13dn = pow(d2[jk1 - 1], third);
+        vm23up = vm13up * vm13up;
+        vm23dn = vm13dn * vm13dn;
+        double vm2tup = 2.0 * vm23up, vm3tup = threeh * vm23up, vm2tdn = 2.0 * vm23dn, vm3tdn = threeh * vm23dn;
+        double drhoup = twtrd * v1[jk1 - 1] / vm13up, drhodn = twtrd * v2[jk1 - 1] / vm13dn;
+        for (int k = 0; k < 4; ++k) {
+            double dpup = drhoup * (P1[ip + 2] + vm2tup * (P1[ip + 3] + vm3tup * P1[ip + 4]));
+            double dpdn = drhodn * (P2[ip + 2] + vm2tdn * (P2[ip + 3] + vm3tdn * P2[ip + 4]));
+            dparos[4 * iat + k] = half * (dpup + dpdn);
+            dspnos[4 * iat + k] = half * (dpup - dpdn);
+            ip += 4;
+        }
+        for (int jk2 = 1; jk2 <= kinds; ++jk2) {
+            if (jk2 == jk1 || d1[jk2 - 1] == 0.0) continue;
+            vm13up = pow(d1[jk2 - 1], third);
+            vm23up = vm13up * vm13up;
+            vm2tup = 2.0 * vm23up;
+            vm3tup = threeh * vm23up;
+            drhoup = twtrd * v1[jk2 - 1] / vm13up;
+            vm13dn = pow(d2[jk2 - 1], third);
+            vm23dn = vm13dn * vm13dn;
+            vm2tdn = 2.0 * vm23dn;
+            vm3tdn = threeh * vm23dn;
+            drhodn = twtrd * v1[jk2 - 1] / vm13dn;
+            ip = ip_cross_onsite(kinds, jk1, jk2);
+            for (int k = 0; k < 4; ++k) {
+                double dpup = drhoup * (P1[ip + 2] + vm2tup * (P1[ip + 3] + vm3tup * P1[ip + 4]));
+                double dpdn = drhodn * (P2[ip + 2] + vm2tdn * (P2[ip + 3] + vm3tdn * P2[ip + 4]));
+                dparos[4 * iat + k] = half * (dpup + dpdn);
+                dspnos[4 * iat + k] = half * (dpup - dpdn);
+                ip += 3;
+            }
+        }
+    }
+}
+
+/* The non-collinear on-site terms alone, for a given pair list (test entry). */
+int oracle_noncol_onsite(const nrltb_structure *st, const nrltb_params *par, const nrltb_pairs *pr, double *paros,
+                         double *spinos)
+{
+    if (par->jspins != 2) return NRLTB_E_ARG;
+    nrltb_structure stn = *st;
+    stn.flip = NULL;
+    const size_t P = (size_t)pr->npairs, na = (size_t)st->natoms, nkd = na * par->kinds;
+    double *h = calloc(14 * P + 1, 8), *o = calloc(14 * P + 1, 8), *t = calloc(4 * na, 8);
+    double *den1 = calloc(nkd, 8), *den2 = calloc(nkd, 8);
+    setpar_chan(&stn, par, 0, pr, h, o, t, den1);
+    setpar_chan(&stn, par, 1, pr, h, o, t, den2);
+    onsite_noncol(st, par, den1, den2, NULL, NULL, paros, spinos, NULL, NULL);
+    free(h); free(o); free(t); free(den1); free(den2);
+    return NRLTB_OK;
+}
+
+/* spinham.f:122-158: per orbital the diagonal and mixing spin terms of
+ * spinos (or its volume derivative) along each atom's direction */
+static void spinham(const nrltb_structure *st, const nrltb_params *par, const double *spinos, double *diag, zc *mix)
+{
+    int i = 0;
+    for (int j = 0; j < st->natoms; ++j) {
+        const int nb = par->kbas[st->kkind[j] - 1];
+        for (int k = 1; k <= nb; ++k, ++i) {
+            const int q = (k == 1) ? 0 : (k < 5) ? 1 : (k < 8) ? 2 : 3;
+            const double so = spinos[4 * j + q];
+            const double *m = st->spinat + 3 * j;
+            diag[i] = so * m[2];
+            mix[i] = so * m[0] + I * (so * m[1]);
+        }
+    }
+}
+
+/* addspins.f:77-110: the packed-upper N x N H and S into 2N x 2N:
+ * [H + D, M; M^H, H - D] and [S, 0; 0, S], D = diag(diag), M = diag(mix) */
+static void addspins(int nv, const double *diag, const zc *mix, const zc *h, const zc *s, zc *h2, zc *s2)
+{
+    const int n2 = 2 * nv;
+    memset(h2, 0, sizeof(zc) * (size_t)n2 * (n2 + 1) / 2);
+    memset(s2, 0, sizeof(zc) * (size_t)n2 * (n2 + 1) / 2);
+    for (int j = 0; j < nv; ++j) {
+        for (int i = 0; i < j; ++i) {
+            h2[pk(i, j)] = h[pk(i, j)];
+            s2[pk(i, j)] = s[pk(i, j)];
+            h2[pk(i + nv, j + nv)] = h[pk(i, j)];
+            s2[pk(i + nv, j + nv)] = s[pk(i, j)];
+        }
+        h2[pk(j + nv, j + nv)] = h[pk(j, j)] - diag[j];
+        s2[pk(j + nv, j + nv)] = s[pk(j, j)];
+        h2[pk(j, j)] = h[pk(j, j)] + diag[j];
+        s2[pk(j, j)] = s[pk(j, j)];
+        h2[pk(j, j + nv)] = mix[j];
+    }
+}
+
 /* diag.f:526-700: Lowdin charges |(U z_k)_i|^2 of every state k, U = S^1/2 formed
  * from zhpev's eigenpairs of S as diag.f:603-614 forms it (U = 1 for an
  * orthogonal set); sp is S packed upper, z the S-orthonormal eigenvectors
@@ -831,9 +971,12 @@ int oracle_bande(const nrltb_structure *st, const nrltb_params *par, const nrltb
                  const nrltb_opts *opt, nrltb_result *res, int nthreads)
 {
     if (!p_zhpgv || !p_zhpev) return NRLTB_E_ARG;
-    /* bande.f:711-730: spin channels, pressure and entropy switches */
-    const int nsp = (par->jspins == 2) ? 2 : 1;
-    if (nsp == 1 && st->flip)
+    /* bande.f:694-730: spin channels (two for a collinear two-set run, one
+     * doubled problem for non-collinear spins), pressure and entropy switches */
+    const int noncol = st->spinat != NULL;
+    if (noncol && par->jspins != 2) return NRLTB_E_ARG;   /* bande.f:696-702 */
+    const int nsp = (!noncol && par->jspins == 2) ? 2 : 1;
+    if (!noncol && nsp == 1 && st->flip)
         for (int i = 0; i < st->natoms; ++i)
             if (st->flip[i]) return NRLTB_E_ARG;   /* spin flips need two parameter sets */
     int lpress = (opt->mode == 2 || opt->mode == 4);
@@ -841,6 +984,7 @@ int oracle_bande(const nrltb_structure *st, const nrltb_params *par, const nrltb
     int nv = 0;
     double zfill = st->zcharge;
     for (int i = 0; i < st->natoms; ++i) { nv += par->kbas[st->kkind[i] - 1]; zfill += par->valence[st->kkind[i] - 1]; }
+    const int nvx = noncol ? 2 * nv : nv;   /* order of the secular equation */
     nrltb_pairs pr;
     long cap = pair_bound(st);
     if (alloc_pairs(&pr, (int)cap)) return NRLTB_E_NOMEM;
@@ -848,52 +992,86 @@ int oracle_bande(const nrltb_structure *st, const nrltb_params *par, const nrltb
     double dismin = 0;
     oracle_search2(st, par, opt->kneigh_in, &pr, &kneigh_out, &dismin);
     size_t P = (size_t)pr.npairs;
+    const size_t na = (size_t)st->natoms, nkd = na * par->kinds;
     double *hop = calloc(14 * P + 1, 8), *over = calloc(14 * P + 1, 8);
-    double *paros = calloc(4 * (size_t)st->natoms, 8), *den = calloc((size_t)st->natoms * par->kinds, 8);
-    double *dhop = calloc(14 * P + 1, 8), *dover = calloc(14 * P + 1, 8), *dparos = calloc(4 * (size_t)st->natoms, 8);
+    double *paros = calloc(4 * na, 8), *den = calloc(nkd, 8);
+    double *dhop = calloc(14 * P + 1, 8), *dover = calloc(14 * P + 1, 8), *dparos = calloc(4 * na, 8);
+    /* non-collinear: spin splittings and their rotated matrix terms */
+    double *sdiag = NULL, *dsdiag = NULL;
+    zc *smix = NULL, *dsmix = NULL;
+    if (noncol) {
+        nrltb_structure stn = *st;
+        stn.flip = NULL;   /* lnoncol overrides spin flips (input1.f:259-262) */
+        double *den2 = calloc(nkd, 8), *vden1 = calloc(nkd, 8), *vden2 = calloc(nkd, 8);
+        double *tmp = calloc(14 * P + 1, 8), *tmp2 = calloc(14 * P + 1, 8), *tpar = calloc(4 * na, 8);
+        double *spinos = calloc(4 * na, 8), *dspnos = calloc(4 * na, 8);
+        setpar_chan(&stn, par, 0, &pr, hop, over, tpar, den);
+        setpar_chan(&stn, par, 1, &pr, tmp, tmp2, tpar, den2);
+        if (lpress) {
+            setparv_chan(&stn, par, 0, &pr, den, dhop, dover, tpar, vden1);
+            setparv_chan(&stn, par, 1, &pr, den2, tmp, tmp2, tpar, vden2);
+        }
+        onsite_noncol(st, par, den, den2, vden1, vden2, paros, spinos, lpress ? dparos : NULL, dspnos);
+        sdiag = malloc(sizeof(double) * nv);
+        smix = malloc(sizeof(zc) * nv);
+        spinham(st, par, spinos, sdiag, smix);
+        if (lpress) {
+            dsdiag = malloc(sizeof(double) * nv);
+            dsmix = malloc(sizeof(zc) * nv);
+            spinham(st, par, dspnos, dsdiag, dsmix);
+        }
+        free(den2); free(vden1); free(vden2); free(tmp); free(tmp2); free(tpar); free(spinos); free(dspnos);
+    }
     const int nk = km->nk, nrow = nsp * nk;   /* rows: spin 1's k points, then spin 2's */
-    double *esk = malloc(sizeof(double) * (size_t)nv * nrow);
-    double *desk = calloc((size_t)nv * nrow, sizeof(double));
+    double *esk = malloc(sizeof(double) * (size_t)nvx * nrow);
+    double *desk = calloc((size_t)nvx * nrow, sizeof(double));
     double *wrow = malloc(sizeof(double) * (size_t)nrow);
     int *ncut = calloc((size_t)nrow, sizeof(int));
     int *kst = calloc((size_t)nrow, sizeof(int));
     for (int r = 0; r < nrow; ++r) wrow[r] = km->w[r % nk];
-    size_t np = (size_t)nv * (nv + 1) / 2;
+    const size_t np = (size_t)nv * (nv + 1) / 2, npx = (size_t)nvx * (nvx + 1) / 2;
 #ifdef _OPENMP
     if (nthreads > 0) omp_set_num_threads(nthreads);
 #endif
     for (int js = 0; js < nsp; ++js) {   /* bande.f:816 */
-        setpar_chan(st, par, js, &pr, hop, over, paros, den);
-        if (lpress) setparv_chan(st, par, js, &pr, den, dhop, dover, dparos);
+        if (!noncol) {
+            setpar_chan(st, par, js, &pr, hop, over, paros, den);
+            if (lpress) setparv_chan(st, par, js, &pr, den, dhop, dover, dparos, NULL);
+        }
 #pragma omp parallel for schedule(dynamic, 1)
         for (int k = 0; k < nk; ++k) {
             const int r = js * nk + k;
             zc *hp = malloc(sizeof(zc) * np), *sp = malloc(sizeof(zc) * np);
-            zc *z = (lpress || lqlmt) ? malloc(sizeof(zc) * (size_t)nv * nv) : NULL;
-            zc *sc = lqlmt ? malloc(sizeof(zc) * np) : NULL;
+            zc *hx = hp, *sx = sp;
+            if (noncol) { hx = malloc(sizeof(zc) * npx); sx = malloc(sizeof(zc) * npx); }
+            zc *z = (lpress || lqlmt) ? malloc(sizeof(zc) * (size_t)nvx * nvx) : NULL;
+            zc *sc = lqlmt ? malloc(sizeof(zc) * npx) : NULL;
             oracle_setham_packed(st, par, &pr, hop, over, paros, km->k + 3 * k, 0, hp, sp);
-            if (sc) memcpy(sc, sp, sizeof(zc) * np);
-            int ioverr = oracle_diag_packed(nv, lpress || lqlmt, par->jsover, hp, sp, esk + (size_t)r * nv, z);
+            if (noncol) addspins(nv, sdiag, smix, hp, sp, hx, sx);   /* bande.f:955-958 */
+            if (sc) memcpy(sc, sx, sizeof(zc) * npx);
+            int ioverr = oracle_diag_packed(nvx, lpress || lqlmt, par->jsover, hx, sx, esk + (size_t)r * nvx, z);
             kst[r] = ioverr ? NRLTB_K_S_NOT_PD : NRLTB_K_OK;
             if (lqlmt) {
-                double *orb = res->orbocc + (size_t)r * nv * nv;
-                if (ioverr) for (size_t i = 0; i < (size_t)nv * nv; ++i) orb[i] = -1.0;
-                else oracle_lowdin(nv, par->jsover, sc, z, orb);
+                double *orb = res->orbocc + (size_t)r * nvx * nvx;
+                if (ioverr) for (size_t i = 0; i < (size_t)nvx * nvx; ++i) orb[i] = -1.0;
+                else oracle_lowdin(nvx, par->jsover, sc, z, orb);
             }
             free(sc);
             if (!ioverr && lpress) {
                 oracle_setham_packed(st, par, &pr, dhop, dover, dparos, km->k + 3 * k, 1, hp, sp);
-                if (!par->jsover) for (size_t i = 0; i < np; ++i) sp[i] = 0;
-                oracle_perturb(nv, hp, sp, z, esk + (size_t)r * nv, opt->eigcut, &ncut[r], desk + (size_t)r * nv);
+                if (noncol) addspins(nv, dsdiag, dsmix, hp, sp, hx, sx);   /* bande.f:1033-1034 */
+                if (!par->jsover) for (size_t i = 0; i < npx; ++i) sx[i] = 0;
+                oracle_perturb(nvx, hx, sx, z, esk + (size_t)r * nvx, opt->eigcut, &ncut[r], desk + (size_t)r * nvx);
             }
+            if (noncol) { free(hx); free(sx); }
             free(hp); free(sp); free(z);
         }
     }
     /* fermi.f with el = sfac electrons per band (bande.f:1065-1080), then the
      * sums of bande.f:1162-1330 in the reference's spin-then-k order */
-    const double sfac = (nsp == 2) ? 1.0 : 2.0;
+    const double sfac = (nsp == 2 || noncol) ? 1.0 : 2.0;
     double tkb = opt->tkb;
-    double efermi = oracle_fermi_el(nv, nrow, esk, wrow, tkb, zfill, opt->fermi_tol, sfac, NULL);
+    double efermi = oracle_fermi_el(nvx, nrow, esk, wrow, tkb, zfill, opt->fermi_tol, sfac, NULL);
     double tkbi = (tkb < 1e-5) ? 1e5 : 1.0 / tkb;
 #define FB(x) (1.0 / (1.0 + exp(tkbi * (x))))
     double etol = 20.0 * tkb, efp = efermi + etol, efm = efermi - etol;
@@ -901,9 +1079,9 @@ int oracle_bande(const nrltb_structure *st, const nrltb_params *par, const nrltb
     double entropy = 0, dent1 = 0, dent2 = 0;
     const int lentro = opt->mode < 3;
     for (int r = 0; r < nrow; ++r) {
-        const double *e = esk + (size_t)r * nv, *de = desk + (size_t)r * nv;
+        const double *e = esk + (size_t)r * nvx, *de = desk + (size_t)r * nvx;
         double wt = sfac * wrow[r];
-        int nlim = lpress ? ncut[r] : nv;
+        int nlim = lpress ? ncut[r] : nvx;
         for (int i = 0; i < nlim; ++i) {
             if (!(e[i] < efp)) continue;
             double ewt = wt * e[i];
@@ -932,15 +1110,15 @@ int oracle_bande(const nrltb_structure *st, const nrltb_params *par, const nrltb
             }
         }
     }
-    /* spin populations and moment, bande.f:1336-1395 (all nv states, weight
+    /* spin populations and moment, bande.f:1336-1395 (all states, weight
      * without sfac, which is 1 here) */
     double smag = 0.0;
     if (nsp == 2) {
         for (int js = 0; js < 2; ++js) {
             double sptemp = 0.0;
             for (int k = 0; k < nk; ++k) {
-                const double *e = esk + (size_t)(js * nk + k) * nv;
-                for (int i = 0; i < nv; ++i) {
+                const double *e = esk + (size_t)(js * nk + k) * nvx;
+                for (int i = 0; i < nvx; ++i) {
                     if (e[i] < efm) sptemp = sptemp + km->w[k];
                     else if (e[i] < efp) sptemp = sptemp + km->w[k] * FB(e[i] - efermi);
                 }
@@ -977,16 +1155,17 @@ int oracle_bande(const nrltb_structure *st, const nrltb_params *par, const nrltb
     res->smag = smag;
     res->dismin = dismin;
     res->npairs = pr.npairs;
-    res->nv = nv;
+    res->nv = nvx;
     res->nk = nk;
     res->kneigh_out = kneigh_out;
     res->nonphysical_k = 0;
     for (int r = 0; r < nrow; ++r) res->nonphysical_k += (kst[r] != 0);
-    if (res->eig) memcpy(res->eig, esk, sizeof(double) * (size_t)nv * nrow);
-    if (res->deig) memcpy(res->deig, desk, sizeof(double) * (size_t)nv * nrow);
+    if (res->eig) memcpy(res->eig, esk, sizeof(double) * (size_t)nvx * nrow);
+    if (res->deig) memcpy(res->deig, desk, sizeof(double) * (size_t)nvx * nrow);
     if (res->ncut) memcpy(res->ncut, ncut, sizeof(int) * (size_t)nrow);
     if (res->k_status) memcpy(res->k_status, kst, sizeof(int) * (size_t)nrow);
     free(esk); free(desk); free(wrow); free(ncut); free(kst);
+    free(sdiag); free(smix); free(dsdiag); free(dsmix);
     free(hop); free(over); free(paros); free(den); free(dhop); free(dover); free(dparos);
     free_pairs(&pr);
     return NRLTB_OK;

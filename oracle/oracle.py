@@ -69,6 +69,7 @@ def load():
         ("oracle_bande", [vp, vp, vp, vp, vp, C.c_int]),
         ("oracle_ksolve_sample", [vp, vp, vp, vp, C.c_int, C.c_int, C.c_int, vp]),
         ("oracle_pair_bound", [vp]),
+        ("oracle_noncol_onsite", [vp, vp, vp, vp, vp]),
     ]:
         fn = getattr(lib, name)
         fn.argtypes = args
@@ -118,6 +119,17 @@ def setpar(st, par, pairs, deriv=True):
     return out
 
 
+def noncol_onsite(st, par, pairs):
+    """Non-collinear on-site average and splitting per atom and orbital class."""
+    from nrltb import api
+    lib = load()
+    cs, cp, cpr = st.to_c(), par.to_c(), api.pairs_to_c(pairs)
+    paros, spinos = np.zeros((st.natoms, 4)), np.zeros((st.natoms, 4))
+    rc = lib.oracle_noncol_onsite(_ref(cs), _ref(cp), _ref(cpr), _p(paros), _p(spinos))
+    assert rc == 0, rc
+    return paros, spinos
+
+
 def setham(st, par, km, which=0, kneigh_in=0):
     """Dense Hermitian H, S (which=0) or dH, dS (which=1): (nk, nv, nv) complex."""
     lib = load()
@@ -156,7 +168,11 @@ def bande(st, par, km, opts, nthreads=0):
     from nrltb import api
     lib = load()
     nv, nk = par.nv(st), km.nk
-    r, arrays = api.new_result(nv, nk, jspins=par.jspins, want_orbocc=opts.mode in (5, 6, 10))
+    if st.spinat is not None:   # non-collinear: one 2N x 2N problem per k
+        nv, jsp = 2 * nv, 1
+    else:
+        jsp = par.jspins
+    r, arrays = api.new_result(nv, nk, jspins=jsp, want_orbocc=opts.mode in (5, 6, 10))
     cs, cp, ck, co = st.to_c(), par.to_c(), km.to_c(), opts.to_c()
     rc = lib.oracle_bande(_ref(cs), _ref(cp), _ref(ck), _ref(co), _ref(r), nthreads)
     assert rc == 0, rc

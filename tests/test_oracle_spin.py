@@ -150,8 +150,10 @@ def test_reader_magnetic_file_and_flips(tmp_path, mag, km):
     assert s3.flip is None
 
 
-@pytest.mark.parametrize("flag", ["N", "D", "S"])
-def test_reader_non_collinear_flags_are_refused(tmp_path, km, flag):
+@pytest.mark.parametrize("flag,code", [("D", "-7"), ("S", "-7"), ("N", "-5")])
+def test_reader_non_collinear_flags_are_refused(tmp_path, km, flag, code):
+    """Torque (D) and spin-direction (S) runs are not built; N is, but needs a
+    direction (theta, phi) on every atom line."""
     d = str(tmp_path)
     synth.write_skin(d, [(_cscl(), km)], synth.make_params([9], [10.0], 7), mode=4, tkb=TKB)
     path = os.path.join(d, "SKIN")
@@ -159,5 +161,5 @@ def test_reader_non_collinear_flags_are_refused(tmp_path, km, flag):
     i = next(j for j, ln in enumerate(lines) if ln == "F")
     lines[i] = "F" + flag
     open(path, "w").write("\n".join(lines) + "\n")
-    with pytest.raises(RuntimeError, match="-7"):
+    with pytest.raises(RuntimeError, match=code):
         read_skin(path)

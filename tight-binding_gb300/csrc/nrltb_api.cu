@@ -223,6 +223,7 @@ static int check_inputs(const nrltb_structure *st, const nrltb_params *par)
         return NRLTB_E_ARG;
     }
     if (par->jspins < 0 || par->jspins > 2) { set_err("jspins %d", par->jspins); return NRLTB_E_ARG; }
+    if (st->spinat) { set_err("non-collinear spins are not built on the GPU path"); return NRLTB_E_UNSUPPORTED; }
     if (par->jspins != 2 && st->flip)
         for (int i = 0; i < st->natoms; ++i)
             if (st->flip[i]) { set_err("atom %d is spin-flipped but the parameters have one spin", i + 1); return NRLTB_E_ARG; }

@@ -264,7 +264,7 @@ struct nrltb_skin {
     /* current structure */
     int natoms;
     int *kkind, *flip;
-    double *posn, *posq;
+    double *posn, *posq, *spinat;
     /* k list, kept across structures (kptin.f `save nk`) */
     int nk;
     double *kq, *kw;
@@ -1060,7 +1060,8 @@ int nrltb_skin_next(nrltb_skin *s, nrltb_structure *st, nrltb_kmesh *km, char *t
     /* input1.f:535-546: T spin flips (a magdir per atom); N, D, S non-collinear
      * runs (not built); anything else plain */
     int spinflip = (c2 == 'T' || c2 == 't');
-    if (c2 == 'N' || c2 == 'n' || c2 == 'D' || c2 == 'd' || c2 == 'S' || c2 == 's') { rc = NRLTB_E_UNSUPPORTED; goto fail; }
+    int noncol = (c2 == 'N' || c2 == 'n');   /* theta, phi per atom (input1.f:754-771) */
+    if (c2 == 'D' || c2 == 'd' || c2 == 'S' || c2 == 's') { rc = NRLTB_E_UNSUPPORTED; goto fail; }
     /* reciprocal vectors without 2 pi (input1.f:612-624) */
     double bvec[3][3];
     for (int i = 0; i < 3; ++i) {
@@ -1097,20 +1098,29 @@ int nrltb_skin_next(nrltb_skin *s, nrltb_structure *st, nrltb_kmesh *km, char *t
             }
         }
     }
-    free(s->kkind); free(s->flip); free(s->posn); free(s->posq);
+    free(s->kkind); free(s->flip); free(s->spinat); free(s->posn); free(s->posq);
     s->natoms = natoms;
     s->kkind = malloc(sizeof(int) * natoms);
     s->flip = calloc((size_t)natoms, sizeof(int));
+    s->spinat = calloc(3 * (size_t)natoms, sizeof(double));
     s->posn = malloc(sizeof(double) * 3 * natoms);
     s->posq = malloc(sizeof(double) * 3 * natoms);
-    if (!s->kkind || !s->flip || !s->posn || !s->posq) { free(shift); free(epsl); rc = NRLTB_E_NOMEM; goto fail; }
+    if (!s->kkind || !s->flip || !s->spinat || !s->posn || !s->posq) {
+        free(shift); free(epsl); rc = NRLTB_E_NOMEM; goto fail;
+    }
     int anyflip = 0;
+    const double deg2rad = 3.14159265358979323846 / 180.0;
     for (int i = 0; i < natoms; ++i) {
-        double v[8];
-        if (ld_reals(r, spinflip ? 8 : 7, v)) { free(shift); free(epsl); goto fail; }
+        double v[9];
+        if (ld_reals(r, noncol ? 9 : spinflip ? 8 : 7, v)) { free(shift); free(epsl); goto fail; }
         if (spinflip) {   /* input1.f:778-787: magdir 2 flips the atom */
             s->flip[i] = (v[7] == 2.0);
             anyflip |= s->flip[i];
+        }
+        if (noncol) {     /* unit vector from theta, phi in degrees (input1.f:760-762) */
+            s->spinat[3 * i] = sin(deg2rad * v[7]) * cos(deg2rad * v[8]);
+            s->spinat[3 * i + 1] = sin(deg2rad * v[7]) * sin(deg2rad * v[8]);
+            s->spinat[3 * i + 2] = cos(deg2rad * v[7]);
         }
         int kind = (int)v[0];
         double p[3] = {v[1], v[2], v[3]};
@@ -1145,6 +1155,7 @@ int nrltb_skin_next(nrltb_skin *s, nrltb_structure *st, nrltb_kmesh *km, char *t
     st->posn = s->posn;
     st->posq = s->posq;
     st->flip = anyflip ? s->flip : NULL;
+    st->spinat = noncol ? s->spinat : NULL;
     memcpy(st->plv, plv, sizeof plv);
     memcpy(st->nd, nd, sizeof nd);
     st->volume = vol;
@@ -1163,6 +1174,6 @@ void nrltb_skin_close(nrltb_skin *s)
     if (!s) return;
     lr_close(&s->r);
     nrltb_parfile_close(s->pf);
-    free(s->kkind); free(s->flip); free(s->posn); free(s->posq); free(s->kq); free(s->kw);
+    free(s->kkind); free(s->flip); free(s->spinat); free(s->posn); free(s->posq); free(s->kq); free(s->kw);
     free(s);
 }

@@ -66,6 +66,7 @@ int nrltb_qlmt_write(const char *path, int append, int mode, const nrltb_structu
     if (!path || !st || !par || !km || !res || !res->eig || !st->kkind || !par->kbas) return NRLTB_E_ARG;
     if (!(mode == 6 || mode == 8 || mode == 9 || mode == 10)) return NRLTB_E_UNSUPPORTED;
     if ((mode == 6 || mode == 10) && !res->orbocc) return NRLTB_E_ARG;
+    if (st->spinat) return NRLTB_E_UNSUPPORTED;   /* non-collinear records are not written */
     FILE *f = fopen(path, append ? "a" : "w");
     if (!f) return NRLTB_E_IO;
     const int nv = res->nv, nk = km->nk, nsp = (par->jspins == 2) ? 2 : 1;

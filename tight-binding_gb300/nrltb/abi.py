@@ -41,7 +41,7 @@ _ip = C.POINTER(C.c_int)
 class Structure_(C.Structure):
     _fields_ = [("natoms", C.c_int), ("kkind", _ip), ("posn", _dp), ("posq", _dp),
                 ("plv", (C.c_double * 3) * 3), ("nd", C.c_int * 3),
-                ("volume", C.c_double), ("zcharge", C.c_double), ("flip", _ip)]
+                ("volume", C.c_double), ("zcharge", C.c_double), ("flip", _ip), ("spinat", _dp)]
 
 
 class Params_(C.Structure):

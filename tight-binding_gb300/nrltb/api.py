@@ -33,6 +33,7 @@ class Structure:
     zcharge: float = 0.0
     posq: np.ndarray = None      # (natoms, 3) phase offsets, default zero
     flip: np.ndarray = None      # (natoms,) nonzero = spin flipped (two-spin sets only)
+    spinat: np.ndarray = None    # (natoms, 3) unit spin directions: non-collinear spins
 
     def __post_init__(self):
         self.kkind = np.ascontiguousarray(self.kkind, dtype=np.int32)
@@ -43,6 +44,8 @@ class Structure:
         self.posq = np.ascontiguousarray(self.posq, dtype=np.float64).reshape(-1, 3)
         if self.flip is not None:
             self.flip = np.ascontiguousarray(self.flip, dtype=np.int32).reshape(-1)
+        if self.spinat is not None:
+            self.spinat = np.ascontiguousarray(self.spinat, dtype=np.float64).reshape(-1, 3)
 
     @property
     def natoms(self):
@@ -61,6 +64,7 @@ class Structure:
         s.volume = float(self.volume)
         s.zcharge = float(self.zcharge)
         s.flip = _iptr(self.flip)
+        s.spinat = _dptr(self.spinat)
         s._keep = (self,)
         return s
 
@@ -290,7 +294,8 @@ def read_skin(path, lib=None):
                            np.array([[cs.plv[i][j] for j in range(3)] for i in range(3)]),
                            tuple(cs.nd), cs.volume, cs.zcharge,
                            np.ctypeslib.as_array(cs.posq, (n, 3)).copy(),
-                           np.ctypeslib.as_array(cs.flip, (n,)).copy() if cs.flip else None)
+                           np.ctypeslib.as_array(cs.flip, (n,)).copy() if cs.flip else None,
+                           np.ctypeslib.as_array(cs.spinat, (n, 3)).copy() if cs.spinat else None)
             km = KMesh(np.ctypeslib.as_array(ck.k, (ck.nk, 3)).copy(),
                        np.ctypeslib.as_array(ck.w, (ck.nk,)).copy())
             out.structures.append((title.value.decode(), label.value.decode(), st, km))

@@ -233,10 +233,17 @@ def write_skin(dirname, entries, par, mode=4, tkb=0.005, eigcut=1e3):
             f.write("0\n")
             for v in st.plv:
                 f.write("%.17g %.17g %.17g\n" % tuple(v))
-            flips = st.flip is not None
-            # (2a1) lphonon, spin flag: T means a magdir (1 up, 2 flipped) per atom
-            f.write("1 1 1\n0\n%d\n%d %d %d\n%s\n" % ((st.natoms,) + tuple(st.nd) + ("FT" if flips else "F",)))
+            flips, noncol = st.flip is not None, st.spinat is not None
+            # (2a1) lphonon, spin flag: T means a magdir (1 up, 2 flipped) per atom,
+            # N a spin direction (theta, phi in degrees) per atom
+            flag = "FN" if noncol else "FT" if flips else "F"
+            f.write("1 1 1\n0\n%d\n%d %d %d\n%s\n" % ((st.natoms,) + tuple(st.nd) + (flag,)))
             for i, (kk, p, q) in enumerate(zip(st.kkind, st.posn, st.posq)):
                 f.write("%d %.17g %.17g %.17g %.17g %.17g %.17g" % ((-int(kk),) + tuple(p) + tuple(q)))
-                f.write(" %d\n" % (2 if st.flip[i] else 1) if flips else "\n")
+                if noncol:
+                    m = st.spinat[i]
+                    f.write(" %.17g %.17g\n" % (math.degrees(math.acos(max(-1.0, min(1.0, m[2])))),
+                                                 math.degrees(math.atan2(m[1], m[0]))))
+                else:
+                    f.write(" %d\n" % (2 if st.flip[i] else 1) if flips else "\n")
             f.write("NEWSYM=T\nLATTIC=1\nsg\nILAT=F\n-1313\n%s\n" % kname)
