@@ -59,3 +59,16 @@ def test_bande_forms(ctx, case, nltype, jsover, precision):
     assert abs(g.efermi - o.efermi) <= 1e-9
     assert abs(g.e_total - o.e_total) / st.natoms <= 1e-8
     assert abs(g.pressure - o.pressure) <= 1e-3 * KBAR
+
+
+def test_setham_with_phase_offsets(ctx):
+    """Per-atom Bloch phase offsets (rotate.f:144-146) in the GPU Bloch sums."""
+    st, par, km, _ = synth.bcc32()
+    rng = np.random.default_rng(4)
+    st = Structure(st.kkind, st.posn, st.plv, st.nd, st.volume, st.zcharge, rng.uniform(-0.5, 0.5, (32, 3)))
+    sub = KMesh(km.k[[0, 9, 37, 63]], np.full(4, 0.25))
+    for which in (0, 1):
+        gh, gs = ctx.setham(st, par, sub, which)
+        oh, os_ = oracle.setham(st, par, sub, which)
+        for g, o in ((gh, oh), (gs, os_)):
+            assert np.abs(g - o).max() <= 1e-13 * max(np.abs(o).max(), 1e-300)
