@@ -62,8 +62,8 @@ typedef struct {
                            /* spin's parameters (setpar.f:500-536, 806-867)      */
     const double *spinat;  /* optional [natoms][3] unit spin direction per atom:  */
                            /* non-collinear spins (input1.f:754-771, flag N),    */
-                           /* jspins = 2 sets, a 2N x 2N problem; flips ignored. */
-                           /* The GPU path returns NRLTB_E_UNSUPPORTED for it    */
+                           /* jspins = 2 sets, a 2N x 2N problem (per-k outputs  */
+                           /* then have 2N columns, one block); flips ignored    */
 } nrltb_structure;
 
 /*

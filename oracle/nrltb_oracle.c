@@ -874,20 +874,24 @@ static void onsite_noncol(const nrltb_structure *st, const nrltb_params *par, co
     }
 }
 
-/* The non-collinear on-site terms alone, for a given pair list (test entry). */
-int oracle_noncol_onsite(const nrltb_structure *st, const nrltb_params *par, const nrltb_pairs *pr, double *paros,
-                         double *spinos)
+/* The non-collinear on-site terms for a given pair list (test entry): both
+ * sets' densities and their volume derivatives [natoms][kinds], and the
+ * on-site average, splitting and their derivatives [natoms][4]. */
+int oracle_noncol_onsite(const nrltb_structure *st, const nrltb_params *par, const nrltb_pairs *pr, double *den1,
+                         double *den2, double *vden1, double *vden2, double *paros, double *spinos, double *dparos,
+                         double *dspnos)
 {
     if (par->jspins != 2) return NRLTB_E_ARG;
     nrltb_structure stn = *st;
     stn.flip = NULL;
-    const size_t P = (size_t)pr->npairs, na = (size_t)st->natoms, nkd = na * par->kinds;
+    const size_t P = (size_t)pr->npairs, na = (size_t)st->natoms;
     double *h = calloc(14 * P + 1, 8), *o = calloc(14 * P + 1, 8), *t = calloc(4 * na, 8);
-    double *den1 = calloc(nkd, 8), *den2 = calloc(nkd, 8);
     setpar_chan(&stn, par, 0, pr, h, o, t, den1);
     setpar_chan(&stn, par, 1, pr, h, o, t, den2);
-    onsite_noncol(st, par, den1, den2, NULL, NULL, paros, spinos, NULL, NULL);
-    free(h); free(o); free(t); free(den1); free(den2);
+    setparv_chan(&stn, par, 0, pr, den1, h, o, t, vden1);
+    setparv_chan(&stn, par, 1, pr, den2, h, o, t, vden2);
+    onsite_noncol(st, par, den1, den2, vden1, vden2, paros, spinos, dparos, dspnos);
+    free(h); free(o); free(t);
     return NRLTB_OK;
 }
 

@@ -69,7 +69,7 @@ def load():
         ("oracle_bande", [vp, vp, vp, vp, vp, C.c_int]),
         ("oracle_ksolve_sample", [vp, vp, vp, vp, C.c_int, C.c_int, C.c_int, vp]),
         ("oracle_pair_bound", [vp]),
-        ("oracle_noncol_onsite", [vp, vp, vp, vp, vp]),
+        ("oracle_noncol_onsite", [vp] * 11),
     ]:
         fn = getattr(lib, name)
         fn.argtypes = args
@@ -120,14 +120,18 @@ def setpar(st, par, pairs, deriv=True):
 
 
 def noncol_onsite(st, par, pairs):
-    """Non-collinear on-site average and splitting per atom and orbital class."""
+    """Non-collinear on-site terms: dict of both sets' densities den1, den2 and
+    their volume derivatives vden1, vden2 (natoms, kinds), and paros, spinos,
+    dparos, dspnos (natoms, 4)."""
     from nrltb import api
     lib = load()
     cs, cp, cpr = st.to_c(), par.to_c(), api.pairs_to_c(pairs)
-    paros, spinos = np.zeros((st.natoms, 4)), np.zeros((st.natoms, 4))
-    rc = lib.oracle_noncol_onsite(_ref(cs), _ref(cp), _ref(cpr), _p(paros), _p(spinos))
+    out = {k: np.zeros((st.natoms, par.kinds)) for k in ("den1", "den2", "vden1", "vden2")}
+    out.update({k: np.zeros((st.natoms, 4)) for k in ("paros", "spinos", "dparos", "dspnos")})
+    keys = ("den1", "den2", "vden1", "vden2", "paros", "spinos", "dparos", "dspnos")
+    rc = lib.oracle_noncol_onsite(_ref(cs), _ref(cp), _ref(cpr), *[_p(out[k]) for k in keys])
     assert rc == 0, rc
-    return paros, spinos
+    return out
 
 
 def setham(st, par, km, which=0, kneigh_in=0):
@@ -167,11 +171,7 @@ def fermi(eig, w, tkb, zfill, tol=0.0):
 def bande(st, par, km, opts, nthreads=0):
     from nrltb import api
     lib = load()
-    nv, nk = par.nv(st), km.nk
-    if st.spinat is not None:   # non-collinear: one 2N x 2N problem per k
-        nv, jsp = 2 * nv, 1
-    else:
-        jsp = par.jspins
+    (nv, jsp), nk = api.result_shape(st, par), km.nk
     r, arrays = api.new_result(nv, nk, jspins=jsp, want_orbocc=opts.mode in (5, 6, 10))
     cs, cp, ck, co = st.to_c(), par.to_c(), km.to_c(), opts.to_c()
     rc = lib.oracle_bande(_ref(cs), _ref(cp), _ref(ck), _ref(co), _ref(r), nthreads)

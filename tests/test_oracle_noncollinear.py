@@ -117,7 +117,8 @@ def test_cross_species_onsite_terms_restated():
     mag2 = synth.make_magnetic_params([9, 9], [10.0, 9.0], 3, split=0.05)
     st = _cscl(angles=[(0, 0), (0, 0)], kinds=(1, 2))
     pairs, _, _ = oracle.search2(st, mag2)
-    paros, spinos = oracle.noncol_onsite(st, mag2, pairs)
+    nc = oracle.noncol_onsite(st, mag2, pairs)
+    paros, spinos = nc["paros"], nc["spinos"]
     npar = mag2.param.size // 2
     p1 = replace(mag2, param=mag2.param[:npar], jspins=1)
     p2 = replace(mag2, param=mag2.param[npar:], jspins=1)

@@ -89,8 +89,9 @@ struct Staged {
     bool valid = false;
     int natoms = 0, kinds = 0, jsover = 1, nltype = 0, nv = 0, nk = 0;
     int jspins = 1, anyflip = 0;   // spin channels; any atom spin-flipped
+    int noncol = 0, nvs = 0, nspb = 1;   // non-collinear spins; secular order; spin blocks of rows
     std::vector<int> kkind, kbas, ksk, orb_atom, flip;
-    std::vector<double> posn, posq, dnn, screenl, param, valence, kq, kw;
+    std::vector<double> posn, posq, dnn, screenl, param, valence, kq, kw, spinat;
     double plv[3][3];
     int nd[3];
     double volume = 0, zfill = 0;
@@ -105,7 +106,8 @@ struct nrltb_ctx {
     std::vector<nrltb_ctx *> workers;   // nrltb_bande_batch: one context and stream per host worker
     Staged st;
     // device inputs
-    DBuf d_kkind, d_posn, d_posq, d_kbas, d_dnn, d_screenl, d_param, d_kq, d_kw, d_ksk, d_orb, d_flip;
+    DBuf d_kkind, d_posn, d_posq, d_kbas, d_dnn, d_screenl, d_param, d_kq, d_kw, d_ksk, d_orb, d_flip, d_spinat;
+    DBuf d_nc, d_Hn, d_Sn;   // non-collinear: spin terms; the N x N Bloch sums before doubling
     // search2
     DBuf d_code, d_blk, d_misc;
     DBuf d_pairs;
@@ -152,6 +154,7 @@ static DevSK sk_view(nrltb_ctx *c, int P, int natoms, int kinds)
     s.dent = (double *)take(sizeof(double) * 2 * (size_t)P);
     s.vdent = (double *)take(sizeof(double) * 2 * (size_t)P);
     s.den = (double *)take(sizeof(double) * (size_t)natoms * kinds);
+    s.vden = (double *)take(sizeof(double) * (size_t)natoms * kinds);
     s.paros = (double *)take(sizeof(double) * 4 * (size_t)natoms);
     s.dparos = (double *)take(sizeof(double) * 4 * (size_t)natoms);
     s.E = (double *)take(sizeof(double) * 4 * 81 * (size_t)P);
@@ -159,7 +162,7 @@ static DevSK sk_view(nrltb_ctx *c, int P, int natoms, int kinds)
 }
 static size_t sk_bytes(int P, int natoms, int kinds)
 {
-    return sizeof(double) * ((size_t)P * (56 + 4 + 4 * 81) + (size_t)natoms * (kinds + 8)) + 12 * 256;
+    return sizeof(double) * ((size_t)P * (56 + 4 + 4 * 81) + (size_t)natoms * (2 * kinds + 8)) + 13 * 256;
 }
 
 static DevStructure dev_structure(nrltb_ctx *c)
@@ -223,7 +226,10 @@ static int check_inputs(const nrltb_structure *st, const nrltb_params *par)
         return NRLTB_E_ARG;
     }
     if (par->jspins < 0 || par->jspins > 2) { set_err("jspins %d", par->jspins); return NRLTB_E_ARG; }
-    if (st->spinat) { set_err("non-collinear spins are not built on the GPU path"); return NRLTB_E_UNSUPPORTED; }
+    if (st->spinat && par->jspins != 2) {   // bande.f:696-702
+        set_err("non-collinear spins need a two-set (magnetic) parameter file");
+        return NRLTB_E_ARG;
+    }
     if (par->jspins != 2 && st->flip)
         for (int i = 0; i < st->natoms; ++i)
             if (st->flip[i]) { set_err("atom %d is spin-flipped but the parameters have one spin", i + 1); return NRLTB_E_ARG; }
@@ -252,7 +258,10 @@ static int stage_host(nrltb_ctx *c, const nrltb_structure *st, const nrltb_param
     S.param.assign(par->param, par->param + (size_t)S.jspins * par->kinds * (29 + 68 * par->kinds));
     S.flip.assign(st->natoms, 0);
     S.anyflip = 0;
-    if (st->flip && S.jspins == 2)
+    S.noncol = st->spinat ? 1 : 0;   // non-collinear runs ignore flips (input1.f:259-262)
+    if (S.noncol) S.spinat.assign(st->spinat, st->spinat + 3 * st->natoms);
+    else S.spinat.assign(3, 0.0);
+    if (st->flip && S.jspins == 2 && !S.noncol)
         for (int i = 0; i < st->natoms; ++i) { S.flip[i] = st->flip[i] ? 1 : 0; S.anyflip |= S.flip[i]; }
     S.valence.assign(par->valence ? par->valence : nullptr, par->valence ? par->valence + par->kinds : nullptr);
     memcpy(S.plv, st->plv, sizeof S.plv);
@@ -270,6 +279,8 @@ static int stage_host(nrltb_ctx *c, const nrltb_structure *st, const nrltb_param
         if (par->valence) zfill += par->valence[st->kkind[i] - 1];
     }
     S.nv = nv;
+    S.nvs = S.noncol ? 2 * nv : nv;
+    S.nspb = S.noncol ? 1 : S.jspins;
     S.zfill = zfill;
     if (km) {
         if (km->nk < 1 || !km->k || !km->w) { set_err("empty k list"); return NRLTB_E_ARG; }
@@ -277,7 +288,7 @@ static int stage_host(nrltb_ctx *c, const nrltb_structure *st, const nrltb_param
         S.kq.assign(km->k, km->k + 3 * km->nk);
         S.kw.assign(km->w, km->w + km->nk);
         // one weight per row of the Fermi sums: every spin channel's k points
-        if (S.jspins == 2) S.kw.insert(S.kw.end(), km->w, km->w + km->nk);
+        if (S.nspb == 2) S.kw.insert(S.kw.end(), km->w, km->w + km->nk);
     } else {
         S.nk = 0;
         S.kq.clear();
@@ -296,6 +307,7 @@ static int stage_host(nrltb_ctx *c, const nrltb_structure *st, const nrltb_param
     RET(upload(c->d_ksk, S.ksk, s));
     RET(upload(c->d_orb, S.orb_atom, s));
     RET(upload(c->d_flip, S.flip, s));
+    RET(upload(c->d_spinat, S.spinat, s));
     if (km) {
         RET(upload(c->d_kq, S.kq, s));
         RET(upload(c->d_kw, S.kw, s));
@@ -364,6 +376,75 @@ static int run_setpar(nrltb_ctx *c, int deriv, int js = 0)
     DevParams DP = dev_params(c, js);
     if (c->npairs > 0) NRLTB_LAUNCH(k_setpar_pairs, cdiv(c->npairs, 128), 128, 0, s, DS, DP, pr, c->npairs, sk, deriv);
     NRLTB_LAUNCH(k_setpar_atoms, cdiv((long)S.natoms * 32, 256), 256, 0, s, DS, DP, pr, c->npairs, sk, deriv);
+    CKL();
+    return NRLTB_OK;
+}
+
+// ---- non-collinear spins (setpar.f/setparv.f lnoncol, spinham.f, addspins.f) ----
+// d_nc: spinos, dspnos [4 natoms]; the second set's den, vden [natoms kinds];
+// the spin terms diag, mix_re, mix_im and their volume derivatives [nv]
+struct NcView { double *spinos, *dspnos, *den2, *vden2, *diag, *mre, *mim, *ddiag, *dmre, *dmim; };
+static size_t nc_bytes(int natoms, int kinds, int nv)
+{
+    return sizeof(double) * (8 * (size_t)natoms + 2 * (size_t)natoms * kinds + 6 * (size_t)nv) + 10 * 256;
+}
+static NcView nc_view(nrltb_ctx *c)
+{
+    const Staged &S = c->st;
+    NcView v;
+    char *b = c->d_nc.as<char>();
+    size_t o = 0;
+    auto take = [&](size_t n) { double *q = (double *)(b + o); o += (sizeof(double) * n + 255) & ~size_t(255); return q; };
+    v.spinos = take(4 * (size_t)S.natoms);
+    v.dspnos = take(4 * (size_t)S.natoms);
+    v.den2 = take((size_t)S.natoms * S.kinds);
+    v.vden2 = take((size_t)S.natoms * S.kinds);
+    v.diag = take(S.nv);
+    v.mre = take(S.nv);
+    v.mim = take(S.nv);
+    v.ddiag = take(S.nv);
+    v.dmre = take(S.nv);
+    v.dmim = take(S.nv);
+    return v;
+}
+
+// hopping and overlap integrals from the first set; densities from both; the
+// non-collinear on-site terms and the per-orbital spin terms
+static int run_noncol_setup(nrltb_ctx *c, int lpress)
+{
+    const Staged &S = c->st;
+    cudaStream_t s = c->stream;
+    RET(c->d_nc.ensure(nc_bytes(S.natoms, S.kinds, S.nv)));
+    const NcView v = nc_view(c);
+    const size_t nkd = (size_t)S.natoms * S.kinds;
+    RET(run_setpar(c, lpress, 1));   // the second set's densities (and their derivatives)
+    DevSK sk = sk_view(c, std::max(c->npairs, 1), S.natoms, S.kinds);
+    CK(cudaMemcpyAsync(v.den2, sk.den, sizeof(double) * nkd, cudaMemcpyDeviceToDevice, s));
+    if (lpress) CK(cudaMemcpyAsync(v.vden2, sk.vden, sizeof(double) * nkd, cudaMemcpyDeviceToDevice, s));
+    RET(run_setpar(c, lpress, 0));   // the first set: integrals, densities, derivatives
+    const double *P1 = c->d_param.as<double>(), *P2 = P1 + (size_t)S.kinds * (29 + 68 * S.kinds);
+    NRLTB_LAUNCH(k_noncol_onsite, cdiv(S.natoms, 128), 128, 0, s, S.natoms, S.kinds, c->d_kkind.as<int>(), sk.den,
+                 v.den2, sk.vden, v.vden2, P1, P2, lpress, sk.paros, v.spinos, sk.dparos, v.dspnos);
+    NRLTB_LAUNCH(k_noncol_spin_terms, cdiv(S.nv, 128), 128, 0, s, S.nv, c->d_orb.as<int>(), c->d_ksk.as<int>(),
+                 v.spinos, c->d_spinat.as<double>(), v.diag, v.mre, v.mim);
+    if (lpress)
+        NRLTB_LAUNCH(k_noncol_spin_terms, cdiv(S.nv, 128), 128, 0, s, S.nv, c->d_orb.as<int>(), c->d_ksk.as<int>(),
+                     v.dspnos, c->d_spinat.as<double>(), v.ddiag, v.dmre, v.dmim);
+    CKL();
+    return NRLTB_OK;
+}
+
+// N x N Bloch sums of nkc k points (Hn, Sn) into the 2N x 2N d_H, d_S
+static int run_noncol_expand(nrltb_ctx *c, int nkc, const double2 *Hn, const double2 *Sn, bool deriv)
+{
+    const Staged &S = c->st;
+    cudaStream_t s = c->stream;
+    const NcView v = nc_view(c);
+    const long tot = 4L * S.nv * S.nv * nkc;
+    NRLTB_LAUNCH(k_noncol_expand, cdiv(tot, 256), 256, 0, s, S.nv, nkc, Hn, deriv ? v.ddiag : v.diag,
+                 deriv ? v.dmre : v.mre, deriv ? v.dmim : v.mim, c->d_H.as<double2>());
+    NRLTB_LAUNCH(k_noncol_expand, cdiv(tot, 256), 256, 0, s, S.nv, nkc, Sn, (const double *)nullptr,
+                 (const double *)nullptr, (const double *)nullptr, c->d_S.as<double2>());
     CKL();
     return NRLTB_OK;
 }
@@ -579,16 +660,25 @@ static int run_all(nrltb_ctx *c)
     c->nonpd.clear();
     do {
         if ((rc = run_search2(c, o.kneigh_in))) break;
-        if ((rc = run_setpar(c, lpress, 0))) break;
+        if (S.noncol) { if ((rc = run_noncol_setup(c, lpress))) break; }
+        else if ((rc = run_setpar(c, lpress, 0))) break;
         if ((rc = run_skblocks(c, lpress ? 4 : 2))) break;
-        const int nv = S.nv, nk = S.nk, nsp = S.jspins, nrow = nsp * nk;
+        // nv: order of the secular equation (2N for non-collinear spins)
+        const int nv = S.nvs, nk = S.nk, nsp = S.nspb, nrow = nsp * nk;
         // per-k outputs: one block of nk rows per spin channel, spin 1 first
         if ((rc = c->d_eig.ensure(sizeof(double) * (size_t)nv * nrow))) break;
         if ((rc = c->d_deig.ensure(sizeof(double) * (size_t)nv * nrow))) break;
         if ((rc = c->d_ncut.ensure(sizeof(int) * (size_t)nrow))) break;
         if ((rc = c->d_status.ensure(sizeof(int) * (size_t)nrow))) break;
-        const int chunk = choose_chunk(nv, nk, o.precision, lqlmt ? lowdin_bytes_per_k(nv) : 0);
+        const size_t nnb = (size_t)S.nv * S.nv;   // the Bloch sums before doubling
+        const int chunk = choose_chunk(nv, nk, o.precision,
+                                       (lqlmt ? lowdin_bytes_per_k(nv) : 0) + (S.noncol ? 32 * nnb : 0));
         const size_t nn = (size_t)nv * nv;
+        if (S.noncol) {
+            if ((rc = c->d_Hn.ensure(sizeof(double2) * nnb * chunk))) break;
+            if ((rc = c->d_Sn.ensure(sizeof(double2) * nnb * chunk))) break;
+        }
+        double2 *Hn = S.noncol ? c->d_Hn.as<double2>() : nullptr, *Sn = S.noncol ? c->d_Sn.as<double2>() : nullptr;
         if (lqlmt && (rc = c->d_orbq.ensure(sizeof(double) * nn * nrow))) break;
         if ((rc = c->d_H.ensure(sizeof(double2) * nn * chunk))) break;
         if ((rc = c->d_S.ensure(sizeof(double2) * nn * chunk))) break;
@@ -603,7 +693,12 @@ static int run_all(nrltb_ctx *c)
                 const int r0 = js * nk + k0;   // first row of this chunk
                 double *eig = c->d_eig.as<double>() + (size_t)r0 * nv;
                 int *status = c->d_status.as<int>() + r0;
-                if ((rc = run_bloch(c, k0, nkc, 0, c->d_H.as<double2>(), c->d_S.as<double2>()))) break;
+                if (S.noncol) {   // Bloch sums at order N, then the doubled problem
+                    if ((rc = run_bloch(c, k0, nkc, 0, Hn, Sn))) break;
+                    if ((rc = run_noncol_expand(c, nkc, Hn, Sn, false))) break;
+                } else if ((rc = run_bloch(c, k0, nkc, 0, c->d_H.as<double2>(), c->d_S.as<double2>()))) {
+                    break;
+                }
                 double2 *Z = nullptr;
                 if (lpress || lqlmt) {
                     // FP64 eigenvectors live after the FP32 staging area of d_X
@@ -624,7 +719,12 @@ static int run_all(nrltb_ctx *c)
                                               c->d_orbq.as<double>() + (size_t)r0 * nn)))
                     break;
                 if (lpress) {
-                    if ((rc = run_bloch(c, k0, nkc, 2, c->d_H.as<double2>(), c->d_S.as<double2>()))) break;
+                    if (S.noncol) {
+                        if ((rc = run_bloch(c, k0, nkc, 2, Hn, Sn))) break;
+                        if ((rc = run_noncol_expand(c, nkc, Hn, Sn, true))) break;
+                    } else if ((rc = run_bloch(c, k0, nkc, 2, c->d_H.as<double2>(), c->d_S.as<double2>()))) {
+                        break;
+                    }
                     if ((rc = c->d_hf.ensure(hf_scratch_bytes(nv, nkc)))) break;
                     if ((rc = run_hf(s, nv, nkc, o.precision, c->d_H.as<double2>(), c->d_S.as<double2>(), Z, eig,
                                      c->d_deig.as<double>() + (size_t)r0 * nv, c->d_hf.p, nullptr)))
@@ -650,7 +750,7 @@ static int run_all(nrltb_ctx *c)
         job.nv = nv; job.nk = nrow; job.ldk = nv; job.lpress = lpress;
         job.lentro = lentro;
         job.nks = (nsp == 2) ? nk : 0;
-        job.el = (nsp == 2) ? 1.0 : 2.0;   // electrons per band, bande.f:1065-1073
+        job.el = (nsp == 2 || S.noncol) ? 1.0 : 2.0;   // electrons per band, bande.f:1065-1073
         job.tkb = o.tkb; job.zfill = S.zfill; job.tol = (o.fermi_tol > 0) ? o.fermi_tol : 1e-8;
         if ((rc = c->d_fout.ensure(sizeof(FermiOut)))) break;
         if ((rc = c->d_fjob.ensure(sizeof(FermiJob)))) break;
@@ -672,7 +772,7 @@ static int fetch(nrltb_ctx *c, nrltb_result *res)
     if (!c->ran) { set_err("nothing run"); return NRLTB_E_ARG; }
     cudaStream_t s = c->stream;
     const Staged &S = c->st;
-    const int nv = S.nv, nk = S.nk, nrow = S.jspins * S.nk;
+    const int nv = S.nvs, nk = S.nk, nrow = S.nspb * S.nk;
     const int mode = S.opt.mode, lpress = (mode == 2 || mode == 4), lentro = (mode < 3);
     CK(cudaMemcpyAsync(&c->fout, c->d_fout.p, sizeof(FermiOut), cudaMemcpyDeviceToHost, s));
     std::vector<int> status(nrow);
@@ -713,7 +813,7 @@ static int fetch(nrltb_ctx *c, nrltb_result *res)
         }
     }
     // magnetic moment, bande.f:1388-1392
-    res->smag = (S.jspins == 2) ? c->fout.spin_up - c->fout.spin_dn : 0.0;
+    res->smag = (S.nspb == 2) ? c->fout.spin_up - c->fout.spin_dn : 0.0;
     res->dismin = c->dismin;
     res->npairs = c->npairs;
     res->nv = nv;
@@ -759,7 +859,7 @@ int nrltb_ctx_destroy(nrltb_ctx *c)
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
     DBuf *bufs[] = {&c->d_kkind, &c->d_posn, &c->d_posq, &c->d_kbas, &c->d_dnn, &c->d_screenl, &c->d_param,
-                    &c->d_kq, &c->d_kw, &c->d_ksk, &c->d_orb, &c->d_flip, &c->d_code, &c->d_blk, &c->d_misc, &c->d_pairs,
+                    &c->d_kq, &c->d_kw, &c->d_ksk, &c->d_orb, &c->d_flip, &c->d_spinat, &c->d_nc, &c->d_Hn, &c->d_Sn, &c->d_code, &c->d_blk, &c->d_misc, &c->d_pairs,
                     &c->d_sk, &c->d_seg, &c->d_ph, &c->d_H, &c->d_S, &c->d_X, &c->d_work, &c->d_ref, &c->d_hf, &c->d_np,
                     &c->d_qw, &c->d_eig, &c->d_deig, &c->d_ncut, &c->d_status, &c->d_fjob, &c->d_fout,
                     &c->d_orbq};

@@ -14,6 +14,7 @@
 //                      its atom block with Bloch phases e^{2 pi i k.(dlv - q_j + q_i)}.
 #include <cfloat>
 #include "setup.cuh"
+#include "noncol_math.h"
 
 namespace nrltb {
 
@@ -340,6 +341,8 @@ __global__ void k_setpar_atoms(DevStructure S, DevParams P, DevPairs pr, int npa
     const double *Pm = atom_params(S, P, a);   // on-site terms from the atom's own spin set
     const int jk1 = S.kkind[a];
     for (int k = 0; k < kinds; ++k) sk.den[(long)a * kinds + k] = den[k];
+    if (deriv)
+        for (int k = 0; k < kinds; ++k) sk.vden[(long)a * kinds + k] = vden[k];
     double paros[4], dparos[4];
     {
         int ip = ip_density(jk1);
@@ -573,6 +576,48 @@ k_bloch_build(DevStructure S, DevParams P, DevPairs pr, int npairs, DevSK sk, co
         M1[off] = make_double2(h_re, h_im);
         M2[off] = make_double2(s_re, s_im);
     }
+}
+
+// ---------------------------------------------------------------------------
+// Non-collinear spins.  One thread per atom: the on-site average and splitting
+// of the two parameter sets (setpar.f:746-796, setparv.f:723-795); P1, P2 are
+// the two sets (0-based pointers).
+__global__ void k_noncol_onsite(int natoms, int kinds, const int *kkind, const double *den1, const double *den2,
+                                const double *vden1, const double *vden2, const double *P1, const double *P2,
+                                int deriv, double *paros, double *spinos, double *dparos, double *dspnos)
+{
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= natoms) return;
+    const long o = (long)a * kinds;
+    nc_onsite_atom(kinds, kkind[a], den1 + o, den2 + o, vden1 + o, vden2 + o, P1 - 1, P2 - 1, deriv,
+                   paros + 4 * (long)a, spinos + 4 * (long)a, dparos + 4 * (long)a, dspnos + 4 * (long)a);
+}
+
+// One thread per orbital: spinham.f's diagonal and mixing terms
+__global__ void k_noncol_spin_terms(int nv, const int *orb_atom, const int *ksk, const double *spinos,
+                                    const double *spinat, double *diag, double *mix_re, double *mix_im)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nv) return;
+    const int a = orb_atom[i];
+    nc_spin_terms(i - ksk[a], spinos + 4 * (long)a, spinat + 3 * (long)a, diag + i, mix_re + i, mix_im + i);
+}
+
+// One thread per element of the doubled matrices (addspins.f:77-110); Hn holds
+// batch column-major N x N matrices, H2 receives the 2N x 2N ones.  diag = NULL
+// doubles an overlap block-diagonally.
+__global__ void k_noncol_expand(int nv, int batch, const double2 *Hn, const double *diag, const double *mix_re,
+                                const double *mix_im, double2 *H2)
+{
+    const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    const long n2 = 2L * nv, nn2 = n2 * n2, nn = (long)nv * nv;
+    if (t >= nn2 * batch) return;
+    const long b = t / nn2, e = t - b * nn2;
+    const int r = (int)(e % n2), c = (int)(e / n2);
+    const double *hb = (const double *)(Hn + b * nn);
+    double re, im;
+    nc_expand(nv, r, c, hb, hb + 1, 2, diag, mix_re, mix_im, &re, &im);
+    H2[t] = make_double2(re, im);
 }
 
 }  // namespace nrltb

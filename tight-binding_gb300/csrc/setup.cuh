@@ -40,6 +40,7 @@ struct DevSK {
     double *hop, *over, *dhop, *dover;  // [P][14]
     double *dent, *vdent;               // [P][2] density terms of atom 1, atom 2
     double *den;                        // [natoms][kinds]
+    double *vden;                       // [natoms][kinds] volume derivatives of den (deriv)
     double *paros, *dparos;             // [natoms][4]
     double *E;                          // [4][P][81] SK blocks: H, S, dH, dS
 };
@@ -54,6 +55,15 @@ __global__ void k_search_scatter(DevStructure S, DevParams P, const unsigned cha
 __global__ void k_setpar_pairs(DevStructure S, DevParams P, DevPairs pr, int npairs, DevSK sk, int deriv);
 __global__ void k_setpar_atoms(DevStructure S, DevParams P, DevPairs pr, int npairs, DevSK sk, int deriv);
 __global__ void k_sk_blocks(DevPairs pr, int npairs, DevSK sk, int nwhich);
+// non-collinear spins (noncol_math.h): on-site terms per atom, spin terms per
+// orbital, and the N x N -> 2N x 2N expansion of a batch of matrices
+__global__ void k_noncol_onsite(int natoms, int kinds, const int *kkind, const double *den1, const double *den2,
+                                const double *vden1, const double *vden2, const double *P1, const double *P2,
+                                int deriv, double *paros, double *spinos, double *dparos, double *dspnos);
+__global__ void k_noncol_spin_terms(int nv, const int *orb_atom, const int *ksk, const double *spinos,
+                                    const double *spinat, double *diag, double *mix_re, double *mix_im);
+__global__ void k_noncol_expand(int nv, int batch, const double2 *Hn, const double *diag, const double *mix_re,
+                                const double *mix_im, double2 *H2);
 __global__ void k_segments(DevPairs pr, int npairs, int natoms, int2 *seg);
 __global__ void k_phases(DevStructure S, DevPairs pr, int npairs, const double *kq, int nk, double2 *ph);
 __global__ void k_bloch_build(DevStructure S, DevParams P, DevPairs pr, int npairs, DevSK sk, const int2 *seg,

@@ -177,6 +177,15 @@ class Result:
     orbocc: np.ndarray = None   # (jspins*nk, nv states, nv orbitals), modes 5, 6, 10
 
 
+def result_shape(st, par):
+    """(order of the secular equation, spin blocks of rows) of nrltb_bande's
+    per-k outputs: 2N and one block for non-collinear spins, else N and jspins."""
+    nv = par.nv(st)
+    if st.spinat is not None:
+        return 2 * nv, 1
+    return nv, max(par.jspins, 1)
+
+
 def new_result(nv, nk, want_eig=True, want_deig=True, jspins=1, want_orbocc=False):
     """Result struct with per-k arrays of jspins * nk rows (spin 1's k points
     first); want_orbocc adds the (rows, states, orbitals) Lowdin charges."""
@@ -341,17 +350,18 @@ class Context:
         return int(self.lib.nrltb_ctx_launch_count(self.h))
 
     def bande(self, st, par, km, opts, want_eig=True, want_orbocc=None):
-        nv, nk = par.nv(st), km.nk
+        (nv, nsp), nk = result_shape(st, par), km.nk
         if want_orbocc is None:
             want_orbocc = opts.mode in (5, 6, 10)
-        r, arrays = new_result(nv, nk, want_eig, want_eig, par.jspins, want_orbocc)
+        r, arrays = new_result(nv, nk, want_eig, want_eig, nsp, want_orbocc)
         cs, cp, ck, co = st.to_c(), par.to_c(), km.to_c(), opts.to_c()
         self._check(self.lib.nrltb_bande(self.h, C.byref(cs), C.byref(cp), C.byref(ck),
                                          C.byref(co), C.byref(r)), "nrltb_bande")
         return result_from_c(r, arrays)
 
     def stage(self, st, par, km, opts):
-        self._staged = (st.to_c(), par.to_c(), km.to_c(), opts.to_c(), par.nv(st), km.nk, par.jspins)
+        nv, nsp = result_shape(st, par)
+        self._staged = (st.to_c(), par.to_c(), km.to_c(), opts.to_c(), nv, km.nk, nsp)
         cs, cp, ck, co = self._staged[:4]
         self._check(self.lib.nrltb_stage(self.h, C.byref(cs), C.byref(cp), C.byref(ck),
                                          C.byref(co)), "nrltb_stage")
