@@ -43,6 +43,9 @@ extern "C" {
 #define NRLTB_PREC_FP64   0      /* plain FP64 drop-in                              */
 #define NRLTB_PREC_MIXED  1      /* FP32 eigensolve + FP64-accurate refinement      */
 
+/* ---- option flags (nrltb_opts.flags) ------------------------------------ */
+#define NRLTB_OPT_SPIN_DIRECTIONS 1  /* non-collinear runs: fill nrltb_result.spdir    */
+
 /*
  * One periodic structure, after input1.f and the lattice-to-Cartesian conversion
  * of static.f:1088-1103 (the common blocks /codes/, /latt1/, /fazon/, /disply/).
@@ -102,7 +105,7 @@ typedef struct {
     double eigcut;         /* eigenvalue cutoff for the pressure sums, Ry       */
     double fermi_tol;      /* |N - zfill| and bracket tolerance; 0 -> 1e-8      */
     int kneigh_in;         /* search2's carried /relat/ kneigh flag (0 at start)*/
-    int flags;             /* reserved, must be 0                               */
+    int flags;             /* NRLTB_OPT_* bits, 0 for none                      */
 } nrltb_opts;
 
 /* Pair list of search2.f (common /pairs/ and /neigh/), caller-allocated. */
@@ -143,6 +146,10 @@ typedef struct {
     double earg1, earg2;
     double smag;           /* jspins = 2: spin-up minus spin-down electrons per */
                            /* cell (bande.f:1336-1395), SKENG's last column; 0  */
+    double *spdir;         /* optional out [natoms][3], non-collinear runs with  */
+                           /* NRLTB_OPT_SPIN_DIRECTIONS: each atom's spin vector */
+                           /* summed over occupied states (diag.f:458-524,      */
+                           /* bande.f:1480-1537), SPNDIR's columns              */
     double *orbocc;        /* optional out [jspins][nk][nv][nv], modes 5, 6, 10: */
                            /* [row][state n][orbital i] = |(S^1/2 z_n)_i|^2, the */
                            /* Lowdin charges of diag.f:526-700; -1 at a k whose  */

@@ -26,12 +26,19 @@ int nrltb_skin_info(const nrltb_skin *s, int *mode, double *tkb, double *eigcut,
 /* Read the next structure: title, label, zcharge (static.f:938-950), input1.f,
  * setlat.f, the lattice-to-Cartesian step (static.f:1088-1103) and kptin.f.
  * With the spin-flip flag T on the (2a1) line each atom line carries magdir
- * and st->flip marks the atoms with magdir 2 (NULL when none is flipped); the
- * non-collinear flags N, D, S give NRLTB_E_UNSUPPORTED.  Returns NRLTB_E_EOF
+ * and st->flip marks the atoms with magdir 2 (NULL when none is flipped); with
+ * the non-collinear flags N, D, S it carries theta, phi and st->spinat holds
+ * the unit directions.  Returns NRLTB_E_EOF
  * after the last structure.  title must hold 71 chars and label 21 (NUL
  * included). */
 int nrltb_skin_next(nrltb_skin *s, nrltb_structure *st, nrltb_kmesh *km,
                     char *title, char *label);
+/* The spin options of the structure nrltb_skin_next last read: flag S asks for
+ * output spin directions (SPNDIR), flag D for torques (SKDERIV, which the
+ * reference opens but never writes); both make the run non-collinear. */
+#define NRLTB_SKIN_SPIN_DIRECTIONS 1
+#define NRLTB_SKIN_TORQUES         2
+int nrltb_skin_spin_options(const nrltb_skin *s);
 /* Line number (1-based) of the SKIN file where the last error happened. */
 int nrltb_skin_error_line(const nrltb_skin *s);
 void nrltb_skin_close(nrltb_skin *s);

@@ -985,6 +985,7 @@ int oracle_bande(const nrltb_structure *st, const nrltb_params *par, const nrltb
             if (st->flip[i]) return NRLTB_E_ARG;   /* spin flips need two parameter sets */
     int lpress = (opt->mode == 2 || opt->mode == 4);
     const int lqlmt = (opt->mode == 5 || opt->mode == 6 || opt->mode == 10) && res->orbocc;
+    const int lspdir = noncol && (opt->flags & NRLTB_OPT_SPIN_DIRECTIONS) && res->spdir;
     int nv = 0;
     double zfill = st->zcharge;
     for (int i = 0; i < st->natoms; ++i) { nv += par->kbas[st->kkind[i] - 1]; zfill += par->valence[st->kkind[i] - 1]; }
@@ -1027,6 +1028,8 @@ int oracle_bande(const nrltb_structure *st, const nrltb_params *par, const nrltb
         free(den2); free(vden1); free(vden2); free(tmp); free(tmp2); free(tpar); free(spinos); free(dspnos);
     }
     const int nk = km->nk, nrow = nsp * nk;   /* rows: spin 1's k points, then spin 2's */
+    /* per row, state and atom the spin vector of diag.f:458-524 */
+    double *spev = lspdir ? calloc((size_t)nrow * nvx * na * 3, sizeof(double)) : NULL;
     double *esk = malloc(sizeof(double) * (size_t)nvx * nrow);
     double *desk = calloc((size_t)nvx * nrow, sizeof(double));
     double *wrow = malloc(sizeof(double) * (size_t)nrow);
@@ -1048,13 +1051,35 @@ int oracle_bande(const nrltb_structure *st, const nrltb_params *par, const nrltb
             zc *hp = malloc(sizeof(zc) * np), *sp = malloc(sizeof(zc) * np);
             zc *hx = hp, *sx = sp;
             if (noncol) { hx = malloc(sizeof(zc) * npx); sx = malloc(sizeof(zc) * npx); }
-            zc *z = (lpress || lqlmt) ? malloc(sizeof(zc) * (size_t)nvx * nvx) : NULL;
+            zc *z = (lpress || lqlmt || lspdir) ? malloc(sizeof(zc) * (size_t)nvx * nvx) : NULL;
             zc *sc = lqlmt ? malloc(sizeof(zc) * npx) : NULL;
             oracle_setham_packed(st, par, &pr, hop, over, paros, km->k + 3 * k, 0, hp, sp);
             if (noncol) addspins(nv, sdiag, smix, hp, sp, hx, sx);   /* bande.f:955-958 */
             if (sc) memcpy(sc, sx, sizeof(zc) * npx);
-            int ioverr = oracle_diag_packed(nvx, lpress || lqlmt, par->jsover, hx, sx, esk + (size_t)r * nvx, z);
+            int ioverr = oracle_diag_packed(nvx, lpress || lqlmt || lspdir, par->jsover, hx, sx, esk + (size_t)r * nvx, z);
             kst[r] = ioverr ? NRLTB_K_S_NOT_PD : NRLTB_K_OK;
+            if (lspdir) {
+                /* up (first N) and down (last N) halves of each state on each
+                 * atom's orbitals; the reference takes the atom's basis size as
+                 * kbas(kkind(matom)), here the atom's own */
+                for (int ie = 0; ie < nvx; ++ie) {
+                    const zc *zc_ = z + (size_t)ie * nvx;
+                    for (int ia = 0; ia < st->natoms; ++ia) {
+                        int i0 = 0;
+                        for (int q = 0; q < ia; ++q) i0 += par->kbas[st->kkind[q] - 1];
+                        const int nb = par->kbas[st->kkind[ia] - 1];
+                        double sx_ = 0, sy_ = 0, sz_ = 0;
+                        for (int ib = i0; ib < i0 + nb; ++ib) {
+                            const zc a = zc_[ib], b = zc_[ib + nv];
+                            sx_ = creal(sx_ - conj(a) * b - conj(b) * a);
+                            sy_ = sy_ + cimag(conj(a) * b - conj(b) * a);
+                            sz_ = creal(sz_ + conj(b) * b - conj(a) * a);
+                        }
+                        double *o = spev + (((size_t)r * nvx + ie) * na + ia) * 3;
+                        o[0] = sx_; o[1] = sy_; o[2] = sz_;
+                    }
+                }
+            }
             if (lqlmt) {
                 double *orb = res->orbocc + (size_t)r * nvx * nvx;
                 if (ioverr) for (size_t i = 0; i < (size_t)nvx * nvx; ++i) orb[i] = -1.0;
@@ -1130,6 +1155,21 @@ int oracle_bande(const nrltb_structure *st, const nrltb_params *par, const nrltb
             smag = (js == 0) ? sptemp : smag - sptemp;
         }
     }
+    /* occupied-state sum of the spin vectors, bande.f:1484-1537 */
+    if (lspdir) {
+        for (size_t i = 0; i < 3 * na; ++i) res->spdir[i] = 0.0;
+        for (int r = 0; r < nrow; ++r) {
+            const double wt = sfac * wrow[r];
+            const double *e = esk + (size_t)r * nvx;
+            for (int i = 0; i < nvx; ++i) {
+                if (!(e[i] < efp)) continue;
+                double fbe = wt;
+                if (e[i] > efm) fbe = wt * FB(e[i] - efermi);
+                const double *sv = spev + ((size_t)r * nvx + i) * na * 3;
+                for (size_t j = 0; j < 3 * na; ++j) res->spdir[j] = res->spdir[j] + fbe * sv[j];
+            }
+        }
+    }
 #undef FB
     res->efermi = efermi;
     res->e_total = esum;
@@ -1169,7 +1209,7 @@ int oracle_bande(const nrltb_structure *st, const nrltb_params *par, const nrltb
     if (res->ncut) memcpy(res->ncut, ncut, sizeof(int) * (size_t)nrow);
     if (res->k_status) memcpy(res->k_status, kst, sizeof(int) * (size_t)nrow);
     free(esk); free(desk); free(wrow); free(ncut); free(kst);
-    free(sdiag); free(smix); free(dsdiag); free(dsmix);
+    free(sdiag); free(smix); free(dsdiag); free(dsmix); free(spev);
     free(hop); free(over); free(paros); free(den); free(dhop); free(dover); free(dparos);
     free_pairs(&pr);
     return NRLTB_OK;

@@ -169,10 +169,11 @@ def fermi(eig, w, tkb, zfill, tol=0.0):
 
 
 def bande(st, par, km, opts, nthreads=0):
-    from nrltb import api
+    from nrltb import abi, api
     lib = load()
     (nv, jsp), nk = api.result_shape(st, par), km.nk
-    r, arrays = api.new_result(nv, nk, jspins=jsp, want_orbocc=opts.mode in (5, 6, 10))
+    nsd = st.natoms if (st.spinat is not None and opts.flags & abi.OPT_SPIN_DIRECTIONS) else 0
+    r, arrays = api.new_result(nv, nk, jspins=jsp, want_orbocc=opts.mode in (5, 6, 10), natoms_spdir=nsd)
     cs, cp, ck, co = st.to_c(), par.to_c(), km.to_c(), opts.to_c()
     rc = lib.oracle_bande(_ref(cs), _ref(cp), _ref(ck), _ref(co), _ref(r), nthreads)
     assert rc == 0, rc

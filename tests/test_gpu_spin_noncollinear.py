@@ -95,3 +95,39 @@ def test_noncollinear_needs_two_sets(ctx, km):
     p1 = synth.make_params([9], [10.0], 7)
     with pytest.raises(NrltbError):
         ctx.bande(_cscl([(0, 0), (0, 0)]), p1, km, Opts(mode=3, tkb=TKB))
+
+
+@pytest.mark.parametrize("precision", [abi.PREC_FP64, abi.PREC_MIXED])
+@pytest.mark.parametrize("angles", [[(37, 110), (37, 110)], [(0, 0), (180, 0)], [(0, 0), (90, 30)]])
+def test_spin_directions(ctx, mag, km, angles, precision):
+    st = _cscl(angles)
+    op = dict(tkb=TKB, eigcut=1e3, fermi_tol=1e-11, flags=abi.OPT_SPIN_DIRECTIONS)
+    g = ctx.bande(st, mag, km, Opts(mode=3, precision=precision, **op))
+    o = oracle.bande(st, mag, km, Opts(mode=3, **op))
+    assert g.spdir.shape == o.spdir.shape == (2, 3)
+    assert np.abs(g.spdir - o.spdir).max() <= 1e-8
+
+
+def test_host_driver_spin_directions(tmp_path, mag, km):
+    import subprocess
+    from nrltb import build, read_skin
+    sts = [(_cscl([(0, 0), (90, 30)]), km), (_cscl([(20, 40), (160, -30)]), km)]
+    synth.write_skin(str(tmp_path), sts, mag, mode=3, tkb=TKB)
+    path = tmp_path / "SKIN"
+    path.write_text(path.read_text().replace("\nFN\n", "\nFS\n"))
+    r = subprocess.run([build.DRIVER, "SKIN"], cwd=tmp_path, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    lines = (tmp_path / "SPNDIR").read_text().splitlines()
+    assert len(lines) == 4
+    sk = read_skin(str(path))
+    for j, (_, label, s2, k2) in enumerate(sk.structures):
+        o = oracle.bande(s2, sk.params, k2, Opts(mode=3, tkb=sk.tkb, eigcut=sk.eigcut,
+                                                 flags=abi.OPT_SPIN_DIRECTIONS))
+        for i in range(2):
+            line = lines[2 * j + i]
+            assert line[:20].split() == label.split() and int(line[20:25]) == i + 1
+            vals = [float(x) for x in line[25:].split()]
+            np.testing.assert_allclose(vals[:3], o.spdir[i], atol=1.01e-6)
+            assert vals[3] == pytest.approx(np.linalg.norm(o.spdir[i]), abs=1.01e-6)
+    skeng = (tmp_path / "SKENG").read_text().splitlines()
+    assert len(skeng) == 2 and len(skeng[0][20:].split()) == 3   # volume, E_F, E(T): no moment column

@@ -25,7 +25,7 @@ import numpy as np
 import pytest
 
 import oracle
-from nrltb import Opts, Structure, read_skin, synth
+from nrltb import Opts, Structure, abi, read_skin, synth
 
 A, TKB = 5.6, 0.01
 
@@ -159,3 +159,43 @@ def test_reader_spin_directions(tmp_path, mag, km):
     s2 = read_skin(os.path.join(str(tmp_path), "SKIN")).structures[0][2]
     assert s2.spinat is not None and s2.flip is None
     np.testing.assert_allclose(s2.spinat, st.spinat, atol=1e-14)
+
+
+def _sd(mode=3):
+    return Opts(mode=mode, tkb=TKB, eigcut=1e3, fermi_tol=1e-12, flags=abi.OPT_SPIN_DIRECTIONS)
+
+
+def test_spin_directions(mag, km):
+    """diag.f:458-524 / bande.f:1480-1560: each atom's occupied-state spin
+    vector (the reference's sign convention: along -m for a common m)."""
+    z = oracle.bande(_cscl(angles=[(0, 0), (0, 0)]), mag, km, _sd())
+    assert z.spdir.shape == (2, 3)
+    assert np.abs(z.spdir[:, :2]).max() == 0.0 and (z.spdir[:, 2] < -0.5).all()
+    for t, p in ((37, 110), (150, -70)):
+        r = oracle.bande(_cscl(angles=[(t, p), (t, p)]), mag, km, _sd())
+        m = _dirs([(t, p)])[0]
+        for j in range(2):   # the vectors turn with the common direction
+            np.testing.assert_allclose(r.spdir[j], z.spdir[j, 2] * m, atol=1e-12)
+    afm = oracle.bande(_cscl(angles=[(0, 0), (180, 0)]), mag, km, _sd())
+    np.testing.assert_allclose(afm.spdir[1], -afm.spdir[0], atol=1e-12)
+    assert afm.spdir[0, 2] < -0.5
+
+
+def test_spin_directions_count_the_moment_for_an_orthogonal_set(mag, km):
+    """Without an overlap the z components are populations: their sum is the
+    collinear run's spin-down minus spin-up electrons."""
+    orth = replace(mag, jsover=0)
+    col = oracle.bande(_cscl(), orth, km, _opts(3))
+    nc = oracle.bande(_cscl(angles=[(0, 0), (0, 0)]), orth, km, _sd())
+    assert nc.spdir[:, 2].sum() == pytest.approx(-col.smag, abs=1e-9)
+
+
+def test_reader_spin_options(tmp_path, mag, km):
+    for flag, want in (("FS", 1), ("FD", 2), ("FN", 0)):
+        d = os.path.join(str(tmp_path), flag)
+        synth.write_skin(d, [(_cscl(angles=[(10, 20), (30, 40)]), km)], mag, mode=3, tkb=TKB)
+        path = os.path.join(d, "SKIN")
+        text = open(path).read().replace("\nFN\n", "\n%s\n" % flag)
+        open(path, "w").write(text)
+        sk = read_skin(path)
+        assert sk.spin_options == [want] and sk.structures[0][2].spinat is not None

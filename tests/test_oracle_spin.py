@@ -150,9 +150,9 @@ def test_reader_magnetic_file_and_flips(tmp_path, mag, km):
     assert s3.flip is None
 
 
-@pytest.mark.parametrize("flag,code", [("D", "-7"), ("S", "-7"), ("N", "-5")])
-def test_reader_non_collinear_flags_are_refused(tmp_path, km, flag, code):
-    """Torque (D) and spin-direction (S) runs are not built; N is, but needs a
+@pytest.mark.parametrize("flag,code", [("D", "-5"), ("S", "-5"), ("N", "-5")])
+def test_reader_non_collinear_flags_need_directions(tmp_path, km, flag, code):
+    """The non-collinear flags N, D (torques) and S (spin directions) need a
     direction (theta, phi) on every atom line."""
     d = str(tmp_path)
     synth.write_skin(d, [(_cscl(), km)], synth.make_params([9], [10.0], 7), mode=4, tkb=TKB)

@@ -119,7 +119,7 @@ struct nrltb_ctx {
     DBuf d_H, d_S, d_X, d_work, d_ref, d_hf, d_np, d_qw;
     std::vector<std::pair<int, int>> nonpd;   // (k, chunk) of k points whose S is not positive definite
     // results
-    DBuf d_eig, d_deig, d_ncut, d_status, d_fjob, d_fout, d_orbq;
+    DBuf d_eig, d_deig, d_ncut, d_status, d_fjob, d_fout, d_orbq, d_spev, d_spdir;
     FermiOut fout;
     int ran = 0;
 };
@@ -651,6 +651,8 @@ static int run_all(nrltb_ctx *c)
     const int lpress = (o.mode == 2 || o.mode == 4);   // bande.f:726-730
     const int lentro = (o.mode < 3);
     const int lqlmt = (o.mode == 5 || o.mode == 6 || o.mode == 10);   // orbital charges, diag.f:526
+    const int lspdir = S.noncol && (o.flags & NRLTB_OPT_SPIN_DIRECTIONS);   // spin directions, diag.f:458
+    const bool vectors = lpress || lqlmt || lspdir;
     cudaStream_t s = c->stream;
     long long *prev = g_launch_counter;
     KTimer *prev_kt = g_ktimer;
@@ -680,6 +682,10 @@ static int run_all(nrltb_ctx *c)
         }
         double2 *Hn = S.noncol ? c->d_Hn.as<double2>() : nullptr, *Sn = S.noncol ? c->d_Sn.as<double2>() : nullptr;
         if (lqlmt && (rc = c->d_orbq.ensure(sizeof(double) * nn * nrow))) break;
+        if (lspdir) {
+            if ((rc = c->d_spev.ensure(sizeof(double) * 3 * (size_t)nv * S.natoms * nrow))) break;
+            if ((rc = c->d_spdir.ensure(sizeof(double) * 3 * (size_t)S.natoms))) break;
+        }
         if ((rc = c->d_H.ensure(sizeof(double2) * nn * chunk))) break;
         if ((rc = c->d_S.ensure(sizeof(double2) * nn * chunk))) break;
         if ((rc = c->d_X.ensure(zoff(nn, chunk) + sizeof(double2) * nn * chunk))) break;
@@ -700,12 +706,12 @@ static int run_all(nrltb_ctx *c)
                     break;
                 }
                 double2 *Z = nullptr;
-                if (lpress || lqlmt) {
+                if (vectors) {
                     // FP64 eigenvectors live after the FP32 staging area of d_X
                     Z = (double2 *)(c->d_X.as<char>() + zoff(nn, chunk));
                 }
                 if ((rc = run_solve(c, nv, nkc, o.precision, c->d_H.as<double2>(), c->d_S.as<double2>(), eig, Z,
-                                    status, (lpress || lqlmt) != 0)))
+                                    status, vectors)))
                     break;
                 std::vector<int> hst(nkc), bad;
                 if (cudaMemcpyAsync(hst.data(), status, sizeof(int) * nkc, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
@@ -718,6 +724,12 @@ static int run_all(nrltb_ctx *c)
                 if (lqlmt && (rc = run_lowdin(c, nv, nkc, c->d_S.as<double2>(), Z, status,
                                               c->d_orbq.as<double>() + (size_t)r0 * nn)))
                     break;
+                if (lspdir) {
+                    const long nt = (long)nkc * nv * S.natoms;
+                    NRLTB_LAUNCH(k_spin_expect, cdiv(nt, 256), 256, 0, s, Z, nv, nkc, S.natoms, c->d_ksk.as<int>(),
+                                 c->d_spev.as<double>() + 3 * (size_t)r0 * nv * S.natoms);
+                    CKL();
+                }
                 if (lpress) {
                     if (S.noncol) {
                         if ((rc = run_bloch(c, k0, nkc, 2, Hn, Sn))) break;
@@ -760,6 +772,10 @@ static int run_all(nrltb_ctx *c)
         NRLTB_LAUNCH(k_fermi_sums, 1, 1024, 0, s, c->d_fjob.as<FermiJob>());
         e = cudaGetLastError();
         if (e != cudaSuccess) { set_err("fermi: %s", cudaGetErrorString(e)); rc = NRLTB_E_CUDA; break; }
+        if (lspdir)
+            NRLTB_LAUNCH(k_spin_dir_sum, 3 * S.natoms, 256, 0, s, c->d_eig.as<double>(), c->d_kw.as<double>(),
+                         c->d_spev.as<double>(), c->d_fout.as<FermiOut>(), o.tkb, job.el, nrow, nv, S.natoms,
+                         c->d_spdir.as<double>());
         c->ran = 1;
     } while (0);
     g_launch_counter = prev;
@@ -787,6 +803,9 @@ static int fetch(nrltb_ctx *c, nrltb_result *res)
         if (lpress) CK(cudaMemcpyAsync(res->ncut, c->d_ncut.p, sizeof(int) * nrow, cudaMemcpyDeviceToHost, s));
         else for (int k = 0; k < nrow; ++k) res->ncut[k] = nv;
     }
+    if (res->spdir && S.noncol && (S.opt.flags & NRLTB_OPT_SPIN_DIRECTIONS))
+        CK(cudaMemcpyAsync(res->spdir, c->d_spdir.p, sizeof(double) * 3 * (size_t)S.natoms, cudaMemcpyDeviceToHost,
+                           s));
     if (res->orbocc && (mode == 5 || mode == 6 || mode == 10))
         CK(cudaMemcpyAsync(res->orbocc, c->d_orbq.p, sizeof(double) * (size_t)nv * nv * nrow, cudaMemcpyDeviceToHost,
                            s));
@@ -862,7 +881,7 @@ int nrltb_ctx_destroy(nrltb_ctx *c)
                     &c->d_kq, &c->d_kw, &c->d_ksk, &c->d_orb, &c->d_flip, &c->d_spinat, &c->d_nc, &c->d_Hn, &c->d_Sn, &c->d_code, &c->d_blk, &c->d_misc, &c->d_pairs,
                     &c->d_sk, &c->d_seg, &c->d_ph, &c->d_H, &c->d_S, &c->d_X, &c->d_work, &c->d_ref, &c->d_hf, &c->d_np,
                     &c->d_qw, &c->d_eig, &c->d_deig, &c->d_ncut, &c->d_status, &c->d_fjob, &c->d_fout,
-                    &c->d_orbq};
+                    &c->d_orbq, &c->d_spev, &c->d_spdir};
     for (DBuf *b : bufs) b->release();
     if (c->kt) {
         for (int i = 0; i < c->kt->npool; ++i) cudaEventDestroy(c->kt->pool[i]);

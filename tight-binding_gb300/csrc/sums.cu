@@ -173,6 +173,59 @@ __global__ void __launch_bounds__(1024) k_fermi_sums(FermiJob *jobs)
     }
 }
 
+// One thread per (k, state, atom).  Z: batch column-major n2 x n2 eigenvectors
+// (n2 = 2N, the up half first); ksk: first orbital of each atom.  The spin
+// vector of diag.f:486-513 as written there: x = -2 Re(u* d), y = 2 Im(u* d),
+// z = |d|^2 - |u|^2 summed over the atom's orbitals, without the overlap.
+__global__ void k_spin_expect(const double2 *Z, int n2, int batch, int natoms, const int *ksk, double *spev)
+{
+    const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (t >= (long)batch * n2 * natoms) return;
+    const int a = (int)(t % natoms);
+    const long q = t / natoms;
+    const int ie = (int)(q % n2);
+    const long b = q / n2;
+    const int nh = n2 / 2, i0 = ksk[a], i1 = (a + 1 < natoms) ? ksk[a + 1] : nh;
+    const double2 *z = Z + b * (long)n2 * n2 + (long)ie * n2;
+    double sx = 0.0, sy = 0.0, sz = 0.0;
+    for (int ib = i0; ib < i1; ++ib) {
+        const double2 u = z[ib], d = z[ib + nh];
+        const double re_ud = u.x * d.x + u.y * d.y, im_ud = u.x * d.y - u.y * d.x;   // conj(u) d
+        const double re_du = d.x * u.x + d.y * u.y, im_du = d.x * u.y - d.y * u.x;   // conj(d) u
+        sx = (sx - re_ud) - re_du;
+        sy = sy + (im_ud - im_du);
+        sz = (sz + (d.x * d.x + d.y * d.y)) - (u.x * u.x + u.y * u.y);
+    }
+    double *o = spev + 3 * t;
+    o[0] = sx;
+    o[1] = sy;
+    o[2] = sz;
+}
+
+// One block per atom and component: the occupation-weighted sum over every
+// row and state, weight el w(k) below E_F - 20 kT and el w(k) f inside the
+// window (bande.f:1505-1516); E_F from the Fermi kernel's output
+__global__ void __launch_bounds__(256) k_spin_dir_sum(const double *eig, const double *w, const double *spev,
+                                                      const FermiOut *fo, double tkb, double el, int nrow, int n2,
+                                                      int natoms, double *spdir)
+{
+    __shared__ double sh[32];
+    const int j = blockIdx.x;   // 3 * atom + component
+    const double mu = fo->efermi, tkbi = (tkb < 1e-5) ? 1e5 : 1.0 / tkb;
+    const double efp = mu + 20.0 * tkb, efm = mu - 20.0 * tkb;
+    double acc = 0.0;
+    for (long q = threadIdx.x; q < (long)nrow * n2; q += blockDim.x) {
+        const double e = eig[q];
+        if (!(e < efp)) continue;
+        const double wt = el * w[q / n2];
+        double fbe = wt;
+        if (e > efm) fbe = wt * (1.0 / (1.0 + exp(tkbi * (e - mu))));
+        acc += fbe * spev[q * 3L * natoms + j];
+    }
+    acc = block_sum_d(acc, sh);
+    if (threadIdx.x == 0) spdir[j] = acc;
+}
+
 // ncut[k] = number of eigenvalues <= eigcut (perturb.f:87-95)
 __global__ void k_ncut(const double *eig, int ldk, int nv, int nk, double eigcut, int *ncut)
 {

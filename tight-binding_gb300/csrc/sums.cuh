@@ -25,6 +25,12 @@ struct FermiJob {
 };
 
 __global__ void k_fermi_sums(FermiJob *jobs);
+// non-collinear spin directions (diag.f:458-524, bande.f:1480-1537): per k,
+// state and atom the spin vector of the up and down halves of the
+// eigenvector; then its occupied-state sum per atom and component
+__global__ void k_spin_expect(const double2 *Z, int n2, int batch, int natoms, const int *ksk, double *spev);
+__global__ void k_spin_dir_sum(const double *eig, const double *w, const double *spev, const FermiOut *fo,
+                               double tkb, double el, int nrow, int n2, int natoms, double *spdir);
 __global__ void k_ncut(const double *eig, int ldk, int nv, int nk, double eigcut, int *ncut);
 void launch_hf_dots(cudaStream_t s, const double2 *Z, const double2 *P, const double2 *Q, const double2 *dH,
                     const double2 *dS, const double *eig, double *deig, int n, int batch);

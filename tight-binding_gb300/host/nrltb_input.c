@@ -265,6 +265,7 @@ struct nrltb_skin {
     int natoms;
     int *kkind, *flip;
     double *posn, *posq, *spinat;
+    int spinopt;   /* NRLTB_SKIN_* of the current structure */
     /* k list, kept across structures (kptin.f `save nk`) */
     int nk;
     double *kq, *kw;
@@ -332,6 +333,8 @@ int nrltb_skin_info(const nrltb_skin *s, int *mode, double *tkb, double *eigcut,
     if (par) *par = s->par;
     return NRLTB_OK;
 }
+
+int nrltb_skin_spin_options(const nrltb_skin *s) { return s ? s->spinopt : 0; }
 
 int nrltb_skin_error_line(const nrltb_skin *s) { return s ? s->errline : 0; }
 
@@ -1059,9 +1062,10 @@ int nrltb_skin_next(nrltb_skin *s, nrltb_structure *st, nrltb_kmesh *km, char *t
     int lphonon = (c1 == 'T' || c1 == 't');
     /* input1.f:535-546: T spin flips (a magdir per atom); N, D, S non-collinear
      * runs (not built); anything else plain */
+    /* D (torques) and S (spin directions) imply N (input1.f:535-546) */
     int spinflip = (c2 == 'T' || c2 == 't');
-    int noncol = (c2 == 'N' || c2 == 'n');   /* theta, phi per atom (input1.f:754-771) */
-    if (c2 == 'D' || c2 == 'd' || c2 == 'S' || c2 == 's') { rc = NRLTB_E_UNSUPPORTED; goto fail; }
+    int noncol = (c2 == 'N' || c2 == 'n' || c2 == 'D' || c2 == 'd' || c2 == 'S' || c2 == 's');
+    s->spinopt = (c2 == 'S' || c2 == 's') ? NRLTB_SKIN_SPIN_DIRECTIONS : (c2 == 'D' || c2 == 'd') ? NRLTB_SKIN_TORQUES : 0;
     /* reciprocal vectors without 2 pi (input1.f:612-624) */
     double bvec[3][3];
     for (int i = 0; i < 3; ++i) {

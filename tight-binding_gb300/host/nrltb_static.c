@@ -15,6 +15,7 @@
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+#include <math.h>
 #include "nrltb.h"
 #include "nrltb_input.h"
 
@@ -80,6 +81,7 @@ int main(int argc, char **argv)
     /* static.f:759-781: QLMT for modes 6, 9, 10, QAPW for mode 8, one file for
      * every structure */
     const char *qfile = (mode == 8) ? "QAPW" : (mode == 6 || mode == 9 || mode == 10) ? "QLMT" : NULL;
+    FILE *spndir = NULL;   /* static.f:1012-1017: SPNDIR for flag S, SKDERIV for flag D */
     int kneigh = 0, jstruc = 0, status = 0;
     for (;;) {
         nrltb_structure st;
@@ -101,8 +103,16 @@ int main(int argc, char **argv)
         opt.eigcut = eigcut;
         opt.fermi_tol = fermi_tol;
         opt.kneigh_in = kneigh;
+        const int spinopt = nrltb_skin_spin_options(skin);
+        if (spinopt & NRLTB_SKIN_SPIN_DIRECTIONS) opt.flags |= NRLTB_OPT_SPIN_DIRECTIONS;
+        if (spinopt & NRLTB_SKIN_TORQUES) {   /* opened, never written, as in the reference */
+            FILE *fd = fopen("SKDERIV", "a");
+            if (fd) fclose(fd);
+        }
         nrltb_result res;
         memset(&res, 0, sizeof res);
+        double spdir[3 * 4096];
+        if ((spinopt & NRLTB_SKIN_SPIN_DIRECTIONS) && st.natoms <= 4096) res.spdir = spdir;
         const int nsp = (par.jspins == 2) ? 2 : 1;
         size_t nv = 0;
         for (int i = 0; i < st.natoms; ++i) nv += (size_t)par.kbas[st.kkind[i] - 1];
@@ -156,12 +166,23 @@ int main(int argc, char **argv)
                 fprintf(skout, " P(0) = %.17G + O[T**4]\n", res.earg2);
             }
         }
-        if (par.jspins == 2)   /* bande.f:1390-1394 */
+        if (res.spdir && st.spinat) {   /* bande.f:1545-1560, (a20,i5,4f10.6,2f12.6) */
+            if (!spndir) spndir = fopen("SPNDIR", "w");
+            for (int i = 0; spndir && i < st.natoms; ++i) {
+                const double *v = spdir + 3 * i;
+                const double sm = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+                const double rad2deg = 180.0 / 3.14159265358979323846;
+                fprintf(spndir, "%-20.20s%5d%10.6f%10.6f%10.6f%10.6f%12.6f%12.6f\n", label, i + 1, v[0], v[1], v[2], sm,
+                        rad2deg * acos(v[2] / sm), rad2deg * atan2(v[1], v[0]));
+            }
+            if (spndir) fflush(spndir);
+        }
+        if (par.jspins == 2 && !st.spinat)   /* bande.f:1390-1394; none for a non-collinear run */
             fprintf(skout, "for a total magnetization of %10.5f electrons per unit cell.\n", res.smag);
         /* static.f:1238-1254: E_F and bande's two outputs (mode 3 has one), then
          * the moment for a collinear spin-polarized set */
         char tail[32] = "";
-        if (par.jspins == 2) snprintf(tail, sizeof tail, "%10.6f", res.smag);
+        if (par.jspins == 2 && !st.spinat) snprintf(tail, sizeof tail, "%10.6f", res.smag);   /* static.f:1238 */
         if (mode == 3 || mode > 4)
             fprintf(skeng, "%-20.20s%12.6f%15.9f%15.9f%s\n", label, st.volume, res.efermi, res.earg1, tail);
         else
@@ -172,6 +193,7 @@ int main(int argc, char **argv)
     }
     fclose(skout);
     fclose(skeng);
+    if (spndir) fclose(spndir);
     nrltb_ctx_destroy(ctx);
     nrltb_skin_close(skin);
     return status;

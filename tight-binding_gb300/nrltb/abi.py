@@ -33,6 +33,7 @@ NRLTB_K_TIMEOUT = 4
 
 PREC_FP64 = 0
 PREC_MIXED = 1
+OPT_SPIN_DIRECTIONS = 1
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
@@ -72,7 +73,7 @@ class Result_(C.Structure):
                 ("nonphysical_k", C.c_int), ("eig", _dp), ("deig", _dp), ("ncut", _ip),
                 ("k_status", _ip), ("entropy", C.c_double), ("free_energy", C.c_double),
                 ("entropy_shift", C.c_double), ("earg1", C.c_double), ("earg2", C.c_double),
-                ("smag", C.c_double), ("orbocc", _dp)]
+                ("smag", C.c_double), ("spdir", _dp), ("orbocc", _dp)]
 
 
 _vp = C.c_void_p
@@ -121,6 +122,7 @@ HOST_SYMBOLS = [
     ("nrltb_skin_info", C.c_int, [_vp, _ip, _dp, _dp, _pp]),
     ("nrltb_skin_next", C.c_int, [_vp, _sp, _kp, C.c_char_p, C.c_char_p]),
     ("nrltb_skin_error_line", C.c_int, [_vp]),
+    ("nrltb_skin_spin_options", C.c_int, [_vp]),
     ("nrltb_skin_close", None, [_vp]),
     ("nrltb_parfile_read", C.c_int, [C.c_char_p, C.POINTER(_vp), _pp]),
     ("nrltb_parfile_close", None, [_vp]),

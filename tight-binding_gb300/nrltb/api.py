@@ -143,12 +143,13 @@ class Opts:
     eigcut: float = 1e3
     fermi_tol: float = 0.0
     kneigh_in: int = 0
+    flags: int = 0               # abi.OPT_* bits
 
     def to_c(self):
         o = abi.Opts_()
         o.mode, o.precision = self.mode, self.precision
         o.tkb, o.eigcut, o.fermi_tol = self.tkb, self.eigcut, self.fermi_tol
-        o.kneigh_in, o.flags = self.kneigh_in, 0
+        o.kneigh_in, o.flags = self.kneigh_in, self.flags
         return o
 
 
@@ -174,6 +175,7 @@ class Result:
     earg1: float = 0.0
     earg2: float = 0.0
     smag: float = 0.0
+    spdir: np.ndarray = None    # (natoms, 3) spin vector per atom, non-collinear runs
     orbocc: np.ndarray = None   # (jspins*nk, nv states, nv orbitals), modes 5, 6, 10
 
 
@@ -186,18 +188,20 @@ def result_shape(st, par):
     return nv, max(par.jspins, 1)
 
 
-def new_result(nv, nk, want_eig=True, want_deig=True, jspins=1, want_orbocc=False):
+def new_result(nv, nk, want_eig=True, want_deig=True, jspins=1, want_orbocc=False, natoms_spdir=0):
     """Result struct with per-k arrays of jspins * nk rows (spin 1's k points
     first); want_orbocc adds the (rows, states, orbitals) Lowdin charges."""
     nrow = max(jspins, 1) * nk
     arrays = dict(eig=np.zeros((nrow, nv)) if want_eig else None,
                   deig=np.zeros((nrow, nv)) if want_deig else None,
                   ncut=np.zeros(nrow, np.int32), k_status=np.zeros(nrow, np.int32),
-                  orbocc=np.zeros((nrow, nv, nv)) if want_orbocc else None)
+                  orbocc=np.zeros((nrow, nv, nv)) if want_orbocc else None,
+                  spdir=np.zeros((natoms_spdir, 3)) if natoms_spdir else None)
     r = abi.Result_()
     r.eig = _dptr(arrays["eig"])
     r.deig = _dptr(arrays["deig"])
     r.orbocc = _dptr(arrays["orbocc"])
+    r.spdir = _dptr(arrays["spdir"])
     r.ncut = _iptr(arrays["ncut"])
     r.k_status = _iptr(arrays["k_status"])
     r._keep = arrays
@@ -267,6 +271,7 @@ class SkinFile:
     eigcut: float
     params: Params
     structures: list = field(default_factory=list)   # (title, label, Structure, KMesh)
+    spin_options: list = field(default_factory=list)  # per structure: bit 1 directions, 2 torques
 
 
 def read_skin(path, lib=None):
@@ -308,6 +313,7 @@ def read_skin(path, lib=None):
             km = KMesh(np.ctypeslib.as_array(ck.k, (ck.nk, 3)).copy(),
                        np.ctypeslib.as_array(ck.w, (ck.nk,)).copy())
             out.structures.append((title.value.decode(), label.value.decode(), st, km))
+            out.spin_options.append(lib.nrltb_skin_spin_options(h))
         return out
     finally:
         lib.nrltb_skin_close(h)
@@ -353,7 +359,8 @@ class Context:
         (nv, nsp), nk = result_shape(st, par), km.nk
         if want_orbocc is None:
             want_orbocc = opts.mode in (5, 6, 10)
-        r, arrays = new_result(nv, nk, want_eig, want_eig, nsp, want_orbocc)
+        nsd = st.natoms if (st.spinat is not None and opts.flags & abi.OPT_SPIN_DIRECTIONS) else 0
+        r, arrays = new_result(nv, nk, want_eig, want_eig, nsp, want_orbocc, nsd)
         cs, cp, ck, co = st.to_c(), par.to_c(), km.to_c(), opts.to_c()
         self._check(self.lib.nrltb_bande(self.h, C.byref(cs), C.byref(cp), C.byref(ck),
                                          C.byref(co), C.byref(r)), "nrltb_bande")
