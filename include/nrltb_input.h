@@ -58,7 +58,9 @@ int nrltb_nparams(int kinds);
  * with per-atom s, p, d or per-orbital Lowdin charges of the states below
  * eigcut; res->orbocc required), 9 (QLMT with every eigenvalue, no atoms) or 8
  * (QAPW, eigenvalues per k point).  res holds nrltb_bande's per-k arrays for
- * par->jspins spin blocks; km is the k list the structure was run on.  Mode 5
+ * par->jspins spin blocks (one block of 2N columns for non-collinear spins,
+ * whose charges go to 2 natoms pseudo-atoms, spin-down copies second); km is
+ * the k list the structure was run on.  Mode 5
  * is not written: the reference mixes formatted records into its unformatted
  * QLMT and stops there. */
 int nrltb_qlmt_write(const char *path, int append, int mode, const nrltb_structure *st,

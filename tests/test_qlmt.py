@@ -44,7 +44,9 @@ def krec(k, w, ntot):
 
 def expected(mode, st, par, km, eigcut, eig, orb):
     nv = eig.shape[1]
-    nsp = par.jspins
+    noncol = st.spinat is not None
+    nsp = 1 if noncol else par.jspins
+    atoms = list(range(st.natoms)) * (2 if noncol else 1)   # diag.f:670-693
     out = []
     if mode in (6, 10):
         out.append("%5d%5d%5d%5d     SPINS, WIND., SC. WIND." % (1, 1, 0, st.natoms))
@@ -78,7 +80,7 @@ def expected(mode, st, par, km, eigcut, eig, orb):
                 big = mode == 6 and (e <= -10.0 or e >= 100.0)
                 out.append(F(e, 10, 6 if big else 7) + E(0.0, 15, 6))
                 i0 = 0
-                for a in range(st.natoms):
+                for a in atoms:
                     nb = int(par.kbas[st.kkind[a] - 1])
                     oc = orb[row, n, i0:i0 + nb]
                     if mode == 6:
@@ -182,3 +184,19 @@ def test_oracle_charges_nonpositive_overlap():
     assert bad.sum() >= 2
     assert (r.orbocc[bad] == -1.0).all()
     assert np.abs(r.orbocc[~bad].sum(axis=2) - 1.0).max() <= 1e-12
+
+
+@pytest.mark.parametrize("mode", [6, 9, 10])
+def test_writer_noncollinear_records(tmp_path, mode):
+    """A non-collinear run: one block of 2N eigenvalues per k, charges on the
+    spin-up then the spin-down copies of every atom."""
+    st, par, km, eig, orb = _case([9, 4], 2, 2, 5)
+    nv2 = 2 * eig.shape[1]
+    rng = np.random.default_rng(9)
+    eig = np.sort(rng.uniform(-1.5, 1.5, (km.nk, nv2)), axis=1)
+    orb = rng.dirichlet(np.ones(nv2), size=(km.nk, nv2))
+    st = replace(st, spinat=np.array([[0.0, 0.0, 1.0], [1.0, 0.0, 0.0]]))
+    res = Result(0.0, 0.0, 0.0, 0.0, 0.0, 0, nv2, km.nk, 0, 0, eig=eig, orbocc=orb)
+    path = str(tmp_path / "Q")
+    write_qlmt(path, mode, st, par, km, 0.7, res)
+    assert open(path).read().split("\n")[:-1] == expected(mode, st, par, km, 0.7, eig, orb)

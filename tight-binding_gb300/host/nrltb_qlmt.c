@@ -66,10 +66,14 @@ int nrltb_qlmt_write(const char *path, int append, int mode, const nrltb_structu
     if (!path || !st || !par || !km || !res || !res->eig || !st->kkind || !par->kbas) return NRLTB_E_ARG;
     if (!(mode == 6 || mode == 8 || mode == 9 || mode == 10)) return NRLTB_E_UNSUPPORTED;
     if ((mode == 6 || mode == 10) && !res->orbocc) return NRLTB_E_ARG;
-    if (st->spinat) return NRLTB_E_UNSUPPORTED;   /* non-collinear records are not written */
     FILE *f = fopen(path, append ? "a" : "w");
     if (!f) return NRLTB_E_IO;
-    const int nv = res->nv, nk = km->nk, nsp = (par->jspins == 2) ? 2 : 1;
+    /* a non-collinear run is one 2N x 2N problem per k, its charges on 2 natoms
+     * pseudo-atoms: every atom's spin-up orbitals, then the spin-down copies
+     * (diag.f:670-693) */
+    const int noncol = st->spinat != NULL;
+    const int nv = res->nv, nk = km->nk, nsp = (par->jspins == 2 && !noncol) ? 2 : 1;
+    const int natx = noncol ? 2 * st->natoms : st->natoms;
     /* static.f:1138-1144: one header line per structure (spins written as 1) */
     if (mode == 6 || mode == 10) fprintf(f, "%5d%5d%5d%5d     SPINS, WIND., SC. WIND.\n", 1, 1, 0, st->natoms);
     else if (mode == 9) fprintf(f, "%5d%5d%5d%5d     SPINS, WIND., SC. WIND.\n", 1, 1, 0, 0);
@@ -116,8 +120,8 @@ int nrltb_qlmt_write(const char *path, int append, int mode, const nrltb_structu
                 fputc('\n', f);
                 const double *oc = orb + (size_t)n * nv;
                 int i0 = 0;
-                for (int a = 0; a < st->natoms; ++a) {
-                    const int nbas = par->kbas[st->kkind[a] - 1];
+                for (int a = 0; a < natx; ++a) {
+                    const int nbas = par->kbas[st->kkind[a % st->natoms] - 1];
                     if (mode == 6) {   /* s, p, d sums (diag.f:705-721), then 0 */
                         double s = oc[i0], p = 0.0, d = 0.0;
                         for (int q = 1; q < (nbas < 4 ? nbas : 4); ++q) p = p + oc[i0 + q];
