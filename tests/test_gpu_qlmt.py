@@ -113,3 +113,29 @@ def test_host_driver_files(tmp_path, mode):
             last = 10.0 ** -(len(x.split("E")[0].split(".")[1]) if "." in x else 0)
             scale = 10.0 ** int(x.split("E")[1]) if "E" in x else 1.0
             assert abs(float(x) - float(y)) <= 2 * last * scale, (a, b)
+
+
+def test_host_driver_p80_band_structure(tmp_path):
+    """The reference's P80 input (carbon, real-overlap parameters, mode 9 along
+    a 287-point path) with its unreadable comment line removed: the driver's
+    QLMT against the writer fed the oracle's run."""
+    import shutil
+    from conftest import GOLDEN
+    for f in ("SKIN", "C_par", "spcgrp.bcc"):
+        shutil.copy(os.path.join(GOLDEN, "P80", f), tmp_path / f)
+    path = tmp_path / "SKIN"
+    lines = [ln for ln in path.read_text().splitlines() if not ln.strip().startswith("(Position of atom")]
+    path.write_text("\n".join(lines) + "\n")
+    r = subprocess.run([build.DRIVER, "SKIN"], cwd=tmp_path, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    got = (tmp_path / "QLMT").read_text().splitlines()
+    sk = read_skin(str(path))
+    _, _, st, km = sk.structures[0]
+    res = oracle.bande(st, sk.params, km, Opts(mode=9, tkb=sk.tkb, eigcut=sk.eigcut))
+    write_qlmt(str(tmp_path / "ref"), 9, st, sk.params, km, sk.eigcut, res)
+    want = (tmp_path / "ref").read_text().splitlines()
+    assert len(got) == len(want) == 1 + 287 * (1 + 96)
+    for a, b in zip(got, want):
+        for x, y in zip(_fields(a), _fields(b)):
+            if x != y:
+                assert abs(float(x) - float(y)) <= 2e-7, (a, b)
