@@ -41,3 +41,29 @@ def test_bad_arguments_fail_cleanly():
     assert lib.nrltb_fetch(None, None) == abi.NRLTB_E_ARG
     assert lib.nrltb_ctx_create(None, 0) == abi.NRLTB_E_ARG
     assert lib.nrltb_nparams(2) == 330 and lib.nrltb_nparams(1) == 97
+
+
+def test_struct_layouts_match_the_header(tmp_path):
+    """Every field offset and struct size of include/nrltb.h, as the C compiler
+    lays them out, equals the ctypes mirror the tests and the benchmark use."""
+    import subprocess
+    structs = {"nrltb_structure": abi.Structure_, "nrltb_params": abi.Params_, "nrltb_kmesh": abi.KMesh_,
+               "nrltb_opts": abi.Opts_, "nrltb_pairs": abi.Pairs_, "nrltb_result": abi.Result_}
+    src = ["#include <stdio.h>", "#include <stddef.h>", '#include "nrltb.h"', "int main(void) {"]
+    for cname, py in structs.items():
+        src.append('printf("%s size %%zu\\n", sizeof(%s));' % (cname, cname))
+        for fname, _ in py._fields_:
+            src.append('printf("%s %s %%zu\\n", offsetof(%s, %s));' % (cname, fname, cname, fname))
+    src.append("return 0; }")
+    c = tmp_path / "layout.c"
+    c.write_text("\n".join(src) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-std=gnu11", "-I", os.path.join(REPO, "include"), str(c), "-o", str(exe)], check=True)
+    got = {}
+    for line in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.splitlines():
+        a, b, v = line.split()
+        got[(a, b)] = int(v)
+    for cname, py in structs.items():
+        assert got[(cname, "size")] == ctypes.sizeof(py), cname
+        for fname, _ in py._fields_:
+            assert got[(cname, fname)] == getattr(py, fname).offset, (cname, fname)
