@@ -200,3 +200,23 @@ def test_writer_noncollinear_records(tmp_path, mode):
     path = str(tmp_path / "Q")
     write_qlmt(path, mode, st, par, km, 0.7, res)
     assert open(path).read().split("\n")[:-1] == expected(mode, st, par, km, 0.7, eig, orb)
+
+
+def test_writer_errors(tmp_path):
+    import ctypes as C
+    from nrltb import abi
+    st, par, km, eig, orb = _case([9], 2, 1, 1)
+    lib = abi.load_host()
+    r = abi.Result_()
+    r.nv, r.nk = eig.shape[1], km.nk
+    e = np.ascontiguousarray(eig)
+    r.eig = e.ctypes.data_as(C.POINTER(C.c_double))
+    cs, cp, ck = st.to_c(), par.to_c(), km.to_c()
+    args = (C.byref(cs), C.byref(cp), C.byref(ck), 0.7, C.byref(r))
+    path = str(tmp_path / "Q").encode()
+    assert lib.nrltb_qlmt_write(path, 0, 5, *args) == abi.NRLTB_E_UNSUPPORTED    # mode 5 is not written
+    assert lib.nrltb_qlmt_write(path, 0, 4, *args) == abi.NRLTB_E_UNSUPPORTED
+    assert lib.nrltb_qlmt_write(path, 0, 6, *args) == abi.NRLTB_E_ARG            # charges required
+    assert lib.nrltb_qlmt_write(str(tmp_path / "no" / "Q").encode(), 0, 9, *args) == abi.NRLTB_E_IO
+    assert lib.nrltb_qlmt_write(None, 0, 9, *args) == abi.NRLTB_E_ARG
+    assert lib.nrltb_qlmt_write(path, 0, 9, *args) == 0
