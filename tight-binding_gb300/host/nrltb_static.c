@@ -8,9 +8,12 @@
  * names with the C readers (nrltb_input.h), then for every structure calls
  * nrltb_bande -- the drop-in for search2 + bande (static.f:1114, 1218) -- and
  * appends one line to SKENG in the reference's format (static.f:1238-1254) and
- * a summary block to SKOUT (bande.f:1405-1476 wording).  Output files go to the
- * current directory, as in the reference.  search2's carried kneigh flag
- * passes from one structure to the next as the reference's common block does.
+ * a summary block to SKOUT (bande.f:1405-1476 wording); in modes 6, 8, 9, 10
+ * the QLMT / QAPW records (bande.f:1568-1700), for spin flag S the SPNDIR lines
+ * (bande.f:1545-1560), for flag D an SKDERIV file, which the reference opens
+ * and never writes.  Output files go to the current directory, as in the
+ * reference.  search2's carried kneigh flag passes from one structure to the
+ * next as the reference's common block does.
  */
 #include <stdio.h>
 #include <stdlib.h>
