@@ -20,6 +20,13 @@ solves/s = 27 / step time.
 
 The step's working set (H, S, dH, dS and the solver workspace for 27 k) is
 several GB, far larger than L2, so no L2 flush is needed between steps.
+
+--row selects the form of the same step for the rows beyond the path (the
+default line is --row path): gillan (mode 2: entropy, E(0), P(0)), spin (a
+two-set spin-polarized version of the parameters, two spin channels per k),
+noncollinear (the two-set parameters with canted spin directions: one
+2N x 2N problem per k), charges (mode 6: Lowdin orbital charges of every
+state, downloaded in e2e).  Solves are counted per k and spin channel.
 """
 import os
 
@@ -52,9 +59,40 @@ def workload(name):
     return st, par, km, o
 
 
-def workload_desc(name, st, par, km):
-    return (f"{name}: {st.natoms}-atom supercell, N={par.nv(st)}, {km.nk} k, mode 4 "
+def workload_desc(name, st, par, km, row="path"):
+    base = (f"{name}: {st.natoms}-atom supercell, N={par.nv(st)}, {km.nk} k, mode 4 "
             f"(H/S/dH/dS build, eigensolve with vectors, Hellmann-Feynman, E_F, E, P)")
+    extra = {"path": "",
+             "gillan": "; row gillan: mode 2 (also entropy, E(0), P(0))",
+             "spin": "; row spin: two-set spin-polarized parameters, 2 channels per k",
+             "noncollinear": "; row noncollinear: two-set parameters, canted spins, 2N x 2N per k",
+             "charges": "; row charges: mode 6 (no pressure), Lowdin charges of every state"}[row]
+    return base + extra
+
+
+ROWS = ("path", "gillan", "spin", "noncollinear", "charges")
+
+
+def row_setup(row, st, par):
+    """(structure, parameters, mode, option flags, solves per k) of a row."""
+    from dataclasses import replace
+    import numpy as np
+    from nrltb import synth
+    if row == "path":
+        return st, par, 4, 0, 1
+    if row == "gillan":
+        return st, par, 2, 0, 1
+    mag = synth.magnetic_from(par)
+    if row == "spin":
+        return st, mag, 4, 0, 2
+    if row == "noncollinear":
+        # alternate the spin directions of the atoms over four canted orientations
+        dirs = np.array([[0, 0, 1], [1, 0, 0], [0, 0.6, 0.8], [-0.6, 0, -0.8]], float)
+        sp = dirs[np.arange(st.natoms) % 4]
+        return replace(st, spinat=sp), mag, 4, 0, 1
+    if row == "charges":
+        return st, par, 6, 0, 1
+    raise ValueError(row)
 
 
 class ClockSampler:
@@ -106,13 +144,13 @@ class ClockSampler:
                 "samples": len(rows), "reasons": reasons}
 
 
-def cpu_sample(st, par, km, mode, nthreads, nk_sample):
+def cpu_sample(st, par, km, mode, nthreads, nk_sample, flags=0):
     """Oracle (reference algorithm) on the first nk_sample k points, all threads."""
     sys.path.insert(0, os.path.join(REPO, "oracle"))
     import oracle
     from nrltb import KMesh, Opts
     sub = KMesh(km.k[:nk_sample], km.w[:nk_sample] / km.w[:nk_sample].sum())
-    opts = Opts(mode=mode, tkb=0.005, eigcut=1e3)
+    opts = Opts(mode=mode, tkb=0.005, eigcut=1e3, flags=flags)
     t0 = time.perf_counter()
     oracle.bande(st, par, sub, opts, nthreads=nthreads)
     return time.perf_counter() - t0
@@ -122,23 +160,24 @@ def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
         return 0
-    st, par, km, o = workload(args.config)
+    st0, par0, km, o = workload(args.config)
+    st, par, mode, flags, per_k = row_setup(args.row, st0, par0)
     ncores = os.cpu_count() or 1
     nks = min(km.nk, ncores)
     times = []
     for i in range(args.warmup + args.steps):
-        t = cpu_sample(st, par, km, 4, ncores, nks)
+        t = cpu_sample(st, par, km, mode, ncores, nks, flags)
         if i >= args.warmup:
             times.append(t)
     mean = sum(times) / len(times)
-    value = nks / mean
-    sample = (f"{nks} of the {km.nk} k points per step (one per host thread), mode 4: setham + "
+    value = per_k * nks / mean
+    sample = (f"{nks} of the {km.nk} k points per step (one per host thread), mode {mode}: setham + "
               f"zhpgv with vectors + sethamv + perturb, then Fermi/E/P")
     line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference",
             "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": mean * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded structure and parameters)",
-            "config": {"workload": workload_desc(args.config, st, par, km), "host_cores": ncores},
+            "config": {"workload": workload_desc(args.config, st0, par0, km, args.row), "host_cores": ncores},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": ncores, "kind": "port",
                              "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -229,6 +268,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--config", default="fcc128")
+    ap.add_argument("--row", default="path", choices=ROWS)
     ap.add_argument("--precision", default="auto", choices=["auto", "fp64", "mixed"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
@@ -246,12 +286,13 @@ def main():
     from nrltb import Context, Opts, abi
     ctx = Context(local)
     lib = ctx.lib
-    st, par, km, o = workload(args.config)
-    nk = km.nk
+    st0, par0, km, o = workload(args.config)
+    st, par, mode, flags, per_k = row_setup(args.row, st0, par0)
+    nk = km.nk * per_k   # solves per step: k points times spin channels
     prec = {"fp64": abi.PREC_FP64, "mixed": abi.PREC_MIXED}.get(args.precision)
     if prec is None:
-        prec = abi.PREC_MIXED if _mixed_available(ctx, st, par, km) else abi.PREC_FP64
-    opts = Opts(mode=4, precision=prec, tkb=o["tkb"], eigcut=1e3, fermi_tol=1e-11)
+        prec = abi.PREC_MIXED if _mixed_available(ctx, st0, par0, km) else abi.PREC_FP64
+    opts = Opts(mode=mode, precision=prec, tkb=o["tkb"], eigcut=1e3, fermi_tol=1e-11, flags=flags)
 
     stream = torch.cuda.Stream(local)
     ctx.set_stream(stream.cuda_stream)
@@ -312,9 +353,12 @@ def main():
     ms_e2e = max_over_ranks((time.perf_counter() - t0) * 1e3 / args.steps)
     launches_e2e = ctx.launch_count() - l1
     e2e_value = ws * nk / (ms_e2e * 1e-3)
-    h2d = (st.kkind.nbytes + st.posn.nbytes + st.posq.nbytes + par.kbas.nbytes + par.dnn.nbytes +
+    h2d = ((st.spinat.nbytes if st.spinat is not None else 0) +
+           st.kkind.nbytes + st.posn.nbytes + st.posq.nbytes + par.kbas.nbytes + par.dnn.nbytes +
            par.screenl.nbytes + par.param.nbytes + km.k.nbytes + km.w.nbytes + 8 * 3 * st.natoms)
     d2h = r.eig.nbytes + r.deig.nbytes + r.ncut.nbytes + r.k_status.nbytes + 64
+    if r.orbocc is not None:
+        d2h += r.orbocc.nbytes
 
     # ---- roofline of the dominant kernel class, from the timed region's events ----
     roofline = roofline_of(lib, ctx, kernels, prec)
@@ -324,7 +368,7 @@ def main():
             "scaling": "weak", "vs_baseline": None,
             "dtype": "f64" if prec == abi.PREC_FP64 else "f32+f64",
             "data": "synthetic (seeded structure and parameters, no public dataset)",
-            "config": {"workload": workload_desc(args.config, st, par, km),
+            "config": {"workload": workload_desc(args.config, st0, par0, km, args.row),
                        "precision": "fp64" if prec == abi.PREC_FP64 else "mixed",
                        "l2": "inputs larger than L2 (H,S,dH,dS + workspace of 27 k are GBs)",
                        "E_F": res.efermi, "E_total": res.e_total, "P": res.pressure},
@@ -336,10 +380,10 @@ def main():
 
     if rank == 0 and not args.no_cpu_baseline:
         ncores = os.cpu_count() or 1
-        nks = min(nk, ncores)
-        t = cpu_sample(st, par, km, 4, ncores, nks)
-        line["cpu_baseline"] = {"value": nks / t, "unit": UNIT, "cores": ncores, "kind": "port",
-                                "sample": f"{nks} of {nk} k points, one per host thread, mode 4 "
+        nks = min(km.nk, ncores)
+        t = cpu_sample(st, par, km, mode, ncores, nks, flags)
+        line["cpu_baseline"] = {"value": per_k * nks / t, "unit": UNIT, "cores": ncores, "kind": "port",
+                                "sample": f"{nks} of {km.nk} k points, one per host thread, mode {mode} "
                                           f"(setham + zhpgv with vectors + sethamv + perturb + Fermi/E/P)"}
     if rank == 0:
         print(json.dumps(line), flush=True)

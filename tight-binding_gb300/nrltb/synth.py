@@ -87,12 +87,11 @@ def make_params(kbas_list, valence_list, seed, dnn=16.5, screenl=0.5, s_scale=1.
                   np.full(nint, dnn), np.full(nint, screenl), p, 1, 0)
 
 
-def make_magnetic_params(kbas_list, valence_list, seed, split=0.08, dnn=16.5, screenl=0.5):
-    """A collinear spin-polarized set (jspins = 2): the spin-1 set drawn as
-    make_params does, the spin-2 set equal to it except for the on-site
-    polynomials' constant terms, raised by `split` Ry (an exchange splitting),
-    and the density parameters, scaled by 1.05."""
-    base = make_params(kbas_list, valence_list, seed, dnn=dnn, screenl=screenl)
+def magnetic_from(base, split=0.08):
+    """A collinear spin-polarized set (jspins = 2) from a spin-restricted one:
+    the spin-2 set equals it except for the on-site polynomials' constant terms,
+    raised by `split` Ry (an exchange splitting), and the density parameters,
+    scaled by 1.05; hopping and overlap integrals are shared."""
     p2 = base.param.copy()
     for k in range(base.kinds):
         ip = k * 17
@@ -100,7 +99,12 @@ def make_magnetic_params(kbas_list, valence_list, seed, split=0.08, dnn=16.5, sc
         for o in range(4):
             p2[ip + 1 + 4 * o] += split
     return Params(base.kinds, base.kbas, base.valence, base.dnn, base.screenl,
-                  np.concatenate([base.param, p2]), 1, 0, 2)
+                  np.concatenate([base.param, p2]), base.jsover, base.nltype, 2)
+
+
+def make_magnetic_params(kbas_list, valence_list, seed, split=0.08, dnn=16.5, screenl=0.5):
+    """make_params' set made spin-polarized by magnetic_from."""
+    return magnetic_from(make_params(kbas_list, valence_list, seed, dnn=dnn, screenl=screenl), split)
 
 
 def search_box(plv, dnn):
