@@ -990,6 +990,7 @@ int oracle_bande(const nrltb_structure *st, const nrltb_params *par, const nrltb
     double zfill = st->zcharge;
     for (int i = 0; i < st->natoms; ++i) { nv += par->kbas[st->kkind[i] - 1]; zfill += par->valence[st->kkind[i] - 1]; }
     const int nvx = noncol ? 2 * nv : nv;   /* order of the secular equation */
+    if (!(zfill > 0)) return NRLTB_E_ARG;   /* fermi.f:165 stops: no solution */
     nrltb_pairs pr;
     long cap = pair_bound(st);
     if (alloc_pairs(&pr, (int)cap)) return NRLTB_E_NOMEM;

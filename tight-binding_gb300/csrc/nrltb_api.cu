@@ -648,6 +648,7 @@ static int run_all(nrltb_ctx *c)
     }
     if (!(o.precision == NRLTB_PREC_FP64 || o.precision == NRLTB_PREC_MIXED)) { set_err("precision"); return NRLTB_E_ARG; }
     if (S.nk < 1) { set_err("no k points"); return NRLTB_E_ARG; }
+    if (!(S.zfill > 0)) { set_err("zfill = %g <= 0: no Fermi level (fermi.f:165)", S.zfill); return NRLTB_E_ARG; }
     const int lpress = (o.mode == 2 || o.mode == 4);   // bande.f:726-730
     const int lentro = (o.mode < 3);
     const int lqlmt = (o.mode == 5 || o.mode == 6 || o.mode == 10);   // orbital charges, diag.f:526
