@@ -17,6 +17,7 @@
 #include <mutex>
 #include <new>
 #include <thread>
+#include <nvtx3/nvToolsExt.h>
 #include "nrltb.h"
 #include "nrltb_bench.h"
 #include "common.cuh"
@@ -201,6 +202,15 @@ template <typename T> static int upload(DBuf &b, const std::vector<T> &v, cudaSt
     return NRLTB_OK;
 }
 
+// NVTX range over a scope: each stage of the path is a named range for
+// profilers (a no-op when none is attached)
+struct NvtxRange {
+    explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange &) = delete;
+    NvtxRange &operator=(const NvtxRange &) = delete;
+};
+
 // ---- validation and staging ----------------------------------------------
 static int check_inputs(const nrltb_structure *st, const nrltb_params *par)
 {
@@ -319,6 +329,7 @@ static int stage_host(nrltb_ctx *c, const nrltb_structure *st, const nrltb_param
 // ---- stages on the device -------------------------------------------------
 static int run_search2(nrltb_ctx *c, int kneigh_in)
 {
+    NvtxRange nv_("search2");
     cudaStream_t s = c->stream;
     const Staged &S = c->st;
     const long box = (long)(2 * S.nd[0] + 1) * (2 * S.nd[1] + 1) * (2 * S.nd[2] + 1);
@@ -366,6 +377,7 @@ static int run_search2(nrltb_ctx *c, int kneigh_in)
 
 static int run_setpar(nrltb_ctx *c, int deriv, int js = 0)
 {
+    NvtxRange nv_("setpar");
     cudaStream_t s = c->stream;
     const Staged &S = c->st;
     const int P = std::max(c->npairs, 1);
@@ -412,6 +424,7 @@ static NcView nc_view(nrltb_ctx *c)
 // non-collinear on-site terms and the per-orbital spin terms
 static int run_noncol_setup(nrltb_ctx *c, int lpress)
 {
+    NvtxRange nv_("noncollinear setup");
     const Staged &S = c->st;
     cudaStream_t s = c->stream;
     RET(c->d_nc.ensure(nc_bytes(S.natoms, S.kinds, S.nv)));
@@ -451,6 +464,7 @@ static int run_noncol_expand(nrltb_ctx *c, int nkc, const double2 *Hn, const dou
 
 static int run_skblocks(nrltb_ctx *c, int nwhich)
 {
+    NvtxRange nv_("Slater-Koster blocks");
     cudaStream_t s = c->stream;
     const Staged &S = c->st;
     const int P = std::max(c->npairs, 1);
@@ -469,6 +483,7 @@ static int run_skblocks(nrltb_ctx *c, int nwhich)
 // dense matrices of k points [k0, k0+nk) into H, S (which0 0: H/S, 2: dH/dS)
 static int run_bloch(nrltb_ctx *c, int k0, int nk, int which0, double2 *M1, double2 *M2)
 {
+    NvtxRange nv_(which0 ? "Bloch sums dH dS" : "Bloch sums H S");
     cudaStream_t s = c->stream;
     const Staged &S = c->st;
     const int P = std::max(c->npairs, 1), nv = S.nv;
@@ -514,6 +529,7 @@ static int choose_chunk(int nv, int nk, int prec, size_t extra_per_k = 0)
 static int run_solve(nrltb_ctx *c, int nv, int nkc, int prec, const double2 *H, const double2 *S, double *eig,
                      double2 *Zout, int *status, bool vectors)
 {
+    NvtxRange nv_(prec == NRLTB_PREC_FP64 ? "eigensolve FP64" : "eigensolve mixed");
     cudaStream_t s = c->stream;
     if (prec == NRLTB_PREC_FP64) {
         RET(c->d_work.ensure(eig_work_bytes<double>(nv, nkc)));
@@ -581,6 +597,7 @@ static size_t lowdin_bytes_per_k(int nv) { return 3 * sizeof(double2) * (size_t)
 static int run_lowdin(nrltb_ctx *c, int nv, int nkc, const double2 *S, const double2 *Z, const int *status,
                       double *orb)
 {
+    NvtxRange nv_("orbital charges");
     cudaStream_t s = c->stream;
     const size_t nn = (size_t)nv * nv;
     const size_t mat = (sizeof(double2) * nn * nkc + 255) & ~size_t(255);
@@ -732,6 +749,7 @@ static int run_all(nrltb_ctx *c)
                     CKL();
                 }
                 if (lpress) {
+                    NvtxRange nv_("Hellmann-Feynman");
                     if (S.noncol) {
                         if ((rc = run_bloch(c, k0, nkc, 2, Hn, Sn))) break;
                         if ((rc = run_noncol_expand(c, nkc, Hn, Sn, true))) break;
@@ -755,6 +773,7 @@ static int run_all(nrltb_ctx *c)
                 cudaMemsetAsync(c->d_deig.as<double>() + (size_t)kc.first * nv, 0, sizeof(double) * nv, s);
             }
         }
+        NvtxRange nv_("Fermi level and sums");
         FermiJob job;
         job.eig = c->d_eig.as<double>();
         job.deig = c->d_deig.as<double>();
