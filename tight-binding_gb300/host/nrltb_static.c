@@ -114,8 +114,8 @@ int main(int argc, char **argv)
         }
         nrltb_result res;
         memset(&res, 0, sizeof res);
-        double spdir[3 * 4096];
-        if ((spinopt & NRLTB_SKIN_SPIN_DIRECTIONS) && st.natoms <= 4096) res.spdir = spdir;
+        double *spdir = (spinopt & NRLTB_SKIN_SPIN_DIRECTIONS) ? malloc(sizeof(double) * 3 * (size_t)st.natoms) : NULL;
+        res.spdir = spdir;
         const int nsp = (par.jspins == 2) ? 2 : 1;
         size_t nv = 0;
         for (int i = 0; i < st.natoms; ++i) nv += (size_t)par.kbas[st.kkind[i] - 1];
@@ -125,7 +125,7 @@ int main(int argc, char **argv)
             if (mode == 6 || mode == 10) orbbuf = malloc(sizeof(double) * nv * nv * (size_t)km.nk * nsp);
             if (!eigbuf || ((mode == 6 || mode == 10) && !orbbuf)) {
                 fprintf(stderr, "nrltb_static: structure %d: out of host memory\n", jstruc);
-                free(eigbuf); free(orbbuf);
+                free(eigbuf); free(orbbuf); free(spdir);
                 status = 1;
                 break;
             }
@@ -140,6 +140,7 @@ int main(int argc, char **argv)
         free(eigbuf);
         free(orbbuf);
         if (rc != NRLTB_OK) {
+            free(spdir);
             if (rc != NRLTB_E_IO) fprintf(stderr, "nrltb_static: structure %d: %s\n", jstruc, nrltb_last_error());
             status = 1;
             break;
@@ -180,6 +181,7 @@ int main(int argc, char **argv)
             }
             if (spndir) fflush(spndir);
         }
+        free(spdir);
         if (par.jspins == 2 && !st.spinat)   /* bande.f:1390-1394; none for a non-collinear run */
             fprintf(skout, "for a total magnetization of %10.5f electrons per unit cell.\n", res.smag);
         /* static.f:1238-1254: E_F and bande's two outputs (mode 3 has one), then
