@@ -1,6 +1,14 @@
 """Mixed-precision form (FP32 eigensolve + FP64-accurate refinement) against the
 FP64 oracle.  Tolerances: eigenvalues 1e-9 Ry, E_F 1e-9 Ry, E_total 1e-8 Ry/atom,
-pressure 1e-3 kbar (6.8e-9 Ry/bohr^3)."""
+pressure 1e-3 kbar (6.8e-9 Ry/bohr^3).
+
+Eigenvectors: each z_j is S-normalised to 1e-9 (z_j^H S z_j = 1 is what the
+orbital charges sum to), and distinct eigenvectors are S-orthogonal to 1e-7.
+The off-diagonal bound is the refinement's: its two FP32 products X'^H r' and
+X' E run on the tensor cores, whose FP32 accumulation truncates, and an error
+of ~1e-12 in a residual projection divided by a gap of ~1e-4 Ry leaves
+~1e-8 between near-degenerate states (no output of the path depends on the
+off-diagonal)."""
 import numpy as np
 import pytest
 
@@ -29,6 +37,9 @@ def _check(ctx, H, S):
         Z = gz[k]
         res = H[k] @ Z - (S[k] @ Z) * ge[k][None, :]
         assert np.abs(res).max() < 1e-6
+        gram = Z.conj().T @ S[k] @ Z - np.eye(Z.shape[1])
+        assert np.abs(np.diag(gram)).max() <= 1e-9, np.abs(np.diag(gram)).max()
+        assert np.abs(gram).max() <= 1e-7, np.abs(gram).max()
     return err
 
 

@@ -6,20 +6,28 @@
 //   1. Y_H = H X, Y_S = S X to FP64 accuracy on the bf16 tensor cores
 //      (exact digit splitting, ozaki.cuh; X is first rounded to 24 bits below
 //      each column's largest element so that the products are exact for the
-//      X used by every later step), and the
-//      residuals r_j = Y_H[:, j] - l~_j Y_S[:, j] in FP64.  The residuals are
-//      small (~1e-6), so G = X^H r (G_ij = T_ij - l~_j R_ij with T = X^H H X,
-//      R = X^H S X) is accurate to ~1e-13 even as an FP32 GEMM; only the
-//      diagonals T_jj, R_jj and the cluster blocks below need FP64 dot products.
-//   2. Clusters: estimates T_jj / R_jj closer than delta (a fraction of the
-//      spectral span) are grouped; each cluster's block (T_c, R_c) is solved
-//      exactly (Cholesky + complex Jacobi, FP64), giving a rotation U_c
-//      (Rayleigh-Ritz inside the cluster).
-//   3. With G' = U^H G U (U block diagonal), one Newton-type correction of the
-//      whole basis (Ogita-Aishima): for i, j in different clusters
-//      E_ij = G'_ij / (l_j - l_i), E_jj = (1 - R'_jj) / 2, and the eigenvalue
-//      with its second-order term  l_j + sum_{i not in c(j)} |G'_ij|^2 / (l_j - l_i).
-//   4. Z = X U (I + E) in FP64 (X U in FP64, the small X U E in FP32), columns
+//      X used by every later step), and the diagonals T_jj = x_j^H H x_j,
+//      R_jj = x_j^H S x_j by FP64 dot products.
+//   2. Clusters: Rayleigh quotients T_jj / R_jj closer than delta (a fraction
+//      of the spectral span) are grouped; each cluster's block (T_c, R_c) is
+//      solved exactly (Cholesky + complex Jacobi, FP64), giving a rotation U_c
+//      (Rayleigh-Ritz inside the cluster) and the eigenvalues l_j.
+//   3. In the rotated basis X' = X U (FP64) the residuals
+//      r'_j = Y_H u_j - l_j Y_S u_j (FP64; u_j column j of the block-diagonal
+//      U), and G' = X'^H r' as an FP32 GEMM: r' ~ 1e-6, so G'_ij =
+//      T'_ij - l_j R'_ij is accurate to ~1e-13 and uses, for every column, the
+//      same l_j as the gaps below.
+//   4. One Newton-type correction of the whole basis (Ogita-Aishima): for i, j
+//      in different clusters E_ij = G'_ij / (l_j - l_i), E_jj = (1 - R'_jj) / 2,
+//      zero inside a cluster; the eigenvalue with its second-order term
+//      l_j + sum_{i not in c(j)} |G'_ij|^2 / (l_j - l_i).  Because every G'_ij
+//      carries the l_j of its own gap, E + E^H = -(R' - I) exactly to first
+//      order, and the Gram matrix of X'(I + E) is I - F to second order with
+//      F = E^H E + E E + E^H E^H; adding F / 2 to E leaves an S-orthonormality
+//      error third order in E.  F's diagonal is summed over all i; its
+//      off-diagonal, where the large (small-gap) entries of E meet, over the
+//      sorted neighbours within REF_BAND positions.
+//   5. Z = X' (I + E) in FP64 (X' in FP64, the small X' E in FP32), columns
 //      reordered by ascending eigenvalue.
 // One step takes FP32-level eigenpairs (errors ~1e-6 Ry) to eigenvalue errors
 // far below 1e-9 Ry; the remaining error is third order in the FP32 error.
@@ -34,6 +42,9 @@ namespace nrltb {
 
 constexpr int REF_CMAX = 16;            // largest cluster solved exactly
 constexpr double REF_DELTA_REL = 5e-5;  // cluster threshold, fraction of the spectral span
+// second-order Gram terms: sorted neighbours within REF_BAND positions; REF_BT
+// sorted positions per CTA
+constexpr int REF_BAND = 16, REF_BT = 64, REF_BR = REF_BT + 2 * REF_BAND;
 
 static inline size_t al256(size_t x) { return (x + 255) & ~size_t(255); }
 
@@ -52,32 +63,22 @@ void refine_work_carve(RefineWork &w, void *base, int n, int batch)
     char *b = (char *)base;
     auto take = [&](size_t bytes) { void *p = b + off; off = al256(off + bytes); return p; };
     w.n = n; w.batch = batch;
-    w.YH = (double2 *)take(sizeof(double2) * nn);                  // H X, later X U in FP64
-    w.YS = (double2 *)take(sizeof(double2) * nn);                  // S X, later the corrected eigenvalues
-    w.G = (float2 *)take(sizeof(float2) * nn);                     // X^H r
+    w.YH = (double2 *)take(sizeof(double2) * nn);                  // H X, later X'^H and E^H E + ...
+    w.YS = (double2 *)take(sizeof(double2) * nn);                  // S X, later G'^H, E^H
+    w.Xd = (double2 *)take(sizeof(double2) * nn);                  // X' = X U in FP64
+    w.G = (float2 *)take(sizeof(float2) * nn);                     // X'^H r', later E + E^H
     w.U = (double2 *)take(sizeof(double2) * nb * REF_CMAX);       // per column: coefficients on its cluster
-    w.Ef = (float2 *)take(sizeof(float2) * nn);                    // residuals r, later E
-    w.Xr = (float2 *)take(sizeof(float2) * nn);
+    w.Ef = (float2 *)take(sizeof(float2) * nn);                    // residuals r', later E
+    w.Xr = (float2 *)take(sizeof(float2) * nn);                    // X' in FP32
     w.XE = (float2 *)take(sizeof(float2) * nn);
+    w.Fb = (float2 *)take(sizeof(float2) * nb * (2 * REF_BAND + 1));   // band of the Gram term
     w.oz = take(ozaki_work_bytes(n, batch));
     w.lam = (double *)take(sizeof(double) * nb * 4);               // l | R'_jj | T_jj | R_jj
     w.cl = (int *)take(sizeof(int) * nb * 4);                      // ord | pos0 | size | rank
     if (!base) w.cl = (int *)(uintptr_t)off;
 }
 
-// ---- 1. residuals and accurate diagonals -----------------------------------
-__global__ void k_ref_resid(RefineWork w, const double *lt)
-{
-    const int n = w.n;
-    const long nn = (long)n * n;
-    const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
-    if (t >= nn * w.batch) return;
-    const int b = (int)(t / nn), j = (int)((t - b * nn) / n);
-    const double l = lt[(long)b * n + j];
-    const double2 yh = w.YH[t], ys = w.YS[t];
-    w.Ef[t] = make_float2((float)(yh.x - l * ys.x), (float)(yh.y - l * ys.y));
-}
-
+// ---- 1. accurate diagonals -------------------------------------------------
 // T_jj = x_j^H (H x_j), R_jj = x_j^H (S x_j) in FP64; warp per column
 __global__ void k_ref_diag(RefineWork w, const float2 *X)
 {
@@ -375,73 +376,10 @@ __global__ void __launch_bounds__(REF_CMAX * REF_CMAX) k_ref_rr(RefineWork w, co
     const int *csz = w.cl + 2 * nb + (long)b * n;                              \
     const double2 *U = w.U + (long)b * n * REF_CMAX;
 
-// element (i, j) of G' = U^H G U for the block-diagonal cluster rotation U,
-// in FP32 (G itself is an FP32 product; its entries are residual-sized)
-__device__ __forceinline__ float2 rotated_g(const float2 *G, const double2 *U, const int *ord, const int *pos0,
-                                            const int *csz, int n, int i, int j)
-{
-    const int ci = csz[i], cj = csz[j];
-    if (ci == 1 && cj == 1) return G[i + (long)j * n];
-    float2 s = make_float2(0.f, 0.f);
-    for (int a = 0; a < ci; ++a) {
-        const int ga = (ci == 1) ? i : ord[pos0[i] + a];
-        float2 ua = make_float2(1.f, 0.f);
-        if (ci > 1) {
-            const double2 u = U[(long)i * REF_CMAX + a];
-            ua = make_float2((float)u.x, (float)-u.y);
-        }
-        float2 t = make_float2(0.f, 0.f);
-        for (int bb = 0; bb < cj; ++bb) {
-            const int gb = (cj == 1) ? j : ord[pos0[j] + bb];
-            float2 ub = make_float2(1.f, 0.f);
-            if (cj > 1) {
-                const double2 u = U[(long)j * REF_CMAX + bb];
-                ub = make_float2((float)u.x, (float)u.y);
-            }
-            cfma(t, G[ga + (long)gb * n], ub);
-        }
-        cfma(s, ua, t);
-    }
-    return s;
-}
-
-// 3. E column j and the second-order eigenvalue term (warp per column).  The
-// gaps l_j - l_i are formed in FP64; E and the second-order terms (products of
-// residual-sized FP32 entries) in FP32.
-__global__ void k_ref_update(RefineWork w, double *l2out)
-{
-    const int warp = (int)((blockIdx.x * (long)blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
-    const int n = w.n;
-    if (warp >= n * w.batch) return;
-    const int b = warp / n, j = warp % n;
-    const long mo = (long)b * n * n;
-    REF_VIEWS
-    const double *l1 = w.lam + (long)b * n;
-    const double lj = l1[j], rjj = w.lam[nb + (long)b * n + j];
-    const int pj = pos0[j];
-    float corr = 0.f;
-    float2 *E = w.Ef + mo + (long)j * n;
-    const float2 *G = w.G + mo;
-    for (int i = lane; i < n; i += 32) {
-        float2 e;
-        if (i == j) {
-            e = make_float2((float)(0.5 * (1.0 - rjj)), 0.f);
-        } else if (pos0[i] == pj) {
-            e = make_float2(0.f, 0.f);
-        } else {
-            const float2 g = rotated_g(G, U, ord, pos0, csz, n, i, j);
-            const float rden = 1.f / (float)(lj - l1[i]);
-            e = make_float2(g.x * rden, g.y * rden);
-            corr += (g.x * g.x + g.y * g.y) * rden;
-        }
-        E[i] = e;
-    }
-    corr = warp_sum(corr);
-    if (lane == 0) l2out[(long)b * n + j] = lj + (double)corr;
-}
-
-// 4a. X U in FP64 (into YH) and FP32 (into Xr); thread per element
-__global__ void k_ref_rotate(RefineWork w, const float2 *X)
+// 3. X' = X U in FP64 (Xd) and FP32 (Xr), and the residuals of the rotated
+// basis r'_j = sum_a (Y_H[:, m_a] - l_j Y_S[:, m_a]) U_aj in FP64 (into Ef as
+// FP32), m_a the members of column j's cluster; thread per element
+__global__ void k_ref_rotres(RefineWork w, const float2 *X)
 {
     const int n = w.n;
     const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
@@ -451,23 +389,150 @@ __global__ void k_ref_rotate(RefineWork w, const float2 *X)
     const long e = t - b * nn;
     const int r = (int)(e % n), j = (int)(e / n);
     REF_VIEWS
-    const float2 *Xb = X + b * nn;
-    double2 v;
+    const long mo = b * nn;
+    const double l = w.lam[(long)b * n + j];
+    double2 v, res;
     if (csz[j] == 1) {
-        const float2 x = Xb[r + (long)j * n];
+        const float2 x = X[mo + r + (long)j * n];
         v = make_double2(x.x, x.y);
+        const double2 yh = w.YH[t], ys = w.YS[t];
+        res = make_double2(yh.x - l * ys.x, yh.y - l * ys.y);
     } else {
         v = make_double2(0, 0);
+        double2 h = make_double2(0, 0), sx = make_double2(0, 0);
         for (int a = 0; a < csz[j]; ++a) {
-            const float2 x = Xb[r + (long)ord[pos0[j] + a] * n];
-            v = cadd(v, cmul(make_double2(x.x, x.y), U[(long)j * REF_CMAX + a]));
+            const long src = mo + r + (long)ord[pos0[j] + a] * n;
+            const double2 u = U[(long)j * REF_CMAX + a];
+            const float2 x = X[src];
+            v = cadd(v, cmul(make_double2(x.x, x.y), u));
+            h = cadd(h, cmul(w.YH[src], u));
+            sx = cadd(sx, cmul(w.YS[src], u));
         }
+        res = make_double2(h.x - l * sx.x, h.y - l * sx.y);
     }
-    w.YH[t] = v;
+    w.Xd[t] = v;
     w.Xr[t] = make_float2((float)v.x, (float)v.y);
+    w.Ef[t] = make_float2((float)res.x, (float)res.y);
 }
 
-// 4b. ascending order of the refined eigenvalues
+// 4. E column j and the second-order eigenvalue term (warp per column), from
+// G' (column j) and Gt = G'^H (column j = the conjugate of row j of G').  The
+// gaps l_j - l_i are formed in FP64; E and the second-order terms (products of
+// residual-sized FP32 entries) in FP32.  Also the diagonal of the second-order
+// Gram term F = E^H (E + E^H) + E E over all i, F_jj = sum_i |E_ij|^2 +
+// 2 Re(E_ij E_ji), into lam[3 nb ..] (the R_jj slots, no longer read); the
+// refined eigenvalues go to lam[2 nb ..] (the T_jj slots).
+__global__ void k_ref_update(RefineWork w, const float2 *Gt)
+{
+    const int warp = (int)((blockIdx.x * (long)blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+    const int n = w.n;
+    if (warp >= n * w.batch) return;
+    const int b = warp / n, j = warp % n;
+    const long mo = (long)b * n * n;
+    const long nb = (long)n * w.batch;
+    const int *pos0 = w.cl + nb + (long)b * n;
+    const double *l1 = w.lam + (long)b * n;
+    const double lj = l1[j], rjj = w.lam[nb + (long)b * n + j];
+    const int pj = pos0[j];
+    float corr = 0.f, fjj = 0.f;
+    float2 *E = w.Ef + mo + (long)j * n;
+    const float2 *Gj = w.G + mo + (long)j * n, *Gtj = Gt + mo + (long)j * n;
+    for (int i = lane; i < n; i += 32) {
+        float2 e;
+        if (i == j) {
+            const float ed = (float)(0.5 * (1.0 - rjj));
+            e = make_float2(ed, 0.f);
+            fjj += 3.f * ed * ed;
+        } else if (pos0[i] == pj) {
+            e = make_float2(0.f, 0.f);
+        } else {
+            const float2 g = Gj[i], gt = Gtj[i];
+            const float rden = 1.f / (float)(lj - l1[i]);
+            e = make_float2(g.x * rden, g.y * rden);
+            // E_ji = G'_ji / (l_i - l_j) = -conj(Gt_ij) rden
+            const float2 c = make_float2(-gt.x * rden, gt.y * rden);
+            fjj += e.x * e.x + e.y * e.y + 2.f * (e.x * c.x - e.y * c.y);
+            corr += (g.x * g.x + g.y * g.y) * rden;
+        }
+        E[i] = e;
+    }
+    corr = warp_sum(corr);
+    fjj = warp_sum(fjj);
+    if (lane == 0) {
+        w.lam[2 * nb + (long)b * n + j] = lj + (double)corr;
+        w.lam[3 * nb + (long)b * n + j] = (double)fjj;
+    }
+}
+
+// 4b. Off-diagonal second-order Gram terms near the diagonal of the sorted
+// spectrum.  F_ij = sum_k conj(E_ki) (E_kj + conj(E_jk)) + E_ik E_kj is
+// formed for the sorted neighbours i of j within REF_BAND positions, summing
+// over the k within REF_BAND positions of j: the large entries of E, those of
+// small gaps, all lie there (away from it |E| ~ |r| / gap is ~1e-7 and its
+// products ~1e-13).  A CTA takes REF_BT consecutive sorted positions and
+// gathers the (REF_BT + 2 REF_BAND)^2 block of E they need into shared memory
+// (sorted coordinates); output Fb[b][j][d + REF_BAND] for i = ord[pos(j) + d].
+constexpr int REF_BAND_SMEM = REF_BR * REF_BR * (int)sizeof(float2);
+
+__global__ void __launch_bounds__(256) k_ref_band(RefineWork w, float2 *Fb)
+{
+    extern __shared__ float2 eb[];   // eb[c * REF_BR + r] = E[ord[q0 + r], ord[q0 + c]]
+    const int n = w.n, b = blockIdx.y, p0 = blockIdx.x * REF_BT, q0 = p0 - REF_BAND, tid = threadIdx.x;
+    const long mo = (long)b * n * n;
+    const int *ord = w.cl + (long)b * n;
+    const float2 *E = w.Ef + mo;
+    for (int t = tid; t < REF_BR * REF_BR; t += blockDim.x) {
+        const int c = t / REF_BR, r = t - c * REF_BR, qc = q0 + c, qr = q0 + r;
+        float2 v = make_float2(0.f, 0.f);
+        if (qc >= 0 && qc < n && qr >= 0 && qr < n) v = E[(long)ord[qr] + (long)ord[qc] * n];
+        eb[t] = v;
+    }
+    __syncthreads();
+    constexpr int W = 2 * REF_BAND + 1;
+    for (int t = tid; t < REF_BT * W; t += blockDim.x) {
+        const int pl = t / W, d = t - pl * W - REF_BAND;
+        const int p = p0 + pl;
+        if (p >= n) continue;
+        const int cj = pl + REF_BAND, ci = cj + d;        // local sorted coordinates of j and i
+        float2 f = make_float2(0.f, 0.f);
+        if (d != 0 && p + d >= 0 && p + d < n) {
+            for (int ck = cj - REF_BAND; ck <= cj + REF_BAND; ++ck) {
+                const float2 eki = eb[ci * REF_BR + ck], ekj = eb[cj * REF_BR + ck];
+                const float2 ejk = eb[ck * REF_BR + cj], eik = eb[ck * REF_BR + ci];
+                const float2 pkj = make_float2(ekj.x + ejk.x, ekj.y - ejk.y);
+                cfmac(f, eki, pkj);
+                cfma(f, eik, ekj);
+            }
+        }
+        Fb[((long)b * n + ord[p]) * W + d + REF_BAND] = f;
+    }
+}
+
+// 4c. E += F / 2 on the band and the diagonal (thread per band entry)
+__global__ void k_ref_band_apply(RefineWork w, const float2 *Fb)
+{
+    constexpr int W = 2 * REF_BAND + 1;
+    const int n = w.n;
+    const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (t >= (long)n * w.batch * W) return;
+    const int d = (int)(t % W) - REF_BAND;
+    const long bp = t / W;
+    const int b = (int)(bp / n), p = (int)(bp - (long)b * n);   // sorted position p
+    const long nb = (long)n * w.batch;
+    const int *ord = w.cl + (long)b * n;
+    const int j = ord[p];
+    float2 *E = w.Ef + (long)b * n * n;
+    if (d == 0) {
+        E[j + (long)j * n].x += 0.5f * (float)w.lam[3 * nb + (long)b * n + j];
+    } else if (p + d >= 0 && p + d < n) {
+        const float2 f = Fb[((long)b * n + j) * W + d + REF_BAND];
+        float2 &e = E[ord[p + d] + (long)j * n];
+        e.x += 0.5f * f.x;
+        e.y += 0.5f * f.y;
+    }
+}
+
+// 5a. ascending order of the refined eigenvalues
 __global__ void k_ref_rank(RefineWork w, const double *l2, double *eig)
 {
     const int b = blockIdx.y, n = w.n;
@@ -484,7 +549,7 @@ __global__ void k_ref_rank(RefineWork w, const double *l2, double *eig)
     eig[(long)b * n + r] = v;
 }
 
-// 4c. Z[:, rank(j)] = (X U)[:, j] + (X U E)[:, j]
+// 5b. Z[:, rank(j)] = X'[:, j] + (X' E)[:, j]
 __global__ void k_ref_finish(RefineWork w, double2 *Z)
 {
     const int n = w.n;
@@ -495,7 +560,7 @@ __global__ void k_ref_finish(RefineWork w, double2 *Z)
     const long e = t - b * nn;
     const int r = (int)(e % n), j = (int)(e / n);
     const int dst = w.cl[(long)3 * n * w.batch + (long)b * n + j];
-    const double2 x = w.YH[t];
+    const double2 x = w.Xd[t];
     const float2 d = w.XE[t];
     Z[b * nn + r + (long)dst * n] = make_double2(x.x + (double)d.x, x.y + (double)d.y);
 }
@@ -504,30 +569,39 @@ void refine_eigen(cudaStream_t s, RefineWork &w, const double2 *H, const double2
                   double *eig, double2 *Z, int *status)
 {
     const int n = w.n, B = w.batch;
-    const long nn = (long)n * n;
+    const long nn = (long)n * n, nb = (long)n * B;
     const float2 onef = make_float2(1.f, 0.f), zerof = make_float2(0.f, 0.f);
-    // 1. H X, S X (tensor cores, FP64-accurate), residuals, G = X^H r (FP32),
-    //    accurate diagonals
+    // 1. H X, S X (tensor cores, FP64-accurate), accurate diagonals
     const OzakiX ox = ozaki_prepare_x(s, X, n, B, w.oz);
     ozaki_gemm(s, ox, H, w.YH);
     ozaki_gemm(s, ox, S, w.YS);
-    NRLTB_LAUNCH(k_ref_resid, cdiv(nn * B, 256), 256, 0, s, w, eig);
-    // X^H formed explicitly (Xr is free until step 4): the tensor-core GEMM
-    // streams an A operand in its stored orientation twice as fast
-    conj_transpose<float>(s, X, w.Xr, n, B);
-    zgemm<float>(s, n, n, n, B, onef, w.Xr, n, nn, 0, w.Ef, n, nn, 0, zerof, w.G, n, nn);
-    NRLTB_LAUNCH(k_ref_diag, cdiv((long)n * B * 32, 256), 256, 0, s, w, X);
+    NRLTB_LAUNCH(k_ref_diag, cdiv(nb * 32, 256), 256, 0, s, w, X);
     // 2. clusters and their Rayleigh-Ritz rotations
     const size_t csm = n <= REF_KEYS_MAX ? sizeof(unsigned long long) * n : 0;
     if (csm > 48 * 1024) cudaFuncSetAttribute(k_ref_clusters, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)csm);
     NRLTB_LAUNCH(k_ref_clusters, B, 1024, csm, s, w, status);
     NRLTB_LAUNCH(k_ref_rr, dim3(n, B), REF_CMAX * REF_CMAX, 0, s, w, X);
-    // 3. correction matrix and second-order eigenvalues (YS is free: it holds them)
-    double *l2 = (double *)w.YS;
-    NRLTB_LAUNCH(k_ref_update, cdiv((long)n * B * 32, 256), 256, 0, s, w, l2);
-    // 4. Z = X U + (X U) E, reordered
-    NRLTB_LAUNCH(k_ref_rotate, cdiv(nn * B, 256), 256, 0, s, w, X);
+    // 3. rotated basis, its residuals, G' = X'^H r' (X'^H formed explicitly in
+    //    the YH area, free from here on: the tensor-core GEMM streams an A
+    //    operand in its stored orientation twice as fast)
+    NRLTB_LAUNCH(k_ref_rotres, cdiv(nn * B, 256), 256, 0, s, w, X);
+    float2 *T1 = (float2 *)w.YH, *T2 = (float2 *)w.YS;
+    conj_transpose<float>(s, w.Xr, T1, n, B);
+    zgemm<float>(s, n, n, n, B, onef, T1, n, nn, 0, w.Ef, n, nn, 0, zerof, w.G, n, nn);
+    // 4. E and the second-order Gram term F = E^H (E + E^H) + E E: its
+    //    diagonal over all i, its off-diagonal on the band of near neighbours
+    conj_transpose<float>(s, w.G, T2, n, B);
+    NRLTB_LAUNCH(k_ref_update, cdiv(nb * 32, 256), 256, 0, s, w, T2);
+    static const bool band_attr = [] {
+        cudaFuncSetAttribute(k_ref_band, cudaFuncAttributeMaxDynamicSharedMemorySize, REF_BAND_SMEM);
+        return true;
+    }();
+    (void)band_attr;
+    NRLTB_LAUNCH(k_ref_band, dim3(cdiv(n, REF_BT), B), 256, REF_BAND_SMEM, s, w, w.Fb);
+    NRLTB_LAUNCH(k_ref_band_apply, cdiv(nb * (2 * REF_BAND + 1), 256), 256, 0, s, w, w.Fb);
+    // 5. Z = X' + X' E, reordered
     zgemm<float>(s, n, n, n, B, onef, w.Xr, n, nn, 0, w.Ef, n, nn, 0, zerof, w.XE, n, nn);
+    const double *l2 = w.lam + 2 * nb;
     NRLTB_LAUNCH(k_ref_rank, dim3(cdiv(n, 128), B), 128, 0, s, w, l2, eig);
     if (Z) NRLTB_LAUNCH(k_ref_finish, cdiv(nn * B, 256), 256, 0, s, w, Z);
 }

@@ -8,11 +8,13 @@ namespace nrltb {
 struct RefineWork {
     int n, batch;
     double2 *YH, *YS;       // H X, S X
-    float2 *G;              // X^H r, r the residuals H x_j - l_j S x_j
+    double2 *Xd;            // rotated vectors X' = X U (FP64)
+    float2 *G;              // X'^H r', r'_j = H x'_j - l_j S x'_j
     double2 *U;             // cluster rotations
     float2 *Ef;             // FP32 update matrix
     float2 *Xr;             // rotated FP32 vectors
-    float2 *XE;             // X E (FP32)
+    float2 *XE;             // X' E (FP32)
+    float2 *Fb;             // second-order Gram terms near the sorted diagonal
     double *lam;            // refined eigenvalues
     int *cl;                // cluster id per eigenvalue
     void *oz;               // digit planes of the tensor-core products (ozaki.cuh)
