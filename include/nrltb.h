@@ -31,6 +31,8 @@ extern "C" {
 #define NRLTB_E_UNSUPPORTED -7   /* option outside the implemented scope            */
 #define NRLTB_E_EOF         -8   /* no more structures in the SKIN file             */
 #define NRLTB_E_NODEVICE    -9   /* no CUDA device / driver                          */
+#define NRLTB_E_TIMEOUT    -10   /* a bounded device wait gave up (k_status has      */
+                                 /* NRLTB_K_TIMEOUT at the k points it hit)         */
 
 /* ---- per-k status (k_status[k]) ---------------------------------------- */
 #define NRLTB_K_OK            0
@@ -215,6 +217,14 @@ int nrltb_diag(nrltb_ctx *ctx, int nv, int nk, const double *hmat, const double 
 /* fermi.f:1-434, non-spin (el = 2): Fermi level of eig[nk][nv] with weights w. */
 int nrltb_fermi(nrltb_ctx *ctx, int nv, int nk, const double *eig, const double *w,
                 double tkb, double zfill, double tol, double *efermi);
+/* fermi.f:1-434 and the sums of bande.f:1162-1330 on caller eigenvalues
+ * eig[nk][nv] (ascending per row), weights w[nk], and in modes 2 and 4 the
+ * eigenvalue derivatives deig[nk][nv] (all states below eigcut); el electrons
+ * per band (2 spin-restricted, 1 one spin channel).  out = {E_F, E(T), P(T),
+ * Fermi-level shift, S(T) (modes 1, 2), the two entropy-derivative sums
+ * (mode 2), Newton iterations}.  Every sum is compensated. */
+int nrltb_sums(nrltb_ctx *ctx, int nv, int nk, const double *eig, const double *deig, const double *w,
+               int mode, double el, double tkb, double zfill, double tol, double out[8]);
 
 /* ---- neighbour list without allocation ----------------------------------
  * No counterpart in the reference.  nrltb_search2 above sizes its buffers with
@@ -224,7 +234,8 @@ int nrltb_fermi(nrltb_ctx *ctx, int nv, int nk, const double *eig, const double 
  * stalled by the device-wide synchronisation a cudaMalloc/cudaFree can cause.
  * It performs no allocation: positions, kinds and the pair arrays are the
  * caller's device buffers (pair arrays of `capacity` entries, laid out as in
- * nrltb_pairs), and its scratch is a fixed device array of
+ * nrltb_pairs; every atom kind must lie in 1..kinds, others are refused with
+ * NRLTB_E_ARG before the search reads them), and its scratch is a fixed device array of
  * NRLTB_NOALLOC_SCRATCH_BYTES that every GPU which loads the library keeps
  * until the process exits.  Search boxes with more than
  * NRLTB_NOALLOC_MAX_CANDIDATES candidate images (natoms^2 (2nd1+1)(2nd2+1)

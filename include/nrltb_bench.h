@@ -13,7 +13,8 @@ extern "C" {
 /* Peak of one instruction pipe on this GPU: kind 0 = FP64 FMA, 1 = FP32 FMA
  * (2 flops per FMA), 2 = mma.sync bf16 m16n8k16, 3 = mma.sync tf32 m16n8k8
  * (FP32 accumulate; 2 m n k flops per MMA).  Independent chains on every SM;
- * returns TFLOP/s. */
+ * returns TFLOP/s.  kind 4 = L2 read bandwidth (every SM streaming a 48 MiB
+ * buffer that L2 holds, loads cached in L2 only); returns GB/s. */
 int nrltb_bench_peak(nrltb_ctx *ctx, int kind, double *tflops);
 
 /* One batched complex GEMM launch of the eigensolver's kernel (C = A B, n x n x n,
@@ -56,6 +57,13 @@ int nrltb_bench_cgemm_run(nrltb_ctx *ctx, int method, int m, int n, int k, int o
  * that kernel ran out (the kernel then leaves its output untouched).
  * clear = 1 resets both. */
 int nrltb_bench_umma_fault(int clear);
+
+/* Raise the context's own bounded-wait expiry word, as a tcgen05 kernel of
+ * that context does when one of its barrier waits runs out.  The next solve
+ * or Hellmann-Feynman step of the context then marks its k points
+ * NRLTB_K_TIMEOUT and the call returns NRLTB_E_TIMEOUT; the word is cleared
+ * when it is read.  For tests of that path (no device wait is made to expire). */
+int nrltb_bench_raise_fault_word(nrltb_ctx *ctx);
 
 /* Kernel-class timing of the context's own calls: with on = 1 every later
  * launch of a timed class (0 = FP32 tensor-core GEMM, 1 = SIMT GEMM, 2 = the

@@ -60,13 +60,59 @@ __global__ void k_mma_peak(float *out, int iters)
     if (s == -1.2345f) out[0] = s;
 }
 
+// L2 read bandwidth: every SM streams a buffer that L2 holds (no L1
+// allocation), many times over
+__global__ void k_l2_read(const float4 *buf, long n4, int reps, float *out)
+{
+    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+    const long stride = (long)gridDim.x * blockDim.x;
+    for (int r = 0; r < reps; ++r)
+        for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n4; i += stride) {
+            const float4 v = __ldcg(buf + i);
+            acc.x += v.x; acc.y += v.y; acc.z += v.z; acc.w += v.w;
+        }
+    if (acc.x + acc.y + acc.z + acc.w == -1.2345f) out[0] = acc.x;
+}
+
+static int l2_read_gbs(cudaStream_t s, int sms, double *gbs)
+{
+    const long bytes = 48l << 20, n4 = bytes / 16;
+    const int reps = 24;
+    float4 *buf = nullptr;
+    float *out = nullptr;
+    if (cudaMalloc(&buf, bytes) != cudaSuccess) return NRLTB_E_NOMEM;
+    if (cudaMalloc(&out, 64) != cudaSuccess) { cudaFree(buf); return NRLTB_E_NOMEM; }
+    cudaMemsetAsync(buf, 0, bytes, s);
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float best = 1e30f;
+    for (int rep = 0; rep < 4; ++rep) {
+        cudaEventRecord(e0, s);
+        k_l2_read<<<sms * 4, 512, 0, s>>>(buf, n4, reps, out);
+        cudaEventRecord(e1, s);
+        cudaEventSynchronize(e1);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (rep > 0 && ms < best) best = ms;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(buf);
+    cudaFree(out);
+    if (cudaGetLastError() != cudaSuccess) return NRLTB_E_CUDA;
+    *gbs = (double)bytes * reps / (best * 1e-3) / 1e9;
+    return NRLTB_OK;
+}
+
 extern "C" int nrltb_bench_peak(nrltb_ctx *ctx, int kind, double *tflops)
 {
-    if (!ctx || !tflops || kind < 0 || kind > 3) return NRLTB_E_ARG;
+    if (!ctx || !tflops || kind < 0 || kind > 4) return NRLTB_E_ARG;
     cudaStream_t s = nrltb_ctx_stream_internal(ctx);
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (kind == 4) return l2_read_gbs(s, sms, tflops);
     void *buf = nullptr;
     if (cudaMalloc(&buf, 64) != cudaSuccess) return NRLTB_E_NOMEM;
     const int threads = (kind >= 2) ? 256 : 512, blocks = sms * 4;

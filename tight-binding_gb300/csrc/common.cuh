@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <stdio.h>
+#include <vector>
 
 namespace nrltb {
 
@@ -83,6 +84,12 @@ __host__ __device__ inline int cdiv(long a, long b) { return (int)((a + b - 1) /
 // that the context can report how many device kernels a call issued.
 extern thread_local long long *g_launch_counter;
 
+// Bounded-wait expiry: the tcgen05 kernels OR 1 into this device word when a
+// barrier wait runs out (null: a per-library global flag, read by the test
+// hooks).  A context points it at its own word for the duration of a call, so
+// concurrent contexts never see each other's faults.
+extern thread_local unsigned *g_fault_word;
+
 // Kernel-class timing (off unless a context enables it): CUDA events on the
 // launching stream around each launch of a timed class, with the launch's
 // algorithmic work (flops or bytes), summed by nrltb_bench_kernel_stats.
@@ -90,16 +97,15 @@ enum KClass { KC_GEMM_TC = 0, KC_GEMM_SIMT = 1, KC_DIGIT_GEMM = 2, KC_TRI_PANEL 
 struct KTimer {
     bool on = false;
     struct Rec { int cls; cudaEvent_t a, b; double work; };
-    Rec recs[4096];
-    int nrec = 0;
-    cudaEvent_t pool[8192];
-    int npool = 0, used = 0;
+    std::vector<Rec> recs;          // every timed launch since timing was turned on
+    std::vector<cudaEvent_t> pool;  // events, reused from one timing period to the next
+    size_t used = 0;
     cudaEvent_t next()
     {
-        if (used == npool) {
-            if (npool == 8192) return nullptr;
-            if (cudaEventCreate(&pool[npool]) != cudaSuccess) return nullptr;
-            ++npool;
+        if (used == pool.size()) {
+            cudaEvent_t e;
+            if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+            pool.push_back(e);
         }
         return pool[used++];
     }
@@ -109,7 +115,7 @@ extern thread_local KTimer *g_ktimer;
 inline cudaEvent_t kt_begin(cudaStream_t s)
 {
     KTimer *k = g_ktimer;
-    if (!k || !k->on || k->nrec == 4096) return nullptr;
+    if (!k || !k->on) return nullptr;
     cudaEvent_t e = k->next();
     if (e) cudaEventRecord(e, s);
     return e;
@@ -121,7 +127,7 @@ inline void kt_end(cudaEvent_t a, cudaStream_t s, int cls, double work)
     cudaEvent_t b = k->next();
     if (!b) return;
     cudaEventRecord(b, s);
-    k->recs[k->nrec++] = {cls, a, b, work};
+    k->recs.push_back({cls, a, b, work});
 }
 #define NRLTB_LAUNCH(kernel, grid, block, smem, stream, ...)                 \
     do {                                                                     \

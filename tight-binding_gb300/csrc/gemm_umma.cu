@@ -141,7 +141,7 @@ __device__ __forceinline__ void um_put4(unsigned char *ph, unsigned char *pl, ui
 }
 
 template <int TB>   // 1: op(B) = B^H
-__global__ void __launch_bounds__(UM_THREADS, 2) zgemm_umma_kernel(GemmArgs<float> g, int va, int vb)
+__global__ void __launch_bounds__(UM_THREADS, 2) zgemm_umma_kernel(GemmArgs<float> g, int va, int vb, unsigned *fault)
 {
     extern __shared__ __align__(16) unsigned char um_raw[];
     const int b = blockIdx.z;
@@ -319,7 +319,7 @@ __global__ void __launch_bounds__(UM_THREADS, 2) zgemm_umma_kernel(GemmArgs<floa
         if (__syncthreads_or(!ok)) fail = true;
     }
     if (fail) {
-        if (tid == 0) atomicOr(&g_umma_fault, 1u);
+        if (tid == 0) atomicOr(fault ? fault : &g_umma_fault, 1u);
         // give MMAs still in flight a second bounded wait before the memory is released
         if (tid == 0 && nk > 0) um_wait(bar0, (nk - 1) & 1);
     } else {
@@ -389,8 +389,8 @@ void zgemm_umma_launch(cudaStream_t s, const GemmArgs<float> &g)
     // 16-byte aligned: an aligned base, even leading dimension and batch stride
     const int va = ((uintptr_t)g.A % 16 == 0) && g.lda % 2 == 0 && g.sA % 2 == 0;
     const int vb = ((uintptr_t)g.B % 16 == 0) && g.ldb % 2 == 0 && g.sB % 2 == 0;
-    if (g.opB) NRLTB_LAUNCH(zgemm_umma_kernel<1>, grid, UM_THREADS, UM_SMEM, s, g, va, vb);
-    else NRLTB_LAUNCH(zgemm_umma_kernel<0>, grid, UM_THREADS, UM_SMEM, s, g, va, vb);
+    if (g.opB) NRLTB_LAUNCH(zgemm_umma_kernel<1>, grid, UM_THREADS, UM_SMEM, s, g, va, vb, g_fault_word);
+    else NRLTB_LAUNCH(zgemm_umma_kernel<0>, grid, UM_THREADS, UM_SMEM, s, g, va, vb, g_fault_word);
 }
 
 unsigned zgemm_umma_fault(bool clear)

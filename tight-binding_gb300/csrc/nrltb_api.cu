@@ -29,6 +29,7 @@
 namespace nrltb {
 thread_local long long *g_launch_counter = nullptr;
 thread_local KTimer *g_ktimer = nullptr;
+thread_local unsigned *g_fault_word = nullptr;
 }
 using namespace nrltb;
 
@@ -121,9 +122,53 @@ struct nrltb_ctx {
     std::vector<std::pair<int, int>> nonpd;   // (k, chunk) of k points whose S is not positive definite
     // results
     DBuf d_eig, d_deig, d_ncut, d_status, d_fjob, d_fout, d_orbq, d_spev, d_spdir;
+    DBuf d_fault;   // bounded-wait expiry word of this context's tcgen05 kernels
     FermiOut fout;
     int ran = 0;
 };
+
+// For the duration of one library call: count its launches and time its
+// kernel classes in the context, and point the tcgen05 kernels' expiry flag at
+// the context's own word (cleared when it is first allocated, and by
+// k_fault_mark every time it is read).
+struct CallScope {
+    long long *prev_count;
+    KTimer *prev_kt;
+    unsigned *prev_fault;
+    explicit CallScope(nrltb_ctx *c)
+        : prev_count(g_launch_counter), prev_kt(g_ktimer), prev_fault(g_fault_word)
+    {
+        g_launch_counter = &c->launches;
+        g_ktimer = c->kt;
+        if (!c->d_fault.p && c->d_fault.ensure(256) == NRLTB_OK) cudaMemset(c->d_fault.p, 0, 256);
+        g_fault_word = c->d_fault.as<unsigned>();
+    }
+    ~CallScope()
+    {
+        g_launch_counter = prev_count;
+        g_ktimer = prev_kt;
+        g_fault_word = prev_fault;
+    }
+};
+
+// A bounded device wait of a tcgen05 kernel ran out: every k of the chunk
+// that launched it gets NRLTB_K_TIMEOUT, and the word is cleared for the next
+// chunk (one CTA, stream-ordered after the kernels it checks).
+__global__ void k_fault_mark(unsigned *fault, int *status, int nk)
+{
+    __shared__ unsigned f;
+    if (threadIdx.x == 0) f = *fault;
+    __syncthreads();
+    if (f) {
+        for (int k = threadIdx.x; k < nk; k += blockDim.x) status[k] = NRLTB_K_TIMEOUT;
+        __syncthreads();
+        if (threadIdx.x == 0) *fault = 0;
+    }
+}
+static void fault_mark(cudaStream_t s, int *status, int nk)
+{
+    if (g_fault_word) NRLTB_LAUNCH(k_fault_mark, 1, 128, 0, s, g_fault_word, status, nk);
+}
 
 static DevPairs pairs_view(nrltb_ctx *c, int cap)
 {
@@ -552,6 +597,7 @@ static int run_solve(nrltb_ctx *c, int nv, int nkc, int prec, const double2 *H, 
         refine_work_carve(rw, c->d_ref.p, nv, nkc);
         refine_eigen(s, rw, H, S, c->d_X.as<float2>(), eig, Zout, status);
         CKL();
+        fault_mark(s, status, nkc);
     }
     return NRLTB_OK;
 }
@@ -672,10 +718,7 @@ static int run_all(nrltb_ctx *c)
     const int lspdir = S.noncol && (o.flags & NRLTB_OPT_SPIN_DIRECTIONS);   // spin directions, diag.f:458
     const bool vectors = lpress || lqlmt || lspdir;
     cudaStream_t s = c->stream;
-    long long *prev = g_launch_counter;
-    KTimer *prev_kt = g_ktimer;
-    g_launch_counter = &c->launches;
-    g_ktimer = c->kt;
+    CallScope scope(c);
     int rc = NRLTB_OK;
     c->nonpd.clear();
     do {
@@ -735,6 +778,11 @@ static int run_all(nrltb_ctx *c)
                 if (cudaMemcpyAsync(hst.data(), status, sizeof(int) * nkc, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
                     cudaStreamSynchronize(s) != cudaSuccess) { set_err("status readback failed"); rc = NRLTB_E_CUDA; break; }
                 for (int k = 0; k < nkc; ++k) if (hst[k] == NRLTB_K_S_NOT_PD) bad.push_back(k);
+                if (std::count(hst.begin(), hst.end(), NRLTB_K_TIMEOUT)) {
+                    set_err("a bounded device wait gave up in the eigensolve of k points %d-%d", r0, r0 + nkc - 1);
+                    rc = NRLTB_E_TIMEOUT;
+                    break;
+                }
                 if (!bad.empty()) {
                     if ((rc = fix_nonpd(c, nv, bad, c->d_S.as<double2>(), eig))) break;
                     for (int k : bad) c->nonpd.push_back(std::make_pair(r0 + k, 0));
@@ -761,6 +809,7 @@ static int run_all(nrltb_ctx *c)
                                      c->d_deig.as<double>() + (size_t)r0 * nv, c->d_hf.p, nullptr)))
                         { set_err("hf failed"); break; }
                     CKL();
+                    fault_mark(s, status, nkc);
                 }
             }
         }
@@ -798,8 +847,6 @@ static int run_all(nrltb_ctx *c)
                          c->d_spdir.as<double>());
         c->ran = 1;
     } while (0);
-    g_launch_counter = prev;
-    g_ktimer = prev_kt;
     return rc;
 }
 
@@ -858,10 +905,17 @@ static int fetch(nrltb_ctx *c, nrltb_result *res)
     res->nv = nv;
     res->nk = nk;
     res->kneigh_out = c->kneigh_out;
-    int bad = 0;
-    for (int k = 0; k < nrow; ++k) bad += (status[k] == NRLTB_K_S_NOT_PD);
+    int bad = 0, timeout = 0;
+    for (int k = 0; k < nrow; ++k) {
+        bad += (status[k] == NRLTB_K_S_NOT_PD);
+        timeout += (status[k] == NRLTB_K_TIMEOUT);
+    }
     res->nonphysical_k = bad;
     if (res->k_status) memcpy(res->k_status, status.data(), sizeof(int) * nrow);
+    if (timeout) {
+        set_err("a bounded device wait gave up at %d k point(s); their results are not valid", timeout);
+        return NRLTB_E_TIMEOUT;
+    }
     return NRLTB_OK;
 }
 
@@ -901,10 +955,10 @@ int nrltb_ctx_destroy(nrltb_ctx *c)
                     &c->d_kq, &c->d_kw, &c->d_ksk, &c->d_orb, &c->d_flip, &c->d_spinat, &c->d_nc, &c->d_Hn, &c->d_Sn, &c->d_code, &c->d_blk, &c->d_misc, &c->d_pairs,
                     &c->d_sk, &c->d_seg, &c->d_ph, &c->d_H, &c->d_S, &c->d_X, &c->d_work, &c->d_ref, &c->d_hf, &c->d_np,
                     &c->d_qw, &c->d_eig, &c->d_deig, &c->d_ncut, &c->d_status, &c->d_fjob, &c->d_fout,
-                    &c->d_orbq, &c->d_spev, &c->d_spdir};
+                    &c->d_orbq, &c->d_spev, &c->d_spdir, &c->d_fault};
     for (DBuf *b : bufs) b->release();
     if (c->kt) {
-        for (int i = 0; i < c->kt->npool; ++i) cudaEventDestroy(c->kt->pool[i]);
+        for (cudaEvent_t e : c->kt->pool) cudaEventDestroy(e);
         delete c->kt;
     }
     for (nrltb_ctx *w : c->workers) nrltb_ctx_destroy(w);
@@ -922,7 +976,7 @@ extern "C" int nrltb_bench_kernel_timing(nrltb_ctx *c, int on)
         if (!c->kt) return NRLTB_E_NOMEM;
         cudaSetDevice(c->device);
         cudaStreamSynchronize(c->stream);
-        c->kt->nrec = 0;
+        c->kt->recs.clear();
         c->kt->used = 0;
         c->kt->on = true;
     } else if (c->kt) {
@@ -940,7 +994,7 @@ extern "C" int nrltb_bench_kernel_stats(nrltb_ctx *c, int cls, double *ms, doubl
     if (!c->kt) return NRLTB_OK;
     cudaSetDevice(c->device);
     if (cudaStreamSynchronize(c->stream) != cudaSuccess) return NRLTB_E_CUDA;
-    for (int i = 0; i < c->kt->nrec; ++i) {
+    for (size_t i = 0; i < c->kt->recs.size(); ++i) {
         const KTimer::Rec &r = c->kt->recs[i];
         if (r.cls != cls) continue;
         float t = 0;
@@ -1061,13 +1115,11 @@ int nrltb_search2(nrltb_ctx *c, const nrltb_structure *st, const nrltb_params *p
     if (!c || !out) return NRLTB_E_ARG;
     CK(cudaSetDevice(c->device));
     RET(stage_host(c, st, par, nullptr, nullptr));
-    long long *prev = g_launch_counter;
-    KTimer *prev_kt = g_ktimer;
-    g_launch_counter = &c->launches;
-    g_ktimer = c->kt;
-    int rc = run_search2(c, kneigh_in);
-    g_launch_counter = prev;
-    g_ktimer = prev_kt;
+    int rc;
+    {
+        CallScope scope(c);
+        rc = run_search2(c, kneigh_in);
+    }
     RET(rc);
     out->npairs = c->npairs;
     if (kneigh_out) *kneigh_out = c->kneigh_out;
@@ -1106,13 +1158,11 @@ int nrltb_setpar(nrltb_ctx *c, const nrltb_structure *st, const nrltb_params *pa
     CK(cudaMemcpyAsync(pr.jkind, pairs->jkind, sizeof(int) * 2 * P, cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(pr.jatm, pairs->jatm, sizeof(int) * 2 * P, cudaMemcpyHostToDevice, s));
     const int deriv = (dhop && dover && dparos) ? 1 : 0;
-    long long *prev = g_launch_counter;
-    KTimer *prev_kt = g_ktimer;
-    g_launch_counter = &c->launches;
-    g_ktimer = c->kt;
-    int rc = run_setpar(c, deriv);
-    g_launch_counter = prev;
-    g_ktimer = prev_kt;
+    int rc;
+    {
+        CallScope scope(c);
+        rc = run_setpar(c, deriv);
+    }
     RET(rc);
     DevSK sk = sk_view(c, std::max(P, 1), st->natoms, par->kinds);
     CK(cudaMemcpyAsync(hop, sk.hop, sizeof(double) * 14 * P, cudaMemcpyDeviceToHost, s));
@@ -1137,20 +1187,18 @@ int nrltb_setham(nrltb_ctx *c, const nrltb_structure *st, const nrltb_params *pa
     memset(&o, 0, sizeof o);
     o.mode = which ? 4 : 3;
     RET(stage_host(c, st, par, km, &o));
-    long long *prev = g_launch_counter;
-    KTimer *prev_kt = g_ktimer;
-    g_launch_counter = &c->launches;
-    g_ktimer = c->kt;
-    int rc = run_search2(c, 0);
-    if (!rc) rc = run_setpar(c, which);
-    if (!rc) rc = run_skblocks(c, which ? 4 : 2);
     const int nv = c->st.nv, nk = c->st.nk;
     const size_t nn = (size_t)nv * nv;
-    if (!rc) rc = c->d_H.ensure(sizeof(double2) * nn * nk);
-    if (!rc) rc = c->d_S.ensure(sizeof(double2) * nn * nk);
-    if (!rc) rc = run_bloch(c, 0, nk, which ? 2 : 0, c->d_H.as<double2>(), c->d_S.as<double2>());
-    g_launch_counter = prev;
-    g_ktimer = prev_kt;
+    int rc;
+    {
+        CallScope scope(c);
+        rc = run_search2(c, 0);
+        if (!rc) rc = run_setpar(c, which);
+        if (!rc) rc = run_skblocks(c, which ? 4 : 2);
+        if (!rc) rc = c->d_H.ensure(sizeof(double2) * nn * nk);
+        if (!rc) rc = c->d_S.ensure(sizeof(double2) * nn * nk);
+        if (!rc) rc = run_bloch(c, 0, nk, which ? 2 : 0, c->d_H.as<double2>(), c->d_S.as<double2>());
+    }
     RET(rc);
     cudaStream_t s = c->stream;
     CK(cudaMemcpyAsync(hmat, c->d_H.p, sizeof(double2) * nn * nk, cudaMemcpyDeviceToHost, s));
@@ -1175,19 +1223,23 @@ int nrltb_diag(nrltb_ctx *c, int nv, int nk, const double *hmat, const double *s
     CK(cudaMemcpyAsync(c->d_H.p, hmat, sizeof(double2) * nn * nk, cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(c->d_S.p, smat, sizeof(double2) * nn * nk, cudaMemcpyHostToDevice, s));
     double2 *Z = (double2 *)(c->d_X.as<char>() + zoff(nn, nk));
-    long long *prev = g_launch_counter;
-    KTimer *prev_kt = g_ktimer;
-    g_launch_counter = &c->launches;
-    g_ktimer = c->kt;
-    int rc = run_solve(c, nv, nk, precision, c->d_H.as<double2>(), c->d_S.as<double2>(), c->d_eig.as<double>(),
+    int rc;
+    {
+        CallScope scope(c);
+        rc = run_solve(c, nv, nk, precision, c->d_H.as<double2>(), c->d_S.as<double2>(), c->d_eig.as<double>(),
                        Z, c->d_status.as<int>(), z != nullptr);
-    g_launch_counter = prev;
-    g_ktimer = prev_kt;
+    }
     RET(rc);
+    std::vector<int> status(nk);
     CK(cudaMemcpyAsync(eig, c->d_eig.p, sizeof(double) * (size_t)nv * nk, cudaMemcpyDeviceToHost, s));
     if (z) CK(cudaMemcpyAsync(z, Z, sizeof(double2) * nn * nk, cudaMemcpyDeviceToHost, s));
-    if (k_status) CK(cudaMemcpyAsync(k_status, c->d_status.p, sizeof(int) * nk, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(status.data(), c->d_status.p, sizeof(int) * nk, cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
+    if (k_status) memcpy(k_status, status.data(), sizeof(int) * nk);
+    if (std::count(status.begin(), status.end(), NRLTB_K_TIMEOUT)) {
+        set_err("a bounded device wait gave up in the eigensolve; the results are not valid");
+        return NRLTB_E_TIMEOUT;
+    }
     return NRLTB_OK;
 }
 
@@ -1213,18 +1265,85 @@ int nrltb_fermi(nrltb_ctx *c, int nv, int nk, const double *eig, const double *w
     job.tkb = tkb; job.zfill = zfill; job.tol = tol > 0 ? tol : 1e-8;
     job.out = c->d_fout.as<FermiOut>();
     CK(cudaMemcpyAsync(c->d_fjob.p, &job, sizeof job, cudaMemcpyHostToDevice, s));
-    long long *prev = g_launch_counter;
-    KTimer *prev_kt = g_ktimer;
-    g_launch_counter = &c->launches;
-    g_ktimer = c->kt;
-    NRLTB_LAUNCH(k_fermi_sums, 1, 1024, 0, s, c->d_fjob.as<FermiJob>());
-    g_launch_counter = prev;
-    g_ktimer = prev_kt;
+    {
+        CallScope scope(c);
+        NRLTB_LAUNCH(k_fermi_sums, 1, 1024, 0, s, c->d_fjob.as<FermiJob>());
+    }
     CKL();
     FermiOut o;
     CK(cudaMemcpyAsync(&o, c->d_fout.p, sizeof o, cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
     *efermi = o.efermi;
+    return NRLTB_OK;
+}
+
+int nrltb_sums(nrltb_ctx *c, int nv, int nk, const double *eig, const double *deig, const double *w, int mode,
+               double el, double tkb, double zfill, double tol, double out[8])
+{
+    if (!c || nv < 1 || nk < 1 || !eig || !w || !out) return NRLTB_E_ARG;
+    if (mode < 1 || mode > 4 || !(el == 1.0 || el == 2.0)) { set_err("sums: mode 1-4, el 1 or 2"); return NRLTB_E_ARG; }
+    const int lpress = (mode == 2 || mode == 4), lentro = (mode < 3);
+    if (lpress && !deig) { set_err("sums: modes 2 and 4 need deig"); return NRLTB_E_ARG; }
+    if (!(zfill > 0)) { set_err("zfill <= 0: no Fermi level (fermi.f:165)"); return NRLTB_E_ARG; }
+    CK(cudaSetDevice(c->device));
+    cudaStream_t s = c->stream;
+    const size_t ne = (size_t)nv * nk;
+    RET(c->d_eig.ensure(sizeof(double) * ne));
+    RET(c->d_deig.ensure(sizeof(double) * ne));
+    RET(c->d_ncut.ensure(sizeof(int) * (size_t)nk));
+    RET(c->d_kw.ensure(sizeof(double) * nk));
+    RET(c->d_fout.ensure(sizeof(FermiOut)));
+    RET(c->d_fjob.ensure(sizeof(FermiJob)));
+    CK(cudaMemcpyAsync(c->d_eig.p, eig, sizeof(double) * ne, cudaMemcpyHostToDevice, s));
+    if (lpress) CK(cudaMemcpyAsync(c->d_deig.p, deig, sizeof(double) * ne, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(c->d_kw.p, w, sizeof(double) * nk, cudaMemcpyHostToDevice, s));
+    std::vector<int> ncut(nk, nv);
+    CK(cudaMemcpyAsync(c->d_ncut.p, ncut.data(), sizeof(int) * nk, cudaMemcpyHostToDevice, s));
+    FermiJob job;
+    memset(&job, 0, sizeof job);
+    job.eig = c->d_eig.as<double>();
+    job.deig = c->d_deig.as<double>();
+    job.w = c->d_kw.as<double>();
+    job.ncut = c->d_ncut.as<int>();
+    job.nv = nv; job.nk = nk; job.ldk = nv; job.lpress = lpress;
+    job.lentro = lentro; job.nks = 0; job.el = el;
+    job.tkb = tkb; job.zfill = zfill; job.tol = tol > 0 ? tol : 1e-8;
+    job.out = c->d_fout.as<FermiOut>();
+    CK(cudaMemcpyAsync(c->d_fjob.p, &job, sizeof job, cudaMemcpyHostToDevice, s));
+    {
+        CallScope scope(c);
+        NRLTB_LAUNCH(k_fermi_sums, 1, 1024, 0, s, c->d_fjob.as<FermiJob>());
+    }
+    CKL();
+    FermiOut o;
+    CK(cudaMemcpyAsync(&o, c->d_fout.p, sizeof o, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    out[0] = o.efermi;
+    out[1] = o.e_total;
+    out[2] = o.pressure;
+    out[3] = o.fermi_shift;
+    out[4] = o.entropy;
+    out[5] = o.dent1;
+    out[6] = o.dent2;
+    out[7] = (double)o.iterations;
+    return NRLTB_OK;
+}
+
+// Measurement and test hook: raise the context's bounded-wait expiry word as
+// a tcgen05 kernel whose wait ran out would, so that a test can check the path
+// from the device flag to the per-k status and the returned error without
+// making any device wait run out.
+int nrltb_bench_raise_fault_word(nrltb_ctx *c)
+{
+    if (!c) return NRLTB_E_ARG;
+    CK(cudaSetDevice(c->device));
+    if (!c->d_fault.p) {
+        RET(c->d_fault.ensure(256));
+        CK(cudaMemset(c->d_fault.p, 0, 256));
+    }
+    const unsigned one = 1;
+    CK(cudaMemcpyAsync(c->d_fault.p, &one, sizeof one, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
     return NRLTB_OK;
 }
 

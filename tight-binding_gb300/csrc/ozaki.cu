@@ -320,7 +320,7 @@ __device__ __forceinline__ void df_add(float &hi, float &lo, float v)
 template <int SA>
 __global__ void __maxnreg__(96)
 k_oz_gemm(const unsigned char *DA, const unsigned char *DX, const int *exA, const int *exX, double2 *Y, int n,
-          int np, int batch)
+          int np, int batch, unsigned *fault)
 {
     extern __shared__ __align__(16) unsigned char oz_raw[];
     const int jt = blockIdx.x, it = blockIdx.y, b = blockIdx.z;
@@ -384,7 +384,7 @@ k_oz_gemm(const unsigned char *DA, const unsigned char *DX, const int *exA, cons
                     oz_bulk(oz_saddr(sA + ia * OZ_ABLK), gA + (long)qa * OZ_ABLK, OZ_ABLK, full_a(ia));
                 }
             }
-            if (!ok) { *abort = 1; atomicOr(&g_oz_fault, 1u); }
+            if (!ok) { *abort = 1; atomicOr(fault ? fault : &g_oz_fault, 1u); }
         }
     } else if (warp == OZ_FOLD_WARPS + 1) {
         // ---- MMA issue: plane s takes the digit pairs (s, 0), (s, 1), (s, 2) ----
@@ -433,7 +433,7 @@ k_oz_gemm(const unsigned char *DA, const unsigned char *DX, const int *exA, cons
                 const int jx = (KC - 1) % OZ_NXS, ux = (KC - 1) / OZ_NXS;
                 ok = oz_wait(empty_x(jx), ux & 1, abort);
             }
-            if (!ok) { *abort = 1; atomicOr(&g_oz_fault, 1u); }
+            if (!ok) { *abort = 1; atomicOr(fault ? fault : &g_oz_fault, 1u); }
         }
     } else {
         // ---- fold warps: level sums -> double-float accumulators -> Y ----
@@ -484,7 +484,7 @@ k_oz_gemm(const unsigned char *DA, const unsigned char *DX, const int *exA, cons
                 }
             }
         }
-        if (!ok && lane == 0) { *abort = 1; atomicOr(&g_oz_fault, 1u); }
+        if (!ok && lane == 0) { *abort = 1; atomicOr(fault ? fault : &g_oz_fault, 1u); }
         if (ok) {
             // Y[i, j], i = this thread's A row, j = 16 consecutive X columns:
             // scale by 2^(e_i + 1) 2^(f_j + 1)
@@ -544,7 +544,7 @@ template <int SA> static void ozaki_gemm_sa(cudaStream_t s, const OzakiX &ox, co
     dim3 grid(np / OZ_NX, np / OZ_MA, batch);
     cudaEvent_t ev = kt_begin(s);
     NRLTB_LAUNCH(k_oz_gemm<SA>, grid, OZ_THREADS, OZ_SMEM, s, (const unsigned char *)ox.DA,
-                 (const unsigned char *)ox.DX, ox.exA, ox.exX, Y, n, np, batch);
+                 (const unsigned char *)ox.DX, ox.exA, ox.exX, Y, n, np, batch, g_fault_word);
     kt_end(ev, s, KC_DIGIT_GEMM, 8.0 * n * (double)n * n * batch);
 }
 

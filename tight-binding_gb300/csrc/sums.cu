@@ -9,9 +9,62 @@
 // Occupations are exactly 1 below mu - 20 kT and 0 above mu + 20 kT.  With
 // lentro (modes 1, 2) the same window also gives Gillan's entropy S(T) and its
 // two volume-derivative sums (bande.f:1189-1242).
+//
+// Every sum (the occupation and its derivative in each Newton step, E(T), the
+// pressure partials, the entropy terms, the spin populations) is compensated:
+// each thread keeps a (sum, error) pair updated by Knuth's two-sum, and the
+// block reduction merges the pairs in a fixed tree order, so the result is
+// what an exact summation of the rounded terms would give to within a few
+// units in the last place of the result, however much the terms cancel, and
+// the same from run to run.
 #include "sums.cuh"
 
 namespace nrltb {
+
+// compensated accumulator: the exact sum of the terms added is hi + lo up to
+// the rounding of lo (Knuth's two-sum, no ordering assumption)
+struct DD {
+    double hi = 0.0, lo = 0.0;
+    __device__ __forceinline__ void add(double b)
+    {
+        // _rn intrinsics: a term's product is never contracted into the sum
+        const double s = __dadd_rn(hi, b), bp = __dsub_rn(s, hi);
+        lo += __dadd_rn(__dsub_rn(hi, __dsub_rn(s, bp)), __dsub_rn(b, bp));
+        hi = s;
+    }
+    __device__ __forceinline__ void merge(double bhi, double blo)
+    {
+        lo += blo;
+        add(bhi);
+    }
+};
+
+// block-wide compensated sum; every thread gets hi + lo of the total.  `sh`
+// needs 2 * blockDim.x / 32 entries.
+__device__ double block_sum_dd(DD v, double *sh)
+{
+    for (int o = 16; o > 0; o >>= 1) {
+        const double h = __shfl_xor_sync(0xffffffffu, v.hi, o), l = __shfl_xor_sync(0xffffffffu, v.lo, o);
+        v.merge(h, l);
+    }
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    __syncthreads();
+    if (lane == 0) { sh[wid] = v.hi; sh[32 + wid] = v.lo; }
+    __syncthreads();
+    if (wid == 0) {
+        DD t;
+        if (lane < nw) { t.hi = sh[lane]; t.lo = sh[32 + lane]; }
+        for (int o = 16; o > 0; o >>= 1) {
+            const double h = __shfl_xor_sync(0xffffffffu, t.hi, o), l = __shfl_xor_sync(0xffffffffu, t.lo, o);
+            t.merge(h, l);
+        }
+        if (lane == 0) sh[0] = t.hi + t.lo;
+    }
+    __syncthreads();
+    const double r = sh[0];
+    __syncthreads();
+    return r;
+}
 
 __device__ inline double block_sum_d(double v, double *sh) { return block_sum<double>(v, sh); }
 __device__ inline double block_max_d(double v, double *sh)
@@ -32,7 +85,7 @@ __device__ inline double block_max_d(double v, double *sh)
 
 __global__ void __launch_bounds__(1024) k_fermi_sums(FermiJob *jobs)
 {
-    __shared__ double sh[32];
+    __shared__ double sh[64];
     FermiJob J = jobs[blockIdx.x];
     const int nv = J.nv, nk = J.nk, tid = threadIdx.x, nt = blockDim.x;
     const long tot = (long)nv * nk;
@@ -65,21 +118,21 @@ __global__ void __launch_bounds__(1024) k_fermi_sums(FermiJob *jobs)
         mu = 0.5 * (stlow + sthigh);
         for (it = 1; it <= 10000; ++it) {
             const double mum20 = mu - tkb * 20.0, mup20 = mu + tkb * 20.0, btmu = -beta * mu;
-            double ns = 0, dns = 0;
+            DD ns, dns;
             for (long q = tid; q < tot; q += nt) {
                 const int k = (int)(q / nv), i = (int)(q % nv);
                 const double e = J.eig[(long)k * J.ldk + i];
                 const double wk = J.w[k];
-                if (e < mum20) ns += wk;
+                if (e < mum20) ns.add(wk);
                 else if (e < mup20) {
                     const double ex = exp(beta * e + btmu);
                     const double f = 1.0 / (1.0 + ex);
-                    ns += wk * f;
-                    dns += wk * (ex * f * f);
+                    ns.add(wk * f);
+                    dns.add(wk * (ex * f * f));
                 }
             }
-            double nsum = el * block_sum_d(ns, sh);
-            double dnsum = beta * el * block_sum_d(dns, sh);
+            double nsum = el * block_sum_dd(ns, sh);
+            double dnsum = beta * el * block_sum_dd(dns, sh);
             if (fabs(nsum - zfill) < tol) break;
             if (nsum < zfill) mulow = mu; else muhigh = mu;
             double mu1;
@@ -96,15 +149,15 @@ __global__ void __launch_bounds__(1024) k_fermi_sums(FermiJob *jobs)
     // energy and pressure sums (bande.f:1162-1330)
     const double tkbi = (tkb < 1e-5) ? 1e5 : 1.0 / tkb;
     const double efp = mu + 20.0 * tkb, efm = mu - 20.0 * tkb;
-    double es = 0, d1 = 0, d2 = 0, d3 = 0, dfb = 0, dfe = 0, ent = 0, dn1 = 0, dn2 = 0, sup = 0, sdn = 0;
+    DD es, d1, d2, d3, dfb, dfe, ent, dn1, dn2, sup, sdn;
     for (long q = tid; q < tot; q += nt) {
         const int k = (int)(q / nv), i = (int)(q % nv);
         const double e = J.eig[(long)k * J.ldk + i];
         // spin populations over all nv states (bande.f:1336-1395), weight w(k)
         if (J.nks > 0 && e < efp) {
             const double occ = (e < efm) ? J.w[k] : J.w[k] * (1.0 / (1.0 + exp(tkbi * (e - mu))));
-            if (k < J.nks) sup += occ;
-            else sdn += occ;
+            if (k < J.nks) sup.add(occ);
+            else sdn.add(occ);
         }
         const int lim = J.lpress ? J.ncut[k] : nv;
         if (i >= lim) continue;
@@ -112,61 +165,58 @@ __global__ void __launch_bounds__(1024) k_fermi_sums(FermiJob *jobs)
         const double wt = J.el * J.w[k], ewt = wt * e;
         const double de = J.lpress ? J.deig[(long)k * J.ldk + i] : 0.0;
         if (e < efm) {
-            es += ewt;
-            d1 += wt * de;
+            es.add(ewt);
+            d1.add(wt * de);
         } else {
             const double x = e - mu;
             const double fbe = 1.0 / (1.0 + exp(tkbi * x));
-            es += ewt * fbe;
+            es.add(ewt * fbe);
             // Gillan entropy of the window states (bande.f:1233-1242, 1313)
-            if (J.lentro) ent -= wt * (fbe * log(fbe) + (1.0 - fbe) * log(1.0 - fbe));
+            if (J.lentro) ent.add(-(wt * (fbe * log(fbe) + (1.0 - fbe) * log(1.0 - fbe))));
             if (J.lpress) {
                 const double dfbe = -tkbi * fbe * (1.0 / (1.0 + exp(tkbi * (-x))));
-                dfb += dfbe * wt;
-                d3 += dfbe * ewt;
+                dfb.add(dfbe * wt);
+                d3.add(dfbe * ewt);
                 const double dewt = wt * de;
-                d1 += dewt * fbe;
-                dfe += dfbe * dewt;
-                d2 += dfbe * ewt * de;
+                d1.add(dewt * fbe);
+                dfe.add(dfbe * dewt);
+                d2.add(dfbe * ewt * de);
                 if (J.lentro) {
                     const double con1 = dfbe * wt * x;
-                    dn1 += con1 * de;
-                    dn2 += con1;
+                    dn1.add(con1 * de);
+                    dn2.add(con1);
                 }
             }
         }
     }
-    es = block_sum_d(es, sh);
-    d1 = block_sum_d(d1, sh);
-    d2 = block_sum_d(d2, sh);
-    d3 = block_sum_d(d3, sh);
-    dfb = block_sum_d(dfb, sh);
-    dfe = block_sum_d(dfe, sh);
+    const double es_ = block_sum_dd(es, sh), d1_ = block_sum_dd(d1, sh), d2_ = block_sum_dd(d2, sh);
+    const double d3_ = block_sum_dd(d3, sh), dfb_ = block_sum_dd(dfb, sh), dfe_ = block_sum_dd(dfe, sh);
+    double ent_ = 0, dn1_ = 0, dn2_ = 0, sup_ = 0, sdn_ = 0;
     if (J.lentro) {
-        ent = block_sum_d(ent, sh);
-        dn1 = block_sum_d(dn1, sh);
-        dn2 = block_sum_d(dn2, sh);
+        ent_ = block_sum_dd(ent, sh);
+        dn1_ = block_sum_dd(dn1, sh);
+        dn2_ = block_sum_dd(dn2, sh);
     }
     if (J.nks > 0) {
-        sup = block_sum_d(sup, sh);
-        sdn = block_sum_d(sdn, sh);
+        sup_ = block_sum_dd(sup, sh);
+        sdn_ = block_sum_dd(sdn, sh);
     }
     if (tid == 0) {
         FermiOut o;
         o.efermi = mu;
-        o.e_total = es;
+        o.e_total = es_;
         o.fermi_shift = 0;
         o.pressure = 0;
         if (J.lpress) {
-            const double dfermi = (fabs(dfb) > 1e-10) ? dfe / dfb : 0.0;
+            const double dfermi = (fabs(dfb_) > 1e-10) ? dfe_ / dfb_ : 0.0;
             o.fermi_shift = dfermi;
-            o.pressure = -(d1 + (d2 - dfermi * d3));
+            o.pressure = -(d1_ + (d2_ - dfermi * d3_));
         }
-        o.entropy = ent;
-        o.dent1 = dn1;
-        o.dent2 = dn2;
-        o.spin_up = sup;
-        o.spin_dn = sdn;
+        o.entropy = ent_;
+        o.dent1 = dn1_;
+        o.dent2 = dn2_;
+        o.spin_up = sup_;
+        o.spin_dn = sdn_;
         o.iterations = it;
         o.pad = 0;
         J.out[0] = o;

@@ -25,6 +25,7 @@ NRLTB_E_IO = -6
 NRLTB_E_UNSUPPORTED = -7
 NRLTB_E_EOF = -8
 NRLTB_E_NODEVICE = -9
+NRLTB_E_TIMEOUT = -10
 
 NRLTB_K_OK = 0
 NRLTB_K_S_NOT_PD = 1
@@ -103,6 +104,8 @@ GPU_SYMBOLS = [
     ("nrltb_diag", C.c_int, [_vp, C.c_int, C.c_int, _dp, _dp, C.c_int, _dp, _dp, _ip]),
     ("nrltb_fermi", C.c_int, [_vp, C.c_int, C.c_int, _dp, _dp, C.c_double, C.c_double,
                               C.c_double, _dp]),
+    ("nrltb_sums", C.c_int, [_vp, C.c_int, C.c_int, _dp, _dp, _dp, C.c_int, C.c_double, C.c_double,
+                             C.c_double, C.c_double, _dp]),
     ("nrltb_search2_noalloc", C.c_int, [C.c_int, _vp, C.c_int, _vp, _vp, _dp, _ip, C.c_int, _dp, _dp,
                                         C.c_int, C.c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _ip, _ip, _dp]),
     # measurement hooks (include/nrltb_bench.h)
@@ -115,6 +118,7 @@ GPU_SYMBOLS = [
     ("nrltb_bench_cgemm_run", C.c_int, [_vp] + [C.c_int] * 9 + [_vp, _vp, _vp, C.c_int, _vp, C.c_int, _vp,
                                                                   C.c_int]),
     ("nrltb_bench_umma_fault", C.c_int, [C.c_int]),
+    ("nrltb_bench_raise_fault_word", C.c_int, [_vp]),
 ]
 
 HOST_SYMBOLS = [

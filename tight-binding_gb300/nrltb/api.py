@@ -321,7 +321,11 @@ def read_skin(path, lib=None):
 
 # ---- GPU context ---------------------------------------------------------------
 class NrltbError(RuntimeError):
-    pass
+    """A library call returned a negative NRLTB_E_* code (``code``)."""
+
+    def __init__(self, msg, code=None):
+        super().__init__(msg)
+        self.code = code
 
 
 class Context:
@@ -336,7 +340,7 @@ class Context:
 
     def _check(self, rc, what):
         if rc != 0:
-            raise NrltbError(f"{what} returned {rc}: {self.lib.nrltb_last_error().decode()}")
+            raise NrltbError(f"{what} returned {rc}: {self.lib.nrltb_last_error().decode()}", rc)
 
     def close(self):
         if getattr(self, "h", None):
