@@ -73,3 +73,12 @@ def test_search2_noalloc_limits():
     rc, _, _, _, _ = _noalloc(lib, big, par, 1, stream)
     assert rc == abi.NRLTB_E_CAPACITY
     assert b"no-allocation path takes at most" in lib.nrltb_last_error()
+    # an atom kind outside 1..kinds is refused before the search reads it
+    bad = synth.Structure(st.kkind.copy(), st.posn, st.plv, st.nd, st.volume)
+    bad.kkind[5] = par.kinds + 1
+    rc, _, _, _, _ = _noalloc(lib, bad, par, 1, stream)
+    assert rc == abi.NRLTB_E_ARG
+    assert b"outside 1.." in lib.nrltb_last_error()
+    # and the next well-formed call is unaffected
+    ref_rc, _, npairs, _, _ = _noalloc(lib, st, par, 1, stream)
+    assert ref_rc == abi.NRLTB_E_CAPACITY and npairs > 1

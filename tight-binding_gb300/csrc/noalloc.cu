@@ -12,7 +12,8 @@
 //
 // The array's host-side name is only a stand-in: its device address is taken
 // once per device with cudaGetSymbolAddress, on the first call made with that
-// device current, and every call after that reuses it.
+// device current (retried by later calls if that lookup failed), and every
+// call after that reuses it.
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -39,8 +40,17 @@ __device__ __align__(256) unsigned char g_noalloc_scratch[SCRATCH_BYTES];
 
 constexpr int MAX_DEVICES = 64;
 unsigned char *g_scratch_addr[MAX_DEVICES];
-std::once_flag g_scratch_once[MAX_DEVICES];
-cudaError_t g_scratch_err[MAX_DEVICES];
+std::mutex g_scratch_mutex;
+
+// atom kinds outside 1..kinds would index the cut-off tables out of range:
+// count them before the search reads them
+__global__ void k_noalloc_kinds(const int *kkind, int natoms, int kinds, int *bad)
+{
+    int nbad = 0;
+    for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < natoms; a += gridDim.x * blockDim.x)
+        nbad += (kkind[a] < 1 || kkind[a] > kinds);
+    if (nbad) atomicAdd(bad, nbad);
+}
 
 }  // namespace
 
@@ -69,14 +79,25 @@ extern "C" int nrltb_search2_noalloc(int device, void *stream, int natoms, const
         return NRLTB_E_CAPACITY;
     }
     if (cudaSetDevice(device) != cudaSuccess) return NRLTB_E_CUDA;
-    // set-up, once per device, with that device current
-    std::call_once(g_scratch_once[device], [device]() {
-        void *p = nullptr;
-        g_scratch_err[device] = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        g_scratch_addr[device] = (unsigned char *)p;
-    });
-    if (g_scratch_err[device] != cudaSuccess || !g_scratch_addr[device]) return NRLTB_E_CUDA;
-    unsigned char *base = g_scratch_addr[device];
+    // set-up, once per device, with that device current; a failed lookup is
+    // not remembered, so a later call tries again
+    unsigned char *base;
+    {
+        std::lock_guard<std::mutex> lock(g_scratch_mutex);
+        if (!g_scratch_addr[device]) {
+            void *p = nullptr;
+            const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+            if (e != cudaSuccess || !p) {
+                char msg[200];
+                snprintf(msg, sizeof msg, "cudaGetSymbolAddress of the no-allocation scratch array failed: %s",
+                         cudaGetErrorString(e));
+                nrltb_internal_set_error(msg);
+                return NRLTB_E_CUDA;
+            }
+            g_scratch_addr[device] = (unsigned char *)p;
+        }
+        base = g_scratch_addr[device];
+    }
     cudaStream_t s = (cudaStream_t)stream;
     unsigned char *code = base;
     int *blk = (int *)(base + OFF_BLK);
@@ -110,8 +131,18 @@ extern "C" int nrltb_search2_noalloc(int device, void *stream, int natoms, const
     P.param = nullptr;
     P.param_alt = nullptr;
     const int nblk = cdiv(ncand, SEARCH_BLOCK);
-    k_search_eval<<<std::min(cdiv(ncand, 256), 152 * 16), 256, 0, s>>>(S, P, ncand, code, misc, dmin);
     int host_misc[6];
+    k_noalloc_kinds<<<cdiv(natoms, 256) < 152 ? cdiv(natoms, 256) : 152, 256, 0, s>>>(d_kkind, natoms, kinds, misc + 3);
+    if (cudaMemcpyAsync(host_misc, misc, sizeof host_misc, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess)
+        return NRLTB_E_CUDA;
+    if (host_misc[3] != 0) {
+        char msg[200];
+        snprintf(msg, sizeof msg, "%d atom kind(s) outside 1..%d", host_misc[3], kinds);
+        nrltb_internal_set_error(msg);
+        return NRLTB_E_ARG;
+    }
+    k_search_eval<<<std::min(cdiv(ncand, 256), 152 * 16), 256, 0, s>>>(S, P, ncand, code, misc, dmin);
     if (cudaMemcpyAsync(host_misc, misc, sizeof host_misc, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
         cudaStreamSynchronize(s) != cudaSuccess)
         return NRLTB_E_CUDA;

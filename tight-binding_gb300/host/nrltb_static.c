@@ -115,6 +115,11 @@ int main(int argc, char **argv)
         nrltb_result res;
         memset(&res, 0, sizeof res);
         double *spdir = (spinopt & NRLTB_SKIN_SPIN_DIRECTIONS) ? malloc(sizeof(double) * 3 * (size_t)st.natoms) : NULL;
+        if ((spinopt & NRLTB_SKIN_SPIN_DIRECTIONS) && !spdir) {
+            fprintf(stderr, "nrltb_static: structure %d: out of host memory\n", jstruc);
+            status = 1;
+            break;
+        }
         res.spdir = spdir;
         const int nsp = (par.jspins == 2) ? 2 : 1;
         size_t nv = 0;
