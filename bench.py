@@ -13,10 +13,15 @@ solves/s = 27 / step time.
            library's stream.
   e2e      the same step through the reference-facing call nrltb_bande with
            host buffers (input upload and result download inside the region).
+  fp64     the same step in the FP64 form (plain FP64 eigensolve), timed
+           right after the mixed form in the same process; mixed_over_fp64 is
+           the ratio, and fp64.mixed_vs_fp64 the mixed form's error against it
+           over every k point (eigenvalues, E_F, E per atom, P in kbar).
   --impl reference
            the reference algorithm on the host cores: the C restatement in
            oracle/ (the Fortran reference cannot be compiled here), one k per
-           thread on all host threads, single-threaded LAPACK zhpgv per k.
+           thread on every host core this process may run on (its affinity
+           mask), single-threaded LAPACK zhpgv per k.
 
 The step's working set (H, S, dH, dS and the solver workspace for 27 k) is
 several GB, far larger than L2, so no L2 flush is needed between steps.
@@ -145,15 +150,25 @@ class ClockSampler:
 
 
 def cpu_sample(st, par, km, mode, nthreads, nk_sample, flags=0):
-    """Oracle (reference algorithm) on the first nk_sample k points, all threads."""
+    """Oracle (reference algorithm) on the first nk_sample k points, all
+    threads: (seconds, the oracle's result for those k points)."""
     sys.path.insert(0, os.path.join(REPO, "oracle"))
     import oracle
     from nrltb import KMesh, Opts
     sub = KMesh(km.k[:nk_sample], km.w[:nk_sample] / km.w[:nk_sample].sum())
     opts = Opts(mode=mode, tkb=0.005, eigcut=1e3, flags=flags)
     t0 = time.perf_counter()
-    oracle.bande(st, par, sub, opts, nthreads=nthreads)
-    return time.perf_counter() - t0
+    r = oracle.bande(st, par, sub, opts, nthreads=nthreads)
+    return time.perf_counter() - t0, r
+
+
+def host_cores():
+    """The host cores this process may run on (its affinity mask), which is
+    what the container exposes; os.cpu_count() if the mask is unavailable."""
+    try:
+        return len(os.sched_getaffinity(0))
+    except (AttributeError, OSError):
+        return os.cpu_count() or 1
 
 
 def run_reference(args):
@@ -162,11 +177,11 @@ def run_reference(args):
         return 0
     st0, par0, km, o = workload(args.config)
     st, par, mode, flags, per_k = row_setup(args.row, st0, par0)
-    ncores = os.cpu_count() or 1
+    ncores = host_cores()
     nks = min(km.nk, ncores)
     times = []
     for i in range(args.warmup + args.steps):
-        t = cpu_sample(st, par, km, mode, ncores, nks, flags)
+        t, _ = cpu_sample(st, par, km, mode, ncores, nks, flags)
         if i >= args.warmup:
             times.append(t)
     mean = sum(times) / len(times)
@@ -177,7 +192,8 @@ def run_reference(args):
             "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": mean * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded structure and parameters)",
-            "config": {"workload": workload_desc(args.config, st0, par0, km, args.row), "host_cores": ncores},
+            "config": {"workload": workload_desc(args.config, st0, par0, km, args.row), "host_cores": ncores,
+                       "host_cores_note": "the cores this process may run on (its affinity mask)"},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": ncores, "kind": "port",
                              "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -185,14 +201,15 @@ def run_reference(args):
     return 0
 
 
-KCLASSES = [  # (class id, name, bound, unit of work)
+KCLASSES = [  # (class id, name, bound, unit of work, kernel name prefix in ncu)
     (0, "zgemm_umma_kernel / zgemm_tc_kernel: FP32 complex GEMM on the tensor cores (3xTF32; tcgen05 with "
-        "tensor-memory accumulators for op(A) = A, mma.sync for op(A) = A^H)", "tensor", "flop"),
+        "tensor-memory accumulators for op(A) = A, mma.sync for op(A) = A^H)", "tensor", "flop", "zgemm_umma"),
     (1, "zgemm_kernel: complex GEMM on the FMA pipe (FP64 form; FP32 shapes below the tensor-core thresholds)",
-     "fma", "flop"),
+     "fma", "flop", "zgemm_kernel"),
     (2, "k_oz_gemm: bf16 digit products on tcgen05 (refinement H X, S X to FP64 accuracy; Hellmann-Feynman "
-        "dH Z, dS Z from 3-digit dH, dS)", "tensor", "flop"),
-    (3, "k_tri_panel: tridiagonalisation panel (cluster per matrix, Hermitian mat-vec)", "hbm", "byte"),
+        "dH Z, dS Z from 3-digit dH, dS)", "tensor", "flop", "k_oz_gemm"),
+    (3, "k_tri_panel: tridiagonalisation panel (cluster per matrix, Hermitian mat-vec)", "hbm", "byte",
+     "k_tri_panel"),
 ]
 
 
@@ -200,13 +217,14 @@ def kernel_stats(lib, ctx, steps):
     """Per-class totals of the timed region: ms per step, launches per step, work per step."""
     import ctypes as C
     out = []
-    for cls, name, bound, unit in KCLASSES:
+    for cls, name, bound, unit, ncu_name in KCLASSES:
         ms, work, n = C.c_double(), C.c_double(), C.c_int()
         lib.nrltb_bench_kernel_stats(ctx.h, cls, C.byref(ms), C.byref(work), C.byref(n))
         if n.value == 0:
             continue
         rate = work.value / (ms.value * 1e-3)
-        out.append({"class": cls, "kernel": name, "bound": bound, "ms_per_step": ms.value / steps,
+        out.append({"class": cls, "kernel": name, "ncu_name": ncu_name, "bound": bound,
+                    "ms_per_step": ms.value / steps,
                     "launches_per_step": n.value / steps,
                     ("tflops" if unit == "flop" else "gbs"): rate / (1e12 if unit == "flop" else 1e9),
                     "work_unit": unit})
@@ -221,18 +239,45 @@ def measured_peaks():
         return {}
 
 
-def roofline_of(lib, ctx, kernels, prec):
-    """Roofline entry of the class with the most time in the timed region."""
+def pipe_peaks(lib, ctx):
+    """Live microbenchmarks of the pipes MEASURED_PEAKS.json does not cover."""
     import ctypes as C
+    pipe = {}
+    for kind, name in ((0, "fp64_fma_tflops"), (1, "fp32_fma_tflops"), (2, "mma_sync_bf16_tflops"),
+                       (3, "mma_sync_tf32_tflops"), (4, "l2_read_gbs")):
+        t = C.c_double()
+        if lib.nrltb_bench_peak(ctx.h, kind, C.byref(t)) == 0:
+            pipe[name] = t.value
+    return pipe
+
+
+def profile_traffic(kernel_prefix):
+    """DRAM bytes per launch of a kernel from a committed ncu summary: the
+    summaries in profiles/ carry a line 'traffic_per_launch <kernel> <bytes>
+    <what one launch processed>' taken from the capture they describe."""
+    pdir = os.path.join(REPO, "profiles")
+    try:
+        names = sorted(os.listdir(pdir))
+    except OSError:
+        return None
+    for f in names:
+        if not f.endswith(".md"):
+            continue
+        with open(os.path.join(pdir, f)) as fh:
+            for line in fh:
+                parts = line.strip().strip("`").split(None, 3)
+                if len(parts) >= 3 and parts[0] == "traffic_per_launch" and parts[1].startswith(kernel_prefix):
+                    return {"bytes": float(parts[2]), "per": parts[3] if len(parts) > 3 else "",
+                            "source": "profiles/" + f}
+    return None
+
+
+def roofline_of(kernels, prec, pipe):
+    """Roofline entry of the class with the most time in the timed region."""
     if not kernels:
         return None
     dom = max(kernels, key=lambda k: k["ms_per_step"])
     peaks = measured_peaks()
-    pipe = {}
-    for kind, name in ((0, "fp64_fma"), (1, "fp32_fma"), (2, "mma_sync_bf16"), (3, "mma_sync_tf32")):
-        t = C.c_double()
-        if lib.nrltb_bench_peak(ctx.h, kind, C.byref(t)) == 0:
-            pipe[name + "_tflops"] = t.value
     r = {"kernel": dom["kernel"], "ms_per_step": dom["ms_per_step"], "launches_per_step": dom["launches_per_step"],
          "traffic": None, "measured_live": "CUDA events around each launch of the class on the library stream, "
                                            "summed over K instrumented steps run right after the timed ones"}
@@ -241,15 +286,29 @@ def roofline_of(lib, ctx, kernels, prec):
         r.update({"bound": "hbm", "achieved": dom["gbs"], "peak": peak, "unit": "GB/s", "frac": dom["gbs"] / peak,
                   "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if "hbm_gbs" in peaks
                   else "fallback 6.8 TB/s",
-                  "algorithmic": "lower triangle of the trailing matrix per column, read once (FP32 complex)"})
+                  "algorithmic": "lower triangle of the trailing matrix per column, read once (FP32 complex): "
+                                 "N^3/6 elements x 8 B per matrix"})
+        tr = profile_traffic(dom.get("ncu_name", ""))
+        if tr:
+            r["traffic"] = tr["bytes"]
+            r["traffic_source"] = f"{tr['source']} ({tr['per']})"
+        if "l2_read_gbs" in pipe:
+            r["l2"] = {"peak_gbs": pipe["l2_read_gbs"], "frac": dom["gbs"] / pipe["l2_read_gbs"],
+                       "peak_source": "live L2 read microbenchmark (nrltb_bench_peak kind 4)"}
+        r["bound_note"] = ("the panel kernel's operands mostly stay in L2 (DRAM traffic well below the "
+                           "algorithmic bytes); it is latency- and barrier-bound, so the fraction is also "
+                           "given against the live L2 read bandwidth")
     elif dom["bound"] == "tensor":
         peak = peaks.get("bf16_tflops", 1900.0)
         r.update({"bound": "tensor", "achieved": dom["tflops"], "peak": peak, "unit": "TFLOP/s",
                   "frac": dom["tflops"] / peak,
                   "peak_source": "MEASURED_PEAKS.json bf16_tflops (cuBLAS dense bf16, burst; of measured)",
                   "algorithmic": "8 flops per complex multiply-add the GEMM needs (triangular zeros and "
-                                 "skipped C triangles excluded)",
-                  "pipe_peaks_live": pipe})
+                                 "skipped C triangles excluded)"})
+        tr = profile_traffic(dom.get("ncu_name", ""))
+        if tr:
+            r["traffic"] = tr["bytes"]
+            r["traffic_source"] = f"{tr['source']} ({tr['per']})"
     else:
         kind = "fp64_fma_tflops" if prec == 0 else "fp32_fma_tflops"
         peak = pipe.get(kind)
@@ -257,7 +316,8 @@ def roofline_of(lib, ctx, kernels, prec):
                   "frac": dom["tflops"] / peak if peak else None,
                   "peak_source": "live FMA-pipe microbenchmark (GB300 has no FP64 tensor path; "
                                  "MEASURED_PEAKS.json has no FMA-pipe figure)",
-                  "algorithmic": "8 flops per complex multiply-add the GEMM needs", "pipe_peaks_live": pipe})
+                  "algorithmic": "8 flops per complex multiply-add the GEMM needs"})
+    r["pipe_peaks_live"] = pipe
     return r
 
 
@@ -271,6 +331,8 @@ def main():
     ap.add_argument("--row", default="path", choices=ROWS)
     ap.add_argument("--precision", default="auto", choices=["auto", "fp64", "mixed"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true", help="skip the FP64-form timing of the same step")
+    ap.add_argument("--fp64-steps", type=int, default=2, help="timed steps of the FP64 form (after one untimed)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -360,8 +422,48 @@ def main():
     if r.orbocc is not None:
         d2h += r.orbocc.nbytes
 
+    # ---- the FP64 form on the same step (the metric's other half) ----
+    fp64 = None
+    if prec == abi.PREC_MIXED and not args.no_fp64:
+        opts64 = Opts(mode=mode, precision=abi.PREC_FP64, tkb=o["tkb"], eigcut=1e3, fermi_tol=1e-11, flags=flags)
+        ctx.stage(st, par, km, opts64)
+        ctx.run()                                   # one untimed step (buffers sized, clocks up)
+        k64 = max(1, min(args.steps, args.fp64_steps))
+        barrier()
+        e0.record(stream)
+        for _ in range(k64):
+            ctx.run()
+        e1.record(stream)
+        barrier()
+        ms64 = max_over_ranks(e0.elapsed_time(e1) / k64)
+        r64 = ctx.fetch()
+        fp64 = {"value": ws * nk / (ms64 * 1e-3), "unit": UNIT, "ms_per_step": ms64, "steps": k64,
+                "warmup": 1, "dtype": "f64"}
+        # accuracy of the mixed form against the FP64 GPU form, every k point
+        # of the step (outside any timed region)
+        ok = (res.k_status == 0) & (r64.k_status == 0)
+        fp64["mixed_vs_fp64"] = {
+            "k_points_compared": int(ok.sum()),
+            "max_abs_eig_ry": float(np.abs(res.eig[ok] - r64.eig[ok]).max()) if ok.any() else None,
+            "abs_efermi_ry": abs(res.efermi - r64.efermi),
+            "abs_etotal_ry_per_atom": abs(res.e_total - r64.e_total) / st.natoms,
+            "abs_pressure_kbar": abs(res.pressure - r64.pressure) * 147105.08,
+            "tolerances": {"eig_ry": 1e-9, "efermi_ry": 1e-9, "etotal_ry_per_atom": 1e-8, "pressure_kbar": 1e-3}}
+
     # ---- roofline of the dominant kernel class, from the timed region's events ----
-    roofline = roofline_of(lib, ctx, kernels, prec)
+    pipe = pipe_peaks(lib, ctx)
+    roofline = roofline_of(kernels, prec, pipe)
+    # whole-eigensolve figure: F_eig(N) = 24 N^3 real flops per k-point solve
+    nv = int(res.nv)
+    eig_tflops = value * 24.0 * nv ** 3 / 1e12
+    peaks = measured_peaks()
+    tf32 = peaks.get("bf16_tflops", 1900.0) / 2.0
+    eigensolve = {"flops_per_solve": 24.0 * nv ** 3, "achieved_tflops": eig_tflops,
+                  "tf32_peak_tflops": tf32, "frac": eig_tflops / tf32,
+                  "peak_source": "half of MEASURED_PEAKS.json bf16_tflops (TF32 runs at half the bf16 rate "
+                                 "on the tcgen05 tensor cores; no measured TF32 figure)",
+                  "note": "k-point solves/s x 24 N^3, the complex LAPACK operation count of one generalized "
+                          "eigensolve with vectors"}
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_dev, "higher_is_better": True,
@@ -376,15 +478,27 @@ def main():
                     "d2h_bytes_per_step": int(d2h), "ms_per_step": ms_e2e},
             "gpu_launches": int(launches_value),
             "gpu_launches_e2e": int(launches_e2e),
-            "clocks": clocks, "roofline": roofline, "kernels": kernels}
+            "clocks": clocks, "roofline": roofline, "eigensolve_roofline": eigensolve, "kernels": kernels}
+    if fp64 is not None:
+        line["fp64"] = fp64
+        line["fp64_value"] = fp64["value"]
+        line["mixed_over_fp64"] = value / fp64["value"]
 
     if rank == 0 and not args.no_cpu_baseline:
-        ncores = os.cpu_count() or 1
+        ncores = host_cores()
         nks = min(km.nk, ncores)
-        t = cpu_sample(st, par, km, mode, ncores, nks, flags)
+        t, ro = cpu_sample(st, par, km, mode, ncores, nks, flags)
         line["cpu_baseline"] = {"value": per_k * nks / t, "unit": UNIT, "cores": ncores, "kind": "port",
                                 "sample": f"{nks} of {km.nk} k points, one per host thread, mode {mode} "
-                                          f"(setham + zhpgv with vectors + sethamv + perturb + Fermi/E/P)"}
+                                          f"(setham + zhpgv with vectors + sethamv + perturb + Fermi/E/P)",
+                                "cores_note": "the host cores this process may run on (its affinity mask)"}
+        if args.row == "path":
+            # the same k points' eigenvalues from the GPU step against the oracle's
+            rows = np.arange(nks)
+            ok = res.k_status[rows] == 0
+            line["accuracy_vs_oracle"] = {
+                "k_points": int(ok.sum()), "form": "mixed" if prec == abi.PREC_MIXED else "fp64",
+                "max_abs_eig_ry": float(np.abs(res.eig[rows][ok] - ro.eig[ok]).max()) if ok.any() else None}
     if rank == 0:
         print(json.dumps(line), flush=True)
     ctx.close()
