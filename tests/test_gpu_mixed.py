@@ -106,6 +106,15 @@ def test_mixed_bande_fcc128_two_k(ctx):
     _compare(ctx, st, par, _sub(km, [0, 13]), o["tkb"])
 
 
+def test_mixed_bande_fcc128_full_mesh(ctx):
+    """The benchmarked step itself: fcc128 (N = 1152), all 27 k of the 3x3x3
+    mesh, mode 4, mixed form against the oracle (the oracle's 27 solves take
+    tens of seconds on the host cores)."""
+    st, par, km, o = synth.fcc128()
+    g, oo = _compare(ctx, st, par, km, o["tkb"])
+    assert g.eig.shape == (27, 1152)
+
+
 def test_mixed_bande_ex1_against_skout(ctx, ex1, ex1_gold):
     for idx in (0, 9):
         _, _, st, km = ex1.structures[idx]

@@ -49,7 +49,7 @@ template <typename T> void eig_work_carve(EigWork<T> &w, void *base, int n, int 
     w.e = (double *)take(sizeof(double) * n * nb);
     w.lam = (double *)take(sizeof(double) * n * nb);
     // inverse iteration: 6 arrays of n per thread slot, 64 cdiv(n, 64) slots per matrix
-    w.ylu = (double *)take(sizeof(double) * 6 * (size_t)n * (64 * (size_t)cdiv(n, 64)) * nb);
+    w.ylu = (double *)take(sizeof(double) * 4 * (size_t)n * (64 * (size_t)cdiv(n, 64)) * nb);
     w.yvec = (double *)take(sizeof(double) * nn * nb);
     w.perm = (int *)take(sizeof(int) * 4 * n * nb);
     w.counter = (unsigned *)take(sizeof(unsigned) * nb);
@@ -580,8 +580,20 @@ template <typename TB> struct Strided {
 // independent random combinations inside its invariant subspace, and a member
 // separated by g from the others keeps only ~eps ||T|| / g of their
 // directions, so orthonormalising after the iteration spans the same subspace
-// as re-orthogonalising during it.  Scratch: 6 arrays of n TB per thread,
-// interleaved across the launch's threads.
+// as re-orthogonalising during it.
+//
+// Each iteration is two sweeps.  The forward sweep factors T_block - lam I =
+// P L U (dgttrf, the running row in registers) and applies P and L at the
+// same time; the multipliers are used as they are made and never stored, and
+// U's three diagonals are stored in the first iteration only (every
+// iteration recomputes the same factor).  The backward sweep solves with U
+// and accumulates the norm and the largest component; the normalisation is
+// applied as the next sweep reads the vector.  Scratch: 4 arrays of n TB per
+// thread, interleaved across the launch's threads (a warp's accesses to one
+// element index are one coalesced line); the backward sweep loads INV_BLK
+// steps' operands at once so that their latencies overlap.
+constexpr int INV_BLK = 8;
+
 template <typename TB>
 __global__ void k_tri_invit(const double *dd, const double *ee, const double *lamloc, const int *blk,
                             const int *rank, double *yvec, TB *scratch, int n)
@@ -595,74 +607,92 @@ __global__ void k_tri_invit(const double *dd, const double *ee, const double *la
     double tnorm = 0;
     for (int k = b0; k <= b1; ++k)
         tnorm = fmax(tnorm, fabs(d[k]) + (k > b0 ? fabs(e[k - 1]) : 0.0) + (k < b1 ? fabs(e[k]) : 0.0));
-    // thread-interleaved scratch: element k of array a at S[(a n + k) NT]
     const long NT = (long)gridDim.y * gridDim.x * blockDim.x;
     Strided<TB> S(scratch + ((long)blockIdx.y * gridDim.x + blockIdx.x) * blockDim.x + threadIdx.x, NT);
-    // multipliers, 1 / pivots, first and second super-diagonals of U, pivot flags, iterate
-    Strided<TB> DL = S, RG = S + n, DU = S + 2 * n, DU2 = S + 3 * n, PV = S + 4 * n, v = S + 5 * n;
+    // 1 / pivots, first and second super-diagonals of U, iterate
+    Strided<TB> RG = S, DU = S + n, DU2 = S + 2 * n, v = S + 3 * n;
     const TB tiny = eps_of<TB>() * TB(2) * TB(fmax(tnorm, (double)tiny_of<TB>()));
     const TB lam = TB(L[r]);
     auto pivot = [&](TB g) { return (fabs(g) < tiny) ? ((g < TB(0)) ? -tiny : tiny) : g; };
-    // factor T_block - lam I = P L U (dgttrf), the running row carried in registers
-    {
-        TB dcur = TB(d[b0]) - lam, ducur = (len > 1) ? TB(e[b0]) : TB(0);
-        for (int k = 0; k < len - 1; ++k) {
-            const TB dlk = TB(e[b0 + k]);
-            TB dnext = TB(d[b0 + k + 1]) - lam;
-            TB dunext = (k < len - 2) ? TB(e[b0 + k + 1]) : TB(0);
-            if (fabs(dcur) >= fabs(dlk)) {
-                const TB f = (dcur != TB(0)) ? tri_div(dlk, dcur) : TB(0);
-                DL[k] = f; RG[k] = tri_div(TB(1), pivot(dcur)); DU[k] = ducur; DU2[k] = TB(0); PV[k] = TB(0);
-                dnext -= f * ducur;
-            } else {
-                const TB f = tri_div(dcur, dlk);
-                DL[k] = f; RG[k] = tri_div(TB(1), pivot(dlk)); DU[k] = dnext; DU2[k] = dunext; PV[k] = TB(1);
-                dnext = ducur - f * dnext;
-                dunext = -f * dunext;
-            }
-            dcur = dnext;
-            ducur = dunext;
-        }
-        RG[len - 1] = tri_div(TB(1), pivot(dcur));
-    }
-    for (int k = 0; k < len; ++k) v[k] = TB(hash_unit((unsigned)(b * 7919 + r), (unsigned)k));
+    const unsigned seed = (unsigned)(b * 7919 + r);
     // dstein's one converging solve and two extra (FP64); the FP32 solve of the
     // mixed form is refined afterwards, so one extra suffices there
     const int iters = sizeof(TB) == 8 ? 3 : 2;
+    TB inv = TB(1);
+    int kmax = 0;
+    TB vmax = TB(-1), vkmax = TB(0);
     for (int it = 0; it < iters; ++it) {
-        // solve: apply P and L (running element in a register)
-        TB vc = v[0];
-        for (int k = 0; k < len - 1; ++k) {
-            const TB vn = v[k + 1], f = DL[k];
-            if (PV[k] == TB(0)) { v[k] = vc; vc = vn - f * vc; }
-            else { v[k] = vn; vc = vc - f * vn; }
+        // forward: factor (dgttrf) and apply P, L; element k + 1 of the
+        // right-hand side is the previous iterate scaled by inv (the random
+        // start in the first iteration)
+        auto rhs = [&](int k) { return it == 0 ? TB(hash_unit(seed, (unsigned)k)) : v[k] * inv; };
+        TB dcur = TB(d[b0]) - lam, ducur = (len > 1) ? TB(e[b0]) : TB(0);
+        TB vc = rhs(0);
+        for (int kb = 0; kb < len - 1; kb += INV_BLK) {
+            TB vn[INV_BLK];
+#pragma unroll
+            for (int u = 0; u < INV_BLK; ++u)
+                if (kb + u < len - 1) vn[u] = rhs(kb + u + 1);
+#pragma unroll
+            for (int u = 0; u < INV_BLK; ++u) {
+                const int k = kb + u;
+                if (k >= len - 1) break;
+                const TB dlk = TB(e[b0 + k]);
+                TB dnext = TB(d[b0 + k + 1]) - lam;
+                TB dunext = (k < len - 2) ? TB(e[b0 + k + 1]) : TB(0);
+                if (fabs(dcur) >= fabs(dlk)) {
+                    const TB f = (dcur != TB(0)) ? tri_div(dlk, dcur) : TB(0);
+                    if (it == 0) { RG[k] = tri_div(TB(1), pivot(dcur)); DU[k] = ducur; DU2[k] = TB(0); }
+                    dnext -= f * ducur;
+                    v[k] = vc;
+                    vc = vn[u] - f * vc;
+                } else {
+                    const TB f = tri_div(dcur, dlk);
+                    if (it == 0) { RG[k] = tri_div(TB(1), pivot(dlk)); DU[k] = dnext; DU2[k] = dunext; }
+                    dnext = ducur - f * dnext;
+                    dunext = -f * dunext;
+                    v[k] = vn[u];
+                    vc = vc - f * vn[u];
+                }
+                dcur = dnext;
+                ducur = dunext;
+            }
         }
-        v[len - 1] = vc;
-        // U back-substitution (the two following elements in registers)
-        TB x1 = v[len - 1] * RG[len - 1], x2 = TB(0);
+        if (it == 0) RG[len - 1] = tri_div(TB(1), pivot(dcur));
+        // backward: U solve (the two following elements in registers), the
+        // norm and the largest component (first in increasing k on ties)
+        TB x1 = vc * RG[len - 1], x2 = TB(0);
         v[len - 1] = x1;
-        for (int k = len - 2; k >= 0; --k) {
-            const TB xk = (v[k] - DU[k] * x1 - DU2[k] * x2) * RG[k];
-            v[k] = xk;
-            x2 = x1;
-            x1 = xk;
+        TB nrm = x1 * x1;
+        vmax = fabs(x1); kmax = len - 1; vkmax = x1;
+        for (int kb = len - 2; kb >= 0; kb -= INV_BLK) {
+            TB du[INV_BLK], du2[INV_BLK], rg[INV_BLK], vv[INV_BLK];
+#pragma unroll
+            for (int u = 0; u < INV_BLK; ++u) {
+                const int k = kb - u;
+                if (k >= 0) { du[u] = DU[k]; du2[u] = DU2[k]; rg[u] = RG[k]; vv[u] = v[k]; }
+            }
+#pragma unroll
+            for (int u = 0; u < INV_BLK; ++u) {
+                const int k = kb - u;
+                if (k >= 0) {
+                    const TB xk = (vv[u] - du[u] * x1 - du2[u] * x2) * rg[u];
+                    v[k] = xk;
+                    nrm += xk * xk;
+                    if (fabs(xk) >= vmax) { vmax = fabs(xk); kmax = k; vkmax = xk; }
+                    x2 = x1;
+                    x1 = xk;
+                }
+            }
         }
-        TB nrm = 0;
-        for (int k = 0; k < len; ++k) nrm += v[k] * v[k];
         nrm = sqrt(nrm);
-        const TB inv = (nrm > TB(0)) ? TB(1) / nrm : TB(0);
-        for (int k = 0; k < len; ++k) v[k] *= inv;
+        inv = (nrm > TB(0)) ? TB(1) / nrm : TB(0);
     }
     // sign convention: largest component positive
-    int kmax = 0;
-    TB vmax = TB(-1);
-    for (int k = 0; k < len; ++k) {
-        const TB a = fabs(v[k]);
-        if (a > vmax) { vmax = a; kmax = k; }
-    }
-    const double sg = (v[kmax] < TB(0)) ? -1.0 : 1.0;
+    (void)kmax;
+    const double sg = (vkmax < TB(0)) ? -1.0 : 1.0;
     double *z = yvec + (long)b * n * n + (long)rank[(long)b * n + r] * n;
-    for (int k = 0; k < n; ++k) z[k] = (k >= b0 && k <= b1) ? sg * (double)v[k - b0] : 0.0;
+    for (int k = 0; k < n; ++k) z[k] = (k >= b0 && k <= b1) ? sg * (double)(v[k - b0] * inv) : 0.0;
 }
 
 // Orthonormalise each cluster of eigenvalues closer than ctol ||T|| (within

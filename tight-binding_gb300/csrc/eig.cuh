@@ -54,7 +54,7 @@ template <typename T> struct EigWork {
     C2 *Xt;                         // EIG_NB x n per matrix
     double *d, *e;                  // tridiagonal, n per matrix
     double *lam;                    // eigenvalues, n per matrix (ascending)
-    double *ylu;                    // inverse-iteration scratch, 5 n per thread
+    double *ylu;                    // inverse-iteration scratch, 4 n per thread
     double *yvec;                   // real eigenvectors of T, n x n per matrix
     int *perm;                      // eigenvalue -> block bookkeeping, 3 n per matrix
     unsigned *counter;              // per-matrix ticket counters (last-CTA pattern)

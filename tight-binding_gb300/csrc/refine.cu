@@ -215,9 +215,30 @@ __global__ void __launch_bounds__(1024) k_ref_clusters(RefineWork w, int *status
     }
 }
 
+// Double-float accumulator of exact products on the FP32 pipe: x * (yh + yl)
+// with x, yh, yl floats; x * yh is split into its rounded value and rounding
+// error (FMA), the rounded values are summed by Knuth's two-sum, and the
+// errors and the small x * yl terms go into the low word.
+struct DFAcc {
+    float hi = 0.f, lo = 0.f;
+    __device__ __forceinline__ void add_prod(float x, float yh, float yl)
+    {
+        // _rn intrinsics: no contraction into FMAs, which would break the
+        // exactness of the product split and of the two-sum
+        const float pr = __fmul_rn(x, yh);
+        const float pe = fmaf(x, yh, -pr);
+        const float s = __fadd_rn(hi, pr), bp = __fsub_rn(s, hi);
+        const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bp)), __fsub_rn(pr, bp));
+        hi = s;
+        lo += err + fmaf(x, yl, pe);
+    }
+    __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
+};
+
 // ---- 2b. Rayleigh-Ritz inside each cluster: one CTA per cluster -------------
 // The cluster block T_ab = x_a^H (H x_b), R_ab = x_a^H (S x_b) is formed with
-// FP64 dot products (a thread per entry); one warp then solves the pencil.  Column j's rotation is stored as w.U[j*CMAX + a], its
+// exact products in double-float (a warp per entry); one warp then solves the
+// pencil in FP64.  Column j's rotation is stored as w.U[j*CMAX + a], its
 // coefficient on the cluster's a-th member (sorted position pos0 + a); the
 // members' eigenvalues replace the estimates and their R'_jj becomes 1.
 __global__ void __launch_bounds__(REF_CMAX * REF_CMAX) k_ref_rr(RefineWork w, const float2 *X)
@@ -238,27 +259,40 @@ __global__ void __launch_bounds__(REF_CMAX * REF_CMAX) k_ref_rr(RefineWork w, co
         return;
     }
     const long mo = (long)b * n * n;
-    // T_rq = x_r^H (H x_q), R_rq = x_r^H (S x_q) in FP64, one thread per (q, r)
-    // pair: the FP64 work of a large cluster is spread over the SM's four
-    // sub-partitions
-    // (Hermitian blocks: only r <= q is formed, the other triangle is its conjugate)
-    if (tid < c * (c + 1) / 2) {
-        int q = 0, rem = tid;
+    // T_rq = x_r^H (H x_q), R_rq = x_r^H (S x_q), r <= q (Hermitian blocks: the
+    // other triangle is the conjugate).  A warp per entry, its lanes over the
+    // rows; the products of the FP32 x with the FP64 H x, S x are formed
+    // exactly on the FP32 pipe (the FP64 factor split into two floats, the
+    // leading product's rounding error recovered by an FMA) and summed in
+    // double-float (Knuth's two-sum): ~2^-46 relative, without the FP64 pipe.
+    const int ne = c * (c + 1) / 2, nwarps = blockDim.x >> 5;
+    for (int e = warp; e < ne; e += nwarps) {
+        int q = 0, rem = e;
         while (rem > q) { rem -= q + 1; ++q; }
         const int r = rem;
         const float2 *xr = X + mo + (long)ord[p + r] * n;
         const double2 *hq = w.YH + mo + (long)ord[p + q] * n, *sq = w.YS + mo + (long)ord[p + q] * n;
-        double2 t = make_double2(0, 0), u = make_double2(0, 0);
-        for (int i = 0; i < n; ++i) {
-            const float2 xf = xr[i];
-            const double2 x = make_double2(xf.x, xf.y);
-            t = cadd(t, cmulc(x, hq[i]));
-            u = cadd(u, cmulc(x, sq[i]));
+        DFAcc tre, tim, rre, rim;
+        for (int i = lane; i < n; i += 32) {
+            const float2 x = xr[i];
+            const double2 h = hq[i], sv = sq[i];
+            const float2 hh = make_float2((float)h.x, (float)h.y), sh = make_float2((float)sv.x, (float)sv.y);
+            const float2 hl = make_float2((float)(h.x - (double)hh.x), (float)(h.y - (double)hh.y));
+            const float2 sl = make_float2((float)(sv.x - (double)sh.x), (float)(sv.y - (double)sh.y));
+            // conj(x) y = (xr yr + xi yi) + i (xr yi - xi yr)
+            tre.add_prod(x.x, hh.x, hl.x); tre.add_prod(x.y, hh.y, hl.y);
+            tim.add_prod(x.x, hh.y, hl.y); tim.add_prod(-x.y, hh.x, hl.x);
+            rre.add_prod(x.x, sh.x, sl.x); rre.add_prod(x.y, sh.y, sl.y);
+            rim.add_prod(x.x, sh.y, sl.y); rim.add_prod(-x.y, sh.x, sl.x);
         }
-        A[q][r] = t;
-        Bm[q][r] = u;
-        A[r][q] = cconj(t);
-        Bm[r][q] = cconj(u);
+        const double2 t = make_double2(warp_sum(tre.value()), warp_sum(tim.value()));
+        const double2 u = make_double2(warp_sum(rre.value()), warp_sum(rim.value()));
+        if (lane == 0) {
+            A[q][r] = t;
+            Bm[q][r] = u;
+            A[r][q] = cconj(t);
+            Bm[r][q] = cconj(u);
+        }
     }
     __syncthreads();
     if (warp != 0) return;
