@@ -151,6 +151,10 @@ struct CallScope {
     }
 };
 
+// d_fout: the FermiOut record, then the sums' per-CTA partials
+static size_t fermi_out_bytes() { return 256 + fermi_part_bytes(); }
+static double *fermi_part(nrltb_ctx *c) { return (double *)(c->d_fout.as<char>() + 256); }
+
 // A bounded device wait of a tcgen05 kernel ran out: every k of the chunk
 // that launched it gets NRLTB_K_TIMEOUT, and the word is cleared for the next
 // chunk (one CTA, stream-ordered after the kernels it checks).
@@ -833,12 +837,12 @@ static int run_all(nrltb_ctx *c)
         job.nks = (nsp == 2) ? nk : 0;
         job.el = (nsp == 2 || S.noncol) ? 1.0 : 2.0;   // electrons per band, bande.f:1065-1073
         job.tkb = o.tkb; job.zfill = S.zfill; job.tol = (o.fermi_tol > 0) ? o.fermi_tol : 1e-8;
-        if ((rc = c->d_fout.ensure(sizeof(FermiOut)))) break;
+        if ((rc = c->d_fout.ensure(fermi_out_bytes()))) break;
         if ((rc = c->d_fjob.ensure(sizeof(FermiJob)))) break;
         job.out = c->d_fout.as<FermiOut>();
         cudaError_t e = cudaMemcpyAsync(c->d_fjob.p, &job, sizeof job, cudaMemcpyHostToDevice, s);
         if (e != cudaSuccess) { set_err("copy: %s", cudaGetErrorString(e)); rc = NRLTB_E_CUDA; break; }
-        NRLTB_LAUNCH(k_fermi_sums, 1, 1024, 0, s, c->d_fjob.as<FermiJob>());
+        launch_fermi_sums(s, c->d_fjob.as<FermiJob>(), fermi_part(c));
         e = cudaGetLastError();
         if (e != cudaSuccess) { set_err("fermi: %s", cudaGetErrorString(e)); rc = NRLTB_E_CUDA; break; }
         if (lspdir)
@@ -1252,7 +1256,7 @@ int nrltb_fermi(nrltb_ctx *c, int nv, int nk, const double *eig, const double *w
     cudaStream_t s = c->stream;
     RET(c->d_eig.ensure(sizeof(double) * (size_t)nv * nk));
     RET(c->d_kw.ensure(sizeof(double) * nk));
-    RET(c->d_fout.ensure(sizeof(FermiOut)));
+    RET(c->d_fout.ensure(fermi_out_bytes()));
     RET(c->d_fjob.ensure(sizeof(FermiJob)));
     CK(cudaMemcpyAsync(c->d_eig.p, eig, sizeof(double) * (size_t)nv * nk, cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(c->d_kw.p, w, sizeof(double) * nk, cudaMemcpyHostToDevice, s));
@@ -1267,7 +1271,7 @@ int nrltb_fermi(nrltb_ctx *c, int nv, int nk, const double *eig, const double *w
     CK(cudaMemcpyAsync(c->d_fjob.p, &job, sizeof job, cudaMemcpyHostToDevice, s));
     {
         CallScope scope(c);
-        NRLTB_LAUNCH(k_fermi_sums, 1, 1024, 0, s, c->d_fjob.as<FermiJob>());
+        launch_fermi_sums(s, c->d_fjob.as<FermiJob>(), fermi_part(c));
     }
     CKL();
     FermiOut o;
@@ -1292,7 +1296,7 @@ int nrltb_sums(nrltb_ctx *c, int nv, int nk, const double *eig, const double *de
     RET(c->d_deig.ensure(sizeof(double) * ne));
     RET(c->d_ncut.ensure(sizeof(int) * (size_t)nk));
     RET(c->d_kw.ensure(sizeof(double) * nk));
-    RET(c->d_fout.ensure(sizeof(FermiOut)));
+    RET(c->d_fout.ensure(fermi_out_bytes()));
     RET(c->d_fjob.ensure(sizeof(FermiJob)));
     CK(cudaMemcpyAsync(c->d_eig.p, eig, sizeof(double) * ne, cudaMemcpyHostToDevice, s));
     if (lpress) CK(cudaMemcpyAsync(c->d_deig.p, deig, sizeof(double) * ne, cudaMemcpyHostToDevice, s));
@@ -1312,7 +1316,7 @@ int nrltb_sums(nrltb_ctx *c, int nv, int nk, const double *eig, const double *de
     CK(cudaMemcpyAsync(c->d_fjob.p, &job, sizeof job, cudaMemcpyHostToDevice, s));
     {
         CallScope scope(c);
-        NRLTB_LAUNCH(k_fermi_sums, 1, 1024, 0, s, c->d_fjob.as<FermiJob>());
+        launch_fermi_sums(s, c->d_fjob.as<FermiJob>(), fermi_part(c));
     }
     CKL();
     FermiOut o;

@@ -297,44 +297,59 @@ __global__ void __launch_bounds__(REF_CMAX * REF_CMAX) k_ref_rr(RefineWork w, co
     __syncthreads();
     if (warp != 0) return;
     __syncwarp();
-    if (lane == 0) {
-        // Hermitian by construction up to rounding: symmetrise
-        for (int q = 0; q < c; ++q)
-            for (int r = q; r < c; ++r) {
-                const double2 a = cscale(cadd(A[q][r], cconj(A[r][q])), 0.5), bm = cscale(cadd(Bm[q][r], cconj(Bm[r][q])), 0.5);
-                A[q][r] = a; A[r][q] = cconj(a);
-                Bm[q][r] = bm; Bm[r][q] = cconj(bm);
-            }
-        // Cholesky Bm = L L^H (lower, in place; Bm[q][r] = element (r, q))
-        for (int k = 0; k < c; ++k) {
-            double piv = Bm[k][k].x;
-            for (int q = 0; q < k; ++q) piv -= Bm[q][k].x * Bm[q][k].x + Bm[q][k].y * Bm[q][k].y;
-            piv = sqrt(fmax(piv, 1e-300));
-            Bm[k][k] = make_double2(piv, 0.0);
-            for (int r = k + 1; r < c; ++r) {
-                double2 s2 = Bm[k][r];
-                for (int q = 0; q < k; ++q) s2 = csub(s2, cmul(Bm[q][r], cconj(Bm[q][k])));
-                Bm[k][r] = cscale(s2, 1.0 / piv);
-            }
-        }
-        // A <- L^{-1} A (columns), then A <- A L^{-H} (rows)
-        for (int q = 0; q < c; ++q)
-            for (int r = 0; r < c; ++r) {
-                double2 s2 = A[q][r];
-                for (int t = 0; t < r; ++t) s2 = csub(s2, cmul(Bm[t][r], A[q][t]));
-                A[q][r] = cscale(s2, 1.0 / Bm[r][r].x);
-            }
-        for (int r = 0; r < c; ++r)
-            for (int q = 0; q < c; ++q) {
-                double2 s2 = A[q][r];
-                for (int t = 0; t < q; ++t) s2 = csub(s2, cmul(A[t][r], cconj(Bm[t][q])));
-                A[q][r] = cscale(s2, 1.0 / Bm[q][q].x);
-            }
-        for (int q = 0; q < c; ++q)
-            for (int r = 0; r < c; ++r) Vv[q][r] = make_double2(r == q ? 1.0 : 0.0, 0.0);
+    // Hermitian by construction up to rounding: symmetrise (lanes over entries)
+    for (int e = lane; e < c * c; e += 32) {
+        const int r = e % c, q = e / c;
+        if (r < q) continue;
+        const double2 a = cscale(cadd(A[q][r], cconj(A[r][q])), 0.5), bm = cscale(cadd(Bm[q][r], cconj(Bm[r][q])), 0.5);
+        A[q][r] = a; A[r][q] = cconj(a);
+        Bm[q][r] = bm; Bm[r][q] = cconj(bm);
     }
     __syncwarp();
-    // cyclic complex Jacobi on the Hermitian A, accumulating V
+    // Cholesky Bm = L L^H (lower, in place; Bm[q][r] = element (r, q)),
+    // left-looking: lane r forms element (r, k) of column k
+    for (int k = 0; k < c; ++k) {
+        double2 s2 = make_double2(0, 0);
+        if (lane >= k && lane < c) {
+            s2 = Bm[k][lane];
+            for (int q = 0; q < k; ++q) s2 = csub(s2, cmul(Bm[q][lane], cconj(Bm[q][k])));
+        }
+        if (lane == k) Bm[k][k] = make_double2(sqrt(fmax(s2.x, 1e-300)), 0.0);
+        __syncwarp();
+        if (lane > k && lane < c) Bm[k][lane] = cscale(s2, 1.0 / Bm[k][k].x);
+        __syncwarp();
+    }
+    // A <- L^{-1} A (lane per column), then A <- A L^{-H} (lane per row)
+    if (lane < c) {
+        const int q = lane;
+        for (int r = 0; r < c; ++r) {
+            double2 s2 = A[q][r];
+            for (int t = 0; t < r; ++t) s2 = csub(s2, cmul(Bm[t][r], A[q][t]));
+            A[q][r] = cscale(s2, 1.0 / Bm[r][r].x);
+        }
+    }
+    __syncwarp();
+    if (lane < c) {
+        const int r = lane;
+        for (int q = 0; q < c; ++q) {
+            double2 s2 = A[q][r];
+            for (int t = 0; t < q; ++t) s2 = csub(s2, cmul(A[t][r], cconj(Bm[t][q])));
+            A[q][r] = cscale(s2, 1.0 / Bm[q][q].x);
+        }
+    }
+    for (int e = lane; e < c * c; e += 32) {
+        const int r = e % c, q = e / c;
+        Vv[q][r] = make_double2(r == q ? 1.0 : 0.0, 0.0);
+    }
+    __syncwarp();
+    // parallel complex Jacobi on the Hermitian A, accumulating V: a sweep is
+    // c' - 1 steps of c'/2 disjoint pairs (round-robin: position 0 fixed, the
+    // others rotating; c' = c rounded up to even, pairs with the extra
+    // position skipped).  A step's rotations come from the same A; all their
+    // column rotations (A J, V J) are applied, then all row rotations (J^H A).
+    __shared__ double2 rot[REF_CMAX / 2][2];   // (cs, sn), phase conj(g) / |g| of each pair
+    __shared__ int rpair[REF_CMAX / 2][2];
+    const int ce = c + (c & 1), m = ce - 1, np = ce / 2;
     for (int sweep = 0; sweep < 30; ++sweep) {
         double offd = 0, dsum = 0;
         for (int e = lane; e < c * c; e += 32) {
@@ -345,52 +360,81 @@ __global__ void __launch_bounds__(REF_CMAX * REF_CMAX) k_ref_rr(RefineWork w, co
         offd = warp_sum(offd);
         dsum = warp_sum(dsum);
         if (!(offd > 1e-32 * dsum)) break;
-        for (int pp = 0; pp < c - 1; ++pp)
-            for (int qq = pp + 1; qq < c; ++qq) {
-                __syncwarp();
-                const double2 g = A[qq][pp];            // element (pp, qq)
-                const double ag = sqrt(g.x * g.x + g.y * g.y);
-                if (!(ag > 1e-300)) continue;
-                const double app = A[pp][pp].x, aqq = A[qq][qq].x;
-                const double tau = (aqq - app) / (2.0 * ag);
-                const double t = (tau >= 0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
-                const double cs = 1.0 / sqrt(1.0 + t * t), sn = t * cs;
-                // J = diag(1, e^{-i phi}) [[cs, sn], [-sn, cs]], g = |g| e^{i phi}
-                const double2 phc = make_double2(g.x / ag, -g.y / ag), ph = cconj(phc);
-                __syncwarp();
-                for (int r = lane; r < c; r += 32) {     // A J and V J (columns pp, qq)
-                    const double2 ap = A[pp][r], aq = cmul(A[qq][r], phc);
-                    A[pp][r] = csub(cscale(ap, cs), cscale(aq, sn));
-                    A[qq][r] = cadd(cscale(ap, sn), cscale(aq, cs));
-                    const double2 vp = Vv[pp][r], vq = cmul(Vv[qq][r], phc);
-                    Vv[pp][r] = csub(cscale(vp, cs), cscale(vq, sn));
-                    Vv[qq][r] = cadd(cscale(vp, sn), cscale(vq, cs));
+        for (int st = 0; st < m; ++st) {
+            if (lane < np) {
+                int pa, pb;
+                if (lane == 0) { pa = 0; pb = 1 + st % m; }
+                else { pa = 1 + (st + lane) % m; pb = 1 + (st - lane + m) % m; }
+                const int pp = min(pa, pb), qq = max(pa, pb);
+                int live = qq < c;
+                double2 cssn = make_double2(1.0, 0.0), phc = make_double2(1.0, 0.0);
+                if (live) {
+                    const double2 g = A[qq][pp];            // element (pp, qq)
+                    const double ag = sqrt(g.x * g.x + g.y * g.y);
+                    if (ag > 1e-300) {
+                        const double app = A[pp][pp].x, aqq = A[qq][qq].x;
+                        const double tau = (aqq - app) / (2.0 * ag);
+                        const double t = (tau >= 0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
+                        const double cs = 1.0 / sqrt(1.0 + t * t);
+                        // J = diag(1, e^{-i phi}) [[cs, sn], [-sn, cs]], g = |g| e^{i phi}
+                        cssn = make_double2(cs, t * cs);
+                        phc = make_double2(g.x / ag, -g.y / ag);
+                    } else {
+                        live = 0;
+                    }
                 }
-                __syncwarp();
-                for (int q = lane; q < c; q += 32) {     // J^H A (rows pp, qq)
-                    const double2 ap = A[q][pp], aq = cmul(A[q][qq], ph);
-                    A[q][pp] = csub(cscale(ap, cs), cscale(aq, sn));
-                    A[q][qq] = cadd(cscale(ap, sn), cscale(aq, cs));
-                }
-                __syncwarp();
-                if (lane == 0) {
-                    A[qq][pp] = make_double2(0, 0);
-                    A[pp][qq] = make_double2(0, 0);
-                    A[pp][pp].y = 0;
-                    A[qq][qq].y = 0;
-                }
+                rot[lane][0] = cssn;
+                rot[lane][1] = phc;
+                rpair[lane][0] = pp;
+                rpair[lane][1] = live ? qq : -1;
             }
-        __syncwarp();
+            __syncwarp();
+            // A J and V J: columns pp, qq of every live pair, all rows
+            for (int e = lane; e < np * c; e += 32) {
+                const int pr = e / c, r = e % c, qq = rpair[pr][1];
+                if (qq < 0) continue;
+                const int pp = rpair[pr][0];
+                const double cs = rot[pr][0].x, sn = rot[pr][0].y;
+                const double2 phc = rot[pr][1];
+                const double2 ap = A[pp][r], aq = cmul(A[qq][r], phc);
+                A[pp][r] = csub(cscale(ap, cs), cscale(aq, sn));
+                A[qq][r] = cadd(cscale(ap, sn), cscale(aq, cs));
+                const double2 vp = Vv[pp][r], vq = cmul(Vv[qq][r], phc);
+                Vv[pp][r] = csub(cscale(vp, cs), cscale(vq, sn));
+                Vv[qq][r] = cadd(cscale(vp, sn), cscale(vq, cs));
+            }
+            __syncwarp();
+            // J^H A: rows pp, qq of every live pair, all columns
+            for (int e = lane; e < np * c; e += 32) {
+                const int pr = e / c, q = e % c, qq = rpair[pr][1];
+                if (qq < 0) continue;
+                const int pp = rpair[pr][0];
+                const double cs = rot[pr][0].x, sn = rot[pr][0].y;
+                const double2 ph = cconj(rot[pr][1]);
+                const double2 ap = A[q][pp], aq = cmul(A[q][qq], ph);
+                A[q][pp] = csub(cscale(ap, cs), cscale(aq, sn));
+                A[q][qq] = cadd(cscale(ap, sn), cscale(aq, cs));
+            }
+            __syncwarp();
+            if (lane < np && rpair[lane][1] >= 0) {
+                const int pp = rpair[lane][0], qq = rpair[lane][1];
+                A[qq][pp] = make_double2(0, 0);
+                A[pp][qq] = make_double2(0, 0);
+                A[pp][pp].y = 0;
+                A[qq][qq].y = 0;
+            }
+            __syncwarp();
+        }
     }
     __syncwarp();
-    // eigenvectors of the pencil: x = L^{-H} y
-    if (lane == 0) {
-        for (int q = 0; q < c; ++q)
-            for (int r = c - 1; r >= 0; --r) {
-                double2 s2 = Vv[q][r];
-                for (int t = r + 1; t < c; ++t) s2 = csub(s2, cmul(cconj(Bm[r][t]), Vv[q][t]));
-                Vv[q][r] = cscale(s2, 1.0 / Bm[r][r].x);
-            }
+    // eigenvectors of the pencil: x = L^{-H} y (lane per column)
+    if (lane < c) {
+        const int q = lane;
+        for (int r = c - 1; r >= 0; --r) {
+            double2 s2 = Vv[q][r];
+            for (int t = r + 1; t < c; ++t) s2 = csub(s2, cmul(cconj(Bm[r][t]), Vv[q][t]));
+            Vv[q][r] = cscale(s2, 1.0 / Bm[r][r].x);
+        }
     }
     __syncwarp();
     for (int e = lane; e < c * c; e += 32) {

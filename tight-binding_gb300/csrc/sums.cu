@@ -1,9 +1,10 @@
 // sums.cu -- Fermi level, band energy, pressure (fermi.f, bande.f sums) and the
 // Hellmann-Feynman eigenvalue derivatives (perturb.f).
 //
-// k_fermi_sums: one CTA per structure.  The MPI_ALLREDUCE of every Newton step
-// (fermi.f:365-376) and the final MPI_REDUCEs (bande.f:1255-1331) become block
-// reductions; the iteration itself is the reference's: start at the middle of
+// launch_fermi_sums: k_fermi_level finds E_F in one CTA, k_band_sums and
+// k_band_finish form the sums over the whole GPU.  The MPI_ALLREDUCE of every
+// Newton step (fermi.f:365-376) and the final MPI_REDUCEs (bande.f:1255-1331)
+// become block and grid reductions; the iteration itself is the reference's: start at the middle of
 // the band-nfill / nfill+1 edges, Newton steps clamped to the bracket, bisection
 // when dN/dmu is small, stop when |N - zfill| < tol or the bracket closes.
 // Occupations are exactly 1 below mu - 20 kT and 0 above mu + 20 kT.  With
@@ -83,16 +84,47 @@ __device__ inline double block_max_d(double v, double *sh)
     return r;
 }
 
-__global__ void __launch_bounds__(1024) k_fermi_sums(FermiJob *jobs)
+// number of entries of the ascending row e[0..m) below x
+__device__ __forceinline__ int count_below(const double *e, int m, double x)
+{
+    int lo = 0, hi = m;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (e[mid] < x) lo = mid + 1; else hi = mid;
+    }
+    return lo;
+}
+
+// E_F (fermi.f:162-425).  When every row is ascending (the eigensolver's
+// output always is) the band edges are row ends and each Newton step's
+// occupation needs only the states inside the +-20 kT window: a row's fully
+// occupied states below it are counted by a binary search (their w_k add up
+// to count x w_k), a warp per row takes the window.  Rows that are not
+// ascending (caller eigenvalues) fall back to a scan of every state.
+__global__ void __launch_bounds__(1024) k_fermi_level(FermiJob *jobs)
 {
     __shared__ double sh[64];
+    __shared__ int s_sorted;
     FermiJob J = jobs[blockIdx.x];
-    const int nv = J.nv, nk = J.nk, tid = threadIdx.x, nt = blockDim.x;
+    const int nv = J.nv, nk = J.nk, tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5;
+    const int nwarps = nt >> 5;
     const long tot = (long)nv * nk;
     const double el = J.el, nearz = 1e-5, tkb = J.tkb, zfill = J.zfill, tol = J.tol;
     const double beta = (tkb < nearz) ? 1.0 / nearz : 1.0 / tkb;
     const int nfill = (int)(zfill / el + nearz);
     const bool linst = fabs(zfill / el - (double)nfill) < tol;
+    if (tid == 0) s_sorted = 1;
+    __syncthreads();
+    {
+        int uns = 0;
+        for (long q = tid; q < tot; q += nt) {
+            const int k = (int)(q / nv), i = (int)(q % nv);
+            if (i + 1 < nv && J.eig[(long)k * J.ldk + i + 1] < J.eig[(long)k * J.ldk + i]) uns = 1;
+        }
+        if (__syncthreads_or(uns) && tid == 0) s_sorted = 0;
+        __syncthreads();
+    }
+    const bool sorted = s_sorted != 0;
     // bounds (fermi.f:197-261) from bands nfill and nfill+1; where those lie
     // outside the nv computed bands (nfill >= nv happens with one electron per
     // band) the reference reads past them: here the band indices are clamped
@@ -100,13 +132,23 @@ __global__ void __launch_bounds__(1024) k_fermi_sums(FermiJob *jobs)
     const int ilo = max(min(nfill, nv) - 1, 0), ihi = min(nfill, nv - 1);
     const bool inrange = nfill >= 1 && nfill < nv;
     double stl = -1e308, sth = 1e308, mul = 1e308, muh = -1e308;
-    for (long q = tid; q < tot; q += nt) {
-        const int k = (int)(q / nv), i = (int)(q % nv);
-        const double e = J.eig[(long)k * J.ldk + i];
-        if (i == ilo) stl = fmax(stl, e);
-        if (i == ihi) sth = fmin(sth, e);
-        muh = fmax(muh, e);
-        mul = fmin(mul, e);
+    if (sorted) {
+        for (int k = tid; k < nk; k += nt) {
+            const double *e = J.eig + (long)k * J.ldk;
+            stl = fmax(stl, e[ilo]);
+            sth = fmin(sth, e[ihi]);
+            muh = fmax(muh, e[nv - 1]);
+            mul = fmin(mul, e[0]);
+        }
+    } else {
+        for (long q = tid; q < tot; q += nt) {
+            const int k = (int)(q / nv), i = (int)(q % nv);
+            const double e = J.eig[(long)k * J.ldk + i];
+            if (i == ilo) stl = fmax(stl, e);
+            if (i == ihi) sth = fmin(sth, e);
+            muh = fmax(muh, e);
+            mul = fmin(mul, e);
+        }
     }
     double stlow = block_max_d(stl, sh), sthigh = -block_max_d(-sth, sh);
     double muhigh = block_max_d(muh, sh), mulow = -block_max_d(-mul, sh);
@@ -119,16 +161,31 @@ __global__ void __launch_bounds__(1024) k_fermi_sums(FermiJob *jobs)
         for (it = 1; it <= 10000; ++it) {
             const double mum20 = mu - tkb * 20.0, mup20 = mu + tkb * 20.0, btmu = -beta * mu;
             DD ns, dns;
-            for (long q = tid; q < tot; q += nt) {
-                const int k = (int)(q / nv), i = (int)(q % nv);
-                const double e = J.eig[(long)k * J.ldk + i];
-                const double wk = J.w[k];
-                if (e < mum20) ns.add(wk);
-                else if (e < mup20) {
-                    const double ex = exp(beta * e + btmu);
-                    const double f = 1.0 / (1.0 + ex);
-                    ns.add(wk * f);
-                    dns.add(wk * (ex * f * f));
+            if (sorted) {
+                for (int k = warp; k < nk; k += nwarps) {
+                    const double *e = J.eig + (long)k * J.ldk;
+                    const double wk = J.w[k];
+                    const int lo = count_below(e, nv, mum20), hi = count_below(e, nv, mup20);
+                    if (lane == 0) ns.add(wk * (double)lo);
+                    for (int i = lo + lane; i < hi; i += 32) {
+                        const double ex = exp(beta * e[i] + btmu);
+                        const double f = 1.0 / (1.0 + ex);
+                        ns.add(wk * f);
+                        dns.add(wk * (ex * f * f));
+                    }
+                }
+            } else {
+                for (long q = tid; q < tot; q += nt) {
+                    const int k = (int)(q / nv), i = (int)(q % nv);
+                    const double e = J.eig[(long)k * J.ldk + i];
+                    const double wk = J.w[k];
+                    if (e < mum20) ns.add(wk);
+                    else if (e < mup20) {
+                        const double ex = exp(beta * e + btmu);
+                        const double f = 1.0 / (1.0 + ex);
+                        ns.add(wk * f);
+                        dns.add(wk * (ex * f * f));
+                    }
                 }
             }
             double nsum = el * block_sum_dd(ns, sh);
@@ -146,18 +203,35 @@ __global__ void __launch_bounds__(1024) k_fermi_sums(FermiJob *jobs)
             else break;
         }
     }
-    // energy and pressure sums (bande.f:1162-1330)
+    if (tid == 0) {
+        J.out->efermi = mu;
+        J.out->iterations = it;
+    }
+}
+
+// The sums after E_F (bande.f:1162-1330), spread over the GPU: each CTA
+// forms compensated partial sums over a stride of the states and stores
+// them (hi, lo) in part[blockIdx.x][2 x FERMI_NSUM]; k_band_finish merges the
+// CTAs' partials in CTA order.
+constexpr int FERMI_NSUM = 11;
+__global__ void __launch_bounds__(256) k_band_sums(FermiJob *jobs, double *part)
+{
+    __shared__ double sh[64];
+    FermiJob J = jobs[0];
+    const int nv = J.nv, nk = J.nk, tid = threadIdx.x;
+    const long tot = (long)nv * nk, stride = (long)gridDim.x * blockDim.x;
+    const double tkb = J.tkb, mu = J.out->efermi;
     const double tkbi = (tkb < 1e-5) ? 1e5 : 1.0 / tkb;
     const double efp = mu + 20.0 * tkb, efm = mu - 20.0 * tkb;
-    DD es, d1, d2, d3, dfb, dfe, ent, dn1, dn2, sup, sdn;
-    for (long q = tid; q < tot; q += nt) {
+    DD acc[FERMI_NSUM];   // es, d1, d2, d3, dfb, dfe, ent, dn1, dn2, sup, sdn
+    for (long q = blockIdx.x * (long)blockDim.x + tid; q < tot; q += stride) {
         const int k = (int)(q / nv), i = (int)(q % nv);
         const double e = J.eig[(long)k * J.ldk + i];
         // spin populations over all nv states (bande.f:1336-1395), weight w(k)
         if (J.nks > 0 && e < efp) {
             const double occ = (e < efm) ? J.w[k] : J.w[k] * (1.0 / (1.0 + exp(tkbi * (e - mu))));
-            if (k < J.nks) sup.add(occ);
-            else sdn.add(occ);
+            if (k < J.nks) acc[9].add(occ);
+            else acc[10].add(occ);
         }
         const int lim = J.lpress ? J.ncut[k] : nv;
         if (i >= lim) continue;
@@ -165,62 +239,89 @@ __global__ void __launch_bounds__(1024) k_fermi_sums(FermiJob *jobs)
         const double wt = J.el * J.w[k], ewt = wt * e;
         const double de = J.lpress ? J.deig[(long)k * J.ldk + i] : 0.0;
         if (e < efm) {
-            es.add(ewt);
-            d1.add(wt * de);
+            acc[0].add(ewt);
+            acc[1].add(wt * de);
         } else {
             const double x = e - mu;
             const double fbe = 1.0 / (1.0 + exp(tkbi * x));
-            es.add(ewt * fbe);
+            acc[0].add(ewt * fbe);
             // Gillan entropy of the window states (bande.f:1233-1242, 1313)
-            if (J.lentro) ent.add(-(wt * (fbe * log(fbe) + (1.0 - fbe) * log(1.0 - fbe))));
+            if (J.lentro) acc[6].add(-(wt * (fbe * log(fbe) + (1.0 - fbe) * log(1.0 - fbe))));
             if (J.lpress) {
                 const double dfbe = -tkbi * fbe * (1.0 / (1.0 + exp(tkbi * (-x))));
-                dfb.add(dfbe * wt);
-                d3.add(dfbe * ewt);
+                acc[4].add(dfbe * wt);
+                acc[3].add(dfbe * ewt);
                 const double dewt = wt * de;
-                d1.add(dewt * fbe);
-                dfe.add(dfbe * dewt);
-                d2.add(dfbe * ewt * de);
+                acc[1].add(dewt * fbe);
+                acc[5].add(dfbe * dewt);
+                acc[2].add(dfbe * ewt * de);
                 if (J.lentro) {
                     const double con1 = dfbe * wt * x;
-                    dn1.add(con1 * de);
-                    dn2.add(con1);
+                    acc[7].add(con1 * de);
+                    acc[8].add(con1);
                 }
             }
         }
     }
-    const double es_ = block_sum_dd(es, sh), d1_ = block_sum_dd(d1, sh), d2_ = block_sum_dd(d2, sh);
-    const double d3_ = block_sum_dd(d3, sh), dfb_ = block_sum_dd(dfb, sh), dfe_ = block_sum_dd(dfe, sh);
-    double ent_ = 0, dn1_ = 0, dn2_ = 0, sup_ = 0, sdn_ = 0;
-    if (J.lentro) {
-        ent_ = block_sum_dd(ent, sh);
-        dn1_ = block_sum_dd(dn1, sh);
-        dn2_ = block_sum_dd(dn2, sh);
+    // CTA-wide merge of each pair (fixed tree order), then one store per sum
+#pragma unroll
+    for (int s = 0; s < FERMI_NSUM; ++s) {
+        DD v = acc[s];
+        for (int o = 16; o > 0; o >>= 1) {
+            const double h = __shfl_xor_sync(0xffffffffu, v.hi, o), l = __shfl_xor_sync(0xffffffffu, v.lo, o);
+            v.merge(h, l);
+        }
+        const int lane = tid & 31, wid = tid >> 5, nw = blockDim.x >> 5;
+        __syncthreads();
+        if (lane == 0) { sh[wid] = v.hi; sh[32 + wid] = v.lo; }
+        __syncthreads();
+        if (tid == 0) {
+            DD t;
+            for (int q2 = 0; q2 < nw; ++q2) t.merge(sh[q2], sh[32 + q2]);
+            part[(long)blockIdx.x * 2 * FERMI_NSUM + 2 * s] = t.hi;
+            part[(long)blockIdx.x * 2 * FERMI_NSUM + 2 * s + 1] = t.lo;
+        }
     }
-    if (J.nks > 0) {
-        sup_ = block_sum_dd(sup, sh);
-        sdn_ = block_sum_dd(sdn, sh);
+}
+
+__global__ void k_band_finish(FermiJob *jobs, const double *part, int nblk)
+{
+    FermiJob J = jobs[0];
+    const int s = threadIdx.x;
+    __shared__ double tot[FERMI_NSUM];
+    if (s < FERMI_NSUM) {
+        DD t;
+        for (int b = 0; b < nblk; ++b) t.merge(part[(long)b * 2 * FERMI_NSUM + 2 * s], part[(long)b * 2 * FERMI_NSUM + 2 * s + 1]);
+        tot[s] = t.hi + t.lo;
     }
-    if (tid == 0) {
-        FermiOut o;
-        o.efermi = mu;
-        o.e_total = es_;
+    __syncthreads();
+    if (s == 0) {
+        FermiOut o = *J.out;
+        o.e_total = tot[0];
         o.fermi_shift = 0;
         o.pressure = 0;
         if (J.lpress) {
-            const double dfermi = (fabs(dfb_) > 1e-10) ? dfe_ / dfb_ : 0.0;
+            const double dfermi = (fabs(tot[4]) > 1e-10) ? tot[5] / tot[4] : 0.0;
             o.fermi_shift = dfermi;
-            o.pressure = -(d1_ + (d2_ - dfermi * d3_));
+            o.pressure = -(tot[1] + (tot[2] - dfermi * tot[3]));
         }
-        o.entropy = ent_;
-        o.dent1 = dn1_;
-        o.dent2 = dn2_;
-        o.spin_up = sup_;
-        o.spin_dn = sdn_;
-        o.iterations = it;
+        o.entropy = J.lentro ? tot[6] : 0.0;
+        o.dent1 = J.lentro ? tot[7] : 0.0;
+        o.dent2 = J.lentro ? tot[8] : 0.0;
+        o.spin_up = J.nks > 0 ? tot[9] : 0.0;
+        o.spin_dn = J.nks > 0 ? tot[10] : 0.0;
         o.pad = 0;
-        J.out[0] = o;
+        *J.out = o;
     }
+}
+
+size_t fermi_part_bytes() { return sizeof(double) * 2 * FERMI_NSUM * FERMI_BLOCKS; }
+
+void launch_fermi_sums(cudaStream_t s, FermiJob *djob, double *part)
+{
+    NRLTB_LAUNCH(k_fermi_level, 1, 1024, 0, s, djob);
+    NRLTB_LAUNCH(k_band_sums, FERMI_BLOCKS, 256, 0, s, djob, part);
+    NRLTB_LAUNCH(k_band_finish, 1, 32, 0, s, djob, part, FERMI_BLOCKS);
 }
 
 // One thread per (k, state, atom).  Z: batch column-major n2 x n2 eigenvectors

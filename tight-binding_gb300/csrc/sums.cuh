@@ -24,7 +24,12 @@ struct FermiJob {
     FermiOut *out;
 };
 
-__global__ void k_fermi_sums(FermiJob *jobs);
+// E_F, then the energy / pressure / entropy / spin sums: three launches on s
+// (one CTA for the Newton iteration, FERMI_BLOCKS CTAs for the sums, one to
+// merge them); part holds fermi_part_bytes() of device scratch.
+constexpr int FERMI_BLOCKS = 152;
+size_t fermi_part_bytes();
+void launch_fermi_sums(cudaStream_t s, FermiJob *djob, double *part);
 // non-collinear spin directions (diag.f:458-524, bande.f:1480-1537): per k,
 // state and atom the spin vector of the up and down halves of the
 // eigenvector; then its occupied-state sum per atom and component
