@@ -115,6 +115,40 @@ def test_mixed_bande_fcc128_full_mesh(ctx):
     assert g.eig.shape == (27, 1152)
 
 
+def test_mixed_batch_matches_single_calls_and_oracle(ctx):
+    """The structure batch in the mixed form: nrltb_bande_batch over uneven
+    structures (spd and sp3, 4-64 atoms) returns what one nrltb_bande call per
+    structure returns, bit for bit, and the smallest members agree with the
+    oracle within the mixed form's tolerances."""
+    from nrltb.api import new_result, result_from_c
+    items = synth.batch256(count=10)
+    opts = [Opts(mode=4, precision=MIXED, tkb=o["tkb"], eigcut=1e3, fermi_tol=1e-11) for (_, _, _, o) in items]
+    single = [ctx.bande(st, par, km, op) for (st, par, km, _), op in zip(items, opts)]
+    n = len(items)
+    cs = (abi.Structure_ * n)(*[it[0].to_c() for it in items])
+    cp = (abi.Params_ * n)(*[it[1].to_c() for it in items])
+    ck = (abi.KMesh_ * n)(*[it[2].to_c() for it in items])
+    co = (abi.Opts_ * n)(*[op.to_c() for op in opts])
+    made = [new_result(it[1].nv(it[0]), it[2].nk) for it in items]
+    cr = (abi.Result_ * n)(*[m[0] for m in made])
+    assert ctx.lib.nrltb_bande_batch(ctx.h, n, cs, cp, ck, co, cr) == 0, ctx.lib.nrltb_last_error()
+    for i in range(n):
+        b = result_from_c(cr[i], made[i][1])
+        a = single[i]
+        assert b.efermi == a.efermi and b.e_total == a.e_total and b.pressure == a.pressure
+        assert np.array_equal(b.eig, a.eig) and np.array_equal(b.deig, a.deig)
+    by_cost = sorted(range(n), key=lambda i: items[i][1].nv(items[i][0]) ** 3 * items[i][2].nk)
+    for i in by_cost[:4]:
+        st, par, km, o = items[i]
+        ref = oracle.bande(st, par, km, Opts(mode=4, tkb=o["tkb"], eigcut=1e3, fermi_tol=1e-11))
+        g = single[i]
+        assert (g.k_status == 0).all()
+        assert np.abs(g.eig - ref.eig).max() <= 1e-9
+        assert abs(g.efermi - ref.efermi) <= 1e-9
+        assert abs(g.e_total - ref.e_total) / st.natoms <= 1e-8
+        assert abs(g.pressure - ref.pressure) <= P_TOL
+
+
 def test_mixed_bande_ex1_against_skout(ctx, ex1, ex1_gold):
     for idx in (0, 9):
         _, _, st, km = ex1.structures[idx]
