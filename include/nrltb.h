@@ -178,10 +178,11 @@ int nrltb_bande(nrltb_ctx *ctx, const nrltb_structure *st, const nrltb_params *p
                 const nrltb_kmesh *km, const nrltb_opts *opt, nrltb_result *res);
 
 /* Many structures of uneven size in one call (the MPI k split becomes a batch).
- * Structures are processed concurrently by up to 4 host worker threads, each
+ * Structures are processed concurrently by up to 8 host worker threads, each
  * with its own context and stream created on first use (kept until the
- * context is destroyed); each result equals what nrltb_bande returns for that
- * structure alone.  On error the first failing structure's message is kept. */
+ * context is destroyed), largest structures first; each result equals what
+ * nrltb_bande returns for that structure alone.  On error the first failing
+ * structure's message is kept. */
 int nrltb_bande_batch(nrltb_ctx *ctx, int nstruct, const nrltb_structure *st,
                       const nrltb_params *par, const nrltb_kmesh *km,
                       const nrltb_opts *opt, nrltb_result *res);

@@ -74,6 +74,12 @@ CASES = [
     (256, 256, 200, 0, 0, 0, 2, 1),
     (257, 100, 161, 0, 0, 1, 0, 0),
     (129, 65, 1, 0, 0, 0, 0, 0),
+    # long K (8 or more 32-deep slices): the two-stage tcgen05 form, odd and even
+    # slice counts, triangles that cut some tiles' slices to one or none
+    (300, 130, 520, 0, 1, 0, 0, 0),
+    (200, 150, 450, 0, 0, 2, 0, 0),
+    (256, 192, 512, 0, 0, 0, 1, 0),
+    (130, 300, 257, 0, 0, 1, 0, 2),
     # rank-32 / 64 updates with op(B) = B^H (Cholesky and tridiagonal trailing updates)
     (300, 300, 64, 0, 1, 0, 0, 1),
     (256, 200, 32, 0, 1, 0, 0, 0),

@@ -1059,10 +1059,29 @@ int nrltb_bande(nrltb_ctx *c, const nrltb_structure *st, const nrltb_params *par
 
 // Structures are independent: BATCH_WORKERS host threads, each with its own
 // context (workspace) and stream, take structures from a shared counter, so
-// the GPU overlaps the small structures' launch-latency-bound solves.  Each
-// structure's result is the one nrltb_bande gives for it alone (every kernel
-// works per matrix and the k sums have a fixed order).
-constexpr int BATCH_WORKERS = 4;
+// the GPU overlaps the small structures' launch-latency-bound solves.  The
+// counter walks the structures largest first (estimated work: order^3 x k
+// points x spin channels), so that the last structures to start are small
+// ones and no worker finishes a large solve long after the others are idle.
+// Each structure's result is the one nrltb_bande gives for it alone (every
+// kernel works per matrix and the k sums have a fixed order).
+constexpr int BATCH_WORKERS = 8;
+
+// work estimate of one structure for the batch order (0 if its input is
+// malformed: nrltb_bande reports the error when the structure's turn comes)
+static double batch_work(const nrltb_structure &st, const nrltb_params &par, const nrltb_kmesh &km)
+{
+    if (st.natoms <= 0 || !st.kkind || !par.kbas || par.kinds <= 0 || km.nk <= 0) return 0.0;
+    double nv = 0.0;
+    for (int i = 0; i < st.natoms; ++i) {
+        const int k = st.kkind[i];
+        if (k < 1 || k > par.kinds) return 0.0;
+        nv += par.kbas[k - 1];
+    }
+    if (st.spinat) nv *= 2.0;
+    const double nsp = (!st.spinat && par.jspins == 2) ? 2.0 : 1.0;
+    return nv * nv * nv * km.nk * nsp;
+}
 
 int nrltb_bande_batch(nrltb_ctx *c, int nstruct, const nrltb_structure *st, const nrltb_params *par,
                       const nrltb_kmesh *km, const nrltb_opts *opt, nrltb_result *res)
@@ -1080,6 +1099,15 @@ int nrltb_bande_batch(nrltb_ctx *c, int nstruct, const nrltb_structure *st, cons
         RET(nrltb_ctx_create(&w, c->device));
         c->workers.push_back(w);
     }
+    std::vector<int> order(nstruct);
+    {
+        std::vector<double> work(nstruct);
+        for (int i = 0; i < nstruct; ++i) {
+            order[i] = i;
+            work[i] = batch_work(st[i], par[i], km[i]);
+        }
+        std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return work[x] > work[y]; });
+    }
     std::atomic<int> next(0), failed(0);
     std::mutex mu;
     int first_rc = NRLTB_OK;
@@ -1089,8 +1117,9 @@ int nrltb_bande_batch(nrltb_ctx *c, int nstruct, const nrltb_structure *st, cons
     auto body = [&](int wi) {
         nrltb_ctx *wc = c->workers[wi];
         for (;;) {
-            const int i = next.fetch_add(1);
-            if (i >= nstruct || failed.load()) return;
+            const int t = next.fetch_add(1);
+            if (t >= nstruct || failed.load()) return;
+            const int i = order[t];
             const int rc = nrltb_bande(wc, st + i, par + i, km + i, opt + i, res + i);
             if (rc != NRLTB_OK) {
                 std::lock_guard<std::mutex> g(mu);
