@@ -54,6 +54,63 @@ template <typename C> __device__ __forceinline__ void cfmac(C &acc, C a, C b)
     acc.y = fma(-a.y, b.x, acc.y);
 }
 
+// FP32 -> FP64 (exact) from the bit pattern with integer operations: the same
+// value as the hardware conversion, which GB300 runs on its narrow FP64 pipe.
+__device__ __forceinline__ double f2d_exact(float f)
+{
+    const unsigned u = __float_as_uint(f);
+    const unsigned long long sign = (unsigned long long)(u >> 31) << 63;
+    const unsigned E = (u >> 23) & 0xFFu, m = u & 0x7FFFFFu;
+    unsigned long long bits;
+    if (E == 0) {
+        if (m == 0) return __longlong_as_double((long long)sign);
+        const int p = 31 - __clz(m);   // subnormal: m 2^-149 = 1.f 2^(p - 149)
+        bits = ((unsigned long long)(p + 874) << 52) | (((unsigned long long)m << (52 - p)) & 0xFFFFFFFFFFFFFull);
+    } else if (E == 0xFFu) {
+        bits = (0x7FFull << 52) | ((unsigned long long)m << 29);
+    } else {
+        bits = ((unsigned long long)(E + 896) << 52) | ((unsigned long long)m << 29);
+    }
+    return __longlong_as_double((long long)(bits | sign));
+}
+
+// FP64 -> FP32 rounded to nearest even, from the bit pattern with integer
+// operations: the same value as the hardware conversion (overflow to
+// infinity, subnormal results, NaN kept a NaN).
+__device__ __forceinline__ float d2f_rn(double x)
+{
+    const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
+    const unsigned sign = (unsigned)(bits >> 63) << 31;
+    const int E = (int)((bits >> 52) & 0x7FF);
+    const unsigned long long m = bits & 0xFFFFFFFFFFFFFull;
+    unsigned f;
+    if (E == 0x7FF) {
+        f = m ? (0x7FC00000u | (unsigned)(m >> 29)) : 0x7F800000u;
+    } else if (E == 0) {
+        f = 0;   // below 2^-1022: rounds to zero
+    } else {
+        const int e = E - 1023;
+        if (e > 127) {
+            f = 0x7F800000u;
+        } else if (e >= -126) {
+            f = ((unsigned)(e + 127) << 23) | (unsigned)(m >> 29);
+            const unsigned long long rem = m & ((1ull << 29) - 1), half = 1ull << 28;
+            if (rem > half || (rem == half && (f & 1u))) f += 1;   // a carry moves into the exponent
+        } else {
+            const unsigned long long M = m | (1ull << 52);
+            const int s = -(e + 97);   // subnormal result: M 2^-s units of 2^-149, s > 29
+            if (s > 60) {
+                f = 0;
+            } else {
+                const unsigned long long k = M >> s, rem = M & ((1ull << s) - 1), half = 1ull << (s - 1);
+                f = (unsigned)k;
+                if (rem > half || (rem == half && (k & 1ull))) f += 1;
+            }
+        }
+    }
+    return __uint_as_float(f | sign);
+}
+
 template <typename T> __device__ __forceinline__ T warp_sum(T v)
 {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);

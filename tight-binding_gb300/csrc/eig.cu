@@ -64,7 +64,13 @@ __global__ void k_convert_h(const double2 *__restrict__ src, C2 *__restrict__ ds
     for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < count; i += (long)gridDim.x * blockDim.x) {
         double2 v = src[i];
         C2 o;
-        o.x = v.x; o.y = v.y;
+        if constexpr (sizeof(o.x) == 4) {   // rounded with integer operations, off the FP64 pipe
+            o.x = d2f_rn(v.x);
+            o.y = d2f_rn(v.y);
+        } else {
+            o.x = v.x;
+            o.y = v.y;
+        }
         dst[i] = o;
     }
 }
@@ -424,6 +430,52 @@ template <> __device__ inline double tiny_of<double>() { return DBL_MIN; }
 __device__ inline float tri_div(float a, float b) { return __fdividef(a, b); }
 __device__ inline double tri_div(double a, double b) { return a / b; }
 
+// Bounds of an unreduced block [b0, b1] of T: Gershgorin interval [lo, hi],
+// max row sum tnorm and max e^2.  When every valid thread of the CTA is in
+// the same block (the usual case: one block per matrix) the CTA computes them
+// together, each thread a strided part, then min / max over the CTA (exact in
+// any order, so the values equal the one-thread loop's); otherwise each
+// thread loops over its own block.  Every thread of the CTA must call it.
+__device__ void block_bounds(const double *d, const double *e, bool valid, int b0, int b1, double &lo, double &hi,
+                             double &tnorm, double &emax2)
+{
+    __shared__ int sblk[2];
+    __shared__ double sred[4][32];
+    if (threadIdx.x == 0) { sblk[0] = b0; sblk[1] = b1; }
+    __syncthreads();
+    const int c0 = sblk[0], c1 = sblk[1];
+    const bool all = __syncthreads_and(!valid || (b0 == c0 && b1 == c1));
+    auto part = [&](int k0, int k1, int step, int kb0, int kb1) {
+        for (int k = k0; k <= k1; k += step) {
+            const double off = (k > kb0 ? fabs(e[k - 1]) : 0.0) + (k < kb1 ? fabs(e[k]) : 0.0);
+            lo = fmin(lo, d[k] - off);
+            hi = fmax(hi, d[k] + off);
+            tnorm = fmax(tnorm, fabs(d[k]) + off);
+            if (k < kb1) emax2 = fmax(emax2, e[k] * e[k]);
+        }
+    };
+    if (!all) {
+        if (valid) part(b0, b1, 1, b0, b1);
+        return;
+    }
+    part(c0 + (int)threadIdx.x, c1, (int)blockDim.x, c0, c1);
+    for (int o = 16; o > 0; o >>= 1) {
+        lo = fmin(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+        hi = fmax(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+        tnorm = fmax(tnorm, __shfl_xor_sync(0xffffffffu, tnorm, o));
+        emax2 = fmax(emax2, __shfl_xor_sync(0xffffffffu, emax2, o));
+    }
+    const int wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    if ((threadIdx.x & 31) == 0) { sred[0][wid] = lo; sred[1][wid] = hi; sred[2][wid] = tnorm; sred[3][wid] = emax2; }
+    __syncthreads();
+    for (int q = 0; q < nw; ++q) {
+        lo = fmin(lo, sred[0][q]);
+        hi = fmax(hi, sred[1][q]);
+        tnorm = fmax(tnorm, sred[2][q]);
+        emax2 = fmax(emax2, sred[3][q]);
+    }
+}
+
 // One thread per (matrix, row r): eigenvalue number r - b0 of r's block.
 // FP32: the matrix's d and e^2 in FP32 and the split flags of find_block are
 // staged once per CTA in shared memory (2 n floats + n bytes of dynamic shared
@@ -440,40 +492,44 @@ __global__ void k_tri_bisect(const double *dd, const double *ee, double *lamloc,
     unsigned char *ssp = (unsigned char *)(bis_s + 2 * n);
     if (sizeof(TB) == 4) {
         for (int k = threadIdx.x; k < n; k += blockDim.x) {
-            sd[k] = (float)d[k];
-            const float ek = (float)e[k];
+            sd[k] = d2f_rn(d[k]);
+            const float ek = d2f_rn(e[k]);
             se2[k] = ek * ek;
             // find_block's split test, once per row
             ssp[k] = k < n - 1 && fabs(d[k] * d[k + 1]) * DBL_EPSILON * DBL_EPSILON + DBL_MIN >= e[k] * e[k];
         }
         __syncthreads();
     }
-    if (r >= n) return;
-    int b0, b1;
-    if (sizeof(TB) == 4) find_block_flags(ssp, n, r, b0, b1);
-    else find_block(d, e, n, r, b0, b1);
-    double tnorm = 0, lo = 1e300, hi = -1e300, emax2 = 0;
-    for (int k = b0; k <= b1; ++k) {
-        double off = (k > b0 ? fabs(e[k - 1]) : 0.0) + (k < b1 ? fabs(e[k]) : 0.0);
-        lo = fmin(lo, d[k] - off);
-        hi = fmax(hi, d[k] + off);
-        tnorm = fmax(tnorm, fabs(d[k]) + off);
-        if (k < b1) emax2 = fmax(emax2, e[k] * e[k]);
+    const bool valid = r < n;
+    int b0 = 0, b1 = -1;
+    if (valid) {
+        if (sizeof(TB) == 4) find_block_flags(ssp, n, r, b0, b1);
+        else find_block(d, e, n, r, b0, b1);
     }
+    double tnorm = 0, lo = 1e300, hi = -1e300, emax2 = 0;
+    block_bounds(d, e, valid, b0, b1, lo, hi, tnorm, emax2);
+    if (!valid) return;
     const TB eps = eps_of<TB>();
     const TB pivmin = tiny_of<TB>() * TB(fmax(1.0, emax2));
     const TB atol = eps * TB(tnorm);
     const int j = r - b0;
     TB a = TB(lo) - TB(2) * atol - pivmin, z = TB(hi) + TB(2) * atol + pivmin;
-    // Sturm count: eigenvalues of the block below x
+    // Sturm count: eigenvalues of the block below x (FP32: from the shared
+    // copies, the same values as converting d and e here)
     auto count = [&](TB x) {
         int cnt = 0;
-        TB q = TB(d[b0]) - x;
+        TB q = (sizeof(TB) == 4 ? TB(sd[b0]) : TB(d[b0])) - x;
         if (fabs(q) < pivmin) q = -pivmin;
         cnt += (q < TB(0));
         for (int k = b0 + 1; k <= b1; ++k) {
-            const TB ek = TB(e[k - 1]);
-            q = TB(d[k]) - x - ek * ek / q;
+            TB e2;
+            if (sizeof(TB) == 4) {
+                e2 = TB(se2[k - 1]);
+            } else {
+                const TB ek = TB(e[k - 1]);
+                e2 = ek * ek;
+            }
+            q = (sizeof(TB) == 4 ? TB(sd[k]) : TB(d[k])) - x - e2 / q;
             if (fabs(q) < pivmin) q = -pivmin;
             cnt += (q < TB(0));
         }
@@ -600,13 +656,33 @@ __global__ void k_tri_invit(const double *dd, const double *ee, const double *la
 {
     const int b = blockIdx.y;
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= n) return;
+    const bool valid = r < n;
     const double *d = dd + (long)b * n, *e = ee + (long)b * n, *L = lamloc + (long)b * n;
-    const int b0 = blk[((long)b * n + r) * 2], b1 = blk[((long)b * n + r) * 2 + 1];
+    const int b0 = valid ? blk[((long)b * n + r) * 2] : 0, b1 = valid ? blk[((long)b * n + r) * 2 + 1] : -1;
     const int len = b1 - b0 + 1;
+    // the block's max row sum: by the whole CTA when its threads share one
+    // block (max is exact in any order), else per thread
     double tnorm = 0;
-    for (int k = b0; k <= b1; ++k)
-        tnorm = fmax(tnorm, fabs(d[k]) + (k > b0 ? fabs(e[k - 1]) : 0.0) + (k < b1 ? fabs(e[k]) : 0.0));
+    {
+        __shared__ int iblk[2];
+        __shared__ double ired[32];
+        if (threadIdx.x == 0) { iblk[0] = b0; iblk[1] = b1; }
+        __syncthreads();
+        const int c0 = iblk[0], c1 = iblk[1];
+        const bool all = __syncthreads_and(!valid || (b0 == c0 && b1 == c1));
+        const int k0 = all ? c0 + (int)threadIdx.x : b0, step = all ? (int)blockDim.x : 1;
+        if (all || valid)
+            for (int k = k0; k <= (all ? c1 : b1); k += step)
+                tnorm = fmax(tnorm, fabs(d[k]) + (k > (all ? c0 : b0) ? fabs(e[k - 1]) : 0.0) +
+                                        (k < (all ? c1 : b1) ? fabs(e[k]) : 0.0));
+        if (all) {
+            for (int o = 16; o > 0; o >>= 1) tnorm = fmax(tnorm, __shfl_xor_sync(0xffffffffu, tnorm, o));
+            if ((threadIdx.x & 31) == 0) ired[threadIdx.x >> 5] = tnorm;
+            __syncthreads();
+            for (int q = 0; q < (int)((blockDim.x + 31) >> 5); ++q) tnorm = fmax(tnorm, ired[q]);
+        }
+    }
+    if (!valid) return;
     const long NT = (long)gridDim.y * gridDim.x * blockDim.x;
     Strided<TB> S(scratch + ((long)blockIdx.y * gridDim.x + blockIdx.x) * blockDim.x + threadIdx.x, NT);
     // 1 / pivots, first and second super-diagonals of U, iterate
@@ -759,7 +835,9 @@ __global__ void k_real_to_cplx(const double *y, C2 *z, long count)
 {
     for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < count; i += (long)gridDim.x * blockDim.x) {
         C2 o;
-        o.x = y[i]; o.y = 0;
+        if constexpr (sizeof(o.x) == 4) o.x = d2f_rn(y[i]);
+        else o.x = y[i];
+        o.y = 0;
         z[i] = o;
     }
 }

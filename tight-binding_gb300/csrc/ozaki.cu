@@ -80,6 +80,12 @@ size_t ozaki_work_bytes(int n, int batch)
 __device__ unsigned g_oz_fault;
 
 // column exponents: e_j = smallest e with |M_kj| < 2^e for all k (re and im)
+// (from the largest |M_kj| rounded to FP32, with a margin for that rounding).
+// FP64 M: the largest magnitude is found on the bit patterns (for finite
+// non-negative doubles the integer order of the bits is the numeric order) and
+// rounded to FP32 once per column, which gives the same value as rounding
+// every element first (rounding is monotonic) without a conversion on the
+// FP64 pipe per element.
 template <typename C2>
 __global__ void k_oz_colexp(const C2 *M, int n, int np, int *ex, int batch)
 {
@@ -87,14 +93,29 @@ __global__ void k_oz_colexp(const C2 *M, int n, int np, int *ex, int batch)
     if (warp >= np * batch) return;
     const int b = warp / np, j = warp % np;
     float mx = 0.f;
-    if (j < n) {
-        const C2 *col = M + (long)b * n * n + (long)j * n;
-        for (int k = lane; k < n; k += 32) {
-            const C2 v = col[k];
-            mx = fmaxf(mx, fmaxf(fabsf((float)v.x), fabsf((float)v.y)));
+    if constexpr (sizeof(M->x) == 8) {
+        unsigned long long mb = 0;
+        if (j < n) {
+            const C2 *col = M + (long)b * n * n + (long)j * n;
+            for (int k = lane; k < n; k += 32) {
+                const C2 v = col[k];
+                const unsigned long long ar = (unsigned long long)__double_as_longlong(v.x) & 0x7FFFFFFFFFFFFFFFull;
+                const unsigned long long ai = (unsigned long long)__double_as_longlong(v.y) & 0x7FFFFFFFFFFFFFFFull;
+                mb = max(mb, max(ar, ai));
+            }
         }
+        for (int o = 16; o > 0; o >>= 1) mb = max(mb, (unsigned long long)__shfl_xor_sync(0xffffffffu, (long long)mb, o));
+        mx = (float)__longlong_as_double((long long)mb);
+    } else {
+        if (j < n) {
+            const C2 *col = M + (long)b * n * n + (long)j * n;
+            for (int k = lane; k < n; k += 32) {
+                const C2 v = col[k];
+                mx = fmaxf(mx, fmaxf(fabsf(v.x), fabsf(v.y)));
+            }
+        }
+        for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
     }
-    for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
     if (lane == 0) {
         int e;
         if (mx > 0.f) { frexpf(mx * 1.0000001f, &e); } else e = 0;   // |v| < 2^e (float max rounded up)
@@ -105,6 +126,30 @@ __global__ void k_oz_colexp(const C2 *M, int n, int np, int *ex, int batch)
 // 2^k for -1022 <= k <= 1023, exact
 __device__ __forceinline__ double pow2d(int k) { return __longlong_as_double((long long)(1023 + k) << 52); }
 __device__ __forceinline__ float pow2f(int k) { return __int_as_float((127 + k) << 23); }
+
+// rint(v 2^p) (round half to even) on the bit pattern of v, with integer
+// operations only: the same integer as rounding the exactly scaled double,
+// for |v 2^p| < 2^62 (no FP64-pipe multiply or conversion).
+__device__ __forceinline__ long long oz_scaled_rint(double v, int p)
+{
+    const unsigned long long bits = (unsigned long long)__double_as_longlong(v);
+    const int E = (int)((bits >> 52) & 0x7FF);
+    unsigned long long m = bits & 0xFFFFFFFFFFFFFull;
+    if (E != 0) m |= 1ull << 52;
+    if (m == 0) return 0;
+    const int sh = (E == 0 ? 1 : E) - 1075 + p;   // |v| 2^p = m 2^sh
+    unsigned long long u;
+    if (sh >= 0) {
+        u = m << sh;
+    } else if (sh < -62) {
+        u = 0;   // m 2^sh < 2^-9
+    } else {
+        const int r = -sh;
+        const unsigned long long q = m >> r, rem = m & ((1ull << r) - 1), half = 1ull << (r - 1);
+        u = q + ((rem > half || (rem == half && (q & 1ull))) ? 1ull : 0ull);
+    }
+    return (bits >> 63) ? -(long long)u : (long long)u;
+}
 
 // Balanced base-256 digits of an integer U (|U| <= 2^(8 nd - 1)), lowest first
 // in d[nd-1]: every digit in [-128, 127] except the top one, which is in
@@ -142,7 +187,8 @@ __device__ __forceinline__ uint4 oz_pack8(const float d[8])
 // A digits.  Thread: row i, 8 consecutive k.  A is Hermitian: A_ik = conj(A_ki)
 // is read down column i (coalesced).  U = rint(A_ik 2^(8 SA - 1 - e_i))
 // (|U| <= 2^(8 SA - 1), one rounding at 2^-(8 SA) of 2^(e_i+1)) is cut into SA
-// digits.  Layout: blocks [b][i / 128][k / 64][s] of 32 KB = [Ar_s | Ai_s],
+// digits; U is formed from the bits of A_ik with integer operations, since
+// GB300's FP64 pipe would bound this kernel otherwise.  Layout: blocks [b][i / 128][k / 64][s] of 32 KB = [Ar_s | Ai_s],
 // 128 rows each.
 template <int SA>
 __global__ void k_oz_digits_a(const double2 *A, int n, int np, const int *ex, unsigned char *D, int batch)
@@ -153,7 +199,7 @@ __global__ void k_oz_digits_a(const double2 *A, int n, int np, const int *ex, un
     const int b = (int)(t / ((long)np * kg8));
     const long e = t - (long)b * np * kg8;
     const int i = (int)(e / kg8), kq = (int)(e % kg8), k0 = 8 * kq;
-    const double sc = pow2d(8 * SA - 1 - ex[(long)b * np + i]);
+    const int p = 8 * SA - 1 - ex[(long)b * np + i];
     float dr[SA][8], di[SA][8];
 #pragma unroll
     for (int u = 0; u < 8; ++u) {
@@ -164,8 +210,8 @@ __global__ void k_oz_digits_a(const double2 *A, int n, int np, const int *ex, un
             v.y = -v.y;
         }
         float xr[SA], xi[SA];
-        digits_of<SA>(__double2ll_rn(v.x * sc), xr);
-        digits_of<SA>(__double2ll_rn(v.y * sc), xi);
+        digits_of<SA>(oz_scaled_rint(v.x, p), xr);
+        digits_of<SA>(oz_scaled_rint(v.y, p), xi);
 #pragma unroll
         for (int q = 0; q < SA; ++q) { dr[q][u] = xr[q]; di[q][u] = xi[q]; }
     }

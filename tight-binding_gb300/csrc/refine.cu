@@ -91,8 +91,9 @@ __global__ void k_ref_diag(RefineWork w, const float2 *X)
     for (int i = lane; i < n; i += 32) {
         const float2 x = X[off + i];
         const double2 yh = w.YH[off + i], ys = w.YS[off + i];
-        t += (double)x.x * yh.x + (double)x.y * yh.y;
-        r += (double)x.x * ys.x + (double)x.y * ys.y;
+        const double xr = f2d_exact(x.x), xi = f2d_exact(x.y);   // widened off the FP64 pipe
+        t += xr * yh.x + xi * yh.y;
+        r += xr * ys.x + xi * ys.y;
     }
     t = warp_sum(t);
     r = warp_sum(r);
@@ -264,7 +265,8 @@ __global__ void __launch_bounds__(REF_CMAX * REF_CMAX) k_ref_rr(RefineWork w, co
     // rows; the products of the FP32 x with the FP64 H x, S x are formed
     // exactly on the FP32 pipe (the FP64 factor split into two floats, the
     // leading product's rounding error recovered by an FMA) and summed in
-    // double-float (Knuth's two-sum): ~2^-46 relative, without the FP64 pipe.
+    // double-float (Knuth's two-sum): ~2^-46 relative; the FP64 pipe takes
+    // only the split's exact remainder.
     const int ne = c * (c + 1) / 2, nwarps = blockDim.x >> 5;
     for (int e = warp; e < ne; e += nwarps) {
         int q = 0, rem = e;
@@ -276,9 +278,11 @@ __global__ void __launch_bounds__(REF_CMAX * REF_CMAX) k_ref_rr(RefineWork w, co
         for (int i = lane; i < n; i += 32) {
             const float2 x = xr[i];
             const double2 h = hq[i], sv = sq[i];
-            const float2 hh = make_float2((float)h.x, (float)h.y), sh = make_float2((float)sv.x, (float)sv.y);
-            const float2 hl = make_float2((float)(h.x - (double)hh.x), (float)(h.y - (double)hh.y));
-            const float2 sl = make_float2((float)(sv.x - (double)sh.x), (float)(sv.y - (double)sh.y));
+            // (conversions with integer operations: only the exact remainders
+            // take the FP64 pipe)
+            const float2 hh = make_float2(d2f_rn(h.x), d2f_rn(h.y)), sh = make_float2(d2f_rn(sv.x), d2f_rn(sv.y));
+            const float2 hl = make_float2(d2f_rn(h.x - f2d_exact(hh.x)), d2f_rn(h.y - f2d_exact(hh.y)));
+            const float2 sl = make_float2(d2f_rn(sv.x - f2d_exact(sh.x)), d2f_rn(sv.y - f2d_exact(sh.y)));
             // conj(x) y = (xr yr + xi yi) + i (xr yi - xi yr)
             tre.add_prod(x.x, hh.x, hl.x); tre.add_prod(x.y, hh.y, hl.y);
             tim.add_prod(x.x, hh.y, hl.y); tim.add_prod(-x.y, hh.x, hl.x);
@@ -470,9 +474,13 @@ __global__ void k_ref_rotres(RefineWork w, const float2 *X)
     const long mo = b * nn;
     const double l = w.lam[(long)b * n + j];
     double2 v, res;
+    float2 xr;
     if (csz[j] == 1) {
-        const float2 x = X[mo + r + (long)j * n];
-        v = make_double2(x.x, x.y);
+        // the FP32 vector itself: widened with integer operations (exact) and
+        // kept as it is for the FP32 copy, so that only the residual uses the
+        // FP64 pipe
+        xr = X[mo + r + (long)j * n];
+        v = make_double2(f2d_exact(xr.x), f2d_exact(xr.y));
         const double2 yh = w.YH[t], ys = w.YS[t];
         res = make_double2(yh.x - l * ys.x, yh.y - l * ys.y);
     } else {
@@ -482,15 +490,16 @@ __global__ void k_ref_rotres(RefineWork w, const float2 *X)
             const long src = mo + r + (long)ord[pos0[j] + a] * n;
             const double2 u = U[(long)j * REF_CMAX + a];
             const float2 x = X[src];
-            v = cadd(v, cmul(make_double2(x.x, x.y), u));
+            v = cadd(v, cmul(make_double2(f2d_exact(x.x), f2d_exact(x.y)), u));
             h = cadd(h, cmul(w.YH[src], u));
             sx = cadd(sx, cmul(w.YS[src], u));
         }
         res = make_double2(h.x - l * sx.x, h.y - l * sx.y);
+        xr = make_float2(d2f_rn(v.x), d2f_rn(v.y));
     }
     w.Xd[t] = v;
-    w.Xr[t] = make_float2((float)v.x, (float)v.y);
-    w.Ef[t] = make_float2((float)res.x, (float)res.y);
+    w.Xr[t] = xr;
+    w.Ef[t] = make_float2(d2f_rn(res.x), d2f_rn(res.y));
 }
 
 // 4. E column j and the second-order eigenvalue term (warp per column), from
@@ -640,7 +649,7 @@ __global__ void k_ref_finish(RefineWork w, double2 *Z)
     const int dst = w.cl[(long)3 * n * w.batch + (long)b * n + j];
     const double2 x = w.Xd[t];
     const float2 d = w.XE[t];
-    Z[b * nn + r + (long)dst * n] = make_double2(x.x + (double)d.x, x.y + (double)d.y);
+    Z[b * nn + r + (long)dst * n] = make_double2(x.x + f2d_exact(d.x), x.y + f2d_exact(d.y));
 }
 
 void refine_eigen(cudaStream_t s, RefineWork &w, const double2 *H, const double2 *S, float2 *X,
@@ -696,7 +705,7 @@ __global__ void k_to_f32(const double2 *src, float2 *dst, long count)
 {
     for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < count; i += (long)gridDim.x * blockDim.x) {
         const double2 v = src[i];
-        dst[i] = make_float2((float)v.x, (float)v.y);
+        dst[i] = make_float2(d2f_rn(v.x), d2f_rn(v.y));
     }
 }
 void launch_to_f32(cudaStream_t s, const double2 *src, float2 *dst, long count)
