@@ -847,31 +847,42 @@ __global__ void k_real_to_cplx(const double *y, C2 *z, long count)
 // T[0:c, c] = -tau_c T[0:c, 0:c] G[0:c, c], T[c, c] = tau_c (LAPACK's larft,
 // forward columnwise).  One CTA of EIG_WY threads per matrix, thread = row;
 // T is built in shared memory when it fits (FP32: 128 x 129 complex = 132 KB,
-// dynamic), else in global memory.
+// dynamic), else in global memory.  The columns of G (and the taus) come in
+// groups of LARFT_GC through shared memory, one global round trip per group
+// rather than per column.
+constexpr int LARFT_GC = 8;
 template <typename T, bool SMEM>
 __global__ void __launch_bounds__(EIG_WY) k_larft_wy(const typename cplx<T>::t *G, typename cplx<T>::t *Tm,
                                                      const typename cplx<T>::t *tau, int n, int j0, int jb, int nbw)
 {
     typedef typename cplx<T>::t C2;
-    __shared__ C2 g[EIG_WY];
+    __shared__ C2 g[LARFT_GC][EIG_WY];
+    __shared__ C2 tg[LARFT_GC];
     extern __shared__ __align__(16) unsigned char larft_smem[];
     const int b = blockIdx.x, r = threadIdx.x;
     const C2 *Gb = G + (long)b * nbw * nbw;
     C2 *Tb = Tm + (long)b * nbw * nbw;
     const int lt = SMEM ? EIG_WY + 1 : nbw;   // column stride of the working T
     C2 *Tw = SMEM ? (C2 *)larft_smem : Tb;
-    for (int c = 0; c < jb; ++c) {
-        if (r < c) g[r] = Gb[r + (long)c * nbw];
+    for (int c0 = 0; c0 < jb; c0 += LARFT_GC) {
+        const int cn = min(LARFT_GC, jb - c0);
+        __syncthreads();   // the previous group's columns are consumed
+        for (int q = 0; q < cn; ++q)
+            if (r < c0 + q) g[q][r] = Gb[r + (long)(c0 + q) * nbw];
+        if (r < cn) tg[r] = tau[(long)b * n + j0 + c0 + r];
         __syncthreads();
-        const C2 tc = tau[(long)b * n + j0 + c];
-        if (r < c) {
-            C2 acc = cmk<T>(0, 0);
-            for (int k = r; k < c; ++k) cfma(acc, Tw[r + (long)k * lt], g[k]);
-            Tw[r + (long)c * lt] = cscale(cmul(tc, acc), T(-1));
-        } else if (r == c) {
-            Tw[c + (long)c * lt] = tc;
+        for (int q = 0; q < cn; ++q) {
+            const int c = c0 + q;
+            const C2 tc = tg[q];
+            if (r < c) {
+                C2 acc = cmk<T>(0, 0);
+                for (int k = r; k < c; ++k) cfma(acc, Tw[r + (long)k * lt], g[q][k]);
+                Tw[r + (long)c * lt] = cscale(cmul(tc, acc), T(-1));
+            } else if (r == c) {
+                Tw[c + (long)c * lt] = tc;
+            }
+            __syncthreads();
         }
-        __syncthreads();
     }
     if (SMEM)
         for (int c = 0; c < jb; ++c)

@@ -544,7 +544,8 @@ static int run_bloch(nrltb_ctx *c, int k0, int nk, int which0, double2 *M1, doub
     if (c->npairs > 0)
         NRLTB_LAUNCH(k_phases, cdiv((long)c->npairs * nk, 256), 256, 0, s, DS, pr, c->npairs,
                      c->d_kq.as<double>() + 3 * (long)k0, nk, c->d_ph.as<double2>());
-    NRLTB_LAUNCH(k_bloch_build, cdiv((long)nv * nv, 256), 256, 0, s, DS, DP, pr, c->npairs, sk, c->d_seg.as<int2>(),
+    const long tiles = cdiv(nv, 32);
+    NRLTB_LAUNCH(k_bloch_build, tiles * (tiles + 1) / 2, 256, 0, s, DS, DP, pr, c->npairs, sk, c->d_seg.as<int2>(),
                  c->d_orb.as<int>(), c->d_ksk.as<int>(), c->d_ph.as<double2>(), nk, nv, which0, M1, M2, S.jsover);
     CKL();
     return NRLTB_OK;

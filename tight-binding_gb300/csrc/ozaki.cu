@@ -127,6 +127,17 @@ __global__ void k_oz_colexp(const C2 *M, int n, int np, int *ex, int batch)
 __device__ __forceinline__ double pow2d(int k) { return __longlong_as_double((long long)(1023 + k) << 52); }
 __device__ __forceinline__ float pow2f(int k) { return __int_as_float((127 + k) << 23); }
 
+// v 2^k, exact: on the exponent field when the result stays a normal number
+// (integer operations), else by the FP64 multiply
+__device__ __forceinline__ double oz_scale2(double v, int k)
+{
+    const long long bits = __double_as_longlong(v);
+    const int E = (int)((bits >> 52) & 0x7FF);
+    if ((bits & 0x7FFFFFFFFFFFFFFFll) == 0) return v;
+    if (E == 0 || E + k <= 0 || E + k >= 0x7FF) return v * pow2d(k);
+    return __longlong_as_double(bits + ((long long)k << 52));
+}
+
 // rint(v 2^p) (round half to even) on the bit pattern of v, with integer
 // operations only: the same integer as rounding the exactly scaled double,
 // for |v 2^p| < 2^62 (no FP64-pipe multiply or conversion).
@@ -542,9 +553,11 @@ k_oz_gemm(const unsigned char *DA, const unsigned char *DX, const int *exA, cons
                 for (int c = 0; c < 16; ++c) {
                     const int j = jt * OZ_NX + 16 * h + c;
                     if (j >= n) break;
-                    const double sc = pow2d(ei + exX[(long)b * np + j] + 2);   // exact power of two
-                    yb[(long)j * n] = make_double2(((double)hr[c] + (double)lr[c]) * sc,
-                                                   ((double)hi[c] + (double)li[c]) * sc);
+                    // widening and the power-of-two scale with integer operations:
+                    // only the double-float sum takes the FP64 pipe
+                    const int k2 = ei + exX[(long)b * np + j] + 2;
+                    yb[(long)j * n] = make_double2(oz_scale2(f2d_exact(hr[c]) + f2d_exact(lr[c]), k2),
+                                                   oz_scale2(f2d_exact(hi[c]) + f2d_exact(li[c]), k2));
                 }
             }
         }

@@ -529,52 +529,109 @@ __global__ void k_phases(DevStructure S, DevPairs pr, int npairs, const double *
     ph[(long)kk * npairs + p] = make_double2(cs, sn);
 }
 
-// Dense Hermitian matrices for a chunk of k points.  One thread per (row, column)
-// element; `which0` selects H/S (0) or dH/dS (2).  Column-major, leading dim nv.
-__global__ void __launch_bounds__(256)
-k_bloch_build(DevStructure S, DevParams P, DevPairs pr, int npairs, DevSK sk, const int2 *seg,
-              const int *orb_atom, const int *ksk, const double2 *ph, int nk, int nv, int which0,
-              double2 *M1, double2 *M2, int jsover)
+// Dense Hermitian matrices for a chunk of k points; `which0` selects H/S (0) or
+// dH/dS (2).  Column-major, leading dimension nv.  One CTA per pair of 32 x 32
+// tiles (R, C), R <= C: thread (row tr, column tc) forms elements (32 R + tr,
+// 32 C + tc + 8 q), q < 4.  Element (r, c) is the sum over the images of its
+// atom pair taken in the reference's upper storage (min-atom row, max-atom
+// column) and conjugated when (r, c) is the lower one, so the two elements of
+// a mirrored pair are conjugates of one sum: off the diagonal tiles each sum is
+// formed once and its conjugate written to (c, r) through a shared-memory
+// transpose (coalesced both ways), halving the FP64 work; diagonal tiles form
+// every element.  The values are those of one thread per element.
+__device__ __forceinline__ void bloch_elem(const DevStructure &S, const DevSK &sk, int npairs, const int2 *seg,
+                                           const int *orb_atom, const int *ksk, int r, int c, int which0,
+                                           int &a1, int &a2, int &oi, int &oj, bool &conjg, int2 &sg, double &on1,
+                                           double &on2)
 {
-    const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
-    if (t >= (long)nv * nv) return;
-    const int r = (int)(t % nv), c = (int)(t / nv);
     const int ar = orb_atom[r], ac = orb_atom[c];
     const int i = r - ksk[ar], j = c - ksk[ac];
     // element (r, c): upper storage of the reference is (min-atom row, max-atom col)
-    int a1, a2, oi, oj;
-    bool conjg;
     if (ar < ac || (ar == ac && i <= j)) { a1 = ar; a2 = ac; oi = i; oj = j; conjg = false; }
     else { a1 = ac; a2 = ar; oi = j; oj = i; conjg = true; }
-    const int2 sg = seg[(long)a1 * S.natoms + a2];
-    const double *E1 = sk.E + (long)which0 * npairs * 81;
-    const double *E2 = sk.E + (long)(which0 + 1) * npairs * 81;
-    double on1 = 0.0, on2 = 0.0;
+    sg = seg[(long)a1 * S.natoms + a2];
+    on1 = 0.0;
+    on2 = 0.0;
     if (r == c) {
         const int cls = (i == 0) ? 0 : (i <= 3) ? 1 : (i <= 6) ? 2 : 3;
         on1 = (which0 == 0 ? sk.paros : sk.dparos)[4 * (long)ar + cls];
         on2 = (which0 == 0) ? 1.0 : 0.0;
     }
+}
+
+__global__ void __launch_bounds__(256)
+k_bloch_build(DevStructure S, DevParams P, DevPairs pr, int npairs, DevSK sk, const int2 *seg,
+              const int *orb_atom, const int *ksk, const double2 *ph, int nk, int nv, int which0,
+              double2 *M1, double2 *M2, int jsover)
+{
+    __shared__ double2 t1[32][33], t2[32][33];   // [row in R][column in C]
+    // tile pair of this CTA: blockIdx.x = C (C + 1) / 2 + R
+    const int u = blockIdx.x;
+    int C = (int)((sqrtf(8.f * u + 1.f) - 1.f) * 0.5f);
+    while ((C + 1) * (C + 2) / 2 <= u) ++C;
+    while (C * (C + 1) / 2 > u) --C;
+    const int R = u - C * (C + 1) / 2;
+    const bool diag = R == C;
+    const int tr = threadIdx.x & 31, tc = threadIdx.x >> 5;
+    const int r = 32 * R + tr;
+    const double *E1 = sk.E + (long)which0 * npairs * 81;
+    const double *E2 = sk.E + (long)(which0 + 1) * npairs * 81;
+    int a1[4], a2[4], oi[4], oj[4];
+    bool conjg[4], ok[4];
+    int2 sg[4];
+    double on1[4], on2[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int c = 32 * C + tc + 8 * q;
+        ok[q] = r < nv && c < nv;
+        if (ok[q]) bloch_elem(S, sk, npairs, seg, orb_atom, ksk, r, c, which0, a1[q], a2[q], oi[q], oj[q], conjg[q],
+                              sg[q], on1[q], on2[q]);
+    }
     for (int kk = 0; kk < nk; ++kk) {
-        double h_re = 0, h_im = 0, s_re = 0, s_im = 0;
-        for (int p = sg.x; p < sg.y; ++p) {
-            const double2 z = ph[(long)kk * npairs + p];
-            const double e1 = E1[(long)p * 81 + oi * 9 + oj];
-            h_re += e1 * z.x;
-            h_im += e1 * z.y;
-            if (jsover) {
-                const double e2 = E2[(long)p * 81 + oi * 9 + oj];
-                s_re += e2 * z.x;
-                s_im += e2 * z.y;
+        const double2 *phk = ph + (long)kk * npairs;
+        double2 *m1 = M1 + (long)kk * nv * nv, *m2 = M2 + (long)kk * nv * nv;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            if (!ok[q]) continue;
+            const int c = 32 * C + tc + 8 * q;
+            double h_re = 0, h_im = 0, s_re = 0, s_im = 0;
+            for (int p = sg[q].x; p < sg[q].y; ++p) {
+                const double2 z = phk[p];
+                const double e1 = E1[(long)p * 81 + oi[q] * 9 + oj[q]];
+                h_re += e1 * z.x;
+                h_im += e1 * z.y;
+                if (jsover) {
+                    const double e2 = E2[(long)p * 81 + oi[q] * 9 + oj[q]];
+                    s_re += e2 * z.x;
+                    s_im += e2 * z.y;
+                }
+            }
+            h_re += on1[q];
+            if (jsover) s_re += on2[q];
+            else s_re = (r == c && which0 == 0) ? 1.0 : 0.0;
+            if (conjg[q]) { h_im = -h_im; s_im = -s_im; }
+            const long off = r + (long)c * nv;
+            m1[off] = make_double2(h_re, h_im);
+            m2[off] = make_double2(s_re, s_im);
+            if (!diag) {
+                t1[tr][tc + 8 * q] = make_double2(h_re, -h_im);
+                t2[tr][tc + 8 * q] = make_double2(s_re, -s_im);
             }
         }
-        h_re += on1;
-        if (jsover) s_re += on2;
-        else s_re = (r == c && which0 == 0) ? 1.0 : 0.0;
-        if (conjg) { h_im = -h_im; s_im = -s_im; }
-        const long off = (long)kk * nv * nv + r + (long)c * nv;
-        M1[off] = make_double2(h_re, h_im);
-        M2[off] = make_double2(s_re, s_im);
+        if (!diag) {
+            // (c, r) = conj (r, c): rows 32 C + tr, columns 32 R + tc + 8 q
+            __syncthreads();
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int rr = 32 * C + tr, cc = 32 * R + tc + 8 * q;
+                if (rr < nv && cc < nv) {
+                    const long off = rr + (long)cc * nv;
+                    m1[off] = t1[tc + 8 * q][tr];
+                    m2[off] = t2[tc + 8 * q][tr];
+                }
+            }
+            __syncthreads();
+        }
     }
 }
 
