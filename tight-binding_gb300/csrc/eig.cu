@@ -116,7 +116,18 @@ __global__ void __launch_bounds__(256) k_potrf_diag(EigWork<T> w, int j0, int jb
         x[c][c] = cmk<T>(T(1) / a[c][c].x, T(0));
         for (int r = c + 1; r < jb; ++r) {
             C2 s = cmk<T>(0, 0);
-            for (int k = c; k < r; ++k) s = cadd(s, cmul(a[k][r], x[c][k]));
+            int k = c;
+            for (; k + 8 <= r; k += 8) {
+                C2 av[8], xv[8];
+#pragma unroll
+                for (int u = 0; u < 8; ++u) {
+                    av[u] = a[k + u][r];
+                    xv[u] = x[c][k + u];
+                }
+#pragma unroll
+                for (int u = 0; u < 8; ++u) s = cadd(s, cmul(av[u], xv[u]));
+            }
+            for (; k < r; ++k) s = cadd(s, cmul(a[k][r], x[c][k]));
             x[c][r] = cscale(s, -T(1) / a[r][r].x);
         }
     }
@@ -610,11 +621,22 @@ __global__ void k_tri_rank(const double *lamloc, int *rank, double *lam, int n)
     lam[(long)b * n + cnt] = v;
 }
 
-__device__ inline double hash_unit(unsigned a, unsigned b)
+__device__ inline unsigned hash_bits(unsigned a, unsigned b)
 {
     unsigned h = a * 0x9E3779B1u ^ (b + 0x7F4A7C15u) * 0x85EBCA77u;
     h ^= h >> 15; h *= 0x2C1B3C6Du; h ^= h >> 12; h *= 0x297A2D39u; h ^= h >> 15;
-    return (double)(h & 0xFFFFFF) / (double)0x800000 - 1.0;   // [-1, 1)
+    return h & 0xFFFFFFu;
+}
+// m 2^-23 - 1 in [-1, 1) for a 24-bit m: exact in FP32 as in FP64, so the FP32
+// form gives the same values without the FP64 pipe
+template <typename TB> __device__ inline TB hash_unit(unsigned a, unsigned b);
+template <> __device__ inline double hash_unit<double>(unsigned a, unsigned b)
+{
+    return (double)hash_bits(a, b) / (double)0x800000 - 1.0;
+}
+template <> __device__ inline float hash_unit<float>(unsigned a, unsigned b)
+{
+    return (float)hash_bits(a, b) * (1.0f / 8388608.0f) - 1.0f;
 }
 
 // An array of one thread whose elements are `st` apart (thread-interleaved
@@ -682,6 +704,19 @@ __global__ void k_tri_invit(const double *dd, const double *ee, const double *la
             for (int q = 0; q < (int)((blockDim.x + 31) >> 5); ++q) tnorm = fmax(tnorm, ired[q]);
         }
     }
+    // FP32: the matrix's d and e rounded once per CTA into shared memory (the
+    // same values as converting at each step, without the FP64 pipe)
+    extern __shared__ float invit_s[];
+    const float *sdf = invit_s, *sef = invit_s + n;
+    if (sizeof(TB) == 4) {
+        for (int k = threadIdx.x; k < n; k += blockDim.x) {
+            invit_s[k] = d2f_rn(d[k]);
+            invit_s[n + k] = d2f_rn(e[k]);
+        }
+        __syncthreads();
+    }
+    auto Dk = [&](int k) { return sizeof(TB) == 4 ? TB(sdf[k]) : TB(d[k]); };
+    auto Ek = [&](int k) { return sizeof(TB) == 4 ? TB(sef[k]) : TB(e[k]); };
     if (!valid) return;
     const long NT = (long)gridDim.y * gridDim.x * blockDim.x;
     Strided<TB> S(scratch + ((long)blockIdx.y * gridDim.x + blockIdx.x) * blockDim.x + threadIdx.x, NT);
@@ -701,8 +736,8 @@ __global__ void k_tri_invit(const double *dd, const double *ee, const double *la
         // forward: factor (dgttrf) and apply P, L; element k + 1 of the
         // right-hand side is the previous iterate scaled by inv (the random
         // start in the first iteration)
-        auto rhs = [&](int k) { return it == 0 ? TB(hash_unit(seed, (unsigned)k)) : v[k] * inv; };
-        TB dcur = TB(d[b0]) - lam, ducur = (len > 1) ? TB(e[b0]) : TB(0);
+        auto rhs = [&](int k) { return it == 0 ? hash_unit<TB>(seed, (unsigned)k) : v[k] * inv; };
+        TB dcur = Dk(b0) - lam, ducur = (len > 1) ? Ek(b0) : TB(0);
         TB vc = rhs(0);
         for (int kb = 0; kb < len - 1; kb += INV_BLK) {
             TB vn[INV_BLK];
@@ -713,9 +748,9 @@ __global__ void k_tri_invit(const double *dd, const double *ee, const double *la
             for (int u = 0; u < INV_BLK; ++u) {
                 const int k = kb + u;
                 if (k >= len - 1) break;
-                const TB dlk = TB(e[b0 + k]);
-                TB dnext = TB(d[b0 + k + 1]) - lam;
-                TB dunext = (k < len - 2) ? TB(e[b0 + k + 1]) : TB(0);
+                const TB dlk = Ek(b0 + k);
+                TB dnext = Dk(b0 + k + 1) - lam;
+                TB dunext = (k < len - 2) ? Ek(b0 + k + 1) : TB(0);
                 if (fabs(dcur) >= fabs(dlk)) {
                     const TB f = (dcur != TB(0)) ? tri_div(dlk, dcur) : TB(0);
                     if (it == 0) { RG[k] = tri_div(TB(1), pivot(dcur)); DU[k] = ducur; DU2[k] = TB(0); }
@@ -766,9 +801,19 @@ __global__ void k_tri_invit(const double *dd, const double *ee, const double *la
     }
     // sign convention: largest component positive
     (void)kmax;
-    const double sg = (vkmax < TB(0)) ? -1.0 : 1.0;
+    // (widening and the sign with integer operations: the same values as
+    // sg * (double) x, off the FP64 pipe)
+    const long long sgbit = (vkmax < TB(0)) ? (long long)0x8000000000000000ull : 0ll;
     double *z = yvec + (long)b * n * n + (long)rank[(long)b * n + r] * n;
-    for (int k = 0; k < n; ++k) z[k] = (k >= b0 && k <= b1) ? sg * (double)(v[k - b0] * inv) : 0.0;
+    for (int k = 0; k < n; ++k) {
+        double x = 0.0;
+        if (k >= b0 && k <= b1) {
+            if constexpr (sizeof(TB) == 4) x = f2d_exact(v[k - b0] * inv);
+            else x = (double)(v[k - b0] * inv);
+            x = __longlong_as_double(__double_as_longlong(x) ^ sgbit);
+        }
+        z[k] = x;
+    }
 }
 
 // Orthonormalise each cluster of eigenvalues closer than ctol ||T|| (within
@@ -847,9 +892,12 @@ __global__ void k_real_to_cplx(const double *y, C2 *z, long count)
 // T[0:c, c] = -tau_c T[0:c, 0:c] G[0:c, c], T[c, c] = tau_c (LAPACK's larft,
 // forward columnwise).  One CTA of EIG_WY threads per matrix, thread = row;
 // T is built in shared memory when it fits (FP32: 128 x 129 complex = 132 KB,
-// dynamic), else in global memory.  The columns of G (and the taus) come in
-// groups of LARFT_GC through shared memory, one global round trip per group
-// rather than per column.
+// dynamic), else in global memory.  Row r of T depends only on row r and on
+// G, so the threads need no barrier between columns: the columns of G (and
+// the taus) come in groups of LARFT_GC through shared memory, with a barrier
+// per group.  The lanes of a warp walk k together from the warp's first row,
+// so that their reads of T are consecutive and G[k, c] is one broadcast; row r
+// adds its terms k >= r in order of k (the one-row-at-a-time sums).
 constexpr int LARFT_GC = 8;
 template <typename T, bool SMEM>
 __global__ void __launch_bounds__(EIG_WY) k_larft_wy(const typename cplx<T>::t *G, typename cplx<T>::t *Tm,
@@ -859,14 +907,14 @@ __global__ void __launch_bounds__(EIG_WY) k_larft_wy(const typename cplx<T>::t *
     __shared__ C2 g[LARFT_GC][EIG_WY];
     __shared__ C2 tg[LARFT_GC];
     extern __shared__ __align__(16) unsigned char larft_smem[];
-    const int b = blockIdx.x, r = threadIdx.x;
+    const int b = blockIdx.x, r = threadIdx.x, kw = r & ~31;
     const C2 *Gb = G + (long)b * nbw * nbw;
     C2 *Tb = Tm + (long)b * nbw * nbw;
     const int lt = SMEM ? EIG_WY + 1 : nbw;   // column stride of the working T
     C2 *Tw = SMEM ? (C2 *)larft_smem : Tb;
     for (int c0 = 0; c0 < jb; c0 += LARFT_GC) {
         const int cn = min(LARFT_GC, jb - c0);
-        __syncthreads();   // the previous group's columns are consumed
+        __syncthreads();   // every thread is done with the previous group's columns
         for (int q = 0; q < cn; ++q)
             if (r < c0 + q) g[q][r] = Gb[r + (long)(c0 + q) * nbw];
         if (r < cn) tg[r] = tau[(long)b * n + j0 + c0 + r];
@@ -874,16 +922,28 @@ __global__ void __launch_bounds__(EIG_WY) k_larft_wy(const typename cplx<T>::t *
         for (int q = 0; q < cn; ++q) {
             const int c = c0 + q;
             const C2 tc = tg[q];
-            if (r < c) {
+            if (kw < c) {   // warp-uniform
                 C2 acc = cmk<T>(0, 0);
-                for (int k = r; k < c; ++k) cfma(acc, Tw[r + (long)k * lt], g[q][k]);
-                Tw[r + (long)c * lt] = cscale(cmul(tc, acc), T(-1));
-            } else if (r == c) {
-                Tw[c + (long)c * lt] = tc;
+                int k = kw;
+                for (; k + 8 <= c; k += 8) {
+                    C2 tv[8], gv[8];
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) {
+                        tv[u] = Tw[r + (k + u) * lt];
+                        gv[u] = g[q][k + u];
+                    }
+#pragma unroll
+                    for (int u = 0; u < 8; ++u)
+                        if (k + u >= r) cfma(acc, tv[u], gv[u]);
+                }
+                for (; k < c; ++k)
+                    if (k >= r) cfma(acc, Tw[r + k * lt], g[q][k]);
+                if (r < c) Tw[r + (long)c * lt] = cscale(cmul(tc, acc), T(-1));
             }
-            __syncthreads();
+            if (r == c) Tw[c + (long)c * lt] = tc;
         }
     }
+    __syncthreads();
     if (SMEM)
         for (int c = 0; c < jb; ++c)
             if (r <= c) Tb[r + (long)c * nbw] = Tw[r + (long)c * lt];
@@ -1073,7 +1133,10 @@ void eig_solve(cudaStream_t s, EigWork<T> &w, const double2 *H, const double2 *S
         // overlap is ~ eps ||T|| / gap <= 1e-11 for FP64)
         const double ctol = 1e-5;
         // 64 threads per CTA: cdiv(n, 64) * 64 * B thread slots <= the scratch carve's 64 cdiv(n, 64) n B
-        NRLTB_LAUNCH(k_tri_invit<T>, dim3(cdiv(n, 64), B), 64, 0, s, w.d, w.e, lamloc, blk, rank, w.yvec,
+        const size_t ism = sizeof(T) == 4 ? 2 * sizeof(float) * n : 0;
+        if (ism > 48 * 1024)
+            cudaFuncSetAttribute(k_tri_invit<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ism);
+        NRLTB_LAUNCH(k_tri_invit<T>, dim3(cdiv(n, 64), B), 64, ism, s, w.d, w.e, lamloc, blk, rank, w.yvec,
                      (T *)w.ylu, n);
         NRLTB_LAUNCH(k_tri_cluster_orth, dim3(cdiv(n, 8), B), 256, 0, s, w.d, w.e, lamloc, blk, rank, w.yvec, n,
                      ctol);

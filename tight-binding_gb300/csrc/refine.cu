@@ -534,7 +534,7 @@ __global__ void k_ref_update(RefineWork w, const float2 *Gt)
             e = make_float2(0.f, 0.f);
         } else {
             const float2 g = Gj[i], gt = Gtj[i];
-            const float rden = 1.f / (float)(lj - l1[i]);
+            const float rden = 1.f / d2f_rn(lj - l1[i]);   // FP64 gap, rounded off the FP64 pipe
             e = make_float2(g.x * rden, g.y * rden);
             // E_ji = G'_ji / (l_i - l_j) = -conj(Gt_ij) rden
             const float2 c = make_float2(-gt.x * rden, gt.y * rden);
