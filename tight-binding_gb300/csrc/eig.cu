@@ -1023,7 +1023,7 @@ __global__ void k_fill_int(int *p, int v, int count)
 // ---------------------------------------------------------------------------
 template <typename T>
 void eig_solve(cudaStream_t s, EigWork<T> &w, const double2 *H, const double2 *S, double *eig,
-               typename cplx<T>::t *X, bool vectors)
+               typename cplx<T>::t *X, bool vectors, cudaEvent_t tri_start)
 {
     typedef typename cplx<T>::t C2;
     const int n = w.n, B = w.batch;
@@ -1076,6 +1076,7 @@ void eig_solve(cudaStream_t s, EigWork<T> &w, const double2 *H, const double2 *S
         zgemm<T>(s, n, n, n, B, one, w.A, ld, ms, 0, w.Wi, ld, ms, 1, zero, w.Y, ld, ms, 0, 1, 0);
     }
     zgemm<T>(s, n, n, n, B, one, w.Wi, ld, ms, 0, w.Y, ld, ms, 0, zero, w.A, ld, ms, 1, 0, 1);
+    if (tri_start) cudaEventRecord(tri_start, s);
     // 4. tridiagonalisation: one cluster launch per panel (tri_panel.cuh); the
     //    per-column launch chain below is the path for devices or sizes where
     //    such a cluster cannot be scheduled
@@ -1189,8 +1190,8 @@ template size_t eig_work_bytes<float>(int, int);
 template void eig_work_carve<double>(EigWork<double> &, void *, int, int);
 template void eig_work_carve<float>(EigWork<float> &, void *, int, int);
 template void eig_solve<double>(cudaStream_t, EigWork<double> &, const double2 *, const double2 *, double *,
-                                double2 *, bool);
+                                double2 *, bool, cudaEvent_t);
 template void eig_solve<float>(cudaStream_t, EigWork<float> &, const double2 *, const double2 *, double *,
-                               float2 *, bool);
+                               float2 *, bool, cudaEvent_t);
 
 }  // namespace nrltb

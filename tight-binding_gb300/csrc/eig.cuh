@@ -66,9 +66,11 @@ template <typename T> void eig_work_carve(EigWork<T> &w, void *base, int n, int 
 
 // Full solve.  H and S (FP64, column-major, leading dimension n, stride n*n)
 // are converted to T inside.  eig: n per matrix; X (optional, precision T):
-// S-orthonormal eigenvectors, column-major, stride n*n.
+// S-orthonormal eigenvectors, column-major, stride n*n.  tri_start (optional)
+// is recorded on s when the tridiagonalisation begins (its latency-bound
+// panels leave most of the GPU to work on other streams).
 template <typename T>
 void eig_solve(cudaStream_t s, EigWork<T> &w, const double2 *H, const double2 *S,
-               double *eig, typename cplx<T>::t *X, bool vectors);
+               double *eig, typename cplx<T>::t *X, bool vectors, cudaEvent_t tri_start = nullptr);
 
 }  // namespace nrltb

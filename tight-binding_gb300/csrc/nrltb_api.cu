@@ -13,6 +13,7 @@
 #include <string>
 #include <vector>
 #include <algorithm>
+#include <functional>
 #include <atomic>
 #include <mutex>
 #include <new>
@@ -103,6 +104,10 @@ struct Staged {
 struct nrltb_ctx {
     int device = 0;
     cudaStream_t own = nullptr, stream = nullptr;
+    // mixed form: the digits of H, S, dH, dS (and the dH, dS Bloch sums) are
+    // made on `side` while the FP32 eigensolve runs on `stream`
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_in = nullptr, ev_side = nullptr;
     long long launches = 0;
     KTimer *kt = nullptr;   // kernel-class timing (measurement hooks)
     std::vector<nrltb_ctx *> workers;   // nrltb_bande_batch: one context and stream per host worker
@@ -119,6 +124,7 @@ struct nrltb_ctx {
     DBuf d_sk, d_seg, d_ph;
     // k-chunk matrices and solver
     DBuf d_H, d_S, d_X, d_work, d_ref, d_hf, d_np, d_qw;
+    DBuf d_dH, d_dS, d_ph2, d_oa;   // side stream: dH, dS, their phases, the prepared digits
     std::vector<std::pair<int, int>> nonpd;   // (k, chunk) of k points whose S is not positive definite
     // results
     DBuf d_eig, d_deig, d_ncut, d_status, d_fjob, d_fout, d_orbq, d_spev, d_spdir;
@@ -530,25 +536,30 @@ static int run_skblocks(nrltb_ctx *c, int nwhich)
 }
 
 // dense matrices of k points [k0, k0+nk) into H, S (which0 0: H/S, 2: dH/dS)
-static int run_bloch(nrltb_ctx *c, int k0, int nk, int which0, double2 *M1, double2 *M2)
+static int run_bloch_on(nrltb_ctx *c, cudaStream_t s, DBuf &phb, int k0, int nk, int which0, double2 *M1,
+                        double2 *M2)
 {
     NvtxRange nv_(which0 ? "Bloch sums dH dS" : "Bloch sums H S");
-    cudaStream_t s = c->stream;
     const Staged &S = c->st;
     const int P = std::max(c->npairs, 1), nv = S.nv;
-    RET(c->d_ph.ensure(sizeof(double2) * (size_t)P * nk));
+    RET(phb.ensure(sizeof(double2) * (size_t)P * nk));
     DevSK sk = sk_view(c, P, S.natoms, S.kinds);
     DevPairs pr = pairs_view(c, P);
     DevStructure DS = dev_structure(c);
     DevParams DP = dev_params(c);
     if (c->npairs > 0)
         NRLTB_LAUNCH(k_phases, cdiv((long)c->npairs * nk, 256), 256, 0, s, DS, pr, c->npairs,
-                     c->d_kq.as<double>() + 3 * (long)k0, nk, c->d_ph.as<double2>());
+                     c->d_kq.as<double>() + 3 * (long)k0, nk, phb.as<double2>());
     const long tiles = cdiv(nv, 32);
     NRLTB_LAUNCH(k_bloch_build, tiles * (tiles + 1) / 2, 256, 0, s, DS, DP, pr, c->npairs, sk, c->d_seg.as<int2>(),
-                 c->d_orb.as<int>(), c->d_ksk.as<int>(), c->d_ph.as<double2>(), nk, nv, which0, M1, M2, S.jsover);
+                 c->d_orb.as<int>(), c->d_ksk.as<int>(), phb.as<double2>(), nk, nv, which0, M1, M2, S.jsover);
     CKL();
     return NRLTB_OK;
+}
+
+static int run_bloch(nrltb_ctx *c, int k0, int nk, int which0, double2 *M1, double2 *M2)
+{
+    return run_bloch_on(c, c->stream, c->d_ph, k0, nk, which0, M1, M2);
 }
 
 // The FP64 eigenvectors sit after the FP32 staging area of d_X, at a 256-byte
@@ -576,8 +587,13 @@ static int choose_chunk(int nv, int nk, int prec, size_t extra_per_k = 0)
 }
 
 // eigensolve of nkc matrices in H, S; eigenvalues into eig (ld nv), vectors into Z (FP64, optional)
+// side (mixed form, optional): issues the side stream's work once the FP32
+// eigensolve's tridiagonalisation has been queued (it waits for the event it
+// is given, recorded when the tridiagonalisation begins) and records
+// c->ev_side when done; pre: the H and S digits that work makes
 static int run_solve(nrltb_ctx *c, int nv, int nkc, int prec, const double2 *H, const double2 *S, double *eig,
-                     double2 *Zout, int *status, bool vectors)
+                     double2 *Zout, int *status, bool vectors, const OzakiA *pre = nullptr,
+                     const std::function<int(cudaEvent_t)> &side = {})
 {
     NvtxRange nv_(prec == NRLTB_PREC_FP64 ? "eigensolve FP64" : "eigensolve mixed");
     cudaStream_t s = c->stream;
@@ -594,13 +610,15 @@ static int run_solve(nrltb_ctx *c, int nv, int nkc, int prec, const double2 *H, 
         RET(c->d_X.ensure(sizeof(float2) * (size_t)nv * nv * nkc));
         EigWork<float> w;
         eig_work_carve<float>(w, c->d_work.p, nv, nkc);
-        eig_solve<float>(s, w, H, S, eig, c->d_X.as<float2>(), true);
+        eig_solve<float>(s, w, H, S, eig, c->d_X.as<float2>(), true, side ? c->ev_in : nullptr);
         CKL();
+        if (side) RET(side(c->ev_in));
         CK(cudaMemcpyAsync(status, w.status, sizeof(int) * nkc, cudaMemcpyDeviceToDevice, s));
         RET(c->d_ref.ensure(refine_work_bytes(nv, nkc)));
         RefineWork rw;
         refine_work_carve(rw, c->d_ref.p, nv, nkc);
-        refine_eigen(s, rw, H, S, c->d_X.as<float2>(), eig, Zout, status);
+        if (side) CK(cudaStreamWaitEvent(s, c->ev_side, 0));
+        refine_eigen(s, rw, H, S, c->d_X.as<float2>(), eig, Zout, status, pre);
         CKL();
         fault_mark(s, status, nkc);
     }
@@ -739,9 +757,25 @@ static int run_all(nrltb_ctx *c)
         if ((rc = c->d_ncut.ensure(sizeof(int) * (size_t)nrow))) break;
         if ((rc = c->d_status.ensure(sizeof(int) * (size_t)nrow))) break;
         const size_t nnb = (size_t)S.nv * S.nv;   // the Bloch sums before doubling
+        // mixed form, collinear: the digits of H and S (and dH, dS with their
+        // Bloch sums) are made on the side stream during the FP32 eigensolve
+        const bool overlap = o.precision == NRLTB_PREC_MIXED && !S.noncol;
+        const size_t side_per_k = overlap ? 2 * ozaki_a_bytes(nv, 1, 6) +
+                                                (lpress ? 2 * ozaki_a_bytes(nv, 1, 3) + 32 * (size_t)nv * nv : 0)
+                                          : 0;
         const int chunk = choose_chunk(nv, nk, o.precision,
-                                       (lqlmt ? lowdin_bytes_per_k(nv) : 0) + (S.noncol ? 32 * nnb : 0));
+                                       (lqlmt ? lowdin_bytes_per_k(nv) : 0) + (S.noncol ? 32 * nnb : 0) +
+                                           side_per_k);
         const size_t nn = (size_t)nv * nv;
+        const size_t oa6 = overlap ? ozaki_a_bytes(nv, chunk, 6) : 0;
+        const size_t oa3 = (overlap && lpress) ? ozaki_a_bytes(nv, chunk, 3) : 0;
+        if (overlap) {
+            if ((rc = c->d_oa.ensure(2 * oa6 + 2 * oa3))) break;
+            if (lpress) {
+                if ((rc = c->d_dH.ensure(sizeof(double2) * nn * chunk))) break;
+                if ((rc = c->d_dS.ensure(sizeof(double2) * nn * chunk))) break;
+            }
+        }
         if (S.noncol) {
             if ((rc = c->d_Hn.ensure(sizeof(double2) * nnb * chunk))) break;
             if ((rc = c->d_Sn.ensure(sizeof(double2) * nnb * chunk))) break;
@@ -771,13 +805,33 @@ static int run_all(nrltb_ctx *c)
                 } else if ((rc = run_bloch(c, k0, nkc, 0, c->d_H.as<double2>(), c->d_S.as<double2>()))) {
                     break;
                 }
+                OzakiA pre[4];
+                // the side stream's work: H's and S's digits for the refinement, and
+                // (modes 2, 4) the dH, dS Bloch sums with their digits for the
+                // Hellmann-Feynman products, while the tridiagonalisation runs
+                auto side = [&](cudaEvent_t start) -> int {
+                    NvtxRange nv_("digits of H, S, dH, dS (side stream)");
+                    cudaStream_t sd = c->side;
+                    char *oa = c->d_oa.as<char>();
+                    CK(cudaStreamWaitEvent(sd, start, 0));
+                    pre[0] = ozaki_prepare_a(sd, c->d_H.as<double2>(), nv, nkc, 6, oa);
+                    pre[1] = ozaki_prepare_a(sd, c->d_S.as<double2>(), nv, nkc, 6, oa + oa6);
+                    if (lpress) {
+                        RET(run_bloch_on(c, sd, c->d_ph2, k0, nkc, 2, c->d_dH.as<double2>(), c->d_dS.as<double2>()));
+                        pre[2] = ozaki_prepare_a(sd, c->d_dH.as<double2>(), nv, nkc, 3, oa + 2 * oa6);
+                        pre[3] = ozaki_prepare_a(sd, c->d_dS.as<double2>(), nv, nkc, 3, oa + 2 * oa6 + oa3);
+                    }
+                    CK(cudaEventRecord(c->ev_side, sd));
+                    return NRLTB_OK;
+                };
                 double2 *Z = nullptr;
                 if (vectors) {
                     // FP64 eigenvectors live after the FP32 staging area of d_X
                     Z = (double2 *)(c->d_X.as<char>() + zoff(nn, chunk));
                 }
                 if ((rc = run_solve(c, nv, nkc, o.precision, c->d_H.as<double2>(), c->d_S.as<double2>(), eig, Z,
-                                    status, vectors)))
+                                    status, vectors, overlap ? pre : nullptr,
+                                    overlap ? std::function<int(cudaEvent_t)>(side) : std::function<int(cudaEvent_t)>())))
                     break;
                 std::vector<int> hst(nkc), bad;
                 if (cudaMemcpyAsync(hst.data(), status, sizeof(int) * nkc, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
@@ -806,12 +860,15 @@ static int run_all(nrltb_ctx *c)
                     if (S.noncol) {
                         if ((rc = run_bloch(c, k0, nkc, 2, Hn, Sn))) break;
                         if ((rc = run_noncol_expand(c, nkc, Hn, Sn, true))) break;
-                    } else if ((rc = run_bloch(c, k0, nkc, 2, c->d_H.as<double2>(), c->d_S.as<double2>()))) {
+                    } else if (!overlap &&
+                               (rc = run_bloch(c, k0, nkc, 2, c->d_H.as<double2>(), c->d_S.as<double2>()))) {
                         break;
                     }
                     if ((rc = c->d_hf.ensure(hf_scratch_bytes(nv, nkc)))) break;
-                    if ((rc = run_hf(s, nv, nkc, o.precision, c->d_H.as<double2>(), c->d_S.as<double2>(), Z, eig,
-                                     c->d_deig.as<double>() + (size_t)r0 * nv, c->d_hf.p, nullptr)))
+                    const double2 *dH = overlap ? c->d_dH.as<double2>() : c->d_H.as<double2>();
+                    const double2 *dS = overlap ? c->d_dS.as<double2>() : c->d_S.as<double2>();
+                    if ((rc = run_hf(s, nv, nkc, o.precision, dH, dS, Z, eig, c->d_deig.as<double>() + (size_t)r0 * nv,
+                                     c->d_hf.p, overlap ? pre + 2 : nullptr)))
                         { set_err("hf failed"); break; }
                     CKL();
                     fault_mark(s, status, nkc);
@@ -852,6 +909,9 @@ static int run_all(nrltb_ctx *c)
                          c->d_spdir.as<double>());
         c->ran = 1;
     } while (0);
+    // whatever the side stream was given comes before the stream's later work
+    // (also when a chunk stopped early)
+    cudaStreamWaitEvent(s, c->ev_side, 0);
     return rc;
 }
 
@@ -945,7 +1005,17 @@ int nrltb_ctx_create(nrltb_ctx **out, int device)
     nrltb_ctx *c = new nrltb_ctx();
     c->device = device;
     e = cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking);
-    if (e != cudaSuccess) { set_err("stream: %s", cudaGetErrorString(e)); delete c; return NRLTB_E_CUDA; }
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_in, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_side, cudaEventDisableTiming);
+    if (e != cudaSuccess) {
+        set_err("stream: %s", cudaGetErrorString(e));
+        if (c->ev_in) cudaEventDestroy(c->ev_in);
+        if (c->side) cudaStreamDestroy(c->side);
+        if (c->own) cudaStreamDestroy(c->own);
+        delete c;
+        return NRLTB_E_CUDA;
+    }
     c->stream = c->own;
     *out = c;
     return NRLTB_OK;
@@ -956,17 +1026,22 @@ int nrltb_ctx_destroy(nrltb_ctx *c)
     if (!c) return NRLTB_OK;
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
+    if (c->side) cudaStreamSynchronize(c->side);
     DBuf *bufs[] = {&c->d_kkind, &c->d_posn, &c->d_posq, &c->d_kbas, &c->d_dnn, &c->d_screenl, &c->d_param,
                     &c->d_kq, &c->d_kw, &c->d_ksk, &c->d_orb, &c->d_flip, &c->d_spinat, &c->d_nc, &c->d_Hn, &c->d_Sn, &c->d_code, &c->d_blk, &c->d_misc, &c->d_pairs,
                     &c->d_sk, &c->d_seg, &c->d_ph, &c->d_H, &c->d_S, &c->d_X, &c->d_work, &c->d_ref, &c->d_hf, &c->d_np,
                     &c->d_qw, &c->d_eig, &c->d_deig, &c->d_ncut, &c->d_status, &c->d_fjob, &c->d_fout,
-                    &c->d_orbq, &c->d_spev, &c->d_spdir, &c->d_fault};
+                    &c->d_orbq, &c->d_spev, &c->d_spdir, &c->d_fault, &c->d_dH, &c->d_dS, &c->d_ph2,
+                    &c->d_oa};
     for (DBuf *b : bufs) b->release();
     if (c->kt) {
         for (cudaEvent_t e : c->kt->pool) cudaEventDestroy(e);
         delete c->kt;
     }
     for (nrltb_ctx *w : c->workers) nrltb_ctx_destroy(w);
+    if (c->ev_in) cudaEventDestroy(c->ev_in);
+    if (c->ev_side) cudaEventDestroy(c->ev_side);
+    if (c->side) cudaStreamDestroy(c->side);
     if (c->own) cudaStreamDestroy(c->own);
     delete c;
     return NRLTB_OK;

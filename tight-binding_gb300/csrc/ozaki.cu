@@ -588,13 +588,19 @@ OzakiX ozaki_prepare_x(cudaStream_t s, float2 *X, int n, int batch, void *work)
     return ox;
 }
 
-template <int SA> static void ozaki_gemm_sa(cudaStream_t s, const OzakiX &ox, const double2 *A, double2 *Y)
+// digits and row exponents of A into D, ex
+template <int SA> static void ozaki_digits_a(cudaStream_t s, const double2 *A, int n, int np, int batch, int *ex,
+                                             unsigned char *D)
+{
+    const size_t npp = (size_t)np * np;
+    NRLTB_LAUNCH(k_oz_colexp<double2>, cdiv((long)np * batch * 32, 256), 256, 0, s, A, n, np, ex, batch);
+    NRLTB_LAUNCH(k_oz_digits_a<SA>, cdiv((long)npp / 8 * batch, 256), 256, 0, s, A, n, np, ex, D, batch);
+}
+
+template <int SA> static void ozaki_product(cudaStream_t s, const OzakiX &ox, const unsigned char *DA, const int *exA,
+                                            double2 *Y)
 {
     const int n = ox.n, np = ox.np, batch = ox.batch;
-    const size_t npp = (size_t)np * np;
-    NRLTB_LAUNCH(k_oz_colexp<double2>, cdiv((long)np * batch * 32, 256), 256, 0, s, A, n, np, ox.exA, batch);
-    NRLTB_LAUNCH(k_oz_digits_a<SA>, cdiv((long)npp / 8 * batch, 256), 256, 0, s, A, n, np, ox.exA,
-                 (unsigned char *)ox.DA, batch);
     static const bool attr = [] {
         cudaFuncSetAttribute(k_oz_gemm<SA>, cudaFuncAttributeMaxDynamicSharedMemorySize, OZ_SMEM);
         return true;
@@ -602,15 +608,47 @@ template <int SA> static void ozaki_gemm_sa(cudaStream_t s, const OzakiX &ox, co
     (void)attr;
     dim3 grid(np / OZ_NX, np / OZ_MA, batch);
     cudaEvent_t ev = kt_begin(s);
-    NRLTB_LAUNCH(k_oz_gemm<SA>, grid, OZ_THREADS, OZ_SMEM, s, (const unsigned char *)ox.DA,
-                 (const unsigned char *)ox.DX, ox.exA, ox.exX, Y, n, np, batch, g_fault_word);
+    NRLTB_LAUNCH(k_oz_gemm<SA>, grid, OZ_THREADS, OZ_SMEM, s, DA, (const unsigned char *)ox.DX, exA, ox.exX, Y, n,
+                 np, batch, g_fault_word);
     kt_end(ev, s, KC_DIGIT_GEMM, 8.0 * n * (double)n * n * batch);
 }
 
 void ozaki_gemm(cudaStream_t s, const OzakiX &ox, const double2 *A, double2 *Y, int adigits)
 {
-    if (adigits == 3) ozaki_gemm_sa<3>(s, ox, A, Y);
-    else ozaki_gemm_sa<6>(s, ox, A, Y);
+    if (adigits == 3) {
+        ozaki_digits_a<3>(s, A, ox.n, ox.np, ox.batch, ox.exA, (unsigned char *)ox.DA);
+        ozaki_product<3>(s, ox, (const unsigned char *)ox.DA, ox.exA, Y);
+    } else {
+        ozaki_digits_a<6>(s, A, ox.n, ox.np, ox.batch, ox.exA, (unsigned char *)ox.DA);
+        ozaki_product<6>(s, ox, (const unsigned char *)ox.DA, ox.exA, Y);
+    }
+}
+
+size_t ozaki_a_bytes(int n, int batch, int adigits)
+{
+    const size_t np = (size_t)padn(n), nb = (size_t)batch;
+    return al256(sizeof(__nv_bfloat16) * np * np * nb * 2 * (adigits == 3 ? 3 : OZ_SA)) +
+           al256(sizeof(int) * np * nb) + 256;
+}
+
+OzakiA ozaki_prepare_a(cudaStream_t s, const double2 *A, int n, int batch, int adigits, void *work)
+{
+    const int np = padn(n), sa = adigits == 3 ? 3 : OZ_SA;
+    unsigned char *D = (unsigned char *)work;
+    int *ex = (int *)(D + al256(sizeof(__nv_bfloat16) * (size_t)np * np * batch * 2 * sa));
+    if (sa == 3) ozaki_digits_a<3>(s, A, n, np, batch, ex, D);
+    else ozaki_digits_a<6>(s, A, n, np, batch, ex, D);
+    OzakiA oa;
+    oa.D = D;
+    oa.ex = ex;
+    oa.sa = sa;
+    return oa;
+}
+
+void ozaki_gemm_prepared(cudaStream_t s, const OzakiX &ox, const OzakiA &oa, double2 *Y)
+{
+    if (oa.sa == 3) ozaki_product<3>(s, ox, oa.D, oa.ex, Y);
+    else ozaki_product<6>(s, ox, oa.D, oa.ex, Y);
 }
 
 unsigned ozaki_fault(bool clear)

@@ -22,6 +22,18 @@ OzakiX ozaki_prepare_x(cudaStream_t s, float2 *X, int n, int batch, void *work);
 // adigits = 3: A rounded to 24 bits of its row scale, all 9 digit pairs
 // (the exact product of the rounded A and X, FP32-class accuracy).
 void ozaki_gemm(cudaStream_t s, const OzakiX &ox, const double2 *A, double2 *Y, int adigits = 6);
+// A's digits prepared ahead of the product (on another stream, while other
+// work runs): digit blocks and row exponents in caller-owned memory of
+// ozaki_a_bytes(n, batch, adigits) bytes, 256-byte aligned.
+struct OzakiA {
+    const unsigned char *D;   // digit blocks of A (adigits planes)
+    const int *ex;            // per-row binary exponents
+    int sa;                   // digits: 6 or 3
+};
+size_t ozaki_a_bytes(int n, int batch, int adigits);
+OzakiA ozaki_prepare_a(cudaStream_t s, const double2 *A, int n, int batch, int adigits, void *work);
+// Y = A X with A's digits from ozaki_prepare_a (the same result as ozaki_gemm)
+void ozaki_gemm_prepared(cudaStream_t s, const OzakiX &ox, const OzakiA &oa, double2 *Y);
 // fault flag of the product kernel (a barrier wait that ran out); clear resets it
 unsigned ozaki_fault(bool clear);
 

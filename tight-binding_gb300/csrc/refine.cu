@@ -653,15 +653,20 @@ __global__ void k_ref_finish(RefineWork w, double2 *Z)
 }
 
 void refine_eigen(cudaStream_t s, RefineWork &w, const double2 *H, const double2 *S, float2 *X,
-                  double *eig, double2 *Z, int *status)
+                  double *eig, double2 *Z, int *status, const OzakiA *pre)
 {
     const int n = w.n, B = w.batch;
     const long nn = (long)n * n, nb = (long)n * B;
     const float2 onef = make_float2(1.f, 0.f), zerof = make_float2(0.f, 0.f);
     // 1. H X, S X (tensor cores, FP64-accurate), accurate diagonals
     const OzakiX ox = ozaki_prepare_x(s, X, n, B, w.oz);
-    ozaki_gemm(s, ox, H, w.YH);
-    ozaki_gemm(s, ox, S, w.YS);
+    if (pre) {
+        ozaki_gemm_prepared(s, ox, pre[0], w.YH);
+        ozaki_gemm_prepared(s, ox, pre[1], w.YS);
+    } else {
+        ozaki_gemm(s, ox, H, w.YH);
+        ozaki_gemm(s, ox, S, w.YS);
+    }
     NRLTB_LAUNCH(k_ref_diag, cdiv(nb * 32, 256), 256, 0, s, w, X);
     // 2. clusters and their Rayleigh-Ritz rotations
     const size_t csm = n <= REF_KEYS_MAX ? sizeof(unsigned long long) * n : 0;
@@ -714,9 +719,8 @@ void launch_to_f32(cudaStream_t s, const double2 *src, float2 *dst, long count)
 }
 
 int run_hf(cudaStream_t s, int n, int nkc, int prec, const double2 *dH, const double2 *dS, const double2 *Z,
-           const double *eig, double *deig, void *scratch, void *unused)
+           const double *eig, double *deig, void *scratch, const OzakiA *pre)
 {
-    (void)unused;
     const long nn = (long)n * n;
     double2 *P = (double2 *)scratch;
     double2 *Q = (double2 *)((char *)scratch + al256(sizeof(double2) * nn * nkc));
@@ -740,8 +744,13 @@ int run_hf(cudaStream_t s, int n, int nkc, int prec, const double2 *dH, const do
         void *oz = (char *)z32 + al256(sizeof(float2) * nn * nkc);
         launch_to_f32(s, Z, z32, nn * nkc);
         const OzakiX ox = ozaki_prepare_x(s, z32, n, nkc, oz);
-        ozaki_gemm(s, ox, dH, P, 3);
-        ozaki_gemm(s, ox, dS, Q, 3);
+        if (pre) {
+            ozaki_gemm_prepared(s, ox, pre[0], P);
+            ozaki_gemm_prepared(s, ox, pre[1], Q);
+        } else {
+            ozaki_gemm(s, ox, dH, P, 3);
+            ozaki_gemm(s, ox, dS, Q, 3);
+        }
         launch_hf_dots_full(s, Z, P, Q, eig, deig, n, nkc);
     }
     return cudaGetLastError() == cudaSuccess ? NRLTB_OK : NRLTB_E_CUDA;

@@ -2,6 +2,7 @@
 // eigenpairs, and the Hellmann-Feynman products of both forms.
 #pragma once
 #include "common.cuh"
+#include "ozaki.cuh"
 
 namespace nrltb {
 
@@ -28,13 +29,17 @@ void refine_work_carve(RefineWork &w, void *base, int n, int batch);
 // eigenvectors.  status[k] gets NRLTB_K_NOT_CONVERGED when a cluster exceeds the
 // handled size.
 // X is rounded in place to the representation the tensor-core products use.
+// pre (optional): the 6-digit forms of H and S from ozaki_prepare_a, already
+// made (or being made on a stream this one waits for).
 void refine_eigen(cudaStream_t s, RefineWork &w, const double2 *H, const double2 *S, float2 *X,
-                  double *eig, double2 *Z, int *status);
+                  double *eig, double2 *Z, int *status, const OzakiA *pre = nullptr);
 
 // Hellmann-Feynman shifts deig = diag(Z^H dH Z) - eig * diag(Z^H dS Z) for nkc
 // matrices; scratch must hold hf_scratch_bytes(n, nkc), 256-byte aligned.
+// pre (optional, mixed form): the 3-digit forms of dH and dS from
+// ozaki_prepare_a (dH, dS are then not read).
 int run_hf(cudaStream_t s, int n, int nkc, int prec, const double2 *dH, const double2 *dS, const double2 *Z,
-           const double *eig, double *deig, void *scratch, void *unused);
+           const double *eig, double *deig, void *scratch, const OzakiA *pre = nullptr);
 size_t hf_scratch_bytes(int n, int nkc);
 
 }  // namespace nrltb
