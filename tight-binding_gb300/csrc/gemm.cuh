@@ -125,6 +125,20 @@ zgemm_kernel(GemmArgs<T> g)
         __syncthreads();
     }
     const bool beta0 = (g.beta.x == T(0) && g.beta.y == T(0));
+    // FP32: the old C first (loads in flight together: a load after a store to
+    // C could alias it and would wait for it); FP64 keeps the registers for
+    // occupancy and loads each element before its store
+    constexpr bool PRE = sizeof(T) == 4;
+    C2 cold[PRE ? TM : 1][PRE ? TN : 1];
+    if (PRE && !beta0) {
+#pragma unroll
+        for (int i = 0; i < TM; ++i)
+#pragma unroll
+            for (int j = 0; j < TN; ++j) {
+                const int m = m0 + tx + i * (BM / TM), n = n0 + ty + j * (BN / TN);
+                cold[PRE ? i : 0][PRE ? j : 0] = (m < g.m && n < g.n) ? Cm[m + (long)n * g.ldc] : cmk<T>(0, 0);
+            }
+    }
 #pragma unroll
     for (int i = 0; i < TM; ++i) {
         int m = m0 + tx + i * (BM / TM);
@@ -135,7 +149,7 @@ zgemm_kernel(GemmArgs<T> g)
             if (n >= g.n) continue;
             C2 *c = Cm + m + (long)n * g.ldc;
             C2 v = cmul(g.alpha, acc[i][j]);
-            if (!beta0) v = cadd(v, cmul(g.beta, *c));
+            if (!beta0) v = cadd(v, cmul(g.beta, PRE ? cold[PRE ? i : 0][PRE ? j : 0] : *c));
             *c = v;
         }
     }

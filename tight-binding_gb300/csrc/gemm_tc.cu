@@ -194,6 +194,21 @@ __global__ void __launch_bounds__(TC_THREADS, 2) zgemm_tc_kernel(GemmArgs<float>
         }
     }
     const bool beta0 = (g.beta.x == 0.f && g.beta.y == 0.f);
+    // the old C first (loads in flight together: a load after a store to C
+    // could alias it and would wait for it)
+    float2 cold[2][TC_NT][4];
+    if (!beta0) {
+#pragma unroll
+        for (int a = 0; a < 2; ++a)
+#pragma unroll
+            for (int c = 0; c < TC_NT; ++c)
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const int m = m0 + wm + a * 16 + gq + (q >= 2 ? 8 : 0);
+                    const int n = n0 + wn + c * 8 + 2 * tq + (q & 1);
+                    cold[a][c][q] = (m < g.m && n < g.n) ? Cm[m + (long)n * g.ldc] : make_float2(0.f, 0.f);
+                }
+    }
 #pragma unroll
     for (int a = 0; a < 2; ++a)
 #pragma unroll
@@ -205,7 +220,7 @@ __global__ void __launch_bounds__(TC_THREADS, 2) zgemm_tc_kernel(GemmArgs<float>
                 if (m >= g.m || n >= g.n) continue;
                 float2 *cp = Cm + m + (long)n * g.ldc;
                 float2 v = cmul(g.alpha, make_float2(accr[a][c][q], acci[a][c][q]));
-                if (!beta0) v = cadd(v, cmul(g.beta, *cp));
+                if (!beta0) v = cadd(v, cmul(g.beta, cold[a][c][q]));
                 *cp = v;
             }
 }

@@ -350,13 +350,23 @@ __global__ void __launch_bounds__(UM_THREADS, 2) zgemm_umma_kernel(GemmArgs<floa
                 for (int j = 0; j < 16; ++j) re[j] = im[j] = 0.f;
             }
             if (m < g.m) {
+                // the old C of all 16 columns first (their loads in flight together:
+                // a load after a store to C could alias it and would wait for it)
+                float2 cold[16];
+                if (!beta0) {
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) {
+                        const int n = n0 + 32 * h + cc + j;
+                        cold[j] = (n < g.n) ? Cm[m + (long)n * g.ldc] : make_float2(0.f, 0.f);
+                    }
+                }
 #pragma unroll
                 for (int j = 0; j < 16; ++j) {
                     const int n = n0 + 32 * h + cc + j;
                     if (n >= g.n) break;
                     float2 *cp = Cm + m + (long)n * g.ldc;
                     float2 v = cmul(g.alpha, make_float2(re[j], im[j]));
-                    if (!beta0) v = cadd(v, cmul(g.beta, *cp));
+                    if (!beta0) v = cadd(v, cmul(g.beta, cold[j]));
                     *cp = v;
                 }
             }
