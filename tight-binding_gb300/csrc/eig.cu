@@ -805,14 +805,27 @@ __global__ void k_tri_invit(const double *dd, const double *ee, const double *la
     // sg * (double) x, off the FP64 pipe)
     const long long sgbit = (vkmax < TB(0)) ? (long long)0x8000000000000000ull : 0ll;
     double *z = yvec + (long)b * n * n + (long)rank[(long)b * n + r] * n;
-    for (int k = 0; k < n; ++k) {
-        double x = 0.0;
-        if (k >= b0 && k <= b1) {
-            if constexpr (sizeof(TB) == 4) x = f2d_exact(v[k - b0] * inv);
-            else x = (double)(v[k - b0] * inv);
-            x = __longlong_as_double(__double_as_longlong(x) ^ sgbit);
+    // eight elements' loads before their stores (a load after a store to z
+    // could alias it and would wait for it)
+    for (int k8 = 0; k8 < n; k8 += 8) {
+        TB vv[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            const int k = k8 + u;
+            vv[u] = (k < n && k >= b0 && k <= b1) ? v[k - b0] : TB(0);
         }
-        z[k] = x;
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            const int k = k8 + u;
+            if (k >= n) break;
+            double x = 0.0;
+            if (k >= b0 && k <= b1) {
+                if constexpr (sizeof(TB) == 4) x = f2d_exact(vv[u] * inv);
+                else x = (double)(vv[u] * inv);
+                x = __longlong_as_double(__double_as_longlong(x) ^ sgbit);
+            }
+            z[k] = x;
+        }
     }
 }
 

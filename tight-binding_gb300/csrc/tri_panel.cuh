@@ -218,6 +218,7 @@ __global__ void __launch_bounds__(TP_THREADS, 2) k_tri_panel(EigWork<T> w, int j
         for (int k = warp; k < nown; k += TP_WARPS) {
             const int r = 32 * (q + CL * k) + lane;
             if (r < i || r >= n) continue;
+            C2 a = A[r + (long)i * ld];   // before the store to Wp, which it could alias
             C2 wl = zero;
             const int slot = 32 * k + lane;
             if (c > 0) {
@@ -225,7 +226,6 @@ __global__ void __launch_bounds__(TP_THREADS, 2) k_tri_panel(EigWork<T> w, int j
                 Wp[r + (long)(c - 1) * n] = wl;
                 sm.Ws[(c - 1) * ns + slot] = wl;
             }
-            C2 a = A[r + (long)i * ld];
             // eight panel columns per round: their loads are issued together
             for (int j8 = 0; j8 < c; j8 += 8) {
                 C2 vv[8], ww[8];
