@@ -5,6 +5,9 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <stdio.h>
+#include <map>
+#include <mutex>
+#include <utility>
 #include <vector>
 
 namespace nrltb {
@@ -151,6 +154,25 @@ extern thread_local unsigned *g_fault_word;
 // launching stream around each launch of a timed class, with the launch's
 // algorithmic work (flops or bytes), summed by nrltb_bench_kernel_stats.
 enum KClass { KC_GEMM_TC = 0, KC_GEMM_SIMT = 1, KC_DIGIT_GEMM = 2, KC_TRI_PANEL = 3, KC_COUNT = 4 };
+// Raise a kernel's dynamic shared-memory limit on the current device to at
+// least `bytes`, never lowering it: host threads that launch the same kernel
+// with different sizes (the structure batch) must not lower the limit between
+// another thread's setting and its launch.  Returns the CUDA status.
+inline cudaError_t smem_attr_at_least(const void *func, int bytes)
+{
+    static std::mutex mu;
+    static std::map<std::pair<int, const void *>, int> set;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> g(mu);
+    int &cur = set[std::make_pair(dev, func)];
+    if (bytes <= cur) return cudaSuccess;
+    e = cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e == cudaSuccess) cur = bytes;
+    return e;
+}
+
 struct KTimer {
     bool on = false;
     struct Rec { int cls; cudaEvent_t a, b; double work; };

@@ -1135,7 +1135,7 @@ void eig_solve(cudaStream_t s, EigWork<T> &w, const double2 *H, const double2 *S
         dim3 g(cdiv(n, 128), B);
         const size_t bsm = sizeof(T) == 4 ? 2 * sizeof(float) * n + n : 0;
         if (bsm > 48 * 1024)
-            cudaFuncSetAttribute(k_tri_bisect<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bsm);
+            smem_attr_at_least((const void *)k_tri_bisect<T>, (int)bsm);
         NRLTB_LAUNCH(k_tri_bisect<T>, g, 128, bsm, s, w.d, w.e, lamloc, blk, n);
         NRLTB_LAUNCH(k_tri_rank, g, 128, 0, s, lamloc, rank, w.lam, n);
         cudaMemcpyAsync(eig, w.lam, sizeof(double) * n * B, cudaMemcpyDeviceToDevice, s);
@@ -1149,7 +1149,7 @@ void eig_solve(cudaStream_t s, EigWork<T> &w, const double2 *H, const double2 *S
         // 64 threads per CTA: cdiv(n, 64) * 64 * B thread slots <= the scratch carve's 64 cdiv(n, 64) n B
         const size_t ism = sizeof(T) == 4 ? 2 * sizeof(float) * n : 0;
         if (ism > 48 * 1024)
-            cudaFuncSetAttribute(k_tri_invit<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ism);
+            smem_attr_at_least((const void *)k_tri_invit<T>, (int)ism);
         NRLTB_LAUNCH(k_tri_invit<T>, dim3(cdiv(n, 64), B), 64, ism, s, w.d, w.e, lamloc, blk, rank, w.yvec,
                      (T *)w.ylu, n);
         NRLTB_LAUNCH(k_tri_cluster_orth, dim3(cdiv(n, 8), B), 256, 0, s, w.d, w.e, lamloc, blk, rank, w.yvec, n,

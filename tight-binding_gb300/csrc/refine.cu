@@ -670,7 +670,7 @@ void refine_eigen(cudaStream_t s, RefineWork &w, const double2 *H, const double2
     NRLTB_LAUNCH(k_ref_diag, cdiv(nb * 32, 256), 256, 0, s, w, X);
     // 2. clusters and their Rayleigh-Ritz rotations
     const size_t csm = n <= REF_KEYS_MAX ? sizeof(unsigned long long) * n : 0;
-    if (csm > 48 * 1024) cudaFuncSetAttribute(k_ref_clusters, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)csm);
+    if (csm > 48 * 1024) smem_attr_at_least((const void *)k_ref_clusters, (int)csm);
     NRLTB_LAUNCH(k_ref_clusters, B, 1024, csm, s, w, status);
     NRLTB_LAUNCH(k_ref_rr, dim3(n, B), REF_CMAX * REF_CMAX, 0, s, w, X);
     // 3. rotated basis, its residuals, G' = X'^H r' (X'^H formed explicitly in

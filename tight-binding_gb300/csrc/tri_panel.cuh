@@ -429,8 +429,6 @@ bool tri_panel_launch(cudaStream_t s, const EigWork<T> &w, int j0, int jb)
     if (sizeof(T) == 8) return false;
     const size_t smem = tp_smem_bytes(w.n, 0, sizeof(typename cplx<T>::t));
     if (smem > 200 * 1024) return false;
-    static thread_local int checked_dev = -1;
-    static thread_local bool ok_dev = false;
     int dev = 0;
     cudaGetDevice(&dev);
     cudaLaunchConfig_t cfg = {};
@@ -445,17 +443,27 @@ bool tri_panel_launch(cudaStream_t s, const EigWork<T> &w, int j0, int jb)
     cfg.stream = s;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    if (cudaFuncSetAttribute(k_tri_panel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+    if (smem_attr_at_least((const void *)k_tri_panel<T>, (int)smem) != cudaSuccess) {
         cudaGetLastError();   // not sticky: the per-column path takes over
         return false;
     }
-    if (checked_dev != dev) {
-        int nclusters = 0;
-        ok_dev = cudaOccupancyMaxActiveClusters(&nclusters, k_tri_panel<T>, &cfg) == cudaSuccess && nclusters > 0;
-        checked_dev = dev;
-        cudaGetLastError();
+    {
+        // whether a cluster of this shared-memory size can be scheduled, once per
+        // (device, size) for the whole process (the answer does not depend on
+        // which thread asks or on what ran before)
+        static std::mutex mu;
+        static std::map<std::pair<int, size_t>, bool> fits;
+        std::lock_guard<std::mutex> g(mu);
+        auto it = fits.find(std::make_pair(dev, smem));
+        if (it == fits.end()) {
+            int nclusters = 0;
+            const bool ok = cudaOccupancyMaxActiveClusters(&nclusters, k_tri_panel<T>, &cfg) == cudaSuccess &&
+                            nclusters > 0;
+            cudaGetLastError();
+            it = fits.emplace(std::make_pair(dev, smem), ok).first;
+        }
+        if (!it->second) return false;
     }
-    if (!ok_dev) return false;
     cudaEvent_t ev = kt_begin(s);
     if (cudaLaunchKernelEx(&cfg, k_tri_panel<T>, w, j0, jb) != cudaSuccess) {
         cudaGetLastError();
