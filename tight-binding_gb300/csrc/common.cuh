@@ -114,6 +114,48 @@ __device__ __forceinline__ float d2f_rn(double x)
     return __uint_as_float(f | sign);
 }
 
+// order-preserving 64-bit key of a double (not NaN; -0 and +0 share the key
+// of 0): key(u) < key(v) exactly when u < v
+__device__ __forceinline__ unsigned long long ord_key(double v)
+{
+    const long long bits = v == 0.0 ? 0ll : __double_as_longlong(v);
+    return bits >= 0 ? (unsigned long long)bits ^ 0x8000000000000000ull : ~(unsigned long long)bits;
+}
+
+// Rank of L[j] among L[0..n) (ties by index): the number of q with L[q] < L[j]
+// or L[q] == L[j] and q < j.  With `keys` (shared memory of n keys, filled
+// here by the whole CTA, which must all call this) the comparisons are
+// integer ones on order-preserving keys; the same ranks either way.
+__device__ __forceinline__ int rank_of(const double *L, int n, int j, unsigned long long *keys)
+{
+    if (keys) {
+        for (int q = threadIdx.x; q < n; q += blockDim.x) keys[q] = ord_key(L[q]);
+        __syncthreads();
+        if (j >= n) return 0;
+        const unsigned long long kv = keys[j];
+        int r = 0;
+        for (int q = 0; q < n; ++q) {
+            const unsigned long long ku = keys[q];
+            r += (ku < kv) || (ku == kv && q < j);
+        }
+        return r;
+    }
+    if (j >= n) return 0;
+    const double v = L[j];
+    int r = 0;
+    for (int q = 0; q < n; ++q) {
+        const double u = L[q];
+        r += (u < v) || (u == v && q < j);
+    }
+    return r;
+}
+// shared memory for rank_of's keys (0: compare in FP64 from global memory)
+inline size_t rank_keys_bytes(int n)
+{
+    const size_t b = sizeof(unsigned long long) * (size_t)n;
+    return b <= 160 * 1024 ? b : 0;
+}
+
 template <typename T> __device__ __forceinline__ T warp_sum(T v)
 {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);

@@ -605,20 +605,16 @@ __global__ void k_tri_bisect(const double *dd, const double *ee, double *lamloc,
 }
 
 // Global ascending order: rank of (lamloc[r], r).
-__global__ void k_tri_rank(const double *lamloc, int *rank, double *lam, int n)
+__global__ void k_tri_rank(const double *lamloc, int *rank, double *lam, int n, int keys)
 {
+    extern __shared__ unsigned long long trk_keys[];
     const int b = blockIdx.y;
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= n) return;
     const double *L = lamloc + (long)b * n;
-    double v = L[r];
-    int cnt = 0;
-    for (int s = 0; s < n; ++s) {
-        double u = L[s];
-        cnt += (u < v) || (u == v && s < r);
-    }
+    const int cnt = rank_of(L, n, r, keys ? trk_keys : nullptr);
+    if (r >= n) return;
     rank[(long)b * n + r] = cnt;
-    lam[(long)b * n + cnt] = v;
+    lam[(long)b * n + cnt] = L[r];
 }
 
 __device__ inline unsigned hash_bits(unsigned a, unsigned b)
@@ -1137,7 +1133,9 @@ void eig_solve(cudaStream_t s, EigWork<T> &w, const double2 *H, const double2 *S
         if (bsm > 48 * 1024)
             smem_attr_at_least((const void *)k_tri_bisect<T>, (int)bsm);
         NRLTB_LAUNCH(k_tri_bisect<T>, g, 128, bsm, s, w.d, w.e, lamloc, blk, n);
-        NRLTB_LAUNCH(k_tri_rank, g, 128, 0, s, lamloc, rank, w.lam, n);
+        const size_t rsm = rank_keys_bytes(n);
+        if (rsm > 48 * 1024) smem_attr_at_least((const void *)k_tri_rank, (int)rsm);
+        NRLTB_LAUNCH(k_tri_rank, g, 128, rsm, s, lamloc, rank, w.lam, n, rsm > 0 ? 1 : 0);
         cudaMemcpyAsync(eig, w.lam, sizeof(double) * n * B, cudaMemcpyDeviceToDevice, s);
     }
     if (!vectors) return;

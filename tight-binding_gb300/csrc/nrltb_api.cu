@@ -877,7 +877,7 @@ static int run_all(nrltb_ctx *c)
         }
         if (rc) break;
         if (lpress) {
-            NRLTB_LAUNCH(k_ncut, cdiv(nrow, 128), 128, 0, s, c->d_eig.as<double>(), nv, nv, nrow, o.eigcut,
+            NRLTB_LAUNCH(k_ncut, cdiv(nrow, 4), 128, 0, s, c->d_eig.as<double>(), nv, nv, nrow, o.eigcut,
                          c->d_ncut.as<int>());
             for (auto &kc : c->nonpd) {
                 cudaMemsetAsync(c->d_ncut.as<int>() + kc.first, 0, sizeof(int), s);

@@ -105,13 +105,6 @@ __global__ void k_ref_diag(RefineWork w, const float2 *X)
 }
 
 // ---- 2. clusters: one CTA per matrix ----------------------------------------
-// order-preserving 64-bit key of a double (not NaN; -0 and +0 share the key
-// of 0): key(u) < key(v) exactly when u < v
-__device__ __forceinline__ unsigned long long ord_key(double v)
-{
-    const long long bits = v == 0.0 ? 0ll : __double_as_longlong(v);
-    return bits >= 0 ? (unsigned long long)bits ^ 0x8000000000000000ull : ~(unsigned long long)bits;
-}
 
 // the rank sort takes its keys from shared memory up to this order
 constexpr int REF_KEYS_MAX = 24576;
@@ -620,20 +613,16 @@ __global__ void k_ref_band_apply(RefineWork w, const float2 *Fb)
 }
 
 // 5a. ascending order of the refined eigenvalues
-__global__ void k_ref_rank(RefineWork w, const double *l2, double *eig)
+__global__ void k_ref_rank(RefineWork w, const double *l2, double *eig, int keys)
 {
+    extern __shared__ unsigned long long rank_keys[];
     const int b = blockIdx.y, n = w.n;
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= n) return;
     const double *L = l2 + (long)b * n;
-    const double v = L[j];
-    int r = 0;
-    for (int q = 0; q < n; ++q) {
-        const double u = L[q];
-        r += (u < v) || (u == v && q < j);
-    }
+    const int r = rank_of(L, n, j, keys ? rank_keys : nullptr);
+    if (j >= n) return;
     w.cl[(long)3 * n * w.batch + (long)b * n + j] = r;
-    eig[(long)b * n + r] = v;
+    eig[(long)b * n + r] = L[j];
 }
 
 // 5b. Z[:, rank(j)] = X'[:, j] + (X' E)[:, j]
@@ -694,7 +683,9 @@ void refine_eigen(cudaStream_t s, RefineWork &w, const double2 *H, const double2
     // 5. Z = X' + X' E, reordered
     zgemm<float>(s, n, n, n, B, onef, w.Xr, n, nn, 0, w.Ef, n, nn, 0, zerof, w.XE, n, nn);
     const double *l2 = w.lam + 2 * nb;
-    NRLTB_LAUNCH(k_ref_rank, dim3(cdiv(n, 128), B), 128, 0, s, w, l2, eig);
+    const size_t rsm = rank_keys_bytes(n);
+    if (rsm > 48 * 1024) smem_attr_at_least((const void *)k_ref_rank, (int)rsm);
+    NRLTB_LAUNCH(k_ref_rank, dim3(cdiv(n, 128), B), 128, rsm, s, w, l2, eig, rsm > 0 ? 1 : 0);
     if (Z) NRLTB_LAUNCH(k_ref_finish, cdiv(nn * B, 256), 256, 0, s, w, Z);
 }
 

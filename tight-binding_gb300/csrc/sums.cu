@@ -378,13 +378,19 @@ __global__ void __launch_bounds__(256) k_spin_dir_sum(const double *eig, const d
 }
 
 // ncut[k] = number of eigenvalues <= eigcut (perturb.f:87-95)
+// ncut[k] = the first band whose eigenvalue exceeds eigcut (nv if none); one
+// warp per row, 32 bands per step
 __global__ void k_ncut(const double *eig, int ldk, int nv, int nk, double eigcut, int *ncut)
 {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= nk) return;
-    int c = 0;
-    while (c < nv && !(eig[(long)k * ldk + c] > eigcut)) ++c;
-    ncut[k] = c;
+    const int k = (int)((blockIdx.x * (long)blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+    if (k >= nk) return;   // warp-uniform
+    int c = nv;
+    for (int c0 = 0; c0 < nv; c0 += 32) {
+        const int q = c0 + lane;
+        const unsigned above = __ballot_sync(0xffffffffu, q < nv && eig[(long)k * ldk + q] > eigcut);
+        if (above) { c = c0 + __ffs(above) - 1; break; }
+    }
+    if (lane == 0) ncut[k] = c;
 }
 
 // Hellmann-Feynman shifts from P = triu(dH) Z and Q = triu(dS) Z:
