@@ -54,6 +54,7 @@ constexpr int OZ_XBLK = 3 * OZ_NX * 128;          // X digit block (one t): -Xi_
 constexpr int OZ_XSTAGE = OZ_SB * OZ_XBLK;        // a chunk's X digits, 72 KB
 constexpr int OZ_NXS = 2;                 // X chunk stages
 constexpr int OZ_NAS = 2;                 // A blocks in flight
+constexpr int OZ_APF = 4;                 // A blocks ahead of the one being copied brought into L2
 constexpr int OZ_NBUF = 4;                // tensor-memory level buffers, 128 columns each
 constexpr int OZ_FOLD_WARPS = 16;         // 4 per 32-lane quarter, 16 columns each
 constexpr int OZ_THREADS = 32 * (OZ_FOLD_WARPS + 2);   // + producer warp + MMA warp
@@ -348,6 +349,12 @@ __device__ __forceinline__ void oz_bulk(uint32_t dst, const void *src, uint32_t 
                  :: "r"(dst), "l"(src), "r"(bytes), "r"(bar) : "memory");
 }
 
+// hint: bring a block of global memory into L2 ahead of its bulk copy
+__device__ __forceinline__ void oz_prefetch_l2(const void *src, uint32_t bytes)
+{
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" :: "l"(src), "r"(bytes) : "memory");
+}
+
 __device__ __forceinline__ void oz_arrive(uint32_t bar)
 {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" :: "r"(bar) : "memory");
@@ -427,6 +434,10 @@ k_oz_gemm(const unsigned char *DA, const unsigned char *DX, const int *exA, cons
         // ---- producer: bulk copies of the pre-swizzled digit tiles ----
         if (lane == 0) {
             bool ok = true;
+            // the A ring holds two planes: later planes are brought into L2 ahead
+            // of their copies (a chunk's X digits, needed a whole chunk later, too)
+            const int QA = KC * SA;
+            for (int qa = OZ_NAS; qa < min(OZ_APF, QA); ++qa) oz_prefetch_l2(gA + (long)qa * OZ_ABLK, OZ_ABLK);
             for (int kc = 0; kc < KC && ok; ++kc) {
                 const int jx = kc % OZ_NXS, ux = kc / OZ_NXS;
                 if (ux > 0 && !(ok = oz_wait(empty_x(jx), (ux - 1) & 1, abort))) break;
@@ -434,8 +445,11 @@ k_oz_gemm(const unsigned char *DA, const unsigned char *DX, const int *exA, cons
                 for (int q = 0; q < OZ_SB; ++q)
                     oz_bulk(oz_saddr(sX + jx * OZ_XSTAGE + q * OZ_XBLK), gX + ((long)kc * OZ_SB + q) * OZ_XBLK,
                             OZ_XBLK, full_x(jx));
+                if (kc + 1 < KC)
+                    for (int q = 0; q < OZ_SB; ++q) oz_prefetch_l2(gX + ((long)(kc + 1) * OZ_SB + q) * OZ_XBLK, OZ_XBLK);
                 for (int sdig = 0; sdig < SA; ++sdig) {
                     const int qa = kc * SA + sdig, ia = qa % OZ_NAS, ua = qa / OZ_NAS;
+                    if (qa + OZ_APF < QA) oz_prefetch_l2(gA + (long)(qa + OZ_APF) * OZ_ABLK, OZ_ABLK);
                     if (ua > 0 && !(ok = oz_wait(empty_a(ia), (ua - 1) & 1, abort))) break;
                     oz_expect(full_a(ia), OZ_ABLK);
                     oz_bulk(oz_saddr(sA + ia * OZ_ABLK), gA + (long)qa * OZ_ABLK, OZ_ABLK, full_a(ia));
@@ -469,11 +483,15 @@ k_oz_gemm(const unsigned char *DA, const unsigned char *DX, const int *exA, cons
                         // X block rows: [-Xi | Xr | Xi]; w1 = [Xr | Xi], w2 = [-Xi | Xr]
                         const uint32_t w2 = sx0 + jx * OZ_XSTAGE + tdig * OZ_XBLK, w1 = w2 + OZ_NX * 128;
                         const uint32_t tl = tmem + 128u * buf;
+                        // a 16-deep step is 32 bytes along the swizzled row: 2 in the
+                        // descriptor's address field (which no step carries out of)
+                        const uint64_t dar = oz_desc(ar), dai = oz_desc(ai), dw1 = oz_desc(w1), dw2 = oz_desc(w2);
+                        oz_mma(tl, dar, dw1, first ? 0u : 1u);
+                        oz_mma(tl, dai, dw2, 1u);
 #pragma unroll
-                        for (int ks = 0; ks < OZ_BK / 16; ++ks) {
-                            const uint32_t ko = 32u * ks;
-                            oz_mma(tl, oz_desc(ar + ko), oz_desc(w1 + ko), (first && ks == 0) ? 0u : 1u);
-                            oz_mma(tl, oz_desc(ai + ko), oz_desc(w2 + ko), 1u);
+                        for (int ks = 1; ks < OZ_BK / 16; ++ks) {
+                            oz_mma(tl, dar + 2 * ks, dw1 + 2 * ks, 1u);
+                            oz_mma(tl, dai + 2 * ks, dw2 + 2 * ks, 1u);
                         }
                     }
                     if (!ok) break;
