@@ -38,6 +38,7 @@
 //
 // Because A is Hermitian, its row scale equals its column scale and row m is
 // the conjugate of column m, so both are read with coalesced column accesses.
+#include <algorithm>
 #include <cstdint>
 #include "common.cuh"
 #include "ozaki.cuh"
@@ -377,8 +378,11 @@ __device__ __forceinline__ void df_add(float &hi, float &lo, float v)
     hi = s;
 }
 
-// One CTA: rows i0..i0+127 of Y (A rows) x columns j0..j0+63 (X columns) of
-// one matrix (see the file header).
+// Persistent: each CTA takes tiles t = blockIdx.x, blockIdx.x + gridDim.x, ...,
+// a tile being rows i0..i0+127 of Y (A rows) x columns j0..j0+63 (X columns)
+// of one matrix (see the file header).  The barrier phases run on across
+// tiles, so the producer and the MMA thread start the next tile while the fold
+// warps write the previous one out.
 // 18 warps: at most 5 per SM sub-partition, whose 16K registers allow 96
 // registers a thread
 template <int SA>
@@ -387,8 +391,8 @@ k_oz_gemm(const unsigned char *DA, const unsigned char *DX, const int *exA, cons
           int np, int batch, unsigned *fault)
 {
     extern __shared__ __align__(16) unsigned char oz_raw[];
-    const int jt = blockIdx.x, it = blockIdx.y, b = blockIdx.z;
-    const int KC = np / OZ_BK;
+    const int KC = np / OZ_BK, NJ = np / OZ_NX, NI = np / OZ_MA;
+    const int ntiles = NJ * NI * batch;
     const uint32_t raw_s = oz_saddr(oz_raw);
     unsigned char *base = oz_raw + (((raw_s + 1023u) & ~1023u) - raw_s);
     unsigned char *sX = base;                                   // OZ_NXS x 72 KB
@@ -404,6 +408,15 @@ k_oz_gemm(const unsigned char *DA, const unsigned char *DX, const int *exA, cons
     auto empty_a = [&](int q) { return bar0 + 8u * (2 * OZ_NXS + OZ_NAS + q); };
     auto tfull = [&](int q) { return bar0 + 8u * (2 * OZ_NXS + 2 * OZ_NAS + q); };
     auto tempty = [&](int q) { return bar0 + 8u * (2 * OZ_NXS + 2 * OZ_NAS + OZ_NBUF + q); };
+    // a tile's digit blocks: X chunks of its 64 columns, A planes of its 128 rows
+    auto tile_x = [&](int t) {
+        const int jt = t % NJ, b = t / (NJ * NI);
+        return DX + (((long)b * NJ + jt) * KC) * OZ_SB * OZ_XBLK;
+    };
+    auto tile_a = [&](int t) {
+        const int it = (t / NJ) % NI, b = t / (NJ * NI);
+        return DA + (((long)b * NI + it) * KC) * SA * OZ_ABLK;
+    };
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     if (warp == 0) {
@@ -425,34 +438,43 @@ k_oz_gemm(const unsigned char *DA, const unsigned char *DX, const int *exA, cons
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = *tslot;
 
-    const unsigned char *gX = DX + (((long)b * (np / OZ_NX) + jt) * KC) * OZ_SB * OZ_XBLK;
-    const unsigned char *gA = DA + (((long)b * (np / OZ_MA) + it) * KC) * SA * OZ_ABLK;
     // digit levels L = s + t kept per chunk: L <= 5 of 6 x 3 digits, all of 3 x 3
     constexpr int NL = SA == 6 ? 6 : SA + OZ_SB - 1;
+    const int QA = KC * SA;   // A planes per tile
 
     if (warp == OZ_FOLD_WARPS) {
         // ---- producer: bulk copies of the pre-swizzled digit tiles ----
         if (lane == 0) {
             bool ok = true;
-            // the A ring holds two planes: later planes are brought into L2 ahead
-            // of their copies (a chunk's X digits, needed a whole chunk later, too)
-            const int QA = KC * SA;
-            for (int qa = OZ_NAS; qa < min(OZ_APF, QA); ++qa) oz_prefetch_l2(gA + (long)qa * OZ_ABLK, OZ_ABLK);
-            for (int kc = 0; kc < KC && ok; ++kc) {
-                const int jx = kc % OZ_NXS, ux = kc / OZ_NXS;
-                if (ux > 0 && !(ok = oz_wait(empty_x(jx), (ux - 1) & 1, abort))) break;
-                oz_expect(full_x(jx), OZ_XSTAGE);
-                for (int q = 0; q < OZ_SB; ++q)
-                    oz_bulk(oz_saddr(sX + jx * OZ_XSTAGE + q * OZ_XBLK), gX + ((long)kc * OZ_SB + q) * OZ_XBLK,
-                            OZ_XBLK, full_x(jx));
-                if (kc + 1 < KC)
-                    for (int q = 0; q < OZ_SB; ++q) oz_prefetch_l2(gX + ((long)(kc + 1) * OZ_SB + q) * OZ_XBLK, OZ_XBLK);
-                for (int sdig = 0; sdig < SA; ++sdig) {
-                    const int qa = kc * SA + sdig, ia = qa % OZ_NAS, ua = qa / OZ_NAS;
-                    if (qa + OZ_APF < QA) oz_prefetch_l2(gA + (long)(qa + OZ_APF) * OZ_ABLK, OZ_ABLK);
-                    if (ua > 0 && !(ok = oz_wait(empty_a(ia), (ua - 1) & 1, abort))) break;
-                    oz_expect(full_a(ia), OZ_ABLK);
-                    oz_bulk(oz_saddr(sA + ia * OZ_ABLK), gA + (long)qa * OZ_ABLK, OZ_ABLK, full_a(ia));
+            // the A ring holds two planes: later planes (of this tile or the next)
+            // are brought into L2 ahead of their copies, and so is the next chunk's X
+            if (blockIdx.x < ntiles)
+                for (int qa = OZ_NAS; qa < min(OZ_APF, QA); ++qa)
+                    oz_prefetch_l2(tile_a(blockIdx.x) + (long)qa * OZ_ABLK, OZ_ABLK);
+            int ti = 0;
+            for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x, ++ti) {
+                const int tn = t + gridDim.x;   // the next tile, if any
+                const unsigned char *gX = tile_x(t), *gA = tile_a(t);
+                for (int kc = 0; kc < KC && ok; ++kc) {
+                    const int g = ti * KC + kc, jx = g % OZ_NXS, ux = g / OZ_NXS;
+                    if (ux > 0 && !(ok = oz_wait(empty_x(jx), (ux - 1) & 1, abort))) break;
+                    oz_expect(full_x(jx), OZ_XSTAGE);
+                    for (int q = 0; q < OZ_SB; ++q)
+                        oz_bulk(oz_saddr(sX + jx * OZ_XSTAGE + q * OZ_XBLK), gX + ((long)kc * OZ_SB + q) * OZ_XBLK,
+                                OZ_XBLK, full_x(jx));
+                    const unsigned char *pX = kc + 1 < KC ? gX + (long)(kc + 1) * OZ_XSTAGE
+                                                          : (tn < ntiles ? tile_x(tn) : nullptr);
+                    if (pX)
+                        for (int q = 0; q < OZ_SB; ++q) oz_prefetch_l2(pX + (long)q * OZ_XBLK, OZ_XBLK);
+                    for (int sdig = 0; sdig < SA; ++sdig) {
+                        const int qa = kc * SA + sdig, qg = ti * QA + qa, ia = qg % OZ_NAS, ua = qg / OZ_NAS;
+                        if (qa + OZ_APF < QA) oz_prefetch_l2(gA + (long)(qa + OZ_APF) * OZ_ABLK, OZ_ABLK);
+                        else if (tn < ntiles && qa + OZ_APF - QA < QA)
+                            oz_prefetch_l2(tile_a(tn) + (long)(qa + OZ_APF - QA) * OZ_ABLK, OZ_ABLK);
+                        if (ua > 0 && !(ok = oz_wait(empty_a(ia), (ua - 1) & 1, abort))) break;
+                        oz_expect(full_a(ia), OZ_ABLK);
+                        oz_bulk(oz_saddr(sA + ia * OZ_ABLK), gA + (long)qa * OZ_ABLK, OZ_ABLK, full_a(ia));
+                    }
                 }
             }
             if (!ok) { *abort = 1; atomicOr(fault ? fault : &g_oz_fault, 1u); }
@@ -462,50 +484,53 @@ k_oz_gemm(const unsigned char *DA, const unsigned char *DX, const int *exA, cons
         if (lane == 0) {
             bool ok = true;
             const uint32_t sx0 = oz_saddr(sX), sa0 = oz_saddr(sA);
-            for (int kc = 0; kc < KC && ok; ++kc) {
-                const int jx = kc % OZ_NXS, ux = kc / OZ_NXS;
-                if (!(ok = oz_wait(full_x(jx), ux & 1, abort))) break;
-                for (int sdig = 0; sdig < SA; ++sdig) {
-                    const int qa = kc * SA + sdig, ia = qa % OZ_NAS, ua = qa / OZ_NAS;
-                    if (!(ok = oz_wait(full_a(ia), ua & 1, abort))) break;
-                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                    const uint32_t ar = sa0 + ia * OZ_ABLK, ai = ar + OZ_MA * 128;
-                    for (int tdig = 0; tdig < OZ_SB; ++tdig) {
-                        const int L = sdig + tdig;
-                        if (L > NL - 1) break;
-                        const int ql = kc * NL + L, buf = ql % OZ_NBUF;
-                        const bool first = sdig == (L > 2 ? L - 2 : 0);
-                        if (first && ql >= OZ_NBUF) {
-                            // the fold of level ql - 4 has emptied this buffer
-                            if (!(ok = oz_wait(tempty(buf), ((ql - OZ_NBUF) / OZ_NBUF) & 1, abort))) break;
-                            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                        }
-                        // X block rows: [-Xi | Xr | Xi]; w1 = [Xr | Xi], w2 = [-Xi | Xr]
-                        const uint32_t w2 = sx0 + jx * OZ_XSTAGE + tdig * OZ_XBLK, w1 = w2 + OZ_NX * 128;
-                        const uint32_t tl = tmem + 128u * buf;
-                        // a 16-deep step is 32 bytes along the swizzled row: 2 in the
-                        // descriptor's address field (which no step carries out of)
-                        const uint64_t dar = oz_desc(ar), dai = oz_desc(ai), dw1 = oz_desc(w1), dw2 = oz_desc(w2);
-                        oz_mma(tl, dar, dw1, first ? 0u : 1u);
-                        oz_mma(tl, dai, dw2, 1u);
+            int g = 0;   // chunks issued by this CTA, over all its tiles
+            for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+                for (int kc = 0; kc < KC && ok; ++kc, ++g) {
+                    const int jx = g % OZ_NXS, ux = g / OZ_NXS;
+                    if (!(ok = oz_wait(full_x(jx), ux & 1, abort))) break;
+                    for (int sdig = 0; sdig < SA; ++sdig) {
+                        const int qg = g * SA + sdig, ia = qg % OZ_NAS, ua = qg / OZ_NAS;
+                        if (!(ok = oz_wait(full_a(ia), ua & 1, abort))) break;
+                        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                        const uint32_t ar = sa0 + ia * OZ_ABLK, ai = ar + OZ_MA * 128;
+                        for (int tdig = 0; tdig < OZ_SB; ++tdig) {
+                            const int L = sdig + tdig;
+                            if (L > NL - 1) break;
+                            const int ql = g * NL + L, buf = ql % OZ_NBUF;
+                            const bool first = sdig == (L > 2 ? L - 2 : 0);
+                            if (first && ql >= OZ_NBUF) {
+                                // the fold of level ql - OZ_NBUF has emptied this buffer
+                                if (!(ok = oz_wait(tempty(buf), ((ql - OZ_NBUF) / OZ_NBUF) & 1, abort))) break;
+                                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                            }
+                            // X block rows: [-Xi | Xr | Xi]; w1 = [Xr | Xi], w2 = [-Xi | Xr]
+                            const uint32_t w2 = sx0 + jx * OZ_XSTAGE + tdig * OZ_XBLK, w1 = w2 + OZ_NX * 128;
+                            const uint32_t tl = tmem + 128u * buf;
+                            // a 16-deep step is 32 bytes along the swizzled row: 2 in the
+                            // descriptor's address field (which no step carries out of)
+                            const uint64_t dar = oz_desc(ar), dai = oz_desc(ai), dw1 = oz_desc(w1), dw2 = oz_desc(w2);
+                            oz_mma(tl, dar, dw1, first ? 0u : 1u);
+                            oz_mma(tl, dai, dw2, 1u);
 #pragma unroll
-                        for (int ks = 1; ks < OZ_BK / 16; ++ks) {
-                            oz_mma(tl, dar + 2 * ks, dw1 + 2 * ks, 1u);
-                            oz_mma(tl, dai + 2 * ks, dw2 + 2 * ks, 1u);
+                            for (int ks = 1; ks < OZ_BK / 16; ++ks) {
+                                oz_mma(tl, dar + 2 * ks, dw1 + 2 * ks, 1u);
+                                oz_mma(tl, dai + 2 * ks, dw2 + 2 * ks, 1u);
+                            }
                         }
+                        if (!ok) break;
+                        oz_commit(empty_a(ia));
+                        // level sdig of this chunk is complete; after the last plane, all remaining ones
+                        for (int L = sdig; L < (sdig == SA - 1 ? NL : sdig + 1); ++L)
+                            oz_commit(tfull((g * NL + L) % OZ_NBUF));
                     }
                     if (!ok) break;
-                    oz_commit(empty_a(ia));
-                    // level sdig of this chunk is complete; after the last plane, all remaining ones
-                    for (int L = sdig; L < (sdig == SA - 1 ? NL : sdig + 1); ++L)
-                        oz_commit(tfull((kc * NL + L) % OZ_NBUF));
+                    oz_commit(empty_x(jx));
                 }
-                if (!ok) break;
-                oz_commit(empty_x(jx));
             }
-            if (ok && KC > 0) {
+            if (ok && g > 0) {
                 // the last commit has landed: every MMA of the CTA has finished
-                const int jx = (KC - 1) % OZ_NXS, ux = (KC - 1) / OZ_NXS;
+                const int jx = (g - 1) % OZ_NXS, ux = (g - 1) / OZ_NXS;
                 ok = oz_wait(empty_x(jx), ux & 1, abort);
             }
             if (!ok) { *abort = 1; atomicOr(fault ? fault : &g_oz_fault, 1u); }
@@ -514,55 +539,57 @@ k_oz_gemm(const unsigned char *DA, const unsigned char *DX, const int *exA, cons
         // ---- fold warps: level sums -> double-float accumulators -> Y ----
         const int q4 = warp & 3, h = warp >> 2;
         const uint32_t trow = tmem + ((uint32_t)(32 * q4) << 16);
-        float hr[16], lr[16], hi[16], li[16];
-#pragma unroll
-        for (int c = 0; c < 16; ++c) hr[c] = lr[c] = hi[c] = li[c] = 0.f;
         bool ok = true;
-        for (int kc = 0; kc < KC && ok; ++kc) {
+        int g = 0;   // chunks folded by this CTA, over all its tiles
+        for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+            float hr[16], lr[16], hi[16], li[16];
+#pragma unroll
+            for (int c = 0; c < 16; ++c) hr[c] = lr[c] = hi[c] = li[c] = 0.f;
+            for (int kc = 0; kc < KC && ok; ++kc, ++g) {
 #pragma unroll 1
-            for (int L = 0; L < NL; ++L) {
-                const int ql = kc * NL + L, buf = ql % OZ_NBUF;
-                ok = __all_sync(0xffffffffu, oz_wait(tfull(buf), (ql / OZ_NBUF) & 1, abort));
-                if (!ok) break;
-                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                const float w = ldexpf(1.0f, -8 * (L + 2));
-                // four groups of 4 columns (fewer live registers); the buffer is
-                // released once all are in registers
+                for (int L = 0; L < NL; ++L) {
+                    const int ql = g * NL + L, buf = ql % OZ_NBUF;
+                    ok = __all_sync(0xffffffffu, oz_wait(tfull(buf), (ql / OZ_NBUF) & 1, abort));
+                    if (!ok) break;
+                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                    const float w = ldexpf(1.0f, -8 * (L + 2));
+                    // four groups of 4 columns (fewer live registers); the buffer is
+                    // released once all are in registers
 #pragma unroll
-                for (int hf = 0; hf < 4; ++hf) {
-                    float re[4], im[4];
-                    const uint32_t c0 = trow + 128u * buf + 16u * h + 4u * hf;
-                    oz_ld4(c0, re);           // Ar Xr - Ai Xi
-                    oz_ld4(c0 + 64u, im);     // Ar Xi + Ai Xr
-                    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-                    if (hf == 3) {
-                        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-                        __syncwarp();
-                        if (lane == 0) oz_arrive(tempty(buf));
-                    }
-                    if (L < 3) {
-                        // levels 0-2: exact two-sum into (hi, lo)
-#pragma unroll
-                        for (int c = 0; c < 4; ++c) {
-                            df_add(hr[4 * hf + c], lr[4 * hf + c], re[c] * w);
-                            df_add(hi[4 * hf + c], li[4 * hf + c], im[c] * w);
+                    for (int hf = 0; hf < 4; ++hf) {
+                        float re[4], im[4];
+                        const uint32_t c0 = trow + 128u * buf + 16u * h + 4u * hf;
+                        oz_ld4(c0, re);           // Ar Xr - Ai Xi
+                        oz_ld4(c0 + 64u, im);     // Ar Xi + Ai Xr
+                        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                        if (hf == 3) {
+                            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+                            __syncwarp();
+                            if (lane == 0) oz_arrive(tempty(buf));
                         }
-                    } else {
-                        // from level 3 on the contribution (< 2^-17 of the unit scale) goes
-                        // straight into lo, whose own rounding already bounds the pair's error
+                        if (L < 3) {
+                            // levels 0-2: exact two-sum into (hi, lo)
 #pragma unroll
-                        for (int c = 0; c < 4; ++c) {
-                            lr[4 * hf + c] = fmaf(re[c], w, lr[4 * hf + c]);
-                            li[4 * hf + c] = fmaf(im[c], w, li[4 * hf + c]);
+                            for (int c = 0; c < 4; ++c) {
+                                df_add(hr[4 * hf + c], lr[4 * hf + c], re[c] * w);
+                                df_add(hi[4 * hf + c], li[4 * hf + c], im[c] * w);
+                            }
+                        } else {
+                            // from level 3 on the contribution (< 2^-17 of the unit scale) goes
+                            // straight into lo, whose own rounding already bounds the pair's error
+#pragma unroll
+                            for (int c = 0; c < 4; ++c) {
+                                lr[4 * hf + c] = fmaf(re[c], w, lr[4 * hf + c]);
+                                li[4 * hf + c] = fmaf(im[c], w, li[4 * hf + c]);
+                            }
                         }
                     }
                 }
             }
-        }
-        if (!ok && lane == 0) { *abort = 1; atomicOr(fault ? fault : &g_oz_fault, 1u); }
-        if (ok) {
+            if (!ok) break;
             // Y[i, j], i = this thread's A row, j = 16 consecutive X columns:
             // scale by 2^(e_i + 1) 2^(f_j + 1)
+            const int jt = t % NJ, it = (t / NJ) % NI, b = t / (NJ * NI);
             const int i = it * OZ_MA + 32 * q4 + lane;
             if (i < n) {
                 const int ei = exA[(long)b * np + i];
@@ -579,6 +606,7 @@ k_oz_gemm(const unsigned char *DA, const unsigned char *DX, const int *exA, cons
                 }
             }
         }
+        if (!ok && lane == 0) { *abort = 1; atomicOr(fault ? fault : &g_oz_fault, 1u); }
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
@@ -587,6 +615,21 @@ k_oz_gemm(const unsigned char *DA, const unsigned char *DX, const int *exA, cons
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tmem), "r"(OZ_TMEM_COLS)
                      : "memory");
     }
+}
+
+// SMs of the current device (cached per device)
+static int oz_device_sms()
+{
+    static std::mutex m;
+    static std::map<int, int> cache;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> lock(m);
+    auto f = cache.find(dev);
+    if (f != cache.end()) return f->second;
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    return cache[dev] = sms > 0 ? sms : 1;
 }
 
 OzakiX ozaki_prepare_x(cudaStream_t s, float2 *X, int n, int batch, void *work)
@@ -624,7 +667,10 @@ template <int SA> static void ozaki_product(cudaStream_t s, const OzakiX &ox, co
         return true;
     }();
     (void)attr;
-    dim3 grid(np / OZ_NX, np / OZ_MA, batch);
+    // one CTA per SM (its shared and tensor memory allow no second), each
+    // looping over tiles
+    const long ntiles = (long)(np / OZ_NX) * (np / OZ_MA) * batch;
+    const int grid = (int)std::min<long>(ntiles, oz_device_sms());
     cudaEvent_t ev = kt_begin(s);
     NRLTB_LAUNCH(k_oz_gemm<SA>, grid, OZ_THREADS, OZ_SMEM, s, DA, (const unsigned char *)ox.DX, exA, ox.exX, Y, n,
                  np, batch, g_fault_word);
