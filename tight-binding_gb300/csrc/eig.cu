@@ -42,8 +42,8 @@ template <typename T> void eig_work_carve(EigWork<T> &w, void *base, int n, int 
     w.pp = (C2 *)take(sizeof(C2) * 2 * EIG_NB * nb);
     w.part = (C2 *)take(sizeof(C2) * (2 * EIG_NB + 2) * ncta * nb);
     w.sc = (C2 *)take(sizeof(C2) * 4 * nb);
-    const size_t nbw = (size_t)std::min(EIG_WY, n);
-    w.Tt = (C2 *)take(sizeof(C2) * std::max(EIG_NB * (size_t)std::max(n, 2 * EIG_NB), 2 * nbw * nbw) * nb);
+    const size_t nbw = (size_t)std::min(EIG_WY, n), nblk = n > 1 ? (size_t)cdiv(n - 1, (int)nbw) : 0;
+    w.Tt = (C2 *)take(sizeof(C2) * (1 + nblk) * nbw * nbw * nb);   // G | T of each block
     w.Xt = (C2 *)take(sizeof(C2) * std::max(EIG_NB, (int)nbw) * (size_t)n * nb);
     w.d = (double *)take(sizeof(double) * n * nb);
     w.e = (double *)take(sizeof(double) * n * nb);
@@ -1032,7 +1032,7 @@ __global__ void k_fill_int(int *p, int v, int count)
 // ---------------------------------------------------------------------------
 template <typename T>
 void eig_solve(cudaStream_t s, EigWork<T> &w, const double2 *H, const double2 *S, double *eig,
-               typename cplx<T>::t *X, bool vectors, cudaEvent_t tri_start)
+               typename cplx<T>::t *X, bool vectors, cudaEvent_t tri_start, const EigAux *ax)
 {
     typedef typename cplx<T>::t C2;
     const int n = w.n, B = w.batch;
@@ -1124,6 +1124,33 @@ void eig_solve(cudaStream_t s, EigWork<T> &w, const double2 *H, const double2 *S
             }
         }
     }
+    // the back-transform's WY factors need only V and tau: with a second stream
+    // they are formed there while this one solves the tridiagonal problem
+    const int nbw = std::min(EIG_WY, n), nref = n - 1;
+    const long sG = (long)nbw * nbw;
+    C2 *const G = w.Tt;
+    auto Tf_of = [&](int j0) { return w.Tt + (long)(1 + j0 / nbw) * sG * B; };
+    auto wy_factors = [&](cudaStream_t st) {
+        for (int j0 = (nref >= 1 ? ((nref - 1) / nbw) * nbw : -1); j0 >= 0; j0 -= nbw) {
+            const int jb = std::min(nbw, nref - j0), mb = n - j0 - 1;
+            const C2 *Vb = w.V + (j0 + 1) + (long)j0 * ld;
+            zgemm<T>(st, jb, jb, mb, B, one, Vb, ld, ms, 1, Vb, ld, ms, 0, zero, G, nbw, sG);
+            if (sizeof(T) == 4) {
+                const int sm = (int)(sizeof(C2) * EIG_WY * (EIG_WY + 1));
+                smem_attr_at_least((const void *)k_larft_wy<T, true>, sm);
+                NRLTB_LAUNCH((k_larft_wy<T, true>), B, EIG_WY, sm, st, G, Tf_of(j0), w.tau, n, j0, jb, nbw);
+            } else {
+                NRLTB_LAUNCH((k_larft_wy<T, false>), B, EIG_WY, 0, st, G, Tf_of(j0), w.tau, n, j0, jb, nbw);
+            }
+        }
+    };
+    const bool on_aux = vectors && ax && ax->aux && ax->tri_done && ax->wy_done;
+    if (on_aux) {
+        cudaEventRecord(ax->tri_done, s);
+        cudaStreamWaitEvent(ax->aux, ax->tri_done, 0);
+        wy_factors(ax->aux);
+        cudaEventRecord(ax->wy_done, ax->aux);
+    }
     // 5. tridiagonal eigenproblem (FP64 inverse iteration; bisection in T)
     double *lamloc = (double *)w.Xt;   // free at this point: n doubles per matrix fit
     int *blk = w.perm, *rank = w.perm + 2 * (long)n * B;
@@ -1159,21 +1186,14 @@ void eig_solve(cudaStream_t s, EigWork<T> &w, const double2 *H, const double2 *S
     //    reflectors of the block vanish above row j0+1); then X = Wi^H Z.
     //    A (free after step 4) holds Vb^H Y, L (free after step 2) holds Tb Vb^H Y.
     {
-        const int nbw = std::min(EIG_WY, n), nref = n - 1;
-        C2 *G = w.Tt, *Tf = w.Tt + (long)nbw * nbw * B;
-        const long sG = (long)nbw * nbw, sX = (long)nbw * n;
+        if (on_aux) cudaStreamWaitEvent(s, ax->wy_done, 0);
+        else wy_factors(s);
+        const long sX = (long)nbw * n;
         for (int j0 = (nref >= 1 ? ((nref - 1) / nbw) * nbw : -1); j0 >= 0; j0 -= nbw) {
             const int jb = std::min(nbw, nref - j0), mb = n - j0 - 1;
             const C2 *Vb = w.V + (j0 + 1) + (long)j0 * ld;
             C2 *Yb = w.Y + (j0 + 1);
-            zgemm<T>(s, jb, jb, mb, B, one, Vb, ld, ms, 1, Vb, ld, ms, 0, zero, G, nbw, sG);
-            if (sizeof(T) == 4) {
-                const int sm = (int)(sizeof(C2) * EIG_WY * (EIG_WY + 1));
-                cudaFuncSetAttribute(k_larft_wy<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
-                NRLTB_LAUNCH((k_larft_wy<T, true>), B, EIG_WY, sm, s, G, Tf, w.tau, n, j0, jb, nbw);
-            } else {
-                NRLTB_LAUNCH((k_larft_wy<T, false>), B, EIG_WY, 0, s, G, Tf, w.tau, n, j0, jb, nbw);
-            }
+            const C2 *Tf = Tf_of(j0);
             if (sizeof(T) == 4) {
                 // Vb^H formed explicitly in Xt: the tensor-core GEMM streams an A
                 // operand in its stored orientation twice as fast
@@ -1201,8 +1221,8 @@ template size_t eig_work_bytes<float>(int, int);
 template void eig_work_carve<double>(EigWork<double> &, void *, int, int);
 template void eig_work_carve<float>(EigWork<float> &, void *, int, int);
 template void eig_solve<double>(cudaStream_t, EigWork<double> &, const double2 *, const double2 *, double *,
-                                double2 *, bool, cudaEvent_t);
+                                double2 *, bool, cudaEvent_t, const EigAux *);
 template void eig_solve<float>(cudaStream_t, EigWork<float> &, const double2 *, const double2 *, double *,
-                               float2 *, bool, cudaEvent_t);
+                               float2 *, bool, cudaEvent_t, const EigAux *);
 
 }  // namespace nrltb

@@ -50,7 +50,7 @@ template <typename T> struct EigWork {
     C2 *pp;                         // p1 | p2, 2*EIG_NB per matrix
     C2 *part;                       // per-CTA partial sums, [batch][ncta][2*EIG_NB+2]
     C2 *sc;                         // per-matrix scalars: [0] scale, [1] alpha
-    C2 *Tt;                         // compact-WY T factors / small temporaries, EIG_NB*n per matrix
+    C2 *Tt;                         // back-transform: G = Vb^H Vb, then the T factor of every block
     C2 *Xt;                         // EIG_NB x n per matrix
     double *d, *e;                  // tridiagonal, n per matrix
     double *lam;                    // eigenvalues, n per matrix (ascending)
@@ -64,6 +64,16 @@ template <typename T> struct EigWork {
 template <typename T> size_t eig_work_bytes(int n, int batch);
 template <typename T> void eig_work_carve(EigWork<T> &w, void *base, int n, int batch);
 
+// Optional second stream for the back-transform's WY factors: given `aux`
+// and two events, eig_solve forms every block's G = Vb^H Vb and T factor on
+// aux (after `tri_done`, recorded on s when the tridiagonalisation is queued)
+// while s solves the tridiagonal eigenproblem, and s waits for `wy_done`
+// before the back-transform.  The results are the same either way.
+struct EigAux {
+    cudaStream_t aux = nullptr;
+    cudaEvent_t tri_done = nullptr, wy_done = nullptr;
+};
+
 // Full solve.  H and S (FP64, column-major, leading dimension n, stride n*n)
 // are converted to T inside.  eig: n per matrix; X (optional, precision T):
 // S-orthonormal eigenvectors, column-major, stride n*n.  tri_start (optional)
@@ -71,6 +81,7 @@ template <typename T> void eig_work_carve(EigWork<T> &w, void *base, int n, int 
 // panels leave most of the GPU to work on other streams).
 template <typename T>
 void eig_solve(cudaStream_t s, EigWork<T> &w, const double2 *H, const double2 *S,
-               double *eig, typename cplx<T>::t *X, bool vectors, cudaEvent_t tri_start = nullptr);
+               double *eig, typename cplx<T>::t *X, bool vectors, cudaEvent_t tri_start = nullptr,
+               const EigAux *ax = nullptr);
 
 }  // namespace nrltb

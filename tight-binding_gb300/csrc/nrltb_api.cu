@@ -108,6 +108,10 @@ struct nrltb_ctx {
     // made on `side` while the FP32 eigensolve runs on `stream`
     cudaStream_t side = nullptr;
     cudaEvent_t ev_in = nullptr, ev_side = nullptr;
+    // the back-transform's WY factors are formed on `aux` while `stream`
+    // solves the tridiagonal eigenproblem (eig_solve)
+    cudaStream_t aux = nullptr;
+    cudaEvent_t ev_tri = nullptr, ev_wy = nullptr;
     long long launches = 0;
     KTimer *kt = nullptr;   // kernel-class timing (measurement hooks)
     std::vector<nrltb_ctx *> workers;   // nrltb_bande_batch: one context and stream per host worker
@@ -597,10 +601,16 @@ static int run_solve(nrltb_ctx *c, int nv, int nkc, int prec, const double2 *H, 
 {
     NvtxRange nv_(prec == NRLTB_PREC_FP64 ? "eigensolve FP64" : "eigensolve mixed");
     cudaStream_t s = c->stream;
+    EigAux ax;
+    ax.aux = c->aux;
+    ax.tri_done = c->ev_tri;
+    ax.wy_done = c->ev_wy;
     if (prec == NRLTB_PREC_FP64) {
         RET(c->d_work.ensure(eig_work_bytes<double>(nv, nkc)));
         EigWork<double> w;
         eig_work_carve<double>(w, c->d_work.p, nv, nkc);
+        // one stream: the WY factors and the tridiagonal solve both load the
+        // FP64 pipe, and overlapping them measured slower
         eig_solve<double>(s, w, H, S, eig, Zout, vectors);
         CKL();
         CK(cudaMemcpyAsync(status, w.status, sizeof(int) * nkc, cudaMemcpyDeviceToDevice, s));
@@ -610,7 +620,7 @@ static int run_solve(nrltb_ctx *c, int nv, int nkc, int prec, const double2 *H, 
         RET(c->d_X.ensure(sizeof(float2) * (size_t)nv * nv * nkc));
         EigWork<float> w;
         eig_work_carve<float>(w, c->d_work.p, nv, nkc);
-        eig_solve<float>(s, w, H, S, eig, c->d_X.as<float2>(), true, side ? c->ev_in : nullptr);
+        eig_solve<float>(s, w, H, S, eig, c->d_X.as<float2>(), true, side ? c->ev_in : nullptr, &ax);
         CKL();
         if (side) RET(side(c->ev_in));
         CK(cudaMemcpyAsync(status, w.status, sizeof(int) * nkc, cudaMemcpyDeviceToDevice, s));
@@ -1008,8 +1018,14 @@ int nrltb_ctx_create(nrltb_ctx **out, int device)
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_in, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_side, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->aux, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_tri, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_wy, cudaEventDisableTiming);
     if (e != cudaSuccess) {
         set_err("stream: %s", cudaGetErrorString(e));
+        if (c->ev_tri) cudaEventDestroy(c->ev_tri);
+        if (c->aux) cudaStreamDestroy(c->aux);
+        if (c->ev_side) cudaEventDestroy(c->ev_side);
         if (c->ev_in) cudaEventDestroy(c->ev_in);
         if (c->side) cudaStreamDestroy(c->side);
         if (c->own) cudaStreamDestroy(c->own);
@@ -1027,6 +1043,7 @@ int nrltb_ctx_destroy(nrltb_ctx *c)
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
     if (c->side) cudaStreamSynchronize(c->side);
+    if (c->aux) cudaStreamSynchronize(c->aux);
     DBuf *bufs[] = {&c->d_kkind, &c->d_posn, &c->d_posq, &c->d_kbas, &c->d_dnn, &c->d_screenl, &c->d_param,
                     &c->d_kq, &c->d_kw, &c->d_ksk, &c->d_orb, &c->d_flip, &c->d_spinat, &c->d_nc, &c->d_Hn, &c->d_Sn, &c->d_code, &c->d_blk, &c->d_misc, &c->d_pairs,
                     &c->d_sk, &c->d_seg, &c->d_ph, &c->d_H, &c->d_S, &c->d_X, &c->d_work, &c->d_ref, &c->d_hf, &c->d_np,
@@ -1041,7 +1058,10 @@ int nrltb_ctx_destroy(nrltb_ctx *c)
     for (nrltb_ctx *w : c->workers) nrltb_ctx_destroy(w);
     if (c->ev_in) cudaEventDestroy(c->ev_in);
     if (c->ev_side) cudaEventDestroy(c->ev_side);
+    if (c->ev_tri) cudaEventDestroy(c->ev_tri);
+    if (c->ev_wy) cudaEventDestroy(c->ev_wy);
     if (c->side) cudaStreamDestroy(c->side);
+    if (c->aux) cudaStreamDestroy(c->aux);
     if (c->own) cudaStreamDestroy(c->own);
     delete c;
     return NRLTB_OK;
