@@ -76,68 +76,86 @@ __global__ void k_convert_h(const double2 *__restrict__ src, C2 *__restrict__ ds
 }
 
 // ---------------------------------------------------------------------------
+// v s, each part rounded on its own (never contracted into a later add)
+__device__ __forceinline__ float2 scale_rn(float2 v, float s) { return make_float2(__fmul_rn(v.x, s), __fmul_rn(v.y, s)); }
+__device__ __forceinline__ double2 scale_rn(double2 v, double s)
+{
+    return make_double2(__dmul_rn(v.x, s), __dmul_rn(v.y, s));
+}
+
 // Diagonal block: Cholesky L_jj L_jj^H = S_jj and its inverse, in shared memory.
 template <typename T>
 __global__ void __launch_bounds__(256) k_potrf_diag(EigWork<T> w, int j0, int jb)
 {
     typedef typename cplx<T>::t C2;
-    __shared__ C2 a[EIG_NB][EIG_NB + 1];   // a[c][r]
+    __shared__ C2 a[EIG_NB][EIG_NB + 1];   // a[c][r], updated in place
     __shared__ C2 x[EIG_NB][EIG_NB + 1];   // inverse, x[c][r]
     __shared__ int bad;
     const int b = blockIdx.x, tid = threadIdx.x;
+    // lane = row r, warp = columns c = warp, warp + 8, ... (no index division)
+    const int r = tid & 31, cg = tid >> 5;
     C2 *L = w.L + b * w.mstride + j0 + (long)j0 * w.ld;
     C2 *Wi = w.Wi + b * w.mstride + j0 + (long)j0 * w.ld;
-    for (int e = tid; e < jb * jb; e += blockDim.x) {
-        int r = e % jb, c = e / jb;
-        a[c][r] = L[r + (long)c * w.ld];
-    }
+    if (r < jb)
+        for (int c = cg; c < jb; c += 8) a[c][r] = L[r + (long)c * w.ld];
     if (tid == 0) bad = 0;
     __syncthreads();
+    // one barrier per column: every thread forms the pivot of column k itself,
+    // and the scaled column k = a[k][.] / sqrt(pivot) on the fly for its
+    // updates (the values the stored scaled column would hold).  Column k is
+    // read but not written in step k; its finished values are written back by
+    // its warp at the start of step k + 1, which reads only later columns.
+    C2 held = cmk<T>(0, 0);
+    int heldk = -1;
     for (int k = 0; k < jb; ++k) {
-        if (tid == 0) {
-            T piv = a[k][k].x;
-            if (!(piv > T(0))) { bad = 1; piv = T(1); }
-            a[k][k] = cmk<T>(sqrt(piv), T(0));
-        }
-        __syncthreads();
-        T inv = T(1) / a[k][k].x;
-        for (int r = k + 1 + tid; r < jb; r += blockDim.x) a[k][r] = cscale(a[k][r], inv);
-        __syncthreads();
-        for (int e = tid; e < jb * jb; e += blockDim.x) {
-            int r = e % jb, c = e / jb;
-            if (c > k && r >= c) a[c][r] = csub(a[c][r], cmul(a[k][r], cconj(a[k][c])));
+        if (heldk >= 0) { a[heldk][r] = held; heldk = -1; }
+        T piv = a[k][k].x;
+        const bool badk = !(piv > T(0));
+        if (badk) piv = T(1);
+        const T dk = sqrt(piv);
+        const T inv = T(1) / dk;
+        if (badk && tid == 0) bad = 1;
+        if (r < jb && r >= k) {
+            const C2 akr = r == k ? cmk<T>(dk, T(0)) : scale_rn(a[k][r], inv);
+            if (cg == (k & 7)) { held = akr; heldk = k; }
+            if (r > k) {
+                int c = k + 1 + ((cg - (k + 1)) & 7);   // first column > k of this warp's group
+                for (; c <= r; c += 8) a[c][r] = csub(a[c][r], cmul(akr, cconj(scale_rn(a[k][c], inv))));
+            }
         }
         __syncthreads();
     }
+    if (heldk >= 0) a[heldk][r] = held;
+    __syncthreads();
     // inverse of the lower-triangular block, one column per thread
     if (tid < jb) {
         int c = tid;
-        for (int r = 0; r < c; ++r) x[c][r] = cmk<T>(0, 0);
+        for (int rr = 0; rr < c; ++rr) x[c][rr] = cmk<T>(0, 0);
         x[c][c] = cmk<T>(T(1) / a[c][c].x, T(0));
-        for (int r = c + 1; r < jb; ++r) {
+        for (int rr = c + 1; rr < jb; ++rr) {
             C2 s = cmk<T>(0, 0);
             int k = c;
-            for (; k + 8 <= r; k += 8) {
+            for (; k + 8 <= rr; k += 8) {
                 C2 av[8], xv[8];
 #pragma unroll
                 for (int u = 0; u < 8; ++u) {
-                    av[u] = a[k + u][r];
+                    av[u] = a[k + u][rr];
                     xv[u] = x[c][k + u];
                 }
 #pragma unroll
                 for (int u = 0; u < 8; ++u) s = cadd(s, cmul(av[u], xv[u]));
             }
-            for (; k < r; ++k) s = cadd(s, cmul(a[k][r], x[c][k]));
-            x[c][r] = cscale(s, -T(1) / a[r][r].x);
+            for (; k < rr; ++k) s = cadd(s, cmul(a[k][rr], x[c][k]));
+            x[c][rr] = cscale(s, -T(1) / a[rr][rr].x);
         }
     }
     __syncthreads();
-    for (int e = tid; e < jb * jb; e += blockDim.x) {
-        int r = e % jb, c = e / jb;
-        C2 z = cmk<T>(0, 0);
-        L[r + (long)c * w.ld] = (r >= c) ? a[c][r] : z;
-        Wi[r + (long)c * w.ld] = (r >= c) ? x[c][r] : z;
-    }
+    if (r < jb)
+        for (int c = cg; c < jb; c += 8) {
+            const C2 z = cmk<T>(0, 0);
+            L[r + (long)c * w.ld] = (r >= c) ? a[c][r] : z;
+            Wi[r + (long)c * w.ld] = (r >= c) ? x[c][r] : z;
+        }
     if (tid == 0 && bad) w.status[b] = 1;
 }
 
