@@ -43,7 +43,7 @@ template <typename T> void eig_work_carve(EigWork<T> &w, void *base, int n, int 
     w.part = (C2 *)take(sizeof(C2) * (2 * EIG_NB + 2) * ncta * nb);
     w.sc = (C2 *)take(sizeof(C2) * 4 * nb);
     const size_t nbw = (size_t)std::min(EIG_WY, n), nblk = n > 1 ? (size_t)cdiv(n - 1, (int)nbw) : 0;
-    w.Tt = (C2 *)take(sizeof(C2) * (1 + nblk) * nbw * nbw * nb);   // G | T of each block
+    w.Tt = (C2 *)take(sizeof(C2) * (EIG_NAUX + nblk) * nbw * nbw * nb);   // G per aux stream | T of each block
     w.Xt = (C2 *)take(sizeof(C2) * std::max(EIG_NB, (int)nbw) * (size_t)n * nb);
     w.d = (double *)take(sizeof(double) * n * nb);
     w.e = (double *)take(sizeof(double) * n * nb);
@@ -1146,28 +1146,29 @@ void eig_solve(cudaStream_t s, EigWork<T> &w, const double2 *H, const double2 *S
     // they are formed there while this one solves the tridiagonal problem
     const int nbw = std::min(EIG_WY, n), nref = n - 1;
     const long sG = (long)nbw * nbw;
-    C2 *const G = w.Tt;
-    auto Tf_of = [&](int j0) { return w.Tt + (long)(1 + j0 / nbw) * sG * B; };
-    auto wy_factors = [&](cudaStream_t st) {
-        for (int j0 = (nref >= 1 ? ((nref - 1) / nbw) * nbw : -1); j0 >= 0; j0 -= nbw) {
-            const int jb = std::min(nbw, nref - j0), mb = n - j0 - 1;
-            const C2 *Vb = w.V + (j0 + 1) + (long)j0 * ld;
-            zgemm<T>(st, jb, jb, mb, B, one, Vb, ld, ms, 1, Vb, ld, ms, 0, zero, G, nbw, sG);
-            if (sizeof(T) == 4) {
-                const int sm = (int)(sizeof(C2) * EIG_WY * (EIG_WY + 1));
-                smem_attr_at_least((const void *)k_larft_wy<T, true>, sm);
-                NRLTB_LAUNCH((k_larft_wy<T, true>), B, EIG_WY, sm, st, G, Tf_of(j0), w.tau, n, j0, jb, nbw);
-            } else {
-                NRLTB_LAUNCH((k_larft_wy<T, false>), B, EIG_WY, 0, st, G, Tf_of(j0), w.tau, n, j0, jb, nbw);
-            }
+    auto Tf_of = [&](int j0) { return w.Tt + (long)(EIG_NAUX + j0 / nbw) * sG * B; };
+    // block j0's G and T on stream st, with G buffer g
+    auto wy_block = [&](cudaStream_t st, int g, int j0) {
+        C2 *const G = w.Tt + (long)g * sG * B;
+        const int jb = std::min(nbw, nref - j0), mb = n - j0 - 1;
+        const C2 *Vb = w.V + (j0 + 1) + (long)j0 * ld;
+        zgemm<T>(st, jb, jb, mb, B, one, Vb, ld, ms, 1, Vb, ld, ms, 0, zero, G, nbw, sG);
+        if (sizeof(T) == 4) {
+            const int sm = (int)(sizeof(C2) * EIG_WY * (EIG_WY + 1));
+            smem_attr_at_least((const void *)k_larft_wy<T, true>, sm);
+            NRLTB_LAUNCH((k_larft_wy<T, true>), B, EIG_WY, sm, st, G, Tf_of(j0), w.tau, n, j0, jb, nbw);
+        } else {
+            NRLTB_LAUNCH((k_larft_wy<T, false>), B, EIG_WY, 0, st, G, Tf_of(j0), w.tau, n, j0, jb, nbw);
         }
     };
-    const bool on_aux = vectors && ax && ax->aux && ax->tri_done && ax->wy_done;
+    const int j0last = nref >= 1 ? ((nref - 1) / nbw) * nbw : -1;
+    bool on_aux = vectors && ax && ax->tri_done;
+    for (int q = 0; q < EIG_NAUX; ++q) on_aux = on_aux && ax->aux[q] && ax->wy_done[q];
     if (on_aux) {
         cudaEventRecord(ax->tri_done, s);
-        cudaStreamWaitEvent(ax->aux, ax->tri_done, 0);
-        wy_factors(ax->aux);
-        cudaEventRecord(ax->wy_done, ax->aux);
+        for (int q = 0; q < EIG_NAUX; ++q) cudaStreamWaitEvent(ax->aux[q], ax->tri_done, 0);
+        for (int j0 = j0last, q = 0; j0 >= 0; j0 -= nbw, q = (q + 1) % EIG_NAUX) wy_block(ax->aux[q], q, j0);
+        for (int q = 0; q < EIG_NAUX; ++q) cudaEventRecord(ax->wy_done[q], ax->aux[q]);
     }
     // 5. tridiagonal eigenproblem (FP64 inverse iteration; bisection in T)
     double *lamloc = (double *)w.Xt;   // free at this point: n doubles per matrix fit
@@ -1204,8 +1205,10 @@ void eig_solve(cudaStream_t s, EigWork<T> &w, const double2 *H, const double2 *S
     //    reflectors of the block vanish above row j0+1); then X = Wi^H Z.
     //    A (free after step 4) holds Vb^H Y, L (free after step 2) holds Tb Vb^H Y.
     {
-        if (on_aux) cudaStreamWaitEvent(s, ax->wy_done, 0);
-        else wy_factors(s);
+        if (on_aux)
+            for (int q = 0; q < EIG_NAUX; ++q) cudaStreamWaitEvent(s, ax->wy_done[q], 0);
+        else
+            for (int j0 = j0last; j0 >= 0; j0 -= nbw) wy_block(s, 0, j0);
         const long sX = (long)nbw * n;
         for (int j0 = (nref >= 1 ? ((nref - 1) / nbw) * nbw : -1); j0 >= 0; j0 -= nbw) {
             const int jb = std::min(nbw, nref - j0), mb = n - j0 - 1;

@@ -64,14 +64,16 @@ template <typename T> struct EigWork {
 template <typename T> size_t eig_work_bytes(int n, int batch);
 template <typename T> void eig_work_carve(EigWork<T> &w, void *base, int n, int batch);
 
-// Optional second stream for the back-transform's WY factors: given `aux`
-// and two events, eig_solve forms every block's G = Vb^H Vb and T factor on
-// aux (after `tri_done`, recorded on s when the tridiagonalisation is queued)
-// while s solves the tridiagonal eigenproblem, and s waits for `wy_done`
-// before the back-transform.  The results are the same either way.
+// Optional streams for the back-transform's WY factors: given them and their
+// events, eig_solve forms the blocks' G = Vb^H Vb and T factors on the aux
+// streams, block by block in turn (after `tri_done`, recorded on s when the
+// tridiagonalisation is queued), while s solves the tridiagonal eigenproblem,
+// and s waits for every `wy_done` before the back-transform.  The results are
+// the same either way.
+constexpr int EIG_NAUX = 3;   // auxiliary streams for the WY factors (blocks dealt round-robin)
 struct EigAux {
-    cudaStream_t aux = nullptr;
-    cudaEvent_t tri_done = nullptr, wy_done = nullptr;
+    cudaStream_t aux[EIG_NAUX] = {};
+    cudaEvent_t tri_done = nullptr, wy_done[EIG_NAUX] = {};
 };
 
 // Full solve.  H and S (FP64, column-major, leading dimension n, stride n*n)

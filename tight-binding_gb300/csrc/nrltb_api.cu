@@ -108,10 +108,10 @@ struct nrltb_ctx {
     // made on `side` while the FP32 eigensolve runs on `stream`
     cudaStream_t side = nullptr;
     cudaEvent_t ev_in = nullptr, ev_side = nullptr;
-    // the back-transform's WY factors are formed on `aux` while `stream`
-    // solves the tridiagonal eigenproblem (eig_solve)
-    cudaStream_t aux = nullptr;
-    cudaEvent_t ev_tri = nullptr, ev_wy = nullptr;
+    // the back-transform's WY factors are formed on the `aux` streams while
+    // `stream` solves the tridiagonal eigenproblem (eig_solve)
+    cudaStream_t aux[EIG_NAUX] = {};
+    cudaEvent_t ev_tri = nullptr, ev_wy[EIG_NAUX] = {};
     long long launches = 0;
     KTimer *kt = nullptr;   // kernel-class timing (measurement hooks)
     std::vector<nrltb_ctx *> workers;   // nrltb_bande_batch: one context and stream per host worker
@@ -602,9 +602,11 @@ static int run_solve(nrltb_ctx *c, int nv, int nkc, int prec, const double2 *H, 
     NvtxRange nv_(prec == NRLTB_PREC_FP64 ? "eigensolve FP64" : "eigensolve mixed");
     cudaStream_t s = c->stream;
     EigAux ax;
-    ax.aux = c->aux;
     ax.tri_done = c->ev_tri;
-    ax.wy_done = c->ev_wy;
+    for (int q = 0; q < EIG_NAUX; ++q) {
+        ax.aux[q] = c->aux[q];
+        ax.wy_done[q] = c->ev_wy[q];
+    }
     if (prec == NRLTB_PREC_FP64) {
         RET(c->d_work.ensure(eig_work_bytes<double>(nv, nkc)));
         EigWork<double> w;
@@ -1018,13 +1020,18 @@ int nrltb_ctx_create(nrltb_ctx **out, int device)
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_in, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_side, cudaEventDisableTiming);
-    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->aux, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_tri, cudaEventDisableTiming);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_wy, cudaEventDisableTiming);
+    for (int q = 0; q < EIG_NAUX; ++q) {
+        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->aux[q], cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_wy[q], cudaEventDisableTiming);
+    }
     if (e != cudaSuccess) {
         set_err("stream: %s", cudaGetErrorString(e));
+        for (int q = 0; q < EIG_NAUX; ++q) {
+            if (c->ev_wy[q]) cudaEventDestroy(c->ev_wy[q]);
+            if (c->aux[q]) cudaStreamDestroy(c->aux[q]);
+        }
         if (c->ev_tri) cudaEventDestroy(c->ev_tri);
-        if (c->aux) cudaStreamDestroy(c->aux);
         if (c->ev_side) cudaEventDestroy(c->ev_side);
         if (c->ev_in) cudaEventDestroy(c->ev_in);
         if (c->side) cudaStreamDestroy(c->side);
@@ -1043,7 +1050,8 @@ int nrltb_ctx_destroy(nrltb_ctx *c)
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
     if (c->side) cudaStreamSynchronize(c->side);
-    if (c->aux) cudaStreamSynchronize(c->aux);
+    for (int q = 0; q < EIG_NAUX; ++q)
+        if (c->aux[q]) cudaStreamSynchronize(c->aux[q]);
     DBuf *bufs[] = {&c->d_kkind, &c->d_posn, &c->d_posq, &c->d_kbas, &c->d_dnn, &c->d_screenl, &c->d_param,
                     &c->d_kq, &c->d_kw, &c->d_ksk, &c->d_orb, &c->d_flip, &c->d_spinat, &c->d_nc, &c->d_Hn, &c->d_Sn, &c->d_code, &c->d_blk, &c->d_misc, &c->d_pairs,
                     &c->d_sk, &c->d_seg, &c->d_ph, &c->d_H, &c->d_S, &c->d_X, &c->d_work, &c->d_ref, &c->d_hf, &c->d_np,
@@ -1059,9 +1067,11 @@ int nrltb_ctx_destroy(nrltb_ctx *c)
     if (c->ev_in) cudaEventDestroy(c->ev_in);
     if (c->ev_side) cudaEventDestroy(c->ev_side);
     if (c->ev_tri) cudaEventDestroy(c->ev_tri);
-    if (c->ev_wy) cudaEventDestroy(c->ev_wy);
+    for (int q = 0; q < EIG_NAUX; ++q) {
+        if (c->ev_wy[q]) cudaEventDestroy(c->ev_wy[q]);
+        if (c->aux[q]) cudaStreamDestroy(c->aux[q]);
+    }
     if (c->side) cudaStreamDestroy(c->side);
-    if (c->aux) cudaStreamDestroy(c->aux);
     if (c->own) cudaStreamDestroy(c->own);
     delete c;
     return NRLTB_OK;
