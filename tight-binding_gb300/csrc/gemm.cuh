@@ -264,9 +264,14 @@ void zgemm_simt(cudaStream_t s, int m, int n, int k, int batch, typename cplx<T>
     dim3 grid(cdiv(m, BM), cdiv(n, BN), batch);
     cudaEvent_t ev = kt_begin(s);
     // short k (the rank-32 panel updates): the whole k range in one or two
-    // shared-memory stages instead of four to eight
+    // shared-memory stages instead of four to eight; n <= 32 (the Cholesky
+    // panel solves) on 64 x 32 tiles.  Every element's k loop is the same in
+    // each form.
     constexpr int BKS = sizeof(T) == 4 ? 32 : 16;
-    if (k <= 64)
+    if (k <= 64 && n <= 32)
+        NRLTB_LAUNCH((zgemm_kernel<T, BM, 32, BKS, TM, 2>), dim3(cdiv(m, BM), 1, batch), (BM / TM) * (32 / 2), 0,
+                     s, g);
+    else if (k <= 64)
         NRLTB_LAUNCH((zgemm_kernel<T, BM, BN, BKS, TM, TN>), grid, (BM / TM) * (BN / TN), 0, s, g);
     else
         NRLTB_LAUNCH((zgemm_kernel<T, BM, BN, 8, TM, TN>), grid, (BM / TM) * (BN / TN), 0, s, g);

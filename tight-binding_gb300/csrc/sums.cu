@@ -117,9 +117,10 @@ __global__ void __launch_bounds__(1024) k_fermi_level(FermiJob *jobs)
     __syncthreads();
     {
         int uns = 0;
-        for (long q = tid; q < tot; q += nt) {
-            const int k = (int)(q / nv), i = (int)(q % nv);
-            if (i + 1 < nv && J.eig[(long)k * J.ldk + i + 1] < J.eig[(long)k * J.ldk + i]) uns = 1;
+        for (int k = warp; k < nk; k += nwarps) {   // a warp per row
+            const double *e = J.eig + (long)k * J.ldk;
+            for (int i = lane; i + 1 < nv; i += 32)
+                if (e[i + 1] < e[i]) uns = 1;
         }
         if (__syncthreads_or(uns) && tid == 0) s_sorted = 0;
         __syncthreads();
