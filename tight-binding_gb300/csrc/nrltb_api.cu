@@ -109,7 +109,10 @@ struct nrltb_ctx {
     cudaStream_t side = nullptr;
     cudaEvent_t ev_in = nullptr, ev_side = nullptr;
     // the back-transform's WY factors are formed on the `aux` streams while
-    // `stream` solves the tridiagonal eigenproblem (eig_solve)
+    // `stream` solves the tridiagonal eigenproblem (eig_solve); off in the
+    // structure batch's workers, whose concurrent structures fill the GPU
+    // already (the overlap measured 3 % slower there)
+    bool wy_overlap = true;
     cudaStream_t aux[EIG_NAUX] = {};
     cudaEvent_t ev_tri = nullptr, ev_wy[EIG_NAUX] = {};
     long long launches = 0;
@@ -622,7 +625,8 @@ static int run_solve(nrltb_ctx *c, int nv, int nkc, int prec, const double2 *H, 
         RET(c->d_X.ensure(sizeof(float2) * (size_t)nv * nv * nkc));
         EigWork<float> w;
         eig_work_carve<float>(w, c->d_work.p, nv, nkc);
-        eig_solve<float>(s, w, H, S, eig, c->d_X.as<float2>(), true, side ? c->ev_in : nullptr, &ax);
+        eig_solve<float>(s, w, H, S, eig, c->d_X.as<float2>(), true, side ? c->ev_in : nullptr,
+                         c->wy_overlap ? &ax : nullptr);
         CKL();
         if (side) RET(side(c->ev_in));
         CK(cudaMemcpyAsync(status, w.status, sizeof(int) * nkc, cudaMemcpyDeviceToDevice, s));
@@ -1203,6 +1207,7 @@ int nrltb_bande_batch(nrltb_ctx *c, int nstruct, const nrltb_structure *st, cons
     while ((int)c->workers.size() < W) {
         nrltb_ctx *w = nullptr;
         RET(nrltb_ctx_create(&w, c->device));
+        w->wy_overlap = false;
         c->workers.push_back(w);
     }
     std::vector<int> order(nstruct);
