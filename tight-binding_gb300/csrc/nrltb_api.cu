@@ -634,7 +634,11 @@ static int run_solve(nrltb_ctx *c, int nv, int nkc, int prec, const double2 *H, 
         RefineWork rw;
         refine_work_carve(rw, c->d_ref.p, nv, nkc);
         if (side) CK(cudaStreamWaitEvent(s, c->ev_side, 0));
-        refine_eigen(s, rw, H, S, c->d_X.as<float2>(), eig, Zout, status, pre);
+        RefAux ra;   // the WY factors' stream and events are free again by now
+        ra.aux = c->aux[0];
+        ra.ev_a = c->ev_tri;
+        ra.ev_b = c->ev_wy[0];
+        refine_eigen(s, rw, H, S, c->d_X.as<float2>(), eig, Zout, status, pre, c->wy_overlap ? &ra : nullptr);
         CKL();
         fault_mark(s, status, nkc);
     }

@@ -453,8 +453,9 @@ __global__ void __launch_bounds__(REF_CMAX * REF_CMAX) k_ref_rr(RefineWork w, co
 
 // 3. X' = X U in FP64 (Xd) and FP32 (Xr), and the residuals of the rotated
 // basis r'_j = sum_a (Y_H[:, m_a] - l_j Y_S[:, m_a]) U_aj in FP64 (into Ef as
-// FP32), m_a the members of column j's cluster; thread per element
-__global__ void k_ref_rotres(RefineWork w, const float2 *X)
+// FP32), m_a the members of column j's cluster; thread per element.  part:
+// 0 every column, 1 the columns outside clusters (U not read), 2 the rest.
+__global__ void k_ref_rotres(RefineWork w, const float2 *X, int part)
 {
     const int n = w.n;
     const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
@@ -465,6 +466,7 @@ __global__ void k_ref_rotres(RefineWork w, const float2 *X)
     const int r = (int)(e % n), j = (int)(e / n);
     REF_VIEWS
     const long mo = b * nn;
+    if ((part == 1 && csz[j] != 1) || (part == 2 && csz[j] == 1)) return;
     const double l = w.lam[(long)b * n + j];
     double2 v, res;
     float2 xr;
@@ -642,7 +644,7 @@ __global__ void k_ref_finish(RefineWork w, double2 *Z)
 }
 
 void refine_eigen(cudaStream_t s, RefineWork &w, const double2 *H, const double2 *S, float2 *X,
-                  double *eig, double2 *Z, int *status, const OzakiA *pre)
+                  double *eig, double2 *Z, int *status, const OzakiA *pre, const RefAux *ra)
 {
     const int n = w.n, B = w.batch;
     const long nn = (long)n * n, nb = (long)n * B;
@@ -661,11 +663,23 @@ void refine_eigen(cudaStream_t s, RefineWork &w, const double2 *H, const double2
     const size_t csm = n <= REF_KEYS_MAX ? sizeof(unsigned long long) * n : 0;
     if (csm > 48 * 1024) smem_attr_at_least((const void *)k_ref_clusters, (int)csm);
     NRLTB_LAUNCH(k_ref_clusters, B, 1024, csm, s, w, status);
-    NRLTB_LAUNCH(k_ref_rr, dim3(n, B), REF_CMAX * REF_CMAX, 0, s, w, X);
     // 3. rotated basis, its residuals, G' = X'^H r' (X'^H formed explicitly in
     //    the YH area, free from here on: the tensor-core GEMM streams an A
-    //    operand in its stored orientation twice as fast)
-    NRLTB_LAUNCH(k_ref_rotres, cdiv(nn * B, 256), 256, 0, s, w, X);
+    //    operand in its stored orientation twice as fast).  With a second
+    //    stream the columns outside clusters are done there while the cluster
+    //    solves (a few long CTAs for the largest clusters) run here.
+    if (ra && ra->aux && ra->ev_a && ra->ev_b) {
+        cudaEventRecord(ra->ev_a, s);
+        cudaStreamWaitEvent(ra->aux, ra->ev_a, 0);
+        NRLTB_LAUNCH(k_ref_rotres, cdiv(nn * B, 256), 256, 0, ra->aux, w, X, 1);
+        cudaEventRecord(ra->ev_b, ra->aux);
+        NRLTB_LAUNCH(k_ref_rr, dim3(n, B), REF_CMAX * REF_CMAX, 0, s, w, X);
+        NRLTB_LAUNCH(k_ref_rotres, cdiv(nn * B, 256), 256, 0, s, w, X, 2);
+        cudaStreamWaitEvent(s, ra->ev_b, 0);
+    } else {
+        NRLTB_LAUNCH(k_ref_rr, dim3(n, B), REF_CMAX * REF_CMAX, 0, s, w, X);
+        NRLTB_LAUNCH(k_ref_rotres, cdiv(nn * B, 256), 256, 0, s, w, X, 0);
+    }
     float2 *T1 = (float2 *)w.YH, *T2 = (float2 *)w.YS;
     conj_transpose<float>(s, w.Xr, T1, n, B);
     zgemm<float>(s, n, n, n, B, onef, T1, n, nn, 0, w.Ef, n, nn, 0, zerof, w.G, n, nn);

@@ -31,8 +31,15 @@ void refine_work_carve(RefineWork &w, void *base, int n, int batch);
 // X is rounded in place to the representation the tensor-core products use.
 // pre (optional): the 6-digit forms of H and S from ozaki_prepare_a, already
 // made (or being made on a stream this one waits for).
+// aux (optional): a second stream and two events; the rotated residuals of
+// the columns outside clusters, which need no cluster solve, are then formed
+// on it beside the cluster Rayleigh-Ritz solves (the same values either way).
+struct RefAux {
+    cudaStream_t aux = nullptr;
+    cudaEvent_t ev_a = nullptr, ev_b = nullptr;
+};
 void refine_eigen(cudaStream_t s, RefineWork &w, const double2 *H, const double2 *S, float2 *X,
-                  double *eig, double2 *Z, int *status, const OzakiA *pre = nullptr);
+                  double *eig, double2 *Z, int *status, const OzakiA *pre = nullptr, const RefAux *ra = nullptr);
 
 // Hellmann-Feynman shifts deig = diag(Z^H dH Z) - eig * diag(Z^H dS Z) for nkc
 // matrices; scratch must hold hf_scratch_bytes(n, nkc), 256-byte aligned.
