@@ -163,11 +163,17 @@ typedef struct nrltb_ctx nrltb_ctx;
 /* ---- library and context ------------------------------------------------ */
 int nrltb_abi_version(void);
 const char *nrltb_last_error(void);
-/* Create a context on one CUDA device: one stream, library-owned device buffers. */
+/* Create a context on one CUDA device: its stream, library-owned device
+ * buffers, and four internal streams onto which the mixed form forks
+ * independent work (the refinement's digits and the dH, dS Bloch sums during
+ * the tridiagonalisation; the back-transform's WY factors during the
+ * tridiagonal solve) and which it joins back with events, so that every call's
+ * work stays ordered on the context's stream. */
 int nrltb_ctx_create(nrltb_ctx **out, int device);
 int nrltb_ctx_destroy(nrltb_ctx *ctx);
 /* Run the context's work on a caller stream (cudaStream_t passed as void*), or
- * NULL for the context's own stream. */
+ * NULL for the context's own stream; the internal streams fork from and join
+ * back to it. */
 int nrltb_ctx_set_stream(nrltb_ctx *ctx, void *stream);
 /* Number of kernels this library has launched through ctx (for accounting). */
 long long nrltb_ctx_launch_count(const nrltb_ctx *ctx);
