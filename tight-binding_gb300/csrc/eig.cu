@@ -1142,8 +1142,9 @@ void eig_solve(cudaStream_t s, EigWork<T> &w, const double2 *H, const double2 *S
             }
         }
     }
-    // the back-transform's WY factors need only V and tau: with a second stream
-    // they are formed there while this one solves the tridiagonal problem
+    // the back-transform's WY factors need only V and tau: with the auxiliary
+    // streams they are formed there, a block on each in turn, while this one
+    // solves the tridiagonal problem
     const int nbw = std::min(EIG_WY, n), nref = n - 1;
     const long sG = (long)nbw * nbw;
     auto Tf_of = [&](int j0) { return w.Tt + (long)(EIG_NAUX + j0 / nbw) * sG * B; };

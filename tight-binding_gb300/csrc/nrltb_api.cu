@@ -109,9 +109,11 @@ struct nrltb_ctx {
     cudaStream_t side = nullptr;
     cudaEvent_t ev_in = nullptr, ev_side = nullptr;
     // the back-transform's WY factors are formed on the `aux` streams while
-    // `stream` solves the tridiagonal eigenproblem (eig_solve); off in the
-    // structure batch's workers, whose concurrent structures fill the GPU
-    // already (the overlap measured 3 % slower there)
+    // `stream` solves the tridiagonal eigenproblem (eig_solve), and the
+    // refinement's rotated residuals outside clusters on the first of them
+    // beside the cluster solves (refine_eigen); off in the structure batch's
+    // workers, whose concurrent structures fill the GPU already (the overlap
+    // measured 3 % slower there)
     bool wy_overlap = true;
     cudaStream_t aux[EIG_NAUX] = {};
     cudaEvent_t ev_tri = nullptr, ev_wy[EIG_NAUX] = {};
