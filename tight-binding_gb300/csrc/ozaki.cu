@@ -20,13 +20,17 @@
 // product of the rounded operands for the Hellmann-Feynman products.
 //
 // Tensor cores: tcgen05.mma kind::f16 (bf16 digits, FP32 accumulators in
-// tensor memory).  One CTA computes a 128 x 64 tile of Y: the MMA's M = 128
-// rows are rows i of A (digit tiles Ar_s, Ai_s), its N = 128 columns come
+// tensor memory).  Persistent CTAs, one per SM, take the 128 x 64 tiles of Y
+// in turn (the barrier phases run on from tile to tile, so the next tile's
+// copies and MMAs start while the folds write the last one).  In a tile the
+// MMA's M = 128 rows are rows i of A (digit tiles Ar_s, Ai_s), its N = 128
+// columns come
 // from the digit rows [-Xi_t | Xr_t | Xi_t] of 64 columns j of X, so that
 // Ar_s [Xr_t | Xi_t] + Ai_s [-Xi_t | Xr_t] accumulates [Re | Im] of a digit
 // pair's product in one 128-column accumulator.  Digits are written pre-tiled
 // in the 128-byte-swizzled K-major layout the MMA reads, so each tile is one
-// bulk asynchronous copy (cp.async.bulk with a transaction-count barrier).
+// bulk asynchronous copy (cp.async.bulk with a transaction-count barrier),
+// and the planes a few ahead are brought into L2 by cp.async.bulk.prefetch.
 // Warp roles: one producer thread (copies), one MMA thread, sixteen fold warps
 // (tensor memory -> registers, double-float accumulation, output).  Within a
 // chunk the A digit planes s = 0..5 stream through a ring while the chunk's X
