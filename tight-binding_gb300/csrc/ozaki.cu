@@ -674,6 +674,7 @@ template <int SA> static void ozaki_product(cudaStream_t s, const OzakiX &ox, co
     // one CTA per SM (its shared and tensor memory allow no second), each
     // looping over tiles
     const long ntiles = (long)(np / OZ_NX) * (np / OZ_MA) * batch;
+    if (ntiles <= 0) return;
     const int grid = (int)std::min<long>(ntiles, oz_device_sms());
     cudaEvent_t ev = kt_begin(s);
     NRLTB_LAUNCH(k_oz_gemm<SA>, grid, OZ_THREADS, OZ_SMEM, s, DA, (const unsigned char *)ox.DX, exA, ox.exX, Y, n,
